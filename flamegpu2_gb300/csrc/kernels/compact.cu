@@ -1,0 +1,285 @@
+// Fused, order-preserving birth/death compaction (one pass over the agents).
+//
+// Each block owns a tile of 2048 agents, read "striped" (item k of thread t is
+// agent tile*2048 + k*256 + t) so that every flag load and column copy is
+// coalesced. Survivor and birth ranks inside the tile come from warp ballots;
+// the tile's offsets among all tiles come from a decoupled look-back on a
+// packed (survivors, births) pair. Survivors land at their rank, births at
+// S + birth rank where S = total survivors, so the reference's order —
+// survivors in order, then children in parent order — falls out of one kernel.
+// Tile statuses live in two arrays used on alternate calls; every call clears
+// the array the next call will use, so nothing is reset from the host.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace fgk {
+
+constexpr int kCompItems = 8;
+constexpr uint32_t kCompTile = kThreads * kCompItems;  // 2048
+constexpr uint64_t kPairMask = (1ull << 62) - 1ull;
+
+struct CompactParams {
+    fg_column col[FG_MAX_COLUMNS];
+    fg_column bcol[FG_MAX_COLUMNS];
+    uint32_t ncols;
+    int32_t id_col;
+};
+
+__device__ __forceinline__ uint64_t pair_pack(uint32_t flag, uint32_t a, uint32_t b) {
+    return (static_cast<uint64_t>(flag) << 62) | (static_cast<uint64_t>(a) << 31) | static_cast<uint64_t>(b);
+}
+
+// Look back over predecessor tiles; returns the exclusive packed (a << 31 | b).
+__device__ __forceinline__ uint64_t lookback_pair(const uint64_t* status, uint32_t tile, WsHeader* h) {
+    const uint32_t lane = lane_id();
+    uint64_t excl = 0;
+    int64_t pred = static_cast<int64_t>(tile) - 1;
+    while (pred >= 0) {
+        const int64_t t = pred - lane;
+        uint32_t flag = 2;
+        uint64_t val = 0;
+        if (t >= 0) {
+            uint32_t spins = 0;
+            for (;;) {
+                const uint64_t s = ld_acquire_u64(status + t);
+                flag = static_cast<uint32_t>(s >> 62);
+                val = s & kPairMask;
+                if (flag != 0) break;
+                if (++spins > kSpinLimit) {
+                    record_status(h, FG_ERR_DEVICE_TIMEOUT);
+                    flag = 2;
+                    val = 0;
+                    break;
+                }
+                if (spins > 16) __nanosleep(spins > 1024 ? 256 : 32);
+            }
+        }
+        const uint32_t pmask = __ballot_sync(0xFFFFFFFFu, flag == 2);
+        uint64_t contrib;
+        if (pmask) {
+            const uint32_t k = __ffs(pmask) - 1;
+            contrib = lane <= k ? val : 0;
+        } else {
+            contrib = val;
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
+        excl += contrib;
+        if (pmask) break;
+        pred -= 32;
+    }
+    return excl;
+}
+
+__device__ __forceinline__ void copy_col(const fg_column& c, uint32_t src, uint32_t dst) {
+    switch (c.elem_bytes) {
+        case 4: reinterpret_cast<uint32_t*>(c.out)[dst] = reinterpret_cast<const uint32_t*>(c.in)[src]; break;
+        case 8: reinterpret_cast<uint2*>(c.out)[dst] = reinterpret_cast<const uint2*>(c.in)[src]; break;
+        case 16: reinterpret_cast<uint4*>(c.out)[dst] = reinterpret_cast<const uint4*>(c.in)[src]; break;
+        case 1: reinterpret_cast<uint8_t*>(c.out)[dst] = reinterpret_cast<const uint8_t*>(c.in)[src]; break;
+        case 2: reinterpret_cast<uint16_t*>(c.out)[dst] = reinterpret_cast<const uint16_t*>(c.in)[src]; break;
+        default: {
+            const uint8_t* a = reinterpret_cast<const uint8_t*>(c.in) + static_cast<size_t>(src) * c.elem_bytes;
+            uint8_t* b = reinterpret_cast<uint8_t*>(c.out) + static_cast<size_t>(dst) * c.elem_bytes;
+            for (uint32_t k = 0; k < c.elem_bytes; ++k) b[k] = a[k];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_count_alive(uint32_t max_n, const uint32_t* d_n,
+                                                          const uint32_t* __restrict__ alive, WsHeader* h) {
+    const uint32_t n = d_n ? min(*d_n, max_n) : max_n;
+    uint32_t c = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        c += alive[i] != 0 ? 1u : 0u;
+    c = __reduce_add_sync(0xFFFFFFFFu, c);
+    if (lane_id() == 0 && c) atomicAdd(&h->alive_total, c);
+}
+
+__global__ void k_set_alive_total(uint32_t max_n, const uint32_t* d_n, WsHeader* h) {
+    h->alive_total = d_n ? min(*d_n, max_n) : max_n;
+}
+
+__global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ CompactParams cp, uint32_t max_n,
+                                                      const uint32_t* d_n, const uint32_t* __restrict__ alive,
+                                                      const uint32_t* __restrict__ born, uint32_t* d_next_id,
+                                                      const uint32_t* d_alive_total, uint32_t* d_n_out,
+                                                      uint32_t out_capacity, uint64_t* status0, uint32_t stride_tiles,
+                                                      WsHeader* h) {
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_cnt_a[kCompItems][kThreads / 32];
+    __shared__ uint32_t s_cnt_b[kCompItems][kThreads / 32];
+    __shared__ uint32_t s_tot[2];
+    __shared__ uint64_t s_excl;
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(&h->comp_ticket, 1u);
+    const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
+    const uint32_t n = d_n ? min(*d_n, max_n) : max_n;
+    const uint32_t S = d_alive_total ? *d_alive_total : h->alive_total;
+    const uint32_t next_id = d_next_id ? *d_next_id : 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    uint64_t* status = status0 + static_cast<size_t>(parity) * stride_tiles;
+    // clear the whole status array the next call will use (its grid may differ)
+    uint64_t* other = status0 + static_cast<size_t>(parity ^ 1u) * stride_tiles;
+    for (uint32_t t = blockIdx.x * blockDim.x + tid; t < stride_tiles; t += gridDim.x * blockDim.x) other[t] = 0;
+    const uint32_t base = tile * kCompTile;
+    const bool active_tile = base < n;
+    uint32_t ba[kCompItems], bb[kCompItems];
+    if (active_tile) {
+#pragma unroll
+        for (int k = 0; k < kCompItems; ++k) {
+            const uint32_t i = base + k * kThreads + tid;
+            const bool in = i < n;
+            const bool a = in && (alive == nullptr || alive[i] != 0);
+            const bool b = in && born != nullptr && born[i] != 0;
+            ba[k] = __ballot_sync(0xFFFFFFFFu, a);
+            bb[k] = __ballot_sync(0xFFFFFFFFu, b);
+            if (lane == 0) {
+                s_cnt_a[k][warp] = __popc(ba[k]);
+                s_cnt_b[k][warp] = __popc(bb[k]);
+            }
+        }
+    }
+    __syncthreads();
+    if (active_tile && tid == 0) {
+        uint32_t ra = 0, rb = 0;
+        for (int k = 0; k < kCompItems; ++k)
+            for (int w = 0; w < kThreads / 32; ++w) {
+                const uint32_t a = s_cnt_a[k][w], b = s_cnt_b[k][w];
+                s_cnt_a[k][w] = ra;
+                s_cnt_b[k][w] = rb;
+                ra += a;
+                rb += b;
+            }
+        s_tot[0] = ra;
+        s_tot[1] = rb;
+    }
+    __syncthreads();
+    if (active_tile && tid < 32) {
+        const uint64_t agg = (static_cast<uint64_t>(s_tot[0]) << 31) | s_tot[1];
+        uint64_t excl = 0;
+        if (tile == 0) {
+            if (tid == 0) st_release_u64(status, pair_pack(2, s_tot[0], s_tot[1]));
+        } else {
+            if (tid == 0) st_release_u64(status + tile, (1ull << 62) | agg);
+            excl = lookback_pair(status, tile, h);
+            if (tid == 0) st_release_u64(status + tile, (2ull << 62) | ((excl + agg) & kPairMask));
+        }
+        if (tid == 0) {
+            s_excl = excl;
+            if (base + kCompTile >= n) {  // last active tile: publish the totals
+                const uint64_t inc = excl + agg;
+                h->pad[0] = static_cast<uint32_t>(inc & 0x7FFFFFFFu);          // births
+                h->pad[1] = static_cast<uint32_t>((inc >> 31) & 0x7FFFFFFFu);  // survivors
+            }
+        }
+    }
+    __syncthreads();
+    if (active_tile) {
+        const uint32_t ea = static_cast<uint32_t>((s_excl >> 31) & 0x7FFFFFFFu);
+        const uint32_t eb = static_cast<uint32_t>(s_excl & 0x7FFFFFFFu);
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (int k = 0; k < kCompItems; ++k) {
+            const uint32_t i = base + k * kThreads + tid;
+            if ((ba[k] >> lane) & 1u) {
+                const uint32_t dst = ea + s_cnt_a[k][warp] + __popc(ba[k] & lt);
+                if (dst < out_capacity)
+                    for (uint32_t c = 0; c < cp.ncols; ++c) copy_col(cp.col[c], i, dst);
+            }
+            if ((bb[k] >> lane) & 1u) {
+                const uint32_t r = eb + s_cnt_b[k][warp] + __popc(bb[k] & lt);
+                const uint32_t dst = S + r;
+                if (dst < out_capacity) {
+                    for (uint32_t c = 0; c < cp.ncols; ++c) {
+                        if (static_cast<int32_t>(c) == cp.id_col)
+                            reinterpret_cast<uint32_t*>(cp.col[c].out)[dst] = next_id + r;
+                        else
+                            copy_col(cp.bcol[c], i, dst);
+                    }
+                } else {
+                    record_status(h, FG_ERR_CAPACITY);
+                }
+            }
+        }
+    }
+    // the last block to finish publishes the new count and resets the tickets
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&h->comp_done, 1u) == gridDim.x - 1) {
+            const uint32_t births = h->pad[0];
+            uint32_t total = S + births;
+            if (total > out_capacity) total = out_capacity;
+            if (d_n_out) *d_n_out = total;
+            if (d_next_id && cp.id_col >= 0) *d_next_id = next_id + births;
+            h->pad[0] = 0;
+            h->pad[1] = 0;
+            h->alive_total = 0;
+            h->comp_ticket = 0;
+            h->comp_done = 0;
+            atomicExch(&h->comp_parity, parity ^ 1u);
+            __threadfence();
+        }
+    }
+}
+
+}  // namespace fgk
+
+using namespace fgk;
+
+namespace {
+int launch_err() {
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FG_OK : FG_ERR_CUDA;
+}
+uint32_t comp_tiles(uint32_t max_n) { return std::max(1u, (max_n + kCompTile - 1) / kCompTile); }
+}  // namespace
+
+extern "C" size_t fg_compact_workspace_size(uint32_t max_n) {
+    return sizeof(WsHeader) + align_up(sizeof(uint64_t) * 2 * comp_tiles(max_n), 256);
+}
+
+extern "C" int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint32_t* alive, const uint32_t* born,
+                                 const fg_column* cols, const fg_column* birth_cols, uint32_t ncols, int32_t id_col,
+                                 uint32_t* d_next_id, const uint32_t* d_alive_total, uint32_t* d_n_out,
+                                 uint32_t out_capacity, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!workspace || ncols > FG_MAX_COLUMNS || (ncols && !cols)) return FG_ERR_INVALID_ARGUMENT;
+    if (born && ncols && !birth_cols) return FG_ERR_INVALID_ARGUMENT;
+    if (id_col >= static_cast<int32_t>(ncols)) return FG_ERR_INVALID_ARGUMENT;
+    if (id_col >= 0 && cols[id_col].elem_bytes != 4) return FG_ERR_INVALID_ARGUMENT;
+    if (max_n >= (1u << 31)) return FG_ERR_UNSUPPORTED;
+    if (workspace_bytes < fg_compact_workspace_size(max_n) || (reinterpret_cast<uintptr_t>(workspace) & 255))
+        return FG_ERR_WORKSPACE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(workspace);
+    WsHeader* h = reinterpret_cast<WsHeader*>(ws);
+    uint64_t* status = reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader));
+    const uint32_t tiles = comp_tiles(max_n);
+    if (!d_alive_total && alive) {
+        cudaMemsetAsync(&h->alive_total, 0, sizeof(uint32_t), st);
+        int dev = 0, sms = 132;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const uint32_t grid = std::max(1u, std::min((max_n + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
+        k_count_alive<<<grid, kThreads, 0, st>>>(max_n, d_n, alive, h);
+    } else if (!d_alive_total) {
+        // every agent survives: S = n
+        k_set_alive_total<<<1, 1, 0, st>>>(max_n, d_n, h);
+    }
+    CompactParams cp{};
+    for (uint32_t c = 0; c < ncols; ++c) {
+        cp.col[c] = cols[c];
+        cp.bcol[c] = birth_cols ? birth_cols[c] : cols[c];
+    }
+    cp.ncols = ncols;
+    cp.id_col = id_col;
+    // both status arrays are strided by the workspace's tile capacity, so a
+    // workspace keeps working when max_n changes between calls
+    const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
+    k_compact<<<tiles, kThreads, 0, st>>>(cp, max_n, d_n, alive, born, d_next_id, d_alive_total, d_n_out,
+                                          out_capacity, status, stride_tiles, h);
+    return launch_err();
+}

@@ -1,0 +1,188 @@
+// Single-pass exclusive scan of u32 values with decoupled look-back
+// (Merrill & Garland, "Single-pass Parallel Prefix Scan with Decoupled
+// Look-back", 2016). Tiles are handed out by a ticket counter in launch order,
+// so every tile a block waits on belongs to a block that is already running;
+// every wait is bounded and a give-up is recorded in the workspace header.
+//
+// Tile statuses are 64-bit words: [63:62] flag (1 aggregate, 2 inclusive
+// prefix), [61:32] a 30-bit epoch, [31:0] the value. The epoch changes after
+// each scan (the last block to finish advances it and resets the ticket), so
+// stale statuses of earlier scans read as "not ready" and the status array
+// never needs clearing.
+#pragma once
+
+#include "common.cuh"
+
+namespace fgk {
+
+constexpr int kScanItems = 16;                       // u32 per thread
+constexpr int kScanTile = kThreads * kScanItems;     // 4096 per tile
+
+__device__ __forceinline__ uint64_t scan_pack(uint32_t flag, uint32_t epoch, uint32_t v) {
+    return (static_cast<uint64_t>(flag) << 62) | (static_cast<uint64_t>(epoch & 0x3FFFFFFFu) << 32) | v;
+}
+
+// Block-wide exclusive scan of one u32 per thread; returns the exclusive
+// prefix of this thread and writes the block total to *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total, uint32_t* smem_warp) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t inc = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+        if (lane >= static_cast<uint32_t>(d)) inc += t;
+    }
+    if (lane == 31) smem_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t nw = blockDim.x >> 5;
+        uint32_t w = lane < nw ? smem_warp[lane] : 0;
+        uint32_t winc = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, winc, d);
+            if (lane >= static_cast<uint32_t>(d)) winc += t;
+        }
+        if (lane < nw) smem_warp[lane] = winc - w;   // exclusive warp offsets
+        if (lane == nw - 1) smem_warp[32] = winc;    // block total
+    }
+    __syncthreads();
+    const uint32_t r = smem_warp[warp] + inc - v;
+    *total = smem_warp[32];
+    return r;
+}
+
+// Warp 0 of a block: look back over predecessor tiles of `tile` and return the
+// exclusive prefix. `status` must already hold this tile's aggregate.
+__device__ __forceinline__ uint32_t lookback_u32(const uint64_t* status, uint32_t tile, uint32_t epoch, WsHeader* h) {
+    const uint32_t lane = lane_id();
+    uint32_t excl = 0;
+    int64_t pred = static_cast<int64_t>(tile) - 1;
+    while (pred >= 0) {
+        const int64_t t = pred - lane;
+        uint32_t flag = 2, val = 0;
+        if (t >= 0) {
+            uint32_t spins = 0;
+            for (;;) {
+                const uint64_t s = ld_acquire_u64(status + t);
+                const uint32_t e = static_cast<uint32_t>(s >> 32) & 0x3FFFFFFFu;
+                flag = static_cast<uint32_t>(s >> 62);
+                val = static_cast<uint32_t>(s);
+                if (flag != 0 && e == (epoch & 0x3FFFFFFFu)) break;
+                if (++spins > kSpinLimit) {
+                    record_status(h, FG_ERR_DEVICE_TIMEOUT);
+                    flag = 2;
+                    val = 0;
+                    break;
+                }
+                if (spins > 16) __nanosleep(spins > 1024 ? 256 : 32);
+            }
+        }
+        const uint32_t pmask = __ballot_sync(0xFFFFFFFFu, flag == 2);
+        if (pmask) {
+            const uint32_t k = __ffs(pmask) - 1;  // nearest inclusive prefix
+            uint32_t contrib = lane <= k ? val : 0;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
+            excl += contrib;
+            break;
+        }
+        uint32_t contrib = val;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
+        excl += contrib;
+        pred -= 32;
+    }
+    return excl;
+}
+
+// Exclusive scan of in[0..n) into out[0..n). If zero_in, in[] is cleared to 0
+// after it has been read (in != out). Launch with ceil(n / kScanTile) blocks of
+// kThreads threads.
+__global__ void __launch_bounds__(kThreads) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
+                                                       uint64_t* status, WsHeader* h) {
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_excl;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&h->scan_ticket, 1u);
+    const uint32_t epoch = ld_acquire_u32(&h->scan_epoch);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = static_cast<uint64_t>(tile) * kScanTile + static_cast<uint64_t>(threadIdx.x) * kScanItems;
+    uint32_t v[kScanItems];
+    const bool full = base + kScanItems <= n;
+    const bool vec = full && ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
+    if (vec) {
+        const uint4* p = reinterpret_cast<const uint4*>(in + base);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            const uint4 q = p[k];
+            v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = (base + k < n) ? in[base + k] : 0u;
+    }
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) tsum += v[k];
+    uint32_t btotal;
+    const uint32_t texcl = block_exclusive_scan(tsum, &btotal, s_warp);
+    // publish this tile and look back
+    if (threadIdx.x < 32) {
+        uint32_t excl = 0;
+        if (tile == 0) {
+            if (threadIdx.x == 0) st_release_u64(status, scan_pack(2, epoch, btotal));
+        } else {
+            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(1, epoch, btotal));
+            excl = lookback_u32(status, tile, epoch, h);
+            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(2, epoch, excl + btotal));
+        }
+        if (threadIdx.x == 0) s_excl = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_excl + texcl;
+    uint32_t o[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        o[k] = run;
+        run += v[k];
+    }
+    const bool ovec = full && ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
+    if (ovec) {
+        uint4* p = reinterpret_cast<uint4*>(out + base);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) p[k] = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < n) out[base + k] = o[k];
+    }
+    if (zero_in) {
+        uint32_t* zin = const_cast<uint32_t*>(in);
+        if (vec) {
+            uint4* p = reinterpret_cast<uint4*>(zin + base);
+#pragma unroll
+            for (int k = 0; k < kScanItems / 4; ++k) p[k] = make_uint4(0, 0, 0, 0);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanItems; ++k)
+                if (base + k < n) zin[base + k] = 0;
+        }
+    }
+    // the last block to finish resets the ticket and advances the epoch
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&h->scan_done, 1u) == gridDim.x - 1) {
+            h->scan_ticket = 0;
+            h->scan_done = 0;
+            atomicExch(&h->scan_epoch, (epoch + 1) & 0x3FFFFFFFu);
+            __threadfence();
+        }
+    }
+}
+
+inline uint32_t scan_tiles(uint32_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+}  // namespace fgk

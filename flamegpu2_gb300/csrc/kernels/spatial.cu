@@ -1,0 +1,500 @@
+// Spatial message index build and automatic spatial agent sort on GB300.
+//
+// One build = five kernels, no host synchronisation, no allocation:
+//   k_bin        bin index per message (clamped floor((p-min)/r), the reference's
+//                getGridPosition3D/getHash3D) + warp-aggregated histogram atomics;
+//                keeps each message's slot from the atomic
+//   k_scan_u32   single-pass exclusive scan histogram -> PBM (clears the histogram)
+//   k_perm       unstable placement perm[PBM[bin] + slot] = message
+//   k_stabilize  per sorted position: restores ascending original index inside
+//                short bins (<= kShortBin) and emits the record (or index);
+//                long bins are queued as 256-element chunks
+//   k_long       ranks the chunks of long bins against their whole bin
+// The automatic agent sort runs the same pipeline on the reference's sort key
+// and finally gathers every agent column by the stable permutation.
+#include <algorithm>
+
+#include "common.cuh"
+#include "scan.cuh"
+
+namespace fgk {
+
+constexpr uint32_t kShortBin = 32;
+constexpr uint32_t kChunk = 256;     // elements of a long bin ranked by one block pass
+constexpr uint32_t kRankTile = 2048; // bin elements staged in shared memory per pass
+
+enum KeyMode { kMessageBin = 0, kSortKey = 1 };
+enum EmitMode { kEmitRecord = 0, kEmitPerm = 1 };
+
+struct SortGrid {
+    float min[3];
+    float width[3];
+    float gd_f[3];
+    uint32_t gd[3];
+    uint32_t mask;
+};
+
+__device__ __forceinline__ uint32_t load_count(const uint32_t* d_n, uint32_t max_n) {
+    if (!d_n) return max_n;
+    const uint32_t n = *d_n;
+    return n < max_n ? n : max_n;
+}
+
+// getGridPosition3D + getHash3D (MessageSpatial3DDevice.cuh:646-672) /
+// getGridPosition2D + getHash2D (MessageSpatial2DDevice.cuh:605-627).
+__device__ __forceinline__ uint32_t message_bin(const fg_spatial_grid& g, float x, float y, float z) {
+    int gx = static_cast<int>(floorf((x - g.min[0]) / g.radius));
+    int gy = static_cast<int>(floorf((y - g.min[1]) / g.radius));
+    const int dx = static_cast<int>(g.gridDim[0]), dy = static_cast<int>(g.gridDim[1]);
+    gx = gx < 0 ? 0 : (gx >= dx ? dx - 1 : gx);
+    gy = gy < 0 ? 0 : (gy >= dy ? dy - 1 : gy);
+    if (g.dims == 3) {
+        int gz = static_cast<int>(floorf((z - g.min[2]) / g.radius));
+        const int dz = static_cast<int>(g.gridDim[2]);
+        gz = gz < 0 ? 0 : (gz >= dz ? dz - 1 : gz);
+        return static_cast<uint32_t>(gz) * g.gridDim[0] * g.gridDim[1] + static_cast<uint32_t>(gy) * g.gridDim[0] +
+               static_cast<uint32_t>(gx);
+    }
+    return static_cast<uint32_t>(gy) * g.gridDim[0] + static_cast<uint32_t>(gx);
+}
+
+// calculateSpatialHash (src/flamegpu/simulation/CUDASimulation.cu:380-408): unclamped,
+// width based; masked to the radix sort's bit range (:569-571).
+__device__ __forceinline__ uint32_t sort_key(const SortGrid& s, int dims, float x, float y, float z) {
+    const int gx = static_cast<int>(floorf(((x - s.min[0]) / s.width[0]) * s.gd_f[0]));
+    const int gy = static_cast<int>(floorf(((y - s.min[1]) / s.width[1]) * s.gd_f[1]));
+    uint32_t h;
+    if (dims == 3) {
+        const int gz = static_cast<int>(floorf(((z - s.min[2]) / s.width[2]) * s.gd_f[2]));
+        h = static_cast<uint32_t>(gz * s.gd[0] * s.gd[1] + (gy * s.gd[0]) + gx);
+    } else {
+        h = static_cast<uint32_t>((gy * s.gd[0]) + gx);
+    }
+    return h & s.mask;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg, uint32_t max_n, const uint32_t* d_n,
+                                                  const float* __restrict__ x, const float* __restrict__ y,
+                                                  const float* __restrict__ z, const uint32_t* __restrict__ valid,
+                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
+                                                  uint32_t* hist, WsHeader* h) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) h->long_count = 0;
+    const uint32_t n = load_count(d_n, max_n);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < n;
+        uint32_t key = kInvalid;
+        if (act && (valid == nullptr || valid[i] != 0)) {
+            const float px = x[i], py = y[i], pz = (g.dims == 3) ? z[i] : 0.0f;
+            key = (MODE == kMessageBin) ? message_bin(g, px, py, pz) : sort_key(sg, g.dims, px, py, pz);
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, key != kInvalid);
+        uint32_t s = 0;
+        if (key != kInvalid) s = warp_aggregated_inc(hist, key, m);
+        if (act) {
+            keys[i] = key;
+            slot[i] = s;
+        }
+    }
+}
+
+// The slot came from the histogram atomics, so pbm[k] + slot < n holds as long
+// as the histogram started at zero (fg_workspace_init); a workspace that broke
+// that invariant is reported instead of written out of bounds.
+__global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_t* d_n,
+                                                   const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
+                                                   const uint32_t* __restrict__ pbm, uint32_t* __restrict__ perm,
+                                                   WsHeader* h) {
+    const uint32_t n = load_count(d_n, max_n);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        if (k != kInvalid) {
+            const uint32_t at = pbm[k] + slot[i];
+            if (at < n)
+                perm[at] = i;
+            else
+                record_status(h, FG_ERR_WORKSPACE);
+        }
+    }
+}
+
+struct RecordParams {
+    fg_record_desc rec;
+    uint32_t* out;
+};
+
+__device__ __forceinline__ void emit_record(const RecordParams& rp, uint32_t i, uint32_t dst) {
+    const uint32_t words = rp.rec.words;
+    uint4* o = reinterpret_cast<uint4*>(rp.out + static_cast<size_t>(dst) * words);
+    for (uint32_t w = 0; w < words; w += 4) {
+        uint32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t* src = rp.rec.src[w + k];
+            v[k] = src ? ld_nc_u32(src + static_cast<size_t>(i) * rp.rec.src_stride[w + k] + rp.rec.src_word[w + k]) : 0u;
+        }
+        o[w >> 2] = make_uint4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+template <int EMIT>
+__device__ __forceinline__ void emit(const RecordParams& rp, uint32_t* sperm, uint32_t i, uint32_t dst) {
+    if (EMIT == kEmitRecord) {
+        emit_record(rp, i, dst);
+    } else {
+        sperm[dst] = i;
+    }
+}
+
+// Sorted positions p < total = pbm[nbuckets]. Short bins are ranked in place
+// (count of smaller original indices in the bin); long bins are queued as
+// chunks (bucket, chunk index) for k_long.
+template <int EMIT>
+__global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ RecordParams rp, uint32_t nbuckets,
+                                                        const uint32_t* __restrict__ keys,
+                                                        const uint32_t* __restrict__ pbm,
+                                                        const uint32_t* __restrict__ perm, uint32_t* sperm,
+                                                        uint2* chunk_list, uint32_t chunk_cap, WsHeader* h) {
+    const uint32_t total = pbm[nbuckets];
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        const uint32_t i = perm[p];
+        const uint32_t b = keys[i];
+        const uint32_t s = pbm[b], e = pbm[b + 1];
+        const uint32_t len = e - s;
+        if (len > kShortBin) {
+            if (p == s) {
+                const uint32_t nch = (len + kChunk - 1) / kChunk;
+                const uint32_t at = atomicAdd(&h->long_count, nch);
+                for (uint32_t c = 0; c < nch; ++c)
+                    if (at + c < chunk_cap) chunk_list[at + c] = make_uint2(b, c);
+                if (at + nch > chunk_cap) record_status(h, FG_ERR_CAPACITY);
+            }
+            continue;
+        }
+        uint32_t dst = s;
+        if (len > 1) {
+            for (uint32_t q = s; q < e; ++q) dst += (perm[q] < i) ? 1u : 0u;
+        }
+        emit<EMIT>(rp, sperm, i, dst);
+    }
+}
+
+// One block per queued chunk: each thread takes one element of the chunk and
+// counts the smaller original indices of its bin, staged through shared memory.
+template <int EMIT>
+__global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ RecordParams rp,
+                                                   const uint32_t* __restrict__ pbm,
+                                                   const uint32_t* __restrict__ perm, uint32_t* sperm,
+                                                   const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
+                                                   const WsHeader* h) {
+    __shared__ uint32_t s_idx[kRankTile];
+    const uint32_t nchunks = min(h->long_count, chunk_cap);
+    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint2 ch = chunk_list[c];
+        const uint32_t s = pbm[ch.x], e = pbm[ch.x + 1];
+        const uint32_t q = s + ch.y * kChunk + threadIdx.x;
+        const bool act = q < e;
+        const uint32_t i = act ? perm[q] : 0u;
+        uint32_t rank = 0;
+        for (uint32_t t0 = s; t0 < e; t0 += kRankTile) {
+            const uint32_t tn = min(kRankTile, e - t0);
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < tn; k += blockDim.x) s_idx[k] = perm[t0 + k];
+            __syncthreads();
+            if (act) {
+                uint32_t r = 0;
+                for (uint32_t k = 0; k < tn; ++k) r += (s_idx[k] < i) ? 1u : 0u;
+                rank += r;
+            }
+        }
+        if (act) emit<EMIT>(rp, sperm, i, s + rank);
+    }
+}
+
+struct ColumnParams {
+    fg_column col[FG_MAX_COLUMNS];
+    uint32_t ncols;
+};
+
+template <typename T>
+__device__ __forceinline__ void copy_elem(const void* in, void* out, uint32_t src, uint32_t dst) {
+    reinterpret_cast<T*>(out)[dst] = reinterpret_cast<const T*>(in)[src];
+}
+
+__device__ __forceinline__ void copy_column_elem(const fg_column& c, uint32_t src, uint32_t dst) {
+    switch (c.elem_bytes) {
+        case 4: copy_elem<uint32_t>(c.in, c.out, src, dst); break;
+        case 8: copy_elem<uint2>(c.in, c.out, src, dst); break;
+        case 16: copy_elem<uint4>(c.in, c.out, src, dst); break;
+        case 1: copy_elem<uint8_t>(c.in, c.out, src, dst); break;
+        case 2: copy_elem<uint16_t>(c.in, c.out, src, dst); break;
+        default: {
+            const uint8_t* a = reinterpret_cast<const uint8_t*>(c.in) + static_cast<size_t>(src) * c.elem_bytes;
+            uint8_t* b = reinterpret_cast<uint8_t*>(c.out) + static_cast<size_t>(dst) * c.elem_bytes;
+            if ((c.elem_bytes & 3) == 0) {
+                for (uint32_t k = 0; k < c.elem_bytes; k += 4)
+                    *reinterpret_cast<uint32_t*>(b + k) = *reinterpret_cast<const uint32_t*>(a + k);
+            } else {
+                for (uint32_t k = 0; k < c.elem_bytes; ++k) b[k] = a[k];
+            }
+        }
+    }
+}
+
+// out_c[p] = in_c[sperm[p]] for every column.
+__global__ void __launch_bounds__(kThreads) k_gather_columns(const __grid_constant__ ColumnParams cp, uint32_t max_n,
+                                                             const uint32_t* d_n, const uint32_t* __restrict__ sperm) {
+    const uint32_t n = load_count(d_n, max_n);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t i = sperm[p];
+        for (uint32_t c = 0; c < cp.ncols; ++c) copy_column_elem(cp.col[c], i, p);
+    }
+}
+
+// ------------------------------------------------------------------- host side
+
+struct BuildLayout {
+    size_t hist, scan_status, keys, slot, perm, sperm, chunks, pbm, total;
+    uint32_t chunk_cap;
+};
+
+static BuildLayout build_layout(uint32_t max_n, uint32_t nbuckets, bool sort_mode) {
+    BuildLayout L{};
+    size_t off = sizeof(WsHeader);
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off = align_up(off + bytes, 256);
+        return at;
+    };
+    // The scan statuses and the (kept-zero) histogram come first: their
+    // offsets depend only on the bucket count, so a workspace stays valid when
+    // max_n changes as long as the grid does not.
+    const uint32_t scan_n = nbuckets + 1;
+    L.scan_status = take(sizeof(uint64_t) * (scan_tiles(scan_n) + 1));
+    L.hist = take(sizeof(uint32_t) * (static_cast<size_t>(scan_n) + 4));
+    L.keys = take(sizeof(uint32_t) * (static_cast<size_t>(max_n) + 1));
+    L.slot = take(sizeof(uint32_t) * (static_cast<size_t>(max_n) + 1));
+    L.perm = take(sizeof(uint32_t) * (static_cast<size_t>(max_n) + 1));
+    L.chunk_cap = max_n / (kShortBin + 1) + max_n / kChunk + 16;
+    L.chunks = take(sizeof(uint2) * L.chunk_cap);
+    if (sort_mode) {
+        L.sperm = take(sizeof(uint32_t) * (static_cast<size_t>(max_n) + 1));
+        L.pbm = take(sizeof(uint32_t) * (static_cast<size_t>(scan_n) + 4));
+    }
+    L.total = off;
+    return L;
+}
+
+}  // namespace fgk
+
+using namespace fgk;
+
+namespace {
+
+thread_local int g_last_cuda_error = 0;
+
+int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (!cached[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cached[dev] = v > 0 ? v : 132;
+    }
+    return cached[dev];
+}
+
+uint32_t grid_for(uint32_t max_n, int per_sm = 8) {
+    const uint32_t need = (max_n + kThreads - 1) / kThreads;
+    const uint32_t cap = static_cast<uint32_t>(sm_count() * per_sm);
+    return std::max(1u, std::min(need, cap));
+}
+
+int check_launch() {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_last_cuda_error = static_cast<int>(e);
+        return FG_ERR_CUDA;
+    }
+    return FG_OK;
+}
+
+bool sort_grid_from(const fg_spatial_grid* g, SortGrid* s, uint32_t* nbuckets) {
+    // CUDASimulation.cu:494-507 and :569-571
+    uint64_t prod = 1;
+    for (int a = 0; a < 3; ++a) {
+        const float w = a < g->dims ? (g->max[a] - g->min[a]) : 0.0f;
+        s->min[a] = a < g->dims ? g->min[a] : 0.0f;
+        s->width[a] = w;
+        s->gd[a] = w != 0.0f ? static_cast<uint32_t>(ceilf(w / g->radius)) : 1u;
+        s->gd_f[a] = static_cast<float>(s->gd[a]);
+        prod *= s->gd[a];
+    }
+    const int bits = static_cast<int>(std::floor(std::log2(static_cast<double>(static_cast<uint32_t>(prod))))) + 1;
+    if (bits > 30 || prod == 0) return false;
+    s->mask = (1u << bits) - 1u;
+    *nbuckets = 1u << bits;
+    return true;
+}
+
+}  // namespace
+
+extern "C" int fg_last_cuda_error(void) { return g_last_cuda_error; }
+
+extern "C" int fg_spatial_grid_init(fg_spatial_grid* g, int32_t dims, const float* mn, const float* mx, float radius) {
+    // MessageSpatial3D::CUDAModelHandler::CUDAModelHandler (MessageSpatial3D.cu:31-52)
+    if (!g || !mn || !mx || (dims != 2 && dims != 3) || !(radius > 0.0f)) return FG_ERR_INVALID_ARGUMENT;
+    *g = fg_spatial_grid{};
+    g->dims = dims;
+    g->radius = radius;
+    g->binCount = 1;
+    g->wrapCompatible = 1;
+    uint64_t prod = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (a < dims) {
+            if (!(mx[a] > mn[a])) return FG_ERR_INVALID_ARGUMENT;
+            g->min[a] = mn[a];
+            g->max[a] = mx[a];
+            g->width[a] = g->max[a] - g->min[a];
+            g->gridDim[a] = static_cast<uint32_t>(std::ceil(g->width[a] / g->radius));
+            prod *= g->gridDim[a];
+            // numeric::approxExactlyDivisible<float> (include/flamegpu/detail/numeric.h:24-31)
+            const float x = g->width[a], y = g->radius;
+            const float eps = std::max(std::fabs(x), std::fabs(y)) * 1.1920929e-07f;
+            const float v = std::fmod(x, y);
+            g->wrapCompatible = g->wrapCompatible && (v <= eps || v > y - eps);
+        } else {
+            g->gridDim[a] = 1;
+        }
+    }
+    if (prod >= 0xFFFFFFF0ull) return FG_ERR_INVALID_ARGUMENT;
+    g->binCount = static_cast<uint32_t>(prod);
+    return FG_OK;
+}
+
+extern "C" size_t fg_spatial_build_workspace_size(uint32_t max_n, uint32_t bin_count) {
+    return build_layout(max_n, bin_count, false).total;
+}
+
+extern "C" size_t fg_spatial_sort_workspace_size(uint32_t max_n, const fg_spatial_grid* g) {
+    SortGrid sg{};
+    uint32_t nb = 0;
+    if (!g || !sort_grid_from(g, &sg, &nb)) return 0;
+    return build_layout(max_n, nb, true).total;
+}
+
+namespace {
+
+template <int MODE, int EMIT>
+int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets, uint32_t max_n, const uint32_t* d_n,
+                 const float* x, const float* y, const float* z, const uint32_t* valid, const RecordParams& rp,
+                 uint32_t* pbm_out, const BuildLayout& L, char* ws, cudaStream_t st) {
+    WsHeader* h = reinterpret_cast<WsHeader*>(ws);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(ws + L.hist);
+    uint64_t* sstat = reinterpret_cast<uint64_t*>(ws + L.scan_status);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(ws + L.keys);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(ws + L.slot);
+    uint32_t* perm = reinterpret_cast<uint32_t*>(ws + L.perm);
+    uint32_t* sperm = EMIT == kEmitPerm ? reinterpret_cast<uint32_t*>(ws + L.sperm) : nullptr;
+    uint2* chunks = reinterpret_cast<uint2*>(ws + L.chunks);
+    const uint32_t grid = grid_for(max_n);
+    k_bin<MODE><<<grid, kThreads, 0, st>>>(*g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
+    const uint32_t scan_n = nbuckets + 1;
+    k_scan_u32<<<scan_tiles(scan_n), kThreads, 0, st>>>(hist, pbm_out, scan_n, 1, sstat, h);
+    k_perm<<<grid, kThreads, 0, st>>>(max_n, d_n, keys, slot, pbm_out, perm, h);
+    k_stabilize<EMIT><<<grid, kThreads, 0, st>>>(rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
+    k_long<EMIT><<<static_cast<uint32_t>(sm_count() * 4), kThreads, 0, st>>>(rp, pbm_out, perm, sperm, chunks,
+                                                                              L.chunk_cap, h);
+    return check_launch();
+}
+
+}  // namespace
+
+extern "C" int fg_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
+                                const float* y, const float* z, const uint32_t* valid, const fg_record_desc* rec,
+                                uint32_t* sorted, uint32_t* pbm, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+    if (!g || !rec || !pbm || !workspace || (g->dims != 2 && g->dims != 3)) return FG_ERR_INVALID_ARGUMENT;
+    if (rec->words == 0 || (rec->words & 3) || rec->words > FG_MAX_RECORD_WORDS) return FG_ERR_INVALID_ARGUMENT;
+    if (max_n && (!x || !y || (g->dims == 3 && !z) || !sorted)) return FG_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(sorted) & 15) return FG_ERR_INVALID_ARGUMENT;
+    const BuildLayout L = build_layout(max_n, g->binCount, false);
+    if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
+    RecordParams rp;
+    rp.rec = *rec;
+    rp.out = sorted;
+    SortGrid sg{};
+    return run_pipeline<kMessageBin, kEmitRecord>(g, sg, g->binCount, max_n, d_n, x, y, z, valid, rp, pbm, L,
+                                                  static_cast<char*>(workspace), static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int fg_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
+                                      const float* y, const float* z, const fg_column* cols, uint32_t ncols,
+                                      uint32_t* perm_out, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!g || !workspace || (g->dims != 2 && g->dims != 3) || ncols > FG_MAX_COLUMNS) return FG_ERR_INVALID_ARGUMENT;
+    if (max_n && (!x || !y || (g->dims == 3 && !z))) return FG_ERR_INVALID_ARGUMENT;
+    if (ncols && !cols) return FG_ERR_INVALID_ARGUMENT;
+    SortGrid sg{};
+    uint32_t nb = 0;
+    if (!sort_grid_from(g, &sg, &nb)) return FG_ERR_UNSUPPORTED;
+    const BuildLayout L = build_layout(max_n, nb, true);
+    if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
+    char* ws = static_cast<char*>(workspace);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RecordParams rp{};
+    int rc = run_pipeline<kSortKey, kEmitPerm>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
+                                               reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st);
+    if (rc != FG_OK) return rc;
+    const uint32_t* sperm = reinterpret_cast<const uint32_t*>(ws + L.sperm);
+    if (ncols) {
+        ColumnParams cp{};
+        for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cols[c];
+        cp.ncols = ncols;
+        k_gather_columns<<<grid_for(max_n), kThreads, 0, st>>>(cp, max_n, d_n, sperm);
+    }
+    if (perm_out && max_n) {
+        cudaMemcpyAsync(perm_out, sperm, sizeof(uint32_t) * max_n, cudaMemcpyDeviceToDevice, st);
+    }
+    return check_launch();
+}
+
+extern "C" size_t fg_scan_workspace_size(uint32_t n) {
+    return sizeof(WsHeader) + align_up(sizeof(uint64_t) * (scan_tiles(n) + 1), 256);
+}
+
+extern "C" int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+    if (!workspace || (n && (!in || !out))) return FG_ERR_INVALID_ARGUMENT;
+    if (workspace_bytes < fg_scan_workspace_size(n) || (reinterpret_cast<uintptr_t>(workspace) & 255))
+        return FG_ERR_WORKSPACE;
+    if (!n) return FG_OK;
+    char* ws = static_cast<char*>(workspace);
+    k_scan_u32<<<scan_tiles(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+        in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
+    return check_launch();
+}
+
+extern "C" int fg_workspace_init(void* workspace, size_t workspace_bytes, void* stream) {
+    if (!workspace) return FG_ERR_INVALID_ARGUMENT;
+    if (cudaMemsetAsync(workspace, 0, workspace_bytes, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        return check_launch();
+    return FG_OK;
+}
+
+extern "C" int fg_workspace_status(void* workspace, size_t workspace_bytes, void* stream, int32_t clear) {
+    if (!workspace || workspace_bytes < sizeof(WsHeader)) return FG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint32_t v = 0;
+    if (cudaMemcpyAsync(&v, workspace, sizeof(v), cudaMemcpyDeviceToHost, st) != cudaSuccess) return check_launch();
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch();
+    if (clear && v) {
+        if (cudaMemsetAsync(workspace, 0, sizeof(uint32_t), st) != cudaSuccess) return check_launch();
+    }
+    return static_cast<int>(static_cast<int32_t>(v));
+}
+
+extern "C" const char* fg_version(void) { return "flamegpu2_gb300 0.1 (sm_103a)"; }

@@ -1,0 +1,172 @@
+/*
+ * fg_capi.h — the C ABI of the GB300 kernel library (libflamegpu2_gb300.so).
+ *
+ * These entry points replace the device work behind FLAME GPU 2's
+ * MessageSpecialisationHandler::buildIndex, CUDAScatter and
+ * CUDAScanCompaction (see each declaration for the reference interface it
+ * stands in for). Plain C: device pointers, sizes, a cudaStream_t passed as
+ * void*. No entry point allocates device memory: callers own every buffer and
+ * size the scratch ("workspace") with the *_workspace_size() query, then clear
+ * it once with fg_workspace_init().
+ *
+ * Counts may live on the device so that a whole simulation step can be
+ * captured into a CUDA graph: wherever a `const uint32_t* d_n` is taken, a
+ * non-NULL pointer is read on the device (the host-side `max_n` is then only
+ * an upper bound used to size grids); a NULL pointer means "exactly max_n".
+ *
+ * Every function returns FG_OK (0) or a negative fg_status. Launch errors are
+ * reported as FG_ERR_CUDA with cudaGetLastError() left readable by
+ * fg_last_cuda_error(). Device-side failures (a bounded wait that gave up)
+ * are recorded in the workspace and read back with fg_workspace_status().
+ */
+#ifndef FLAMEGPU_GB300_FG_CAPI_H_
+#define FLAMEGPU_GB300_FG_CAPI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fg_status {
+    FG_OK = 0,
+    FG_ERR_INVALID_ARGUMENT = -1,   /* exception::InvalidArgument */
+    FG_ERR_WORKSPACE = -2,          /* workspace too small / misaligned */
+    FG_ERR_CUDA = -3,               /* a CUDA runtime call failed */
+    FG_ERR_DEVICE_TIMEOUT = -4,     /* a bounded device-side wait gave up (recorded on the device) */
+    FG_ERR_CAPACITY = -5,           /* an output would exceed the caller's capacity */
+    FG_ERR_UNSUPPORTED = -6
+} fg_status;
+
+/* Spatial partitioning grid. Mirrors MessageSpatial3D::MetaData /
+ * MessageSpatial2D::MetaData (include/flamegpu/runtime/messaging/MessageSpatial3D.h:38-68,
+ * MessageSpatial2D.h:39-69); built on the host as
+ * MessageSpatial3D::CUDAModelHandler's constructor does
+ * (src/flamegpu/runtime/messaging/MessageSpatial3D.cu:31-52). */
+typedef struct fg_spatial_grid {
+    int32_t dims;            /* 2 or 3 */
+    float min[3];
+    float max[3];
+    float radius;
+    float width[3];          /* max - min */
+    uint32_t gridDim[3];     /* ceil(width / radius); 1 on unused axes */
+    uint32_t binCount;       /* product of gridDim */
+    int32_t wrapCompatible;  /* radius divides every width (numeric.h:24-31) */
+} fg_spatial_grid;
+
+/* Largest sorted-message record, in 4-byte words. */
+#define FG_MAX_RECORD_WORDS 64
+/* Largest number of agent variable columns moved by one sort / compaction. */
+#define FG_MAX_COLUMNS 48
+
+/* How the build assembles one sorted message record (an array-of-structs row
+ * of `words` 4-byte words, `words` a multiple of 4 so rows are 16-byte aligned)
+ * from the unsorted struct-of-arrays message columns. Word w of the record is
+ * word `src_word[w]` of element i of column `src[w]`, whose elements are
+ * `src_stride[w]` words long; src[w] == NULL writes 0 (padding). */
+typedef struct fg_record_desc {
+    uint32_t words;
+    const uint32_t* src[FG_MAX_RECORD_WORDS];
+    uint32_t src_stride[FG_MAX_RECORD_WORDS];
+    uint32_t src_word[FG_MAX_RECORD_WORDS];
+} fg_record_desc;
+
+/* One agent variable column moved by a sort or compaction: `in` and `out` are
+ * distinct device arrays of elements of `elem_bytes` bytes (any size; 4-, 8-
+ * and 16-byte multiples take vector paths). */
+typedef struct fg_column {
+    const void* in;
+    void* out;
+    uint32_t elem_bytes;
+} fg_column;
+
+/* Host-side grid set-up: MessageSpatial3D.cu:31-52 / MessageSpatial2D.cu:36-54.
+ * Fails with FG_ERR_INVALID_ARGUMENT for radius <= 0, max <= min, dims not 2/3. */
+int fg_spatial_grid_init(fg_spatial_grid* g, int32_t dims, const float* min, const float* max, float radius);
+
+/* Scratch bytes needed by fg_spatial_build / fg_spatial_sort_agents for up to
+ * max_n elements over bin_count bins. */
+size_t fg_spatial_build_workspace_size(uint32_t max_n, uint32_t bin_count);
+size_t fg_spatial_sort_workspace_size(uint32_t max_n, const fg_spatial_grid* msg_grid);
+/* Scratch bytes needed by fg_compact_agents for up to max_n agents. */
+size_t fg_compact_workspace_size(uint32_t max_n);
+/* Zero a freshly allocated workspace once (an async memset on `stream`). The
+ * kernels leave it ready for the next call afterwards. */
+int fg_workspace_init(void* workspace, size_t workspace_bytes, void* stream);
+/* Device-side status recorded in a workspace (FG_OK or FG_ERR_DEVICE_TIMEOUT);
+ * synchronises `stream`. clear != 0 resets it. */
+int fg_workspace_status(void* workspace, size_t workspace_bytes, void* stream, int32_t clear);
+
+/* Spatial message index build. Replaces MessageSpatial3D::CUDAModelHandler::buildIndex
+ * (src/flamegpu/runtime/messaging/MessageSpatial3D.cu:113-146; 2D: MessageSpatial2D.cu:114-141)
+ * together with CUDAScatter::pbm_reorder (src/flamegpu/simulation/detail/CUDAScatter.cu:276-337)
+ * and the optional-output compaction of CUDAMessage::swap (CUDAMessage.cu:171-208).
+ *
+ *   x, y, z      message positions (z ignored/NULL for 2D), device, length >= count
+ *   valid        optional per-message output flags (non-zero = message exists), or NULL
+ *   rec          record layout of the sorted messages (host struct)
+ *   sorted       out: count * rec->words words, device
+ *   pbm          out: binCount + 1 entries: pbm[b] = first sorted message of bin b,
+ *                pbm[binCount] = number of messages (exclusive scan of the bin histogram)
+ *
+ * Within a bin, messages are ordered by ascending original index (stable); the
+ * reference leaves that order unspecified (atomicInc, MessageSpatial3D.cu:70). */
+int fg_spatial_build(const fg_spatial_grid* grid, uint32_t max_n, const uint32_t* d_n,
+                     const float* x, const float* y, const float* z, const uint32_t* valid,
+                     const fg_record_desc* rec, uint32_t* sorted, uint32_t* pbm,
+                     void* workspace, size_t workspace_bytes, void* stream);
+
+/* Automatic spatial agent sort: stable sort of the agents by the reference's
+ * unclamped, width-based bin key masked to floor(log2(bins))+1 bits, applied to
+ * every column. Replaces CUDASimulation::spatialSortAgent_async + HostAgentAPI::sort_async
+ * (src/flamegpu/simulation/CUDASimulation.cu:335-573,
+ * include/flamegpu/runtime/agent/HostAgentAPI.cuh:858-915). msg_grid is the
+ * grid of the message list the sorting function reads. If perm_out is non-NULL
+ * it receives perm[sorted_pos] = original index. */
+int fg_spatial_sort_agents(const fg_spatial_grid* msg_grid, uint32_t max_n, const uint32_t* d_n,
+                           const float* x, const float* y, const float* z,
+                           const fg_column* cols, uint32_t ncols, uint32_t* perm_out,
+                           void* workspace, size_t workspace_bytes, void* stream);
+
+/* Fused, order-preserving birth/death compaction. Replaces the death scan +
+ * scatter (src/flamegpu/simulation/detail/CUDAFatAgent.cu:105-137,
+ * CUDAFatAgentStateList.cu:155-178, CUDAScatter.cu:67-88) and the birth
+ * append (CUDAAgentStateList.cu:189-250, CUDAFatAgent.cu:311-346) in one pass:
+ *
+ *   out[0 .. S)          = rows i with alive[i] != 0, in order
+ *   out[S .. S + births) = birth rows i with born[i] != 0, in parent order
+ *
+ * alive / born may be NULL (all alive / no births). cols move survivors,
+ * birth_cols (same count and order as cols, `in` = per-parent staging rows)
+ * move births; both write into the same `out` arrays. If id_col >= 0, births'
+ * word id_col of cols[] receives *d_next_id + birth rank and *d_next_id is
+ * advanced by the number of births (deterministic: the reference draws child
+ * ids with atomicInc, DeviceAPI.cuh:546-557). d_alive_total (device) may carry
+ * S if the caller already has it (else it is computed here). The new
+ * population S + births is written to *d_n_out (device). out_capacity bounds
+ * the output; births beyond it are dropped and the status word records
+ * FG_ERR_CAPACITY. */
+int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint32_t* alive, const uint32_t* born,
+                      const fg_column* cols, const fg_column* birth_cols, uint32_t ncols,
+                      int32_t id_col, uint32_t* d_next_id, const uint32_t* d_alive_total,
+                      uint32_t* d_n_out, uint32_t out_capacity,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* Exclusive scan of n u32 values (single pass, decoupled look-back); out may
+ * alias in. Used for PBMs built elsewhere; replaces cub::DeviceScan::ExclusiveSum
+ * on this path. */
+size_t fg_scan_workspace_size(uint32_t n);
+int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/* Last CUDA error seen by this library on the calling thread (cudaError_t). */
+int fg_last_cuda_error(void);
+/* Library version string. */
+const char* fg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLAMEGPU_GB300_FG_CAPI_H_ */

@@ -1,0 +1,274 @@
+"""Parity of the C-ABI kernels (libflamegpu2_gb300.so) with the serial oracle.
+
+GPU tests call the kernels through the C ABI on seeded inputs and require
+bit-exact PBMs, stable within-bin order, sorted records, auto-sort
+permutations and compaction order/ids. CPU tests check that the library loads,
+exports every symbol the header declares, and that the host-side grid set-up
+matches the oracle.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _capi():
+    from flamegpu2_gb300 import capi
+    return capi
+
+
+def test_header_symbols_exported():
+    capi = _capi()
+    hdr = open(os.path.join(ROOT, "include", "flamegpu_gb300", "fg_capi.h")).read()
+    declared = set(re.findall(r"^(?:int|size_t|const char\*)\s+(fg_\w+)\(", hdr, re.M))
+    assert declared == set(capi.EXPORTS)
+    L = capi.lib()
+    for name in declared:
+        assert hasattr(L, name), name
+    assert b"sm_103a" in L.fg_version()
+
+
+@pytest.mark.parametrize("dims,mn,mx,r", [(3, (0, 0, 0), (64, 64, 64), 2.0), (3, (0, 0, 0), (50.1, 50.1, 50.1), 10.0),
+                                          (2, (0, 0), (11, 11), 1.0), (3, (141, -540, 200), (211, -470, 270), 3.5),
+                                          (3, (-0.5, -0.5, -0.5), (0.5, 0.5, 0.5), 0.05)])
+def test_grid_init_matches_oracle(dims, mn, mx, r):
+    capi = _capi()
+    g = capi.grid(dims, mn, mx, r)
+    o = O.grid(dims, mn, mx, r)
+    assert tuple(g.gridDim) == tuple(o.gridDim)
+    assert g.binCount == o.binCount
+    assert g.wrapCompatible == o.wrapCompatible
+    assert list(g.width) == list(o.width)
+
+
+def test_grid_init_rejects_bad_arguments():
+    capi = _capi()
+    g = capi.SpatialGrid()
+    mn = (C.c_float * 3)(0, 0, 0)
+    mx = (C.c_float * 3)(1, 1, 1)
+    assert capi.lib().fg_spatial_grid_init(C.byref(g), 3, mn, mx, 0.0) == capi.FG_ERR_INVALID_ARGUMENT
+    assert capi.lib().fg_spatial_grid_init(C.byref(g), 4, mn, mx, 1.0) == capi.FG_ERR_INVALID_ARGUMENT
+    assert capi.lib().fg_spatial_grid_init(C.byref(g), 3, mx, mn, 1.0) == capi.FG_ERR_INVALID_ARGUMENT
+
+
+def test_workspace_sizes():
+    capi = _capi()
+    L = capi.lib()
+    assert L.fg_spatial_build_workspace_size(1000, 125) >= 256 + 3 * 4000
+    assert L.fg_compact_workspace_size(4 << 20) >= 256 + 2 * 8 * 2048
+    g = capi.grid(3, (0, 0, 0), (64, 64, 64), 2.0)
+    assert L.fg_spatial_sort_workspace_size(16384, C.byref(g)) > L.fg_spatial_build_workspace_size(16384, 32768)
+
+
+# ----------------------------------------------------------------------- GPU
+
+
+def _positions(rng, n, mn, mx, kind):
+    mn, mx = np.array(mn, np.float32), np.array(mx, np.float32)
+    d = len(mn)
+    if kind == "uniform":
+        p = rng.uniform(mn, mx, (n, d))
+    elif kind == "outside":  # exercise the clamping of out-of-bounds positions
+        w = mx - mn
+        p = rng.uniform(mn - 0.3 * w, mx + 0.3 * w, (n, d))
+    elif kind == "clusters":  # heavy-tailed bins: long-bin path
+        centres = rng.uniform(mn, mx, (4, d))
+        p = centres[rng.integers(0, 4, n)] + rng.normal(0, 0.02 * (mx - mn).max(), (n, d))
+        p = np.clip(p, mn, mx)
+    elif kind == "onebin":
+        p = np.tile(((mn + mx) / 2)[None, :], (n, 1)) + rng.uniform(0, 1e-3, (n, d))
+    return p.astype(np.float32)
+
+
+def _build(g, pos, valid=None, d_count=None, extra_words=3, ws=None, reps=1):
+    import torch
+    capi = _capi()
+    n = pos.shape[0]
+    dev = "cuda"
+    cols = [torch.from_numpy(np.ascontiguousarray(pos[:, a])).to(dev) for a in range(pos.shape[1])]
+    payload = torch.arange(n * extra_words, dtype=torch.int32, device=dev).reshape(n, extra_words) * 7 + 3
+    rec = capi.record_desc(cols + [payload])
+    sorted_ = torch.zeros((max(n, 1), rec.words), dtype=torch.int32, device=dev)
+    pbm = torch.zeros(g.binCount + 1, dtype=torch.int32, device=dev)
+    if ws is None:
+        ws = capi.Workspace(capi.lib().fg_spatial_build_workspace_size(max(n, 1), g.binCount))
+    vt = None if valid is None else torch.from_numpy(valid.astype(np.uint32)).to(dev)
+    dn = None if d_count is None else torch.tensor([d_count], dtype=torch.int32, device=dev)
+    for _ in range(reps):
+        rc = capi.lib().fg_spatial_build(C.byref(g), n, capi.ptr(dn), cols[0].data_ptr(), cols[1].data_ptr(),
+                                         cols[2].data_ptr() if len(cols) == 3 else None, capi.ptr(vt), C.byref(rec),
+                                         sorted_.data_ptr(), pbm.data_ptr(), ws.ptr, ws.nbytes, capi.stream_handle())
+        capi.check(rc, "fg_spatial_build")
+    torch.cuda.synchronize()
+    assert ws.status() == 0
+    return pbm.cpu().numpy().view(np.uint32), sorted_.cpu().numpy().view(np.uint32), payload.cpu().numpy(), rec
+
+
+def _expect(g, pos, valid=None, d_count=None):
+    n = pos.shape[0] if d_count is None else d_count
+    keep = np.arange(n) if valid is None else np.nonzero(valid[:n])[0]
+    sub = pos[keep]
+    og = O.grid(g.dims, list(g.min)[:g.dims], list(g.max)[:g.dims], g.radius)
+    pbm, perm, _ = O.spatial_build(og, *[sub[:, a] for a in range(pos.shape[1])])
+    return pbm, keep[perm]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [0, 1, 17, 5000, 100_003])
+@pytest.mark.parametrize("kind", ["uniform", "outside", "clusters"])
+def test_spatial3d_build_parity(n, kind):
+    rng = np.random.default_rng(n + len(kind))
+    g = _capi().grid(3, (0, 0, 0), (64, 64, 64), 2.0)
+    pos = _positions(rng, n, (0, 0, 0), (64, 64, 64), kind)
+    pbm, srt, payload, rec = _build(g, pos)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    m = int(epbm[-1])
+    assert m == n
+    # sorted records: x,y,z words then the payload, in the oracle's stable order
+    np.testing.assert_array_equal(srt[:m, 0:3].view(np.float32), pos[eperm])
+    np.testing.assert_array_equal(srt[:m, 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [3000, 70_000])
+def test_spatial2d_build_parity(n):
+    rng = np.random.default_rng(7)
+    g = _capi().grid(2, (0, 0), (400, 400), 4.0)
+    pos = _positions(rng, n, (0, 0), (400, 400), "clusters")
+    pbm, srt, payload, _ = _build(g, pos, extra_words=2)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    np.testing.assert_array_equal(srt[:n, 0:2].view(np.float32), pos[eperm])
+    np.testing.assert_array_equal(srt[:n, 2:4].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
+def test_build_optional_and_device_count():
+    rng = np.random.default_rng(11)
+    g = _capi().grid(3, (0, 0, 0), (20, 20, 20), 1.0)
+    pos = _positions(rng, 20000, (0, 0, 0), (20, 20, 20), "uniform")
+    valid = rng.random(20000) < 0.8
+    pbm, srt, payload, _ = _build(g, pos, valid=valid, d_count=15000)
+    epbm, eperm = _expect(g, pos, valid=valid, d_count=15000)
+    np.testing.assert_array_equal(pbm, epbm)
+    m = int(epbm[-1])
+    np.testing.assert_array_equal(srt[:m, 0:3].view(np.float32), pos[eperm])
+    np.testing.assert_array_equal(srt[:m, 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
+def test_build_one_heavy_bin_and_reuse():
+    # 40k messages in one bin: the long-bin path with 157 chunks; repeated
+    # builds on one workspace (histogram kept zero, scan epochs advance).
+    rng = np.random.default_rng(3)
+    g = _capi().grid(3, (0, 0, 0), (8, 8, 8), 1.0)
+    pos = _positions(rng, 40000, (0, 0, 0), (8, 8, 8), "onebin")
+    pbm, srt, payload, _ = _build(g, pos, reps=3)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    np.testing.assert_array_equal(srt[:40000, 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 4095, 4096, 4097, 1_000_000, 17_000_001])
+def test_exclusive_scan(n):
+    import torch
+    capi = _capi()
+    rng = np.random.default_rng(n % 1000)
+    a = rng.integers(0, 5, n).astype(np.uint32)
+    t = torch.from_numpy(a.view(np.int32)).cuda()
+    out = torch.empty_like(t)
+    ws = capi.Workspace(capi.lib().fg_scan_workspace_size(n))
+    for _ in range(2):
+        capi.check(capi.lib().fg_exclusive_scan_u32(t.data_ptr(), out.data_ptr(), n, ws.ptr, ws.nbytes,
+                                                   capi.stream_handle()), "scan")
+    torch.cuda.synchronize()
+    expect = (np.cumsum(a.astype(np.uint64)) - a).astype(np.uint32)
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), expect)
+    assert ws.status() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,n,kind", [(3, 16384, "uniform"), (3, 50000, "outside"), (2, 30000, "clusters")])
+def test_spatial_sort_agents_parity(dims, n, kind):
+    import torch
+    capi = _capi()
+    rng = np.random.default_rng(n)
+    mn, mx = (0,) * dims, (64,) * dims
+    g = capi.grid(dims, mn, mx, 2.0)
+    pos = _positions(rng, n, mn, mx, kind)
+    cols_in = [torch.from_numpy(np.ascontiguousarray(pos[:, a])).cuda() for a in range(dims)]
+    extra = torch.arange(n, dtype=torch.int64, device="cuda") * 3 + 1  # an 8-byte column
+    tiny = (torch.arange(n, device="cuda") % 251).to(torch.uint8)  # a 1-byte column
+    ins = cols_in + [extra, tiny]
+    outs = [torch.empty_like(c) for c in ins]
+    colarr = capi.columns(list(zip(ins, outs)))
+    perm = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ws = capi.Workspace(capi.lib().fg_spatial_sort_workspace_size(n, C.byref(g)))
+    rc = capi.lib().fg_spatial_sort_agents(C.byref(g), n, None, cols_in[0].data_ptr(), cols_in[1].data_ptr(),
+                                           cols_in[2].data_ptr() if dims == 3 else None, colarr, len(ins),
+                                           perm.data_ptr(), ws.ptr, ws.nbytes, capi.stream_handle())
+    capi.check(rc, "fg_spatial_sort_agents")
+    torch.cuda.synchronize()
+    og = O.grid(dims, mn, mx, 2.0)
+    keys = O.sort_keys(og, pos[:, 0], pos[:, 1], pos[:, 2] if dims == 3 else None)
+    eperm = O.stable_sort_perm(keys, O.sort_max_bit(og))
+    np.testing.assert_array_equal(perm.cpu().numpy().view(np.uint32), eperm)
+    for a in range(dims):
+        np.testing.assert_array_equal(outs[a].cpu().numpy(), pos[eperm, a])
+    np.testing.assert_array_equal(outs[dims].cpu().numpy(), extra.cpu().numpy()[eperm])
+    np.testing.assert_array_equal(outs[dims + 1].cpu().numpy(), tiny.cpu().numpy()[eperm])
+    assert ws.status() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [0, 1, 2047, 2048, 2049, 300_001])
+@pytest.mark.parametrize("with_births", [False, True])
+def test_compact_agents_parity(n, with_births):
+    import torch
+    capi = _capi()
+    rng = np.random.default_rng(n + 17 * with_births)
+    cap = 2 * n + 8
+    alive = (rng.random(n) >= 0.3).astype(np.uint32)
+    born = ((rng.random(n) < 0.2) & (alive == 1)).astype(np.uint32) if with_births else None
+    f = rng.random((n, 2)).astype(np.float32)
+    ids = np.arange(1, n + 1, dtype=np.uint32)
+    dev = "cuda"
+    f_in = torch.from_numpy(f).to(dev)
+    id_in = torch.from_numpy(ids.view(np.int32)).to(dev)
+    f_out = torch.zeros((cap, 2), dtype=torch.float32, device=dev)
+    id_out = torch.zeros(cap, dtype=torch.int32, device=dev)
+    bf_in = (f_in * 10 + 1).contiguous()  # birth staging rows: distinguishable values
+    bid_in = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+    cols = capi.columns([(f_in, f_out), (id_in, id_out)])
+    bcols = capi.columns([(bf_in, f_out), (bid_in, id_out)])
+    a_t = torch.from_numpy(alive.view(np.int32)).to(dev)
+    b_t = None if born is None else torch.from_numpy(born.view(np.int32)).to(dev)
+    next_id = torch.tensor([n + 1], dtype=torch.int32, device=dev)
+    d_n = torch.tensor([n], dtype=torch.int32, device=dev)
+    n_out = torch.zeros(1, dtype=torch.int32, device=dev)
+    ws = capi.Workspace(capi.lib().fg_compact_workspace_size(max(n, 1)))
+    rc = capi.lib().fg_compact_agents(max(n, 1) if n else 0, d_n.data_ptr(), a_t.data_ptr() if n else None,
+                                      capi.ptr(b_t) if n else None, cols, bcols, 2, 1, next_id.data_ptr(), None,
+                                      n_out.data_ptr(), cap, ws.ptr, ws.nbytes, capi.stream_handle())
+    capi.check(rc, "fg_compact_agents")
+    torch.cuda.synchronize()
+    surv = O.compact(alive)
+    kids = O.compact(born) if born is not None else np.zeros(0, np.uint32)
+    m = len(surv) + len(kids)
+    assert int(n_out.item()) == m
+    np.testing.assert_array_equal(f_out.cpu().numpy()[:len(surv)], f[surv])
+    np.testing.assert_array_equal(id_out.cpu().numpy().view(np.uint32)[:len(surv)], ids[surv])
+    if len(kids):
+        np.testing.assert_array_equal(f_out.cpu().numpy()[len(surv):m], f[kids] * 10 + 1)
+        np.testing.assert_array_equal(id_out.cpu().numpy().view(np.uint32)[len(surv):m],
+                                      np.arange(n + 1, n + 1 + len(kids), dtype=np.uint32))
+    assert int(next_id.item()) == n + 1 + len(kids)
+    assert ws.status() == 0
