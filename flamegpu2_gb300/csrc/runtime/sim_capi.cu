@@ -1,0 +1,218 @@
+// C ABI over CUDASimulation (include/flamegpu_gb300/fg_sim.h) and the model registry.
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "flamegpu/flamegpu.h"
+#include "flamegpu_gb300/fg_sim.h"
+
+namespace {
+
+std::mutex g_reg_mu;
+std::map<std::string, fgs_model_factory>& registry() {
+    static std::map<std::string, fgs_model_factory> r;
+    return r;
+}
+thread_local std::string g_err;
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        f();
+        return 0;
+    } catch (const flamegpu::exception::FLAMEGPUException& e) {
+        g_err = std::string(e.exception_type()) + ": " + e.what();
+    } catch (const std::exception& e) {
+        g_err = e.what();
+    } catch (...) {
+        g_err = "unknown exception";
+    }
+    return -1;
+}
+
+}  // namespace
+
+struct fgs_sim {
+    std::unique_ptr<flamegpu::ModelDescription> model;
+    std::unique_ptr<flamegpu::CUDASimulation> sim;
+};
+
+namespace {
+
+const flamegpu::detail::EnvProperty* find_env(fgs_sim* s, const char* name) {
+    for (const auto& p : s->model->getData()->environment)
+        if (p.name == name) return &p;
+    throw flamegpu::exception::InvalidEnvProperty(std::string("no environment property ") + name);
+}
+
+}  // namespace
+
+extern "C" int fgs_register_model(const char* name, fgs_model_factory f) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    registry()[name] = f;
+    return 0;
+}
+
+extern "C" int fgs_list_models(char* buf, size_t len) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    std::string s;
+    for (const auto& kv : registry()) s += (s.empty() ? "" : ",") + kv.first;
+    if (len) {
+        std::strncpy(buf, s.c_str(), len - 1);
+        buf[len - 1] = 0;
+    }
+    return 0;
+}
+
+extern "C" const char* fgs_last_error(void) { return g_err.c_str(); }
+
+extern "C" fgs_sim* fgs_create(const char* model, const double* params, int32_t nparams, int32_t device) {
+    fgs_sim* out = nullptr;
+    guarded([&] {
+        fgs_model_factory f = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(g_reg_mu);
+            auto it = registry().find(model);
+            if (it == registry().end()) throw flamegpu::exception::InvalidArgument(std::string("unknown model ") + model);
+            f = it->second;
+        }
+        auto s = std::make_unique<fgs_sim>();
+        s->model.reset(static_cast<flamegpu::ModelDescription*>(f(params, nparams)));
+        if (device != 0) {
+            // the device is chosen before the simulation allocates
+            cudaSetDevice(device);
+        }
+        s->sim = std::make_unique<flamegpu::CUDASimulation>(*s->model);
+        out = s.release();
+    });
+    return out;
+}
+
+extern "C" void fgs_destroy(fgs_sim* s) { delete s; }
+
+extern "C" int fgs_configure(fgs_sim* s, uint32_t steps, uint64_t seed, int32_t graphs, int32_t check) {
+    return guarded([&] {
+        s->sim->SimulationConfig().steps = steps;
+        s->sim->SimulationConfig().random_seed = seed;
+        s->sim->CUDAConfig().use_graphs = graphs != 0;
+        s->sim->CUDAConfig().check_each_step = check != 0;
+        s->sim->applyConfig();
+    });
+}
+
+extern "C" int fgs_set_population(fgs_sim* s, const char* agent, const char* state, uint32_t n, int32_t nvars,
+                                  const char* const* names, const void* const* cols) {
+    return guarded([&] {
+        flamegpu::AgentVector pop(s->model->Agent(agent), n);
+        for (int32_t k = 0; k < nvars; ++k) {
+            const size_t c = pop.columnIndex(names[k]);
+            std::memcpy(pop.columns()[c].data(), cols[k], pop.columns()[c].size());
+        }
+        s->sim->setPopulationData(pop, state);
+    });
+}
+
+extern "C" int fgs_set_population_device(fgs_sim* s, const char* agent, const char* state, uint32_t n, int32_t nvars,
+                                         const char* const* names, const void* const* dcols) {
+    return guarded([&] {
+        // size the lists and assign ids through the host path (defaults only), then
+        // overwrite the given columns device-to-device
+        flamegpu::AgentVector pop(s->model->Agent(agent), n);
+        s->sim->setPopulationData(pop, state);
+        const auto* ad = pop.getAgentData();
+        for (int32_t k = 0; k < nvars; ++k) {
+            const flamegpu::detail::Variable* v = ad->find(names[k]);
+            if (!v) throw flamegpu::exception::InvalidAgentVar(std::string("no variable ") + names[k]);
+            void* dst = s->sim->getDeviceVariable(agent, names[k], state);
+            if (cudaMemcpyAsync(dst, dcols[k], static_cast<size_t>(v->bytes()) * n, cudaMemcpyDeviceToDevice,
+                                s->sim->getStream()) != cudaSuccess)
+                throw flamegpu::exception::CUDAError("device population copy failed");
+        }
+        cudaStreamSynchronize(s->sim->getStream());
+    });
+}
+
+extern "C" int fgs_get_count(fgs_sim* s, const char* agent, const char* state, uint32_t* n) {
+    return guarded([&] { *n = s->sim->getAgentCount(agent, state); });
+}
+
+extern "C" int fgs_get_variable(fgs_sim* s, const char* agent, const char* state, const char* var, void* out,
+                                size_t bytes) {
+    return guarded([&] {
+        flamegpu::AgentVector pop(s->model->Agent(agent));
+        s->sim->getPopulationData(pop, state);
+        const size_t c = pop.columnIndex(var);
+        const auto& col = pop.columns()[c];
+        if (bytes < col.size()) throw flamegpu::exception::InvalidArgument("output buffer too small");
+        std::memcpy(out, col.data(), col.size());
+    });
+}
+
+extern "C" int fgs_get_variable_device(fgs_sim* s, const char* agent, const char* state, const char* var, void* dst,
+                                       size_t bytes) {
+    return guarded([&] {
+        void* src = s->sim->getDeviceVariable(agent, var, state);
+        if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s->sim->getStream()) != cudaSuccess)
+            throw flamegpu::exception::CUDAError("device copy failed");
+    });
+}
+
+extern "C" int fgs_step(fgs_sim* s, uint32_t steps) {
+    return guarded([&] {
+        for (uint32_t i = 0; i < steps; ++i) s->sim->step();
+    });
+}
+
+extern "C" int fgs_simulate(fgs_sim* s) { return guarded([&] { s->sim->simulate(); }); }
+
+extern "C" int fgs_synchronize(fgs_sim* s) { return guarded([&] { s->sim->synchronize(); }); }
+
+extern "C" int fgs_set_environment(fgs_sim* s, const char* name, const void* value, size_t bytes) {
+    return guarded([&] {
+        const auto* p = find_env(s, name);
+        if (bytes != p->value.size()) throw flamegpu::exception::InvalidEnvPropertyType("size mismatch");
+        flamegpu::HostAPI::Environment e(s->sim->getImpl());
+        if (p->type == std::type_index(typeid(float))) e.setProperty<float>(name, *static_cast<const float*>(value));
+        else if (p->type == std::type_index(typeid(double))) e.setProperty<double>(name, *static_cast<const double*>(value));
+        else if (p->type == std::type_index(typeid(int32_t))) e.setProperty<int32_t>(name, *static_cast<const int32_t*>(value));
+        else if (p->type == std::type_index(typeid(uint32_t))) e.setProperty<uint32_t>(name, *static_cast<const uint32_t*>(value));
+        else throw flamegpu::exception::InvalidEnvPropertyType("unsupported property type for the C ABI");
+    });
+}
+
+extern "C" int fgs_get_environment(fgs_sim* s, const char* name, void* value, size_t bytes) {
+    return guarded([&] {
+        const auto* p = find_env(s, name);
+        if (bytes != p->value.size()) throw flamegpu::exception::InvalidEnvPropertyType("size mismatch");
+        flamegpu::HostAPI::Environment e(s->sim->getImpl());
+        if (p->type == std::type_index(typeid(float))) *static_cast<float*>(value) = e.getProperty<float>(name);
+        else if (p->type == std::type_index(typeid(double))) *static_cast<double*>(value) = e.getProperty<double>(name);
+        else if (p->type == std::type_index(typeid(int32_t))) *static_cast<int32_t*>(value) = e.getProperty<int32_t>(name);
+        else if (p->type == std::type_index(typeid(uint32_t))) *static_cast<uint32_t*>(value) = e.getProperty<uint32_t>(name);
+        else throw flamegpu::exception::InvalidEnvPropertyType("unsupported property type for the C ABI");
+    });
+}
+
+extern "C" int fgs_stream(fgs_sim* s, void** stream) {
+    return guarded([&] { *stream = s->sim->getStream(); });
+}
+
+extern "C" int fgs_stats(fgs_sim* s, uint64_t* gl, uint32_t* kps, uint32_t* sc) {
+    return guarded([&] {
+        if (gl) *gl = s->sim->getGraphLaunches();
+        if (kps) *kps = s->sim->getKernelsPerStep();
+        if (sc) *sc = s->sim->getStepCounter();
+    });
+}
+
+extern "C" int fgs_step_times(fgs_sim* s, double* out, uint32_t cap, uint32_t* n) {
+    return guarded([&] {
+        s->sim->synchronize();
+        const auto t = s->sim->getElapsedTimeSteps();
+        const uint32_t m = static_cast<uint32_t>(std::min<size_t>(cap, t.size()));
+        for (uint32_t i = 0; i < m; ++i) out[i] = t[i];
+        *n = m;
+    });
+}

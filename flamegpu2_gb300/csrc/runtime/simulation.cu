@@ -1,0 +1,1037 @@
+// CUDASimulation on GB300.
+//
+// Per step, in layer order and for each agent function (the reference's
+// CUDASimulation::stepLayer, src/flamegpu/simulation/CUDASimulation.cu:644-1109):
+//   1. automatic spatial sort of the agent list if the function reads a
+//      spatial message (fg_spatial_sort_agents; :670-681)
+//   2. spatial index build of the input message list if it changed
+//      (fg_spatial_build; CUDAMessage::buildIndex :864)
+//   3. the agent function kernel (templated in the model's translation unit)
+//   4. birth/death compaction (fg_compact_agents; processDeath/scatterNew :1064-1081)
+// Everything is issued on one stream without host synchronisation: counts
+// stay on the device, grids are sized by capacity. The whole step is captured
+// once into a CUDA graph per "buffer parity" state (sorts and compactions
+// ping-pong each agent list between two buffers) and replayed. The host
+// synchronises only when a population might outgrow its buffers (births) or
+// when data is read back.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "flamegpu/simulation/CUDASimulation.h"
+#include "flamegpu_gb300/fg_capi.h"
+
+namespace flamegpu {
+namespace detail {
+
+using exception::format;
+
+#define FG_CUDA(call)                                                                                      \
+    do {                                                                                                   \
+        const cudaError_t _e = (call);                                                                     \
+        if (_e != cudaSuccess)                                                                             \
+            THROW exception::CUDAError(format("%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__)); \
+    } while (0)
+
+#define FG_CAPI(call)                                                                                      \
+    do {                                                                                                   \
+        const int _r = (call);                                                                             \
+        if (_r != FG_OK) THROW exception::CUDAError(format("%s returned %d (%s:%d)", #call, _r, __FILE__, __LINE__)); \
+    } while (0)
+
+namespace {
+
+__global__ void k_step_increment(uint32_t* d_step) { *d_step += 1; }
+__global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
+
+struct DevMem {
+    std::vector<void*> ptrs;
+    void* alloc(size_t bytes, bool zero = true) {
+        void* p = nullptr;
+        FG_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 256)));
+        if (zero) FG_CUDA(cudaMemset(p, 0, std::max<size_t>(bytes, 256)));
+        ptrs.push_back(p);
+        return p;
+    }
+    void release(void* p) {
+        if (!p) return;
+        auto it = std::find(ptrs.begin(), ptrs.end(), p);
+        if (it != ptrs.end()) {
+            cudaFree(p);
+            ptrs.erase(it);
+        }
+    }
+    ~DevMem() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+uint32_t round4(uint32_t b) { return (b + 3u) & ~3u; }
+
+int sm_count(int dev) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 132;
+}
+
+}  // namespace
+
+struct AgentList {
+    AgentData* agent = nullptr;
+    std::string state;
+    uint32_t capacity = 0;
+    std::vector<std::array<void*, 2>> cols;  // per agent variable, ping-pong buffers
+    int parity = 0;
+    uint32_t* d_count = nullptr;
+    uint32_t bound = 0;                       // host upper bound of the device count
+    std::map<const void*, std::pair<void*, size_t>> sort_ws;  // per sorting message grid
+    void* comp_ws = nullptr;
+    size_t comp_ws_bytes = 0;
+    int var_index(const std::string& n) const {
+        for (size_t v = 0; v < agent->variables.size(); ++v)
+            if (agent->variables[v].name == n) return static_cast<int>(v);
+        return -1;
+    }
+};
+
+struct MsgList {
+    MessageData* msg = nullptr;
+    uint32_t capacity = 0;
+    std::vector<uint32_t> slot_bytes;  // per variable, rounded up to 4 bytes
+    std::vector<void*> cols;           // unsorted struct-of-arrays, written by the output function
+    uint32_t* valid = nullptr;         // per-row output flags when any output is optional
+    uint32_t* d_count = nullptr;
+    bool optional_any = false;
+    // spatial
+    fg_spatial_grid grid{};
+    uint32_t* pbm = nullptr;
+    uint32_t* records = nullptr;
+    uint32_t record_words = 0;
+    std::vector<uint32_t> field_word;
+    void* build_ws = nullptr;
+    size_t build_ws_bytes = 0;
+    // brute force with optional output: compacted copy
+    std::vector<void*> bf_cols;
+    uint32_t* bf_count = nullptr;
+    void* bf_ws = nullptr;
+    size_t bf_ws_bytes = 0;
+    bool needs_build = true;
+    bool spatial() const { return msg->kind != MessageKind::BruteForce; }
+};
+
+struct FnRt {
+    AgentFunctionData* fn = nullptr;
+    AgentList* list = nullptr;
+    MsgList* in = nullptr;
+    MsgList* out = nullptr;
+    bool births = false;
+    uint32_t* death_flags = nullptr;
+    uint32_t* birth_flags = nullptr;
+    std::vector<void*> birth_cols;
+    void* birth_defaults = nullptr;
+    FunctionTables* d_tables[2] = {nullptr, nullptr};
+    bool sort_trigger = false;
+};
+
+struct SimulationImpl {
+    std::shared_ptr<ModelData> model;
+    CUDASimulation::SimConfig config;
+    CUDASimulation::Config cuda_config;
+    int device = 0;
+    int sms = 132;
+    cudaStream_t stream = nullptr;
+    DevMem mem;
+    std::vector<std::unique_ptr<AgentList>> lists;
+    std::vector<std::unique_ptr<MsgList>> msgs;
+    std::vector<FnRt> fns;
+    // environment
+    std::vector<char> env_host;
+    std::vector<size_t> env_offset;
+    char* d_env = nullptr;
+    bool env_dirty = true;
+    // misc device state
+    uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record, [8..] next ids per agent
+    uint32_t* h_pinned = nullptr;
+    unsigned int step_count = 0;
+    std::vector<uint32_t> next_id;  // host mirror per agent index (valid when synced)
+    bool ids_on_device = true;
+    // graphs
+    std::map<std::vector<int>, cudaGraphExec_t> graphs;
+    unsigned long long graph_launches = 0;
+    unsigned int kernels_last_step = 0;
+    unsigned int kernel_counter = 0;
+    bool allocated = false;
+    // timing
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> step_events;
+    std::vector<double> step_ms;
+    double sim_ms = 0.0;
+
+    explicit SimulationImpl(const std::shared_ptr<ModelData>& m) : model(m) {}
+    ~SimulationImpl() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        for (auto& e : step_events) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+        if (h_pinned) cudaFreeHost(h_pinned);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    uint32_t* d_step() const { return d_misc; }
+    uint32_t* d_error() const { return d_misc + 1; }
+    uint32_t* d_next_id(size_t agent_idx) const { return d_misc + 8 + agent_idx; }
+
+    size_t agent_index(const AgentData* a) const {
+        for (size_t i = 0; i < model->agents.size(); ++i)
+            if (model->agents[i].get() == a) return i;
+        return 0;
+    }
+
+    AgentList* list_of(const std::string& agent, const std::string& state) {
+        for (auto& l : lists)
+            if (l->agent->name == agent && l->state == state) return l.get();
+        THROW exception::InvalidAgentName(format("No agent list '%s' in state '%s'", agent.c_str(), state.c_str()));
+    }
+    MsgList* msg_of(const std::string& name) {
+        for (auto& m : msgs)
+            if (m->msg->name == name) return m.get();
+        return nullptr;
+    }
+
+    // ------------------------------------------------------------- set-up
+
+    void init() {
+        FG_CUDA(cudaSetDevice(cuda_config.device_id));
+        device = cuda_config.device_id;
+        sms = sm_count(device);
+        FG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        FG_CUDA(cudaMallocHost(&h_pinned, 4096));
+        std::memset(h_pinned, 0, 4096);
+        d_misc = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (8 + model->agents.size() + 8)));
+        next_id.assign(model->agents.size(), 1u);
+        std::vector<uint32_t> init_ids(model->agents.size(), 1u);
+        FG_CUDA(cudaMemcpy(d_misc + 8, init_ids.data(), sizeof(uint32_t) * init_ids.size(), cudaMemcpyHostToDevice));
+        validate_model();
+        // environment buffer (8-byte aligned properties)
+        size_t off = 0;
+        for (const auto& p : model->environment) {
+            env_offset.push_back(off);
+            off += (p.value.size() + 7) & ~size_t(7);
+        }
+        env_host.assign(std::max<size_t>(off, 8), 0);
+        for (size_t i = 0; i < model->environment.size(); ++i)
+            std::memcpy(env_host.data() + env_offset[i], model->environment[i].value.data(), model->environment[i].value.size());
+        d_env = static_cast<char*>(mem.alloc(env_host.size()));
+        FG_CUDA(cudaMemcpy(d_env, env_host.data(), env_host.size(), cudaMemcpyHostToDevice));
+        env_dirty = false;
+        // agent lists (one per state)
+        for (const auto& a : model->agents)
+            for (const auto& s : a->states) {
+                auto l = std::make_unique<AgentList>();
+                l->agent = a.get();
+                l->state = s;
+                l->cols.resize(a->variables.size(), {nullptr, nullptr});
+                l->d_count = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
+                lists.push_back(std::move(l));
+            }
+        for (const auto& m : model->messages) {
+            auto ml = std::make_unique<MsgList>();
+            ml->msg = m.get();
+            ml->d_count = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
+            for (const auto& v : m->variables) ml->slot_bytes.push_back(round4(v.bytes()));
+            if (m->kind != MessageKind::BruteForce) {
+                const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
+                FG_CAPI(fg_spatial_grid_init(&ml->grid, dims, m->min, m->max, m->radius));
+                ml->pbm = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(ml->grid.binCount) + 1)));
+                uint32_t w = 0;
+                for (uint32_t b : ml->slot_bytes) {
+                    ml->field_word.push_back(w);
+                    w += b / 4;
+                }
+                ml->record_words = std::max(4u, (w + 3u) & ~3u);
+                if (ml->record_words > FG_MAX_RECORD_WORDS)
+                    THROW exception::InvalidMessage(format("Message '%s' is larger than %d bytes", m->name.c_str(), FG_MAX_RECORD_WORDS * 4));
+            }
+            msgs.push_back(std::move(ml));
+        }
+        for (const auto& a : model->agents)
+            for (const auto& f : a->functions) {
+                if (f->initial_state != f->end_state)
+                    THROW exception::InvalidAgentFunc(format("Function '%s': agent state transitions are not supported yet", f->name.c_str()));
+                FnRt r;
+                r.fn = f.get();
+                r.list = list_of(a->name, f->initial_state);
+                r.in = f->message_input.empty() ? nullptr : msg_of(f->message_input);
+                r.out = f->message_output.empty() ? nullptr : msg_of(f->message_output);
+                if (r.out && f->message_output_optional) r.out->optional_any = true;
+                if (!f->agent_output.empty()) {
+                    if (f->agent_output != a->name || f->agent_output_state != f->initial_state)
+                        THROW exception::InvalidAgentFunc(format("Function '%s': agent output into another agent or state is not supported yet", f->name.c_str()));
+                    r.births = true;
+                }
+                // determineAgentsToSort (CUDASimulation.cu:409-461)
+                if (r.in && r.in->spatial()) {
+                    const int dims = r.in->msg->kind == MessageKind::Spatial3D ? 3 : 2;
+                    bool ok = true;
+                    const char* ax[3] = {"x", "y", "z"};
+                    for (int d = 0; d < dims; ++d) {
+                        const Variable* v = a->find(ax[d]);
+                        ok = ok && v && v->type == std::type_index(typeid(float)) && v->elements == 1;
+                    }
+                    r.sort_trigger = ok;
+                }
+                fns.push_back(std::move(r));
+            }
+    }
+
+    void validate_model() {
+        for (const auto& m : model->messages) {
+            if (m->kind == MessageKind::BruteForce) continue;
+            const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
+            if (std::isnan(m->radius))
+                THROW exception::InvalidMessage(format("Spatial message '%s' has no radius", m->name.c_str()));
+            for (int d = 0; d < dims; ++d)
+                if (std::isnan(m->min[d]) || std::isnan(m->max[d]))
+                    THROW exception::InvalidMessage(format("Spatial message '%s' has unset bounds", m->name.c_str()));
+        }
+        for (const auto& l : model->layers)
+            if (!l->host_functions.empty() && !l->functions.empty())
+                THROW exception::InvalidArgument("A layer may hold agent functions or host functions, not both");
+    }
+
+    // Allocate (or grow) an agent list to `cap` rows, keeping `keep` rows.
+    void ensure_capacity(AgentList& l, uint32_t cap, uint32_t keep) {
+        if (cap <= l.capacity) return;
+        const uint32_t old_cap = l.capacity;
+        for (size_t v = 0; v < l.cols.size(); ++v) {
+            const size_t b = l.agent->variables[v].bytes();
+            void* n0 = mem.alloc(b * cap, false);
+            void* n1 = mem.alloc(b * cap, false);
+            if (l.cols[v][l.parity] && keep)
+                FG_CUDA(cudaMemcpyAsync(n0, l.cols[v][l.parity], b * keep, cudaMemcpyDeviceToDevice, stream));
+            mem.release(l.cols[v][0]);
+            mem.release(l.cols[v][1]);
+            l.cols[v] = {n0, n1};
+        }
+        l.parity = 0;
+        l.capacity = cap;
+        for (auto& s : l.sort_ws) mem.release(s.second.first);
+        l.sort_ws.clear();
+        mem.release(l.comp_ws);
+        l.comp_ws_bytes = fg_compact_workspace_size(cap);
+        l.comp_ws = mem.alloc(l.comp_ws_bytes);
+        (void)old_cap;
+        // dependants: message lists written by this list's functions, birth staging, flags
+        for (auto& f : fns) {
+            if (f.list != &l) continue;
+            if (f.out) ensure_msg_capacity(*f.out, cap);
+            if (f.fn->has_agent_death) {
+                mem.release(f.death_flags);
+                f.death_flags = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
+            }
+            if (f.births) {
+                mem.release(f.birth_flags);
+                f.birth_flags = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
+                for (void* p : f.birth_cols) mem.release(p);
+                f.birth_cols.clear();
+                for (const auto& v : l.agent->variables) f.birth_cols.push_back(mem.alloc(static_cast<size_t>(v.bytes()) * cap));
+            }
+        }
+        invalidate();
+    }
+
+    void ensure_msg_capacity(MsgList& m, uint32_t cap) {
+        if (cap <= m.capacity) return;
+        for (void* p : m.cols) mem.release(p);
+        m.cols.clear();
+        for (uint32_t b : m.slot_bytes) m.cols.push_back(mem.alloc(static_cast<size_t>(b) * cap));
+        if (m.optional_any) {
+            mem.release(m.valid);
+            m.valid = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
+        }
+        if (m.spatial()) {
+            mem.release(m.records);
+            m.records = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * m.record_words * static_cast<size_t>(cap)));
+            mem.release(m.build_ws);
+            m.build_ws_bytes = fg_spatial_build_workspace_size(cap, m.grid.binCount);
+            m.build_ws = mem.alloc(m.build_ws_bytes);
+        } else if (m.optional_any) {
+            for (void* p : m.bf_cols) mem.release(p);
+            m.bf_cols.clear();
+            for (uint32_t b : m.slot_bytes) m.bf_cols.push_back(mem.alloc(static_cast<size_t>(b) * cap));
+            if (!m.bf_count) m.bf_count = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
+            mem.release(m.bf_ws);
+            m.bf_ws_bytes = fg_compact_workspace_size(cap);
+            m.bf_ws = mem.alloc(m.bf_ws_bytes);
+        }
+        m.capacity = cap;
+        invalidate();
+    }
+
+    void invalidate() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+        allocated = false;
+    }
+
+    // Lists with no population yet still need buffers for their functions.
+    void ensure_all_allocated() {
+        if (allocated) return;
+        for (auto& l : lists)
+            if (l->capacity == 0) ensure_capacity(*l, 1024, 0);
+        for (auto& m : msgs)
+            if (m->capacity == 0) ensure_msg_capacity(*m, 1024);
+        // sort workspaces are sized per (list, sorting message grid) up front:
+        // nothing may allocate while a step is being captured
+        for (auto& f : fns) {
+            if (!f.sort_trigger) continue;
+            AgentList& l = *f.list;
+            if (l.sort_ws.count(f.in)) continue;
+            const size_t b = fg_spatial_sort_workspace_size(l.capacity, &f.in->grid);
+            if (!b) THROW exception::InvalidMessage("Spatial grid too large for the automatic agent sort");
+            l.sort_ws.emplace(f.in, std::make_pair(mem.alloc(b), b));
+        }
+        for (auto& f : fns) build_tables(f);
+        allocated = true;
+    }
+
+    // ------------------------------------------------------------- tables
+
+    struct TableEntry {
+        uint32_t hash;
+        char* ptr;
+        uint32_t stride;
+        uint32_t elem_bytes;
+        uint32_t elements;
+    };
+
+    static VarTable make_table(const std::vector<TableEntry>& e, const char* what) {
+        VarTable t;
+        std::memset(&t, 0, sizeof(t));
+        const uint32_t n = static_cast<uint32_t>(e.size());
+        uint32_t size = 2;
+        while (size < n) size <<= 1;
+        std::mt19937 rng(12345u);
+        for (; size <= static_cast<uint32_t>(kMaxVarSlots); size <<= 1) {
+            uint32_t bits = 0;
+            while ((1u << bits) < size) ++bits;
+            const uint32_t shift = 32u - bits;
+            for (int attempt = 0; attempt < 200000; ++attempt) {
+                const uint32_t mult = attempt == 0 ? 1u : (rng() | 1u);
+                uint64_t used = 0;
+                bool ok = true;
+                for (const auto& x : e) {
+                    const uint32_t s = table_slot(mult, shift, x.hash);
+                    if (used & (1ull << s)) {
+                        ok = false;
+                        break;
+                    }
+                    used |= 1ull << s;
+                }
+                if (!ok) continue;
+                t.mult = mult;
+                t.shift = shift;
+                t.count = n;
+                for (const auto& x : e) {
+                    VarSlot& s = t.slot[table_slot(mult, shift, x.hash)];
+                    s.ptr = x.ptr;
+                    s.stride = x.stride;
+                    s.hash = x.hash;
+                    s.elem_bytes = x.elem_bytes;
+                    s.elements = x.elements;
+                }
+                return t;
+            }
+        }
+        THROW exception::InvalidArgument(format("Too many variables (%u) in one %s for the lookup table", n, what));
+    }
+
+    void build_tables(FnRt& f) {
+        AgentList& l = *f.list;
+        for (int par = 0; par < 2; ++par) {
+            FunctionTables* T = new FunctionTables;
+            std::memset(T, 0, sizeof(FunctionTables));
+            std::vector<TableEntry> e;
+            for (size_t v = 0; v < l.agent->variables.size(); ++v) {
+                const Variable& var = l.agent->variables[v];
+                e.push_back({fnv1a32(var.name), static_cast<char*>(l.cols[v][par]), var.bytes(), var.type_size, var.elements});
+            }
+            T->agent = make_table(e, "agent");
+            if (f.out) {
+                e.clear();
+                for (size_t v = 0; v < f.out->msg->variables.size(); ++v) {
+                    const Variable& var = f.out->msg->variables[v];
+                    e.push_back({fnv1a32(var.name), static_cast<char*>(f.out->cols[v]), f.out->slot_bytes[v], var.type_size, var.elements});
+                }
+                T->msg_out = make_table(e, "message");
+            }
+            if (f.in) {
+                e.clear();
+                for (size_t v = 0; v < f.in->msg->variables.size(); ++v) {
+                    const Variable& var = f.in->msg->variables[v];
+                    char* p;
+                    uint32_t stride;
+                    if (f.in->spatial()) {
+                        p = reinterpret_cast<char*>(f.in->records + f.in->field_word[v]);
+                        stride = f.in->record_words * 4;
+                    } else {
+                        p = static_cast<char*>(f.in->optional_any ? f.in->bf_cols[v] : f.in->cols[v]);
+                        stride = f.in->slot_bytes[v];
+                    }
+                    e.push_back({fnv1a32(var.name), p, stride, var.type_size, var.elements});
+                }
+                T->msg_in = make_table(e, "message");
+            }
+            if (f.births) {
+                e.clear();
+                std::vector<TableEntry> d;
+                std::vector<char> defaults;
+                std::vector<size_t> doff;
+                for (const auto& var : l.agent->variables) {
+                    doff.push_back(defaults.size());
+                    defaults.insert(defaults.end(), var.default_value.begin(), var.default_value.end());
+                    defaults.resize((defaults.size() + 7) & ~size_t(7));
+                }
+                if (!f.birth_defaults) f.birth_defaults = mem.alloc(defaults.size());
+                FG_CUDA(cudaMemcpy(f.birth_defaults, defaults.data(), defaults.size(), cudaMemcpyHostToDevice));
+                for (size_t v = 0; v < l.agent->variables.size(); ++v) {
+                    const Variable& var = l.agent->variables[v];
+                    e.push_back({fnv1a32(var.name), static_cast<char*>(f.birth_cols[v]), var.bytes(), var.type_size, var.elements});
+                    d.push_back({fnv1a32(var.name), static_cast<char*>(f.birth_defaults) + doff[v], var.bytes(), var.type_size, var.elements});
+                }
+                T->birth = make_table(e, "agent");
+                T->birth_def = make_table(d, "agent");
+            }
+            e.clear();
+            for (size_t i = 0; i < model->environment.size(); ++i) {
+                const EnvProperty& p = model->environment[i];
+                e.push_back({fnv1a32(p.name), d_env + env_offset[i], 0, p.type_size, p.elements});
+            }
+            T->env = make_table(e, "environment");
+            if (!f.d_tables[par]) f.d_tables[par] = static_cast<FunctionTables*>(mem.alloc(sizeof(FunctionTables)));
+            FG_CUDA(cudaMemcpy(f.d_tables[par], T, sizeof(FunctionTables), cudaMemcpyHostToDevice));
+            delete T;
+        }
+    }
+
+    // ------------------------------------------------------------- step
+
+    uint32_t grid_for(uint32_t n, uint32_t block, int per_sm) const {
+        const uint32_t need = std::max(1u, (n + block - 1) / block);
+        return std::min(need, static_cast<uint32_t>(sms * per_sm));
+    }
+
+    // Capacity check before a step: births can at most double a list per
+    // birth function. Synchronises only if the bound could exceed capacity.
+    void prepare_capacity() {
+        std::vector<uint64_t> bound(lists.size());
+        for (size_t i = 0; i < lists.size(); ++i) bound[i] = lists[i]->bound;
+        bool over = false;
+        for (const auto& layer : model->layers)
+            for (auto* fd : layer->functions) {
+                for (auto& f : fns)
+                    if (f.fn == fd && f.births) {
+                        const size_t li = static_cast<size_t>(std::find_if(lists.begin(), lists.end(), [&](auto& p) { return p.get() == f.list; }) - lists.begin());
+                        bound[li] *= 2;
+                        if (bound[li] > f.list->capacity) over = true;
+                    }
+            }
+        if (!over) {
+            for (size_t i = 0; i < lists.size(); ++i) lists[i]->bound = static_cast<uint32_t>(std::min<uint64_t>(bound[i], 0xFFFFFFFFu));
+            return;
+        }
+        // exact counts, then grow what needs it
+        sync_counts();
+        for (size_t i = 0; i < lists.size(); ++i) bound[i] = lists[i]->bound;
+        for (const auto& layer : model->layers)
+            for (auto* fd : layer->functions)
+                for (auto& f : fns)
+                    if (f.fn == fd && f.births) {
+                        const size_t li = static_cast<size_t>(std::find_if(lists.begin(), lists.end(), [&](auto& p) { return p.get() == f.list; }) - lists.begin());
+                        bound[li] *= 2;
+                    }
+        for (size_t i = 0; i < lists.size(); ++i) {
+            if (bound[i] > lists[i]->capacity) {
+                if (bound[i] >= (1ull << 31)) THROW exception::OutOfMemory("Population bound exceeds 2^31 agents");
+                ensure_capacity(*lists[i], static_cast<uint32_t>(std::max<uint64_t>(bound[i], 2ull * lists[i]->capacity)), lists[i]->bound);
+            }
+            lists[i]->bound = static_cast<uint32_t>(bound[i]);
+        }
+        ensure_all_allocated();
+    }
+
+    void sync_counts() {
+        FG_CUDA(cudaStreamSynchronize(stream));
+        for (auto& l : lists) {
+            uint32_t c = 0;
+            FG_CUDA(cudaMemcpy(&c, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            l->bound = c;
+        }
+    }
+
+    std::vector<int> step_key() const {
+        std::vector<int> k;
+        for (const auto& l : lists) k.push_back(l->parity);
+        for (const auto& layer : model->layers)
+            for (auto* fd : layer->functions) {
+                const unsigned p = fd->parent->sort_period;
+                k.push_back(p != 0 && step_count % p == 0);
+            }
+        return k;
+    }
+
+    void enqueue_sort(FnRt& f) {
+        AgentList& l = *f.list;
+        const fg_spatial_grid* g = &f.in->grid;
+        auto it = l.sort_ws.find(f.in);
+        if (it == l.sort_ws.end()) THROW exception::InvalidOperation("Sort workspace missing (not allocated before capture)");
+        std::vector<fg_column> cols(l.cols.size());
+        for (size_t v = 0; v < l.cols.size(); ++v)
+            cols[v] = fg_column{l.cols[v][l.parity], l.cols[v][l.parity ^ 1], l.agent->variables[v].bytes()};
+        const int xi = l.var_index("x"), yi = l.var_index("y"), zi = l.var_index("z");
+        FG_CAPI(fg_spatial_sort_agents(g, l.capacity, l.d_count, static_cast<const float*>(l.cols[xi][l.parity]),
+                                       static_cast<const float*>(l.cols[yi][l.parity]),
+                                       g->dims == 3 ? static_cast<const float*>(l.cols[zi][l.parity]) : nullptr,
+                                       cols.data(), static_cast<uint32_t>(cols.size()), nullptr, it->second.first,
+                                       it->second.second, stream));
+        l.parity ^= 1;
+        kernel_counter += 6;
+    }
+
+    void enqueue_build(MsgList& m) {
+        fg_record_desc rec;
+        std::memset(&rec, 0, sizeof(rec));
+        rec.words = m.record_words;
+        uint32_t w = 0;
+        for (size_t v = 0; v < m.cols.size(); ++v) {
+            const uint32_t words = m.slot_bytes[v] / 4;
+            for (uint32_t k = 0; k < words; ++k, ++w) {
+                rec.src[w] = static_cast<const uint32_t*>(m.cols[v]);
+                rec.src_stride[w] = words;
+                rec.src_word[w] = k;
+            }
+        }
+        const int dims = m.grid.dims;
+        const int xi = 0, yi = 1, zi = 2;  // x, y, z are the first message variables
+        FG_CAPI(fg_spatial_build(&m.grid, m.capacity, m.d_count, static_cast<const float*>(m.cols[xi]),
+                                 static_cast<const float*>(m.cols[yi]), dims == 3 ? static_cast<const float*>(m.cols[zi]) : nullptr,
+                                 m.optional_any ? m.valid : nullptr, &rec, m.records, m.pbm, m.build_ws, m.build_ws_bytes,
+                                 stream));
+        m.needs_build = false;
+        kernel_counter += 5;
+    }
+
+    void enqueue_function(FnRt& f) {
+        AgentList& l = *f.list;
+        if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0) enqueue_sort(f);
+        if (f.in && f.in->spatial() && f.in->needs_build) enqueue_build(*f.in);
+        if (f.out && f.out->optional_any && !f.fn->message_output_optional)
+            FG_CUDA(cudaMemsetAsync(f.out->valid, 1, sizeof(uint32_t) * f.out->capacity, stream));
+        LaunchParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.T = f.d_tables[l.parity];
+        P.max_n = l.capacity;
+        P.d_n = l.d_count;
+        if (f.out) {
+            P.msg_out_valid = f.fn->message_output_optional ? f.out->valid : nullptr;
+            P.msg_out_count = f.out->d_count;
+            P.msg_out_enabled = 1;
+        }
+        if (f.in) {
+            if (f.in->spatial()) {
+                P.in_grid = f.in->grid;
+                P.in_pbm = f.in->pbm;
+                P.in_count = f.in->pbm + f.in->grid.binCount;
+            } else {
+                P.in_count = f.in->optional_any ? f.in->bf_count : f.in->d_count;
+            }
+        }
+        P.birth_flags = f.births ? f.birth_flags : nullptr;
+        P.death_flags = f.fn->has_agent_death ? f.death_flags : nullptr;
+        P.d_step = d_step();
+        P.seed = config.random_seed;
+        P.fn_uid = f.fn->uid;
+        P.error = d_error();
+        const cudaError_t e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 16), kAgentBlock, stream);
+        if (e != cudaSuccess)
+            THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(e)));
+        kernel_counter += 1;
+        if (f.out) {
+            f.out->needs_build = true;
+            if (!f.out->spatial() && f.out->optional_any) {
+                // brute-force optional output: stable compaction of the message rows
+                std::vector<fg_column> cols(f.out->cols.size());
+                for (size_t v = 0; v < cols.size(); ++v) cols[v] = fg_column{f.out->cols[v], f.out->bf_cols[v], f.out->slot_bytes[v]};
+                FG_CAPI(fg_compact_agents(f.out->capacity, f.out->d_count, f.out->valid, nullptr, cols.data(), nullptr,
+                                          static_cast<uint32_t>(cols.size()), -1, nullptr, nullptr, f.out->bf_count,
+                                          f.out->capacity, f.out->bf_ws, f.out->bf_ws_bytes, stream));
+                kernel_counter += 2;
+            }
+        }
+        if (f.fn->has_agent_death || f.births) {
+            std::vector<fg_column> cols(l.cols.size()), bcols(l.cols.size());
+            int id_col = -1;
+            for (size_t v = 0; v < l.cols.size(); ++v) {
+                const uint32_t b = l.agent->variables[v].bytes();
+                cols[v] = fg_column{l.cols[v][l.parity], l.cols[v][l.parity ^ 1], b};
+                bcols[v] = fg_column{f.births ? f.birth_cols[v] : l.cols[v][l.parity], l.cols[v][l.parity ^ 1], b};
+                if (l.agent->variables[v].name == "_id") id_col = static_cast<int>(v);
+            }
+            FG_CAPI(fg_compact_agents(l.capacity, l.d_count, f.fn->has_agent_death ? f.death_flags : nullptr,
+                                      f.births ? f.birth_flags : nullptr, cols.data(), bcols.data(),
+                                      static_cast<uint32_t>(cols.size()), f.births ? id_col : -1,
+                                      f.births ? d_next_id(agent_index(l.agent)) : nullptr, nullptr, l.d_count,
+                                      l.capacity, l.comp_ws, l.comp_ws_bytes, stream));
+            l.parity ^= 1;
+            kernel_counter += 2;
+        }
+    }
+
+    void enqueue_step() {
+        kernel_counter = 0;
+        for (auto& m : msgs)
+            if (!m->msg->persistent) m->needs_build = true;
+        for (const auto& layer : model->layers) {
+            for (auto* fd : layer->functions)
+                for (auto& f : fns)
+                    if (f.fn == fd) enqueue_function(f);
+        }
+        // non-persistent messages are cleared at the end of the step (CUDASimulation.cu:619-625)
+        for (auto& m : msgs)
+            if (!m->msg->persistent) {
+                FG_CUDA(cudaMemsetAsync(m->d_count, 0, sizeof(uint32_t), stream));
+                if (m->bf_count) FG_CUDA(cudaMemsetAsync(m->bf_count, 0, sizeof(uint32_t), stream));
+            }
+        k_step_increment<<<1, 1, 0, stream>>>(d_step());
+        kernel_counter += 1;
+    }
+
+    bool has_layer_host_functions() const {
+        for (const auto& l : model->layers)
+            if (!l->host_functions.empty()) return true;
+        return false;
+    }
+
+    void run_host_layer(LayerData* layer, HostAPI& api) {
+        FG_CUDA(cudaStreamSynchronize(stream));
+        for (auto fn : layer->host_functions) fn(&api);
+        upload_env_if_dirty();
+    }
+
+    void upload_env_if_dirty() {
+        if (!env_dirty) return;
+        FG_CUDA(cudaMemcpyAsync(d_env, env_host.data(), env_host.size(), cudaMemcpyHostToDevice, stream));
+        FG_CUDA(cudaStreamSynchronize(stream));
+        env_dirty = false;
+    }
+
+    void step_once(CUDASimulation* owner) {
+        ensure_all_allocated();
+        prepare_capacity();
+        upload_env_if_dirty();
+        cudaEvent_t e0, e1;
+        FG_CUDA(cudaEventCreate(&e0));
+        FG_CUDA(cudaEventCreate(&e1));
+        FG_CUDA(cudaEventRecord(e0, stream));
+        if (has_layer_host_functions() || !cuda_config.use_graphs) {
+            HostAPI api(this);
+            kernel_counter = 0;
+            for (auto& m : msgs)
+                if (!m->msg->persistent) m->needs_build = true;
+            for (const auto& layer : model->layers) {
+                if (!layer->host_functions.empty()) {
+                    run_host_layer(layer.get(), api);
+                    continue;
+                }
+                for (auto* fd : layer->functions)
+                    for (auto& f : fns)
+                        if (f.fn == fd) enqueue_function(f);
+            }
+            for (auto& m : msgs)
+                if (!m->msg->persistent) {
+                    FG_CUDA(cudaMemsetAsync(m->d_count, 0, sizeof(uint32_t), stream));
+                    if (m->bf_count) FG_CUDA(cudaMemsetAsync(m->bf_count, 0, sizeof(uint32_t), stream));
+                }
+            k_step_increment<<<1, 1, 0, stream>>>(d_step());
+            kernels_last_step = kernel_counter + 1;
+        } else {
+            const std::vector<int> key = step_key();
+            std::vector<int> parity_before;
+            for (auto& l : lists) parity_before.push_back(l->parity);
+            auto it = graphs.find(key);
+            if (it == graphs.end()) {
+                cudaGraph_t g;
+                FG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                try {
+                    enqueue_step();
+                } catch (...) {
+                    cudaStreamEndCapture(stream, &g);
+                    throw;
+                }
+                FG_CUDA(cudaStreamEndCapture(stream, &g));
+                cudaGraphExec_t ge;
+                FG_CUDA(cudaGraphInstantiate(&ge, g, 0));
+                cudaGraphDestroy(g);
+                it = graphs.emplace(key, ge).first;
+                kernels_last_step = kernel_counter;
+            } else {
+                // replay: apply the host-side effects of the step (buffer parities)
+                for (size_t i = 0; i < lists.size(); ++i) lists[i]->parity = parity_before[i];
+                simulate_parity_flips();
+            }
+            FG_CUDA(cudaGraphLaunch(it->second, stream));
+            ++graph_launches;
+        }
+        FG_CUDA(cudaEventRecord(e1, stream));
+        step_events.emplace_back(e0, e1);
+        ++step_count;
+        if (!model->step_functions.empty()) {
+            FG_CUDA(cudaStreamSynchronize(stream));
+            HostAPI api(this);
+            for (auto fn : model->step_functions) fn(&api);
+            upload_env_if_dirty();
+        }
+        if (cuda_config.check_each_step) owner->synchronize();
+    }
+
+    // The parity changes a step makes, replayed on the host for a cached graph.
+    void simulate_parity_flips() {
+        for (const auto& layer : model->layers)
+            for (auto* fd : layer->functions)
+                for (auto& f : fns) {
+                    if (f.fn != fd) continue;
+                    AgentList& l = *f.list;
+                    if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0) l.parity ^= 1;
+                    if (f.fn->has_agent_death || f.births) l.parity ^= 1;
+                }
+    }
+
+    void check_errors() {
+        FG_CUDA(cudaStreamSynchronize(stream));
+        uint32_t err[4] = {0, 0, 0, 0};
+        FG_CUDA(cudaMemcpy(err, d_error(), sizeof(err), cudaMemcpyDeviceToHost));
+        for (auto& m : msgs) {
+            if (m->build_ws) {
+                const int s = fg_workspace_status(m->build_ws, m->build_ws_bytes, stream, 1);
+                if (s != FG_OK) THROW exception::DeviceError(format("Message '%s' index build reported status %d", m->msg->name.c_str(), s));
+            }
+        }
+        for (auto& l : lists) {
+            if (l->comp_ws) {
+                const int s = fg_workspace_status(l->comp_ws, l->comp_ws_bytes, stream, 1);
+                if (s != FG_OK) THROW exception::DeviceError(format("Compaction of agent '%s' reported status %d", l->agent->name.c_str(), s));
+            }
+        }
+        if (err[0] != 0) {
+            FG_CUDA(cudaMemset(d_error(), 0, sizeof(err)));
+            static const char* names[] = {"ok", "unknown variable name", "variable type mismatch", "array index out of bounds",
+                                          "wrapped iterator location outside the environment bounds",
+                                          "spatial radius is not a factor of the environment width (wrapped iterator)",
+                                          "agent death is not enabled for this function",
+                                          "agent output is not enabled for this function", "reserved variable name",
+                                          "unsupported device call", "message output is not enabled for this function"};
+            const char* what = err[0] < sizeof(names) / sizeof(names[0]) ? names[err[0]] : "device error";
+            THROW exception::DeviceError(format("Device error: %s (name hash 0x%08x, agent index %u, %u occurrences)", what,
+                                                err[1], err[2], err[3]));
+        }
+    }
+};
+
+}  // namespace detail
+
+using detail::SimulationImpl;
+using exception::format;
+
+// ------------------------------------------------------------------ HostAPI
+
+void HostAPI::Environment::get(const std::string& name, const std::type_info& t, size_t size, void* out) const {
+    for (size_t i = 0; i < sim->model->environment.size(); ++i) {
+        const auto& p = sim->model->environment[i];
+        if (p.name != name) continue;
+        if (p.type != std::type_index(t) || p.type_size != size)
+            THROW exception::InvalidEnvPropertyType(format("Environment property '%s' has another type", name.c_str()));
+        std::memcpy(out, sim->env_host.data() + sim->env_offset[i], size);
+        return;
+    }
+    THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+}
+
+void HostAPI::Environment::set(const std::string& name, const std::type_info& t, size_t size, const void* in) {
+    for (size_t i = 0; i < sim->model->environment.size(); ++i) {
+        const auto& p = sim->model->environment[i];
+        if (p.name != name) continue;
+        if (p.type != std::type_index(t) || p.type_size != size)
+            THROW exception::InvalidEnvPropertyType(format("Environment property '%s' has another type", name.c_str()));
+        if (p.is_const) THROW exception::ReservedName(format("Environment property '%s' is constant", name.c_str()));
+        std::memcpy(sim->env_host.data() + sim->env_offset[i], in, size);
+        sim->env_dirty = true;
+        return;
+    }
+    THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+}
+
+unsigned int HostAPI::AgentAPI::count() const {
+    detail::AgentList* l = sim->list_of(agent, state);
+    uint32_t c = 0;
+    FG_CUDA(cudaStreamSynchronize(sim->stream));
+    FG_CUDA(cudaMemcpy(&c, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return c;
+}
+
+unsigned int HostAPI::getStepCounter() const { return sim->step_count; }
+
+// ------------------------------------------------------------ CUDASimulation
+
+CUDASimulation::CUDASimulation(const ModelDescription& model, int, const char**)
+    : impl(std::make_unique<SimulationImpl>(model.getData())) {
+    impl->init();
+}
+
+CUDASimulation::~CUDASimulation() = default;
+
+CUDASimulation::SimConfig& CUDASimulation::SimulationConfig() { return impl->config; }
+CUDASimulation::Config& CUDASimulation::CUDAConfig() { return impl->cuda_config; }
+void CUDASimulation::applyConfig() { impl->invalidate(); }
+cudaStream_t CUDASimulation::getStream() const { return impl->stream; }
+unsigned long long CUDASimulation::getGraphLaunches() const { return impl->graph_launches; }
+unsigned int CUDASimulation::getKernelsPerStep() const { return impl->kernels_last_step; }
+
+void CUDASimulation::setPopulationData(AgentVector& pop, const std::string& state) {
+    detail::AgentList* l = impl->list_of(pop.getAgentName(), state);
+    if (l->agent != pop.getAgentData())
+        THROW exception::InvalidArgument("AgentVector belongs to another agent description");
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    const uint32_t n = pop.size();
+    const size_t ai = impl->agent_index(l->agent);
+    // ids: keep set ones, assign fresh ones to unset (CUDAFatAgent.cu:311-319)
+    uint32_t dev_next = 1;
+    FG_CUDA(cudaMemcpy(&dev_next, impl->d_next_id(ai), sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    {
+        const size_t idc = pop.columnIndex("_id");
+        id_t* ids = reinterpret_cast<id_t*>(pop.columns()[idc].data());
+        id_t mx = 0;
+        for (uint32_t i = 0; i < n; ++i) mx = std::max(mx, ids[i]);
+        uint32_t next = std::max<uint32_t>(dev_next, mx + 1);
+        for (uint32_t i = 0; i < n; ++i)
+            if (ids[i] == ID_NOT_SET) ids[i] = next++;
+        FG_CUDA(cudaMemcpy(impl->d_next_id(ai), &next, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
+    const uint32_t cap = std::max<uint32_t>(1024u, n);
+    if (cap > l->capacity) impl->ensure_capacity(*l, cap, 0);
+    for (size_t v = 0; v < l->cols.size(); ++v) {
+        const size_t b = l->agent->variables[v].bytes();
+        if (n) FG_CUDA(cudaMemcpy(l->cols[v][l->parity], pop.columns()[v].data(), b * n, cudaMemcpyHostToDevice));
+    }
+    FG_CUDA(cudaMemcpy(l->d_count, &n, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    l->bound = n;
+    impl->ensure_all_allocated();
+}
+
+void CUDASimulation::getPopulationData(AgentVector& pop, const std::string& state) {
+    detail::AgentList* l = impl->list_of(pop.getAgentName(), state);
+    synchronize();
+    uint32_t n = 0;
+    FG_CUDA(cudaMemcpy(&n, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    l->bound = n;
+    pop.setCountRaw(n);
+    for (size_t v = 0; v < l->cols.size(); ++v) {
+        const size_t b = l->agent->variables[v].bytes();
+        if (n) FG_CUDA(cudaMemcpy(pop.columns()[v].data(), l->cols[v][l->parity], b * n, cudaMemcpyDeviceToHost));
+    }
+}
+
+bool CUDASimulation::step() {
+    if (impl->step_count == 0 && !impl->model->init_functions.empty()) {
+        HostAPI api(impl.get());
+        for (auto fn : impl->model->init_functions) fn(&api);
+    }
+    impl->step_once(this);
+    return true;
+}
+
+void CUDASimulation::simulate() {
+    impl->ensure_all_allocated();
+    cudaEvent_t s0, s1;
+    FG_CUDA(cudaEventCreate(&s0));
+    FG_CUDA(cudaEventCreate(&s1));
+    FG_CUDA(cudaEventRecord(s0, impl->stream));
+    if (!impl->model->init_functions.empty()) {
+        FG_CUDA(cudaStreamSynchronize(impl->stream));
+        HostAPI api(impl.get());
+        for (auto fn : impl->model->init_functions) fn(&api);
+    }
+    for (unsigned int s = 0; s < impl->config.steps; ++s) impl->step_once(this);
+    if (!impl->model->exit_functions.empty()) {
+        FG_CUDA(cudaStreamSynchronize(impl->stream));
+        HostAPI api(impl.get());
+        for (auto fn : impl->model->exit_functions) fn(&api);
+    }
+    FG_CUDA(cudaEventRecord(s1, impl->stream));
+    synchronize();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s0, s1);
+    impl->sim_ms = ms;
+    cudaEventDestroy(s0);
+    cudaEventDestroy(s1);
+}
+
+unsigned int CUDASimulation::getStepCounter() const { return impl->step_count; }
+
+void CUDASimulation::resetStepCounter() {
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    impl->step_count = 0;
+    FG_CUDA(cudaMemset(impl->d_step(), 0, sizeof(uint32_t)));
+}
+
+void CUDASimulation::synchronize() {
+    impl->check_errors();
+    // resolve the step timers
+    for (auto& e : impl->step_events) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e.first, e.second);
+        impl->step_ms.push_back(ms);
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    impl->step_events.clear();
+}
+
+double CUDASimulation::getElapsedTimeSimulation() const { return impl->sim_ms / 1000.0; }
+
+std::vector<double> CUDASimulation::getElapsedTimeSteps() const {
+    std::vector<double> r;
+    for (double ms : impl->step_ms) r.push_back(ms / 1000.0);
+    return r;
+}
+
+double CUDASimulation::getElapsedTimeStep(unsigned int s) const {
+    if (s >= impl->step_ms.size()) THROW exception::OutOfBoundsException(format("Step %u has no timing", s));
+    return impl->step_ms[s] / 1000.0;
+}
+
+unsigned int CUDASimulation::getAgentCount(const std::string& agent, const std::string& state) {
+    HostAPI api(impl.get());
+    return api.agent(agent, state).count();
+}
+
+void* CUDASimulation::getDeviceVariable(const std::string& agent, const std::string& variable, const std::string& state) {
+    detail::AgentList* l = impl->list_of(agent, state);
+    const int v = l->var_index(variable);
+    if (v < 0) THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), variable.c_str()));
+    impl->ensure_all_allocated();
+    return l->cols[v][l->parity];
+}
+
+const unsigned int* CUDASimulation::getDeviceCount(const std::string& agent, const std::string& state) {
+    return impl->list_of(agent, state)->d_count;
+}
+
+}  // namespace flamegpu

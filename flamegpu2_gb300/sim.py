@@ -1,0 +1,174 @@
+"""ctypes binding of the simulation C ABI (include/flamegpu_gb300/fg_sim.h).
+
+Drives CUDASimulation runs of the models registered in libfg_models.so from
+Python (the tests and the benchmark). No computation happens here: every
+step runs in the native libraries, and loading fails loudly without them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import capi
+
+MODELS_LIB = os.path.join(capi.LIBDIR, "libfg_models.so")
+
+SIM_EXPORTS = [
+    "fgs_register_model", "fgs_list_models", "fgs_last_error", "fgs_create", "fgs_destroy", "fgs_configure",
+    "fgs_set_population", "fgs_set_population_device", "fgs_get_count", "fgs_get_variable",
+    "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
+    "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times",
+]
+
+_lock = threading.Lock()
+_core = None
+_models = None
+
+
+class SimError(RuntimeError):
+    pass
+
+
+def core():
+    """libflamegpu2_gb300.so with the simulation ABI prototypes, plus the model library."""
+    global _core, _models
+    with _lock:
+        if _core is None:
+            L = capi.lib()
+            vp, u32, i32, sz = C.c_void_p, C.c_uint32, C.c_int32, C.c_size_t
+            L.fgs_last_error.restype = C.c_char_p
+            L.fgs_list_models.argtypes = [C.c_char_p, sz]
+            L.fgs_create.argtypes = [C.c_char_p, C.POINTER(C.c_double), i32, i32]
+            L.fgs_create.restype = vp
+            L.fgs_destroy.argtypes = [vp]
+            L.fgs_configure.argtypes = [vp, u32, C.c_uint64, i32, i32]
+            L.fgs_set_population.argtypes = [vp, C.c_char_p, C.c_char_p, u32, i32, C.POINTER(C.c_char_p),
+                                             C.POINTER(vp)]
+            L.fgs_set_population_device.argtypes = L.fgs_set_population.argtypes
+            L.fgs_get_count.argtypes = [vp, C.c_char_p, C.c_char_p, C.POINTER(u32)]
+            L.fgs_get_variable.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
+            L.fgs_get_variable_device.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
+            L.fgs_step.argtypes = [vp, u32]
+            L.fgs_simulate.argtypes = [vp]
+            L.fgs_synchronize.argtypes = [vp]
+            L.fgs_set_environment.argtypes = [vp, C.c_char_p, vp, sz]
+            L.fgs_get_environment.argtypes = [vp, C.c_char_p, vp, sz]
+            L.fgs_stream.argtypes = [vp, C.POINTER(vp)]
+            L.fgs_stats.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(u32), C.POINTER(u32)]
+            L.fgs_step_times.argtypes = [vp, C.POINTER(C.c_double), u32, C.POINTER(u32)]
+            _core = L
+        if _models is None:
+            if not os.path.exists(MODELS_LIB):
+                raise RuntimeError(f"{MODELS_LIB} is missing: run flamegpu2_gb300.build.build() first")
+            _models = C.CDLL(MODELS_LIB, mode=C.RTLD_GLOBAL)
+    return _core
+
+
+def models() -> list[str]:
+    buf = C.create_string_buffer(4096)
+    core().fgs_list_models(buf, 4096)
+    return [m for m in buf.value.decode().split(",") if m]
+
+
+def _check(rc):
+    if rc != 0:
+        raise SimError(core().fgs_last_error().decode())
+
+
+class Simulation:
+    """One CUDASimulation of a registered model."""
+
+    def __init__(self, model: str, params=(), device: int = 0, steps: int = 1, seed: int = 0,
+                 use_graphs: bool = True, check_each_step: bool = False):
+        L = core()
+        arr = (C.c_double * max(1, len(params)))(*[float(p) for p in params])
+        self._h = L.fgs_create(model.encode(), arr, len(params), device)
+        if not self._h:
+            raise SimError(L.fgs_last_error().decode())
+        self.configure(steps, seed, use_graphs, check_each_step)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            core().fgs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def configure(self, steps=1, seed=0, use_graphs=True, check_each_step=False):
+        _check(core().fgs_configure(self._h, steps, seed, int(use_graphs), int(check_each_step)))
+
+    def set_population(self, agent: str, n: int, columns: dict, state: str = "default"):
+        names = list(columns)
+        arrs = [np.ascontiguousarray(columns[k]) for k in names]
+        for k, a in zip(names, arrs):
+            if a.shape[0] != n:
+                raise ValueError(f"column {k} has {a.shape[0]} rows, expected {n}")
+        cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        cp = (C.c_void_p * max(1, len(names)))(*[a.ctypes.data for a in arrs])
+        _check(core().fgs_set_population(self._h, agent.encode(), state.encode(), n, len(names), cn, cp))
+
+    def set_population_device(self, agent: str, n: int, columns: dict, state: str = "default"):
+        """columns: name -> torch CUDA tensor (kept alive by the caller until this returns)."""
+        names = list(columns)
+        cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        cp = (C.c_void_p * max(1, len(names)))(*[columns[k].data_ptr() for k in names])
+        _check(core().fgs_set_population_device(self._h, agent.encode(), state.encode(), n, len(names), cn, cp))
+
+    def count(self, agent: str, state: str = "default") -> int:
+        n = C.c_uint32(0)
+        _check(core().fgs_get_count(self._h, agent.encode(), state.encode(), C.byref(n)))
+        return n.value
+
+    def get(self, agent: str, var: str, dtype, elements: int = 1, state: str = "default") -> np.ndarray:
+        n = self.count(agent, state)
+        out = np.zeros((n, elements) if elements > 1 else n, dtype=dtype)
+        _check(core().fgs_get_variable(self._h, agent.encode(), state.encode(), var.encode(),
+                                       out.ctypes.data, out.nbytes))
+        return out
+
+    def get_device(self, agent: str, var: str, dst, state: str = "default"):
+        """Copy a variable's device column into a torch tensor (async on the sim stream)."""
+        _check(core().fgs_get_variable_device(self._h, agent.encode(), state.encode(), var.encode(),
+                                              dst.data_ptr(), dst.numel() * dst.element_size()))
+
+    def step(self, n: int = 1):
+        _check(core().fgs_step(self._h, n))
+
+    def simulate(self):
+        _check(core().fgs_simulate(self._h))
+
+    def synchronize(self):
+        _check(core().fgs_synchronize(self._h))
+
+    def set_env(self, name: str, value, ctype=C.c_float):
+        v = ctype(value)
+        _check(core().fgs_set_environment(self._h, name.encode(), C.byref(v), C.sizeof(v)))
+
+    def get_env(self, name: str, ctype=C.c_float):
+        v = ctype()
+        _check(core().fgs_get_environment(self._h, name.encode(), C.byref(v), C.sizeof(v)))
+        return v.value
+
+    @property
+    def stream(self) -> int:
+        p = C.c_void_p()
+        _check(core().fgs_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def stats(self) -> dict:
+        g, k, s = C.c_uint64(), C.c_uint32(), C.c_uint32()
+        _check(core().fgs_stats(self._h, C.byref(g), C.byref(k), C.byref(s)))
+        return {"graph_launches": g.value, "kernels_per_step": k.value, "step_counter": s.value}
+
+    def step_times(self, cap: int = 100000) -> np.ndarray:
+        buf = (C.c_double * cap)()
+        n = C.c_uint32()
+        _check(core().fgs_step_times(self._h, buf, cap, C.byref(n)))
+        return np.array(buf[:n.value])

@@ -1,0 +1,115 @@
+#ifndef INCLUDE_FLAMEGPU_DETAIL_DEVICE_TYPES_CUH_
+#define INCLUDE_FLAMEGPU_DETAIL_DEVICE_TYPES_CUH_
+// Types shared by the host runtime and the header-only device API.
+//
+// Variable lookup. The reference resolves getVariable("x") at run time with a
+// 512-slot open-addressing table of FNV-1a hashes copied into shared memory by
+// every block (include/flamegpu/runtime/detail/curve/Curve.cuh:21-84,
+// DeviceCurve.cuh:111-122,342-374). Here the FNV-1a hash of a name literal is
+// computed at compile time (consteval), and the host builds, per agent
+// function, a collision-free multiplicative hash over that function's own
+// variables: slot = (hash * mult) >> shift. A lookup is one multiply, one
+// shift and one read of a read-only table that the compiler hoists out of
+// loops; no shared memory, no probing.
+#include <cstdint>
+#include <string_view>
+
+#include "flamegpu/defines.h"
+#include "flamegpu_gb300/fg_capi.h"
+
+namespace flamegpu {
+namespace detail {
+
+/** 32-bit FNV-1a, the hash the reference's curve uses for names (Curve.cuh:66-84). */
+constexpr uint32_t fnv1a32(const char* s, unsigned n) {
+    uint32_t h = 2166136261u;
+    for (unsigned i = 0; i < n && s[i]; ++i) {
+        h ^= static_cast<uint8_t>(s[i]);
+        h *= 16777619u;
+    }
+    return h;
+}
+inline uint32_t fnv1a32(const std::string_view s) { return fnv1a32(s.data(), static_cast<unsigned>(s.size())); }
+
+/** A variable name given as a string literal, hashed at compile time. */
+struct VarName {
+    uint32_t hash;
+    bool reserved;  // starts with '_' (internal variables such as _id)
+    template <unsigned N>
+    __host__ __device__ consteval VarName(const char (&s)[N]) : hash(fnv1a32(s, N - 1)), reserved(s[0] == '_') {}
+};
+
+constexpr int kMaxVarSlots = 64;
+
+struct VarSlot {
+    char* ptr;            // element 0 of the column (or of field 0 in a record)
+    uint32_t stride;      // bytes between consecutive rows
+    uint32_t hash;        // FNV-1a of the name (0 = empty slot)
+    uint32_t elem_bytes;  // sizeof(T) of one element
+    uint32_t elements;    // array length (1 for scalars)
+};
+
+struct VarTable {
+    uint32_t mult;
+    uint32_t shift;
+    uint32_t count;
+    uint32_t pad;
+    VarSlot slot[kMaxVarSlots];
+};
+
+__host__ __device__ inline uint32_t table_slot(uint32_t mult, uint32_t shift, uint32_t hash) {
+    return (hash * mult) >> shift;
+}
+
+/** Read-only tables of one agent function launch (device memory). */
+struct FunctionTables {
+    VarTable agent;      // the agent's own variables (SoA columns)
+    VarTable msg_out;    // output message list (unsorted SoA columns)
+    VarTable msg_in;     // input message list (sorted records, or SoA for brute force)
+    VarTable birth;      // agent_out staging rows (SoA, indexed by parent)
+    VarTable birth_def;  // default value of each agent_out variable (ptr -> value bytes)
+    VarTable env;        // environment properties (ptr -> value bytes)
+};
+
+/** Device error codes recorded in LaunchParams::error[0]. */
+enum DeviceErrorCode : uint32_t {
+    kDevOk = 0,
+    kDevUnknownVariable = 1,
+    kDevTypeMismatch = 2,
+    kDevArrayIndex = 3,
+    kDevWrapOutOfBounds = 4,
+    kDevWrapIncompatible = 5,
+    kDevDeathNotEnabled = 6,
+    kDevBirthNotEnabled = 7,
+    kDevReservedName = 8,
+    kDevUnsupported = 9,
+    kDevMessageOutNotEnabled = 10,
+};
+
+/** Kernel parameters of one agent function launch (passed __grid_constant__). */
+struct LaunchParams {
+    const FunctionTables* T;
+    uint32_t max_n;              // capacity of the agent list (grid sizing bound)
+    const uint32_t* d_n;         // agents in the list (device)
+    // message output
+    uint32_t* msg_out_valid;     // per-row output flag (optional outputs), or null
+    uint32_t* msg_out_count;     // set to the agent count by the launch
+    int msg_out_enabled;
+    // message input
+    fg_spatial_grid in_grid;     // spatial metadata (MessageSpatial3D::MetaData)
+    const uint32_t* in_pbm;      // partition boundary matrix, binCount + 1 entries
+    const uint32_t* in_count;    // messages in the input list
+    // birth / death
+    uint32_t* birth_flags;       // 1 where agent_out was used (null if disabled)
+    uint32_t* death_flags;       // ALIVE / DEAD per agent (null if death disabled)
+    // step data
+    const uint32_t* d_step;      // step counter
+    uint64_t seed;               // simulation random seed
+    uint32_t fn_uid;             // unique id of this agent function (random streams)
+    uint32_t* error;             // device error record: [code, hash, index, count]
+};
+
+}  // namespace detail
+}  // namespace flamegpu
+
+#endif  // INCLUDE_FLAMEGPU_DETAIL_DEVICE_TYPES_CUH_

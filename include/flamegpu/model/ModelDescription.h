@@ -1,0 +1,464 @@
+#ifndef INCLUDE_FLAMEGPU_MODEL_MODELDESCRIPTION_H_
+#define INCLUDE_FLAMEGPU_MODEL_MODELDESCRIPTION_H_
+// Model description API: ModelDescription, AgentDescription,
+// AgentFunctionDescription, message descriptions, LayerDescription and
+// EnvironmentDescription with the reference's names and signatures
+// (include/flamegpu/model/ModelDescription.h:83-273, AgentDescription.h:209-310,
+// AgentFunctionDescription.h:190-334, LayerDescription.h:152-220,
+// include/flamegpu/runtime/messaging/MessageSpatial3D/MessageSpatial3DHost.h).
+// Descriptions are cheap handles onto shared model data, as in the reference.
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <type_traits>
+#include <typeindex>
+#include <vector>
+
+#include "flamegpu/defines.h"
+#include "flamegpu/exception/FLAMEGPUException.h"
+#include "flamegpu/runtime/AgentFunction.cuh"
+
+namespace flamegpu {
+
+class ModelDescription;
+class AgentDescription;
+class AgentFunctionDescription;
+class LayerDescription;
+class EnvironmentDescription;
+class HostAPI;
+
+typedef void (*FLAMEGPU_HOST_FUNCTION_POINTER)(HostAPI* api);
+
+namespace detail {
+
+enum class MessageKind { BruteForce = 1, Spatial2D = 2, Spatial3D = 3 };
+
+struct Variable {
+    std::string name;
+    std::type_index type = std::type_index(typeid(void));
+    uint32_t type_size = 0;
+    uint32_t elements = 1;
+    std::vector<char> default_value;  // type_size * elements bytes
+    uint32_t bytes() const { return type_size * elements; }
+};
+
+struct AgentData;
+struct MessageData;
+
+struct AgentFunctionData {
+    std::string name;
+    AgentData* parent = nullptr;
+    AgentFunctionLauncher launcher = nullptr;
+    std::type_index msg_in_type = std::type_index(typeid(void));
+    std::type_index msg_out_type = std::type_index(typeid(void));
+    std::string message_input, message_output;
+    bool message_output_optional = false;
+    std::string agent_output, agent_output_state;
+    bool has_agent_death = false;
+    std::string initial_state, end_state;
+    std::vector<AgentFunctionData*> dependencies;
+    uint32_t uid = 0;
+};
+
+struct AgentData {
+    std::string name;
+    std::vector<Variable> variables;  // _id first
+    std::vector<std::shared_ptr<AgentFunctionData>> functions;
+    std::vector<std::string> states{"default"};
+    std::string initial_state = "default";
+    bool explicit_states = false;
+    unsigned int sort_period = 1;  // AgentData.cpp:17
+    const Variable* find(const std::string& n) const {
+        for (const auto& v : variables)
+            if (v.name == n) return &v;
+        return nullptr;
+    }
+};
+
+struct MessageData {
+    std::string name;
+    MessageKind kind = MessageKind::BruteForce;
+    std::vector<Variable> variables;
+    float radius = std::numeric_limits<float>::quiet_NaN();
+    float min[3] = {std::numeric_limits<float>::quiet_NaN(), std::numeric_limits<float>::quiet_NaN(),
+                    std::numeric_limits<float>::quiet_NaN()};
+    float max[3] = {std::numeric_limits<float>::quiet_NaN(), std::numeric_limits<float>::quiet_NaN(),
+                    std::numeric_limits<float>::quiet_NaN()};
+    bool persistent = false;
+    const Variable* find(const std::string& n) const {
+        for (const auto& v : variables)
+            if (v.name == n) return &v;
+        return nullptr;
+    }
+};
+
+struct LayerData {
+    std::string name;
+    std::vector<AgentFunctionData*> functions;
+    std::vector<FLAMEGPU_HOST_FUNCTION_POINTER> host_functions;
+};
+
+struct EnvProperty {
+    std::string name;
+    std::type_index type = std::type_index(typeid(void));
+    uint32_t type_size = 0;
+    uint32_t elements = 1;
+    std::vector<char> value;
+    bool is_const = false;
+};
+
+struct ModelData {
+    std::string name;
+    std::vector<std::shared_ptr<AgentData>> agents;
+    std::vector<std::shared_ptr<MessageData>> messages;
+    std::vector<std::shared_ptr<LayerData>> layers;
+    std::vector<EnvProperty> environment;
+    std::vector<FLAMEGPU_HOST_FUNCTION_POINTER> init_functions, step_functions, exit_functions;
+    std::vector<AgentFunctionData*> execution_roots;
+    uint32_t next_fn_uid = 1;
+    AgentData* agent(const std::string& n) const {
+        for (const auto& a : agents)
+            if (a->name == n) return a.get();
+        return nullptr;
+    }
+    MessageData* message(const std::string& n) const {
+        for (const auto& m : messages)
+            if (m->name == n) return m.get();
+        return nullptr;
+    }
+    EnvProperty* property(const std::string& n) {
+        for (auto& p : environment)
+            if (p.name == n) return &p;
+        return nullptr;
+    }
+};
+
+template <typename T>
+Variable make_variable(const std::string& name, const T* def, uint32_t elements) {
+    Variable v;
+    v.name = name;
+    v.type = std::type_index(typeid(T));
+    v.type_size = sizeof(T);
+    v.elements = elements;
+    v.default_value.resize(sizeof(T) * elements);
+    std::memcpy(v.default_value.data(), def, sizeof(T) * elements);
+    return v;
+}
+
+inline void check_name(const std::string& n, const char* what) {
+    if (n.empty()) THROW exception::InvalidArgument(exception::format("%s name may not be empty", what));
+}
+
+}  // namespace detail
+
+// ---------------------------------------------------------------- messages
+
+/** Base description of a message list: its variables (MessageBruteForce::Description). */
+class MessageBruteForce::Description {
+ public:
+    explicit Description(std::shared_ptr<detail::ModelData> m, detail::MessageData* d) : model(std::move(m)), data(d) {}
+    template <typename T>
+    void newVariable(const std::string& name) {
+        detail::check_name(name, "Message variable");
+        if (!name.empty() && name[0] == '_')
+            THROW exception::ReservedName(exception::format("Message variable '%s' starts with '_'", name.c_str()));
+        if (data->find(name))
+            THROW exception::InvalidMessageVar(exception::format("Message '%s' already has variable '%s'",
+                                                                 data->name.c_str(), name.c_str()));
+        T zero{};
+        data->variables.push_back(detail::make_variable<T>(name, &zero, 1));
+    }
+    template <typename T, flamegpu::size_type N>
+    void newVariable(const std::string& name) {
+        detail::check_name(name, "Message variable");
+        if (data->find(name))
+            THROW exception::InvalidMessageVar(exception::format("Message '%s' already has variable '%s'",
+                                                                 data->name.c_str(), name.c_str()));
+        std::array<T, N> zero{};
+        data->variables.push_back(detail::make_variable<T>(name, zero.data(), N));
+    }
+    void setPersistent(bool p) { data->persistent = p; }
+    bool getPersistent() const { return data->persistent; }
+    std::string getName() const { return data->name; }
+    bool hasVariable(const std::string& name) const { return data->find(name) != nullptr; }
+    flamegpu::size_type getVariablesCount() const { return static_cast<flamegpu::size_type>(data->variables.size()); }
+    detail::MessageData* getData() const { return data; }
+
+ protected:
+    std::shared_ptr<detail::ModelData> model;
+    detail::MessageData* data;
+};
+
+/** MessageSpatial2D::Description (MessageSpatial2DHost.h): radius and 2D bounds; x, y implicit. */
+class MessageSpatial2D::Description : public MessageBruteForce::Description {
+ public:
+    using MessageBruteForce::Description::Description;
+    void setRadius(float r) {
+        if (!(r > 0.0f)) THROW exception::InvalidArgument(exception::format("Spatial radius must be > 0, %g given", r));
+        data->radius = r;
+    }
+    void setMin(float x, float y) {
+        check_min(0, x);
+        check_min(1, y);
+        data->min[0] = x;
+        data->min[1] = y;
+    }
+    void setMax(float x, float y) {
+        check_max(0, x);
+        check_max(1, y);
+        data->max[0] = x;
+        data->max[1] = y;
+    }
+    void setMinX(float v) { check_min(0, v); data->min[0] = v; }
+    void setMinY(float v) { check_min(1, v); data->min[1] = v; }
+    void setMaxX(float v) { check_max(0, v); data->max[0] = v; }
+    void setMaxY(float v) { check_max(1, v); data->max[1] = v; }
+    float getRadius() const { return data->radius; }
+    float getMinX() const { return data->min[0]; }
+    float getMinY() const { return data->min[1]; }
+    float getMaxX() const { return data->max[0]; }
+    float getMaxY() const { return data->max[1]; }
+
+ protected:
+    void check_min(int a, float v) const {
+        if (!std::isnan(data->max[a]) && !(v < data->max[a]))
+            THROW exception::InvalidArgument(exception::format("Spatial min (%g) must be below max (%g)", v, data->max[a]));
+    }
+    void check_max(int a, float v) const {
+        if (!std::isnan(data->min[a]) && !(v > data->min[a]))
+            THROW exception::InvalidArgument(exception::format("Spatial max (%g) must be above min (%g)", v, data->min[a]));
+    }
+};
+
+/** MessageSpatial3D::Description (MessageSpatial3DHost.h:225-240): x, y, z implicit. */
+class MessageSpatial3D::Description : public MessageSpatial2D::Description {
+ public:
+    using MessageSpatial2D::Description::Description;
+    void setMin(float x, float y, float z) {
+        MessageSpatial2D::Description::setMin(x, y);
+        check_min(2, z);
+        data->min[2] = z;
+    }
+    void setMax(float x, float y, float z) {
+        MessageSpatial2D::Description::setMax(x, y);
+        check_max(2, z);
+        data->max[2] = z;
+    }
+    void setMinZ(float v) { check_min(2, v); data->min[2] = v; }
+    void setMaxZ(float v) { check_max(2, v); data->max[2] = v; }
+    float getMinZ() const { return data->min[2]; }
+    float getMaxZ() const { return data->max[2]; }
+};
+
+// --------------------------------------------------------- agent functions
+
+class AgentFunctionDescription {
+ public:
+    AgentFunctionDescription(std::shared_ptr<detail::ModelData> m, detail::AgentFunctionData* f)
+        : model(std::move(m)), fn(f) {}
+    void setMessageInput(const std::string& message_name);
+    void setMessageInput(const MessageBruteForce::Description& message) { setMessageInput(message.getName()); }
+    void setMessageOutput(const std::string& message_name);
+    void setMessageOutput(const MessageBruteForce::Description& message) { setMessageOutput(message.getName()); }
+    void setMessageOutputOptional(bool optional) { fn->message_output_optional = optional; }
+    void setAgentOutput(const std::string& agent_name, const std::string& state = "");
+    void setAgentOutput(const AgentDescription& agent, const std::string& state = "");
+    void setAllowAgentDeath(bool allow) { fn->has_agent_death = allow; }
+    void setInitialState(const std::string& s);
+    void setEndState(const std::string& s);
+    void dependsOn(const AgentFunctionDescription& other) { fn->dependencies.push_back(other.fn); }
+    std::string getName() const { return fn->name; }
+    std::string getMessageInputName() const { return fn->message_input; }
+    std::string getMessageOutputName() const { return fn->message_output; }
+    bool getMessageOutputOptional() const { return fn->message_output_optional; }
+    bool getAllowAgentDeath() const { return fn->has_agent_death; }
+    bool hasMessageInput() const { return !fn->message_input.empty(); }
+    bool hasMessageOutput() const { return !fn->message_output.empty(); }
+    bool hasAgentOutput() const { return !fn->agent_output.empty(); }
+    std::string getInitialState() const { return fn->initial_state; }
+    std::string getEndState() const { return fn->end_state; }
+    detail::AgentFunctionData* getData() const { return fn; }
+
+ private:
+    std::shared_ptr<detail::ModelData> model;
+    detail::AgentFunctionData* fn;
+};
+
+class AgentDescription {
+ public:
+    AgentDescription(std::shared_ptr<detail::ModelData> m, detail::AgentData* a) : model(std::move(m)), agent(a) {}
+    template <typename T>
+    void newVariable(const std::string& name, T default_value = {}) {
+        add_variable(detail::make_variable<T>(name, &default_value, 1));
+    }
+    template <typename T, flamegpu::size_type N>
+    void newVariable(const std::string& name, const std::array<T, N>& default_value = {}) {
+        add_variable(detail::make_variable<T>(name, default_value.data(), N));
+    }
+    template <typename F>
+    AgentFunctionDescription newFunction(const std::string& name, F) {
+        detail::check_name(name, "Agent function");
+        for (const auto& f : agent->functions)
+            if (f->name == name)
+                THROW exception::InvalidAgentFunc(exception::format("Agent '%s' already has function '%s'",
+                                                                    agent->name.c_str(), name.c_str()));
+        auto f = std::make_shared<detail::AgentFunctionData>();
+        f->name = name;
+        f->parent = agent;
+        f->launcher = F::launcher();
+        f->msg_in_type = F::inType();
+        f->msg_out_type = F::outType();
+        f->initial_state = agent->initial_state;
+        f->end_state = agent->initial_state;
+        f->uid = model->next_fn_uid++;
+        agent->functions.push_back(f);
+        return AgentFunctionDescription(model, f.get());
+    }
+    AgentFunctionDescription Function(const std::string& name) const {
+        for (const auto& f : agent->functions)
+            if (f->name == name) return AgentFunctionDescription(model, f.get());
+        THROW exception::InvalidAgentFunc(exception::format("Agent '%s' has no function '%s'", agent->name.c_str(), name.c_str()));
+    }
+    void newState(const std::string& state);
+    void setInitialState(const std::string& state);
+    void setSortPeriod(unsigned int period) { agent->sort_period = period; }
+    unsigned int getSortPeriod() const { return agent->sort_period; }
+    std::string getName() const { return agent->name; }
+    bool hasVariable(const std::string& name) const { return agent->find(name) != nullptr; }
+    flamegpu::size_type getVariablesCount() const { return static_cast<flamegpu::size_type>(agent->variables.size() - 1); }
+    std::type_index getVariableType(const std::string& name) const;
+    flamegpu::size_type getVariableLength(const std::string& name) const;
+    detail::AgentData* getData() const { return agent; }
+    const std::shared_ptr<detail::ModelData>& getModel() const { return model; }
+
+ private:
+    void add_variable(detail::Variable v);
+    std::shared_ptr<detail::ModelData> model;
+    detail::AgentData* agent;
+};
+
+class LayerDescription {
+ public:
+    LayerDescription(std::shared_ptr<detail::ModelData> m, detail::LayerData* l) : model(std::move(m)), layer(l) {}
+    template <typename F>
+    void addAgentFunction(const F&) {
+        const detail::AgentFunctionLauncher l = F::launcher();
+        for (const auto& a : model->agents)
+            for (const auto& f : a->functions)
+                if (f->launcher == l) {
+                    add(f.get());
+                    return;
+                }
+        THROW exception::InvalidAgentFunc("Agent function passed to addAgentFunction() is not part of the model");
+    }
+    void addAgentFunction(const AgentFunctionDescription& f) { add(f.getData()); }
+    void addAgentFunction(const std::string& agent_name, const std::string& function_name);
+    void addHostFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { layer->host_functions.push_back(fn); }
+    std::string getName() const { return layer->name; }
+    flamegpu::size_type getAgentFunctionsCount() const { return static_cast<flamegpu::size_type>(layer->functions.size()); }
+
+ private:
+    void add(detail::AgentFunctionData* f);
+    std::shared_ptr<detail::ModelData> model;
+    detail::LayerData* layer;
+};
+
+class EnvironmentDescription {
+ public:
+    explicit EnvironmentDescription(std::shared_ptr<detail::ModelData> m) : model(std::move(m)) {}
+    template <typename T>
+    void newProperty(const std::string& name, T value, bool isConst = false) {
+        add(name, std::type_index(typeid(T)), sizeof(T), 1, &value, isConst);
+    }
+    template <typename T, flamegpu::size_type N>
+    void newProperty(const std::string& name, const std::array<T, N>& value, bool isConst = false) {
+        add(name, std::type_index(typeid(T)), sizeof(T), N, value.data(), isConst);
+    }
+    template <typename T>
+    T getProperty(const std::string& name) const {
+        const detail::EnvProperty* p = find(name, typeid(T), sizeof(T));
+        T v;
+        std::memcpy(&v, p->value.data(), sizeof(T));
+        return v;
+    }
+    template <typename T, flamegpu::size_type N>
+    std::array<T, N> getProperty(const std::string& name) const {
+        const detail::EnvProperty* p = find(name, typeid(T), sizeof(T));
+        std::array<T, N> v;
+        std::memcpy(v.data(), p->value.data(), sizeof(T) * N);
+        return v;
+    }
+    template <typename T>
+    T setProperty(const std::string& name, T value) {
+        detail::EnvProperty* p = const_cast<detail::EnvProperty*>(find(name, typeid(T), sizeof(T)));
+        T old;
+        std::memcpy(&old, p->value.data(), sizeof(T));
+        std::memcpy(p->value.data(), &value, sizeof(T));
+        return old;
+    }
+    bool hasProperty(const std::string& name) const { return model->property(name) != nullptr; }
+
+ private:
+    void add(const std::string& name, std::type_index t, uint32_t size, uint32_t n, const void* v, bool c);
+    const detail::EnvProperty* find(const std::string& name, const std::type_info& t, size_t size) const;
+    std::shared_ptr<detail::ModelData> model;
+};
+
+class ModelDescription {
+ public:
+    explicit ModelDescription(const std::string& name);
+    AgentDescription newAgent(const std::string& name);
+    AgentDescription Agent(const std::string& name) const;
+    template <typename MsgType>
+    typename MsgType::Description newMessage(const std::string& name) {
+        detail::MessageData* d = new_message(name, kind_of<MsgType>());
+        return typename MsgType::Description(model, d);
+    }
+    template <typename MsgType>
+    typename MsgType::Description Message(const std::string& name) const {
+        detail::MessageData* d = model->message(name);
+        if (!d || d->kind != kind_of<MsgType>())
+            THROW exception::InvalidMessageName(exception::format("Model has no message '%s' of that type", name.c_str()));
+        return typename MsgType::Description(model, d);
+    }
+    LayerDescription newLayer(const std::string& name = "");
+    LayerDescription Layer(flamegpu::size_type index) const;
+    LayerDescription Layer(const std::string& name) const;
+    EnvironmentDescription Environment() const { return EnvironmentDescription(model); }
+    void addInitFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { model->init_functions.push_back(fn); }
+    void addStepFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { model->step_functions.push_back(fn); }
+    void addExitFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { model->exit_functions.push_back(fn); }
+    void addExecutionRoot(const AgentFunctionDescription& f) { model->execution_roots.push_back(f.getData()); }
+    /** Layers from the dependency graph (src/flamegpu/model/DependencyGraph.cpp:89-180). */
+    void generateLayers();
+    std::string getName() const { return model->name; }
+    flamegpu::size_type getLayersCount() const { return static_cast<flamegpu::size_type>(model->layers.size()); }
+    flamegpu::size_type getAgentsCount() const { return static_cast<flamegpu::size_type>(model->agents.size()); }
+    flamegpu::size_type getMessagesCount() const { return static_cast<flamegpu::size_type>(model->messages.size()); }
+    const std::shared_ptr<detail::ModelData>& getData() const { return model; }
+
+ private:
+    template <typename MsgType>
+    static detail::MessageKind kind_of() {
+        if constexpr (std::is_same_v<MsgType, MessageSpatial3D>) return detail::MessageKind::Spatial3D;
+        else if constexpr (std::is_same_v<MsgType, MessageSpatial2D>) return detail::MessageKind::Spatial2D;
+        else return detail::MessageKind::BruteForce;
+    }
+    detail::MessageData* new_message(const std::string& name, detail::MessageKind kind);
+    std::shared_ptr<detail::ModelData> model;
+};
+
+}  // namespace flamegpu
+
+#define FLAMEGPU_INIT_FUNCTION(name) void name(flamegpu::HostAPI* FLAMEGPU)
+#define FLAMEGPU_STEP_FUNCTION(name) void name(flamegpu::HostAPI* FLAMEGPU)
+#define FLAMEGPU_EXIT_FUNCTION(name) void name(flamegpu::HostAPI* FLAMEGPU)
+#define FLAMEGPU_HOST_FUNCTION(name) void name(flamegpu::HostAPI* FLAMEGPU)
+
+#endif  // INCLUDE_FLAMEGPU_MODEL_MODELDESCRIPTION_H_

@@ -1,0 +1,660 @@
+#ifndef INCLUDE_FLAMEGPU_RUNTIME_DEVICEAPI_CUH_
+#define INCLUDE_FLAMEGPU_RUNTIME_DEVICEAPI_CUH_
+// Header-only device API used inside FLAMEGPU_AGENT_FUNCTION bodies: agent
+// variables, message input/output iterators (MessageNone, MessageBruteForce,
+// MessageSpatial2D, MessageSpatial3D), agent output (birth), environment
+// properties and random numbers. Mirrors the reference's device API
+// (include/flamegpu/runtime/DeviceAPI.cuh:163-557,
+// include/flamegpu/runtime/messaging/*/*Device.cuh) with the same names and
+// iteration semantics; the storage behind it is the GB300 layout (sorted
+// message records, per-function lookup tables).
+#include <cstdint>
+#include <type_traits>
+
+#include "flamegpu/defines.h"
+#include "flamegpu/detail/device_types.cuh"
+
+#ifndef FLAMEGPU_SEATBELTS
+#define FLAMEGPU_SEATBELTS 1
+#endif
+
+namespace flamegpu {
+
+class MessageNone;
+class MessageBruteForce;
+class MessageSpatial2D;
+class MessageSpatial3D;
+
+namespace detail {
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void device_error(const LaunchParams& P, uint32_t code, uint32_t hash, uint32_t idx) {
+    if (P.error) {
+        if (atomicCAS(&P.error[0], 0u, code) == 0u) {
+            P.error[1] = hash;
+            P.error[2] = idx;
+        }
+        atomicAdd(&P.error[3], 1u);
+    }
+}
+
+// Address of element `elem` of variable `hash` in row `row` of table `t`.
+// Returns null (after recording a device error) when seatbelts are on and the
+// name, the type size or the array index is wrong.
+template <typename T>
+__device__ __forceinline__ T* var_addr(const LaunchParams& P, const VarTable* __restrict__ t, uint32_t hash,
+                                       uint32_t row, uint32_t elem) {
+    const uint32_t s = table_slot(__ldg(&t->mult), __ldg(&t->shift), hash);
+    const VarSlot* vs = &t->slot[s];
+    char* base = reinterpret_cast<char*>(__ldg(reinterpret_cast<const unsigned long long*>(&vs->ptr)));
+    const uint32_t stride = __ldg(&vs->stride);
+#if FLAMEGPU_SEATBELTS
+    if (__ldg(&vs->hash) != hash || base == nullptr) {
+        device_error(P, kDevUnknownVariable, hash, row);
+        return nullptr;
+    }
+    if (__ldg(&vs->elem_bytes) != sizeof(T)) {
+        device_error(P, kDevTypeMismatch, hash, row);
+        return nullptr;
+    }
+    if (elem >= __ldg(&vs->elements)) {
+        device_error(P, kDevArrayIndex, hash, row);
+        return nullptr;
+    }
+#endif
+    return reinterpret_cast<T*>(base + static_cast<size_t>(row) * stride + static_cast<size_t>(elem) * sizeof(T));
+}
+
+template <typename T>
+__device__ __forceinline__ T ldg_any(const T* p) {
+    if constexpr (sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 2 || sizeof(T) == 1) {
+        return __ldg(p);
+    } else {
+        return *p;
+    }
+}
+template <>
+__device__ __forceinline__ bool ldg_any<bool>(const bool* p) {
+    return *p;
+}
+
+// Read-only read of a variable (messages, environment): non-coherent path.
+template <typename T>
+__device__ __forceinline__ T read_ro(const LaunchParams& P, const VarTable* t, uint32_t hash, uint32_t row,
+                                     uint32_t elem = 0) {
+    const T* a = var_addr<T>(P, t, hash, row, elem);
+    return a ? ldg_any(a) : T{};
+}
+template <typename T>
+__device__ __forceinline__ T read_rw(const LaunchParams& P, const VarTable* t, uint32_t hash, uint32_t row,
+                                     uint32_t elem = 0) {
+    const T* a = var_addr<T>(P, t, hash, row, elem);
+    return a ? *a : T{};
+}
+template <typename T>
+__device__ __forceinline__ void write_var(const LaunchParams& P, const VarTable* t, uint32_t hash, uint32_t row, T v,
+                                          uint32_t elem = 0) {
+    T* a = var_addr<T>(P, t, hash, row, elem);
+    if (a) *a = v;
+}
+
+// SplitMix64 finaliser (Steele, Lea & Flood, OOPSLA 2014).
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+#endif  // __CUDACC__
+
+}  // namespace detail
+
+#ifdef __CUDACC__
+
+// ------------------------------------------------------------------ messages
+
+/** No message input/output (include/flamegpu/runtime/messaging/MessageNone.h). */
+class MessageNone {
+ public:
+    class Description;
+    class In {
+     public:
+        __device__ explicit In(const detail::LaunchParams&) {}
+    };
+    class Out {
+     public:
+        __device__ Out(const detail::LaunchParams&, uint32_t) {}
+        __device__ uint32_t written() const { return 0; }
+    };
+};
+
+/** Output half shared by every message type (MessageBruteForceDevice.cuh:259-294). */
+class MessageOutBase {
+ public:
+    __device__ MessageOutBase(const detail::LaunchParams& p, uint32_t idx) : P(p), index(idx) {}
+    template <typename T>
+    __device__ void setVariable(detail::VarName name, T value) const {
+        if (!P.msg_out_enabled) {
+            detail::device_error(P, detail::kDevMessageOutNotEnabled, name.hash, index);
+            return;
+        }
+        detail::write_var<T>(P, &P.T->msg_out, name.hash, index, value);
+        flag = 1;
+    }
+    template <typename T, flamegpu::size_type N>
+    __device__ void setVariable(detail::VarName name, unsigned int i, T value) const {
+        if (!P.msg_out_enabled) {
+            detail::device_error(P, detail::kDevMessageOutNotEnabled, name.hash, index);
+            return;
+        }
+        detail::write_var<T>(P, &P.T->msg_out, name.hash, index, value, i);
+        flag = 1;
+    }
+    __device__ uint32_t written() const { return flag; }
+
+ protected:
+    const detail::LaunchParams& P;
+    uint32_t index;
+    mutable uint32_t flag = 0;
+};
+
+/** Message in an input list, addressed by its (sorted) index. */
+class MessageView {
+ public:
+    __device__ MessageView(const detail::LaunchParams& p, uint32_t i) : P(p), index(i) {}
+    template <typename T>
+    __device__ T getVariable(detail::VarName name) const {
+        return detail::read_ro<T>(P, &P.T->msg_in, name.hash, index);
+    }
+    template <typename T, flamegpu::size_type N>
+    __device__ T getVariable(detail::VarName name, unsigned int i) const {
+        return detail::read_ro<T>(P, &P.T->msg_in, name.hash, index, i);
+    }
+    __device__ uint32_t getIndex() const { return index; }
+
+ protected:
+    const detail::LaunchParams& P;
+
+ public:
+    uint32_t index;
+};
+
+/** Every message of the list (MessageBruteForceDevice.cuh:19-172,222-257). */
+class MessageBruteForce {
+ public:
+    class Description;
+    class Out : public MessageOutBase {
+     public:
+        __device__ Out(const detail::LaunchParams& p, uint32_t idx) : MessageOutBase(p, idx) {}
+    };
+    class In {
+     public:
+        class Message : public MessageView {
+         public:
+            __device__ Message(const detail::LaunchParams& p, uint32_t i) : MessageView(p, i) {}
+        };
+        class iterator {
+         public:
+            __device__ iterator(const detail::LaunchParams& p, uint32_t i) : m(p, i) {}
+            __device__ iterator& operator++() {
+                ++m.index;
+                return *this;
+            }
+            __device__ bool operator!=(const iterator& o) const { return m.index != o.m.index; }
+            __device__ bool operator==(const iterator& o) const { return m.index == o.m.index; }
+            __device__ const Message& operator*() const { return m; }
+            __device__ const Message* operator->() const { return &m; }
+
+         private:
+            Message m;
+        };
+        __device__ explicit In(const detail::LaunchParams& p) : P(p), len(p.in_count ? *p.in_count : 0u) {}
+        __device__ iterator begin() const { return iterator(P, 0); }
+        __device__ iterator end() const { return iterator(P, len); }
+        __device__ uint32_t size() const { return len; }
+
+     private:
+        const detail::LaunchParams& P;
+        uint32_t len;
+    };
+};
+
+namespace detail {
+__device__ __forceinline__ int clamp_cell(int v, uint32_t dim) {
+    const int d = static_cast<int>(dim);
+    return v < 0 ? 0 : (v >= d ? d - 1 : v);
+}
+// getGridPosition3D / getGridPosition2D (MessageSpatial3DDevice.cuh:646-659)
+__device__ __forceinline__ int grid_cell(const fg_spatial_grid& g, int axis, float p) {
+    return clamp_cell(static_cast<int>(floorf((p - g.min[axis]) / g.radius)), g.gridDim[axis]);
+}
+// getHash3D / getHash2D (MessageSpatial3DDevice.cuh:660-672): x clamped
+__device__ __forceinline__ uint32_t grid_hash(const fg_spatial_grid& g, int x, int y, int z) {
+    const uint32_t ux = static_cast<uint32_t>(clamp_cell(x, g.gridDim[0]));
+    return static_cast<uint32_t>(z) * g.gridDim[0] * g.gridDim[1] + static_cast<uint32_t>(y) * g.gridDim[0] + ux;
+}
+__device__ __forceinline__ float virtual_coord(float p1, float p2, float width) {
+    // getVirtualX (MessageSpatial3DDevice.cuh:373-397)
+    const float d = p2 - p1;
+    return fabsf(d) > width / 2.0f ? p2 - (d / fabsf(d) * width) : p2;
+}
+}  // namespace detail
+
+/**
+ * Spatially partitioned messages; the iterators visit the reference's
+ * Moore neighbourhood in the reference's order. DIMS = 2 or 3.
+ * Filter: 3^(DIMS-1) x-strips, y-offset outer, z-offset inner, each strip
+ * PBM[hash(x-1)] .. PBM[hash(x+1)+1] with x clamped (MessageSpatial3DDevice.cuh:693-719).
+ * WrapFilter: 3^DIMS single bins, x outer, y, z inner, every axis taken
+ * modulo gridDim (:727-749); no radius test — user code filters.
+ */
+template <int DIMS>
+class SpatialIn {
+ public:
+    static constexpr int kStrips = DIMS == 3 ? 9 : 3;
+    static constexpr int kCells = DIMS == 3 ? 27 : 9;
+
+    class Filter {
+     public:
+        class Message : public MessageView {
+         public:
+            __device__ Message(const detail::LaunchParams& p, uint32_t i) : MessageView(p, i) {}
+        };
+        class iterator {
+         public:
+            __device__ iterator(const Filter& f, int strip) : F(f), s(strip), m(f.P, 0), end_(0) {
+                if (s < kStrips) {
+                    m.index = 0;
+                    end_ = 0;
+                    --s;
+                    advance();
+                }
+            }
+            __device__ iterator& operator++() {
+                if (++m.index >= end_) advance();
+                return *this;
+            }
+            __device__ bool operator!=(const iterator&) const { return s < kStrips; }
+            __device__ bool operator==(const iterator& o) const { return !(*this != o); }
+            __device__ const Message& operator*() const { return m; }
+            __device__ const Message* operator->() const { return &m; }
+
+         private:
+            __device__ void advance() {
+                while (++s < kStrips) {
+                    const int ry = DIMS == 3 ? s / 3 - 1 : s - 1;
+                    const int rz = DIMS == 3 ? s % 3 - 1 : 0;
+                    const int ay = F.cell[1] + ry, az = F.cell[2] + rz;
+                    if (ay < 0 || ay >= static_cast<int>(F.P.in_grid.gridDim[1])) continue;
+                    if (DIMS == 3 && (az < 0 || az >= static_cast<int>(F.P.in_grid.gridDim[2]))) continue;
+                    const uint32_t h0 = detail::grid_hash(F.P.in_grid, F.cell[0] - 1, ay, az);
+                    const uint32_t h1 = detail::grid_hash(F.P.in_grid, F.cell[0] + 1, ay, az);
+                    const uint32_t b = __ldg(F.P.in_pbm + h0), e = __ldg(F.P.in_pbm + h1 + 1);
+                    if (b < e) {
+                        m.index = b;
+                        end_ = e;
+                        return;
+                    }
+                }
+            }
+            const Filter& F;
+            int s;
+            Message m;
+            uint32_t end_;
+        };
+        __device__ Filter(const detail::LaunchParams& p, float x, float y, float z) : P(p) {
+            loc[0] = x;
+            loc[1] = y;
+            loc[2] = z;
+            cell[0] = detail::grid_cell(p.in_grid, 0, x);
+            cell[1] = detail::grid_cell(p.in_grid, 1, y);
+            cell[2] = DIMS == 3 ? detail::grid_cell(p.in_grid, 2, z) : 0;
+        }
+        __device__ iterator begin() const { return iterator(*this, 0); }
+        __device__ iterator end() const { return iterator(*this, kStrips); }
+
+        const detail::LaunchParams& P;
+        float loc[3];
+        int cell[3];
+    };
+
+    class WrapFilter {
+     public:
+        class Message : public MessageView {
+         public:
+            __device__ Message(const detail::LaunchParams& p, uint32_t i, const WrapFilter* f)
+                : MessageView(p, i), F(f) {}
+            __device__ float getVirtualX() const { return getVirtualX(F->loc[0]); }
+            __device__ float getVirtualY() const { return getVirtualY(F->loc[1]); }
+            __device__ float getVirtualZ() const { return getVirtualZ(F->loc[2]); }
+            __device__ float getVirtualX(float x1) const {
+                return detail::virtual_coord(x1, getVariable<float>("x"), P.in_grid.width[0]);
+            }
+            __device__ float getVirtualY(float y1) const {
+                return detail::virtual_coord(y1, getVariable<float>("y"), P.in_grid.width[1]);
+            }
+            __device__ float getVirtualZ(float z1) const {
+                return detail::virtual_coord(z1, getVariable<float>("z"), P.in_grid.width[2]);
+            }
+
+         private:
+            const WrapFilter* F;
+        };
+        class iterator {
+         public:
+            __device__ iterator(const WrapFilter& f, int cell) : F(f), c(cell), m(f.P, 0, &f), end_(0) {
+                if (c < kCells) {
+                    --c;
+                    advance();
+                }
+            }
+            __device__ iterator& operator++() {
+                if (++m.index >= end_) advance();
+                return *this;
+            }
+            __device__ bool operator!=(const iterator&) const { return c < kCells; }
+            __device__ bool operator==(const iterator& o) const { return !(*this != o); }
+            __device__ const Message& operator*() const { return m; }
+            __device__ const Message* operator->() const { return &m; }
+
+         private:
+            __device__ void advance() {
+                const fg_spatial_grid& g = F.P.in_grid;
+                while (++c < kCells) {
+                    int rx, ry, rz;
+                    if (DIMS == 3) {
+                        rx = c / 9 - 1;
+                        ry = (c / 3) % 3 - 1;
+                        rz = c % 3 - 1;
+                    } else {
+                        rx = c / 3 - 1;
+                        ry = c % 3 - 1;
+                        rz = 0;
+                    }
+                    const int ax = static_cast<int>(static_cast<uint32_t>(F.cell[0] + rx + static_cast<int>(g.gridDim[0])) % g.gridDim[0]);
+                    const int ay = static_cast<int>(static_cast<uint32_t>(F.cell[1] + ry + static_cast<int>(g.gridDim[1])) % g.gridDim[1]);
+                    const int az = DIMS == 3 ? static_cast<int>(static_cast<uint32_t>(F.cell[2] + rz + static_cast<int>(g.gridDim[2])) % g.gridDim[2]) : 0;
+                    const uint32_t h = detail::grid_hash(g, ax, ay, az);
+                    const uint32_t b = __ldg(F.P.in_pbm + h), e = __ldg(F.P.in_pbm + h + 1);
+                    if (b < e) {
+                        m.index = b;
+                        end_ = e;
+                        return;
+                    }
+                }
+            }
+            const WrapFilter& F;
+            int c;
+            Message m;
+            uint32_t end_;
+        };
+        __device__ WrapFilter(const detail::LaunchParams& p, float x, float y, float z) : P(p) {
+            loc[0] = x;
+            loc[1] = y;
+            loc[2] = z;
+            cell[0] = detail::grid_cell(p.in_grid, 0, x);
+            cell[1] = detail::grid_cell(p.in_grid, 1, y);
+            cell[2] = DIMS == 3 ? detail::grid_cell(p.in_grid, 2, z) : 0;
+        }
+        __device__ iterator begin() const { return iterator(*this, 0); }
+        __device__ iterator end() const { return iterator(*this, kCells); }
+
+        const detail::LaunchParams& P;
+        float loc[3];
+        int cell[3];
+    };
+
+    __device__ explicit SpatialIn(const detail::LaunchParams& p) : P(p) {}
+    __device__ float radius() const { return P.in_grid.radius; }
+
+ protected:
+    // MessageSpatial3D::In::wrap seatbelts (MessageSpatial3DDevice.cuh:527-549)
+    __device__ bool wrap_ok(float x, float y, float z) const {
+#if FLAMEGPU_SEATBELTS
+        const fg_spatial_grid& g = P.in_grid;
+        bool out = x > g.max[0] || y > g.max[1] || x < g.min[0] || y < g.min[1];
+        if (DIMS == 3) out = out || z > g.max[2] || z < g.min[2];
+        if (out) {
+            detail::device_error(P, detail::kDevWrapOutOfBounds, 0, 0);
+            return false;
+        }
+        if (!g.wrapCompatible) detail::device_error(P, detail::kDevWrapIncompatible, 0, 0);
+#endif
+        return true;
+    }
+    const detail::LaunchParams& P;
+};
+
+/** MessageSpatial2D (include/flamegpu/runtime/messaging/MessageSpatial2D/MessageSpatial2DDevice.cuh). */
+class MessageSpatial2D {
+ public:
+    class Description;
+    class In : public SpatialIn<2> {
+     public:
+        __device__ explicit In(const detail::LaunchParams& p) : SpatialIn<2>(p) {}
+        __device__ Filter operator()(float x, float y) const { return Filter(P, x, y, 0.0f); }
+        __device__ WrapFilter wrap(float x, float y) const {
+            if (!wrap_ok(x, y, 0.0f)) return WrapFilter(P, P.in_grid.min[0], P.in_grid.min[1], 0.0f);
+            return WrapFilter(P, x, y, 0.0f);
+        }
+    };
+    class Out : public MessageOutBase {
+     public:
+        __device__ Out(const detail::LaunchParams& p, uint32_t idx) : MessageOutBase(p, idx) {}
+        __device__ void setLocation(float x, float y) const {
+            setVariable<float>("x", x);
+            setVariable<float>("y", y);
+        }
+    };
+};
+
+/** MessageSpatial3D (include/flamegpu/runtime/messaging/MessageSpatial3D/MessageSpatial3DDevice.cuh). */
+class MessageSpatial3D {
+ public:
+    class Description;
+    class In : public SpatialIn<3> {
+     public:
+        __device__ explicit In(const detail::LaunchParams& p) : SpatialIn<3>(p) {}
+        __device__ Filter operator()(float x, float y, float z) const { return Filter(P, x, y, z); }
+        __device__ WrapFilter wrap(float x, float y, float z) const {
+            if (!wrap_ok(x, y, z)) return WrapFilter(P, P.in_grid.min[0], P.in_grid.min[1], P.in_grid.min[2]);
+            return WrapFilter(P, x, y, z);
+        }
+    };
+    class Out : public MessageOutBase {
+     public:
+        __device__ Out(const detail::LaunchParams& p, uint32_t idx) : MessageOutBase(p, idx) {}
+        __device__ void setLocation(float x, float y, float z) const {
+            setVariable<float>("x", x);
+            setVariable<float>("y", y);
+            setVariable<float>("z", z);
+        }
+    };
+};
+
+// ------------------------------------------------------- environment, random
+
+/** Read-only environment properties (include/flamegpu/runtime/environment/DeviceEnvironment.cuh). */
+class DeviceEnvironment {
+ public:
+    __device__ explicit DeviceEnvironment(const detail::LaunchParams& p) : P(p) {}
+    template <typename T>
+    __device__ T getProperty(detail::VarName name) const {
+        return detail::read_ro<T>(P, &P.T->env, name.hash, 0);
+    }
+    template <typename T, flamegpu::size_type N>
+    __device__ T getProperty(detail::VarName name, unsigned int i) const {
+        return detail::read_ro<T>(P, &P.T->env, name.hash, 0, i);
+    }
+
+ private:
+    const detail::LaunchParams& P;
+};
+
+/**
+ * Per-agent random numbers (include/flamegpu/runtime/random/AgentRandom.cuh).
+ * Counter-based: draw k of agent index i in step s of function f is a
+ * SplitMix64 hash of (seed, f, s, i, k); no per-thread generator state is
+ * kept. The reference's curand Philox values are not reproduced.
+ */
+class AgentRandom {
+ public:
+    __device__ AgentRandom(const detail::LaunchParams& p, uint32_t idx) : P(p), index(idx) {}
+    template <typename T>
+    __device__ T uniform() const;
+    template <typename T>
+    __device__ T uniform(T min, T max) const;
+    template <typename T>
+    __device__ T normal() const;
+    template <typename T>
+    __device__ T logNormal(T mean, T stddev) const;
+
+ private:
+    __device__ uint64_t next() const {
+        const uint64_t key = detail::mix64(P.seed ^ (static_cast<uint64_t>(P.fn_uid) << 40) ^ *P.d_step);
+        return detail::mix64(detail::mix64(key + index) + (counter++));
+    }
+    const detail::LaunchParams& P;
+    uint32_t index;
+    mutable uint32_t counter = 0;
+};
+template <>
+__device__ inline float AgentRandom::uniform<float>() const {
+    return static_cast<float>(next() >> 40) * (1.0f / 16777216.0f);
+}
+template <>
+__device__ inline double AgentRandom::uniform<double>() const {
+    return static_cast<double>(next() >> 11) * (1.0 / 9007199254740992.0);
+}
+template <>
+__device__ inline float AgentRandom::normal<float>() const {
+    const float u1 = 1.0f - uniform<float>(), u2 = uniform<float>();
+    return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+}
+template <>
+__device__ inline double AgentRandom::normal<double>() const {
+    const double u1 = 1.0 - uniform<double>(), u2 = uniform<double>();
+    return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+template <>
+__device__ inline float AgentRandom::logNormal<float>(float mean, float stddev) const {
+    return expf(mean + stddev * normal<float>());
+}
+template <>
+__device__ inline double AgentRandom::logNormal<double>(double mean, double stddev) const {
+    return exp(mean + stddev * normal<double>());
+}
+template <typename T>
+__device__ inline T AgentRandom::uniform(T min, T max) const {
+    if constexpr (std::is_integral<T>::value) {
+        const uint64_t span = static_cast<uint64_t>(static_cast<int64_t>(max) - static_cast<int64_t>(min)) + 1;
+        return static_cast<T>(static_cast<int64_t>(min) + static_cast<int64_t>(next() % span));
+    } else {
+        return min + (max - min) * uniform<T>();
+    }
+}
+
+// ------------------------------------------------------------------ DeviceAPI
+
+/** The FLAMEGPU object of an agent function (DeviceAPI.cuh:163-401). */
+template <typename MessageIn, typename MessageOut>
+class DeviceAPI {
+ public:
+    /** agent_out: birth of at most one agent per agent function call (DeviceAPI.cuh:187-236). */
+    class AgentOut {
+     public:
+        __device__ AgentOut(const detail::LaunchParams& p, uint32_t idx) : P(p), index(idx) {}
+        template <typename T>
+        __device__ void setVariable(detail::VarName name, T value) const {
+            if (!start(name)) return;
+            detail::write_var<T>(P, &P.T->birth, name.hash, index, value);
+        }
+        template <typename T, flamegpu::size_type N>
+        __device__ void setVariable(detail::VarName name, unsigned int i, T value) const {
+            if (!start(name)) return;
+            detail::write_var<T>(P, &P.T->birth, name.hash, index, value, i);
+        }
+        /** Ids of new agents are assigned when the step's compaction appends them
+         * (next id + birth rank, deterministic), after this function returns. */
+        __device__ id_t getID() const {
+            detail::device_error(P, detail::kDevUnsupported, 0, index);
+            return ID_NOT_SET;
+        }
+        __device__ uint32_t born() const { return is_born; }
+
+     private:
+        // First write of a birth: fill the staging row with the defaults.
+        __device__ bool start(const detail::VarName& name) const {
+            if (!P.birth_flags) {
+                detail::device_error(P, detail::kDevBirthNotEnabled, name.hash, index);
+                return false;
+            }
+            if (name.reserved) {
+                detail::device_error(P, detail::kDevReservedName, name.hash, index);
+                return false;
+            }
+            if (!is_born) {
+                is_born = 1;
+                const detail::VarTable* def = &P.T->birth_def;
+                const detail::VarTable* dst = &P.T->birth;
+                for (int s = 0; s < detail::kMaxVarSlots; ++s) {
+                    const char* d = reinterpret_cast<const char*>(
+                        __ldg(reinterpret_cast<const unsigned long long*>(&def->slot[s].ptr)));
+                    if (!d) continue;
+                    char* o = reinterpret_cast<char*>(__ldg(reinterpret_cast<const unsigned long long*>(&dst->slot[s].ptr)));
+                    const uint32_t bytes = __ldg(&def->slot[s].stride);
+                    o += static_cast<size_t>(index) * __ldg(&dst->slot[s].stride);
+                    for (uint32_t b = 0; b < bytes; ++b) o[b] = d[b];
+                }
+            }
+            return true;
+        }
+        const detail::LaunchParams& P;
+        uint32_t index;
+        mutable uint32_t is_born = 0;
+    };
+
+    __device__ DeviceAPI(const detail::LaunchParams& p, uint32_t idx)
+        : message_in(p), message_out(p, idx), agent_out(p, idx), environment(p), random(p, idx), P(p), index(idx) {}
+
+    template <typename T>
+    __device__ T getVariable(detail::VarName name) const {
+        return detail::read_rw<T>(P, &P.T->agent, name.hash, index);
+    }
+    template <typename T, flamegpu::size_type N>
+    __device__ T getVariable(detail::VarName name, unsigned int i) const {
+        return detail::read_rw<T>(P, &P.T->agent, name.hash, index, i);
+    }
+    template <typename T>
+    __device__ void setVariable(detail::VarName name, T value) {
+#if FLAMEGPU_SEATBELTS
+        if (name.reserved) {
+            detail::device_error(P, detail::kDevReservedName, name.hash, index);
+            return;
+        }
+#endif
+        detail::write_var<T>(P, &P.T->agent, name.hash, index, value);
+    }
+    template <typename T, flamegpu::size_type N>
+    __device__ void setVariable(detail::VarName name, unsigned int i, T value) {
+        detail::write_var<T>(P, &P.T->agent, name.hash, index, value, i);
+    }
+    __device__ id_t getID() const { return detail::read_rw<id_t>(P, &P.T->agent, detail::VarName("_id").hash, index); }
+    __device__ unsigned int getStepCounter() const { return *P.d_step; }
+    __device__ unsigned int getIndex() const { return index; }
+
+    typename MessageIn::In message_in;
+    typename MessageOut::Out message_out;
+    AgentOut agent_out;
+    DeviceEnvironment environment;
+    AgentRandom random;
+
+ private:
+    const detail::LaunchParams& P;
+    uint32_t index;
+};
+
+#endif  // __CUDACC__
+
+}  // namespace flamegpu
+
+#endif  // INCLUDE_FLAMEGPU_RUNTIME_DEVICEAPI_CUH_

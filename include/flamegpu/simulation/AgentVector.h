@@ -1,0 +1,119 @@
+#ifndef INCLUDE_FLAMEGPU_SIMULATION_AGENTVECTOR_H_
+#define INCLUDE_FLAMEGPU_SIMULATION_AGENTVECTOR_H_
+// Host-side population container (include/flamegpu/simulation/AgentVector.h in
+// the reference): a vector of agents of one AgentDescription, accessed through
+// AgentVector::Agent views. Stored as one byte column per variable (the same
+// struct-of-arrays layout the device uses), including the internal _id.
+#include <array>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <typeindex>
+#include <vector>
+
+#include "flamegpu/model/ModelDescription.h"
+
+namespace flamegpu {
+
+class AgentVector {
+ public:
+    class Agent {
+     public:
+        Agent(AgentVector* v, flamegpu::size_type i) : vec(v), index(i) {}
+        template <typename T>
+        void setVariable(const std::string& name, T value) {
+            if (!name.empty() && name[0] == '_')
+                THROW exception::ReservedName(exception::format("Variable '%s' is internal", name.c_str()));
+            std::memcpy(vec->ptr(name, typeid(T), sizeof(T), index, 0), &value, sizeof(T));
+        }
+        template <typename T, flamegpu::size_type N>
+        void setVariable(const std::string& name, const std::array<T, N>& value) {
+            for (flamegpu::size_type k = 0; k < N; ++k)
+                std::memcpy(vec->ptr(name, typeid(T), sizeof(T), index, k, N), &value[k], sizeof(T));
+        }
+        template <typename T, flamegpu::size_type N = 0>
+        void setVariable(const std::string& name, flamegpu::size_type element, T value) {
+            std::memcpy(vec->ptr(name, typeid(T), sizeof(T), index, element), &value, sizeof(T));
+        }
+        template <typename T>
+        T getVariable(const std::string& name) const {
+            T v;
+            std::memcpy(&v, vec->ptr(name, typeid(T), sizeof(T), index, 0), sizeof(T));
+            return v;
+        }
+        template <typename T, flamegpu::size_type N>
+        std::array<T, N> getVariable(const std::string& name) const {
+            std::array<T, N> v;
+            for (flamegpu::size_type k = 0; k < N; ++k)
+                std::memcpy(&v[k], vec->ptr(name, typeid(T), sizeof(T), index, k, N), sizeof(T));
+            return v;
+        }
+        template <typename T, flamegpu::size_type N = 0>
+        T getVariable(const std::string& name, flamegpu::size_type element) const {
+            T v;
+            std::memcpy(&v, vec->ptr(name, typeid(T), sizeof(T), index, element), sizeof(T));
+            return v;
+        }
+        id_t getID() const {
+            id_t v;
+            std::memcpy(&v, vec->ptr("_id", typeid(id_t), sizeof(id_t), index, 0), sizeof(id_t));
+            return v;
+        }
+        flamegpu::size_type getIndex() const { return index; }
+
+     private:
+        AgentVector* vec;
+        flamegpu::size_type index;
+    };
+
+    class iterator {
+     public:
+        iterator(AgentVector* v, flamegpu::size_type i) : vec(v), index(i) {}
+        Agent operator*() const { return Agent(vec, index); }
+        iterator& operator++() {
+            ++index;
+            return *this;
+        }
+        bool operator!=(const iterator& o) const { return index != o.index; }
+        bool operator==(const iterator& o) const { return index == o.index; }
+
+     private:
+        AgentVector* vec;
+        flamegpu::size_type index;
+    };
+
+    explicit AgentVector(const AgentDescription& agent, flamegpu::size_type count = 0);
+    flamegpu::size_type size() const { return count; }
+    bool empty() const { return count == 0; }
+    Agent operator[](flamegpu::size_type i) { return Agent(this, i); }
+    Agent at(flamegpu::size_type i);
+    Agent front() { return at(0); }
+    Agent back() { return at(count - 1); }
+    void push_back();
+    void resize(flamegpu::size_type n);
+    void reserve(flamegpu::size_type n);
+    void clear() { resize(0); }
+    iterator begin() { return iterator(this, 0); }
+    iterator end() { return iterator(this, count); }
+    std::string getAgentName() const { return agent->name; }
+    const detail::AgentData* getAgentData() const { return agent; }
+
+    // Raw column access (struct of arrays), used by CUDASimulation.
+    char* column(const std::string& name);
+    const char* column(const std::string& name) const;
+    size_t columnIndex(const std::string& name) const;
+    std::vector<std::vector<char>>& columns() { return cols; }
+    void setCountRaw(flamegpu::size_type n);
+
+ private:
+    char* ptr(const std::string& name, const std::type_info& t, size_t size, flamegpu::size_type i,
+              flamegpu::size_type element, flamegpu::size_type expect_len = 0);
+    std::shared_ptr<detail::ModelData> model;
+    detail::AgentData* agent;
+    std::vector<std::vector<char>> cols;
+    flamegpu::size_type count = 0;
+};
+
+}  // namespace flamegpu
+
+#endif  // INCLUDE_FLAMEGPU_SIMULATION_AGENTVECTOR_H_

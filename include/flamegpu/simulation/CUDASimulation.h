@@ -1,0 +1,143 @@
+#ifndef INCLUDE_FLAMEGPU_SIMULATION_CUDASIMULATION_H_
+#define INCLUDE_FLAMEGPU_SIMULATION_CUDASIMULATION_H_
+// CUDASimulation (include/flamegpu/simulation/CUDASimulation.h:177-418 in the
+// reference) on GB300: every step is one captured CUDA graph per buffer
+// parity (auto spatial sort, message index builds, agent function launches
+// and birth/death compaction, with populations kept on the device); the
+// host synchronises only when a population could outgrow its buffers or when
+// results are read back.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "flamegpu/model/ModelDescription.h"
+#include "flamegpu/simulation/AgentVector.h"
+
+namespace flamegpu {
+
+namespace detail {
+struct SimulationImpl;
+}
+
+/** Host-side API of init/step/exit/host-layer functions (reduced to properties and counts). */
+class HostAPI {
+ public:
+    class Environment {
+     public:
+        explicit Environment(detail::SimulationImpl* s) : sim(s) {}
+        template <typename T>
+        T getProperty(const std::string& name) const {
+            T v;
+            get(name, typeid(T), sizeof(T), &v);
+            return v;
+        }
+        template <typename T>
+        T setProperty(const std::string& name, T value) {
+            T old;
+            get(name, typeid(T), sizeof(T), &old);
+            set(name, typeid(T), sizeof(T), &value);
+            return old;
+        }
+
+     private:
+        void get(const std::string& name, const std::type_info& t, size_t size, void* out) const;
+        void set(const std::string& name, const std::type_info& t, size_t size, const void* in);
+        detail::SimulationImpl* sim;
+    };
+    class AgentAPI {
+     public:
+        AgentAPI(detail::SimulationImpl* s, std::string a, std::string st) : sim(s), agent(std::move(a)), state(std::move(st)) {}
+        unsigned int count() const;
+
+     private:
+        detail::SimulationImpl* sim;
+        std::string agent, state;
+    };
+    explicit HostAPI(detail::SimulationImpl* s) : environment(s), sim(s) {}
+    AgentAPI agent(const std::string& name, const std::string& state = "default") { return AgentAPI(sim, name, state); }
+    unsigned int getStepCounter() const;
+    Environment environment;
+
+ private:
+    detail::SimulationImpl* sim;
+};
+
+class CUDASimulation {
+ public:
+    /** Simulation::Config (include/flamegpu/simulation/Simulation.h:37-70). */
+    struct SimConfig {
+        unsigned int steps = 1;
+        uint64_t random_seed = 0;
+        bool verbose = false;
+        bool timing = false;
+    };
+    /** CUDASimulation::Config (CUDASimulation.h:100-128) plus the GB300 switches. */
+    struct Config {
+        int device_id = 0;
+        bool inLayerConcurrency = true;
+        bool use_graphs = true;       // capture each step into a CUDA graph and replay it
+        bool check_each_step = false; // synchronise and check device errors after every step()
+    };
+
+    explicit CUDASimulation(const ModelDescription& model, int argc = 0, const char** argv = nullptr);
+    ~CUDASimulation();
+    CUDASimulation(const CUDASimulation&) = delete;
+    CUDASimulation& operator=(const CUDASimulation&) = delete;
+
+    SimConfig& SimulationConfig();
+    Config& CUDAConfig();
+    void applyConfig();
+
+    void setPopulationData(AgentVector& population, const std::string& state = "default");
+    void getPopulationData(AgentVector& population, const std::string& state = "default");
+
+    /** One step (all layers). Returns false if an exit condition requests a stop. */
+    bool step();
+    /** SimulationConfig().steps steps. */
+    void simulate();
+    unsigned int getStepCounter() const;
+    void resetStepCounter();
+
+    double getElapsedTimeSimulation() const;
+    std::vector<double> getElapsedTimeSteps() const;
+    double getElapsedTimeStep(unsigned int step) const;
+
+    template <typename T>
+    void setEnvironmentProperty(const std::string& name, T value) {
+        HostAPI::Environment e(impl.get());
+        e.setProperty<T>(name, value);
+    }
+    template <typename T>
+    T getEnvironmentProperty(const std::string& name) {
+        HostAPI::Environment e(impl.get());
+        return e.getProperty<T>(name);
+    }
+
+    // ---- GB300 extensions (device-resident access) ----
+    /** Stream every step is issued on. */
+    cudaStream_t getStream() const;
+    /** Waits for the simulation's stream; throws exception::DeviceError for recorded device errors. */
+    void synchronize();
+    /** Agents in a state list (synchronises). */
+    unsigned int getAgentCount(const std::string& agent, const std::string& state = "default");
+    /** Device pointer to the current column of an agent variable (valid until the next step). */
+    void* getDeviceVariable(const std::string& agent, const std::string& variable, const std::string& state = "default");
+    /** Device pointer to the device-resident agent count of a state list. */
+    const unsigned int* getDeviceCount(const std::string& agent, const std::string& state = "default");
+    /** Graph replays issued so far (0 when graphs are disabled). */
+    unsigned long long getGraphLaunches() const;
+    /** Kernel launches issued by the last step (counted at capture / issue). */
+    unsigned int getKernelsPerStep() const;
+
+    detail::SimulationImpl* getImpl() const { return impl.get(); }
+
+ private:
+    std::unique_ptr<detail::SimulationImpl> impl;
+};
+
+}  // namespace flamegpu
+
+#endif  // INCLUDE_FLAMEGPU_SIMULATION_CUDASIMULATION_H_

@@ -1,0 +1,68 @@
+/*
+ * fg_sim.h — C ABI over the C++ simulation runtime (libflamegpu2_gb300.so).
+ *
+ * Lets a non-C++ caller drive CUDASimulation / CUDAEnsemble-style runs of a
+ * registered model: the role pyflamegpu's SWIG layer plays for the reference
+ * (swig/python/flamegpu.i wraps ModelDescription, CUDASimulation::{setPopulationData,
+ * getPopulationData, step, simulate} and CUDAEnsemble::simulate). Models are
+ * C++ translation units that register a factory under a name
+ * (fgs_register_model); the bundled ones live in libfg_models.so.
+ *
+ * Every function returns 0 on success or -1 with a message in fgs_last_error().
+ */
+#ifndef FLAMEGPU_GB300_FG_SIM_H_
+#define FLAMEGPU_GB300_FG_SIM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fgs_sim fgs_sim;
+
+/* A model factory: builds a flamegpu::ModelDescription (returned as void*,
+ * owned by the caller of the factory) from numeric parameters. */
+typedef void* (*fgs_model_factory)(const double* params, int32_t nparams);
+
+int fgs_register_model(const char* name, fgs_model_factory factory);
+/* Comma-separated names of the registered models. */
+int fgs_list_models(char* buf, size_t len);
+const char* fgs_last_error(void);
+
+/* new CUDASimulation(model) (include/flamegpu/simulation/CUDASimulation.h:177). */
+fgs_sim* fgs_create(const char* model, const double* params, int32_t nparams, int32_t device);
+void fgs_destroy(fgs_sim* sim);
+/* SimulationConfig().steps / random_seed and the GB300 switches. */
+int fgs_configure(fgs_sim* sim, uint32_t steps, uint64_t seed, int32_t use_graphs, int32_t check_each_step);
+/* setPopulationData: n agents; the named host columns (struct of arrays, each
+ * n * sizeof(variable) bytes) are copied, other variables take their defaults.
+ * "_id" may be given; unset (0) ids are assigned. */
+int fgs_set_population(fgs_sim* sim, const char* agent, const char* state, uint32_t n, int32_t nvars,
+                       const char* const* names, const void* const* host_cols);
+/* Same, from device columns (no host copy of the data). */
+int fgs_set_population_device(fgs_sim* sim, const char* agent, const char* state, uint32_t n, int32_t nvars,
+                              const char* const* names, const void* const* device_cols);
+int fgs_get_count(fgs_sim* sim, const char* agent, const char* state, uint32_t* n);
+/* getPopulationData for one variable: copies count * sizeof(variable) bytes. */
+int fgs_get_variable(fgs_sim* sim, const char* agent, const char* state, const char* var, void* out, size_t bytes);
+/* Copy one variable's current device column into a device buffer (no host hop). */
+int fgs_get_variable_device(fgs_sim* sim, const char* agent, const char* state, const char* var, void* dst,
+                            size_t bytes);
+int fgs_step(fgs_sim* sim, uint32_t steps);
+int fgs_simulate(fgs_sim* sim);
+/* Waits for the simulation stream and reports recorded device errors. */
+int fgs_synchronize(fgs_sim* sim);
+int fgs_set_environment(fgs_sim* sim, const char* name, const void* value, size_t bytes);
+int fgs_get_environment(fgs_sim* sim, const char* name, void* value, size_t bytes);
+int fgs_stream(fgs_sim* sim, void** stream);
+int fgs_stats(fgs_sim* sim, uint64_t* graph_launches, uint32_t* kernels_per_step, uint32_t* step_counter);
+/* getElapsedTimeSteps (seconds) for up to cap steps; returns the count in *n. */
+int fgs_step_times(fgs_sim* sim, double* out, uint32_t cap, uint32_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLAMEGPU_GB300_FG_SIM_H_ */

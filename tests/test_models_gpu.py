@@ -1,0 +1,196 @@
+"""Model-level parity: agent functions written against the FLAME GPU 2 API run
+through CUDASimulation (C ABI) and are compared with the serial oracle and
+with the reference tests' known answers."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim():
+    from flamegpu2_gb300 import sim
+    return sim
+
+
+def _count_run(dims, mn, mx, r, wrap, optional, pos, do_output=None):
+    S = _sim()
+    n = pos.shape[0]
+    params = [dims] + list(mn) + [0.0] * (3 - len(mn)) + list(mx) + [0.0] * (3 - len(mx)) + [r, int(wrap), int(optional)]
+    s = S.Simulation("spatial_count", params)
+    cols = {"_id": np.arange(1, n + 1, dtype=np.uint32), "x": pos[:, 0].copy(), "y": pos[:, 1].copy()}
+    if dims == 3:
+        cols["z"] = pos[:, 2].copy()
+    if do_output is not None:
+        cols["do_output"] = do_output.astype(np.int32)
+    s.set_population("agent", n, cols)
+    s.step()
+    out = {k: s.get("agent", k, np.uint32) for k in ("_id", "count", "badCount")}
+    for k in ("result_x", "result_y", "result_z", "x", "y"):
+        out[k] = s.get("agent", k, np.float32)
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("optional", [False, True])
+def test_spatial3d_counts_match_reference_expectation(golden, optional):
+    pre = "s3d_optional_" if optional else "s3d_mandatory_"
+    pos = golden[pre + "pos"].reshape(-1, 3)
+    r = _count_run(3, (0, 0, 0), (5, 5, 5), 1.0, False, optional, pos, golden[pre + "do_output"] if optional else None)
+    agent = r["_id"] - 1
+    np.testing.assert_array_equal(r["count"], golden[pre + "expect"][agent])
+    assert int(r["badCount"].sum()) == 0
+    # agent order after the automatic spatial sort matches the oracle's stable sort
+    o = O.count_model(O.grid(3, (0, 0, 0), (5, 5, 5), 1.0), False, pos[:, 0], pos[:, 1], pos[:, 2],
+                      do_output=golden[pre + "do_output"] if optional else None)
+    np.testing.assert_array_equal(agent, o["order"])
+
+
+@pytest.mark.parametrize("optional", [False, True])
+def test_spatial2d_counts_match_reference_expectation(golden, optional):
+    pre = "s2d_optional_" if optional else "s2d_mandatory_"
+    pos = golden[pre + "pos"].reshape(-1, 2)
+    r = _count_run(2, (0, 0), (11, 11), 1.0, False, optional, pos, golden[pre + "do_output"] if optional else None)
+    np.testing.assert_array_equal(r["count"], golden[pre + "expect"][r["_id"] - 1])
+    assert int(r["badCount"].sum()) == 0
+
+
+@pytest.mark.parametrize("off", [(0.0, 0.0, 0.0), (141.0, -540.0, 200.0), (-1401.5, 5640.3, -2008.8)])
+def test_spatial3d_wrapped_lattice(off):
+    i, j, k = np.meshgrid(np.arange(35), np.arange(35), np.arange(35), indexing="ij")
+    pos = np.stack([(i.ravel() * np.float32(2.0) + np.float32(off[0])),
+                    (j.ravel() * np.float32(2.0) + np.float32(off[1])),
+                    (k.ravel() * np.float32(2.0) + np.float32(off[2]))], 1).astype(np.float32)
+    r = _count_run(3, off, tuple(o + 70 for o in off), 3.5, True, False, pos)
+    assert np.all(r["count"] == 27)
+    assert np.all(r["badCount"] <= 189)
+    assert np.all(r["result_x"] == 0.0) and np.all(r["result_y"] == 0.0) and np.all(r["result_z"] == 0.0)
+
+
+@pytest.mark.parametrize("off", [(0.0, 0.0), (141.0, 0.0), (0.0, 3440.0), (-2342.0, 0.0), (141.4, -540.7)])
+def test_spatial2d_wrapped_lattice(off):
+    i, j = np.meshgrid(np.arange(15), np.arange(15), indexing="ij")
+    pos = np.stack([(i.ravel() * np.float32(2.0) + np.float32(off[0])),
+                    (j.ravel() * np.float32(2.0) + np.float32(off[1]))], 1).astype(np.float32)
+    r = _count_run(2, off, tuple(o + 30 for o in off), 3.0, True, False, pos)
+    assert np.all(r["count"] == 9)
+    assert np.all(r["result_x"] == 0.0) and np.all(r["result_y"] == 0.0)
+
+
+def test_spatial3d_bounds_not_factor_radius():
+    h = np.float32(50.1) / np.float32(2)
+    pos = np.array([[h, 0.0, h], [h, 18.0, h], [0.0, h, 0.5], [18.0, h, 0.5], [h, 50.0, 50.1],
+                    [h, 50.0, np.float32(50.1) - np.float32(10.11)]], np.float32)
+    r = _count_run(3, (0, 0, 0), (50.1, 50.1, 50.1), 10.0, False, False, pos)
+    by_id = dict(zip(r["_id"].tolist(), r["count"].tolist()))
+    assert [by_id[i] for i in range(1, 7)] == [2, 2, 2, 2, 1, 1]
+
+
+def test_wrapped_out_of_bounds_raises_device_error():
+    # test_spatial_3d.cu:976-979 (Wrapped_OutOfBounds): a location outside the
+    # bounds given to the wrapped iterator is a device error, reported on the host.
+    S = _sim()
+    i, j, k = np.meshgrid(np.arange(35), np.arange(35), np.arange(35), indexing="ij")
+    pos = np.stack([(i.ravel() * 2.0 + 141.0 + 200.0), (j.ravel() * 2.0 - 540.0), (k.ravel() * 2.0)], 1).astype(np.float32)
+    with pytest.raises(S.SimError, match="DeviceError"):
+        _count_run(3, (141.0, -540.0, 0.0), (211.0, -470.0, 70.0), 3.5, True, False, pos)
+
+
+def test_agent_death_order(golden):
+    S = _sim()
+    x = golden["death_x"]
+    s = S.Simulation("agent_death")
+    s.set_population("agent", len(x), {"x": x.astype(np.uint32)})
+    s.step()
+    np.testing.assert_array_equal(s.get("agent", "x", np.uint32), golden["death_expect"])
+    s.close()
+
+
+@pytest.mark.parametrize("optional", [False, True])
+def test_bruteforce_counts(optional):
+    S = _sim()
+    n = 3000
+    rng = np.random.default_rng(2)
+    x = rng.integers(-50, 50, n).astype(np.int32)
+    do = (rng.random(n) < 0.7).astype(np.int32) if optional else np.ones(n, np.int32)
+    s = S.Simulation("bruteforce_count", [int(optional)])
+    s.set_population("agent", n, {"x": x, "do_output": do})
+    s.step()
+    assert np.all(s.get("agent", "count", np.uint32) == int(do.sum()))
+    assert np.all(s.get("agent", "sum", np.int32) == int((x * do).sum()))
+    s.close()
+
+
+def _boids_run(cfg, steps, use_graphs=True):
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    pop = synth.boids_population(cfg["n"], cfg["min_pos"], cfg["max_pos"], cfg["seed"])
+    s = S.Simulation("boids_spatial3d", synth.boids_params(cfg), steps=steps, use_graphs=use_graphs)
+    s.set_population("Boid", cfg["n"], pop)
+    s.step(steps)
+    out = {"_id": s.get("Boid", "_id", np.uint32)}
+    for k in ("x", "y", "z", "fx", "fy", "fz"):
+        out[k] = s.get("Boid", k, np.float32)
+    st = s.stats()
+    s.close()
+    return pop, out, st
+
+
+def _boids_oracle(cfg, pop, steps):
+    p = O.boids_params(cfg["min_pos"], cfg["max_pos"], cfg["interaction_radius"], cfg["separation_radius"],
+                       cfg["time_scale"], cfg["global_scale"], cfg["steer_scale"], cfg["collision_scale"],
+                       cfg["match_scale"], cfg["wrap"], cfg["sort_period"])
+    st = {"id": pop["_id"], **{k: pop[k] for k in ("x", "y", "z", "fx", "fy", "fz")}}
+    return O.boids_run(p, st, steps)
+
+
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_boids_small_matches_oracle(use_graphs):
+    # Boids on MessageSpatial3D, 16,384 agents, 32^3 bins, wrapped, 10 steps.
+    from flamegpu2_gb300 import synth
+    cfg = dict(synth.BOIDS_SMALL)
+    pop, out, st = _boids_run(cfg, 10, use_graphs)
+    ref = _boids_oracle(cfg, pop, 10)
+    # agent order (auto spatial sort) and ids are exact; positions within 1e-4
+    np.testing.assert_array_equal(out["_id"], ref["id"])
+    for k in ("x", "y", "z"):
+        np.testing.assert_allclose(out[k], ref[k], rtol=0, atol=1e-4)
+    for k in ("fx", "fy", "fz"):
+        np.testing.assert_allclose(out[k], ref[k], rtol=0, atol=1e-4)
+    if use_graphs:
+        assert st["graph_launches"] == 10
+
+
+def test_boids_clamped_matches_oracle():
+    from flamegpu2_gb300 import synth
+    cfg = dict(synth.BOIDS_SMALL, n=6000, wrap=0, min_pos=-0.5, max_pos=0.5, interaction_radius=0.05,
+               separation_radius=0.01, time_scale=0.0005, global_scale=0.15, steer_scale=0.055,
+               collision_scale=10.0, match_scale=0.015, seed=5)
+    pop, out, _ = _boids_run(cfg, 5)
+    ref = _boids_oracle(cfg, pop, 5)
+    np.testing.assert_array_equal(out["_id"], ref["id"])
+    for k in ("x", "y", "z", "fx", "fy", "fz"):
+        np.testing.assert_allclose(out[k], ref[k], rtol=0, atol=1e-4)
+
+
+def test_birth_death_matches_oracle_exactly():
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    n, steps, seed = 100_000, 25, 1
+    pop = synth.birth_death_population(n, seed)
+    s = S.Simulation("birth_death", [0.30, 0.20, seed])
+    s.set_population("agent", n, pop)
+    s.step(steps)
+    f = np.stack([s.get("agent", f"f{v}", np.float32) for v in range(8)])
+    cnt = s.get("agent", "counter", np.int32)
+    ids = s.get("agent", "_id", np.uint32)
+    s.close()
+    fo, co, io, nid, pops = O.birth_death_run(np.stack([pop[f"f{v}"] for v in range(8)]), pop["counter"],
+                                              pop["_id"], n + 1, 4 * n, 0.30, 0.20, seed, steps)
+    assert len(ids) == len(io)
+    np.testing.assert_array_equal(ids, io)
+    np.testing.assert_array_equal(cnt, co)
+    np.testing.assert_array_equal(f, fo)
