@@ -1,4 +1,5 @@
 // C ABI over CUDASimulation (include/flamegpu_gb300/fg_sim.h) and the model registry.
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -150,6 +151,20 @@ extern "C" int fgs_get_variable(fgs_sim* s, const char* agent, const char* state
     });
 }
 
+extern "C" int fgs_get_population(fgs_sim* s, const char* agent, const char* state, int32_t nvars,
+                                  const char* const* names, void* const* out, uint32_t cap, uint32_t* n) {
+    return guarded([&] {
+        flamegpu::AgentVector pop(s->model->Agent(agent));
+        s->sim->getPopulationData(pop, state);
+        if (pop.size() > cap) throw flamegpu::exception::InvalidArgument("output buffers too small");
+        for (int32_t k = 0; k < nvars; ++k) {
+            const auto& col = pop.columns()[pop.columnIndex(names[k])];
+            std::memcpy(out[k], col.data(), col.size());
+        }
+        *n = pop.size();
+    });
+}
+
 extern "C" int fgs_get_variable_device(fgs_sim* s, const char* agent, const char* state, const char* var, void* dst,
                                        size_t bytes) {
     return guarded([&] {
@@ -214,5 +229,24 @@ extern "C" int fgs_step_times(fgs_sim* s, double* out, uint32_t cap, uint32_t* n
         const uint32_t m = static_cast<uint32_t>(std::min<size_t>(cap, t.size()));
         for (uint32_t i = 0; i < m; ++i) out[i] = t[i];
         *n = m;
+    });
+}
+
+extern "C" int fgs_profile_ops(fgs_sim* s, int32_t enable) {
+    return guarded([&] { s->sim->CUDAConfig().profile_ops = enable != 0; });
+}
+
+extern "C" int fgs_take_profile(fgs_sim* s, char* buf, size_t len) {
+    return guarded([&] {
+        std::string out;
+        for (const auto& t : s->sim->takeOperationProfile()) {
+            char tmp[512];
+            std::snprintf(tmp, sizeof(tmp), "%s,%.6f,%llu;", std::get<0>(t).c_str(), std::get<1>(t), std::get<2>(t));
+            out += tmp;
+        }
+        if (len) {
+            std::strncpy(buf, out.c_str(), len - 1);
+            buf[len - 1] = 0;
+        }
     });
 }

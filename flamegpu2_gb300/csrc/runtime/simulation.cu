@@ -24,6 +24,7 @@
 #include <memory>
 #include <random>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "flamegpu/simulation/CUDASimulation.h"
@@ -113,6 +114,7 @@ struct MsgList {
     // spatial
     fg_spatial_grid grid{};
     uint32_t* pbm = nullptr;
+    uint32_t pbm_alloc = 0;
     uint32_t* records = nullptr;
     uint32_t record_words = 0;
     std::vector<uint32_t> field_word;
@@ -139,6 +141,7 @@ struct FnRt {
     void* birth_defaults = nullptr;
     FunctionTables* d_tables[2] = {nullptr, nullptr};
     bool sort_trigger = false;
+    bool stage = false;  // spatial input and the agent has float x, y (, z): stage neighbour windows
 };
 
 struct SimulationImpl {
@@ -169,6 +172,10 @@ struct SimulationImpl {
     unsigned int kernels_last_step = 0;
     unsigned int kernel_counter = 0;
     bool allocated = false;
+    // per-operation profile (eager mode only): label -> events
+    bool profiling = false;
+    std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>> op_events;
+    std::map<std::string, std::pair<double, uint64_t>> op_totals;  // label -> (ms, count)
     // timing
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> step_events;
     std::vector<double> step_ms;
@@ -250,7 +257,9 @@ struct SimulationImpl {
             if (m->kind != MessageKind::BruteForce) {
                 const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
                 FG_CAPI(fg_spatial_grid_init(&ml->grid, dims, m->min, m->max, m->radius));
-                ml->pbm = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(ml->grid.binCount) + 1)));
+                // PBM padded to a multiple of 4 entries (+4): the staging window copies 16-byte aligned slices
+                ml->pbm_alloc = (ml->grid.binCount + 1u + 3u) & ~3u;
+                ml->pbm = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(ml->pbm_alloc) + 4)));
                 uint32_t w = 0;
                 for (uint32_t b : ml->slot_bytes) {
                     ml->field_word.push_back(w);
@@ -287,6 +296,7 @@ struct SimulationImpl {
                         ok = ok && v && v->type == std::type_index(typeid(float)) && v->elements == 1;
                     }
                     r.sort_trigger = ok;
+                    r.stage = ok;
                 }
                 fns.push_back(std::move(r));
             }
@@ -588,6 +598,36 @@ struct SimulationImpl {
         return k;
     }
 
+    // Runs op() on the stream, bracketed by events when profiling (eager mode).
+    template <typename Op>
+    void timed(const std::string& label, Op&& op) {
+        if (!profiling) {
+            op();
+            return;
+        }
+        cudaEvent_t a, b;
+        FG_CUDA(cudaEventCreate(&a));
+        FG_CUDA(cudaEventCreate(&b));
+        FG_CUDA(cudaEventRecord(a, stream));
+        op();
+        FG_CUDA(cudaEventRecord(b, stream));
+        op_events.emplace_back(label, a, b);
+    }
+
+    void resolve_profile() {
+        for (auto& t : op_events) {
+            float ms = 0;
+            cudaEventSynchronize(std::get<2>(t));
+            cudaEventElapsedTime(&ms, std::get<1>(t), std::get<2>(t));
+            auto& acc = op_totals[std::get<0>(t)];
+            acc.first += ms;
+            acc.second += 1;
+            cudaEventDestroy(std::get<1>(t));
+            cudaEventDestroy(std::get<2>(t));
+        }
+        op_events.clear();
+    }
+
     void enqueue_sort(FnRt& f) {
         AgentList& l = *f.list;
         const fg_spatial_grid* g = &f.in->grid;
@@ -631,8 +671,9 @@ struct SimulationImpl {
 
     void enqueue_function(FnRt& f) {
         AgentList& l = *f.list;
-        if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0) enqueue_sort(f);
-        if (f.in && f.in->spatial() && f.in->needs_build) enqueue_build(*f.in);
+        if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0)
+            timed("sort:" + l.agent->name, [&] { enqueue_sort(f); });
+        if (f.in && f.in->spatial() && f.in->needs_build) timed("build:" + f.in->msg->name, [&] { enqueue_build(*f.in); });
         if (f.out && f.out->optional_any && !f.fn->message_output_optional)
             FG_CUDA(cudaMemsetAsync(f.out->valid, 1, sizeof(uint32_t) * f.out->capacity, stream));
         LaunchParams P;
@@ -650,6 +691,11 @@ struct SimulationImpl {
                 P.in_grid = f.in->grid;
                 P.in_pbm = f.in->pbm;
                 P.in_count = f.in->pbm + f.in->grid.binCount;
+                P.in_records = reinterpret_cast<const char*>(f.in->records);
+                P.in_record_bytes = f.in->record_words * 4u;
+                P.in_pbm_alloc = f.in->pbm_alloc;
+                if (f.stage && cuda_config.message_stage_bytes >= 1024u)
+                    P.stage_bytes = (cuda_config.message_stage_bytes + 15u) & ~15u;
             } else {
                 P.in_count = f.in->optional_any ? f.in->bf_count : f.in->d_count;
             }
@@ -660,7 +706,9 @@ struct SimulationImpl {
         P.seed = config.random_seed;
         P.fn_uid = f.fn->uid;
         P.error = d_error();
-        const cudaError_t e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 16), kAgentBlock, stream);
+        cudaError_t e = cudaSuccess;
+        const unsigned int smem = P.stage_bytes ? P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader)) : 0u;
+        timed("fn:" + f.fn->name, [&] { e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 16), kAgentBlock, smem, stream); });
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(e)));
         kernel_counter += 1;
@@ -685,11 +733,13 @@ struct SimulationImpl {
                 bcols[v] = fg_column{f.births ? f.birth_cols[v] : l.cols[v][l.parity], l.cols[v][l.parity ^ 1], b};
                 if (l.agent->variables[v].name == "_id") id_col = static_cast<int>(v);
             }
-            FG_CAPI(fg_compact_agents(l.capacity, l.d_count, f.fn->has_agent_death ? f.death_flags : nullptr,
-                                      f.births ? f.birth_flags : nullptr, cols.data(), bcols.data(),
-                                      static_cast<uint32_t>(cols.size()), f.births ? id_col : -1,
-                                      f.births ? d_next_id(agent_index(l.agent)) : nullptr, nullptr, l.d_count,
-                                      l.capacity, l.comp_ws, l.comp_ws_bytes, stream));
+            timed("compact:" + l.agent->name, [&] {
+                FG_CAPI(fg_compact_agents(l.capacity, l.d_count, f.fn->has_agent_death ? f.death_flags : nullptr,
+                                          f.births ? f.birth_flags : nullptr, cols.data(), bcols.data(),
+                                          static_cast<uint32_t>(cols.size()), f.births ? id_col : -1,
+                                          f.births ? d_next_id(agent_index(l.agent)) : nullptr, nullptr, l.d_count,
+                                          l.capacity, l.comp_ws, l.comp_ws_bytes, stream));
+            });
             l.parity ^= 1;
             kernel_counter += 2;
         }
@@ -741,7 +791,8 @@ struct SimulationImpl {
         FG_CUDA(cudaEventCreate(&e0));
         FG_CUDA(cudaEventCreate(&e1));
         FG_CUDA(cudaEventRecord(e0, stream));
-        if (has_layer_host_functions() || !cuda_config.use_graphs) {
+        profiling = cuda_config.profile_ops;
+        if (has_layer_host_functions() || !cuda_config.use_graphs || profiling) {
             HostAPI api(this);
             kernel_counter = 0;
             for (auto& m : msgs)
@@ -903,6 +954,15 @@ void CUDASimulation::applyConfig() { impl->invalidate(); }
 cudaStream_t CUDASimulation::getStream() const { return impl->stream; }
 unsigned long long CUDASimulation::getGraphLaunches() const { return impl->graph_launches; }
 unsigned int CUDASimulation::getKernelsPerStep() const { return impl->kernels_last_step; }
+
+std::vector<std::tuple<std::string, double, unsigned long long>> CUDASimulation::takeOperationProfile() {
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    impl->resolve_profile();
+    std::vector<std::tuple<std::string, double, unsigned long long>> r;
+    for (const auto& kv : impl->op_totals) r.emplace_back(kv.first, kv.second.first, kv.second.second);
+    impl->op_totals.clear();
+    return r;
+}
 
 void CUDASimulation::setPopulationData(AgentVector& pop, const std::string& state) {
     detail::AgentList* l = impl->list_of(pop.getAgentName(), state);

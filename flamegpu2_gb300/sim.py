@@ -18,9 +18,9 @@ MODELS_LIB = os.path.join(capi.LIBDIR, "libfg_models.so")
 
 SIM_EXPORTS = [
     "fgs_register_model", "fgs_list_models", "fgs_last_error", "fgs_create", "fgs_destroy", "fgs_configure",
-    "fgs_set_population", "fgs_set_population_device", "fgs_get_count", "fgs_get_variable",
+    "fgs_set_population", "fgs_set_population_device", "fgs_get_count", "fgs_get_variable", "fgs_get_population",
     "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
-    "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times",
+    "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
 ]
 
 _lock = threading.Lock()
@@ -50,6 +50,8 @@ def core():
             L.fgs_set_population_device.argtypes = L.fgs_set_population.argtypes
             L.fgs_get_count.argtypes = [vp, C.c_char_p, C.c_char_p, C.POINTER(u32)]
             L.fgs_get_variable.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
+            L.fgs_get_population.argtypes = [vp, C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_char_p), C.POINTER(vp), u32,
+                                             C.POINTER(u32)]
             L.fgs_get_variable_device.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
             L.fgs_step.argtypes = [vp, u32]
             L.fgs_simulate.argtypes = [vp]
@@ -59,6 +61,8 @@ def core():
             L.fgs_stream.argtypes = [vp, C.POINTER(vp)]
             L.fgs_stats.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(u32), C.POINTER(u32)]
             L.fgs_step_times.argtypes = [vp, C.POINTER(C.c_double), u32, C.POINTER(u32)]
+            L.fgs_profile_ops.argtypes = [vp, i32]
+            L.fgs_take_profile.argtypes = [vp, C.c_char_p, sz]
             _core = L
         if _models is None:
             if not os.path.exists(MODELS_LIB):
@@ -133,6 +137,16 @@ class Simulation:
                                        out.ctypes.data, out.nbytes))
         return out
 
+    def get_population(self, agent: str, outs: dict, state: str = "default") -> int:
+        """Fill caller arrays (name -> numpy array with room for every agent); returns the count."""
+        names = list(outs)
+        cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        cp = (C.c_void_p * max(1, len(names)))(*[outs[k].ctypes.data for k in names])
+        cap = min(o.shape[0] for o in outs.values())
+        n = C.c_uint32()
+        _check(core().fgs_get_population(self._h, agent.encode(), state.encode(), len(names), cn, cp, cap, C.byref(n)))
+        return n.value
+
     def get_device(self, agent: str, var: str, dst, state: str = "default"):
         """Copy a variable's device column into a torch tensor (async on the sim stream)."""
         _check(core().fgs_get_variable_device(self._h, agent.encode(), state.encode(), var.encode(),
@@ -172,3 +186,17 @@ class Simulation:
         n = C.c_uint32()
         _check(core().fgs_step_times(self._h, buf, cap, C.byref(n)))
         return np.array(buf[:n.value])
+
+    def profile_ops(self, enable: bool = True):
+        _check(core().fgs_profile_ops(self._h, int(enable)))
+
+    def take_profile(self) -> dict:
+        """label -> (total_ms, count) of the operations issued since the last call."""
+        buf = C.create_string_buffer(1 << 16)
+        _check(core().fgs_take_profile(self._h, buf, 1 << 16))
+        out = {}
+        for rec in buf.value.decode().split(";"):
+            if rec:
+                label, ms, cnt = rec.rsplit(",", 2)
+                out[label] = (float(ms), int(cnt))
+        return out

@@ -71,6 +71,20 @@ struct FunctionTables {
     VarTable env;        // environment properties (ptr -> value bytes)
 };
 
+/** Header of the shared-memory staging window of one block (spatial input). */
+struct StageHeader {
+    uint32_t rec_lo;   // first staged sorted message index
+    uint32_t rec_n;    // staged messages (0 = window empty)
+    uint32_t pbm_lo;   // first staged PBM entry
+    uint32_t pbm_n;    // staged PBM entries
+    uint32_t rec_bytes;
+    uint32_t phase;    // mbarrier phase of the next wait
+    uint32_t pad[2];
+    unsigned long long mbar;
+    unsigned long long pad2[3];
+};
+static_assert(sizeof(StageHeader) == 64, "staging header is 64 bytes");
+
 /** Device error codes recorded in LaunchParams::error[0]. */
 enum DeviceErrorCode : uint32_t {
     kDevOk = 0,
@@ -84,6 +98,7 @@ enum DeviceErrorCode : uint32_t {
     kDevReservedName = 8,
     kDevUnsupported = 9,
     kDevMessageOutNotEnabled = 10,
+    kDevStageTimeout = 11,
 };
 
 /** Kernel parameters of one agent function launch (passed __grid_constant__). */
@@ -99,6 +114,10 @@ struct LaunchParams {
     fg_spatial_grid in_grid;     // spatial metadata (MessageSpatial3D::MetaData)
     const uint32_t* in_pbm;      // partition boundary matrix, binCount + 1 entries
     const uint32_t* in_count;    // messages in the input list
+    const char* in_records;      // sorted message records (spatial input)
+    uint32_t in_record_bytes;    // bytes per record (multiple of 16)
+    uint32_t in_pbm_alloc;       // PBM entries readable (multiple of 4, >= binCount + 1)
+    uint32_t stage_bytes;        // shared memory for staging neighbour records (0 = off)
     // birth / death
     uint32_t* birth_flags;       // 1 where agent_out was used (null if disabled)
     uint32_t* death_flags;       // ALIVE / DEAD per agent (null if death disabled)

@@ -14,6 +14,7 @@
 // the optional-message flag of the row.
 #include <cuda_runtime.h>
 
+#include <type_traits>
 #include <typeindex>
 #include <typeinfo>
 
@@ -24,7 +25,7 @@ namespace detail {
 
 /** Launches the agent function kernel of one FLAMEGPU_AGENT_FUNCTION. */
 typedef cudaError_t (*AgentFunctionLauncher)(const LaunchParams& p, unsigned int grid, unsigned int block,
-                                             cudaStream_t stream);
+                                             unsigned int smem, cudaStream_t stream);
 
 constexpr unsigned int kAgentBlock = 128;
 
@@ -35,7 +36,15 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
     using MsgOut = typename F::MessageOut;
     const uint32_t n = P.d_n ? min(*P.d_n, P.max_n) : P.max_n;
     if (P.msg_out_count && blockIdx.x == 0 && threadIdx.x == 0) *P.msg_out_count = n;
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    constexpr int kDims = std::is_same<MsgIn, MessageSpatial3D>::value ? 3 : (std::is_same<MsgIn, MessageSpatial2D>::value ? 2 : 0);
+    bool first = true;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t idx = base + threadIdx.x;
+        if constexpr (kDims != 0) {
+            if (P.stage_bytes) stage_window<kDims>(P, idx, n, first);
+        }
+        first = false;
+        if (idx >= n) continue;
         DeviceAPI<MsgIn, MsgOut> api(P, idx);
         const AGENT_STATUS st = F()(&api);
         if (P.death_flags) {
@@ -49,8 +58,16 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
 }
 
 template <typename F>
-cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsigned int block, cudaStream_t stream) {
-    agent_function_kernel<F><<<grid, block, 0, stream>>>(p);
+cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int smem,
+                                  cudaStream_t stream) {
+    static unsigned int configured = 48u * 1024u;
+    if (smem > configured) {
+        const cudaError_t e = cudaFuncSetAttribute(agent_function_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    agent_function_kernel<F><<<grid, block, smem, stream>>>(p);
     return cudaGetLastError();
 }
 #endif

@@ -104,6 +104,195 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
     return z ^ (z >> 31);
 }
+
+__device__ __forceinline__ int clamp_cell(int v, uint32_t dim) {
+    const int d = static_cast<int>(dim);
+    return v < 0 ? 0 : (v >= d ? d - 1 : v);
+}
+// getGridPosition3D / getGridPosition2D (MessageSpatial3DDevice.cuh:646-659)
+__device__ __forceinline__ int grid_cell(const fg_spatial_grid& g, int axis, float p) {
+    return clamp_cell(static_cast<int>(floorf((p - g.min[axis]) / g.radius)), g.gridDim[axis]);
+}
+// getHash3D / getHash2D (MessageSpatial3DDevice.cuh:660-672): x clamped
+__device__ __forceinline__ uint32_t grid_hash(const fg_spatial_grid& g, int x, int y, int z) {
+    const uint32_t ux = static_cast<uint32_t>(clamp_cell(x, g.gridDim[0]));
+    return static_cast<uint32_t>(z) * g.gridDim[0] * g.gridDim[1] + static_cast<uint32_t>(y) * g.gridDim[0] + ux;
+}
+__device__ __forceinline__ float virtual_coord(float p1, float p2, float width) {
+    // getVirtualX (MessageSpatial3DDevice.cuh:373-397)
+    const float d = p2 - p1;
+    return fabsf(d) > width / 2.0f ? p2 - (d / fabsf(d) * width) : p2;
+}
+
+// ---- shared-memory staging window of a block's spatial neighbourhood ----
+// Layout of the dynamic shared memory: StageHeader (64 B) | PBM slice | records.
+__device__ __forceinline__ char* dyn_smem() {
+    extern __shared__ __align__(128) char fg_dyn_smem[];
+    return fg_dyn_smem;
+}
+__device__ __forceinline__ StageHeader* stage_hdr() { return reinterpret_cast<StageHeader*>(dyn_smem()); }
+__device__ __forceinline__ const uint32_t* stage_pbm() {
+    return reinterpret_cast<const uint32_t*>(dyn_smem() + sizeof(StageHeader));
+}
+__device__ __forceinline__ const char* stage_records(const StageHeader* h) {
+    return dyn_smem() + sizeof(StageHeader) + static_cast<size_t>(h->pbm_n) * 4u;
+}
+
+// PBM entry h of the input message list: from the staged slice when inside it.
+__device__ __forceinline__ uint32_t pbm_at(const LaunchParams& P, uint32_t h) {
+    if (P.stage_bytes) {
+        const StageHeader* s = stage_hdr();
+        const uint32_t r = h - s->pbm_lo;
+        if (r < s->pbm_n) return stage_pbm()[r];
+    }
+    return __ldg(P.in_pbm + h);
+}
+
+// Read of a variable of message `index` of the input list: staged copy when
+// the message is inside the block's window, else the sorted records in HBM.
+template <typename T>
+__device__ __forceinline__ T read_msg(const LaunchParams& P, uint32_t hash, uint32_t index, uint32_t elem) {
+    const T* a = var_addr<T>(P, &P.T->msg_in, hash, index, elem);
+    if (!a) return T{};
+    if (P.stage_bytes) {
+        const StageHeader* s = stage_hdr();
+        const uint32_t r = index - s->rec_lo;
+        if (r < s->rec_n) {
+            const size_t row = static_cast<size_t>(index) * P.in_record_bytes;
+            const size_t off = static_cast<size_t>(reinterpret_cast<const char*>(a) - P.in_records) - row;
+            return *reinterpret_cast<const T*>(stage_records(s) + static_cast<size_t>(r) * P.in_record_bytes + off);
+        }
+    }
+    return ldg_any(a);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Bounded wait on the staging mbarrier; false if it gave up.
+__device__ __forceinline__ bool stage_wait(StageHeader* h, uint32_t phase) {
+    const uint32_t mb = smem_addr(&h->mbar);
+    for (uint32_t it = 0; it < (1u << 20); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mb), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Stage the window of sorted messages every agent of this block can see:
+// the bins between (lowest agent bin - one z/y/x slab) and (highest + one),
+// a contiguous range of the sorted records, copied with TMA bulk copies
+// (cp.async.bulk) completing on an mbarrier. All threads of the block call it.
+template <int DIMS>
+__device__ void stage_window(const LaunchParams& P, uint32_t idx, uint32_t n, bool first) {
+    __shared__ uint32_t s_min, s_max;
+    StageHeader* h = stage_hdr();
+    if (threadIdx.x == 0) {
+        s_min = 0xFFFFFFFFu;
+        s_max = 0u;
+        if (first) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&h->mbar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            h->phase = 0;
+        }
+    }
+    uint32_t key = 0xFFFFFFFFu, kmax = 0u;
+    if (idx < n) {
+        const fg_spatial_grid& g = P.in_grid;
+        const float x = read_rw<float>(P, &P.T->agent, VarName("x").hash, idx);
+        const float y = read_rw<float>(P, &P.T->agent, VarName("y").hash, idx);
+        const float z = DIMS == 3 ? read_rw<float>(P, &P.T->agent, VarName("z").hash, idx) : 0.0f;
+        const int cx = clamp_cell(static_cast<int>(floorf((x - g.min[0]) / g.radius)), g.gridDim[0]);
+        const int cy = clamp_cell(static_cast<int>(floorf((y - g.min[1]) / g.radius)), g.gridDim[1]);
+        const int cz = DIMS == 3 ? clamp_cell(static_cast<int>(floorf((z - g.min[2]) / g.radius)), g.gridDim[2]) : 0;
+        key = static_cast<uint32_t>(cz) * g.gridDim[0] * g.gridDim[1] + static_cast<uint32_t>(cy) * g.gridDim[0] +
+              static_cast<uint32_t>(cx);
+        kmax = key;
+    }
+    key = __reduce_min_sync(0xFFFFFFFFu, key);
+    kmax = __reduce_max_sync(0xFFFFFFFFu, kmax);
+    __syncthreads();  // everyone is done with the previous window; s_min/s_max initialised
+    if ((threadIdx.x & 31u) == 0) {
+        atomicMin(&s_min, key);
+        atomicMax(&s_max, kmax);
+    }
+    __syncthreads();
+    uint32_t tx = 0;
+    if (threadIdx.x == 0) {
+        h->rec_n = 0;
+        h->pbm_n = 0;
+        h->rec_lo = 0;
+        h->pbm_lo = 0;
+        if (s_min != 0xFFFFFFFFu) {
+            const fg_spatial_grid& g = P.in_grid;
+            const uint32_t B = g.binCount;
+            const uint32_t span = DIMS == 3 ? g.gridDim[0] * g.gridDim[1] + g.gridDim[0] + 1u : g.gridDim[0] + 1u;
+            const uint32_t hlo = s_min > span ? s_min - span : 0u;
+            const uint32_t hhi = (s_max + span < B) ? s_max + span : B - 1u;
+            const uint32_t plo = hlo & ~3u;
+            uint32_t pend = (hhi + 2u + 3u) & ~3u;
+            if (pend > P.in_pbm_alloc) pend = P.in_pbm_alloc;
+            const uint32_t pn = pend - plo;
+            const uint32_t rlo = __ldg(P.in_pbm + hlo), rhi = __ldg(P.in_pbm + hhi + 1u);
+            const size_t pbytes = static_cast<size_t>(pn) * 4u;
+            const size_t rbytes = static_cast<size_t>(rhi - rlo) * P.in_record_bytes;
+            if (pbytes + rbytes <= P.stage_bytes && pn > 0) {
+                h->pbm_lo = plo;
+                h->pbm_n = pn;
+                h->rec_lo = rlo;
+                h->rec_n = rhi - rlo;
+                tx = static_cast<uint32_t>(pbytes + rbytes);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const uint32_t mb = smem_addr(&h->mbar);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(tx) : "memory");
+                // PBM slice, then the records, in chunks of at most 32 KiB
+                auto copy = [&](char* dst, const char* src, size_t bytes) {
+                    while (bytes) {
+                        const uint32_t c = bytes > 32768 ? 32768u : static_cast<uint32_t>(bytes);
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                smem_addr(dst)),
+                            "l"(src), "r"(c), "r"(mb)
+                            : "memory");
+                        dst += c;
+                        src += c;
+                        bytes -= c;
+                    }
+                };
+                char* base = dyn_smem() + sizeof(StageHeader);
+                copy(base, reinterpret_cast<const char*>(P.in_pbm + plo), pbytes);
+                if (rbytes) copy(base + pbytes, P.in_records + static_cast<size_t>(rlo) * P.in_record_bytes, rbytes);
+            }
+        }
+        h->pad[0] = tx;
+    }
+    __syncthreads();
+    if (h->pad[0]) {
+        const uint32_t phase = h->phase;
+        // a copy that has not landed after the bounded wait is waited for once
+        // more (bounded), then the window is dropped: reads fall back to HBM
+        bool ok = stage_wait(h, phase);
+        if (!ok) ok = stage_wait(h, phase);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            h->phase = phase ^ 1u;
+            if (!ok) {
+                device_error(P, kDevStageTimeout, 0, idx);
+                h->rec_n = 0;
+                h->pbm_n = 0;
+            }
+        }
+    }
+    __syncthreads();
+}
 #endif  // __CUDACC__
 
 }  // namespace detail
@@ -163,11 +352,11 @@ class MessageView {
     __device__ MessageView(const detail::LaunchParams& p, uint32_t i) : P(p), index(i) {}
     template <typename T>
     __device__ T getVariable(detail::VarName name) const {
-        return detail::read_ro<T>(P, &P.T->msg_in, name.hash, index);
+        return detail::read_msg<T>(P, name.hash, index, 0);
     }
     template <typename T, flamegpu::size_type N>
     __device__ T getVariable(detail::VarName name, unsigned int i) const {
-        return detail::read_ro<T>(P, &P.T->msg_in, name.hash, index, i);
+        return detail::read_msg<T>(P, name.hash, index, i);
     }
     __device__ uint32_t getIndex() const { return index; }
 
@@ -218,26 +407,6 @@ class MessageBruteForce {
     };
 };
 
-namespace detail {
-__device__ __forceinline__ int clamp_cell(int v, uint32_t dim) {
-    const int d = static_cast<int>(dim);
-    return v < 0 ? 0 : (v >= d ? d - 1 : v);
-}
-// getGridPosition3D / getGridPosition2D (MessageSpatial3DDevice.cuh:646-659)
-__device__ __forceinline__ int grid_cell(const fg_spatial_grid& g, int axis, float p) {
-    return clamp_cell(static_cast<int>(floorf((p - g.min[axis]) / g.radius)), g.gridDim[axis]);
-}
-// getHash3D / getHash2D (MessageSpatial3DDevice.cuh:660-672): x clamped
-__device__ __forceinline__ uint32_t grid_hash(const fg_spatial_grid& g, int x, int y, int z) {
-    const uint32_t ux = static_cast<uint32_t>(clamp_cell(x, g.gridDim[0]));
-    return static_cast<uint32_t>(z) * g.gridDim[0] * g.gridDim[1] + static_cast<uint32_t>(y) * g.gridDim[0] + ux;
-}
-__device__ __forceinline__ float virtual_coord(float p1, float p2, float width) {
-    // getVirtualX (MessageSpatial3DDevice.cuh:373-397)
-    const float d = p2 - p1;
-    return fabsf(d) > width / 2.0f ? p2 - (d / fabsf(d) * width) : p2;
-}
-}  // namespace detail
 
 /**
  * Spatially partitioned messages; the iterators visit the reference's
@@ -247,6 +416,10 @@ __device__ __forceinline__ float virtual_coord(float p1, float p2, float width) 
  * WrapFilter: 3^DIMS single bins, x outer, y, z inner, every axis taken
  * modulo gridDim (:727-749); no radius test — user code filters.
  */
+__device__ __forceinline__ uint32_t pick(int r, uint32_t a, uint32_t b, uint32_t c) {
+    return r == 0 ? a : (r == 1 ? b : c);
+}
+
 template <int DIMS>
 class SpatialIn {
  public:
@@ -288,7 +461,7 @@ class SpatialIn {
                     if (DIMS == 3 && (az < 0 || az >= static_cast<int>(F.P.in_grid.gridDim[2]))) continue;
                     const uint32_t h0 = detail::grid_hash(F.P.in_grid, F.cell[0] - 1, ay, az);
                     const uint32_t h1 = detail::grid_hash(F.P.in_grid, F.cell[0] + 1, ay, az);
-                    const uint32_t b = __ldg(F.P.in_pbm + h0), e = __ldg(F.P.in_pbm + h1 + 1);
+                    const uint32_t b = detail::pbm_at(F.P, h0), e = detail::pbm_at(F.P, h1 + 1);
                     if (b < e) {
                         m.index = b;
                         end_ = e;
@@ -358,23 +531,15 @@ class SpatialIn {
 
          private:
             __device__ void advance() {
-                const fg_spatial_grid& g = F.P.in_grid;
                 while (++c < kCells) {
-                    int rx, ry, rz;
+                    uint32_t h;
                     if (DIMS == 3) {
-                        rx = c / 9 - 1;
-                        ry = (c / 3) % 3 - 1;
-                        rz = c % 3 - 1;
+                        h = pick(c / 9, F.hz0, F.hz1, F.hz2) + pick((c / 3) % 3, F.hy0, F.hy1, F.hy2) +
+                            pick(c % 3, F.hx0, F.hx1, F.hx2);
                     } else {
-                        rx = c / 3 - 1;
-                        ry = c % 3 - 1;
-                        rz = 0;
+                        h = pick(c % 3, F.hy0, F.hy1, F.hy2) + pick(c / 3, F.hx0, F.hx1, F.hx2);
                     }
-                    const int ax = static_cast<int>(static_cast<uint32_t>(F.cell[0] + rx + static_cast<int>(g.gridDim[0])) % g.gridDim[0]);
-                    const int ay = static_cast<int>(static_cast<uint32_t>(F.cell[1] + ry + static_cast<int>(g.gridDim[1])) % g.gridDim[1]);
-                    const int az = DIMS == 3 ? static_cast<int>(static_cast<uint32_t>(F.cell[2] + rz + static_cast<int>(g.gridDim[2])) % g.gridDim[2]) : 0;
-                    const uint32_t h = detail::grid_hash(g, ax, ay, az);
-                    const uint32_t b = __ldg(F.P.in_pbm + h), e = __ldg(F.P.in_pbm + h + 1);
+                    const uint32_t b = detail::pbm_at(F.P, h), e = detail::pbm_at(F.P, h + 1);
                     if (b < e) {
                         m.index = b;
                         end_ = e;
@@ -394,6 +559,26 @@ class SpatialIn {
             cell[0] = detail::grid_cell(p.in_grid, 0, x);
             cell[1] = detail::grid_cell(p.in_grid, 1, y);
             cell[2] = DIMS == 3 ? detail::grid_cell(p.in_grid, 2, z) : 0;
+            // wrapped coordinates of the offsets -1, 0, +1 on each axis (modulo gridDim,
+            // MessageSpatial3DDevice.cuh:736-738), pre-multiplied into hash terms.
+            const fg_spatial_grid& g = p.in_grid;
+            auto wrapc = [](int c, int r, uint32_t d) {
+                return static_cast<uint32_t>(c + r + static_cast<int>(d)) % d;
+            };
+            hx0 = wrapc(cell[0], -1, g.gridDim[0]);
+            hx1 = wrapc(cell[0], 0, g.gridDim[0]);
+            hx2 = wrapc(cell[0], 1, g.gridDim[0]);
+            hy0 = wrapc(cell[1], -1, g.gridDim[1]) * g.gridDim[0];
+            hy1 = wrapc(cell[1], 0, g.gridDim[1]) * g.gridDim[0];
+            hy2 = wrapc(cell[1], 1, g.gridDim[1]) * g.gridDim[0];
+            if (DIMS == 3) {
+                const uint32_t s2 = g.gridDim[0] * g.gridDim[1];
+                hz0 = wrapc(cell[2], -1, g.gridDim[2]) * s2;
+                hz1 = wrapc(cell[2], 0, g.gridDim[2]) * s2;
+                hz2 = wrapc(cell[2], 1, g.gridDim[2]) * s2;
+            } else {
+                hz0 = hz1 = hz2 = 0;
+            }
         }
         __device__ iterator begin() const { return iterator(*this, 0); }
         __device__ iterator end() const { return iterator(*this, kCells); }
@@ -401,6 +586,7 @@ class SpatialIn {
         const detail::LaunchParams& P;
         float loc[3];
         int cell[3];
+        uint32_t hx0, hx1, hx2, hy0, hy1, hy2, hz0, hz1, hz2;
     };
 
     __device__ explicit SpatialIn(const detail::LaunchParams& p) : P(p) {}

@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "flamegpu/model/ModelDescription.h"
@@ -80,6 +81,8 @@ class CUDASimulation {
         bool inLayerConcurrency = true;
         bool use_graphs = true;       // capture each step into a CUDA graph and replay it
         bool check_each_step = false; // synchronise and check device errors after every step()
+        bool profile_ops = false;     // issue steps eagerly and time every operation with CUDA events
+        unsigned int message_stage_bytes = 96u * 1024u;  // shared memory per block for spatial neighbour windows (0: off)
     };
 
     explicit CUDASimulation(const ModelDescription& model, int argc = 0, const char** argv = nullptr);
@@ -131,6 +134,9 @@ class CUDASimulation {
     unsigned long long getGraphLaunches() const;
     /** Kernel launches issued by the last step (counted at capture / issue). */
     unsigned int getKernelsPerStep() const;
+    /** Per-operation device time since the last call ("fn:<name>", "build:<message>",
+     *  "sort:<agent>", "compact:<agent>" -> total ms, count); needs CUDAConfig().profile_ops. */
+    std::vector<std::tuple<std::string, double, unsigned long long>> takeOperationProfile();
 
     detail::SimulationImpl* getImpl() const { return impl.get(); }
 

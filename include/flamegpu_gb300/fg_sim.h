@@ -47,6 +47,10 @@ int fgs_set_population_device(fgs_sim* sim, const char* agent, const char* state
 int fgs_get_count(fgs_sim* sim, const char* agent, const char* state, uint32_t* n);
 /* getPopulationData for one variable: copies count * sizeof(variable) bytes. */
 int fgs_get_variable(fgs_sim* sim, const char* agent, const char* state, const char* var, void* out, size_t bytes);
+/* getPopulationData for several variables at once: out[k] receives *n *
+ * sizeof(variable k) bytes (caller buffers of at least cap agents). */
+int fgs_get_population(fgs_sim* sim, const char* agent, const char* state, int32_t nvars, const char* const* names,
+                       void* const* out, uint32_t cap, uint32_t* n);
 /* Copy one variable's current device column into a device buffer (no host hop). */
 int fgs_get_variable_device(fgs_sim* sim, const char* agent, const char* state, const char* var, void* dst,
                             size_t bytes);
@@ -58,6 +62,11 @@ int fgs_set_environment(fgs_sim* sim, const char* name, const void* value, size_
 int fgs_get_environment(fgs_sim* sim, const char* name, void* value, size_t bytes);
 int fgs_stream(fgs_sim* sim, void** stream);
 int fgs_stats(fgs_sim* sim, uint64_t* graph_launches, uint32_t* kernels_per_step, uint32_t* step_counter);
+/* Enable/disable per-operation CUDA-event timing (steps then run eagerly, not as graphs). */
+int fgs_profile_ops(fgs_sim* sim, int32_t enable);
+/* Per-operation totals since the last call as "label,total_ms,count;..." (see
+ * CUDASimulation::takeOperationProfile). */
+int fgs_take_profile(fgs_sim* sim, char* buf, size_t len);
 /* getElapsedTimeSteps (seconds) for up to cap steps; returns the count in *n. */
 int fgs_step_times(fgs_sim* sim, double* out, uint32_t cap, uint32_t* n);
 
