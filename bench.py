@@ -163,6 +163,8 @@ def run_boids_small(args, world, rank, local):
     torch.cuda.set_device(dev)
     pop = synth.boids_population(n, cfg["min_pos"], cfg["max_pos"], cfg["seed"] + rank)
     s = sim.Simulation("boids_spatial3d", synth.boids_params(cfg), device=local, steps=steps_per)
+    if args.stage_bytes is not None:
+        s.set_stage_bytes(args.stage_bytes)
     s.set_population("Boid", n, pop)
     stream = torch.cuda.ExternalStream(s.stream, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -315,6 +317,8 @@ def main():
                     choices=["boids_small", "birth_death", "spatial3d_large", "spatial2d_large"])
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stage-bytes", type=int, default=None,
+                    help="shared memory per block for spatial neighbour staging (0 disables)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -6,6 +6,12 @@
 // (SEED, agent id, step, stream) — SplitMix64's finaliser (Steele, Lea &
 // Flood 2014) — so the same model gives the same decisions on any build.
 // Registered as "birth_death"; parameters: p_death, p_birth, seed.
+// Benchmark model: built with seatbelts off, as the reference builds its
+// benchmarks (FLAMEGPU_SEATBELTS=OFF, src/CMakeLists.txt:78). The test models
+// keep the device checks on.
+#ifndef FLAMEGPU_SEATBELTS
+#define FLAMEGPU_SEATBELTS 0
+#endif
 #include "flamegpu/flamegpu.h"
 #include "flamegpu_gb300/fg_sim.h"
 

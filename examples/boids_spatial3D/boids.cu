@@ -9,6 +9,12 @@
 //   global_scale, steer_scale, collision_scale, match_scale, wrap (0/1), sort_period
 #include <cmath>
 
+// Benchmark model: built with seatbelts off, as the reference builds its
+// benchmarks (FLAMEGPU_SEATBELTS=OFF, src/CMakeLists.txt:78). The test models
+// keep the device checks on.
+#ifndef FLAMEGPU_SEATBELTS
+#define FLAMEGPU_SEATBELTS 0
+#endif
 #include "flamegpu/flamegpu.h"
 #include "flamegpu_gb300/fg_sim.h"
 

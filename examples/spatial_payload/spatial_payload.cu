@@ -1,0 +1,116 @@
+// Large spatial messaging workload, written against the FLAME GPU 2 API.
+// Agents hold a position and 4 float payload variables p0..p3. Each step they
+// output a spatial message (position + payload) and then mix their payload
+// with the mean payload of the messages within the interaction radius:
+//   p_k <- 0.5 * p_k + 0.5 * mean_{|m - a| < r} m.p_k
+// Positions do not change, so every step does the same build + iterate work.
+// Registered as "spatial_payload"; parameters: dims (2|3), min, max, radius.
+#ifndef FLAMEGPU_SEATBELTS
+#define FLAMEGPU_SEATBELTS 0  // benchmark model: device checks off, as in the reference's benchmark builds
+#endif
+#include "flamegpu/flamegpu.h"
+#include "flamegpu_gb300/fg_sim.h"
+
+FLAMEGPU_AGENT_FUNCTION(payload_out3, flamegpu::MessageNone, flamegpu::MessageSpatial3D) {
+    FLAMEGPU->message_out.setLocation(FLAMEGPU->getVariable<float>("x"), FLAMEGPU->getVariable<float>("y"),
+                                      FLAMEGPU->getVariable<float>("z"));
+    FLAMEGPU->message_out.setVariable<float>("p0", FLAMEGPU->getVariable<float>("p0"));
+    FLAMEGPU->message_out.setVariable<float>("p1", FLAMEGPU->getVariable<float>("p1"));
+    FLAMEGPU->message_out.setVariable<float>("p2", FLAMEGPU->getVariable<float>("p2"));
+    FLAMEGPU->message_out.setVariable<float>("p3", FLAMEGPU->getVariable<float>("p3"));
+    return flamegpu::ALIVE;
+}
+FLAMEGPU_AGENT_FUNCTION(payload_out2, flamegpu::MessageNone, flamegpu::MessageSpatial2D) {
+    FLAMEGPU->message_out.setLocation(FLAMEGPU->getVariable<float>("x"), FLAMEGPU->getVariable<float>("y"));
+    FLAMEGPU->message_out.setVariable<float>("p0", FLAMEGPU->getVariable<float>("p0"));
+    FLAMEGPU->message_out.setVariable<float>("p1", FLAMEGPU->getVariable<float>("p1"));
+    FLAMEGPU->message_out.setVariable<float>("p2", FLAMEGPU->getVariable<float>("p2"));
+    FLAMEGPU->message_out.setVariable<float>("p3", FLAMEGPU->getVariable<float>("p3"));
+    return flamegpu::ALIVE;
+}
+
+template <int DIMS, typename API>
+__device__ __forceinline__ flamegpu::AGENT_STATUS payload_mix(API* FLAMEGPU) {
+    const float x = FLAMEGPU->template getVariable<float>("x");
+    const float y = FLAMEGPU->template getVariable<float>("y");
+    const float z = DIMS == 3 ? FLAMEGPU->template getVariable<float>("z") : 0.0f;
+    const float r = FLAMEGPU->message_in.radius();
+    const float r2 = r * r;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    unsigned int c = 0;
+    auto visit = [&](const auto& m) {
+        const float dx = m.template getVariable<float>("x") - x;
+        const float dy = m.template getVariable<float>("y") - y;
+        const float dz = DIMS == 3 ? m.template getVariable<float>("z") - z : 0.0f;
+        if (dx * dx + dy * dy + dz * dz < r2) {
+            s0 += m.template getVariable<float>("p0");
+            s1 += m.template getVariable<float>("p1");
+            s2 += m.template getVariable<float>("p2");
+            s3 += m.template getVariable<float>("p3");
+            ++c;
+        }
+    };
+    if constexpr (DIMS == 3) {
+        for (const auto& m : FLAMEGPU->message_in(x, y, z)) visit(m);
+    } else {
+        for (const auto& m : FLAMEGPU->message_in(x, y)) visit(m);
+    }
+    if (c) {
+        const float inv = 1.0f / static_cast<float>(c);
+        FLAMEGPU->template setVariable<float>("p0", 0.5f * FLAMEGPU->template getVariable<float>("p0") + 0.5f * s0 * inv);
+        FLAMEGPU->template setVariable<float>("p1", 0.5f * FLAMEGPU->template getVariable<float>("p1") + 0.5f * s1 * inv);
+        FLAMEGPU->template setVariable<float>("p2", 0.5f * FLAMEGPU->template getVariable<float>("p2") + 0.5f * s2 * inv);
+        FLAMEGPU->template setVariable<float>("p3", 0.5f * FLAMEGPU->template getVariable<float>("p3") + 0.5f * s3 * inv);
+    }
+    return flamegpu::ALIVE;
+}
+
+FLAMEGPU_AGENT_FUNCTION(payload_in3, flamegpu::MessageSpatial3D, flamegpu::MessageNone) {
+    return payload_mix<3>(FLAMEGPU);
+}
+FLAMEGPU_AGENT_FUNCTION(payload_in2, flamegpu::MessageSpatial2D, flamegpu::MessageNone) {
+    return payload_mix<2>(FLAMEGPU);
+}
+
+namespace {
+void* make_spatial_payload(const double* p, int32_t np) {
+    auto P = [&](int i, double d) { return i < np ? p[i] : d; };
+    const int dims = static_cast<int>(P(0, 3));
+    const float mn = static_cast<float>(P(1, 0.0)), mx = static_cast<float>(P(2, 256.0)), r = static_cast<float>(P(3, 1.0));
+    auto* model = new flamegpu::ModelDescription("SpatialPayload");
+    flamegpu::AgentDescription a = model->newAgent("agent");
+    a.newVariable<float>("x");
+    a.newVariable<float>("y");
+    if (dims == 3) a.newVariable<float>("z");
+    for (const char* n : {"p0", "p1", "p2", "p3"}) a.newVariable<float>(n);
+    if (dims == 3) {
+        auto m = model->newMessage<flamegpu::MessageSpatial3D>("location");
+        m.setMin(mn, mn, mn);
+        m.setMax(mx, mx, mx);
+        m.setRadius(r);
+        for (const char* n : {"p0", "p1", "p2", "p3"}) m.newVariable<float>(n);
+        auto fo = a.newFunction("out", payload_out3);
+        fo.setMessageOutput("location");
+        auto fi = a.newFunction("in", payload_in3);
+        fi.setMessageInput("location");
+        model->newLayer().addAgentFunction(fo);
+        model->newLayer().addAgentFunction(fi);
+    } else {
+        auto m = model->newMessage<flamegpu::MessageSpatial2D>("location");
+        m.setMin(mn, mn);
+        m.setMax(mx, mx);
+        m.setRadius(r);
+        for (const char* n : {"p0", "p1", "p2", "p3"}) m.newVariable<float>(n);
+        auto fo = a.newFunction("out", payload_out2);
+        fo.setMessageOutput("location");
+        auto fi = a.newFunction("in", payload_in2);
+        fi.setMessageInput("location");
+        model->newLayer().addAgentFunction(fo);
+        model->newLayer().addAgentFunction(fi);
+    }
+    return model;
+}
+struct Register {
+    Register() { fgs_register_model("spatial_payload", &make_spatial_payload); }
+} reg;
+}  // namespace

@@ -5,6 +5,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "flamegpu/flamegpu.h"
 #include "flamegpu_gb300/fg_sim.h"
@@ -135,6 +136,15 @@ extern "C" int fgs_set_population_device(fgs_sim* s, const char* agent, const ch
     });
 }
 
+extern "C" int fgs_reset_population_device(fgs_sim* s, const char* agent, const char* state, uint32_t n, int32_t nvars,
+                                           const char* const* names, const void* const* dcols, uint32_t next_id) {
+    return guarded([&] {
+        std::vector<std::pair<std::string, const void*>> cols;
+        for (int32_t k = 0; k < nvars; ++k) cols.emplace_back(names[k], dcols[k]);
+        s->sim->setPopulationDevice(agent, state, n, cols, next_id);
+    });
+}
+
 extern "C" int fgs_get_count(fgs_sim* s, const char* agent, const char* state, uint32_t* n) {
     return guarded([&] { *n = s->sim->getAgentCount(agent, state); });
 }
@@ -248,5 +258,12 @@ extern "C" int fgs_take_profile(fgs_sim* s, char* buf, size_t len) {
             std::strncpy(buf, out.c_str(), len - 1);
             buf[len - 1] = 0;
         }
+    });
+}
+
+extern "C" int fgs_set_stage_bytes(fgs_sim* s, uint32_t bytes) {
+    return guarded([&] {
+        s->sim->CUDAConfig().message_stage_bytes = bytes;
+        s->sim->applyConfig();
     });
 }

@@ -139,7 +139,7 @@ struct FnRt {
     uint32_t* birth_flags = nullptr;
     std::vector<void*> birth_cols;
     void* birth_defaults = nullptr;
-    FunctionTables* d_tables[2] = {nullptr, nullptr};
+    std::unique_ptr<FunctionTables> tables[2];  // per buffer parity of the agent list
     bool sort_trigger = false;
     bool stage = false;  // spatial input and the agent has float x, y (, z): stage neighbour windows
 };
@@ -151,6 +151,8 @@ struct SimulationImpl {
     int device = 0;
     int sms = 132;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;        // second branch of a layer (build next to sort)
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     DevMem mem;
     std::vector<std::unique_ptr<AgentList>> lists;
     std::vector<std::unique_ptr<MsgList>> msgs;
@@ -189,6 +191,9 @@ struct SimulationImpl {
             cudaEventDestroy(e.second);
         }
         if (h_pinned) cudaFreeHost(h_pinned);
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -220,6 +225,9 @@ struct SimulationImpl {
         device = cuda_config.device_id;
         sms = sm_count(device);
         FG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        FG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        FG_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+        FG_CUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
         FG_CUDA(cudaMallocHost(&h_pinned, 4096));
         std::memset(h_pinned, 0, 4096);
         d_misc = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (8 + model->agents.size() + 8)));
@@ -526,9 +534,7 @@ struct SimulationImpl {
                 e.push_back({fnv1a32(p.name), d_env + env_offset[i], 0, p.type_size, p.elements});
             }
             T->env = make_table(e, "environment");
-            if (!f.d_tables[par]) f.d_tables[par] = static_cast<FunctionTables*>(mem.alloc(sizeof(FunctionTables)));
-            FG_CUDA(cudaMemcpy(f.d_tables[par], T, sizeof(FunctionTables), cudaMemcpyHostToDevice));
-            delete T;
+            f.tables[par].reset(T);
         }
     }
 
@@ -646,7 +652,7 @@ struct SimulationImpl {
         kernel_counter += 6;
     }
 
-    void enqueue_build(MsgList& m) {
+    void enqueue_build(MsgList& m, cudaStream_t st) {
         fg_record_desc rec;
         std::memset(&rec, 0, sizeof(rec));
         rec.words = m.record_words;
@@ -664,21 +670,35 @@ struct SimulationImpl {
         FG_CAPI(fg_spatial_build(&m.grid, m.capacity, m.d_count, static_cast<const float*>(m.cols[xi]),
                                  static_cast<const float*>(m.cols[yi]), dims == 3 ? static_cast<const float*>(m.cols[zi]) : nullptr,
                                  m.optional_any ? m.valid : nullptr, &rec, m.records, m.pbm, m.build_ws, m.build_ws_bytes,
-                                 stream));
+                                 st));
         m.needs_build = false;
         kernel_counter += 5;
     }
 
     void enqueue_function(FnRt& f) {
         AgentList& l = *f.list;
+        bool do_sort = false;
         if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0)
-            timed("sort:" + l.agent->name, [&] { enqueue_sort(f); });
-        if (f.in && f.in->spatial() && f.in->needs_build) timed("build:" + f.in->msg->name, [&] { enqueue_build(*f.in); });
+            do_sort = true;
+        const bool do_build = f.in && f.in->spatial() && f.in->needs_build;
+        if (do_sort && do_build && cuda_config.inLayerConcurrency && !profiling) {
+            // the agent sort and the message index build touch disjoint buffers:
+            // two branches of the step graph (fork/join through events)
+            FG_CUDA(cudaEventRecord(fork_ev, stream));
+            FG_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
+            enqueue_build(*f.in, side);
+            enqueue_sort(f);
+            FG_CUDA(cudaEventRecord(join_ev, side));
+            FG_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
+        } else {
+            if (do_sort) timed("sort:" + l.agent->name, [&] { enqueue_sort(f); });
+            if (do_build) timed("build:" + f.in->msg->name, [&] { enqueue_build(*f.in, stream); });
+        }
         if (f.out && f.out->optional_any && !f.fn->message_output_optional)
             FG_CUDA(cudaMemsetAsync(f.out->valid, 1, sizeof(uint32_t) * f.out->capacity, stream));
         LaunchParams P;
         std::memset(&P, 0, sizeof(P));
-        P.T = f.d_tables[l.parity];
+        P.T = *f.tables[l.parity];
         P.max_n = l.capacity;
         P.d_n = l.d_count;
         if (f.out) {
@@ -1088,6 +1108,30 @@ void* CUDASimulation::getDeviceVariable(const std::string& agent, const std::str
     if (v < 0) THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), variable.c_str()));
     impl->ensure_all_allocated();
     return l->cols[v][l->parity];
+}
+
+void CUDASimulation::setPopulationDevice(const std::string& agent, const std::string& state, unsigned int n,
+                                         const std::vector<std::pair<std::string, const void*>>& columns,
+                                         id_t next_id) {
+    detail::AgentList* l = impl->list_of(agent, state);
+    if (columns.size() != l->cols.size())
+        THROW exception::InvalidArgument(format("setPopulationDevice needs all %zu variables of agent '%s'", l->cols.size(), agent.c_str()));
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    if (n > l->capacity) impl->ensure_capacity(*l, n, 0);
+    impl->ensure_all_allocated();
+    for (const auto& c : columns) {
+        const int v = l->var_index(c.first);
+        if (v < 0) THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), c.first.c_str()));
+        const size_t b = l->agent->variables[v].bytes();
+        if (n) FG_CUDA(cudaMemcpyAsync(l->cols[v][l->parity], c.second, b * n, cudaMemcpyDeviceToDevice, impl->stream));
+    }
+    impl->h_pinned[0] = n;
+    impl->h_pinned[1] = next_id;
+    FG_CUDA(cudaMemcpyAsync(l->d_count, impl->h_pinned, sizeof(uint32_t), cudaMemcpyHostToDevice, impl->stream));
+    FG_CUDA(cudaMemcpyAsync(impl->d_next_id(impl->agent_index(l->agent)), impl->h_pinned + 1, sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, impl->stream));
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    l->bound = n;
 }
 
 const unsigned int* CUDASimulation::getDeviceCount(const std::string& agent, const std::string& state) {

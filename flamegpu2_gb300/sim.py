@@ -21,6 +21,7 @@ SIM_EXPORTS = [
     "fgs_set_population", "fgs_set_population_device", "fgs_get_count", "fgs_get_variable", "fgs_get_population",
     "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
     "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
+    "fgs_set_stage_bytes", "fgs_reset_population_device",
 ]
 
 _lock = threading.Lock()
@@ -62,6 +63,9 @@ def core():
             L.fgs_stats.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(u32), C.POINTER(u32)]
             L.fgs_step_times.argtypes = [vp, C.POINTER(C.c_double), u32, C.POINTER(u32)]
             L.fgs_profile_ops.argtypes = [vp, i32]
+            L.fgs_set_stage_bytes.argtypes = [vp, u32]
+            L.fgs_reset_population_device.argtypes = [vp, C.c_char_p, C.c_char_p, u32, i32, C.POINTER(C.c_char_p),
+                                                      C.POINTER(vp), u32]
             L.fgs_take_profile.argtypes = [vp, C.c_char_p, sz]
             _core = L
         if _models is None:
@@ -125,6 +129,14 @@ class Simulation:
         cp = (C.c_void_p * max(1, len(names)))(*[columns[k].data_ptr() for k in names])
         _check(core().fgs_set_population_device(self._h, agent.encode(), state.encode(), n, len(names), cn, cp))
 
+    def reset_population_device(self, agent: str, n: int, columns: dict, next_id: int, state: str = "default"):
+        """Replace the population from torch CUDA tensors holding every variable (incl. _id)."""
+        names = list(columns)
+        cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        cp = (C.c_void_p * max(1, len(names)))(*[columns[k].data_ptr() for k in names])
+        _check(core().fgs_reset_population_device(self._h, agent.encode(), state.encode(), n, len(names), cn, cp,
+                                                  next_id))
+
     def count(self, agent: str, state: str = "default") -> int:
         n = C.c_uint32(0)
         _check(core().fgs_get_count(self._h, agent.encode(), state.encode(), C.byref(n)))
@@ -186,6 +198,9 @@ class Simulation:
         n = C.c_uint32()
         _check(core().fgs_step_times(self._h, buf, cap, C.byref(n)))
         return np.array(buf[:n.value])
+
+    def set_stage_bytes(self, nbytes: int):
+        _check(core().fgs_set_stage_bytes(self._h, nbytes))
 
     def profile_ops(self, enable: bool = True):
         _check(core().fgs_profile_ops(self._h, int(enable)))

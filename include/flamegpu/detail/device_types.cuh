@@ -61,7 +61,7 @@ __host__ __device__ inline uint32_t table_slot(uint32_t mult, uint32_t shift, ui
     return (hash * mult) >> shift;
 }
 
-/** Read-only tables of one agent function launch (device memory). */
+/** Read-only tables of one agent function launch (kernel parameters). */
 struct FunctionTables {
     VarTable agent;      // the agent's own variables (SoA columns)
     VarTable msg_out;    // output message list (unsorted SoA columns)
@@ -101,9 +101,11 @@ enum DeviceErrorCode : uint32_t {
     kDevStageTimeout = 11,
 };
 
-/** Kernel parameters of one agent function launch (passed __grid_constant__). */
+/** Kernel parameters of one agent function launch (passed __grid_constant__).
+ * The lookup tables travel in the parameter space: table reads are
+ * constant-bank loads the compiler hoists and shares between accesses. */
 struct LaunchParams {
-    const FunctionTables* T;
+    FunctionTables T;
     uint32_t max_n;              // capacity of the agent list (grid sizing bound)
     const uint32_t* d_n;         // agents in the list (device)
     // message output

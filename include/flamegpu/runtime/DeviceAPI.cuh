@@ -44,20 +44,21 @@ __device__ __forceinline__ void device_error(const LaunchParams& P, uint32_t cod
 template <typename T>
 __device__ __forceinline__ T* var_addr(const LaunchParams& P, const VarTable* __restrict__ t, uint32_t hash,
                                        uint32_t row, uint32_t elem) {
-    const uint32_t s = table_slot(__ldg(&t->mult), __ldg(&t->shift), hash);
+    // t points into the kernel's parameter space: plain loads, constant bank
+    const uint32_t s = table_slot(t->mult, t->shift, hash);
     const VarSlot* vs = &t->slot[s];
-    char* base = reinterpret_cast<char*>(__ldg(reinterpret_cast<const unsigned long long*>(&vs->ptr)));
-    const uint32_t stride = __ldg(&vs->stride);
+    char* base = vs->ptr;
+    const uint32_t stride = vs->stride;
 #if FLAMEGPU_SEATBELTS
-    if (__ldg(&vs->hash) != hash || base == nullptr) {
+    if (vs->hash != hash || base == nullptr) {
         device_error(P, kDevUnknownVariable, hash, row);
         return nullptr;
     }
-    if (__ldg(&vs->elem_bytes) != sizeof(T)) {
+    if (vs->elem_bytes != sizeof(T)) {
         device_error(P, kDevTypeMismatch, hash, row);
         return nullptr;
     }
-    if (elem >= __ldg(&vs->elements)) {
+    if (elem >= vs->elements) {
         device_error(P, kDevArrayIndex, hash, row);
         return nullptr;
     }
@@ -152,7 +153,7 @@ __device__ __forceinline__ uint32_t pbm_at(const LaunchParams& P, uint32_t h) {
 // the message is inside the block's window, else the sorted records in HBM.
 template <typename T>
 __device__ __forceinline__ T read_msg(const LaunchParams& P, uint32_t hash, uint32_t index, uint32_t elem) {
-    const T* a = var_addr<T>(P, &P.T->msg_in, hash, index, elem);
+    const T* a = var_addr<T>(P, &P.T.msg_in, hash, index, elem);
     if (!a) return T{};
     if (P.stage_bytes) {
         const StageHeader* s = stage_hdr();
@@ -164,6 +165,29 @@ __device__ __forceinline__ T read_msg(const LaunchParams& P, uint32_t hash, uint
         }
     }
     return ldg_any(a);
+}
+
+// Byte offset of element `elem` of variable `hash` inside a sorted message
+// record: a per-name constant of the launch (slot pointer minus records base).
+template <typename T>
+__device__ __forceinline__ size_t record_offset(const LaunchParams& P, uint32_t hash, uint32_t elem) {
+    const VarTable* t = &P.T.msg_in;
+    const VarSlot* vs = &t->slot[table_slot(t->mult, t->shift, hash)];
+#if FLAMEGPU_SEATBELTS
+    if (vs->hash != hash || vs->ptr == nullptr) {
+        device_error(P, kDevUnknownVariable, hash, 0);
+        return 0;
+    }
+    if (vs->elem_bytes != sizeof(T)) {
+        device_error(P, kDevTypeMismatch, hash, 0);
+        return 0;
+    }
+    if (elem >= vs->elements) {
+        device_error(P, kDevArrayIndex, hash, 0);
+        return 0;
+    }
+#endif
+    return static_cast<size_t>(vs->ptr - P.in_records) + static_cast<size_t>(elem) * sizeof(T);
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -207,9 +231,9 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, uint32_t n, bo
     uint32_t key = 0xFFFFFFFFu, kmax = 0u;
     if (idx < n) {
         const fg_spatial_grid& g = P.in_grid;
-        const float x = read_rw<float>(P, &P.T->agent, VarName("x").hash, idx);
-        const float y = read_rw<float>(P, &P.T->agent, VarName("y").hash, idx);
-        const float z = DIMS == 3 ? read_rw<float>(P, &P.T->agent, VarName("z").hash, idx) : 0.0f;
+        const float x = read_rw<float>(P, &P.T.agent, VarName("x").hash, idx);
+        const float y = read_rw<float>(P, &P.T.agent, VarName("y").hash, idx);
+        const float z = DIMS == 3 ? read_rw<float>(P, &P.T.agent, VarName("z").hash, idx) : 0.0f;
         const int cx = clamp_cell(static_cast<int>(floorf((x - g.min[0]) / g.radius)), g.gridDim[0]);
         const int cy = clamp_cell(static_cast<int>(floorf((y - g.min[1]) / g.radius)), g.gridDim[1]);
         const int cz = DIMS == 3 ? clamp_cell(static_cast<int>(floorf((z - g.min[2]) / g.radius)), g.gridDim[2]) : 0;
@@ -326,7 +350,7 @@ class MessageOutBase {
             detail::device_error(P, detail::kDevMessageOutNotEnabled, name.hash, index);
             return;
         }
-        detail::write_var<T>(P, &P.T->msg_out, name.hash, index, value);
+        detail::write_var<T>(P, &P.T.msg_out, name.hash, index, value);
         flag = 1;
     }
     template <typename T, flamegpu::size_type N>
@@ -335,7 +359,7 @@ class MessageOutBase {
             detail::device_error(P, detail::kDevMessageOutNotEnabled, name.hash, index);
             return;
         }
-        detail::write_var<T>(P, &P.T->msg_out, name.hash, index, value, i);
+        detail::write_var<T>(P, &P.T.msg_out, name.hash, index, value, i);
         flag = 1;
     }
     __device__ uint32_t written() const { return flag; }
@@ -409,16 +433,72 @@ class MessageBruteForce {
 
 
 /**
+ * A message of a spatial input list: a view of its sorted record. `row` is
+ * the record's address — in the block's shared-memory window when the
+ * message is inside it, else in HBM — computed once per message by the
+ * iterator; a field read is then one load at row + field offset, the offset
+ * being a per-name constant of the launch.
+ */
+class RecordView {
+ public:
+    __device__ RecordView(const detail::LaunchParams& p, uint32_t i) : P(p), index(i), row(nullptr) {}
+    template <typename T>
+    __device__ T getVariable(detail::VarName name) const {
+        return *reinterpret_cast<const T*>(row + detail::record_offset<T>(P, name.hash, 0));
+    }
+    template <typename T, flamegpu::size_type N>
+    __device__ T getVariable(detail::VarName name, unsigned int i) const {
+        return *reinterpret_cast<const T*>(row + detail::record_offset<T>(P, name.hash, i));
+    }
+    __device__ uint32_t getIndex() const { return index; }
+
+ protected:
+    const detail::LaunchParams& P;
+
+ public:
+    uint32_t index;
+    const char* row;
+};
+
+/**
  * Spatially partitioned messages; the iterators visit the reference's
  * Moore neighbourhood in the reference's order. DIMS = 2 or 3.
  * Filter: 3^(DIMS-1) x-strips, y-offset outer, z-offset inner, each strip
  * PBM[hash(x-1)] .. PBM[hash(x+1)+1] with x clamped (MessageSpatial3DDevice.cuh:693-719).
  * WrapFilter: 3^DIMS single bins, x outer, y, z inner, every axis taken
  * modulo gridDim (:727-749); no radius test — user code filters.
+ * A cell lies wholly inside or wholly outside the block's staged window, so
+ * within a cell the record address just advances by one record.
  */
 __device__ __forceinline__ uint32_t pick(int r, uint32_t a, uint32_t b, uint32_t c) {
     return r == 0 ? a : (r == 1 ? b : c);
 }
+
+/** The staged window of the calling block, cached in registers by a filter. */
+struct Window {
+    uint32_t rec_lo = 0, rec_n = 0, pbm_lo = 0, pbm_n = 0;
+    const char* rec = nullptr;
+    const uint32_t* pbm = nullptr;
+    __device__ void load(const detail::LaunchParams& P) {
+        if (!P.stage_bytes) return;
+        const detail::StageHeader* h = detail::stage_hdr();
+        rec_lo = h->rec_lo;
+        rec_n = h->rec_n;
+        pbm_lo = h->pbm_lo;
+        pbm_n = h->pbm_n;
+        pbm = detail::stage_pbm();
+        rec = detail::stage_records(h);
+    }
+    __device__ uint32_t pbm_at(const detail::LaunchParams& P, uint32_t h) const {
+        const uint32_t r = h - pbm_lo;
+        return r < pbm_n ? pbm[r] : __ldg(P.in_pbm + h);
+    }
+    __device__ const char* row(const detail::LaunchParams& P, uint32_t index) const {
+        const uint32_t r = index - rec_lo;
+        return r < rec_n ? rec + static_cast<size_t>(r) * P.in_record_bytes
+                         : P.in_records + static_cast<size_t>(index) * P.in_record_bytes;
+    }
+};
 
 template <int DIMS>
 class SpatialIn {
@@ -428,21 +508,20 @@ class SpatialIn {
 
     class Filter {
      public:
-        class Message : public MessageView {
+        class Message : public RecordView {
          public:
-            __device__ Message(const detail::LaunchParams& p, uint32_t i) : MessageView(p, i) {}
+            __device__ Message(const detail::LaunchParams& p, uint32_t i) : RecordView(p, i) {}
         };
         class iterator {
          public:
             __device__ iterator(const Filter& f, int strip) : F(f), s(strip), m(f.P, 0), end_(0) {
                 if (s < kStrips) {
-                    m.index = 0;
-                    end_ = 0;
                     --s;
                     advance();
                 }
             }
             __device__ iterator& operator++() {
+                m.row += F.P.in_record_bytes;
                 if (++m.index >= end_) advance();
                 return *this;
             }
@@ -461,9 +540,10 @@ class SpatialIn {
                     if (DIMS == 3 && (az < 0 || az >= static_cast<int>(F.P.in_grid.gridDim[2]))) continue;
                     const uint32_t h0 = detail::grid_hash(F.P.in_grid, F.cell[0] - 1, ay, az);
                     const uint32_t h1 = detail::grid_hash(F.P.in_grid, F.cell[0] + 1, ay, az);
-                    const uint32_t b = detail::pbm_at(F.P, h0), e = detail::pbm_at(F.P, h1 + 1);
+                    const uint32_t b = F.win.pbm_at(F.P, h0), e = F.win.pbm_at(F.P, h1 + 1);
                     if (b < e) {
                         m.index = b;
+                        m.row = F.win.row(F.P, b);
                         end_ = e;
                         return;
                     }
@@ -481,6 +561,7 @@ class SpatialIn {
             cell[0] = detail::grid_cell(p.in_grid, 0, x);
             cell[1] = detail::grid_cell(p.in_grid, 1, y);
             cell[2] = DIMS == 3 ? detail::grid_cell(p.in_grid, 2, z) : 0;
+            win.load(p);
         }
         __device__ iterator begin() const { return iterator(*this, 0); }
         __device__ iterator end() const { return iterator(*this, kStrips); }
@@ -488,14 +569,15 @@ class SpatialIn {
         const detail::LaunchParams& P;
         float loc[3];
         int cell[3];
+        Window win;
     };
 
     class WrapFilter {
      public:
-        class Message : public MessageView {
+        class Message : public RecordView {
          public:
             __device__ Message(const detail::LaunchParams& p, uint32_t i, const WrapFilter* f)
-                : MessageView(p, i), F(f) {}
+                : RecordView(p, i), F(f) {}
             __device__ float getVirtualX() const { return getVirtualX(F->loc[0]); }
             __device__ float getVirtualY() const { return getVirtualY(F->loc[1]); }
             __device__ float getVirtualZ() const { return getVirtualZ(F->loc[2]); }
@@ -521,6 +603,7 @@ class SpatialIn {
                 }
             }
             __device__ iterator& operator++() {
+                m.row += F.P.in_record_bytes;
                 if (++m.index >= end_) advance();
                 return *this;
             }
@@ -539,9 +622,10 @@ class SpatialIn {
                     } else {
                         h = pick(c % 3, F.hy0, F.hy1, F.hy2) + pick(c / 3, F.hx0, F.hx1, F.hx2);
                     }
-                    const uint32_t b = detail::pbm_at(F.P, h), e = detail::pbm_at(F.P, h + 1);
+                    const uint32_t b = F.win.pbm_at(F.P, h), e = F.win.pbm_at(F.P, h + 1);
                     if (b < e) {
                         m.index = b;
+                        m.row = F.win.row(F.P, b);
                         end_ = e;
                         return;
                     }
@@ -579,6 +663,7 @@ class SpatialIn {
             } else {
                 hz0 = hz1 = hz2 = 0;
             }
+            win.load(p);
         }
         __device__ iterator begin() const { return iterator(*this, 0); }
         __device__ iterator end() const { return iterator(*this, kCells); }
@@ -587,6 +672,7 @@ class SpatialIn {
         float loc[3];
         int cell[3];
         uint32_t hx0, hx1, hx2, hy0, hy1, hy2, hz0, hz1, hz2;
+        Window win;
     };
 
     __device__ explicit SpatialIn(const detail::LaunchParams& p) : P(p) {}
@@ -665,11 +751,11 @@ class DeviceEnvironment {
     __device__ explicit DeviceEnvironment(const detail::LaunchParams& p) : P(p) {}
     template <typename T>
     __device__ T getProperty(detail::VarName name) const {
-        return detail::read_ro<T>(P, &P.T->env, name.hash, 0);
+        return detail::read_ro<T>(P, &P.T.env, name.hash, 0);
     }
     template <typename T, flamegpu::size_type N>
     __device__ T getProperty(detail::VarName name, unsigned int i) const {
-        return detail::read_ro<T>(P, &P.T->env, name.hash, 0, i);
+        return detail::read_ro<T>(P, &P.T.env, name.hash, 0, i);
     }
 
  private:
@@ -752,12 +838,12 @@ class DeviceAPI {
         template <typename T>
         __device__ void setVariable(detail::VarName name, T value) const {
             if (!start(name)) return;
-            detail::write_var<T>(P, &P.T->birth, name.hash, index, value);
+            detail::write_var<T>(P, &P.T.birth, name.hash, index, value);
         }
         template <typename T, flamegpu::size_type N>
         __device__ void setVariable(detail::VarName name, unsigned int i, T value) const {
             if (!start(name)) return;
-            detail::write_var<T>(P, &P.T->birth, name.hash, index, value, i);
+            detail::write_var<T>(P, &P.T.birth, name.hash, index, value, i);
         }
         /** Ids of new agents are assigned when the step's compaction appends them
          * (next id + birth rank, deterministic), after this function returns. */
@@ -780,15 +866,14 @@ class DeviceAPI {
             }
             if (!is_born) {
                 is_born = 1;
-                const detail::VarTable* def = &P.T->birth_def;
-                const detail::VarTable* dst = &P.T->birth;
+                const detail::VarTable* def = &P.T.birth_def;
+                const detail::VarTable* dst = &P.T.birth;
                 for (int s = 0; s < detail::kMaxVarSlots; ++s) {
-                    const char* d = reinterpret_cast<const char*>(
-                        __ldg(reinterpret_cast<const unsigned long long*>(&def->slot[s].ptr)));
+                    const char* d = def->slot[s].ptr;
                     if (!d) continue;
-                    char* o = reinterpret_cast<char*>(__ldg(reinterpret_cast<const unsigned long long*>(&dst->slot[s].ptr)));
-                    const uint32_t bytes = __ldg(&def->slot[s].stride);
-                    o += static_cast<size_t>(index) * __ldg(&dst->slot[s].stride);
+                    char* o = dst->slot[s].ptr;
+                    const uint32_t bytes = def->slot[s].stride;
+                    o += static_cast<size_t>(index) * dst->slot[s].stride;
                     for (uint32_t b = 0; b < bytes; ++b) o[b] = d[b];
                 }
             }
@@ -804,11 +889,11 @@ class DeviceAPI {
 
     template <typename T>
     __device__ T getVariable(detail::VarName name) const {
-        return detail::read_rw<T>(P, &P.T->agent, name.hash, index);
+        return detail::read_rw<T>(P, &P.T.agent, name.hash, index);
     }
     template <typename T, flamegpu::size_type N>
     __device__ T getVariable(detail::VarName name, unsigned int i) const {
-        return detail::read_rw<T>(P, &P.T->agent, name.hash, index, i);
+        return detail::read_rw<T>(P, &P.T.agent, name.hash, index, i);
     }
     template <typename T>
     __device__ void setVariable(detail::VarName name, T value) {
@@ -818,13 +903,13 @@ class DeviceAPI {
             return;
         }
 #endif
-        detail::write_var<T>(P, &P.T->agent, name.hash, index, value);
+        detail::write_var<T>(P, &P.T.agent, name.hash, index, value);
     }
     template <typename T, flamegpu::size_type N>
     __device__ void setVariable(detail::VarName name, unsigned int i, T value) {
-        detail::write_var<T>(P, &P.T->agent, name.hash, index, value, i);
+        detail::write_var<T>(P, &P.T.agent, name.hash, index, value, i);
     }
-    __device__ id_t getID() const { return detail::read_rw<id_t>(P, &P.T->agent, detail::VarName("_id").hash, index); }
+    __device__ id_t getID() const { return detail::read_rw<id_t>(P, &P.T.agent, detail::VarName("_id").hash, index); }
     __device__ unsigned int getStepCounter() const { return *P.d_step; }
     __device__ unsigned int getIndex() const { return index; }
 

@@ -128,6 +128,10 @@ class CUDASimulation {
     unsigned int getAgentCount(const std::string& agent, const std::string& state = "default");
     /** Device pointer to the current column of an agent variable (valid until the next step). */
     void* getDeviceVariable(const std::string& agent, const std::string& variable, const std::string& state = "default");
+    /** Replace a state list's population from device columns (every variable,
+     *  including _id, n rows each); the agent type's next id becomes next_id. */
+    void setPopulationDevice(const std::string& agent, const std::string& state, unsigned int n,
+                             const std::vector<std::pair<std::string, const void*>>& columns, id_t next_id);
     /** Device pointer to the device-resident agent count of a state list. */
     const unsigned int* getDeviceCount(const std::string& agent, const std::string& state = "default");
     /** Graph replays issued so far (0 when graphs are disabled). */

@@ -44,6 +44,10 @@ int fgs_set_population(fgs_sim* sim, const char* agent, const char* state, uint3
 /* Same, from device columns (no host copy of the data). */
 int fgs_set_population_device(fgs_sim* sim, const char* agent, const char* state, uint32_t n, int32_t nvars,
                               const char* const* names, const void* const* device_cols);
+/* Replace a population from device columns without a host copy: every
+ * variable (including "_id") must be given; next_id is the agent type's next id. */
+int fgs_reset_population_device(fgs_sim* sim, const char* agent, const char* state, uint32_t n, int32_t nvars,
+                                const char* const* names, const void* const* device_cols, uint32_t next_id);
 int fgs_get_count(fgs_sim* sim, const char* agent, const char* state, uint32_t* n);
 /* getPopulationData for one variable: copies count * sizeof(variable) bytes. */
 int fgs_get_variable(fgs_sim* sim, const char* agent, const char* state, const char* var, void* out, size_t bytes);
@@ -62,6 +66,9 @@ int fgs_set_environment(fgs_sim* sim, const char* name, const void* value, size_
 int fgs_get_environment(fgs_sim* sim, const char* name, void* value, size_t bytes);
 int fgs_stream(fgs_sim* sim, void** stream);
 int fgs_stats(fgs_sim* sim, uint64_t* graph_launches, uint32_t* kernels_per_step, uint32_t* step_counter);
+/* Shared memory per block used to stage spatial neighbour windows
+ * (CUDASimulation::Config::message_stage_bytes; 0 disables staging). */
+int fgs_set_stage_bytes(fgs_sim* sim, uint32_t bytes);
 /* Enable/disable per-operation CUDA-event timing (steps then run eagerly, not as graphs). */
 int fgs_profile_ops(fgs_sim* sim, int32_t enable);
 /* Per-operation totals since the last call as "label,total_ms,count;..." (see
