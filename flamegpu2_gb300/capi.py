@@ -31,7 +31,8 @@ EXPORTS = [
     "fg_spatial_grid_init", "fg_spatial_build_workspace_size", "fg_spatial_sort_workspace_size",
     "fg_compact_workspace_size", "fg_workspace_init", "fg_workspace_status", "fg_spatial_build",
     "fg_spatial_sort_agents", "fg_compact_agents", "fg_scan_workspace_size", "fg_exclusive_scan_u32",
-    "fg_last_cuda_error", "fg_version",
+    "fg_last_cuda_error", "fg_version", "fg_batch_instance_init", "fg_batched_workspace_size",
+    "fg_spatial_build_batched", "fg_spatial_sort_agents_batched",
 ]
 
 
@@ -46,6 +47,14 @@ class SpatialGrid(C.Structure):
         ("dims", C.c_int32), ("min", C.c_float * 3), ("max", C.c_float * 3), ("radius", C.c_float),
         ("width", C.c_float * 3), ("gridDim", C.c_uint32 * 3), ("binCount", C.c_uint32),
         ("wrapCompatible", C.c_int32),
+    ]
+
+
+class BatchInstance(C.Structure):
+    _fields_ = [
+        ("grid", SpatialGrid), ("row_begin", C.c_uint32), ("row_capacity", C.c_uint32),
+        ("bucket_begin", C.c_uint32), ("nbuckets", C.c_uint32), ("sort_width", C.c_float * 3),
+        ("sort_gd", C.c_uint32 * 3), ("sort_mask", C.c_uint32), ("pad", C.c_uint32),
     ]
 
 
@@ -95,6 +104,14 @@ def lib():
                                             vp, vp, vp, u32, vp, sz, vp]
             L.fg_exclusive_scan_u32.argtypes = [vp, vp, u32, vp, sz, vp]
             L.fg_version.restype = C.c_char_p
+            L.fg_batch_instance_init.argtypes = [C.POINTER(BatchInstance), C.POINTER(SpatialGrid), u32, u32, u32,
+                                                 C.c_int32, C.POINTER(u32)]
+            L.fg_batched_workspace_size.argtypes = [u32, u32]
+            L.fg_batched_workspace_size.restype = sz
+            L.fg_spatial_build_batched.argtypes = [vp, vp, u32, u32, u32, vp, vp, vp, C.c_int32, vp,
+                                                   C.POINTER(RecordDesc), vp, vp, vp, sz, vp]
+            L.fg_spatial_sort_agents_batched.argtypes = [vp, vp, u32, u32, u32, vp, vp, vp, C.c_int32,
+                                                         C.POINTER(Column), u32, vp, sz, vp]
             _lib = L
     return _lib
 

@@ -20,6 +20,11 @@
 namespace fgk {
 
 constexpr uint32_t kShortBin = 32;
+// Batches mark the keys of padding rows (rows past an instance's count, or
+// messages not output) with this bit: they are counted in their instance's
+// padding bucket so positions stay inside the instance's segment, but they are
+// never ranked or copied as messages.
+constexpr uint32_t kPadBit = 0x80000000u;
 constexpr uint32_t kChunk = 256;     // elements of a long bin ranked by one block pass
 constexpr uint32_t kRankTile = 2048; // bin elements staged in shared memory per pass
 
@@ -103,6 +108,69 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
 // The slot came from the histogram atomics, so pbm[k] + slot < n holds as long
 // as the histogram started at zero (fg_workspace_init); a workspace that broke
 // that invariant is reported instead of written out of bounds.
+__device__ __forceinline__ uint32_t find_instance(const fg_batch_instance* inst, uint32_t ninst, uint32_t row) {
+    uint32_t lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&inst[mid].row_begin) <= row)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Keys of a batch: each row's instance (binary search of the row offsets),
+// then the instance's own message bin / sort key shifted into its bucket
+// range; padding rows go to the instance's padding bucket with kPadBit set.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_bin_batched(const fg_batch_instance* __restrict__ inst,
+                                                          const uint32_t* __restrict__ counts, uint32_t ninst,
+                                                          uint32_t total_rows, int dims, const float* __restrict__ x,
+                                                          const float* __restrict__ y, const float* __restrict__ z,
+                                                          const uint32_t* __restrict__ valid,
+                                                          uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
+                                                          uint32_t* hist, WsHeader* h) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) h->long_count = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total_rows; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < total_rows;
+        uint32_t key = kInvalid;
+        if (act) {
+            const uint32_t k = find_instance(inst, ninst, i);
+            const fg_batch_instance& I = inst[k];
+            const uint32_t local = i - I.row_begin;
+            const uint32_t bb = I.bucket_begin;
+            if (local >= __ldg(counts + k) || (valid != nullptr && valid[i] == 0)) {
+                key = (bb + I.nbuckets) | kPadBit;
+            } else {
+                const float px = x[i], py = y[i], pz = dims == 3 ? z[i] : 0.0f;
+                if (MODE == kMessageBin) {
+                    key = bb + message_bin(I.grid, px, py, pz);
+                } else {
+                    SortGrid sg;
+                    for (int a = 0; a < 3; ++a) {
+                        sg.min[a] = a < dims ? I.grid.min[a] : 0.0f;
+                        sg.width[a] = I.sort_width[a];
+                        sg.gd[a] = I.sort_gd[a];
+                        sg.gd_f[a] = static_cast<float>(I.sort_gd[a]);
+                    }
+                    sg.mask = I.sort_mask;
+                    key = bb + sort_key(sg, dims, px, py, pz);
+                }
+            }
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, key != kInvalid);
+        uint32_t sl = 0;
+        if (key != kInvalid) sl = warp_aggregated_inc(hist, key & ~kPadBit, m);
+        if (act) {
+            keys[i] = key;
+            slot[i] = sl;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_t* d_n,
                                                    const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
                                                    const uint32_t* __restrict__ pbm, uint32_t* __restrict__ perm,
@@ -111,7 +179,7 @@ __global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t k = keys[i];
         if (k != kInvalid) {
-            const uint32_t at = pbm[k] + slot[i];
+            const uint32_t at = pbm[k & ~kPadBit] + slot[i];
             if (at < n)
                 perm[at] = i;
             else
@@ -161,6 +229,10 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
         const uint32_t i = perm[p];
         const uint32_t b = keys[i];
+        if (b & kPadBit) {  // padding row of a batch: keeps its slot, carries no message
+            if (EMIT == kEmitPerm) sperm[p] = i;
+            continue;
+        }
         const uint32_t s = pbm[b], e = pbm[b + 1];
         const uint32_t len = e - s;
         if (len > kShortBin) {
@@ -389,10 +461,17 @@ extern "C" size_t fg_spatial_sort_workspace_size(uint32_t max_n, const fg_spatia
 
 namespace {
 
+struct BatchKeys {
+    const fg_batch_instance* inst = nullptr;  // null: single list
+    const uint32_t* counts = nullptr;
+    uint32_t ninst = 0;
+    int dims = 3;
+};
+
 template <int MODE, int EMIT>
 int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets, uint32_t max_n, const uint32_t* d_n,
                  const float* x, const float* y, const float* z, const uint32_t* valid, const RecordParams& rp,
-                 uint32_t* pbm_out, const BuildLayout& L, char* ws, cudaStream_t st) {
+                 uint32_t* pbm_out, const BuildLayout& L, char* ws, cudaStream_t st, const BatchKeys& batch = BatchKeys()) {
     WsHeader* h = reinterpret_cast<WsHeader*>(ws);
     uint32_t* hist = reinterpret_cast<uint32_t*>(ws + L.hist);
     uint64_t* sstat = reinterpret_cast<uint64_t*>(ws + L.scan_status);
@@ -402,7 +481,11 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     uint32_t* sperm = EMIT == kEmitPerm ? reinterpret_cast<uint32_t*>(ws + L.sperm) : nullptr;
     uint2* chunks = reinterpret_cast<uint2*>(ws + L.chunks);
     const uint32_t grid = grid_for(max_n);
-    k_bin<MODE><<<grid, kThreads, 0, st>>>(*g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
+    if (batch.inst)
+        k_bin_batched<MODE><<<grid, kThreads, 0, st>>>(batch.inst, batch.counts, batch.ninst, max_n, batch.dims, x, y, z,
+                                                      valid, keys, slot, hist, h);
+    else
+        k_bin<MODE><<<grid, kThreads, 0, st>>>(*g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
     const uint32_t scan_n = nbuckets + 1;
     k_scan_u32<<<scan_tiles(scan_n), kThreads, 0, st>>>(hist, pbm_out, scan_n, 1, sstat, h);
     k_perm<<<grid, kThreads, 0, st>>>(max_n, d_n, keys, slot, pbm_out, perm, h);
@@ -498,3 +581,94 @@ extern "C" int fg_workspace_status(void* workspace, size_t workspace_bytes, void
 }
 
 extern "C" const char* fg_version(void) { return "flamegpu2_gb300 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------------ batches
+
+extern "C" int fg_batch_instance_init(fg_batch_instance* inst, const fg_spatial_grid* g, uint32_t row_begin,
+                                      uint32_t row_capacity, uint32_t bucket_begin, int32_t mode,
+                                      uint32_t* nbuckets_total) {
+    if (!inst || !g || (mode != 0 && mode != 1)) return FG_ERR_INVALID_ARGUMENT;
+    *inst = fg_batch_instance{};
+    inst->grid = *g;
+    inst->row_begin = row_begin;
+    inst->row_capacity = row_capacity;
+    inst->bucket_begin = bucket_begin;
+    SortGrid sg{};
+    uint32_t nb = 0;
+    if (!sort_grid_from(g, &sg, &nb)) return FG_ERR_UNSUPPORTED;
+    for (int a = 0; a < 3; ++a) {
+        inst->sort_width[a] = sg.width[a];
+        inst->sort_gd[a] = sg.gd[a];
+    }
+    inst->sort_mask = sg.mask;
+    inst->nbuckets = mode == 0 ? g->binCount : nb;
+    if (nbuckets_total) *nbuckets_total = inst->nbuckets + 1;
+    if (static_cast<uint64_t>(bucket_begin) + inst->nbuckets + 1 >= kPadBit) return FG_ERR_UNSUPPORTED;
+    return FG_OK;
+}
+
+extern "C" size_t fg_batched_workspace_size(uint32_t total_rows, uint32_t total_buckets) {
+    // the single-list layout over (bucket count - 1) bins holds total_buckets + 1 scan entries
+    return build_layout(total_rows, total_buckets, true).total;
+}
+
+extern "C" int fg_spatial_build_batched(const fg_batch_instance* instances, const uint32_t* counts, uint32_t ninst,
+                                        uint32_t total_rows, uint32_t total_buckets, const float* x, const float* y,
+                                        const float* z, int32_t dims, const uint32_t* valid, const fg_record_desc* rec,
+                                        uint32_t* sorted, uint32_t* pbm, void* workspace, size_t workspace_bytes,
+                                        void* stream) {
+    if (!instances || !counts || !ninst || !rec || !pbm || !workspace || (dims != 2 && dims != 3))
+        return FG_ERR_INVALID_ARGUMENT;
+    if (rec->words == 0 || (rec->words & 3) || rec->words > FG_MAX_RECORD_WORDS) return FG_ERR_INVALID_ARGUMENT;
+    if (total_rows && (!x || !y || (dims == 3 && !z) || !sorted)) return FG_ERR_INVALID_ARGUMENT;
+    if ((reinterpret_cast<uintptr_t>(sorted) & 15) || total_buckets >= kPadBit) return FG_ERR_INVALID_ARGUMENT;
+    const BuildLayout L = build_layout(total_rows, total_buckets, true);
+    if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
+    RecordParams rp;
+    rp.rec = *rec;
+    rp.out = sorted;
+    SortGrid sg{};
+    BatchKeys bk;
+    bk.inst = instances;
+    bk.counts = counts;
+    bk.ninst = ninst;
+    bk.dims = dims;
+    fg_spatial_grid dummy{};
+    return run_pipeline<kMessageBin, kEmitRecord>(&dummy, sg, total_buckets, total_rows, nullptr, x, y, z, valid, rp, pbm,
+                                                  L, static_cast<char*>(workspace), static_cast<cudaStream_t>(stream), bk);
+}
+
+extern "C" int fg_spatial_sort_agents_batched(const fg_batch_instance* instances, const uint32_t* counts,
+                                              uint32_t ninst, uint32_t total_rows, uint32_t total_buckets,
+                                              const float* x, const float* y, const float* z, int32_t dims,
+                                              const fg_column* cols, uint32_t ncols, void* workspace,
+                                              size_t workspace_bytes, void* stream) {
+    if (!instances || !counts || !ninst || !workspace || (dims != 2 && dims != 3) || ncols > FG_MAX_COLUMNS)
+        return FG_ERR_INVALID_ARGUMENT;
+    if (total_rows && (!x || !y || (dims == 3 && !z))) return FG_ERR_INVALID_ARGUMENT;
+    if (ncols && !cols) return FG_ERR_INVALID_ARGUMENT;
+    if (total_buckets >= kPadBit) return FG_ERR_INVALID_ARGUMENT;
+    const BuildLayout L = build_layout(total_rows, total_buckets, true);
+    if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
+    char* ws = static_cast<char*>(workspace);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RecordParams rp{};
+    SortGrid sg{};
+    BatchKeys bk;
+    bk.inst = instances;
+    bk.counts = counts;
+    bk.ninst = ninst;
+    bk.dims = dims;
+    fg_spatial_grid dummy{};
+    int rc = run_pipeline<kSortKey, kEmitPerm>(&dummy, sg, total_buckets, total_rows, nullptr, x, y, z, nullptr, rp,
+                                               reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st, bk);
+    if (rc != FG_OK) return rc;
+    if (ncols) {
+        ColumnParams cp{};
+        for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cols[c];
+        cp.ncols = ncols;
+        k_gather_columns<<<grid_for(total_rows), kThreads, 0, st>>>(cp, total_rows, nullptr,
+                                                                    reinterpret_cast<const uint32_t*>(ws + L.sperm));
+    }
+    return check_launch();
+}

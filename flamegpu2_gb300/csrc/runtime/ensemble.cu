@@ -1,0 +1,660 @@
+// CUDAEnsemble on GB300: RunPlans become instances of one batched simulation.
+//
+// Layout. Instance k owns rows [row_begin_k, row_begin_k + cap_k) of every
+// agent column and message column (cap_k = its population rounded up to the
+// 128-thread agent block, so no block straddles two instances). Each spatial
+// message list keeps one concatenated record buffer and one PBM: instance k's
+// bins are buckets [bucket_begin_k, bucket_begin_k + binCount_k] (+1 padding
+// bucket), so a single segmented counting sort builds every instance's index
+// and its PBM is the slice at bucket_begin_k. The automatic agent sort is
+// batched the same way over per-instance sort buckets. Agent function kernels
+// find their block's instance in a small table (grid, PBM offset, environment
+// buffer, seed, step offset) and otherwise run the model code unchanged. One
+// CUDA graph per buffer parity replays a whole ensemble step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "flamegpu/simulation/CUDAEnsemble.h"
+#include "flamegpu/simulation/CUDASimulation.h"
+#include "flamegpu_gb300/fg_capi.h"
+#include "runtime/internal.h"
+
+namespace flamegpu {
+
+using exception::format;
+
+#define FG_ECUDA(call)                                                                                     \
+    do {                                                                                                   \
+        const cudaError_t _e = (call);                                                                     \
+        if (_e != cudaSuccess)                                                                             \
+            THROW exception::CUDAError(format("%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__)); \
+    } while (0)
+#define FG_ECAPI(call)                                                                                     \
+    do {                                                                                                   \
+        const int _r = (call);                                                                             \
+        if (_r != FG_OK) THROW exception::CUDAError(format("%s returned %d (%s:%d)", #call, _r, __FILE__, __LINE__)); \
+    } while (0)
+
+// ------------------------------------------------------------------ RunPlan
+
+RunPlan::RunPlan(const ModelDescription& model) : model_(model.getData()) {}
+
+void RunPlan::set_property(const std::string& name, std::type_index t, size_t size, const void* v) {
+    const detail::EnvProperty* p = model_->property(name);
+    if (!p) THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+    if (p->type != t || p->type_size != size || p->elements != 1)
+        THROW exception::InvalidEnvPropertyType(format("Environment property '%s' has another type", name.c_str()));
+    std::vector<char> bytes(size);
+    std::memcpy(bytes.data(), v, size);
+    properties_[name] = std::move(bytes);
+}
+
+void RunPlan::setPopulation(const AgentVector& population, const std::string& state) {
+    populations_[{population.getAgentName(), state}] = std::make_shared<AgentVector>(population);
+}
+
+void RunPlan::setSpatialMessageBounds(const std::string& message, const std::vector<float>& mn,
+                                      const std::vector<float>& mx, float radius) {
+    const detail::MessageData* m = model_->message(message);
+    if (!m || m->kind == detail::MessageKind::BruteForce)
+        THROW exception::InvalidMessageName(format("No spatial message '%s'", message.c_str()));
+    spatial_[message] = SpatialOverride{mn, mx, radius};
+}
+
+RunPlanVector::RunPlanVector(const ModelDescription& model, unsigned int n) {
+    for (unsigned int i = 0; i < n; ++i) emplace_back(model);
+}
+
+void RunPlanVector::setSteps(unsigned int steps) {
+    for (auto& p : *this) p.setSteps(steps);
+}
+
+void RunPlanVector::setRandomSimulationSeed(uint64_t initial_seed, unsigned int step) {
+    uint64_t s = initial_seed;
+    for (auto& p : *this) {
+        p.setRandomSimulationSeed(s);
+        s += step;
+    }
+}
+
+namespace detail {
+
+namespace {
+
+__global__ void k_batch_step_increment(uint32_t* d_step) { *d_step += 1; }
+
+constexpr uint32_t kRowAlign = kAgentBlock;
+
+uint32_t round_rows(uint32_t n) { return std::max(kRowAlign, (n + kRowAlign - 1) / kRowAlign * kRowAlign); }
+
+struct Alloc {
+    std::vector<void*> ptrs;
+    void* get(size_t bytes) {
+        void* p = nullptr;
+        FG_ECUDA(cudaMalloc(&p, std::max<size_t>(bytes, 256)));
+        FG_ECUDA(cudaMemset(p, 0, std::max<size_t>(bytes, 256)));
+        ptrs.push_back(p);
+        return p;
+    }
+    ~Alloc() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+}  // namespace
+
+/** Why a model cannot run as one batched simulation ("" if it can). */
+std::string batch_unsupported(const ModelData& m) {
+    if (m.agents.size() != 1) return "the model has more than one agent type";
+    const AgentData& a = *m.agents[0];
+    if (a.states.size() != 1) return "the agent has more than one state";
+    if (!m.init_functions.empty() || !m.step_functions.empty() || !m.exit_functions.empty())
+        return "the model has host functions";
+    for (const auto& l : m.layers)
+        if (!l->host_functions.empty()) return "the model has host layer functions";
+    for (const auto& f : a.functions) {
+        if (f->has_agent_death || !f->agent_output.empty()) return "agent birth/death";
+        if (f->message_output_optional) return "optional message output";
+        if (!f->message_input.empty() && m.message(f->message_input)->kind == MessageKind::BruteForce)
+            return "brute-force message input";
+    }
+    return "";
+}
+
+/** One ensemble run as a single batched simulation. */
+struct BatchedSim {
+    std::shared_ptr<ModelData> model;
+    AgentData* agent = nullptr;
+    const RunPlanVector& plans;
+    const CUDAEnsemble::EnsembleConfig& cfg;
+    Alloc mem;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    int sms = 132;
+    uint32_t ninst = 0, total_rows = 0;
+    std::vector<uint32_t> row_begin, cap, count;
+    std::vector<std::array<void*, 2>> cols;  // per agent variable
+    int parity = 0;
+    uint32_t* d_counts = nullptr;
+    uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record
+    std::vector<size_t> env_offset;
+    size_t env_stride = 0;
+    char* d_env = nullptr;
+
+    struct BMsg {
+        MessageData* msg = nullptr;
+        int dims = 0;
+        std::vector<uint32_t> slot_bytes, field_word;
+        uint32_t record_words = 0;
+        std::vector<void*> cols;
+        uint32_t* records = nullptr;
+        uint32_t* pbm = nullptr;
+        uint32_t total_buckets = 0;
+        std::vector<fg_batch_instance> inst;
+        fg_batch_instance* d_inst = nullptr;
+        void* ws = nullptr;
+        size_t ws_bytes = 0;
+        bool needs_build = true;
+    };
+    std::vector<std::unique_ptr<BMsg>> msgs;
+
+    struct BFn {
+        AgentFunctionData* fn = nullptr;
+        BMsg* in = nullptr;
+        BMsg* out = nullptr;
+        bool sort = false;
+        std::vector<fg_batch_instance> sort_inst;
+        fg_batch_instance* d_sort_inst = nullptr;
+        uint32_t sort_buckets = 0;
+        void* sort_ws = nullptr;
+        size_t sort_ws_bytes = 0;
+        BatchInstanceRT* d_rt = nullptr;
+        std::unique_ptr<FunctionTables> tables[2];
+    };
+    std::vector<BFn> fns;
+    cudaGraphExec_t graphs[2] = {nullptr, nullptr};
+    unsigned int kernels_per_step = 0;
+    unsigned long long graph_launches = 0;
+
+    BatchedSim(std::shared_ptr<ModelData> m, const RunPlanVector& p, const CUDAEnsemble::EnsembleConfig& c)
+        : model(std::move(m)), plans(p), cfg(c) {}
+    ~BatchedSim() {
+        for (auto& g : graphs)
+            if (g) cudaGraphExecDestroy(g);
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
+        if (side) cudaStreamDestroy(side);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    BMsg* msg_of(const std::string& name) {
+        for (auto& m : msgs)
+            if (m->msg->name == name) return m.get();
+        return nullptr;
+    }
+
+    // Message grid of run k (the plan's override, else the model's bounds).
+    fg_spatial_grid grid_of(const MessageData* m, uint32_t k) const {
+        const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
+        std::vector<float> mn(m->min, m->min + 3), mx(m->max, m->max + 3);
+        float r = m->radius;
+        auto it = plans[k].spatial().find(m->name);
+        if (it != plans[k].spatial().end()) {
+            mn = it->second.min;
+            mx = it->second.max;
+            r = it->second.radius;
+            mn.resize(3, 0.0f);
+            mx.resize(3, 0.0f);
+        }
+        fg_spatial_grid g{};
+        if (fg_spatial_grid_init(&g, dims, mn.data(), mx.data(), r) != FG_OK)
+            THROW exception::InvalidArgument(format("Run %u: invalid bounds/radius for message '%s'", k, m->name.c_str()));
+        return g;
+    }
+
+    void setup() {
+        FG_ECUDA(cudaSetDevice(cfg.device));
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device);
+        if (sms <= 0) sms = 132;
+        FG_ECUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        FG_ECUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        FG_ECUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+        FG_ECUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
+        agent = model->agents[0].get();
+        const std::string state = agent->states[0];
+        ninst = static_cast<uint32_t>(plans.size());
+        // ---- row segments
+        uint32_t row = 0;
+        for (uint32_t k = 0; k < ninst; ++k) {
+            auto it = plans[k].populations().find({agent->name, state});
+            const uint32_t n = it == plans[k].populations().end() ? 0u : it->second->size();
+            row_begin.push_back(row);
+            count.push_back(n);
+            cap.push_back(round_rows(n));
+            if (static_cast<uint64_t>(row) + cap.back() >= (1ull << 31)) THROW exception::OutOfMemory("Ensemble exceeds 2^31 agent rows");
+            row += cap.back();
+        }
+        total_rows = row;
+        cols.resize(agent->variables.size());
+        for (size_t v = 0; v < cols.size(); ++v) {
+            const size_t b = agent->variables[v].bytes();
+            cols[v] = {mem.get(b * total_rows), mem.get(b * total_rows)};
+        }
+        for (uint32_t k = 0; k < ninst; ++k) {
+            auto it = plans[k].populations().find({agent->name, state});
+            if (it == plans[k].populations().end() || count[k] == 0) continue;
+            AgentVector pop = *it->second;  // ids are per run: fill unset ones (CUDAFatAgent.cu:311-319)
+            const size_t idc = pop.columnIndex("_id");
+            id_t* ids = reinterpret_cast<id_t*>(pop.columns()[idc].data());
+            id_t next = 1;
+            for (uint32_t i = 0; i < count[k]; ++i) next = std::max<id_t>(next, ids[i] + 1);
+            for (uint32_t i = 0; i < count[k]; ++i)
+                if (ids[i] == ID_NOT_SET) ids[i] = next++;
+            for (size_t v = 0; v < cols.size(); ++v) {
+                const size_t b = agent->variables[v].bytes();
+                FG_ECUDA(cudaMemcpy(static_cast<char*>(cols[v][0]) + b * row_begin[k], pop.columns()[v].data(),
+                                    b * count[k], cudaMemcpyHostToDevice));
+            }
+        }
+        d_counts = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * ninst));
+        FG_ECUDA(cudaMemcpy(d_counts, count.data(), sizeof(uint32_t) * ninst, cudaMemcpyHostToDevice));
+        d_misc = static_cast<uint32_t*>(mem.get(64));
+        // ---- environments: the model's values with each plan's overrides
+        size_t off = 0;
+        for (const auto& p : model->environment) {
+            env_offset.push_back(off);
+            off += (p.value.size() + 7) & ~size_t(7);
+        }
+        env_stride = std::max<size_t>(256, (off + 255) & ~size_t(255));
+        std::vector<char> envs(env_stride * ninst, 0);
+        for (uint32_t k = 0; k < ninst; ++k)
+            for (size_t i = 0; i < model->environment.size(); ++i) {
+                const auto& p = model->environment[i];
+                auto ov = plans[k].properties().find(p.name);
+                const std::vector<char>& val = ov == plans[k].properties().end() ? p.value : ov->second;
+                std::memcpy(envs.data() + env_stride * k + env_offset[i], val.data(), val.size());
+            }
+        d_env = static_cast<char*>(mem.get(envs.size()));
+        FG_ECUDA(cudaMemcpy(d_env, envs.data(), envs.size(), cudaMemcpyHostToDevice));
+        // ---- message lists
+        for (const auto& m : model->messages) {
+            auto bm = std::make_unique<BMsg>();
+            bm->msg = m.get();
+            bm->dims = m->kind == MessageKind::Spatial3D ? 3 : (m->kind == MessageKind::Spatial2D ? 2 : 0);
+            uint32_t w = 0;
+            for (const auto& v : m->variables) {
+                const uint32_t sb = (v.bytes() + 3u) & ~3u;
+                bm->slot_bytes.push_back(sb);
+                bm->field_word.push_back(w);
+                w += sb / 4;
+                bm->cols.push_back(mem.get(static_cast<size_t>(sb) * total_rows));
+            }
+            if (bm->dims) {
+                bm->record_words = std::max(4u, (w + 3u) & ~3u);
+                if (bm->record_words > FG_MAX_RECORD_WORDS)
+                    THROW exception::InvalidMessage(format("Message '%s' is too large", m->name.c_str()));
+                bm->records = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * bm->record_words * static_cast<size_t>(total_rows)));
+                uint32_t bucket = 0;
+                for (uint32_t k = 0; k < ninst; ++k) {
+                    fg_batch_instance bi{};
+                    const fg_spatial_grid g = grid_of(m.get(), k);
+                    uint32_t nb = 0;
+                    FG_ECAPI(fg_batch_instance_init(&bi, &g, row_begin[k], cap[k], bucket, 0, &nb));
+                    bm->inst.push_back(bi);
+                    bucket += (nb + 3u) & ~3u;  // 16-byte aligned PBM slices (staging copies)
+                }
+                bm->total_buckets = bucket;
+                bm->d_inst = static_cast<fg_batch_instance*>(mem.get(sizeof(fg_batch_instance) * ninst));
+                FG_ECUDA(cudaMemcpy(bm->d_inst, bm->inst.data(), sizeof(fg_batch_instance) * ninst, cudaMemcpyHostToDevice));
+                bm->pbm = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * (static_cast<size_t>(bucket) + 8)));
+                bm->ws_bytes = fg_batched_workspace_size(total_rows, bucket);
+                bm->ws = mem.get(bm->ws_bytes);
+            }
+            msgs.push_back(std::move(bm));
+        }
+        // ---- agent functions
+        for (const auto& f : agent->functions) {
+            BFn b;
+            b.fn = f.get();
+            b.in = f->message_input.empty() ? nullptr : msg_of(f->message_input);
+            b.out = f->message_output.empty() ? nullptr : msg_of(f->message_output);
+            if (b.in && b.in->dims) {
+                bool ok = true;
+                const char* ax[3] = {"x", "y", "z"};
+                for (int d = 0; d < b.in->dims; ++d) {
+                    const Variable* v = agent->find(ax[d]);
+                    ok = ok && v && v->type == std::type_index(typeid(float)) && v->elements == 1;
+                }
+                b.sort = ok;
+            }
+            if (b.sort) {
+                uint32_t bucket = 0;
+                for (uint32_t k = 0; k < ninst; ++k) {
+                    fg_batch_instance bi{};
+                    const fg_spatial_grid g = grid_of(b.in->msg, k);
+                    uint32_t nb = 0;
+                    FG_ECAPI(fg_batch_instance_init(&bi, &g, row_begin[k], cap[k], bucket, 1, &nb));
+                    b.sort_inst.push_back(bi);
+                    bucket += nb;
+                }
+                b.sort_buckets = bucket;
+                b.d_sort_inst = static_cast<fg_batch_instance*>(mem.get(sizeof(fg_batch_instance) * ninst));
+                FG_ECUDA(cudaMemcpy(b.d_sort_inst, b.sort_inst.data(), sizeof(fg_batch_instance) * ninst, cudaMemcpyHostToDevice));
+                b.sort_ws_bytes = fg_batched_workspace_size(total_rows, bucket);
+                b.sort_ws = mem.get(b.sort_ws_bytes);
+            }
+            std::vector<BatchInstanceRT> rt(ninst);
+            for (uint32_t k = 0; k < ninst; ++k) {
+                rt[k].row_begin = row_begin[k];
+                rt[k].row_capacity = cap[k];
+                rt[k].step_offset = 0;
+                rt[k].env = d_env + env_stride * k;
+                rt[k].seed = plans[k].getRandomSimulationSeed();
+                if (b.in && b.in->dims) {
+                    rt[k].in_grid = b.in->inst[k].grid;
+                    rt[k].in_bucket_begin = b.in->inst[k].bucket_begin;
+                }
+            }
+            b.d_rt = static_cast<BatchInstanceRT*>(mem.get(sizeof(BatchInstanceRT) * ninst));
+            FG_ECUDA(cudaMemcpy(b.d_rt, rt.data(), sizeof(BatchInstanceRT) * ninst, cudaMemcpyHostToDevice));
+            for (int par = 0; par < 2; ++par) {
+                auto T = std::make_unique<FunctionTables>();
+                std::memset(T.get(), 0, sizeof(FunctionTables));
+                std::vector<TableEntry> e;
+                for (size_t v = 0; v < agent->variables.size(); ++v) {
+                    const Variable& var = agent->variables[v];
+                    e.push_back({fnv1a32(var.name), static_cast<char*>(cols[v][par]), var.bytes(), var.type_size, var.elements});
+                }
+                T->agent = make_table(e, "agent");
+                if (b.out) {
+                    e.clear();
+                    for (size_t v = 0; v < b.out->msg->variables.size(); ++v) {
+                        const Variable& var = b.out->msg->variables[v];
+                        e.push_back({fnv1a32(var.name), static_cast<char*>(b.out->cols[v]), b.out->slot_bytes[v], var.type_size, var.elements});
+                    }
+                    T->msg_out = make_table(e, "message");
+                }
+                if (b.in) {
+                    e.clear();
+                    for (size_t v = 0; v < b.in->msg->variables.size(); ++v) {
+                        const Variable& var = b.in->msg->variables[v];
+                        e.push_back({fnv1a32(var.name), reinterpret_cast<char*>(b.in->records + b.in->field_word[v]),
+                                     b.in->record_words * 4, var.type_size, var.elements});
+                    }
+                    T->msg_in = make_table(e, "message");
+                }
+                e.clear();
+                for (size_t i = 0; i < model->environment.size(); ++i) {
+                    const EnvProperty& p = model->environment[i];
+                    e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(env_offset[i]), 0, p.type_size, p.elements});
+                }
+                T->env = make_table(e, "environment");
+                b.tables[par] = std::move(T);
+            }
+            fns.push_back(std::move(b));
+        }
+    }
+
+    void enqueue_sort(BFn& b) {
+        std::vector<fg_column> c(cols.size());
+        for (size_t v = 0; v < cols.size(); ++v)
+            c[v] = fg_column{cols[v][parity], cols[v][parity ^ 1], agent->variables[v].bytes()};
+        auto col_of = [&](const char* n) -> const float* {
+            for (size_t v = 0; v < agent->variables.size(); ++v)
+                if (agent->variables[v].name == n) return static_cast<const float*>(cols[v][parity]);
+            return nullptr;
+        };
+        FG_ECAPI(fg_spatial_sort_agents_batched(b.d_sort_inst, d_counts, ninst, total_rows, b.sort_buckets, col_of("x"),
+                                                col_of("y"), b.in->dims == 3 ? col_of("z") : nullptr, b.in->dims,
+                                                c.data(), static_cast<uint32_t>(c.size()), b.sort_ws, b.sort_ws_bytes,
+                                                stream));
+        parity ^= 1;
+        kernels_per_step += 6;
+    }
+
+    void enqueue_build(BMsg& m, cudaStream_t st) {
+        fg_record_desc rec;
+        std::memset(&rec, 0, sizeof(rec));
+        rec.words = m.record_words;
+        uint32_t w = 0;
+        for (size_t v = 0; v < m.cols.size(); ++v) {
+            const uint32_t words = m.slot_bytes[v] / 4;
+            for (uint32_t k = 0; k < words; ++k, ++w) {
+                rec.src[w] = static_cast<const uint32_t*>(m.cols[v]);
+                rec.src_stride[w] = words;
+                rec.src_word[w] = k;
+            }
+        }
+        FG_ECAPI(fg_spatial_build_batched(m.d_inst, d_counts, ninst, total_rows, m.total_buckets,
+                                          static_cast<const float*>(m.cols[0]), static_cast<const float*>(m.cols[1]),
+                                          m.dims == 3 ? static_cast<const float*>(m.cols[2]) : nullptr, m.dims, nullptr,
+                                          &rec, m.records, m.pbm, m.ws, m.ws_bytes, st));
+        m.needs_build = false;
+        kernels_per_step += 5;
+    }
+
+    void launch_fn(BFn& b) {
+        LaunchParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.T = *b.tables[parity];
+        P.max_n = total_rows;
+        P.msg_out_enabled = b.out ? 1 : 0;
+        unsigned int smem = 0;
+        if (b.in && b.in->dims) {
+            P.in_pbm = b.in->pbm;
+            P.in_records = reinterpret_cast<const char*>(b.in->records);
+            P.in_record_bytes = b.in->record_words * 4u;
+            if (b.sort && cfg.message_stage_bytes >= 1024u) {
+                P.stage_bytes = (cfg.message_stage_bytes + 15u) & ~15u;
+                smem = P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader));
+            }
+        }
+        P.d_step = d_misc;
+        P.fn_uid = b.fn->uid;
+        P.error = d_misc + 1;
+        P.batch = b.d_rt;
+        P.batch_counts = d_counts;
+        P.batch_n = ninst;
+        const uint32_t grid = std::min(total_rows / kAgentBlock, static_cast<uint32_t>(sms * 16));
+        const cudaError_t e = b.fn->launcher(P, std::max(1u, grid), kAgentBlock, smem, stream);
+        if (e != cudaSuccess)
+            THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", b.fn->name.c_str(), cudaGetErrorString(e)));
+        kernels_per_step += 1;
+    }
+
+    bool sorts_at(unsigned int step) const {
+        return agent->sort_period != 0 && step % agent->sort_period == 0;
+    }
+
+    void enqueue_step(unsigned int step) {
+        kernels_per_step = 0;
+        for (auto& m : msgs) m->needs_build = true;
+        for (const auto& layer : model->layers)
+            for (auto* fd : layer->functions)
+                for (auto& b : fns) {
+                    if (b.fn != fd) continue;
+                    const bool do_sort = b.sort && sorts_at(step);
+                    const bool do_build = b.in && b.in->dims && b.in->needs_build;
+                    if (do_sort && do_build) {
+                        FG_ECUDA(cudaEventRecord(fork_ev, stream));
+                        FG_ECUDA(cudaStreamWaitEvent(side, fork_ev, 0));
+                        enqueue_build(*b.in, side);
+                        enqueue_sort(b);
+                        FG_ECUDA(cudaEventRecord(join_ev, side));
+                        FG_ECUDA(cudaStreamWaitEvent(stream, join_ev, 0));
+                    } else {
+                        if (do_sort) enqueue_sort(b);
+                        if (do_build) enqueue_build(*b.in, stream);
+                    }
+                    launch_fn(b);
+                    if (b.out) b.out->needs_build = true;
+                }
+        k_batch_step_increment<<<1, 1, 0, stream>>>(d_misc);
+        kernels_per_step += 1;
+    }
+
+    int flips_at(unsigned int step) const {
+        int f = 0;
+        for (const auto& b : fns)
+            if (b.sort && sorts_at(step)) ++f;
+        return f;
+    }
+
+    AgentVector read_instance(uint32_t k) {
+        AgentVector pop(AgentDescription(model, agent), 0);
+        pop.setCountRaw(count[k]);
+        for (size_t v = 0; v < cols.size(); ++v) {
+            const size_t b = agent->variables[v].bytes();
+            if (count[k])
+                FG_ECUDA(cudaMemcpy(pop.columns()[v].data(), static_cast<char*>(cols[v][parity]) + b * row_begin[k],
+                                    b * count[k], cudaMemcpyDeviceToHost));
+        }
+        return pop;
+    }
+
+    // Runs every plan to its step count; fills results[k].
+    void run(std::vector<std::shared_ptr<AgentVector>>& results) {
+        unsigned int max_steps = 0;
+        for (const auto& p : plans) max_steps = std::max(max_steps, p.getSteps());
+        results.assign(ninst, nullptr);
+        std::map<std::pair<int, bool>, cudaGraphExec_t> cache;
+        for (unsigned int s = 0; s < max_steps; ++s) {
+            if (cfg.use_graphs) {
+                const auto key = std::make_pair(parity, sorts_at(s));
+                auto it = cache.find(key);
+                if (it == cache.end()) {
+                    cudaGraph_t g;
+                    FG_ECUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                    try {
+                        enqueue_step(s);
+                    } catch (...) {
+                        cudaStreamEndCapture(stream, &g);
+                        throw;
+                    }
+                    FG_ECUDA(cudaStreamEndCapture(stream, &g));
+                    cudaGraphExec_t ge;
+                    FG_ECUDA(cudaGraphInstantiate(&ge, g, 0));
+                    cudaGraphDestroy(g);
+                    it = cache.emplace(key, ge).first;
+                } else {
+                    if (flips_at(s) & 1) parity ^= 1;
+                }
+                FG_ECUDA(cudaGraphLaunch(it->second, stream));
+                ++graph_launches;
+            } else {
+                enqueue_step(s);
+            }
+            // runs that end here: read them back and drop them from later steps
+            bool any = false;
+            for (uint32_t k = 0; k < ninst; ++k) any = any || (plans[k].getSteps() == s + 1 && s + 1 < max_steps);
+            if (any) {
+                FG_ECUDA(cudaStreamSynchronize(stream));
+                for (uint32_t k = 0; k < ninst; ++k) {
+                    if (plans[k].getSteps() != s + 1 || s + 1 >= max_steps) continue;
+                    results[k] = std::make_shared<AgentVector>(read_instance(k));
+                    count[k] = 0;
+                    FG_ECUDA(cudaMemcpy(d_counts + k, &count[k], sizeof(uint32_t), cudaMemcpyHostToDevice));
+                }
+            }
+        }
+        FG_ECUDA(cudaStreamSynchronize(stream));
+        for (auto& c : cache) cudaGraphExecDestroy(c.second);
+        uint32_t err[4];
+        FG_ECUDA(cudaMemcpy(err, d_misc + 1, sizeof(err), cudaMemcpyDeviceToHost));
+        if (err[0]) THROW exception::DeviceError(format("Device error %u in a batched ensemble step (name hash 0x%08x, row %u)", err[0], err[1], err[2]));
+        for (uint32_t k = 0; k < ninst; ++k)
+            if (!results[k]) results[k] = std::make_shared<AgentVector>(read_instance(k));
+    }
+};
+
+struct EnsembleImpl {
+    ModelDescription desc;
+    CUDAEnsemble::EnsembleConfig cfg;
+    std::vector<std::map<std::pair<std::string, std::string>, std::shared_ptr<AgentVector>>> results;
+    double elapsed = 0.0;
+    bool batched = false;
+    unsigned int kernels_per_step = 0;
+    unsigned long long graph_launches = 0;
+    explicit EnsembleImpl(const ModelDescription& d) : desc(d) {}
+};
+
+}  // namespace detail
+
+CUDAEnsemble::CUDAEnsemble(const ModelDescription& model, int, const char**)
+    : impl(std::make_unique<detail::EnsembleImpl>(model)) {}
+CUDAEnsemble::~CUDAEnsemble() = default;
+CUDAEnsemble::EnsembleConfig& CUDAEnsemble::Config() { return impl->cfg; }
+double CUDAEnsemble::getEnsembleElapsedTime() const { return impl->elapsed; }
+bool CUDAEnsemble::lastRunBatched() const { return impl->batched; }
+unsigned int CUDAEnsemble::getKernelsPerStep() const { return impl->kernels_per_step; }
+unsigned long long CUDAEnsemble::getGraphLaunches() const { return impl->graph_launches; }
+
+unsigned int CUDAEnsemble::simulate(const RunPlanVector& plans) {
+    const auto t0 = std::chrono::steady_clock::now();
+    impl->results.assign(plans.size(), {});
+    const auto& model = impl->desc.getData();
+    for (const auto& p : plans)
+        if (p.model() != model) THROW exception::InvalidArgument("RunPlan belongs to another model");
+    unsigned int failures = 0;
+    impl->batched = impl->cfg.batched && !plans.empty() && detail::batch_unsupported(*model).empty();
+    if (impl->batched) {
+        detail::BatchedSim b(model, plans, impl->cfg);
+        b.setup();
+        std::vector<std::shared_ptr<AgentVector>> res;
+        b.run(res);
+        const auto key = std::make_pair(model->agents[0]->name, model->agents[0]->states[0]);
+        for (size_t k = 0; k < plans.size(); ++k) impl->results[k][key] = res[k];
+        impl->kernels_per_step = b.kernels_per_step;
+        impl->graph_launches = b.graph_launches;
+    } else {
+        // the plain path: one CUDASimulation per plan, one after another
+        for (size_t k = 0; k < plans.size(); ++k) {
+            const RunPlan& p = plans[k];
+            try {
+                CUDASimulation sim(impl->desc);
+                sim.CUDAConfig().device_id = impl->cfg.device;
+                sim.CUDAConfig().use_graphs = impl->cfg.use_graphs;
+                sim.CUDAConfig().message_stage_bytes = impl->cfg.message_stage_bytes;
+                sim.SimulationConfig().random_seed = p.getRandomSimulationSeed();
+                sim.SimulationConfig().steps = p.getSteps();
+                for (const auto& sp : p.spatial()) sim.setSpatialMessageBounds(sp.first, sp.second.min, sp.second.max, sp.second.radius);
+                HostAPI::Environment env(sim.getImpl());
+                for (const auto& pr : p.properties()) env.setRaw(pr.first, pr.second.data(), pr.second.size());
+                for (const auto& pop : p.populations()) {
+                    AgentVector copy = *pop.second;
+                    sim.setPopulationData(copy, pop.first.second);
+                }
+                sim.simulate();
+                for (const auto& a : model->agents)
+                    for (const auto& st : a->states) {
+                        auto out = std::make_shared<AgentVector>(AgentDescription(model, a.get()));
+                        sim.getPopulationData(*out, st);
+                        impl->results[k][{a->name, st}] = out;
+                    }
+            } catch (const exception::FLAMEGPUException&) {
+                ++failures;
+            }
+        }
+    }
+    impl->elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return failures;
+}
+
+void CUDAEnsemble::getPopulationData(unsigned int run, AgentVector& population, const std::string& state) const {
+    if (run >= impl->results.size()) THROW exception::OutOfBoundsException(format("Run %u out of range", run));
+    auto it = impl->results[run].find({population.getAgentName(), state});
+    if (it == impl->results[run].end() || !it->second)
+        THROW exception::InvalidAgentName(format("Run %u has no population of '%s' in state '%s'", run,
+                                                  population.getAgentName().c_str(), state.c_str()));
+    population = *it->second;
+}
+
+}  // namespace flamegpu

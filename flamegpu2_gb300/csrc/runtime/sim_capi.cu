@@ -267,3 +267,111 @@ extern "C" int fgs_set_stage_bytes(fgs_sim* s, uint32_t bytes) {
         s->sim->applyConfig();
     });
 }
+
+// ---------------------------------------------------------------- ensembles
+
+struct fge_ensemble {
+    std::unique_ptr<flamegpu::ModelDescription> model;
+    std::unique_ptr<flamegpu::CUDAEnsemble> ens;
+    std::unique_ptr<flamegpu::RunPlanVector> plans;
+};
+
+extern "C" fge_ensemble* fge_create(const char* model, const double* params, int32_t nparams, int32_t device) {
+    fge_ensemble* out = nullptr;
+    guarded([&] {
+        fgs_model_factory f = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(g_reg_mu);
+            auto it = registry().find(model);
+            if (it == registry().end()) throw flamegpu::exception::InvalidArgument(std::string("unknown model ") + model);
+            f = it->second;
+        }
+        auto e = std::make_unique<fge_ensemble>();
+        e->model.reset(static_cast<flamegpu::ModelDescription*>(f(params, nparams)));
+        e->ens = std::make_unique<flamegpu::CUDAEnsemble>(*e->model);
+        e->ens->Config().device = device;
+        e->plans = std::make_unique<flamegpu::RunPlanVector>(*e->model, 0);
+        out = e.release();
+    });
+    return out;
+}
+
+extern "C" void fge_destroy(fge_ensemble* e) { delete e; }
+
+extern "C" int fge_configure(fge_ensemble* e, int32_t batched, int32_t graphs, uint32_t stage) {
+    return guarded([&] {
+        e->ens->Config().batched = batched != 0;
+        e->ens->Config().use_graphs = graphs != 0;
+        e->ens->Config().message_stage_bytes = stage;
+    });
+}
+
+extern "C" int fge_add_run(fge_ensemble* e, uint32_t steps, uint64_t seed, const char* agent, uint32_t n, int32_t nvars,
+                           const char* const* names, const void* const* cols, const char* message, const float* mn,
+                           const float* mx, float radius) {
+    return guarded([&] {
+        flamegpu::RunPlan plan(*e->model);
+        plan.setSteps(steps);
+        plan.setRandomSimulationSeed(seed);
+        if (agent) {
+            flamegpu::AgentVector pop(e->model->Agent(agent), n);
+            for (int32_t k = 0; k < nvars; ++k) {
+                const size_t c = pop.columnIndex(names[k]);
+                std::memcpy(pop.columns()[c].data(), cols[k], pop.columns()[c].size());
+            }
+            plan.setPopulation(pop);
+        }
+        if (message) plan.setSpatialMessageBounds(message, {mn[0], mn[1], mn[2]}, {mx[0], mx[1], mx[2]}, radius);
+        e->plans->push_back(plan);
+    });
+}
+
+extern "C" int fge_set_run_property(fge_ensemble* e, uint32_t run, const char* name, const void* value, size_t bytes) {
+    return guarded([&] {
+        if (run >= e->plans->size()) throw flamegpu::exception::OutOfBoundsException("run out of range");
+        flamegpu::RunPlan& p = (*e->plans)[run];
+        const flamegpu::detail::EnvProperty* prop = e->model->getData()->property(name);
+        if (!prop || prop->value.size() != bytes) throw flamegpu::exception::InvalidEnvProperty(name);
+        if (prop->type == std::type_index(typeid(float))) p.setProperty<float>(name, *static_cast<const float*>(value));
+        else if (prop->type == std::type_index(typeid(double))) p.setProperty<double>(name, *static_cast<const double*>(value));
+        else if (prop->type == std::type_index(typeid(int32_t))) p.setProperty<int32_t>(name, *static_cast<const int32_t*>(value));
+        else if (prop->type == std::type_index(typeid(uint32_t))) p.setProperty<uint32_t>(name, *static_cast<const uint32_t*>(value));
+        else if (prop->type == std::type_index(typeid(uint64_t))) p.setProperty<uint64_t>(name, *static_cast<const uint64_t*>(value));
+        else throw flamegpu::exception::InvalidEnvPropertyType("unsupported property type for the C ABI");
+    });
+}
+
+extern "C" int fge_simulate(fge_ensemble* e, uint32_t* failures) {
+    return guarded([&] {
+        const unsigned int f = e->ens->simulate(*e->plans);
+        if (failures) *failures = f;
+    });
+}
+
+extern "C" int fge_get_count(fge_ensemble* e, uint32_t run, const char* agent, uint32_t* n) {
+    return guarded([&] {
+        flamegpu::AgentVector pop(e->model->Agent(agent));
+        e->ens->getPopulationData(run, pop);
+        *n = pop.size();
+    });
+}
+
+extern "C" int fge_get_variable(fge_ensemble* e, uint32_t run, const char* agent, const char* var, void* out,
+                                size_t bytes) {
+    return guarded([&] {
+        flamegpu::AgentVector pop(e->model->Agent(agent));
+        e->ens->getPopulationData(run, pop);
+        const auto& col = pop.columns()[pop.columnIndex(var)];
+        if (bytes < col.size()) throw flamegpu::exception::InvalidArgument("output buffer too small");
+        std::memcpy(out, col.data(), col.size());
+    });
+}
+
+extern "C" int fge_stats(fge_ensemble* e, double* el, int32_t* batched, uint32_t* kps, uint64_t* gl) {
+    return guarded([&] {
+        if (el) *el = e->ens->getEnsembleElapsedTime();
+        if (batched) *batched = e->ens->lastRunBatched() ? 1 : 0;
+        if (kps) *kps = e->ens->getKernelsPerStep();
+        if (gl) *gl = e->ens->getGraphLaunches();
+    });
+}

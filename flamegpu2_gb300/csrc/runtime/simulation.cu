@@ -29,6 +29,7 @@
 
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu_gb300/fg_capi.h"
+#include "runtime/internal.h"
 
 namespace flamegpu {
 namespace detail {
@@ -84,6 +85,47 @@ int sm_count(int dev) {
 }
 
 }  // namespace
+
+VarTable make_table(const std::vector<TableEntry>& e, const char* what) {
+    VarTable t;
+    std::memset(&t, 0, sizeof(t));
+    const uint32_t n = static_cast<uint32_t>(e.size());
+    uint32_t size = 2;
+    while (size < n) size <<= 1;
+    std::mt19937 rng(12345u);
+    for (; size <= static_cast<uint32_t>(kMaxVarSlots); size <<= 1) {
+        uint32_t bits = 0;
+        while ((1u << bits) < size) ++bits;
+        const uint32_t shift = 32u - bits;
+        for (int attempt = 0; attempt < 200000; ++attempt) {
+            const uint32_t mult = attempt == 0 ? 1u : (rng() | 1u);
+            uint64_t used = 0;
+            bool ok = true;
+            for (const auto& x : e) {
+                const uint32_t s = table_slot(mult, shift, x.hash);
+                if (used & (1ull << s)) {
+                    ok = false;
+                    break;
+                }
+                used |= 1ull << s;
+            }
+            if (!ok) continue;
+            t.mult = mult;
+            t.shift = shift;
+            t.count = n;
+            for (const auto& x : e) {
+                VarSlot& s = t.slot[table_slot(mult, shift, x.hash)];
+                s.ptr = x.ptr;
+                s.stride = x.stride;
+                s.hash = x.hash;
+                s.elem_bytes = x.elem_bytes;
+                s.elements = x.elements;
+            }
+            return t;
+        }
+    }
+    THROW exception::InvalidArgument(format("Too many variables (%u) in one %s for the lookup table", n, what));
+}
 
 struct AgentList {
     AgentData* agent = nullptr;
@@ -423,55 +465,6 @@ struct SimulationImpl {
 
     // ------------------------------------------------------------- tables
 
-    struct TableEntry {
-        uint32_t hash;
-        char* ptr;
-        uint32_t stride;
-        uint32_t elem_bytes;
-        uint32_t elements;
-    };
-
-    static VarTable make_table(const std::vector<TableEntry>& e, const char* what) {
-        VarTable t;
-        std::memset(&t, 0, sizeof(t));
-        const uint32_t n = static_cast<uint32_t>(e.size());
-        uint32_t size = 2;
-        while (size < n) size <<= 1;
-        std::mt19937 rng(12345u);
-        for (; size <= static_cast<uint32_t>(kMaxVarSlots); size <<= 1) {
-            uint32_t bits = 0;
-            while ((1u << bits) < size) ++bits;
-            const uint32_t shift = 32u - bits;
-            for (int attempt = 0; attempt < 200000; ++attempt) {
-                const uint32_t mult = attempt == 0 ? 1u : (rng() | 1u);
-                uint64_t used = 0;
-                bool ok = true;
-                for (const auto& x : e) {
-                    const uint32_t s = table_slot(mult, shift, x.hash);
-                    if (used & (1ull << s)) {
-                        ok = false;
-                        break;
-                    }
-                    used |= 1ull << s;
-                }
-                if (!ok) continue;
-                t.mult = mult;
-                t.shift = shift;
-                t.count = n;
-                for (const auto& x : e) {
-                    VarSlot& s = t.slot[table_slot(mult, shift, x.hash)];
-                    s.ptr = x.ptr;
-                    s.stride = x.stride;
-                    s.hash = x.hash;
-                    s.elem_bytes = x.elem_bytes;
-                    s.elements = x.elements;
-                }
-                return t;
-            }
-        }
-        THROW exception::InvalidArgument(format("Too many variables (%u) in one %s for the lookup table", n, what));
-    }
-
     void build_tables(FnRt& f) {
         AgentList& l = *f.list;
         for (int par = 0; par < 2; ++par) {
@@ -531,7 +524,8 @@ struct SimulationImpl {
             e.clear();
             for (size_t i = 0; i < model->environment.size(); ++i) {
                 const EnvProperty& p = model->environment[i];
-                e.push_back({fnv1a32(p.name), d_env + env_offset[i], 0, p.type_size, p.elements});
+                // offsets into the environment buffer (LaunchParams::env)
+                e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(env_offset[i]), 0, p.type_size, p.elements});
             }
             T->env = make_table(e, "environment");
             f.tables[par].reset(T);
@@ -726,6 +720,7 @@ struct SimulationImpl {
         P.seed = config.random_seed;
         P.fn_uid = f.fn->uid;
         P.error = d_error();
+        P.env = d_env;
         cudaError_t e = cudaSuccess;
         const unsigned int smem = P.stage_bytes ? P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader)) : 0u;
         timed("fn:" + f.fn->name, [&] { e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 16), kAgentBlock, smem, stream); });
@@ -949,6 +944,18 @@ void HostAPI::Environment::set(const std::string& name, const std::type_info& t,
     THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
 }
 
+void HostAPI::Environment::setRaw(const std::string& name, const void* in, size_t size) {
+    for (size_t i = 0; i < sim->model->environment.size(); ++i) {
+        const auto& p = sim->model->environment[i];
+        if (p.name != name) continue;
+        if (p.value.size() != size) THROW exception::InvalidEnvPropertyType(format("Environment property '%s' has another size", name.c_str()));
+        std::memcpy(sim->env_host.data() + sim->env_offset[i], in, size);
+        sim->env_dirty = true;
+        return;
+    }
+    THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+}
+
 unsigned int HostAPI::AgentAPI::count() const {
     detail::AgentList* l = sim->list_of(agent, state);
     uint32_t c = 0;
@@ -1132,6 +1139,36 @@ void CUDASimulation::setPopulationDevice(const std::string& agent, const std::st
                             cudaMemcpyHostToDevice, impl->stream));
     FG_CUDA(cudaStreamSynchronize(impl->stream));
     l->bound = n;
+}
+
+void CUDASimulation::setSpatialMessageBounds(const std::string& message, const std::vector<float>& mn,
+                                             const std::vector<float>& mx, float radius) {
+    detail::MsgList* m = impl->msg_of(message);
+    if (!m || !m->spatial()) THROW exception::InvalidMessageName(format("No spatial message '%s'", message.c_str()));
+    const int dims = m->grid.dims;
+    if (static_cast<int>(mn.size()) < dims || static_cast<int>(mx.size()) < dims)
+        THROW exception::InvalidArgument("Spatial bounds need one value per dimension");
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    fg_spatial_grid g{};
+    if (fg_spatial_grid_init(&g, dims, mn.data(), mx.data(), radius) != FG_OK)
+        THROW exception::InvalidArgument(format("Invalid bounds/radius for message '%s'", message.c_str()));
+    m->grid = g;
+    impl->mem.release(m->pbm);
+    m->pbm_alloc = (g.binCount + 1u + 3u) & ~3u;
+    m->pbm = static_cast<uint32_t*>(impl->mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(m->pbm_alloc) + 4)));
+    if (m->capacity) {
+        impl->mem.release(m->build_ws);
+        m->build_ws_bytes = fg_spatial_build_workspace_size(m->capacity, g.binCount);
+        m->build_ws = impl->mem.alloc(m->build_ws_bytes);
+    }
+    for (auto& l : impl->lists) {
+        auto it = l->sort_ws.find(m);
+        if (it != l->sort_ws.end()) {
+            impl->mem.release(it->second.first);
+            l->sort_ws.erase(it);
+        }
+    }
+    impl->invalidate();
 }
 
 const unsigned int* CUDASimulation::getDeviceCount(const std::string& agent, const std::string& state) {

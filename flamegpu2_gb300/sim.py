@@ -215,3 +215,89 @@ class Simulation:
                 label, ms, cnt = rec.rsplit(",", 2)
                 out[label] = (float(ms), int(cnt))
         return out
+
+
+ENSEMBLE_EXPORTS = ["fge_create", "fge_destroy", "fge_configure", "fge_add_run", "fge_set_run_property",
+                    "fge_simulate", "fge_get_count", "fge_get_variable", "fge_stats"]
+_ens_ready = False
+
+
+def _ens():
+    global _ens_ready
+    L = core()
+    if not _ens_ready:
+        vp, u32, i32, sz = C.c_void_p, C.c_uint32, C.c_int32, C.c_size_t
+        L.fge_create.argtypes = [C.c_char_p, C.POINTER(C.c_double), i32, i32]
+        L.fge_create.restype = vp
+        L.fge_destroy.argtypes = [vp]
+        L.fge_configure.argtypes = [vp, i32, i32, u32]
+        L.fge_add_run.argtypes = [vp, u32, C.c_uint64, C.c_char_p, u32, i32, C.POINTER(C.c_char_p), C.POINTER(vp),
+                                  C.c_char_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float]
+        L.fge_set_run_property.argtypes = [vp, u32, C.c_char_p, vp, sz]
+        L.fge_simulate.argtypes = [vp, C.POINTER(u32)]
+        L.fge_get_count.argtypes = [vp, u32, C.c_char_p, C.POINTER(u32)]
+        L.fge_get_variable.argtypes = [vp, u32, C.c_char_p, C.c_char_p, vp, sz]
+        L.fge_stats.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(i32), C.POINTER(u32), C.POINTER(C.c_uint64)]
+        _ens_ready = True
+    return L
+
+
+class Ensemble:
+    """CUDAEnsemble of a registered model: runs are added, then simulated together."""
+
+    def __init__(self, model: str, params=(), device: int = 0, batched: bool = True, use_graphs: bool = True,
+                 stage_bytes: int = 96 * 1024):
+        L = _ens()
+        arr = (C.c_double * max(1, len(params)))(*[float(p) for p in params])
+        self._h = L.fge_create(model.encode(), arr, len(params), device)
+        if not self._h:
+            raise SimError(L.fgs_last_error().decode())
+        _check(L.fge_configure(self._h, int(batched), int(use_graphs), stage_bytes))
+        self.runs = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _ens().fge_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_run(self, steps: int, seed: int, agent: str, n: int, columns: dict, message=None, mn=None, mx=None,
+                radius: float = 0.0) -> int:
+        names = list(columns)
+        arrs = [np.ascontiguousarray(columns[k]) for k in names]
+        cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        cp = (C.c_void_p * max(1, len(names)))(*[a.ctypes.data for a in arrs])
+        f3 = lambda v: (C.c_float * 3)(*(list(v) + [0.0] * (3 - len(v)))) if v is not None else None
+        _check(_ens().fge_add_run(self._h, steps, seed, agent.encode(), n, len(names), cn, cp,
+                                  message.encode() if message else None, f3(mn), f3(mx), float(radius)))
+        self.runs += 1
+        return self.runs - 1
+
+    def set_property(self, run: int, name: str, value, ctype=C.c_float):
+        v = ctype(value)
+        _check(_ens().fge_set_run_property(self._h, run, name.encode(), C.byref(v), C.sizeof(v)))
+
+    def simulate(self) -> int:
+        f = C.c_uint32()
+        _check(_ens().fge_simulate(self._h, C.byref(f)))
+        return f.value
+
+    def count(self, run: int, agent: str) -> int:
+        n = C.c_uint32()
+        _check(_ens().fge_get_count(self._h, run, agent.encode(), C.byref(n)))
+        return n.value
+
+    def get(self, run: int, agent: str, var: str, dtype) -> np.ndarray:
+        out = np.zeros(self.count(run, agent), dtype=dtype)
+        _check(_ens().fge_get_variable(self._h, run, agent.encode(), var.encode(), out.ctypes.data, out.nbytes))
+        return out
+
+    def stats(self) -> dict:
+        el, b, k, g = C.c_double(), C.c_int32(), C.c_uint32(), C.c_uint64()
+        _check(_ens().fge_stats(self._h, C.byref(el), C.byref(b), C.byref(k), C.byref(g)))
+        return {"elapsed_s": el.value, "batched": bool(b.value), "kernels_per_step": k.value, "graph_launches": g.value}

@@ -68,3 +68,18 @@ def birth_death_population(n: int, seed: int) -> dict:
     for v in range(8):
         pop[f"f{v}"] = uniform(seed, v, n, 0.0, 1.0)
     return pop
+
+
+def ensemble_instances(count: int, seed: int = 1000, n_lo: int = 1024, n_hi: int = 1 << 20):
+    """Boids ensemble instances: population log-uniform in [n_lo, n_hi], radius
+    uniform in [1, 4], domain edge 4 r cbrt(N / 64) rounded up to a whole number
+    of radii (so the wrapped iterator's radius divides the width)."""
+    out = []
+    for i in range(count):
+        u = float((bits(seed + i, 0, 1) >> np.uint64(11))[0]) / 9007199254740992.0
+        n = int(round(np.exp(np.log(n_lo) + u * (np.log(n_hi) - np.log(n_lo)))))
+        r = float(uniform(seed + i, 1, 1, 1.0, 4.0)[0])
+        cells = int(np.ceil(4.0 * np.cbrt(n / 64.0)))
+        edge = float(np.float32(r) * np.float32(cells))
+        out.append({"n": n, "radius": r, "edge": edge, "seed": seed + i})
+    return out

@@ -71,6 +71,32 @@ struct FunctionTables {
     VarTable env;        // environment properties (ptr -> value bytes)
 };
 
+/** One instance of a batched launch (device array, LaunchParams::batch). Rows
+ * [row_begin, row_begin + row_capacity) of every column belong to it; its
+ * input messages' PBM is pbm + in_bucket_begin. */
+struct BatchInstanceRT {
+    uint32_t row_begin;
+    uint32_t row_capacity;
+    uint32_t in_bucket_begin;
+    uint32_t step_offset;   // the instance's step = launch step - step_offset
+    fg_spatial_grid in_grid;
+    const char* env;        // the instance's environment buffer
+    uint64_t seed;
+};
+
+/** What an agent function's block needs about the instance it runs for; in
+ * shared memory, filled at the start of every grid-stride round. */
+struct InstanceCtx {
+    fg_spatial_grid grid;   // message input grid
+    const uint32_t* pbm;    // PBM of the instance's input messages
+    uint32_t pbm_alloc;     // PBM entries readable from pbm
+    uint32_t step;
+    const char* env;        // environment buffer
+    uint64_t seed;
+    uint32_t row_begin;     // first row of the instance
+    uint32_t count;         // agents in the instance
+};
+
 /** Header of the shared-memory staging window of one block (spatial input). */
 struct StageHeader {
     uint32_t rec_lo;   // first staged sorted message index
@@ -128,6 +154,11 @@ struct LaunchParams {
     uint64_t seed;               // simulation random seed
     uint32_t fn_uid;             // unique id of this agent function (random streams)
     uint32_t* error;             // device error record: [code, hash, index, count]
+    const char* env;             // environment buffer (env table pointers are offsets into it)
+    // batched launch (null batch: a single simulation)
+    const BatchInstanceRT* batch;
+    const uint32_t* batch_counts;
+    uint32_t batch_n;
 };
 
 }  // namespace detail

@@ -8,4 +8,5 @@
 #include "flamegpu/model/ModelDescription.h"
 #include "flamegpu/simulation/AgentVector.h"
 #include "flamegpu/simulation/CUDASimulation.h"
+#include "flamegpu/simulation/CUDAEnsemble.h"
 #endif  // INCLUDE_FLAMEGPU_FLAMEGPU_H_

@@ -30,21 +30,78 @@ typedef cudaError_t (*AgentFunctionLauncher)(const LaunchParams& p, unsigned int
 constexpr unsigned int kAgentBlock = 128;
 
 #ifdef __CUDACC__
+// Instance of row `row` in a batched launch (instances ordered by row_begin).
+__device__ __forceinline__ uint32_t batch_find(const BatchInstanceRT* b, uint32_t n, uint32_t row) {
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&b[mid].row_begin) <= row)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Fill the block's instance context for rows starting at `base`. Single
+// simulations take it from the launch; batched launches from the instance
+// owning `base` (instance segments start at multiples of kAgentBlock, so a
+// block never straddles two instances).
+__device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, uint32_t n_single) {
+    if (threadIdx.x != 0) return;
+    InstanceCtx& c = ctx();
+    if (!P.batch) {
+        c.grid = P.in_grid;
+        c.pbm = P.in_pbm;
+        c.pbm_alloc = P.in_pbm_alloc;
+        c.step = P.d_step ? *P.d_step : 0u;
+        c.env = P.env;
+        c.seed = P.seed;
+        c.row_begin = 0;
+        c.count = n_single;
+        return;
+    }
+    const uint32_t k = batch_find(P.batch, P.batch_n, base);
+    const BatchInstanceRT& I = P.batch[k];
+    c.grid = I.in_grid;
+    c.pbm = P.in_pbm ? P.in_pbm + I.in_bucket_begin : nullptr;
+    // each instance's PBM slice reserves binCount + 1 entries rounded up to 4
+    c.pbm_alloc = (I.in_grid.binCount + 1u + 3u) & ~3u;
+    c.step = (P.d_step ? *P.d_step : 0u) - I.step_offset;
+    c.env = I.env;
+    c.seed = I.seed;
+    c.row_begin = I.row_begin;
+    c.count = __ldg(P.batch_counts + k);
+}
+
 template <typename F>
 __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __grid_constant__ LaunchParams P) {
     using MsgIn = typename F::MessageIn;
     using MsgOut = typename F::MessageOut;
-    const uint32_t n = P.d_n ? min(*P.d_n, P.max_n) : P.max_n;
+    // rows to visit: the population (single) or every row of the batch
+    const uint32_t n = P.batch ? P.max_n : (P.d_n ? min(*P.d_n, P.max_n) : P.max_n);
     if (P.msg_out_count && blockIdx.x == 0 && threadIdx.x == 0) *P.msg_out_count = n;
     constexpr int kDims = std::is_same<MsgIn, MessageSpatial3D>::value ? 3 : (std::is_same<MsgIn, MessageSpatial2D>::value ? 2 : 0);
     bool first = true;
+    if (!P.batch) {
+        fill_ctx(P, 0, n);
+        __syncthreads();
+    }
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        if (P.batch) {
+            __syncthreads();  // the previous round is done with the context
+            fill_ctx(P, base, 0);
+            __syncthreads();
+        }
         const uint32_t idx = base + threadIdx.x;
+        // rows past the instance's count are padding (batched) / past the population (single)
+        const uint32_t limit = P.batch ? ctx().row_begin + ctx().count : n;
+        const uint32_t live = idx < limit ? idx : 0xFFFFFFFFu;
         if constexpr (kDims != 0) {
-            if (P.stage_bytes) stage_window<kDims>(P, idx, n, first);
+            if (P.stage_bytes) stage_window<kDims>(P, idx, live != 0xFFFFFFFFu, first);
         }
         first = false;
-        if (idx >= n) continue;
+        if (live == 0xFFFFFFFFu) continue;
         DeviceAPI<MsgIn, MsgOut> api(P, idx);
         const AGENT_STATUS st = F()(&api);
         if (P.death_flags) {

@@ -38,6 +38,12 @@ __device__ __forceinline__ void device_error(const LaunchParams& P, uint32_t cod
     }
 }
 
+// The calling block's instance context (shared memory).
+__device__ __forceinline__ InstanceCtx& ctx() {
+    __shared__ InstanceCtx c;
+    return c;
+}
+
 // Address of element `elem` of variable `hash` in row `row` of table `t`.
 // Returns null (after recording a device error) when seatbelts are on and the
 // name, the type size or the array index is wrong.
@@ -50,7 +56,7 @@ __device__ __forceinline__ T* var_addr(const LaunchParams& P, const VarTable* __
     char* base = vs->ptr;
     const uint32_t stride = vs->stride;
 #if FLAMEGPU_SEATBELTS
-    if (vs->hash != hash || base == nullptr) {
+    if (vs->hash != hash) {
         device_error(P, kDevUnknownVariable, hash, row);
         return nullptr;
     }
@@ -146,7 +152,7 @@ __device__ __forceinline__ uint32_t pbm_at(const LaunchParams& P, uint32_t h) {
         const uint32_t r = h - s->pbm_lo;
         if (r < s->pbm_n) return stage_pbm()[r];
     }
-    return __ldg(P.in_pbm + h);
+    return __ldg(ctx().pbm + h);
 }
 
 // Read of a variable of message `index` of the input list: staged copy when
@@ -216,7 +222,7 @@ __device__ __forceinline__ bool stage_wait(StageHeader* h, uint32_t phase) {
 // a contiguous range of the sorted records, copied with TMA bulk copies
 // (cp.async.bulk) completing on an mbarrier. All threads of the block call it.
 template <int DIMS>
-__device__ void stage_window(const LaunchParams& P, uint32_t idx, uint32_t n, bool first) {
+__device__ void stage_window(const LaunchParams& P, uint32_t idx, bool active, bool first) {
     __shared__ uint32_t s_min, s_max;
     StageHeader* h = stage_hdr();
     if (threadIdx.x == 0) {
@@ -229,8 +235,8 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, uint32_t n, bo
         }
     }
     uint32_t key = 0xFFFFFFFFu, kmax = 0u;
-    if (idx < n) {
-        const fg_spatial_grid& g = P.in_grid;
+    if (active) {
+        const fg_spatial_grid& g = ctx().grid;
         const float x = read_rw<float>(P, &P.T.agent, VarName("x").hash, idx);
         const float y = read_rw<float>(P, &P.T.agent, VarName("y").hash, idx);
         const float z = DIMS == 3 ? read_rw<float>(P, &P.T.agent, VarName("z").hash, idx) : 0.0f;
@@ -256,19 +262,26 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, uint32_t n, bo
         h->rec_lo = 0;
         h->pbm_lo = 0;
         if (s_min != 0xFFFFFFFFu) {
-            const fg_spatial_grid& g = P.in_grid;
+            const fg_spatial_grid& g = ctx().grid;
+            const uint32_t* pbm = ctx().pbm;
             const uint32_t B = g.binCount;
             const uint32_t span = DIMS == 3 ? g.gridDim[0] * g.gridDim[1] + g.gridDim[0] + 1u : g.gridDim[0] + 1u;
             const uint32_t hlo = s_min > span ? s_min - span : 0u;
             const uint32_t hhi = (s_max + span < B) ? s_max + span : B - 1u;
             const uint32_t plo = hlo & ~3u;
             uint32_t pend = (hhi + 2u + 3u) & ~3u;
-            if (pend > P.in_pbm_alloc) pend = P.in_pbm_alloc;
+            if (pend > ctx().pbm_alloc) pend = ctx().pbm_alloc;
             const uint32_t pn = pend - plo;
-            const uint32_t rlo = __ldg(P.in_pbm + hlo), rhi = __ldg(P.in_pbm + hhi + 1u);
+            const uint32_t rlo = __ldg(pbm + hlo), rhi = __ldg(pbm + hhi + 1u);
             const size_t pbytes = static_cast<size_t>(pn) * 4u;
             const size_t rbytes = static_cast<size_t>(rhi - rlo) * P.in_record_bytes;
-            if (pbytes + rbytes <= P.stage_bytes && pn > 0) {
+            // bulk copies need 16-byte aligned addresses and sizes; anything else
+            // (a caller's layout mistake) is not staged: reads then go to HBM
+            const bool aligned = ((pbytes | rbytes) & 15u) == 0 &&
+                                 (reinterpret_cast<uintptr_t>(pbm + plo) & 15u) == 0 &&
+                                 (reinterpret_cast<uintptr_t>(P.in_records) & 15u) == 0 &&
+                                 (P.in_record_bytes & 15u) == 0;
+            if (aligned && pbytes + rbytes <= P.stage_bytes && pn > 0) {
                 h->pbm_lo = plo;
                 h->pbm_n = pn;
                 h->rec_lo = rlo;
@@ -292,7 +305,7 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, uint32_t n, bo
                     }
                 };
                 char* base = dyn_smem() + sizeof(StageHeader);
-                copy(base, reinterpret_cast<const char*>(P.in_pbm + plo), pbytes);
+                copy(base, reinterpret_cast<const char*>(pbm + plo), pbytes);
                 if (rbytes) copy(base + pbytes, P.in_records + static_cast<size_t>(rlo) * P.in_record_bytes, rbytes);
             }
         }
@@ -479,7 +492,9 @@ struct Window {
     uint32_t rec_lo = 0, rec_n = 0, pbm_lo = 0, pbm_n = 0;
     const char* rec = nullptr;
     const uint32_t* pbm = nullptr;
+    const uint32_t* gpbm = nullptr;  // the instance's PBM in HBM
     __device__ void load(const detail::LaunchParams& P) {
+        gpbm = detail::ctx().pbm;
         if (!P.stage_bytes) return;
         const detail::StageHeader* h = detail::stage_hdr();
         rec_lo = h->rec_lo;
@@ -491,7 +506,7 @@ struct Window {
     }
     __device__ uint32_t pbm_at(const detail::LaunchParams& P, uint32_t h) const {
         const uint32_t r = h - pbm_lo;
-        return r < pbm_n ? pbm[r] : __ldg(P.in_pbm + h);
+        return r < pbm_n ? pbm[r] : __ldg(gpbm + h);
     }
     __device__ const char* row(const detail::LaunchParams& P, uint32_t index) const {
         const uint32_t r = index - rec_lo;
@@ -536,10 +551,11 @@ class SpatialIn {
                     const int ry = DIMS == 3 ? s / 3 - 1 : s - 1;
                     const int rz = DIMS == 3 ? s % 3 - 1 : 0;
                     const int ay = F.cell[1] + ry, az = F.cell[2] + rz;
-                    if (ay < 0 || ay >= static_cast<int>(F.P.in_grid.gridDim[1])) continue;
-                    if (DIMS == 3 && (az < 0 || az >= static_cast<int>(F.P.in_grid.gridDim[2]))) continue;
-                    const uint32_t h0 = detail::grid_hash(F.P.in_grid, F.cell[0] - 1, ay, az);
-                    const uint32_t h1 = detail::grid_hash(F.P.in_grid, F.cell[0] + 1, ay, az);
+                    const fg_spatial_grid& g = detail::ctx().grid;
+                    if (ay < 0 || ay >= static_cast<int>(g.gridDim[1])) continue;
+                    if (DIMS == 3 && (az < 0 || az >= static_cast<int>(g.gridDim[2]))) continue;
+                    const uint32_t h0 = detail::grid_hash(g, F.cell[0] - 1, ay, az);
+                    const uint32_t h1 = detail::grid_hash(g, F.cell[0] + 1, ay, az);
                     const uint32_t b = F.win.pbm_at(F.P, h0), e = F.win.pbm_at(F.P, h1 + 1);
                     if (b < e) {
                         m.index = b;
@@ -558,9 +574,10 @@ class SpatialIn {
             loc[0] = x;
             loc[1] = y;
             loc[2] = z;
-            cell[0] = detail::grid_cell(p.in_grid, 0, x);
-            cell[1] = detail::grid_cell(p.in_grid, 1, y);
-            cell[2] = DIMS == 3 ? detail::grid_cell(p.in_grid, 2, z) : 0;
+            const fg_spatial_grid& gc = detail::ctx().grid;
+            cell[0] = detail::grid_cell(gc, 0, x);
+            cell[1] = detail::grid_cell(gc, 1, y);
+            cell[2] = DIMS == 3 ? detail::grid_cell(gc, 2, z) : 0;
             win.load(p);
         }
         __device__ iterator begin() const { return iterator(*this, 0); }
@@ -582,13 +599,13 @@ class SpatialIn {
             __device__ float getVirtualY() const { return getVirtualY(F->loc[1]); }
             __device__ float getVirtualZ() const { return getVirtualZ(F->loc[2]); }
             __device__ float getVirtualX(float x1) const {
-                return detail::virtual_coord(x1, getVariable<float>("x"), P.in_grid.width[0]);
+                return detail::virtual_coord(x1, getVariable<float>("x"), detail::ctx().grid.width[0]);
             }
             __device__ float getVirtualY(float y1) const {
-                return detail::virtual_coord(y1, getVariable<float>("y"), P.in_grid.width[1]);
+                return detail::virtual_coord(y1, getVariable<float>("y"), detail::ctx().grid.width[1]);
             }
             __device__ float getVirtualZ(float z1) const {
-                return detail::virtual_coord(z1, getVariable<float>("z"), P.in_grid.width[2]);
+                return detail::virtual_coord(z1, getVariable<float>("z"), detail::ctx().grid.width[2]);
             }
 
          private:
@@ -640,12 +657,13 @@ class SpatialIn {
             loc[0] = x;
             loc[1] = y;
             loc[2] = z;
-            cell[0] = detail::grid_cell(p.in_grid, 0, x);
-            cell[1] = detail::grid_cell(p.in_grid, 1, y);
-            cell[2] = DIMS == 3 ? detail::grid_cell(p.in_grid, 2, z) : 0;
+            const fg_spatial_grid& gc = detail::ctx().grid;
+            cell[0] = detail::grid_cell(gc, 0, x);
+            cell[1] = detail::grid_cell(gc, 1, y);
+            cell[2] = DIMS == 3 ? detail::grid_cell(gc, 2, z) : 0;
             // wrapped coordinates of the offsets -1, 0, +1 on each axis (modulo gridDim,
             // MessageSpatial3DDevice.cuh:736-738), pre-multiplied into hash terms.
-            const fg_spatial_grid& g = p.in_grid;
+            const fg_spatial_grid& g = detail::ctx().grid;
             auto wrapc = [](int c, int r, uint32_t d) {
                 return static_cast<uint32_t>(c + r + static_cast<int>(d)) % d;
             };
@@ -676,13 +694,13 @@ class SpatialIn {
     };
 
     __device__ explicit SpatialIn(const detail::LaunchParams& p) : P(p) {}
-    __device__ float radius() const { return P.in_grid.radius; }
+    __device__ float radius() const { return detail::ctx().grid.radius; }
 
  protected:
     // MessageSpatial3D::In::wrap seatbelts (MessageSpatial3DDevice.cuh:527-549)
     __device__ bool wrap_ok(float x, float y, float z) const {
 #if FLAMEGPU_SEATBELTS
-        const fg_spatial_grid& g = P.in_grid;
+        const fg_spatial_grid& g = detail::ctx().grid;
         bool out = x > g.max[0] || y > g.max[1] || x < g.min[0] || y < g.min[1];
         if (DIMS == 3) out = out || z > g.max[2] || z < g.min[2];
         if (out) {
@@ -705,7 +723,7 @@ class MessageSpatial2D {
         __device__ explicit In(const detail::LaunchParams& p) : SpatialIn<2>(p) {}
         __device__ Filter operator()(float x, float y) const { return Filter(P, x, y, 0.0f); }
         __device__ WrapFilter wrap(float x, float y) const {
-            if (!wrap_ok(x, y, 0.0f)) return WrapFilter(P, P.in_grid.min[0], P.in_grid.min[1], 0.0f);
+            if (!wrap_ok(x, y, 0.0f)) return WrapFilter(P, detail::ctx().grid.min[0], detail::ctx().grid.min[1], 0.0f);
             return WrapFilter(P, x, y, 0.0f);
         }
     };
@@ -728,7 +746,7 @@ class MessageSpatial3D {
         __device__ explicit In(const detail::LaunchParams& p) : SpatialIn<3>(p) {}
         __device__ Filter operator()(float x, float y, float z) const { return Filter(P, x, y, z); }
         __device__ WrapFilter wrap(float x, float y, float z) const {
-            if (!wrap_ok(x, y, z)) return WrapFilter(P, P.in_grid.min[0], P.in_grid.min[1], P.in_grid.min[2]);
+            if (!wrap_ok(x, y, z)) return WrapFilter(P, detail::ctx().grid.min[0], detail::ctx().grid.min[1], detail::ctx().grid.min[2]);
             return WrapFilter(P, x, y, z);
         }
     };
@@ -749,13 +767,16 @@ class MessageSpatial3D {
 class DeviceEnvironment {
  public:
     __device__ explicit DeviceEnvironment(const detail::LaunchParams& p) : P(p) {}
+    // env table pointers are offsets into the instance's environment buffer
     template <typename T>
     __device__ T getProperty(detail::VarName name) const {
-        return detail::read_ro<T>(P, &P.T.env, name.hash, 0);
+        const T* off = detail::var_addr<T>(P, &P.T.env, name.hash, 0, 0);
+        return detail::ldg_any(reinterpret_cast<const T*>(detail::ctx().env + reinterpret_cast<size_t>(off)));
     }
     template <typename T, flamegpu::size_type N>
     __device__ T getProperty(detail::VarName name, unsigned int i) const {
-        return detail::read_ro<T>(P, &P.T.env, name.hash, 0, i);
+        const T* off = detail::var_addr<T>(P, &P.T.env, name.hash, 0, i);
+        return detail::ldg_any(reinterpret_cast<const T*>(detail::ctx().env + reinterpret_cast<size_t>(off)));
     }
 
  private:
@@ -782,7 +803,7 @@ class AgentRandom {
 
  private:
     __device__ uint64_t next() const {
-        const uint64_t key = detail::mix64(P.seed ^ (static_cast<uint64_t>(P.fn_uid) << 40) ^ *P.d_step);
+        const uint64_t key = detail::mix64(detail::ctx().seed ^ (static_cast<uint64_t>(P.fn_uid) << 40) ^ detail::ctx().step);
         return detail::mix64(detail::mix64(key + index) + (counter++));
     }
     const detail::LaunchParams& P;
@@ -910,8 +931,8 @@ class DeviceAPI {
         detail::write_var<T>(P, &P.T.agent, name.hash, index, value, i);
     }
     __device__ id_t getID() const { return detail::read_rw<id_t>(P, &P.T.agent, detail::VarName("_id").hash, index); }
-    __device__ unsigned int getStepCounter() const { return *P.d_step; }
-    __device__ unsigned int getIndex() const { return index; }
+    __device__ unsigned int getStepCounter() const { return detail::ctx().step; }
+    __device__ unsigned int getIndex() const { return index - detail::ctx().row_begin; }
 
     typename MessageIn::In message_in;
     typename MessageOut::Out message_out;

@@ -43,6 +43,9 @@ class HostAPI {
             return old;
         }
 
+        /** Set a property from raw bytes (size checked). */
+        void setRaw(const std::string& name, const void* value, size_t size);
+
      private:
         void get(const std::string& name, const std::type_info& t, size_t size, void* out) const;
         void set(const std::string& name, const std::type_info& t, size_t size, const void* in);
@@ -128,6 +131,10 @@ class CUDASimulation {
     unsigned int getAgentCount(const std::string& agent, const std::string& state = "default");
     /** Device pointer to the current column of an agent variable (valid until the next step). */
     void* getDeviceVariable(const std::string& agent, const std::string& variable, const std::string& state = "default");
+    /** Override the bounds and radius of a spatial message list before stepping
+     *  (per-run spatial grids of an ensemble). */
+    void setSpatialMessageBounds(const std::string& message, const std::vector<float>& min,
+                                 const std::vector<float>& max, float radius);
     /** Replace a state list's population from device columns (every variable,
      *  including _id, n rows each); the agent type's next id becomes next_id. */
     void setPopulationDevice(const std::string& agent, const std::string& state, unsigned int n,

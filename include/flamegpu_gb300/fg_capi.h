@@ -160,6 +160,48 @@ size_t fg_scan_workspace_size(uint32_t n);
 int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n,
                           void* workspace, size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------- batches */
+
+/* One instance of a batch: many simulations of one model, concatenated.
+ * Rows [row_begin, row_begin + row_capacity) of every column belong to the
+ * instance; rows at or past its count (fg_*_batched `counts`) are padding.
+ * Its buckets are [bucket_begin, bucket_begin + nbuckets + 1): its own bins
+ * (or sort buckets) plus one bucket that collects its padding rows, so a
+ * single counting sort over the batch leaves every instance in its segment
+ * and instance i's PBM is pbm[bucket_begin .. bucket_begin + binCount]. */
+typedef struct fg_batch_instance {
+    fg_spatial_grid grid;    /* the instance's message grid */
+    uint32_t row_begin;
+    uint32_t row_capacity;
+    uint32_t bucket_begin;
+    uint32_t nbuckets;       /* bins (build) or 2^bits sort buckets (sort); set by fg_batch_instance_init */
+    /* sort key data derived from the grid (CUDASimulation.cu:494-507,569-571) */
+    float sort_width[3];
+    uint32_t sort_gd[3];
+    uint32_t sort_mask;
+    uint32_t pad;
+} fg_batch_instance;
+
+/* Fill an instance record (host). mode 0: message build buckets (binCount),
+ * mode 1: automatic-sort buckets (2^bits). Returns the bucket count the
+ * instance needs including its padding bucket in *nbuckets_total. */
+int fg_batch_instance_init(fg_batch_instance* inst, const fg_spatial_grid* grid, uint32_t row_begin,
+                           uint32_t row_capacity, uint32_t bucket_begin, int32_t mode, uint32_t* nbuckets_total);
+size_t fg_batched_workspace_size(uint32_t total_rows, uint32_t total_buckets);
+
+/* fg_spatial_build over a batch: `instances` (device, ninst records, ordered
+ * by row_begin) and `counts` (device, messages per instance); valid flags are
+ * optional as in fg_spatial_build. Rows are the concatenated message columns. */
+int fg_spatial_build_batched(const fg_batch_instance* instances, const uint32_t* counts, uint32_t ninst,
+                             uint32_t total_rows, uint32_t total_buckets, const float* x, const float* y,
+                             const float* z, int32_t dims, const uint32_t* valid, const fg_record_desc* rec,
+                             uint32_t* sorted, uint32_t* pbm, void* workspace, size_t workspace_bytes, void* stream);
+/* fg_spatial_sort_agents over a batch (sort buckets, mode 1 instances). */
+int fg_spatial_sort_agents_batched(const fg_batch_instance* instances, const uint32_t* counts, uint32_t ninst,
+                                   uint32_t total_rows, uint32_t total_buckets, const float* x, const float* y,
+                                   const float* z, int32_t dims, const fg_column* cols, uint32_t ncols,
+                                   void* workspace, size_t workspace_bytes, void* stream);
+
 /* Last CUDA error seen by this library on the calling thread (cudaError_t). */
 int fg_last_cuda_error(void);
 /* Library version string. */

@@ -77,6 +77,27 @@ int fgs_take_profile(fgs_sim* sim, char* buf, size_t len);
 /* getElapsedTimeSteps (seconds) for up to cap steps; returns the count in *n. */
 int fgs_step_times(fgs_sim* sim, double* out, uint32_t cap, uint32_t* n);
 
+/* ------------------------------------------------------------ ensembles
+ * CUDAEnsemble::simulate(RunPlanVector) (include/flamegpu/simulation/CUDAEnsemble.h:129)
+ * of a registered model; runs are added one by one. */
+typedef struct fge_ensemble fge_ensemble;
+fge_ensemble* fge_create(const char* model, const double* params, int32_t nparams, int32_t device);
+void fge_destroy(fge_ensemble* e);
+/* EnsembleConfig: batched (one batched simulation when the model allows it), graphs, staging bytes. */
+int fge_configure(fge_ensemble* e, int32_t batched, int32_t use_graphs, uint32_t stage_bytes);
+/* Adds a RunPlan: steps, seed, initial population of `agent` (named host columns,
+ * n rows) and, if message != NULL, that spatial message's bounds and radius for the run. */
+int fge_add_run(fge_ensemble* e, uint32_t steps, uint64_t seed, const char* agent, uint32_t n, int32_t nvars,
+                const char* const* names, const void* const* host_cols, const char* message, const float* min,
+                const float* max, float radius);
+int fge_set_run_property(fge_ensemble* e, uint32_t run, const char* name, const void* value, size_t bytes);
+/* Runs every plan; *failures receives the number of failed runs. */
+int fge_simulate(fge_ensemble* e, uint32_t* failures);
+int fge_get_count(fge_ensemble* e, uint32_t run, const char* agent, uint32_t* n);
+int fge_get_variable(fge_ensemble* e, uint32_t run, const char* agent, const char* var, void* out, size_t bytes);
+int fge_stats(fge_ensemble* e, double* elapsed_s, int32_t* batched, uint32_t* kernels_per_step,
+              uint64_t* graph_launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -272,3 +272,98 @@ def test_compact_agents_parity(n, with_births):
                                       np.arange(n + 1, n + 1 + len(kids), dtype=np.uint32))
     assert int(next_id.item()) == n + 1 + len(kids)
     assert ws.status() == 0
+
+
+# ------------------------------------------------------------------ batches
+
+def _batch(mode, specs, rows_align=128):
+    """specs: list of (grid, count, capacity). Returns (instances array, total rows, total buckets)."""
+    capi = _capi()
+    arr = (capi.BatchInstance * len(specs))()
+    row, bucket = 0, 0
+    for k, (g, count, cap) in enumerate(specs):
+        nb = C.c_uint32()
+        capi.check(capi.lib().fg_batch_instance_init(C.byref(arr[k]), C.byref(g), row, cap, bucket, mode, C.byref(nb)),
+                   "fg_batch_instance_init")
+        row += cap
+        bucket += nb.value
+    return arr, row, bucket
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims", [3, 2])
+def test_batched_build_matches_each_instance(dims):
+    import torch
+    capi = _capi()
+    rng = np.random.default_rng(40 + dims)
+    specs, pos_list, grids = [], [], []
+    for k, (count, r, edge) in enumerate([(1000, 1.0, 10.0), (0, 2.0, 8.0), (5000, 3.0, 33.0), (37, 1.5, 4.5),
+                                          (20000, 2.5, 60.0)]):
+        cap = (count + 127) // 128 * 128 + 128
+        g = capi.grid(dims, (0.0,) * dims, (edge,) * dims, r)
+        grids.append(g)
+        specs.append((g, count, cap))
+        pos_list.append(_positions(rng, count, (0.0,) * dims, (edge,) * dims, "clusters" if k % 2 else "uniform"))
+    inst, total_rows, total_buckets = _batch(0, specs)
+    pos = np.zeros((total_rows, dims), np.float32)
+    for (g, count, cap), p, i in zip(specs, pos_list, inst):
+        pos[i.row_begin:i.row_begin + count] = p
+    counts = torch.tensor([c for _, c, _ in specs], dtype=torch.int32, device="cuda")
+    d_inst = torch.frombuffer(bytearray(bytes(inst)), dtype=torch.uint8).cuda()
+    cols = [torch.from_numpy(np.ascontiguousarray(pos[:, a])).cuda() for a in range(dims)]
+    payload = torch.arange(total_rows, dtype=torch.int32, device="cuda") * 3 + 1
+    rec = capi.record_desc(cols + [payload])
+    srt = torch.zeros((total_rows, rec.words), dtype=torch.int32, device="cuda")
+    pbm = torch.zeros(total_buckets + 1, dtype=torch.int32, device="cuda")
+    ws = capi.Workspace(capi.lib().fg_batched_workspace_size(total_rows, total_buckets))
+    for _ in range(2):
+        capi.check(capi.lib().fg_spatial_build_batched(
+            d_inst.data_ptr(), counts.data_ptr(), len(specs), total_rows, total_buckets, cols[0].data_ptr(),
+            cols[1].data_ptr(), cols[2].data_ptr() if dims == 3 else None, dims, None, C.byref(rec), srt.data_ptr(),
+            pbm.data_ptr(), ws.ptr, ws.nbytes, capi.stream_handle()), "fg_spatial_build_batched")
+    torch.cuda.synchronize()
+    assert ws.status() == 0
+    pbm_h = pbm.cpu().numpy().view(np.uint32)
+    srt_h = srt.cpu().numpy().view(np.uint32)
+    pay_h = payload.cpu().numpy()
+    for (g, count, cap), p, i in zip(specs, pos_list, inst):
+        og = O.grid(dims, (0.0,) * dims, list(g.max)[:dims], g.radius)
+        epbm, eperm, _ = O.spatial_build(og, *[p[:, a] for a in range(dims)])
+        got = pbm_h[i.bucket_begin:i.bucket_begin + g.binCount + 1] - i.row_begin
+        np.testing.assert_array_equal(got, epbm)
+        rows = i.row_begin + eperm
+        np.testing.assert_array_equal(srt_h[i.row_begin:i.row_begin + count, dims].view(np.int32), pay_h[rows])
+
+
+@pytest.mark.gpu
+def test_batched_sort_matches_each_instance():
+    import torch
+    capi = _capi()
+    rng = np.random.default_rng(9)
+    specs, pos_list = [], []
+    for k, (count, r, edge) in enumerate([(3000, 2.0, 64.0), (10, 1.0, 5.0), (9000, 4.0, 40.0)]):
+        cap = (count + 127) // 128 * 128
+        g = capi.grid(3, (0.0,) * 3, (edge,) * 3, r)
+        specs.append((g, count, cap))
+        pos_list.append(_positions(rng, count, (0.0,) * 3, (edge,) * 3, "outside"))
+    inst, total_rows, total_buckets = _batch(1, specs)
+    pos = np.zeros((total_rows, 3), np.float32)
+    for (g, count, cap), p, i in zip(specs, pos_list, inst):
+        pos[i.row_begin:i.row_begin + count] = p
+    counts = torch.tensor([c for _, c, _ in specs], dtype=torch.int32, device="cuda")
+    d_inst = torch.frombuffer(bytearray(bytes(inst)), dtype=torch.uint8).cuda()
+    ins = [torch.from_numpy(np.ascontiguousarray(pos[:, a])).cuda() for a in range(3)]
+    ids = torch.arange(total_rows, dtype=torch.int32, device="cuda")
+    outs = [torch.empty_like(c) for c in ins] + [torch.empty_like(ids)]
+    colarr = capi.columns(list(zip(ins + [ids], outs)))
+    ws = capi.Workspace(capi.lib().fg_batched_workspace_size(total_rows, total_buckets))
+    capi.check(capi.lib().fg_spatial_sort_agents_batched(
+        d_inst.data_ptr(), counts.data_ptr(), len(specs), total_rows, total_buckets, ins[0].data_ptr(),
+        ins[1].data_ptr(), ins[2].data_ptr(), 3, colarr, 4, ws.ptr, ws.nbytes, capi.stream_handle()), "sort_batched")
+    torch.cuda.synchronize()
+    got_ids = outs[3].cpu().numpy()
+    for (g, count, cap), p, i in zip(specs, pos_list, inst):
+        og = O.grid(3, (0.0,) * 3, list(g.max)[:3], g.radius)
+        keys = O.sort_keys(og, p[:, 0], p[:, 1], p[:, 2])
+        eperm = O.stable_sort_perm(keys, O.sort_max_bit(og))
+        np.testing.assert_array_equal(got_ids[i.row_begin:i.row_begin + count], i.row_begin + eperm)
