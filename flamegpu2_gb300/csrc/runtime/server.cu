@@ -1,0 +1,184 @@
+// SimulationServer: continuous batching of simulation runs over CUDASimulation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "flamegpu/simulation/CUDASimulation.h"
+#include "flamegpu/simulation/SimulationServer.h"
+
+namespace flamegpu {
+
+struct SimulationServer::Job {
+    uint64_t id = 0;
+    std::shared_ptr<ModelDescription> model;
+    std::vector<std::pair<std::string, AgentVector>> populations;
+    unsigned int steps = 0;
+    uint64_t seed = 0;
+    double arrival = 0, admitted = 0;
+    unsigned int issued = 0;
+    size_t bytes = 0;
+    std::unique_ptr<CUDASimulation> sim;
+    cudaEvent_t done = nullptr;
+    ~Job() {
+        if (done) cudaEventDestroy(done);
+    }
+};
+
+SimulationServer::SimulationServer() : SimulationServer(Config()) {}
+
+SimulationServer::SimulationServer(const Config& c) : cfg(c), t0(std::chrono::steady_clock::now()) {}
+
+SimulationServer::~SimulationServer() {
+    // let in-flight work finish before the simulations free their buffers
+    for (auto& j : running)
+        if (j->sim) cudaStreamSynchronize(j->sim->getStream());
+}
+
+double SimulationServer::now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+size_t SimulationServer::queued() const { return queue.size(); }
+size_t SimulationServer::active() const { return running.size(); }
+size_t SimulationServer::reservedBytes() const { return reserved; }
+
+size_t SimulationServer::estimateBytes(const ModelDescription& model,
+                                       const std::vector<std::pair<std::string, AgentVector>>& pops) {
+    const auto& m = *model.getData();
+    size_t total = 32ull << 20, max_pop = 1024;
+    for (const auto& a : m.agents) {
+        size_t n = 1024;
+        for (const auto& p : pops)
+            if (p.first == a->name) n = std::max<size_t>(n, p.second.size());
+        bool births = false;
+        for (const auto& f : a->functions) births = births || !f->agent_output.empty();
+        size_t row = 0;
+        for (const auto& v : a->variables) row += v.bytes();
+        // ping-pong columns, sort/compaction scratch; births may grow the list fourfold
+        total += n * (2 * row + 24) * (births ? 4 : 1);
+        max_pop = std::max(max_pop, n * (births ? 4 : 1));
+    }
+    for (const auto& msg : m.messages) {
+        size_t row = 0;
+        for (const auto& v : msg->variables) row += (v.bytes() + 3) & ~size_t(3);
+        total += max_pop * (2 * row + 32);  // columns, sorted records, build scratch
+        if (msg->kind != detail::MessageKind::BruteForce) {
+            double bins = 1.0;
+            const int dims = msg->kind == detail::MessageKind::Spatial3D ? 3 : 2;
+            for (int d = 0; d < dims; ++d) bins *= std::ceil((msg->max[d] - msg->min[d]) / msg->radius);
+            total += static_cast<size_t>(bins) * 16;  // histogram, PBM, scan
+        }
+    }
+    return total;
+}
+
+uint64_t SimulationServer::submit(std::shared_ptr<ModelDescription> model,
+                                  std::vector<std::pair<std::string, AgentVector>> pops, unsigned int steps,
+                                  uint64_t seed) {
+    auto j = std::make_unique<Job>();
+    j->id = next_id++;
+    j->model = std::move(model);
+    j->populations = std::move(pops);
+    j->steps = steps;
+    j->seed = seed;
+    j->arrival = now();
+    j->bytes = estimateBytes(*j->model, j->populations);
+    const uint64_t id = j->id;
+    queue.push_back(std::move(j));
+    return id;
+}
+
+void SimulationServer::retire(Job& j, bool failed, const std::string& error) {
+    Result r;
+    r.id = j.id;
+    r.arrival_s = j.arrival;
+    r.admitted_s = j.admitted;
+    r.steps = j.steps;
+    r.reserved_bytes = j.bytes;
+    r.failed = failed;
+    r.error = error;
+    if (!failed && j.sim) {
+        try {
+            for (const auto& a : j.model->getData()->agents)
+                for (const auto& st : a->states) {
+                    auto pop = std::make_shared<AgentVector>(AgentDescription(j.model->getData(), a.get()));
+                    j.sim->getPopulationData(*pop, st);
+                    r.populations[{a->name, st}] = pop;
+                }
+        } catch (const exception::FLAMEGPUException& e) {
+            r.failed = true;
+            r.error = std::string(e.exception_type()) + ": " + e.what();
+        }
+    }
+    r.completed_s = now();
+    j.sim.reset();
+    reserved -= j.bytes;
+    completed.push_back(std::move(r));
+}
+
+size_t SimulationServer::poll() {
+    // 1. retire runs whose last step has completed (non-blocking test)
+    for (size_t k = 0; k < running.size();) {
+        Job& j = *running[k];
+        if (j.issued >= j.steps && j.done && cudaEventQuery(j.done) == cudaSuccess) {
+            retire(j, false, "");
+            running.erase(running.begin() + static_cast<long>(k));
+        } else {
+            ++k;
+        }
+    }
+    // 2. admit queued runs in arrival order while a slot and the budget allow
+    while (!queue.empty() && running.size() < cfg.max_active &&
+           (reserved + queue.front()->bytes <= cfg.memory_budget || running.empty())) {
+        std::unique_ptr<Job> j = std::move(queue.front());
+        queue.pop_front();
+        j->admitted = now();
+        reserved += j->bytes;
+        try {
+            j->sim = std::make_unique<CUDASimulation>(*j->model);
+            j->sim->CUDAConfig().device_id = cfg.device;
+            j->sim->CUDAConfig().use_graphs = cfg.use_graphs;
+            j->sim->SimulationConfig().random_seed = j->seed;
+            j->sim->SimulationConfig().steps = j->steps;
+            for (auto& p : j->populations) j->sim->setPopulationData(p.second);
+            j->populations.clear();
+            if (cudaEventCreateWithFlags(&j->done, cudaEventDisableTiming) != cudaSuccess)
+                throw exception::CUDAError("cudaEventCreate failed");
+            running.push_back(std::move(j));
+        } catch (const exception::FLAMEGPUException& e) {
+            retire(*j, true, std::string(e.exception_type()) + ": " + e.what());
+        }
+    }
+    // 3. issue the next steps of every active run (each on its own stream)
+    for (size_t k = 0; k < running.size();) {
+        Job& j = *running[k];
+        try {
+            for (unsigned int s = 0; s < cfg.steps_per_poll && j.issued < j.steps; ++s) {
+                j.sim->step();
+                ++j.issued;
+                if (j.issued == j.steps && cudaEventRecord(j.done, j.sim->getStream()) != cudaSuccess)
+                    throw exception::CUDAError("cudaEventRecord failed");
+            }
+            ++k;
+        } catch (const exception::FLAMEGPUException& e) {
+            // failure isolation: this run completes with its error, the others go on
+            retire(j, true, std::string(e.exception_type()) + ": " + e.what());
+            running.erase(running.begin() + static_cast<long>(k));
+        }
+    }
+    return queue.size() + running.size();
+}
+
+void SimulationServer::runUntilIdle() {
+    while (poll()) {
+    }
+}
+
+std::vector<SimulationServer::Result> SimulationServer::takeCompleted() {
+    std::vector<Result> out;
+    out.swap(completed);
+    return out;
+}
+
+}  // namespace flamegpu

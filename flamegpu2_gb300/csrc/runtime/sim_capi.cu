@@ -375,3 +375,148 @@ extern "C" int fge_stats(fge_ensemble* e, double* el, int32_t* batched, uint32_t
         if (gl) *gl = e->ens->getGraphLaunches();
     });
 }
+
+// ------------------------------------------------------------------- server
+
+struct fgv_server {
+    std::unique_ptr<flamegpu::SimulationServer> server;
+    // model descriptions shared by the runs that asked for the same (model, params)
+    std::map<std::pair<std::string, std::vector<double>>, std::shared_ptr<flamegpu::ModelDescription>> models;
+    std::map<uint64_t, flamegpu::SimulationServer::Result> results;
+    std::vector<uint64_t> pending;  // completed ids not yet handed out
+};
+
+namespace {
+
+const flamegpu::SimulationServer::Result& result_of(fgv_server* v, uint64_t id) {
+    auto it = v->results.find(id);
+    if (it == v->results.end()) throw flamegpu::exception::InvalidArgument("no completed run with id " + std::to_string(id));
+    return it->second;
+}
+
+const flamegpu::AgentVector& result_population(fgv_server* v, uint64_t id, const char* agent, const char* state) {
+    const auto& r = result_of(v, id);
+    if (r.failed) throw flamegpu::exception::InvalidArgument("run " + std::to_string(id) + " failed: " + r.error);
+    auto it = r.populations.find({agent, state ? state : "default"});
+    if (it == r.populations.end()) throw flamegpu::exception::InvalidAgentName(std::string("no population ") + agent);
+    return *it->second;
+}
+
+}  // namespace
+
+extern "C" fgv_server* fgv_create(int32_t device, uint64_t budget, uint32_t max_active, uint32_t steps_per_poll,
+                                  int32_t graphs) {
+    fgv_server* out = nullptr;
+    guarded([&] {
+        flamegpu::SimulationServer::Config c;
+        c.device = device;
+        if (budget) c.memory_budget = budget;
+        if (max_active) c.max_active = max_active;
+        if (steps_per_poll) c.steps_per_poll = steps_per_poll;
+        c.use_graphs = graphs != 0;
+        auto v = std::make_unique<fgv_server>();
+        v->server = std::make_unique<flamegpu::SimulationServer>(c);
+        out = v.release();
+    });
+    return out;
+}
+
+extern "C" void fgv_destroy(fgv_server* v) { delete v; }
+
+extern "C" int fgv_submit(fgv_server* v, const char* model, const double* params, int32_t nparams, uint32_t steps,
+                          uint64_t seed, int32_t npops, const char* const* agents, const uint32_t* counts,
+                          const int32_t* nvars, const char* const* names, const void* const* cols, uint64_t* id) {
+    return guarded([&] {
+        const auto key = std::make_pair(std::string(model), std::vector<double>(params, params + std::max(nparams, 0)));
+        auto& m = v->models[key];
+        if (!m) {
+            fgs_model_factory f = nullptr;
+            {
+                std::lock_guard<std::mutex> lk(g_reg_mu);
+                auto it = registry().find(model);
+                if (it == registry().end())
+                    throw flamegpu::exception::InvalidArgument(std::string("unknown model ") + model);
+                f = it->second;
+            }
+            m.reset(static_cast<flamegpu::ModelDescription*>(f(params, nparams)));
+        }
+        std::vector<std::pair<std::string, flamegpu::AgentVector>> pops;
+        int32_t c = 0;
+        for (int32_t k = 0; k < npops; ++k) {
+            flamegpu::AgentVector pop(m->Agent(agents[k]), counts[k]);
+            for (int32_t j = 0; j < nvars[k]; ++j, ++c) {
+                const size_t col = pop.columnIndex(names[c]);
+                std::memcpy(pop.columns()[col].data(), cols[c], pop.columns()[col].size());
+            }
+            pops.emplace_back(agents[k], std::move(pop));
+        }
+        const uint64_t rid = v->server->submit(m, std::move(pops), steps, seed);
+        if (id) *id = rid;
+    });
+}
+
+extern "C" int fgv_poll(fgv_server* v, uint32_t* remaining) {
+    return guarded([&] {
+        const size_t r = v->server->poll();
+        if (remaining) *remaining = static_cast<uint32_t>(r);
+    });
+}
+
+extern "C" int fgv_run_until_idle(fgv_server* v) { return guarded([&] { v->server->runUntilIdle(); }); }
+
+extern "C" int fgv_take_completed(fgv_server* v, uint64_t* ids, uint32_t cap, uint32_t* n) {
+    return guarded([&] {
+        auto& pending = v->pending;
+        for (auto& r : v->server->takeCompleted()) {
+            pending.push_back(r.id);
+            v->results.emplace(r.id, std::move(r));
+        }
+        uint32_t k = 0;
+        while (k < cap && k < pending.size()) {
+            ids[k] = pending[k];
+            ++k;
+        }
+        pending.erase(pending.begin(), pending.begin() + k);
+        if (n) *n = k;
+    });
+}
+
+extern "C" int fgv_result_info(fgv_server* v, uint64_t id, double* t, int32_t* failed, char* err, size_t len) {
+    return guarded([&] {
+        const auto& r = result_of(v, id);
+        if (t) {
+            t[0] = r.arrival_s;
+            t[1] = r.admitted_s;
+            t[2] = r.completed_s;
+        }
+        if (failed) *failed = r.failed ? 1 : 0;
+        if (err && len) {
+            std::strncpy(err, r.error.c_str(), len - 1);
+            err[len - 1] = 0;
+        }
+    });
+}
+
+extern "C" int fgv_result_count(fgv_server* v, uint64_t id, const char* agent, const char* state, uint32_t* n) {
+    return guarded([&] { *n = result_population(v, id, agent, state).size(); });
+}
+
+extern "C" int fgv_result_variable(fgv_server* v, uint64_t id, const char* agent, const char* state, const char* var,
+                                   void* out, size_t bytes) {
+    return guarded([&] {
+        const auto& pop = result_population(v, id, agent, state);
+        const auto& col = pop.columns()[pop.columnIndex(var)];
+        if (bytes < col.size()) throw flamegpu::exception::InvalidArgument("output buffer too small");
+        std::memcpy(out, col.data(), col.size());
+    });
+}
+
+extern "C" int fgv_release(fgv_server* v, uint64_t id) { return guarded([&] { v->results.erase(id); }); }
+
+extern "C" int fgv_stats(fgv_server* v, uint32_t* q, uint32_t* a, uint64_t* r) {
+    return guarded([&] {
+        if (q) *q = static_cast<uint32_t>(v->server->queued());
+        if (a) *a = static_cast<uint32_t>(v->server->active());
+        if (r) *r = v->server->reservedBytes();
+    });
+}

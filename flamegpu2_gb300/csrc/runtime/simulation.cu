@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -54,26 +55,46 @@ namespace {
 __global__ void k_step_increment(uint32_t* d_step) { *d_step += 1; }
 __global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
 
+// Device buffers of one simulation, taken stream-ordered from the device's
+// default memory pool: a finished simulation returns its memory without
+// stalling the other simulations of the process (cudaFree would wait for the
+// whole device), and a later one reuses it without a new mapping.
 struct DevMem {
     std::vector<void*> ptrs;
+    cudaStream_t stream = nullptr;  // the owning simulation's stream
+    static void keep_pool(int device) {
+        static std::once_flag once[64];
+        if (device < 0 || device >= 64) return;
+        std::call_once(once[device], [device] {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
+            uint64_t keep = ~0ull;  // freed blocks stay in the pool for the next simulation
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        });
+    }
     void* alloc(size_t bytes, bool zero = true) {
         void* p = nullptr;
-        FG_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 256)));
-        if (zero) FG_CUDA(cudaMemset(p, 0, std::max<size_t>(bytes, 256)));
+        const size_t n = std::max<size_t>(bytes, 256);
+        FG_CUDA(cudaMallocAsync(&p, n, stream));
         ptrs.push_back(p);
+        if (zero) FG_CUDA(cudaMemsetAsync(p, 0, n, stream));
+        // host copies into the buffer may follow on other streams
+        FG_CUDA(cudaStreamSynchronize(stream));
         return p;
     }
     void release(void* p) {
         if (!p) return;
         auto it = std::find(ptrs.begin(), ptrs.end(), p);
         if (it != ptrs.end()) {
-            cudaFree(p);
+            cudaFreeAsync(p, stream);  // after the stream's pending work on it
             ptrs.erase(it);
         }
     }
-    ~DevMem() {
-        for (void* p : ptrs) cudaFree(p);
+    void release_all() {
+        for (void* p : ptrs) cudaFreeAsync(p, stream);
+        ptrs.clear();
     }
+    ~DevMem() { release_all(); }
 };
 
 uint32_t round4(uint32_t b) { return (b + 3u) & ~3u; }
@@ -227,11 +248,19 @@ struct SimulationImpl {
 
     explicit SimulationImpl(const std::shared_ptr<ModelData>& m) : model(m) {}
     ~SimulationImpl() {
+        if (stream) {
+            cudaStreamSynchronize(stream);
+            mem.release_all();
+            cudaStreamSynchronize(stream);
+        }
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         for (auto& e : step_events) {
             cudaEventDestroy(e.first);
             cudaEventDestroy(e.second);
         }
+        for (auto& c : count_ring)
+            if (c.ev) cudaEventDestroy(c.ev);
+        if (count_pinned) cudaFreeHost(count_pinned);
         if (h_pinned) cudaFreeHost(h_pinned);
         if (fork_ev) cudaEventDestroy(fork_ev);
         if (join_ev) cudaEventDestroy(join_ev);
@@ -268,6 +297,8 @@ struct SimulationImpl {
         sms = sm_count(device);
         FG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         FG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        DevMem::keep_pool(device);
+        mem.stream = stream;
         FG_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
         FG_CUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
         FG_CUDA(cudaMallocHost(&h_pinned, 4096));
@@ -541,41 +572,101 @@ struct SimulationImpl {
 
     // Capacity check before a step: births can at most double a list per
     // birth function. Synchronises only if the bound could exceed capacity.
-    void prepare_capacity() {
-        std::vector<uint64_t> bound(lists.size());
-        for (size_t i = 0; i < lists.size(); ++i) bound[i] = lists[i]->bound;
-        bool over = false;
-        for (const auto& layer : model->layers)
-            for (auto* fd : layer->functions) {
-                for (auto& f : fns)
-                    if (f.fn == fd && f.births) {
-                        const size_t li = static_cast<size_t>(std::find_if(lists.begin(), lists.end(), [&](auto& p) { return p.get() == f.list; }) - lists.begin());
-                        bound[li] *= 2;
-                        if (bound[li] > f.list->capacity) over = true;
-                    }
-            }
-        if (!over) {
-            for (size_t i = 0; i < lists.size(); ++i) lists[i]->bound = static_cast<uint32_t>(std::min<uint64_t>(bound[i], 0xFFFFFFFFu));
-            return;
-        }
-        // exact counts, then grow what needs it
-        sync_counts();
-        for (size_t i = 0; i < lists.size(); ++i) bound[i] = lists[i]->bound;
+    // Births can at most double a list per birth function and step. The check
+    // starts from the newest population counts the device has already reported
+    // (copied to pinned memory after every step, tagged by an event), so a
+    // birth model synchronises only when even that bound could overflow.
+    struct CountSlot {
+        unsigned int step_after = 0;
+        cudaEvent_t ev = nullptr;
+        uint32_t* host = nullptr;
+        bool used = false;
+    };
+    std::vector<CountSlot> count_ring;
+    size_t count_next = 0;
+    uint32_t* count_pinned = nullptr;
+
+    int births_per_step(const AgentList* l) const {
+        int b = 0;
         for (const auto& layer : model->layers)
             for (auto* fd : layer->functions)
-                for (auto& f : fns)
-                    if (f.fn == fd && f.births) {
-                        const size_t li = static_cast<size_t>(std::find_if(lists.begin(), lists.end(), [&](auto& p) { return p.get() == f.list; }) - lists.begin());
-                        bound[li] *= 2;
-                    }
-        for (size_t i = 0; i < lists.size(); ++i) {
-            if (bound[i] > lists[i]->capacity) {
-                if (bound[i] >= (1ull << 31)) THROW exception::OutOfMemory("Population bound exceeds 2^31 agents");
-                ensure_capacity(*lists[i], static_cast<uint32_t>(std::max<uint64_t>(bound[i], 2ull * lists[i]->capacity)), lists[i]->bound);
-            }
-            lists[i]->bound = static_cast<uint32_t>(bound[i]);
+                for (const auto& f : fns)
+                    if (f.fn == fd && f.births && f.list == l) ++b;
+        return b;
+    }
+    bool any_births() const {
+        for (const auto& f : fns)
+            if (f.births) return true;
+        return false;
+    }
+    static uint64_t grow_bound(uint64_t base, int doublings) {
+        for (int d = 0; d < doublings && base < (1ull << 33); ++d) base *= 2;
+        return base;
+    }
+
+    // Populations were replaced from the host: earlier reports no longer apply.
+    void forget_counts() {
+        for (auto& c : count_ring) {
+            if (c.used) cudaEventSynchronize(c.ev);
+            c.used = false;
         }
-        ensure_all_allocated();
+    }
+
+    void record_counts() {
+        if (!any_births()) return;
+        if (count_ring.empty()) {
+            FG_CUDA(cudaMallocHost(&count_pinned, sizeof(uint32_t) * lists.size() * 4));
+            count_ring.resize(4);
+            for (size_t k = 0; k < 4; ++k) {
+                FG_CUDA(cudaEventCreateWithFlags(&count_ring[k].ev, cudaEventDisableTiming));
+                count_ring[k].host = count_pinned + k * lists.size();
+            }
+        }
+        CountSlot& c = count_ring[count_next];
+        count_next = (count_next + 1) % count_ring.size();
+        if (c.used) FG_CUDA(cudaEventSynchronize(c.ev));  // never overwrite a copy in flight
+        for (size_t i = 0; i < lists.size(); ++i)
+            FG_CUDA(cudaMemcpyAsync(c.host + i, lists[i]->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        FG_CUDA(cudaEventRecord(c.ev, stream));
+        c.step_after = step_count + 1;
+        c.used = true;
+    }
+
+    void prepare_capacity() {
+        if (!any_births()) return;
+        // newest reported counts
+        const CountSlot* known = nullptr;
+        for (size_t k = 0; k < count_ring.size(); ++k) {
+            const CountSlot& c = count_ring[k];
+            if (!c.used || (known && c.step_after <= known->step_after)) continue;
+            if (cudaEventQuery(c.ev) == cudaSuccess) known = &c;
+        }
+        std::vector<uint64_t> bound(lists.size());
+        bool over = false;
+        for (size_t i = 0; i < lists.size(); ++i) {
+            const int b = births_per_step(lists[i].get());
+            if (known && known->step_after <= step_count) {
+                const unsigned int pending = step_count - known->step_after;  // steps issued after the report
+                bound[i] = grow_bound(std::min<uint64_t>(known->host[i], lists[i]->bound), b * static_cast<int>(pending + 1));
+            } else {
+                bound[i] = grow_bound(lists[i]->bound, b);
+            }
+            if (bound[i] > lists[i]->capacity) over = true;
+        }
+        if (over) {
+            // exact counts after every issued step, then grow what needs it
+            sync_counts();
+            for (size_t i = 0; i < lists.size(); ++i) {
+                bound[i] = grow_bound(lists[i]->bound, births_per_step(lists[i].get()));
+                if (bound[i] > lists[i]->capacity) {
+                    if (bound[i] >= (1ull << 31)) THROW exception::OutOfMemory("Population bound exceeds 2^31 agents");
+                    const uint64_t want = std::max<uint64_t>(2 * bound[i], 2ull * lists[i]->capacity);
+                    ensure_capacity(*lists[i], static_cast<uint32_t>(std::min<uint64_t>(want, (1ull << 31) - 1)), lists[i]->bound);
+                }
+            }
+            ensure_all_allocated();
+        }
+        for (size_t i = 0; i < lists.size(); ++i) lists[i]->bound = static_cast<uint32_t>(std::min<uint64_t>(bound[i], 0xFFFFFFFFu));
     }
 
     void sync_counts() {
@@ -858,6 +949,7 @@ struct SimulationImpl {
         }
         FG_CUDA(cudaEventRecord(e1, stream));
         step_events.emplace_back(e0, e1);
+        record_counts();
         ++step_count;
         if (!model->step_functions.empty()) {
             FG_CUDA(cudaStreamSynchronize(stream));
@@ -1019,6 +1111,7 @@ void CUDASimulation::setPopulationData(AgentVector& pop, const std::string& stat
     }
     FG_CUDA(cudaMemcpy(l->d_count, &n, sizeof(uint32_t), cudaMemcpyHostToDevice));
     l->bound = n;
+    impl->forget_counts();
     impl->ensure_all_allocated();
 }
 
@@ -1139,6 +1232,7 @@ void CUDASimulation::setPopulationDevice(const std::string& agent, const std::st
                             cudaMemcpyHostToDevice, impl->stream));
     FG_CUDA(cudaStreamSynchronize(impl->stream));
     l->bound = n;
+    impl->forget_counts();
 }
 
 void CUDASimulation::setSpatialMessageBounds(const std::string& message, const std::vector<float>& mn,

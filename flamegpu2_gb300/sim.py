@@ -301,3 +301,122 @@ class Ensemble:
         el, b, k, g = C.c_double(), C.c_int32(), C.c_uint32(), C.c_uint64()
         _check(_ens().fge_stats(self._h, C.byref(el), C.byref(b), C.byref(k), C.byref(g)))
         return {"elapsed_s": el.value, "batched": bool(b.value), "kernels_per_step": k.value, "graph_launches": g.value}
+
+
+SERVER_EXPORTS = ["fgv_create", "fgv_destroy", "fgv_submit", "fgv_poll", "fgv_run_until_idle", "fgv_take_completed",
+                  "fgv_result_info", "fgv_result_count", "fgv_result_variable", "fgv_release", "fgv_stats"]
+_srv_ready = False
+
+
+def _srv():
+    global _srv_ready
+    L = core()
+    if not _srv_ready:
+        vp, u32, i32, sz, u64 = C.c_void_p, C.c_uint32, C.c_int32, C.c_size_t, C.c_uint64
+        L.fgv_create.argtypes = [i32, u64, u32, u32, i32]
+        L.fgv_create.restype = vp
+        L.fgv_destroy.argtypes = [vp]
+        L.fgv_submit.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), i32, u32, u64, i32, C.POINTER(C.c_char_p),
+                                 C.POINTER(u32), C.POINTER(i32), C.POINTER(C.c_char_p), C.POINTER(vp), C.POINTER(u64)]
+        L.fgv_poll.argtypes = [vp, C.POINTER(u32)]
+        L.fgv_run_until_idle.argtypes = [vp]
+        L.fgv_take_completed.argtypes = [vp, C.POINTER(u64), u32, C.POINTER(u32)]
+        L.fgv_result_info.argtypes = [vp, u64, C.POINTER(C.c_double), C.POINTER(i32), C.c_char_p, sz]
+        L.fgv_result_count.argtypes = [vp, u64, C.c_char_p, C.c_char_p, C.POINTER(u32)]
+        L.fgv_result_variable.argtypes = [vp, u64, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
+        L.fgv_release.argtypes = [vp, u64]
+        L.fgv_stats.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u64)]
+        _srv_ready = True
+    return L
+
+
+class Server:
+    """SimulationServer: runs of registered models submitted as requests and
+    advanced together (continuous batching) under a device-memory budget."""
+
+    def __init__(self, device: int = 0, memory_budget: int = 150 << 30, max_active: int = 64,
+                 steps_per_poll: int = 1, use_graphs: bool = True):
+        L = _srv()
+        self._h = L.fgv_create(device, memory_budget, max_active, steps_per_poll, int(use_graphs))
+        if not self._h:
+            raise SimError(L.fgs_last_error().decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _srv().fgv_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, model: str, params, steps: int, seed: int, populations: dict) -> int:
+        """populations: {agent: (n, {var: host array})}; returns the run id."""
+        agents = list(populations)
+        names, cols, keep = [], [], []
+        counts, nvars = [], []
+        for a in agents:
+            n, columns = populations[a]
+            counts.append(int(n))
+            nvars.append(len(columns))
+            for k, v in columns.items():
+                arr = np.ascontiguousarray(v)
+                keep.append(arr)
+                names.append(k.encode())
+                cols.append(arr.ctypes.data)
+        k = max(1, len(agents))
+        m = max(1, len(names))
+        arr = (C.c_double * max(1, len(params)))(*[float(p) for p in params])
+        rid = C.c_uint64()
+        _check(_srv().fgv_submit(self._h, model.encode(), arr, len(params), steps, seed, len(agents),
+                                 (C.c_char_p * k)(*[a.encode() for a in agents]), (C.c_uint32 * k)(*counts),
+                                 (C.c_int32 * k)(*nvars), (C.c_char_p * m)(*names), (C.c_void_p * m)(*cols),
+                                 C.byref(rid)))
+        return rid.value
+
+    def poll(self) -> int:
+        r = C.c_uint32()
+        _check(_srv().fgv_poll(self._h, C.byref(r)))
+        return r.value
+
+    def run_until_idle(self):
+        _check(_srv().fgv_run_until_idle(self._h))
+
+    def take_completed(self) -> list[int]:
+        out = []
+        buf = (C.c_uint64 * 256)()
+        n = C.c_uint32()
+        while True:
+            _check(_srv().fgv_take_completed(self._h, buf, 256, C.byref(n)))
+            out += list(buf[:n.value])
+            if n.value < 256:
+                return out
+
+    def info(self, rid: int) -> dict:
+        t = (C.c_double * 3)()
+        f = C.c_int32()
+        err = C.create_string_buffer(1024)
+        _check(_srv().fgv_result_info(self._h, rid, t, C.byref(f), err, 1024))
+        return {"arrival_s": t[0], "admitted_s": t[1], "completed_s": t[2], "failed": bool(f.value),
+                "error": err.value.decode()}
+
+    def count(self, rid: int, agent: str, state: str = "default") -> int:
+        n = C.c_uint32()
+        _check(_srv().fgv_result_count(self._h, rid, agent.encode(), state.encode(), C.byref(n)))
+        return n.value
+
+    def get(self, rid: int, agent: str, var: str, dtype, state: str = "default") -> np.ndarray:
+        out = np.zeros(self.count(rid, agent, state), dtype=dtype)
+        _check(_srv().fgv_result_variable(self._h, rid, agent.encode(), state.encode(), var.encode(),
+                                          out.ctypes.data, out.nbytes))
+        return out
+
+    def release(self, rid: int):
+        _check(_srv().fgv_release(self._h, rid))
+
+    def stats(self) -> dict:
+        q, a, r = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        _check(_srv().fgv_stats(self._h, C.byref(q), C.byref(a), C.byref(r)))
+        return {"queued": q.value, "active": a.value, "reserved_bytes": r.value}

@@ -70,6 +70,18 @@ def birth_death_population(n: int, seed: int) -> dict:
     return pop
 
 
+def predprey_population(n_prey: int, n_pred: int, edge: float, seed: int):
+    """Prey and predators uniform in [0, edge)^2; ids 1..n per agent type."""
+    hi = np.nextafter(np.float32(edge), np.float32(0))
+    prey = {"_id": np.arange(1, n_prey + 1, dtype=np.uint32),
+            "x": np.minimum(uniform(seed, 10, n_prey, 0.0, edge), hi),
+            "y": np.minimum(uniform(seed, 11, n_prey, 0.0, edge), hi)}
+    pred = {"_id": np.arange(1, n_pred + 1, dtype=np.uint32),
+            "x": np.minimum(uniform(seed, 12, n_pred, 0.0, edge), hi),
+            "y": np.minimum(uniform(seed, 13, n_pred, 0.0, edge), hi)}
+    return prey, pred
+
+
 def ensemble_instances(count: int, seed: int = 1000, n_lo: int = 1024, n_hi: int = 1 << 20):
     """Boids ensemble instances: population log-uniform in [n_lo, n_hi], radius
     uniform in [1, 4], domain edge 4 r cbrt(N / 64) rounded up to a whole number

@@ -9,4 +9,5 @@
 #include "flamegpu/simulation/AgentVector.h"
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu/simulation/CUDAEnsemble.h"
+#include "flamegpu/simulation/SimulationServer.h"
 #endif  // INCLUDE_FLAMEGPU_FLAMEGPU_H_

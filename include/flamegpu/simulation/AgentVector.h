@@ -103,6 +103,7 @@ class AgentVector {
     const char* column(const std::string& name) const;
     size_t columnIndex(const std::string& name) const;
     std::vector<std::vector<char>>& columns() { return cols; }
+    const std::vector<std::vector<char>>& columns() const { return cols; }
     void setCountRaw(flamegpu::size_type n);
 
  private:

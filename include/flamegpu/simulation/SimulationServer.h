@@ -1,0 +1,87 @@
+#ifndef INCLUDE_FLAMEGPU_SIMULATION_SIMULATIONSERVER_H_
+#define INCLUDE_FLAMEGPU_SIMULATION_SIMULATIONSERVER_H_
+// A request loop over CUDASimulation (GB300 extension; FLAME GPU 2 has no
+// server): simulation runs of any registered model arrive as requests, are
+// admitted while a slot and the device-memory budget allow, keep their agent
+// and message state resident in HBM, and advance together — every poll issues
+// the next step of every admitted run on that run's own stream, so their
+// kernels overlap on the device, and runs that arrive meanwhile join at the
+// next poll (continuous batching). A finished run is read back and its memory
+// returned without waiting for the others; a run that fails is completed with
+// its error and the others carry on.
+#include <chrono>
+#include <cstdint>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "flamegpu/model/ModelDescription.h"
+#include "flamegpu/simulation/AgentVector.h"
+
+namespace flamegpu {
+
+class CUDASimulation;
+
+class SimulationServer {
+ public:
+    struct Config {
+        size_t memory_budget = 150ull << 30;  // bytes of device memory runs may reserve
+        unsigned int max_active = 64;         // runs on the device at once
+        unsigned int steps_per_poll = 1;      // steps issued per run per poll
+        int device = 0;
+        bool use_graphs = true;
+    };
+    struct Result {
+        uint64_t id = 0;
+        double arrival_s = 0, admitted_s = 0, completed_s = 0;  // seconds since the server started
+        unsigned int steps = 0;
+        bool failed = false;
+        std::string error;
+        size_t reserved_bytes = 0;
+        std::map<std::pair<std::string, std::string>, std::shared_ptr<AgentVector>> populations;
+    };
+
+    SimulationServer();
+    explicit SimulationServer(const Config& cfg);
+    ~SimulationServer();
+    SimulationServer(const SimulationServer&) = delete;
+    SimulationServer& operator=(const SimulationServer&) = delete;
+
+    /** Queues a run of `model` from the given initial populations (agent name,
+     *  population in the agent's initial state); returns its id. */
+    uint64_t submit(std::shared_ptr<ModelDescription> model,
+                    std::vector<std::pair<std::string, AgentVector>> populations, unsigned int steps, uint64_t seed);
+    /** One scheduling round: retire finished runs, admit queued ones, issue
+     *  the next steps of the active ones. Returns runs still queued or active. */
+    size_t poll();
+    /** Polls until every submitted run has completed. */
+    void runUntilIdle();
+    /** Completed runs since the last call (their populations included). */
+    std::vector<Result> takeCompleted();
+    size_t queued() const;
+    size_t active() const;
+    size_t reservedBytes() const;
+    double now() const;
+    /** Device bytes a run is budgeted at: agent columns (twice, with head room
+     *  for births), message columns and records, spatial indexes, scratch. */
+    static size_t estimateBytes(const ModelDescription& model,
+                                const std::vector<std::pair<std::string, AgentVector>>& populations);
+
+ private:
+    struct Job;
+    void retire(Job& j, bool failed, const std::string& error);
+    Config cfg;
+    std::chrono::steady_clock::time_point t0;
+    uint64_t next_id = 1;
+    std::deque<std::unique_ptr<Job>> queue;
+    std::vector<std::unique_ptr<Job>> running;
+    std::vector<Result> completed;
+    size_t reserved = 0;
+};
+
+}  // namespace flamegpu
+
+#endif  // INCLUDE_FLAMEGPU_SIMULATION_SIMULATIONSERVER_H_

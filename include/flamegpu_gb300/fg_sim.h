@@ -98,6 +98,37 @@ int fge_get_variable(fge_ensemble* e, uint32_t run, const char* agent, const cha
 int fge_stats(fge_ensemble* e, double* elapsed_s, int32_t* batched, uint32_t* kernels_per_step,
               uint64_t* graph_launches);
 
+/* --------------------------------------------------------------- server
+ * flamegpu::SimulationServer (include/flamegpu/simulation/SimulationServer.h;
+ * no counterpart in the reference): runs of registered models are submitted as
+ * requests and advance together, each on its own stream, admitted against a
+ * device-memory budget and a slot limit. */
+typedef struct fgv_server fgv_server;
+fgv_server* fgv_create(int32_t device, uint64_t memory_budget, uint32_t max_active, uint32_t steps_per_poll,
+                       int32_t use_graphs);
+void fgv_destroy(fgv_server* v);
+/* Queues a run of model `model` (factory parameters `params`) for `steps` steps
+ * with seed `seed`. Its initial populations: `npops` agents; population k is
+ * agents[k] with counts[k] rows and nvars[k] named host columns, taken in order
+ * from the flattened `names` / `host_cols` arrays. *id receives the run's id. */
+int fgv_submit(fgv_server* v, const char* model, const double* params, int32_t nparams, uint32_t steps, uint64_t seed,
+               int32_t npops, const char* const* agents, const uint32_t* counts, const int32_t* nvars,
+               const char* const* names, const void* const* host_cols, uint64_t* id);
+/* One scheduling round; *remaining receives the runs still queued or active. */
+int fgv_poll(fgv_server* v, uint32_t* remaining);
+int fgv_run_until_idle(fgv_server* v);
+/* Ids of runs completed since the last call (at most cap; *n receives the count). */
+int fgv_take_completed(fgv_server* v, uint64_t* ids, uint32_t cap, uint32_t* n);
+/* Times (seconds since the server started: arrival, admitted, completed) and
+ * status of a completed run; the error text goes to err (len bytes) if failed. */
+int fgv_result_info(fgv_server* v, uint64_t id, double* times3, int32_t* failed, char* err, size_t len);
+int fgv_result_count(fgv_server* v, uint64_t id, const char* agent, const char* state, uint32_t* n);
+int fgv_result_variable(fgv_server* v, uint64_t id, const char* agent, const char* state, const char* var, void* out,
+                        size_t bytes);
+/* Drops a completed run's results. */
+int fgv_release(fgv_server* v, uint64_t id);
+int fgv_stats(fgv_server* v, uint32_t* queued, uint32_t* active, uint64_t* reserved_bytes);
+
 #ifdef __cplusplus
 }
 #endif

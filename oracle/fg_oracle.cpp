@@ -572,3 +572,93 @@ extern "C" uint32_t or_birth_death_run(uint32_t n, uint32_t cap, float* f, int32
     }
     return n;
 }
+
+// ---------------------------------------------------------- predator-prey
+
+extern "C" void or_predprey_run(const or_predprey_params* p, uint32_t steps, uint32_t first_step, uint32_t* n_prey,
+                                uint32_t cap_prey, float* prey_x, float* prey_y, uint32_t* prey_id,
+                                uint32_t* next_prey_id, uint32_t* n_pred, float* pred_x, float* pred_y,
+                                uint32_t* pred_id) {
+    // examples/predprey2D/predprey.cu restated serially; layers as in that model.
+    or_grid g;
+    const float mn[3] = {0.0f, 0.0f, 0.0f};
+    const float mx[3] = {p->edge, p->edge, 0.0f};
+    or_grid_init(&g, 2, mn, mx, p->radius);
+    auto clampf = [](float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); };
+    std::vector<uint32_t> pbm(static_cast<size_t>(g.binCount) + 1), perm, keys, cand(64), tmpu;
+    std::vector<float> mxs, mys, tmpf;
+    for (uint32_t s = 0; s < steps; ++s) {
+        const uint32_t step = first_step + s;
+        // layer 1: predator messages (in predator order)
+        const uint32_t np = *n_pred;
+        std::vector<float> msg_x(pred_x, pred_x + np), msg_y(pred_y, pred_y + np);
+        // layer 2: prey auto-sort (CUDASimulation.cu:670-681), build, prey_step / predator_step
+        uint32_t n = *n_prey;
+        keys.resize(n);
+        perm.resize(std::max<uint32_t>(n, np));
+        for (uint32_t i = 0; i < n; ++i) keys[i] = or_sort_key(&g, prey_x[i], prey_y[i], 0.0f);
+        or_stable_sort_perm(n, keys.data(), or_sort_max_bit(&g), perm.data());
+        apply_perm(tmpf, prey_x, perm.data(), n);
+        apply_perm(tmpf, prey_y, perm.data(), n);
+        apply_perm(tmpu, prey_id, perm.data(), n);
+        std::vector<uint32_t> mperm(np + 1);
+        or_spatial_build(&g, np, msg_x.data(), msg_y.data(), nullptr, pbm.data(), mperm.data(), nullptr);
+        std::vector<float> sx(np), sy(np);
+        for (uint32_t j = 0; j < np; ++j) {
+            sx[j] = msg_x[mperm[j]];
+            sy[j] = msg_y[mperm[j]];
+        }
+        std::vector<float> ox, oy, bx, by;
+        std::vector<uint32_t> oid;
+        for (uint32_t i = 0; i < n; ++i) {
+            const float x = prey_x[i], y = prey_y[i];
+            uint32_t nc = or_neighbours(&g, pbm.data(), x, y, 0.0f, 0, cand.data(), static_cast<uint32_t>(cand.size()));
+            if (nc > cand.size()) {
+                cand.resize(nc);
+                nc = or_neighbours(&g, pbm.data(), x, y, 0.0f, 0, cand.data(), nc);
+            }
+            bool eaten = false;
+            for (uint32_t c = 0; c < nc && !eaten; ++c) {
+                const float dx = sx[cand[c]] - x, dy = sy[cand[c]] - y;
+                if (dx * dx + dy * dy < p->radius * p->radius) eaten = true;
+            }
+            if (eaten) continue;
+            const uint64_t key = prey_id[i];
+            const float nx = clampf(x + p->step * (2.0f * or_hash_uniform(p->seed, key, step, 2) - 1.0f), 0.0f, p->edge);
+            const float ny = clampf(y + p->step * (2.0f * or_hash_uniform(p->seed, key, step, 3) - 1.0f), 0.0f, p->edge);
+            ox.push_back(nx);
+            oy.push_back(ny);
+            oid.push_back(prey_id[i]);
+            if (or_hash_uniform(p->seed, key, step, 1) < p->p_prey_birth) {
+                bx.push_back(nx);
+                by.push_back(ny);
+            }
+        }
+        // survivors, then children in parent order with fresh ids
+        uint32_t k = 0;
+        for (size_t i = 0; i < ox.size() && k < cap_prey; ++i, ++k) {
+            prey_x[k] = ox[i];
+            prey_y[k] = oy[i];
+            prey_id[k] = oid[i];
+        }
+        for (size_t i = 0; i < bx.size() && k < cap_prey; ++i, ++k) {
+            prey_x[k] = bx[i];
+            prey_y[k] = by[i];
+            prey_id[k] = *next_prey_id + static_cast<uint32_t>(i);
+        }
+        *next_prey_id += static_cast<uint32_t>(bx.size());
+        *n_prey = k;
+        // predators
+        uint32_t q = 0;
+        for (uint32_t i = 0; i < np; ++i) {
+            const uint64_t key = pred_id[i];
+            if (or_hash_uniform(p->seed, key, step, 4) < p->p_pred_death) continue;
+            const float x = pred_x[i], y = pred_y[i];
+            pred_x[q] = clampf(x + p->step * (2.0f * or_hash_uniform(p->seed, key, step, 5) - 1.0f), 0.0f, p->edge);
+            pred_y[q] = clampf(y + p->step * (2.0f * or_hash_uniform(p->seed, key, step, 6) - 1.0f), 0.0f, p->edge);
+            pred_id[q] = pred_id[i];
+            ++q;
+        }
+        *n_pred = q;
+    }
+}

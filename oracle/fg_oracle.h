@@ -122,6 +122,20 @@ uint32_t or_birth_death_run(uint32_t n, uint32_t cap, float* f, int32_t* counter
 uint64_t or_mix64(uint64_t z);
 float or_hash_uniform(uint64_t seed, uint64_t key, uint32_t step, uint32_t stream);
 
+/* Predator-prey on MessageSpatial2D (the model of examples/predprey2D/predprey.cu).
+ * Per step: predators output locations; prey are auto-sorted, the index is
+ * built, each prey dies if a predator message lies within radius (clamped
+ * Filter), else moves and may give birth; predators die or move. Prey arrays
+ * have room for cap_prey rows. Returns via *n_prey / *n_pred. */
+typedef struct or_predprey_params {
+    float edge, radius, p_prey_birth, p_pred_death, step;
+    uint64_t seed;
+} or_predprey_params;
+
+void or_predprey_run(const or_predprey_params* p, uint32_t steps, uint32_t first_step,
+                     uint32_t* n_prey, uint32_t cap_prey, float* prey_x, float* prey_y, uint32_t* prey_id,
+                     uint32_t* next_prey_id, uint32_t* n_pred, float* pred_x, float* pred_y, uint32_t* pred_id);
+
 #ifdef __cplusplus
 }
 #endif

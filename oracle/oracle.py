@@ -33,6 +33,11 @@ class Grid(C.Structure):
     ]
 
 
+class PredPreyParams(C.Structure):
+    _fields_ = [("edge", C.c_float), ("radius", C.c_float), ("p_prey_birth", C.c_float),
+                ("p_pred_death", C.c_float), ("step", C.c_float), ("seed", C.c_uint64)]
+
+
 class BoidsParams(C.Structure):
     _fields_ = [
         ("min_pos", C.c_float), ("max_pos", C.c_float),
@@ -81,6 +86,8 @@ def lib():
             L.or_birth_death_run.argtypes = [C.c_uint32, C.c_uint32, f32p, i32p, u32p, u32p, C.c_float, C.c_float,
                                              C.c_uint64, C.c_uint32, C.c_uint32, u32p]
             L.or_birth_death_run.restype = C.c_uint32
+            L.or_predprey_run.argtypes = [P(PredPreyParams), C.c_uint32, C.c_uint32, u32p, C.c_uint32, f32p, f32p,
+                                          u32p, u32p, u32p, f32p, f32p, u32p]
             L.or_mix64.argtypes = [C.c_uint64]
             L.or_mix64.restype = C.c_uint64
             L.or_hash_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32]
@@ -213,3 +220,26 @@ def birth_death_run(f, counter, ids, next_id, cap, p_death, p_birth, seed, steps
 
 def hash_uniform(seed, key, step, stream) -> float:
     return float(lib().or_hash_uniform(seed, key, step, stream))
+
+
+def predprey_run(params: dict, prey: dict, pred: dict, steps: int, next_prey_id: int, cap: int = None):
+    """prey/pred: dicts of x, y (f32) and _id (u32). Returns (prey, pred, next_prey_id)."""
+    p = PredPreyParams(params["edge"], params["radius"], params["p_prey_birth"], params["p_pred_death"],
+                       params["step"], int(params["seed"]))
+    n = len(prey["x"])
+    cap = cap or max(4 * n, 1024)
+    px = np.zeros(cap, np.float32); px[:n] = prey["x"]
+    py = np.zeros(cap, np.float32); py[:n] = prey["y"]
+    pid = np.zeros(cap, np.uint32); pid[:n] = prey["_id"]
+    qx = np.array(pred["x"], np.float32, copy=True)
+    qy = np.array(pred["y"], np.float32, copy=True)
+    qid = np.array(pred["_id"], np.uint32, copy=True)
+    nprey = np.array([n], np.uint32)
+    npred = np.array([len(qx)], np.uint32)
+    nid = np.array([next_prey_id], np.uint32)
+    lib().or_predprey_run(C.byref(p), steps, 0, _p(nprey, C.c_uint32), cap, _p(px, C.c_float), _p(py, C.c_float),
+                          _p(pid, C.c_uint32), _p(nid, C.c_uint32), _p(npred, C.c_uint32), _p(qx, C.c_float),
+                          _p(qy, C.c_float), _p(qid, C.c_uint32))
+    m, q = int(nprey[0]), int(npred[0])
+    return ({"x": px[:m].copy(), "y": py[:m].copy(), "_id": pid[:m].copy()},
+            {"x": qx[:q].copy(), "y": qy[:q].copy(), "_id": qid[:q].copy()}, int(nid[0]))

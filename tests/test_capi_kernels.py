@@ -34,6 +34,16 @@ def test_header_symbols_exported():
     assert b"sm_103a" in L.fg_version()
 
 
+def test_sim_header_symbols_exported():
+    from flamegpu2_gb300 import sim
+    hdr = open(os.path.join(ROOT, "include", "flamegpu_gb300", "fg_sim.h")).read()
+    declared = set(re.findall(r"^(?:int|void|const char\*|fg[sev]_\w+\*)\s+(fg[sev]_\w+)\(", hdr, re.M))
+    assert declared == set(sim.SIM_EXPORTS + sim.ENSEMBLE_EXPORTS + sim.SERVER_EXPORTS)
+    L = sim.core()
+    for name in declared:
+        assert hasattr(L, name), name
+
+
 @pytest.mark.parametrize("dims,mn,mx,r", [(3, (0, 0, 0), (64, 64, 64), 2.0), (3, (0, 0, 0), (50.1, 50.1, 50.1), 10.0),
                                           (2, (0, 0), (11, 11), 1.0), (3, (141, -540, 200), (211, -470, 270), 3.5),
                                           (3, (-0.5, -0.5, -0.5), (0.5, 0.5, 0.5), 0.05)])
