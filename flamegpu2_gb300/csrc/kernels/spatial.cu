@@ -13,6 +13,7 @@
 // The automatic agent sort runs the same pipeline on the reference's sort key
 // and finally gathers every agent column by the stable permutation.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "scan.cuh"
@@ -556,6 +557,70 @@ extern "C" int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t
         return FG_ERR_WORKSPACE;
     if (!n) return FG_OK;
     char* ws = static_cast<char*>(workspace);
+    k_scan_u32<<<scan_tiles(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+        in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
+    return check_launch();
+}
+
+// ------------------------------------------------- allocation-free scan
+
+namespace {
+
+// Header plus one 8-byte status per 4096-value tile (and one spare), rounded to
+// 256 bytes: the layout fg_scan_workspace_size() describes, at the largest n.
+constexpr size_t kNoAllocScanBytes =
+    sizeof(WsHeader) +
+    (sizeof(uint64_t) * ((FG_NOALLOC_SCAN_MAX_N + kScanTile - 1) / kScanTile + 1) + 255) / 256 * 256;
+static_assert(kNoAllocScanBytes == 66048, "scratch size quoted in fg_capi.h");
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[kNoAllocScanBytes];
+
+namespace {
+
+struct NoAllocScratch {
+    std::once_flag once;
+    void* ptr = nullptr;
+    cudaError_t err = cudaSuccess;
+};
+NoAllocScratch g_noalloc_scratch[64];
+
+// The scratch of the current device; set up by the first call on that device.
+int noalloc_scratch(char** out) {
+    int dev = 0;
+    const cudaError_t de = cudaGetDevice(&dev);
+    if (de != cudaSuccess) {
+        g_last_cuda_error = static_cast<int>(de);
+        return FG_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= 64) return FG_ERR_UNSUPPORTED;
+    NoAllocScratch& s = g_noalloc_scratch[dev];
+    std::call_once(s.once, [&s] {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
+        if (e == cudaSuccess) e = cudaMemset(p, 0, kNoAllocScanBytes);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
+        s.err = e;
+        if (e == cudaSuccess) s.ptr = p;
+    });
+    if (s.err != cudaSuccess || !s.ptr) {
+        g_last_cuda_error = static_cast<int>(s.err);
+        return FG_ERR_CUDA;
+    }
+    *out = static_cast<char*>(s.ptr);
+    return FG_OK;
+}
+
+}  // namespace
+
+extern "C" int fg_exclusive_scan_u32_noalloc(const uint32_t* in, uint32_t* out, uint32_t n, void* stream) {
+    if (n && (!in || !out)) return FG_ERR_INVALID_ARGUMENT;
+    if (n > FG_NOALLOC_SCAN_MAX_N) return FG_ERR_WORKSPACE;
+    char* ws = nullptr;
+    const int rc = noalloc_scratch(&ws);
+    if (rc != FG_OK) return rc;
+    if (!n) return FG_OK;
     k_scan_u32<<<scan_tiles(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
         in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
     return check_launch();

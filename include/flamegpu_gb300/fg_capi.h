@@ -160,6 +160,29 @@ size_t fg_scan_workspace_size(uint32_t n);
 int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n,
                           void* workspace, size_t workspace_bytes, void* stream);
 
+/* Largest n fg_exclusive_scan_u32_noalloc accepts (2^25 values, 128 MiB of input). */
+#define FG_NOALLOC_SCAN_MAX_N (1u << 25)
+
+/* The same exclusive scan for a caller that has no scratch to give: one whose
+ * device memory all belongs to another allocator, or that is handed only the
+ * input and output pointers across a language boundary and has no allocator of
+ * its own there. No counterpart in the reference (cub::DeviceScan::ExclusiveSum,
+ * which it uses, always takes caller scratch).
+ *
+ * The scratch is a fixed 66,048-byte array in this library's static device
+ * memory, one per device; nothing is allocated, now or later. Its limit:
+ * n > FG_NOALLOC_SCAN_MAX_N returns FG_ERR_WORKSPACE and launches nothing.
+ * The first call on a device, with that device current, does the set-up: it
+ * looks up the array's address and clears it (the scan's tile ticket, epoch
+ * and tile statuses must start at zero), waiting for that clear to finish.
+ * Make that first call before any stream capture. Every later call only
+ * launches the scan on `stream` and leaves the scratch ready for the next.
+ * All calls on one device share the one scratch: calls that overlap on the
+ * GPU (issued on different streams without ordering, or from several host
+ * threads at once) race and give wrong results. Order them, e.g. on one stream.
+ * out may alias in. */
+int fg_exclusive_scan_u32_noalloc(const uint32_t* in, uint32_t* out, uint32_t n, void* stream);
+
 /* ------------------------------------------------------------- batches */
 
 /* One instance of a batch: many simulations of one model, concatenated.
