@@ -314,7 +314,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="boids_small",
-                    choices=["boids_small", "birth_death", "spatial3d_large", "spatial2d_large"])
+                    choices=["boids_small", "birth_death", "spatial3d_large", "spatial2d_large", "ensemble", "served"])
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stage-bytes", type=int, default=None,

@@ -441,6 +441,19 @@ struct BatchedSim {
         kernels_per_step += 5;
     }
 
+    // Stage neighbourhood windows when the instances holding most of the agents
+    // have windows that fit the staging buffer.
+    bool stage_pays(const BMsg& m) const {
+        double fit = 0.0, all = 0.0;
+        for (uint32_t k = 0; k < ninst && k < m.inst.size(); ++k) {
+            const fg_spatial_grid& g = m.inst[k].grid;
+            const double per_bin = static_cast<double>(count[k]) / std::max<uint32_t>(g.binCount, 1u);
+            all += count[k];
+            if (detail::stage_window_fits(g, per_bin, m.record_words, kAgentBlock, cfg.message_stage_bytes)) fit += count[k];
+        }
+        return all > 0.0 && fit >= 0.5 * all;
+    }
+
     void launch_fn(BFn& b) {
         LaunchParams P;
         std::memset(&P, 0, sizeof(P));
@@ -452,7 +465,7 @@ struct BatchedSim {
             P.in_pbm = b.in->pbm;
             P.in_records = reinterpret_cast<const char*>(b.in->records);
             P.in_record_bytes = b.in->record_words * 4u;
-            if (b.sort && cfg.message_stage_bytes >= 1024u) {
+            if (b.sort && cfg.message_stage_bytes >= 1024u && stage_pays(*b.in)) {
                 P.stage_bytes = (cfg.message_stage_bytes + 15u) & ~15u;
                 smem = P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader));
             }
@@ -508,6 +521,8 @@ struct BatchedSim {
         return f;
     }
 
+    double step_seconds = 0.0;  // device time from the first step's start to the last step's end
+
     AgentVector read_instance(uint32_t k) {
         AgentVector pop(AgentDescription(model, agent), 0);
         pop.setCountRaw(count[k]);
@@ -526,6 +541,10 @@ struct BatchedSim {
         for (const auto& p : plans) max_steps = std::max(max_steps, p.getSteps());
         results.assign(ninst, nullptr);
         std::map<std::pair<int, bool>, cudaGraphExec_t> cache;
+        cudaEvent_t t_begin = nullptr, t_end = nullptr;
+        FG_ECUDA(cudaEventCreate(&t_begin));
+        FG_ECUDA(cudaEventCreate(&t_end));
+        FG_ECUDA(cudaEventRecord(t_begin, stream));
         for (unsigned int s = 0; s < max_steps; ++s) {
             if (cfg.use_graphs) {
                 const auto key = std::make_pair(parity, sorts_at(s));
@@ -565,7 +584,13 @@ struct BatchedSim {
                 }
             }
         }
+        FG_ECUDA(cudaEventRecord(t_end, stream));
         FG_ECUDA(cudaStreamSynchronize(stream));
+        float ms = 0.0f;
+        FG_ECUDA(cudaEventElapsedTime(&ms, t_begin, t_end));
+        step_seconds = ms / 1000.0;
+        cudaEventDestroy(t_begin);
+        cudaEventDestroy(t_end);
         for (auto& c : cache) cudaGraphExecDestroy(c.second);
         uint32_t err[4];
         FG_ECUDA(cudaMemcpy(err, d_misc + 1, sizeof(err), cudaMemcpyDeviceToHost));
@@ -580,6 +605,7 @@ struct EnsembleImpl {
     CUDAEnsemble::EnsembleConfig cfg;
     std::vector<std::map<std::pair<std::string, std::string>, std::shared_ptr<AgentVector>>> results;
     double elapsed = 0.0;
+    double step_seconds = 0.0;
     bool batched = false;
     unsigned int kernels_per_step = 0;
     unsigned long long graph_launches = 0;
@@ -593,6 +619,7 @@ CUDAEnsemble::CUDAEnsemble(const ModelDescription& model, int, const char**)
 CUDAEnsemble::~CUDAEnsemble() = default;
 CUDAEnsemble::EnsembleConfig& CUDAEnsemble::Config() { return impl->cfg; }
 double CUDAEnsemble::getEnsembleElapsedTime() const { return impl->elapsed; }
+double CUDAEnsemble::getEnsembleStepTime() const { return impl->step_seconds; }
 bool CUDAEnsemble::lastRunBatched() const { return impl->batched; }
 unsigned int CUDAEnsemble::getKernelsPerStep() const { return impl->kernels_per_step; }
 unsigned long long CUDAEnsemble::getGraphLaunches() const { return impl->graph_launches; }
@@ -604,6 +631,7 @@ unsigned int CUDAEnsemble::simulate(const RunPlanVector& plans) {
     for (const auto& p : plans)
         if (p.model() != model) THROW exception::InvalidArgument("RunPlan belongs to another model");
     unsigned int failures = 0;
+    impl->step_seconds = 0.0;
     impl->batched = impl->cfg.batched && !plans.empty() && detail::batch_unsupported(*model).empty();
     if (impl->batched) {
         detail::BatchedSim b(model, plans, impl->cfg);
@@ -613,6 +641,7 @@ unsigned int CUDAEnsemble::simulate(const RunPlanVector& plans) {
         const auto key = std::make_pair(model->agents[0]->name, model->agents[0]->states[0]);
         for (size_t k = 0; k < plans.size(); ++k) impl->results[k][key] = res[k];
         impl->kernels_per_step = b.kernels_per_step;
+        impl->step_seconds = b.step_seconds;
         impl->graph_launches = b.graph_launches;
     } else {
         // the plain path: one CUDASimulation per plan, one after another
@@ -633,6 +662,7 @@ unsigned int CUDAEnsemble::simulate(const RunPlanVector& plans) {
                     sim.setPopulationData(copy, pop.first.second);
                 }
                 sim.simulate();
+                for (double t : sim.getElapsedTimeSteps()) impl->step_seconds += t;
                 for (const auto& a : model->agents)
                     for (const auto& st : a->states) {
                         auto out = std::make_shared<AgentVector>(AgentDescription(model, a.get()));

@@ -1,6 +1,7 @@
 // Helpers shared by the simulation and ensemble runtimes (not installed).
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <vector>
 
@@ -20,6 +21,21 @@ struct TableEntry {
 /** Collision-free multiplicative lookup table over the given variables:
  * slot = (hash * mult) >> shift; throws if no multiplier up to 64 slots works. */
 VarTable make_table(const std::vector<TableEntry>& e, const char* what);
+
+// Whether a block's neighbourhood window (the sorted records from one z/y slab
+// below its lowest bin to one above its highest) is expected to fit a staging
+// buffer of stage_bytes, with per_bin messages in every bin of grid g. Staging
+// reserves the buffer's shared memory for every block, which caps occupancy,
+// so it is only worth it when the window usually fits.
+inline bool stage_window_fits(const fg_spatial_grid& g, double per_bin, uint32_t record_words, uint32_t block,
+                              unsigned int stage_bytes) {
+    const double span = g.dims == 3 ? static_cast<double>(g.gridDim[0]) * g.gridDim[1] + g.gridDim[0] + 1.0
+                                    : static_cast<double>(g.gridDim[0]) + 1.0;
+    const double block_bins = std::max(1.0, block / std::max(per_bin, 1e-3));
+    const double bins = 2.0 * span + block_bins;
+    const double bytes = bins * per_bin * record_words * 4.0 + (bins + 8.0) * 4.0;
+    return bytes <= 0.9 * stage_bytes;
+}
 
 }  // namespace detail
 }  // namespace flamegpu

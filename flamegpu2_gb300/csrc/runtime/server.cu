@@ -16,13 +16,20 @@ struct SimulationServer::Job {
     unsigned int steps = 0;
     uint64_t seed = 0;
     double arrival = 0, admitted = 0;
-    unsigned int issued = 0;
+    unsigned int issued = 0;     // steps enqueued on the run's stream
+    unsigned int completed = 0;  // steps known to have finished on the device
+    size_t agents = 0;           // initial agents, all types
     size_t bytes = 0;
     std::unique_ptr<CUDASimulation> sim;
-    cudaEvent_t done = nullptr;
+    std::vector<cudaEvent_t> ring;  // event of step k in ring[k % size]
     ~Job() {
-        if (done) cudaEventDestroy(done);
+        for (cudaEvent_t e : ring) cudaEventDestroy(e);
     }
+    // advance `completed` over the steps whose events have fired
+    void reap() {
+        while (completed < issued && cudaEventQuery(ring[completed % ring.size()]) == cudaSuccess) ++completed;
+    }
+    double remaining_work() const { return static_cast<double>(steps - completed) * static_cast<double>(agents); }
 };
 
 SimulationServer::SimulationServer() : SimulationServer(Config()) {}
@@ -84,6 +91,7 @@ uint64_t SimulationServer::submit(std::shared_ptr<ModelDescription> model,
     j->seed = seed;
     j->arrival = now();
     j->bytes = estimateBytes(*j->model, j->populations);
+    for (const auto& p : j->populations) j->agents += p.second.size();
     const uint64_t id = j->id;
     queue.push_back(std::move(j));
     return id;
@@ -121,7 +129,8 @@ size_t SimulationServer::poll() {
     // 1. retire runs whose last step has completed (non-blocking test)
     for (size_t k = 0; k < running.size();) {
         Job& j = *running[k];
-        if (j.issued >= j.steps && j.done && cudaEventQuery(j.done) == cudaSuccess) {
+        j.reap();
+        if (j.completed >= j.steps) {
             retire(j, false, "");
             running.erase(running.begin() + static_cast<long>(k));
         } else {
@@ -139,35 +148,67 @@ size_t SimulationServer::poll() {
             j->sim = std::make_unique<CUDASimulation>(*j->model);
             j->sim->CUDAConfig().device_id = cfg.device;
             j->sim->CUDAConfig().use_graphs = cfg.use_graphs;
+            j->sim->CUDAConfig().stream_priority = priority_for(static_cast<double>(j->steps) * static_cast<double>(j->agents));
             j->sim->SimulationConfig().random_seed = j->seed;
             j->sim->SimulationConfig().steps = j->steps;
+            // births may grow a population to four times its start (as budgeted), no further
+            size_t largest = 1024;
+            for (const auto& p : j->populations) largest = std::max<size_t>(largest, p.second.size());
+            j->sim->CUDAConfig().max_agents = static_cast<unsigned int>(std::min<size_t>(4 * largest, (1u << 31) - 1));
             for (auto& p : j->populations) j->sim->setPopulationData(p.second);
             j->populations.clear();
-            if (cudaEventCreateWithFlags(&j->done, cudaEventDisableTiming) != cudaSuccess)
-                throw exception::CUDAError("cudaEventCreate failed");
+            j->ring.assign(std::max(1u, cfg.steps_in_flight), nullptr);
+            for (cudaEvent_t& e : j->ring)
+                if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                    throw exception::CUDAError("cudaEventCreate failed");
             running.push_back(std::move(j));
         } catch (const exception::FLAMEGPUException& e) {
             retire(*j, true, std::string(e.exception_type()) + ": " + e.what());
         }
     }
-    // 3. issue the next steps of every active run (each on its own stream)
-    for (size_t k = 0; k < running.size();) {
-        Job& j = *running[k];
+    // 3. issue the next steps, least remaining work first, keeping at most
+    //    steps_in_flight steps of a run queued on the device
+    std::vector<Job*> order;
+    order.reserve(running.size());
+    for (auto& j : running) order.push_back(j.get());
+    std::stable_sort(order.begin(), order.end(),
+                     [](const Job* a, const Job* b) { return a->remaining_work() < b->remaining_work(); });
+    std::vector<Job*> failed;
+    for (Job* jp : order) {
+        Job& j = *jp;
         try {
-            for (unsigned int s = 0; s < cfg.steps_per_poll && j.issued < j.steps; ++s) {
+            j.reap();
+            for (unsigned int s = 0; s < cfg.steps_per_poll && j.issued < j.steps &&
+                                     j.issued - j.completed < j.ring.size();
+                 ++s) {
                 j.sim->step();
-                ++j.issued;
-                if (j.issued == j.steps && cudaEventRecord(j.done, j.sim->getStream()) != cudaSuccess)
+                if (cudaEventRecord(j.ring[j.issued % j.ring.size()], j.sim->getStream()) != cudaSuccess)
                     throw exception::CUDAError("cudaEventRecord failed");
+                ++j.issued;
             }
-            ++k;
         } catch (const exception::FLAMEGPUException& e) {
             // failure isolation: this run completes with its error, the others go on
             retire(j, true, std::string(e.exception_type()) + ": " + e.what());
-            running.erase(running.begin() + static_cast<long>(k));
+            failed.push_back(jp);
         }
     }
+    if (!failed.empty())
+        running.erase(std::remove_if(running.begin(), running.end(),
+                                     [&](const std::unique_ptr<Job>& j) {
+                                         return std::find(failed.begin(), failed.end(), j.get()) != failed.end();
+                                     }),
+                      running.end());
     return queue.size() + running.size();
+}
+
+int SimulationServer::priority_for(double work) const {
+    // the device's priority range split by decades of work (agent-steps):
+    // under 1e7 gets the highest priority, each further decade one level less
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess || least == greatest) return 0;
+    const int levels = least - greatest;  // greatest is the numerically lower
+    int decade = work < 1e7 ? 0 : static_cast<int>(std::floor(std::log10(work))) - 6;
+    return greatest + std::min(std::max(decade, 0), levels);
 }
 
 void SimulationServer::runUntilIdle() {

@@ -376,6 +376,10 @@ extern "C" int fge_stats(fge_ensemble* e, double* el, int32_t* batched, uint32_t
     });
 }
 
+extern "C" int fge_step_time(fge_ensemble* e, double* seconds) {
+    return guarded([&] { *seconds = e->ens->getEnsembleStepTime(); });
+}
+
 // ------------------------------------------------------------------- server
 
 struct fgv_server {

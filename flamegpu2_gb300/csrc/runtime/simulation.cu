@@ -295,8 +295,8 @@ struct SimulationImpl {
         FG_CUDA(cudaSetDevice(cuda_config.device_id));
         device = cuda_config.device_id;
         sms = sm_count(device);
-        FG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        FG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        FG_CUDA(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, cuda_config.stream_priority));
+        FG_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, cuda_config.stream_priority));
         DevMem::keep_pool(device);
         mem.stream = stream;
         FG_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
@@ -658,9 +658,14 @@ struct SimulationImpl {
             sync_counts();
             for (size_t i = 0; i < lists.size(); ++i) {
                 bound[i] = grow_bound(lists[i]->bound, births_per_step(lists[i].get()));
+                if (cuda_config.max_agents && bound[i] > cuda_config.max_agents)
+                    THROW exception::OutOfMemory(format("Agent '%s' may reach %llu agents in the next step, above the limit of %u",
+                                                        lists[i]->agent->name.c_str(), static_cast<unsigned long long>(bound[i]),
+                                                        cuda_config.max_agents));
                 if (bound[i] > lists[i]->capacity) {
                     if (bound[i] >= (1ull << 31)) THROW exception::OutOfMemory("Population bound exceeds 2^31 agents");
-                    const uint64_t want = std::max<uint64_t>(2 * bound[i], 2ull * lists[i]->capacity);
+                    uint64_t want = std::max<uint64_t>(2 * bound[i], 2ull * lists[i]->capacity);
+                    if (cuda_config.max_agents) want = std::min<uint64_t>(want, cuda_config.max_agents);
                     ensure_capacity(*lists[i], static_cast<uint32_t>(std::min<uint64_t>(want, (1ull << 31) - 1)), lists[i]->bound);
                 }
             }
@@ -760,6 +765,11 @@ struct SimulationImpl {
         kernel_counter += 5;
     }
 
+    static bool stage_window_fits(const MsgList& m, unsigned int stage_bytes) {
+        const double per_bin = static_cast<double>(m.capacity) / std::max<uint32_t>(m.grid.binCount, 1u);
+        return detail::stage_window_fits(m.grid, per_bin, m.record_words, kAgentBlock, stage_bytes);
+    }
+
     void enqueue_function(FnRt& f) {
         AgentList& l = *f.list;
         bool do_sort = false;
@@ -799,7 +809,8 @@ struct SimulationImpl {
                 P.in_records = reinterpret_cast<const char*>(f.in->records);
                 P.in_record_bytes = f.in->record_words * 4u;
                 P.in_pbm_alloc = f.in->pbm_alloc;
-                if (f.stage && cuda_config.message_stage_bytes >= 1024u)
+                if (f.stage && cuda_config.message_stage_bytes >= 1024u &&
+                    stage_window_fits(*f.in, cuda_config.message_stage_bytes))
                     P.stage_bytes = (cuda_config.message_stage_bytes + 15u) & ~15u;
             } else {
                 P.in_count = f.in->optional_any ? f.in->bf_count : f.in->d_count;

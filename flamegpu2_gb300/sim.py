@@ -218,7 +218,7 @@ class Simulation:
 
 
 ENSEMBLE_EXPORTS = ["fge_create", "fge_destroy", "fge_configure", "fge_add_run", "fge_set_run_property",
-                    "fge_simulate", "fge_get_count", "fge_get_variable", "fge_stats"]
+                    "fge_simulate", "fge_get_count", "fge_get_variable", "fge_stats", "fge_step_time"]
 _ens_ready = False
 
 
@@ -238,6 +238,7 @@ def _ens():
         L.fge_get_count.argtypes = [vp, u32, C.c_char_p, C.POINTER(u32)]
         L.fge_get_variable.argtypes = [vp, u32, C.c_char_p, C.c_char_p, vp, sz]
         L.fge_stats.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(i32), C.POINTER(u32), C.POINTER(C.c_uint64)]
+        L.fge_step_time.argtypes = [vp, C.POINTER(C.c_double)]
         _ens_ready = True
     return L
 
@@ -300,7 +301,10 @@ class Ensemble:
     def stats(self) -> dict:
         el, b, k, g = C.c_double(), C.c_int32(), C.c_uint32(), C.c_uint64()
         _check(_ens().fge_stats(self._h, C.byref(el), C.byref(b), C.byref(k), C.byref(g)))
-        return {"elapsed_s": el.value, "batched": bool(b.value), "kernels_per_step": k.value, "graph_launches": g.value}
+        t = C.c_double()
+        _check(_ens().fge_step_time(self._h, C.byref(t)))
+        return {"elapsed_s": el.value, "batched": bool(b.value), "kernels_per_step": k.value, "graph_launches": g.value,
+                "step_s": t.value}
 
 
 SERVER_EXPORTS = ["fgv_create", "fgv_destroy", "fgv_submit", "fgv_poll", "fgv_run_until_idle", "fgv_take_completed",

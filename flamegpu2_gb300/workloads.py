@@ -246,7 +246,237 @@ def run_spatial_large(name, args, world, rank, local):
     }
 
 
+# ------------------------------------------------------------ batched ensemble
+
+def _ensemble_once(specs, pops, steps, batched, device, read_back=True):
+    """One CUDAEnsemble::simulate over the given instances through the public
+    API (host populations in, host populations out). Returns timings."""
+    from flamegpu2_gb300 import sim, synth
+    t0 = time.perf_counter()
+    ens = sim.Ensemble("boids_spatial3d", synth.boids_params(dict(synth.BOIDS_SMALL)), device=device, batched=batched)
+    for sp, pop in zip(specs, pops):
+        r = ens.add_run(steps, sp["seed"], "Boid", sp["n"], pop, "location", (0.0, 0.0, 0.0), (sp["edge"],) * 3,
+                        sp["radius"])
+        ens.set_property(r, "MIN_POSITION", 0.0)
+        ens.set_property(r, "MAX_POSITION", sp["edge"])
+        ens.set_property(r, "INTERACTION_RADIUS", sp["radius"])
+    if ens.simulate() != 0:
+        raise RuntimeError("ensemble run failed")
+    d2h = 0
+    if read_back:
+        for i, sp in enumerate(specs):
+            for k in ("x", "y", "z", "fx", "fy", "fz"):
+                d2h += ens.get(i, "Boid", k, np.float32).nbytes
+    wall = time.perf_counter() - t0
+    st = ens.stats()
+    ens.close()
+    return {"wall_s": wall, "step_s": st["step_s"], "simulate_s": st["elapsed_s"], "batched": st["batched"],
+            "kernels_per_step": st["kernels_per_step"], "graph_launches": st["graph_launches"], "d2h": d2h}
+
+
+def run_ensemble(args, world, rank, local):
+    """256 Boids instances, population log-uniform in [1,024, 1,048,576],
+    radius uniform in [1, 4], edge 4 r cbrt(N/64) (whole radii), 100 steps:
+    one batched simulation (segmented kernels, one graph per step) against the
+    same instances run one after another through CUDASimulation."""
+    import torch
+    from flamegpu2_gb300 import synth
+    B = _bench_common()
+    torch.cuda.set_device(local)
+    count, steps = 256, 100
+    specs = synth.ensemble_instances(count, seed=1000 + 1000 * rank, n_lo=1024, n_hi=1 << 20)
+    pops = [synth.boids_population(sp["n"], 0.0, sp["edge"], sp["seed"]) for sp in specs]
+    total_n = sum(sp["n"] for sp in specs)
+    agent_steps = total_n * steps
+    for _ in range(args.warmup):  # graphs, pools, code paths
+        _ensemble_once(specs[:8], pops[:8], 3, True, local, read_back=False)
+    clocks = B.ClockSampler(local)
+    clocks.start()
+    B.barrier(world)
+    k = max(1, min(args.steps, 3))
+    runs = [_ensemble_once(specs, pops, steps, True, local) for _ in range(k)]
+    clk = clocks.stop()
+    step_s = B.allreduce_max(world, sum(r["step_s"] for r in runs))
+    wall_s = B.allreduce_max(world, sum(r["wall_s"] for r in runs))
+    # the plain path: the same instances one after another (CUDASimulation per run)
+    seq = _ensemble_once(specs, pops, steps, False, local)
+    seq_step_s = B.allreduce_max(world, seq["step_s"])
+    seq_wall_s = B.allreduce_max(world, seq["wall_s"])
+    bins = 0
+    for sp in specs:
+        cells = int(round(sp["edge"] / np.float32(sp["radius"])))
+        bins += cells ** 3
+    step_bytes = 136 * total_n + 8 * (bins + count)  # Bd + It, Boids message 28 B
+    peak, peak_kind = B.measured_peaks()
+    achieved = step_bytes * steps * k / step_s / 1e9
+    h2d = total_n * 28
+    return {
+        "metric": B.METRIC, "value": round(agent_steps * k * world / step_s, 1), "unit": UNIT, "n_gpus": world,
+        "steps": k, "warmup": args.warmup, "ms_per_step": round(step_s * 1000.0 / k, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 uniforms; instance sizes and radii from seeds 1000+i)",
+        "config": {"workload": "batched ensemble: 256 Boids instances, N log-uniform [1024, 1048576], r U[1,4], "
+                               "edge 4 r cbrt(N/64), 100 steps",
+                   "instances": count, "agents_total": total_n, "bins_total": bins, "model_steps": steps,
+                   "l2": "working set larger than L2",
+                   "sequential_plain_path": {
+                       "value": round(agent_steps * world / seq_step_s, 1),
+                       "e2e": round(agent_steps * world / seq_wall_s, 1),
+                       "what": "same instances, one CUDASimulation after another (graphs on)"},
+                   "speedup_vs_sequential": round(seq_step_s / (step_s / k), 2),
+                   "e2e_speedup_vs_sequential": round(seq_wall_s / (wall_s / k), 2),
+                   "kernels_per_step": runs[0]["kernels_per_step"]},
+        "wall_s": round(wall_s, 3),
+        "e2e": {"value": round(agent_steps * k * world / wall_s, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": runs[0]["d2h"],
+                "path": "fge_add_run x256 + fge_simulate + fge_get_variable (C ABI, host buffers)"},
+        "roofline": {"bound": "hbm", "kernel": "whole batched step (sort, build, iterate; one graph)",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": None, "peak_source": peak_kind, "per_launch_algorithmic_bytes": step_bytes},
+        "gpu_launches": runs[0]["kernels_per_step"] * steps * k, "clocks": clk,
+    }
+
+
+# ----------------------------------------------------------------- serving
+
+def _served_requests(count, seed):
+    """Requests: 50/50 Boids-3D / predator-prey-2D, N log-uniform in
+    [1024, 4194304], steps uniform in [10, 1000]."""
+    from flamegpu2_gb300 import synth
+    reqs = []
+    for i in range(count):
+        u = (synth.bits(seed, 100 + i, 3) >> np.uint64(11)).astype(np.float64) / 9007199254740992.0
+        n = int(round(np.exp(np.log(1024) + u[0] * (np.log(4194304) - np.log(1024)))))
+        steps = 10 + int(u[1] * 991)
+        if u[2] < 0.5:
+            edge = 2.0 * max(1, int(np.ceil(32.0 * np.cbrt(n / 16384.0))))  # config-0 density, whole radii
+            cfg = dict(synth.BOIDS_SMALL, n=n, max_pos=edge)
+            pop = synth.boids_population(n, 0.0, edge, seed + i)
+            reqs.append({"model": "boids_spatial3d", "params": synth.boids_params(cfg), "steps": steps, "n": n,
+                         "pops": {"Boid": (n, pop)}})
+        else:
+            # three agents per unit area, a quarter of them predators: the prey's
+            # crowding limit (4 others within r) holds them to about 3.5 per unit
+            # area, i.e. below twice their initial number, once the predators die out
+            n_pred = max(1, n // 4)
+            n_prey = n - n_pred
+            edge = float(np.ceil(np.sqrt(n / 3.0)))
+            prey, pred = synth.predprey_population(n_prey, n_pred, edge, seed + i)
+            reqs.append({"model": "predprey2d", "params": [edge, 1.0, 0.05, 0.02, 0.5, seed + i], "steps": steps,
+                         "n": n, "pops": {"prey": (n_prey, prey), "predator": (n_pred, pred)}})
+    return reqs
+
+
+def _percentile(v, q):
+    return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if v else None
+
+
+def run_served(args, world, rank, local):
+    """Poisson request streams served by SimulationServer (continuous
+    batching under a 150 GB budget) against the same requests run one after
+    another through CUDASimulation (FIFO)."""
+    import torch
+    from flamegpu2_gb300 import sim
+    B = _bench_common()
+    torch.cuda.set_device(local)
+    count = max(8, min(int(os.environ.get("FG_SERVED_REQUESTS", "32")), 256))
+    rates = [float(r) for r in os.environ.get("FG_SERVED_RATES", "10,100,1000").split(",")]
+    reqs = _served_requests(count, 4 + 1000 * rank)
+    work = [r["n"] * r["steps"] for r in reqs]  # nominal agent-steps: initial population x steps
+    # warm-up: a few small runs through both paths
+    for _ in range(args.warmup):
+        srv = sim.Server(device=local)
+        for r in reqs[:2]:
+            srv.submit(r["model"], r["params"], 3, 0, r["pops"])
+        srv.run_until_idle()
+        srv.close()
+    # plain path, one request after another: service time of each
+    service = []
+    for r in reqs:
+        t0 = time.perf_counter()
+        s = sim.Simulation(r["model"], r["params"], device=local)
+        for agent, (n, cols) in r["pops"].items():
+            s.set_population(agent, n, cols)
+        s.step(r["steps"])
+        for agent in r["pops"]:
+            s.get(agent, "x", np.float32)
+        s.close()
+        service.append(time.perf_counter() - t0)
+    per_rate = []
+    clocks = B.ClockSampler(local)
+    clocks.start()
+    launches = 0
+    for ri, rate in enumerate(rates):
+        from flamegpu2_gb300 import synth
+        u = (synth.bits(77 + ri, 0, count) >> np.uint64(11)).astype(np.float64) / 9007199254740992.0
+        arrivals = np.cumsum(-np.log(1.0 - u) / rate)  # Poisson process: exponential gaps
+        t_srv = time.perf_counter()  # the server's clock starts inside its constructor
+        srv = sim.Server(device=local, memory_budget=150 << 30, max_active=64)
+        ids, order = {}, {}
+        t_start = time.perf_counter()
+        nxt = 0
+        while True:
+            remaining = srv.poll()
+            now = time.perf_counter() - t_start
+            while nxt < count and arrivals[nxt] <= now:
+                r = reqs[nxt]
+                rid = srv.submit(r["model"], r["params"], r["steps"], 0, r["pops"])
+                ids[rid] = t_start + arrivals[nxt]
+                order[rid] = nxt
+                nxt += 1
+                remaining += 1
+            if nxt >= count and remaining == 0:
+                break
+            if remaining == 0:
+                time.sleep(max(0.0, min(0.001, arrivals[nxt] - now)))
+        makespan = time.perf_counter() - t_start
+        lat, detail = [], []
+        for rid in srv.take_completed():
+            info = srv.info(rid)
+            if info["failed"]:
+                raise RuntimeError(f"request {rid} failed: {info['error']}")
+            # completion on the host clock minus the scheduled arrival
+            lat.append(t_srv + info["completed_s"] - ids[rid])
+            i = order[rid]
+            detail.append([i, reqs[i]["model"][:5], reqs[i]["n"], reqs[i]["steps"], round(lat[-1], 3),
+                           round(info["admitted_s"] - info["arrival_s"], 3)])
+        srv.close()
+        # the sequential plain path on the same arrivals (single FIFO server)
+        done, seq_lat = 0.0, []
+        for i in range(count):
+            start = max(arrivals[i], done)
+            done = start + service[i]
+            seq_lat.append(done - arrivals[i])
+        per_rate.append({"rate_req_s": rate, "throughput": round(sum(work) / makespan, 1),
+                         "p50_s": round(_percentile(lat, 50), 4), "p99_s": round(_percentile(lat, 99), 4),
+                         "makespan_s": round(makespan, 3),
+                         "requests": sorted(detail) if rate == max(rates) else None,
+                         "sequential": {"throughput": round(sum(work) / done, 1),
+                                        "p50_s": round(_percentile(seq_lat, 50), 4),
+                                        "p99_s": round(_percentile(seq_lat, 99), 4), "makespan_s": round(done, 3)}})
+    clk = clocks.stop()
+    top = max(per_rate, key=lambda d: d["rate_req_s"])
+    return {
+        "metric": B.METRIC, "value": top["throughput"], "unit": UNIT + " (initial population x steps per request)",
+        "n_gpus": world, "steps": len(rates), "warmup": args.warmup, "ms_per_step": round(top["makespan_s"] * 1000, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 populations; Poisson arrivals)",
+        "config": {"workload": f"served request stream: {count} requests, 50/50 Boids-3D / predator-prey-2D, "
+                               "N log-uniform [1024, 4194304], steps U[10, 1000], budget 150 GB",
+                   "requests": count, "nominal_agent_steps": int(sum(work)), "rates": per_rate,
+                   "speedup_vs_sequential_at_top_rate": round(top["throughput"] / top["sequential"]["throughput"], 2),
+                   "l2": "working sets larger than L2"},
+        "e2e": {"value": top["throughput"], "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "path": "fgv_submit / fgv_poll / fgv_take_completed (host populations in and out)"},
+        "roofline": None, "gpu_launches": None, "clocks": clk,
+    }
+
+
 def run(name, args, world, rank, local):
+    if name == "ensemble":
+        return run_ensemble(args, world, rank, local)
+    if name == "served":
+        return run_served(args, world, rank, local)
     if name == "birth_death":
         return run_birth_death(args, world, rank, local)
     if name in ("spatial3d_large", "spatial2d_large"):

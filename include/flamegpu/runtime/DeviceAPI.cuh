@@ -478,8 +478,11 @@ class RecordView {
  * Moore neighbourhood in the reference's order. DIMS = 2 or 3.
  * Filter: 3^(DIMS-1) x-strips, y-offset outer, z-offset inner, each strip
  * PBM[hash(x-1)] .. PBM[hash(x+1)+1] with x clamped (MessageSpatial3DDevice.cuh:693-719).
- * WrapFilter: 3^DIMS single bins, x outer, y, z inner, every axis taken
- * modulo gridDim (:727-749); no radius test — user code filters.
+ * WrapFilter: 3^DIMS single bins, x offset outer, then y, z offset inner
+ * (nextCell, MessageSpatial3DDevice.cuh:264-276), every axis taken modulo
+ * gridDim (:727-749); no radius test — user code filters.
+ * Both iterators load the PBM bounds of the next strip or cell while the
+ * current one is being read, so that load's latency is hidden.
  * A cell lies wholly inside or wholly outside the block's staged window, so
  * within a cell the record address just advances by one record.
  */
@@ -546,17 +549,26 @@ class SpatialIn {
             __device__ const Message* operator->() const { return &m; }
 
          private:
+            // PBM bounds of strip t (empty when the strip lies outside the grid)
+            __device__ void bounds(int t, uint32_t& b, uint32_t& e) const {
+                b = e = 0;
+                if (t >= kStrips) return;
+                const int ry = DIMS == 3 ? t / 3 - 1 : t - 1;
+                const int rz = DIMS == 3 ? t % 3 - 1 : 0;
+                const int ay = F.cell[1] + ry, az = F.cell[2] + rz;
+                const fg_spatial_grid& g = detail::ctx().grid;
+                if (ay < 0 || ay >= static_cast<int>(g.gridDim[1])) return;
+                if (DIMS == 3 && (az < 0 || az >= static_cast<int>(g.gridDim[2]))) return;
+                const uint32_t h0 = detail::grid_hash(g, F.cell[0] - 1, ay, az);
+                const uint32_t h1 = detail::grid_hash(g, F.cell[0] + 1, ay, az);
+                b = F.win.pbm_at(F.P, h0);
+                e = F.win.pbm_at(F.P, h1 + 1);
+            }
             __device__ void advance() {
+                if (s < 0) bounds(0, nb_, ne_);
                 while (++s < kStrips) {
-                    const int ry = DIMS == 3 ? s / 3 - 1 : s - 1;
-                    const int rz = DIMS == 3 ? s % 3 - 1 : 0;
-                    const int ay = F.cell[1] + ry, az = F.cell[2] + rz;
-                    const fg_spatial_grid& g = detail::ctx().grid;
-                    if (ay < 0 || ay >= static_cast<int>(g.gridDim[1])) continue;
-                    if (DIMS == 3 && (az < 0 || az >= static_cast<int>(g.gridDim[2]))) continue;
-                    const uint32_t h0 = detail::grid_hash(g, F.cell[0] - 1, ay, az);
-                    const uint32_t h1 = detail::grid_hash(g, F.cell[0] + 1, ay, az);
-                    const uint32_t b = F.win.pbm_at(F.P, h0), e = F.win.pbm_at(F.P, h1 + 1);
+                    const uint32_t b = nb_, e = ne_;
+                    bounds(s + 1, nb_, ne_);  // in flight while strip s is read
                     if (b < e) {
                         m.index = b;
                         m.row = F.win.row(F.P, b);
@@ -569,6 +581,7 @@ class SpatialIn {
             int s;
             Message m;
             uint32_t end_;
+            uint32_t nb_ = 0, ne_ = 0;  // bounds of strip s + 1
         };
         __device__ Filter(const detail::LaunchParams& p, float x, float y, float z) : P(p) {
             loc[0] = x;
@@ -630,16 +643,25 @@ class SpatialIn {
             __device__ const Message* operator->() const { return &m; }
 
          private:
+            // PBM bounds of cell t of the visit order (x offset outer, z inner)
+            __device__ void bounds(int t, uint32_t& b, uint32_t& e) const {
+                b = e = 0;
+                if (t >= kCells) return;
+                uint32_t h;
+                if (DIMS == 3) {
+                    h = pick(t / 9, F.hx0, F.hx1, F.hx2) + pick((t / 3) % 3, F.hy0, F.hy1, F.hy2) +
+                        pick(t % 3, F.hz0, F.hz1, F.hz2);
+                } else {
+                    h = pick(t / 3, F.hx0, F.hx1, F.hx2) + pick(t % 3, F.hy0, F.hy1, F.hy2);
+                }
+                b = F.win.pbm_at(F.P, h);
+                e = F.win.pbm_at(F.P, h + 1);
+            }
             __device__ void advance() {
+                if (c < 0) bounds(0, nb_, ne_);
                 while (++c < kCells) {
-                    uint32_t h;
-                    if (DIMS == 3) {
-                        h = pick(c / 9, F.hz0, F.hz1, F.hz2) + pick((c / 3) % 3, F.hy0, F.hy1, F.hy2) +
-                            pick(c % 3, F.hx0, F.hx1, F.hx2);
-                    } else {
-                        h = pick(c % 3, F.hy0, F.hy1, F.hy2) + pick(c / 3, F.hx0, F.hx1, F.hx2);
-                    }
-                    const uint32_t b = F.win.pbm_at(F.P, h), e = F.win.pbm_at(F.P, h + 1);
+                    const uint32_t b = nb_, e = ne_;
+                    bounds(c + 1, nb_, ne_);  // in flight while cell c is read
                     if (b < e) {
                         m.index = b;
                         m.row = F.win.row(F.P, b);
@@ -652,6 +674,7 @@ class SpatialIn {
             int c;
             Message m;
             uint32_t end_;
+            uint32_t nb_ = 0, ne_ = 0;  // bounds of cell c + 1
         };
         __device__ WrapFilter(const detail::LaunchParams& p, float x, float y, float z) : P(p) {
             loc[0] = x;

@@ -101,6 +101,10 @@ class CUDAEnsemble {
     unsigned int simulate(const RunPlanVector& plans);
     /** Seconds of the last simulate() (getEnsembleElapsedTime). */
     double getEnsembleElapsedTime() const;
+    /** Device seconds of the last simulate()'s steps, by CUDA events: from the
+     *  first step to the last of the batched simulation, or summed over the
+     *  runs on the sequential path (GB300 extension). */
+    double getEnsembleStepTime() const;
     /** True if the last simulate() ran as one batched simulation. */
     bool lastRunBatched() const;
     /** Final population of one run (GB300 extension; the reference reports through logs). */

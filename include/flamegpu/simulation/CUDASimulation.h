@@ -86,6 +86,14 @@ class CUDASimulation {
         bool check_each_step = false; // synchronise and check device errors after every step()
         bool profile_ops = false;     // issue steps eagerly and time every operation with CUDA events
         unsigned int message_stage_bytes = 96u * 1024u;  // shared memory per block for spatial neighbour windows (0: off)
+        // Largest population an agent list may reach, births included: buffers
+        // never grow past it, and a step that could exceed it (checked when the
+        // buffers would have to grow) throws exception::OutOfMemory (0: no limit
+        // below 2^31). Bounds the memory of a served run.
+        unsigned int max_agents = 0;
+        // Priority of the simulation's streams (cudaStreamCreateWithPriority: a
+        // lower number runs first when kernels of several streams are waiting).
+        int stream_priority = 0;
     };
 
     explicit CUDASimulation(const ModelDescription& model, int argc = 0, const char** argv = nullptr);

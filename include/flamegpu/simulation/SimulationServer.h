@@ -6,7 +6,10 @@
 // and message state resident in HBM, and advance together — every poll issues
 // the next step of every admitted run on that run's own stream, so their
 // kernels overlap on the device, and runs that arrive meanwhile join at the
-// next poll (continuous batching). A finished run is read back and its memory
+// next poll (continuous batching). Each run keeps at most steps_in_flight steps
+// queued on the device, so a long run cannot bury a short one under its
+// backlog; runs with the least remaining work are issued first, and their
+// streams get a higher priority. A finished run is read back and its memory
 // returned without waiting for the others; a run that fails is completed with
 // its error and the others carry on.
 #include <chrono>
@@ -31,6 +34,7 @@ class SimulationServer {
         size_t memory_budget = 150ull << 30;  // bytes of device memory runs may reserve
         unsigned int max_active = 64;         // runs on the device at once
         unsigned int steps_per_poll = 1;      // steps issued per run per poll
+        unsigned int steps_in_flight = 2;     // steps of one run queued on the device at once
         int device = 0;
         bool use_graphs = true;
     };
@@ -73,6 +77,7 @@ class SimulationServer {
  private:
     struct Job;
     void retire(Job& j, bool failed, const std::string& error);
+    int priority_for(double work) const;
     Config cfg;
     std::chrono::steady_clock::time_point t0;
     uint64_t next_id = 1;

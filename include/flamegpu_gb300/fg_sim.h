@@ -97,6 +97,8 @@ int fge_get_count(fge_ensemble* e, uint32_t run, const char* agent, uint32_t* n)
 int fge_get_variable(fge_ensemble* e, uint32_t run, const char* agent, const char* var, void* out, size_t bytes);
 int fge_stats(fge_ensemble* e, double* elapsed_s, int32_t* batched, uint32_t* kernels_per_step,
               uint64_t* graph_launches);
+/* Device seconds of the last simulate()'s steps (CUDAEnsemble::getEnsembleStepTime). */
+int fge_step_time(fge_ensemble* e, double* seconds);
 
 /* --------------------------------------------------------------- server
  * flamegpu::SimulationServer (include/flamegpu/simulation/SimulationServer.h;

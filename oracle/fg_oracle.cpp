@@ -592,7 +592,8 @@ extern "C" void or_predprey_run(const or_predprey_params* p, uint32_t steps, uin
         // layer 1: predator messages (in predator order)
         const uint32_t np = *n_pred;
         std::vector<float> msg_x(pred_x, pred_x + np), msg_y(pred_y, pred_y + np);
-        // layer 2: prey auto-sort (CUDASimulation.cu:670-681), build, prey_step / predator_step
+        // prey auto-sort before prey_crowd (CUDASimulation.cu:670-681); the sort
+        // before prey_step finds them already in key order (stable: no change)
         uint32_t n = *n_prey;
         keys.resize(n);
         perm.resize(std::max<uint32_t>(n, np));
@@ -608,6 +609,24 @@ extern "C" void or_predprey_run(const or_predprey_params* p, uint32_t steps, uin
             sx[j] = msg_x[mperm[j]];
             sy[j] = msg_y[mperm[j]];
         }
+        // layer 2: prey_crowd over the prey messages of layer 1 (the count does
+        // not depend on message order; the positions are the sorted prey's)
+        std::vector<uint32_t> crowd(n, 0), ppbm(static_cast<size_t>(g.binCount) + 1), pperm(n + 1);
+        or_spatial_build(&g, n, prey_x, prey_y, nullptr, ppbm.data(), pperm.data(), nullptr);
+        for (uint32_t i = 0; i < n; ++i) {
+            const float x = prey_x[i], y = prey_y[i];
+            uint32_t nc = or_neighbours(&g, ppbm.data(), x, y, 0.0f, 0, cand.data(), static_cast<uint32_t>(cand.size()));
+            if (nc > cand.size()) {
+                cand.resize(nc);
+                nc = or_neighbours(&g, ppbm.data(), x, y, 0.0f, 0, cand.data(), nc);
+            }
+            for (uint32_t c = 0; c < nc; ++c) {
+                const uint32_t j = pperm[cand[c]];
+                const float dx = prey_x[j] - x, dy = prey_y[j] - y;
+                if (dx * dx + dy * dy < p->radius * p->radius && prey_id[j] != prey_id[i]) ++crowd[i];
+            }
+        }
+        // layer 3: prey_step / predator_step
         std::vector<float> ox, oy, bx, by;
         std::vector<uint32_t> oid;
         for (uint32_t i = 0; i < n; ++i) {
@@ -629,7 +648,7 @@ extern "C" void or_predprey_run(const or_predprey_params* p, uint32_t steps, uin
             ox.push_back(nx);
             oy.push_back(ny);
             oid.push_back(prey_id[i]);
-            if (or_hash_uniform(p->seed, key, step, 1) < p->p_prey_birth) {
+            if (or_hash_uniform(p->seed, key, step, 1) < p->p_prey_birth && crowd[i] < p->max_crowd) {
                 bx.push_back(nx);
                 by.push_back(ny);
             }

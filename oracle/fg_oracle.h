@@ -123,13 +123,15 @@ uint64_t or_mix64(uint64_t z);
 float or_hash_uniform(uint64_t seed, uint64_t key, uint32_t step, uint32_t stream);
 
 /* Predator-prey on MessageSpatial2D (the model of examples/predprey2D/predprey.cu).
- * Per step: predators output locations; prey are auto-sorted, the index is
- * built, each prey dies if a predator message lies within radius (clamped
- * Filter), else moves and may give birth; predators die or move. Prey arrays
+ * Per step: predators and prey output locations; prey are auto-sorted and
+ * count the other prey within radius; each prey dies if a predator message
+ * lies within radius (clamped Filter), else moves and, if its count is below
+ * max_crowd, may give birth; predators die or move. Prey arrays
  * have room for cap_prey rows. Returns via *n_prey / *n_pred. */
 typedef struct or_predprey_params {
     float edge, radius, p_prey_birth, p_pred_death, step;
     uint64_t seed;
+    uint32_t max_crowd;  /* prey breed only with fewer other prey than this within radius */
 } or_predprey_params;
 
 void or_predprey_run(const or_predprey_params* p, uint32_t steps, uint32_t first_step,

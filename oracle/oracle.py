@@ -35,7 +35,7 @@ class Grid(C.Structure):
 
 class PredPreyParams(C.Structure):
     _fields_ = [("edge", C.c_float), ("radius", C.c_float), ("p_prey_birth", C.c_float),
-                ("p_pred_death", C.c_float), ("step", C.c_float), ("seed", C.c_uint64)]
+                ("p_pred_death", C.c_float), ("step", C.c_float), ("seed", C.c_uint64), ("max_crowd", C.c_uint32)]
 
 
 class BoidsParams(C.Structure):
@@ -225,7 +225,7 @@ def hash_uniform(seed, key, step, stream) -> float:
 def predprey_run(params: dict, prey: dict, pred: dict, steps: int, next_prey_id: int, cap: int = None):
     """prey/pred: dicts of x, y (f32) and _id (u32). Returns (prey, pred, next_prey_id)."""
     p = PredPreyParams(params["edge"], params["radius"], params["p_prey_birth"], params["p_pred_death"],
-                       params["step"], int(params["seed"]))
+                       params["step"], int(params["seed"]), int(params.get("max_crowd", 4)))
     n = len(prey["x"])
     cap = cap or max(4 * n, 1024)
     px = np.zeros(cap, np.float32); px[:n] = prey["x"]

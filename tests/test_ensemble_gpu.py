@@ -75,4 +75,4 @@ def test_batched_ensemble_matches_oracle():
         ref = O.boids_run(p, {"id": pop["_id"], **{k: pop[k] for k in ("x", "y", "z", "fx", "fy", "fz")}}, 5)
         np.testing.assert_array_equal(got["_id"], ref["id"])
         for k in ("x", "y", "z", "fx", "fy", "fz"):
-            np.testing.assert_allclose(got[k], ref[k], rtol=0, atol=1e-4)
+            np.testing.assert_array_equal(got[k], ref[k], err_msg=k)

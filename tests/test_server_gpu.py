@@ -9,11 +9,14 @@ import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-PP = dict(edge=256.0, radius=1.0, p_prey_birth=0.05, p_pred_death=0.02, step=0.5, seed=7)
+PP = dict(edge=256.0, radius=1.0, p_prey_birth=0.05, p_pred_death=0.02, step=0.5, seed=7, max_crowd=4)
+# served runs are limited to four times their largest initial population: a
+# dense domain keeps the prey below that (crowding caps them near 3.5 per unit area)
+PS = dict(PP, edge=64.0)
 
 
 def _pp_params(p):
-    return [p["edge"], p["radius"], p["p_prey_birth"], p["p_pred_death"], p["step"], p["seed"]]
+    return [p["edge"], p["radius"], p["p_prey_birth"], p["p_pred_death"], p["step"], p["seed"], p["max_crowd"]]
 
 
 def _sim():
@@ -61,14 +64,14 @@ def _collect(srv, rid, model):
 def test_server_result_same_alone_and_in_the_mix():
     from flamegpu2_gb300 import synth
     S = _sim()
-    prey, pred = synth.predprey_population(20_000, 1_000, PP["edge"], 5)
+    prey, pred = synth.predprey_population(12_000, 600, PS["edge"], 5)
     steps = 25
     # alone
     srv = S.Server(max_active=1)
-    rid = srv.submit("predprey2d", _pp_params(PP), steps, 0, {"prey": (20_000, prey), "predator": (1_000, pred)})
+    rid = srv.submit("predprey2d", _pp_params(PS), steps, 0, {"prey": (12_000, prey), "predator": (600, pred)})
     srv.run_until_idle()
     assert srv.take_completed() == [rid]
-    assert not srv.info(rid)["failed"]
+    assert not srv.info(rid)["failed"], srv.info(rid)["error"]
     alone = _collect(srv, rid, "predprey2d")
     srv.close()
     # in a mix: boids and predator-prey runs of other sizes and seeds around it
@@ -80,12 +83,12 @@ def test_server_result_same_alone_and_in_the_mix():
             others.append(("boids", srv.submit("boids_spatial3d", params, 10 + 5 * i, 0,
                                               {"Boid": (len(pop["x"]), pop)})))
         else:
-            p2 = dict(PP, seed=50 + i)
-            q1, q2 = synth.predprey_population(5_000 * i, 400, PP["edge"], 200 + i)
+            p2 = dict(PS, seed=50 + i)
+            q1, q2 = synth.predprey_population(3_000 * i, 400, PS["edge"], 200 + i)
             others.append(("pp", srv.submit("predprey2d", _pp_params(p2), 8 + 4 * i, 0,
                                             {"prey": (len(q1["x"]), q1), "predator": (400, q2)})))
         if i == 2:
-            rid = srv.submit("predprey2d", _pp_params(PP), steps, 0, {"prey": (20_000, prey), "predator": (1_000, pred)})
+            rid = srv.submit("predprey2d", _pp_params(PS), steps, 0, {"prey": (12_000, prey), "predator": (600, pred)})
         srv.poll()
     srv.run_until_idle()
     done = srv.take_completed()
@@ -97,8 +100,8 @@ def test_server_result_same_alone_and_in_the_mix():
         for k in a:
             np.testing.assert_array_equal(a[k], b[k], err_msg=k)
     # and the plain CUDASimulation and the oracle agree with both
-    plain = _plain_predprey(PP, prey, pred, steps)
-    op, oq, _ = O.predprey_run(PP, prey, pred, steps, 20_001)
+    plain = _plain_predprey(PS, prey, pred, steps)
+    op, oq, _ = O.predprey_run(PS, prey, pred, steps, 12_001)
     for k in ("_id", "x", "y"):
         np.testing.assert_array_equal(plain[0][k], mixed[0][k])
         np.testing.assert_array_equal(plain[1][k], mixed[1][k])
@@ -118,21 +121,28 @@ def test_server_result_same_alone_and_in_the_mix():
 def test_server_budget_queues_and_isolates_failures():
     from flamegpu2_gb300 import synth
     S = _sim()
-    prey, pred = synth.predprey_population(4_000, 200, PP["edge"], 9)
+    prey, pred = synth.predprey_population(4_000, 200, 40.0, 9)
     # a budget that fits one run at a time: the second waits in the queue
     one = 1 << 20
     srv = S.Server(memory_budget=one, max_active=8)
-    a = srv.submit("predprey2d", _pp_params(PP), 5, 0, {"prey": (4_000, prey), "predator": (200, pred)})
-    b = srv.submit("predprey2d", _pp_params(PP), 5, 0, {"prey": (4_000, prey), "predator": (200, pred)})
+    a = srv.submit("predprey2d", _pp_params(dict(PS, edge=40.0)), 5, 0, {"prey": (4_000, prey), "predator": (200, pred)})
+    b = srv.submit("predprey2d", _pp_params(dict(PS, edge=40.0)), 5, 0, {"prey": (4_000, prey), "predator": (200, pred)})
     srv.poll()
     st = srv.stats()
     assert st["active"] == 1 and st["queued"] == 1
     # a run with an unknown variable fails at submission; the others are unaffected
     with pytest.raises(S.SimError):
-        srv.submit("predprey2d", _pp_params(PP), 5, 0, {"prey": (1, {"nope": np.zeros(1, np.float32)})})
+        srv.submit("predprey2d", _pp_params(dict(PS, edge=40.0)), 5, 0, {"prey": (1, {"nope": np.zeros(1, np.float32)})})
+    # a run whose prey multiply without limit (no predators, no crowding) stops at
+    # four times its initial population with OutOfMemory; the others complete
+    lone, _ = synth.predprey_population(2_000, 0, 256.0, 10)
+    c = srv.submit("predprey2d", _pp_params(dict(PP, max_crowd=1_000_000)), 60, 0,
+                   {"prey": (2_000, lone), "predator": (0, {"x": np.zeros(0, np.float32), "y": np.zeros(0, np.float32)})})
     srv.run_until_idle()
     done = srv.take_completed()
-    assert sorted(done) == [a, b]
+    assert sorted(done) == [a, b, c]
+    assert srv.info(c)["failed"] and "OutOfMemory" in srv.info(c)["error"]
+    assert not srv.info(a)["failed"] and not srv.info(b)["failed"]
     for k in ("_id", "x", "y"):
         np.testing.assert_array_equal(srv.get(a, "prey", k, np.float32 if k != "_id" else np.uint32),
                                       srv.get(b, "prey", k, np.float32 if k != "_id" else np.uint32))
