@@ -9,7 +9,9 @@
 //   k_stabilize  per sorted position: restores ascending original index inside
 //                short bins (<= kShortBin) and emits the record (or index);
 //                long bins are queued as 256-element chunks
-//   k_long       ranks the chunks of long bins against their whole bin
+//   k_long       orders long bins: up to 8192 messages by a bitonic sort of
+//                their indices in shared memory, longer ones by ranking each
+//                256-element chunk against the whole bin
 // The automatic agent sort runs the same pipeline on the reference's sort key
 // and finally gathers every agent column by the stable permutation.
 #include <algorithm>
@@ -254,19 +256,50 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
     }
 }
 
-// One block per queued chunk: each thread takes one element of the chunk and
-// counts the smaller original indices of its bin, staged through shared memory.
+// Long bins. A bin of up to kSortCap messages is ordered by one block: its
+// original indices (distinct) are sorted ascending in shared memory with a
+// bitonic network (Batcher 1968), padded to a power of two, and emitted in
+// order; the bin's chunk 0 does the work and its other chunks are skipped.
+// Longer bins rank every element against the whole bin, chunk by chunk.
+constexpr uint32_t kSortCap = 8192;
+
 template <int EMIT>
 __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ RecordParams rp,
                                                    const uint32_t* __restrict__ pbm,
                                                    const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                    const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
                                                    const WsHeader* h) {
-    __shared__ uint32_t s_idx[kRankTile];
+    __shared__ uint32_t s_idx[kSortCap];
     const uint32_t nchunks = min(h->long_count, chunk_cap);
     for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint2 ch = chunk_list[c];
         const uint32_t s = pbm[ch.x], e = pbm[ch.x + 1];
+        const uint32_t len = e - s;
+        if (len <= kSortCap) {
+            if (ch.y != 0) continue;  // the bin's chunk 0 orders the whole bin
+            uint32_t p2 = 64;
+            while (p2 < len) p2 <<= 1;
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) s_idx[k] = k < len ? perm[s + k] : 0xFFFFFFFFu;
+            __syncthreads();
+            for (uint32_t k = 2; k <= p2; k <<= 1) {
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    for (uint32_t t = threadIdx.x; t < p2; t += blockDim.x) {
+                        const uint32_t u = t ^ j;
+                        if (u > t) {
+                            const uint32_t a = s_idx[t], b = s_idx[u];
+                            if (((t & k) == 0) == (a > b)) {
+                                s_idx[t] = b;
+                                s_idx[u] = a;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) emit<EMIT>(rp, sperm, s_idx[k], s + k);
+            continue;
+        }
         const uint32_t q = s + ch.y * kChunk + threadIdx.x;
         const bool act = q < e;
         const uint32_t i = act ? perm[q] : 0u;

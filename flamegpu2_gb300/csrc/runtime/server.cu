@@ -157,7 +157,10 @@ size_t SimulationServer::poll() {
             j->sim->CUDAConfig().max_agents = static_cast<unsigned int>(std::min<size_t>(4 * largest, (1u << 31) - 1));
             for (auto& p : j->populations) j->sim->setPopulationData(p.second);
             j->populations.clear();
-            j->ring.assign(std::max(1u, cfg.steps_in_flight), nullptr);
+            const double by_work = cfg.work_in_flight / static_cast<double>(std::max<size_t>(j->agents, 1));
+            const unsigned int depth = static_cast<unsigned int>(
+                std::min(64.0, std::max(static_cast<double>(std::max(1u, cfg.steps_in_flight)), by_work)));
+            j->ring.assign(depth, nullptr);
             for (cudaEvent_t& e : j->ring)
                 if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
                     throw exception::CUDAError("cudaEventCreate failed");
@@ -178,9 +181,8 @@ size_t SimulationServer::poll() {
         Job& j = *jp;
         try {
             j.reap();
-            for (unsigned int s = 0; s < cfg.steps_per_poll && j.issued < j.steps &&
-                                     j.issued - j.completed < j.ring.size();
-                 ++s) {
+            const unsigned int per_poll = std::max<unsigned int>(cfg.steps_per_poll, static_cast<unsigned int>(j.ring.size()));
+            for (unsigned int s = 0; s < per_poll && j.issued < j.steps && j.issued - j.completed < j.ring.size(); ++s) {
                 j.sim->step();
                 if (cudaEventRecord(j.ring[j.issued % j.ring.size()], j.sim->getStream()) != cudaSuccess)
                     throw exception::CUDAError("cudaEventRecord failed");

@@ -246,6 +246,15 @@ extern "C" int fgs_profile_ops(fgs_sim* s, int32_t enable) {
     return guarded([&] { s->sim->CUDAConfig().profile_ops = enable != 0; });
 }
 
+extern "C" int fgs_time_ops_in_graphs(fgs_sim* s, int32_t enable) {
+    return guarded([&] {
+        s->sim->CUDAConfig().time_ops_in_graphs = enable != 0;
+        s->sim->applyConfig();
+    });
+}
+
+extern "C" int fgs_harvest_profile(fgs_sim* s) { return guarded([&] { s->sim->harvestOperationTimes(); }); }
+
 extern "C" int fgs_take_profile(fgs_sim* s, char* buf, size_t len) {
     return guarded([&] {
         std::string out;

@@ -24,6 +24,7 @@
 #include <map>
 #include <memory>
 #include <random>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -241,6 +242,13 @@ struct SimulationImpl {
     bool profiling = false;
     std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>> op_events;
     std::map<std::string, std::pair<double, uint64_t>> op_totals;  // label -> (ms, count)
+    // timing events captured into the step graphs (Config::time_ops_in_graphs):
+    // per graph key, the event pairs around each operation, and the keys
+    // replayed since the last harvest
+    bool capturing = false;
+    std::vector<int> capture_key;
+    std::map<std::vector<int>, std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>>> graph_op_events;
+    std::set<std::vector<int>> replayed;
     // timing
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> step_events;
     std::vector<double> step_ms;
@@ -254,6 +262,7 @@ struct SimulationImpl {
             cudaStreamSynchronize(stream);
         }
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        drop_graph_op_events();
         for (auto& e : step_events) {
             cudaEventDestroy(e.first);
             cudaEventDestroy(e.second);
@@ -470,7 +479,37 @@ struct SimulationImpl {
     void invalidate() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         graphs.clear();
+        drop_graph_op_events();
         allocated = false;
+    }
+
+    void drop_graph_op_events() {
+        for (auto& kv : graph_op_events)
+            for (auto& t : kv.second) {
+                cudaEventDestroy(std::get<1>(t));
+                cudaEventDestroy(std::get<2>(t));
+            }
+        graph_op_events.clear();
+        replayed.clear();
+    }
+
+    // Adds the operation times of the last replay of every graph replayed
+    // since the previous call to the operation profile (waits for the stream).
+    void harvest_graph_ops() {
+        if (replayed.empty()) return;
+        FG_CUDA(cudaStreamSynchronize(stream));
+        for (const auto& key : replayed) {
+            auto it = graph_op_events.find(key);
+            if (it == graph_op_events.end()) continue;
+            for (auto& t : it->second) {
+                float ms = 0.0f;
+                if (cudaEventElapsedTime(&ms, std::get<1>(t), std::get<2>(t)) != cudaSuccess) continue;
+                auto& acc = op_totals[std::get<0>(t)];
+                acc.first += ms;
+                acc.second += 1;
+            }
+        }
+        replayed.clear();
     }
 
     // Lists with no population yet still need buffers for their functions.
@@ -697,17 +736,32 @@ struct SimulationImpl {
     // Runs op() on the stream, bracketed by events when profiling (eager mode).
     template <typename Op>
     void timed(const std::string& label, Op&& op) {
-        if (!profiling) {
+        timed_on(stream, label, std::forward<Op>(op));
+    }
+    // Runs op() on stream `st`: bracketed by events when profiling (eager), or
+    // by event-record nodes of the step graph being captured when
+    // Config::time_ops_in_graphs is set.
+    template <typename Op>
+    void timed_on(cudaStream_t st, const std::string& label, Op&& op) {
+        const bool in_graph = capturing && cuda_config.time_ops_in_graphs;
+        if (!profiling && !in_graph) {
             op();
             return;
         }
         cudaEvent_t a, b;
         FG_CUDA(cudaEventCreate(&a));
         FG_CUDA(cudaEventCreate(&b));
-        FG_CUDA(cudaEventRecord(a, stream));
-        op();
-        FG_CUDA(cudaEventRecord(b, stream));
-        op_events.emplace_back(label, a, b);
+        if (in_graph) {
+            FG_CUDA(cudaEventRecordWithFlags(a, st, cudaEventRecordExternal));
+            op();
+            FG_CUDA(cudaEventRecordWithFlags(b, st, cudaEventRecordExternal));
+            graph_op_events[capture_key].emplace_back(label, a, b);
+        } else {
+            FG_CUDA(cudaEventRecord(a, st));
+            op();
+            FG_CUDA(cudaEventRecord(b, st));
+            op_events.emplace_back(label, a, b);
+        }
     }
 
     void resolve_profile() {
@@ -781,8 +835,8 @@ struct SimulationImpl {
             // two branches of the step graph (fork/join through events)
             FG_CUDA(cudaEventRecord(fork_ev, stream));
             FG_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
-            enqueue_build(*f.in, side);
-            enqueue_sort(f);
+            timed_on(side, "build:" + f.in->msg->name, [&] { enqueue_build(*f.in, side); });
+            timed_on(stream, "sort:" + l.agent->name, [&] { enqueue_sort(f); });
             FG_CUDA(cudaEventRecord(join_ev, side));
             FG_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
         } else {
@@ -938,12 +992,16 @@ struct SimulationImpl {
             if (it == graphs.end()) {
                 cudaGraph_t g;
                 FG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                capturing = true;
+                capture_key = key;
                 try {
                     enqueue_step();
                 } catch (...) {
+                    capturing = false;
                     cudaStreamEndCapture(stream, &g);
                     throw;
                 }
+                capturing = false;
                 FG_CUDA(cudaStreamEndCapture(stream, &g));
                 cudaGraphExec_t ge;
                 FG_CUDA(cudaGraphInstantiate(&ge, g, 0));
@@ -957,6 +1015,7 @@ struct SimulationImpl {
             }
             FG_CUDA(cudaGraphLaunch(it->second, stream));
             ++graph_launches;
+            if (cuda_config.time_ops_in_graphs) replayed.insert(key);
         }
         FG_CUDA(cudaEventRecord(e1, stream));
         step_events.emplace_back(e0, e1);
@@ -1084,6 +1143,8 @@ void CUDASimulation::applyConfig() { impl->invalidate(); }
 cudaStream_t CUDASimulation::getStream() const { return impl->stream; }
 unsigned long long CUDASimulation::getGraphLaunches() const { return impl->graph_launches; }
 unsigned int CUDASimulation::getKernelsPerStep() const { return impl->kernels_last_step; }
+
+void CUDASimulation::harvestOperationTimes() { impl->harvest_graph_ops(); }
 
 std::vector<std::tuple<std::string, double, unsigned long long>> CUDASimulation::takeOperationProfile() {
     FG_CUDA(cudaStreamSynchronize(impl->stream));

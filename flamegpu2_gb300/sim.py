@@ -21,7 +21,7 @@ SIM_EXPORTS = [
     "fgs_set_population", "fgs_set_population_device", "fgs_get_count", "fgs_get_variable", "fgs_get_population",
     "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
     "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
-    "fgs_set_stage_bytes", "fgs_reset_population_device",
+    "fgs_set_stage_bytes", "fgs_reset_population_device", "fgs_time_ops_in_graphs", "fgs_harvest_profile",
 ]
 
 _lock = threading.Lock()
@@ -67,6 +67,8 @@ def core():
             L.fgs_reset_population_device.argtypes = [vp, C.c_char_p, C.c_char_p, u32, i32, C.POINTER(C.c_char_p),
                                                       C.POINTER(vp), u32]
             L.fgs_take_profile.argtypes = [vp, C.c_char_p, sz]
+            L.fgs_time_ops_in_graphs.argtypes = [vp, i32]
+            L.fgs_harvest_profile.argtypes = [vp]
             _core = L
         if _models is None:
             if not os.path.exists(MODELS_LIB):
@@ -204,6 +206,12 @@ class Simulation:
 
     def profile_ops(self, enable: bool = True):
         _check(core().fgs_profile_ops(self._h, int(enable)))
+
+    def time_ops_in_graphs(self, enable: bool = True):
+        _check(core().fgs_time_ops_in_graphs(self._h, int(enable)))
+
+    def harvest_profile(self):
+        _check(core().fgs_harvest_profile(self._h))
 
     def take_profile(self) -> dict:
         """label -> (total_ms, count) of the operations issued since the last call."""

@@ -29,13 +29,16 @@ def _bench_common():
     return bench
 
 
-def _stage_table(prof: dict, algo: dict) -> dict:
+def _stage_table(prof: dict, algo: dict, per_launch: bool = True) -> dict:
+    """prof: label -> (total ms, launches). algo: algorithmic bytes of one
+    launch (per_launch) or of all the profiled launches together."""
     out = {}
     for label, (ms, cnt) in prof.items():
         d = {"launches": cnt, "avg_us": round(ms * 1000.0 / max(cnt, 1), 3), "total_ms": round(ms, 4)}
         if label in algo:
-            d["algorithmic_bytes_total"] = int(algo[label])
-            d["gbs"] = round(algo[label] / (ms * 1e-3) / 1e9, 2) if ms > 0 else None
+            total = algo[label] * cnt if per_launch else algo[label]
+            d["algorithmic_bytes_total"] = int(total)
+            d["gbs"] = round(total / (ms * 1e-3) / 1e9, 2) if ms > 0 else None
         out[label] = d
     return out
 
@@ -64,6 +67,7 @@ def run_birth_death(args, world, rank, local):
     resident = {k: torch.from_numpy(pop[k].view(np.int32) if pop[k].dtype == np.uint32 else pop[k]).to(dev)
                 for k in names}
     s = sim.Simulation("birth_death", [0.30, 0.20, seed], device=local)
+    s.time_ops_in_graphs(True)  # per-operation times from events inside the step graphs
 
     def reset():
         s.reset_population_device("agent", n0, resident, n0 + 1)
@@ -79,6 +83,7 @@ def run_birth_death(args, world, rank, local):
         reset()
         s.step(steps_per)
     s.synchronize()
+    s.take_profile()
     kps = s.stats()["kernels_per_step"]
     stream = torch.cuda.ExternalStream(s.stream, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -102,12 +107,16 @@ def run_birth_death(args, world, rank, local):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     device_ms = B.allreduce_max(world, sum(times))
-    # op profile of one run (eager, event-bracketed)
+    # per-operation times of every one of the 100 steps (the population and so
+    # the work changes each step): the same graph replays, one step at a time,
+    # reading the timing events captured into the graphs after each
     reset()
-    s.profile_ops(True)
-    s.step(steps_per)
+    s.take_profile()
+    for _ in range(steps_per):
+        s.step(1)
+        s.harvest_profile()
     prof = s.take_profile()
-    s.profile_ops(False)
+    s.time_ops_in_graphs(False)
     # e2e: host population in, 100 steps, host population out
     host_in = {k: pop[k] for k in names}
     outs = {k: np.empty(4 * n0, dtype=pop[k].dtype) for k in names}
@@ -123,7 +132,7 @@ def run_birth_death(args, world, rank, local):
     row = 44  # 8 f32 + counter + _id
     comp_bytes = sum(pops[t] * row + (pops[t + 1] if t + 1 < steps_per else final) * row for t in range(steps_per))
     peak, peak_kind = B.measured_peaks()
-    stages = _stage_table(prof, {"compact:agent": comp_bytes})
+    stages = _stage_table(prof, {"compact:agent": comp_bytes}, per_launch=False)
     return {
         "metric": B.METRIC, "value": round(agent_steps * k_steps * world / (device_ms / 1000.0), 1), "unit": UNIT,
         "n_gpus": world, "steps": k_steps, "warmup": args.warmup, "ms_per_step": round(device_ms / k_steps, 4),
@@ -193,9 +202,11 @@ def run_spatial_large(name, args, world, rank, local):
     cand = candidate_pairs(pos, edge, r)
     s = sim.Simulation("spatial_payload", [dims, 0.0, edge, r], device=local)
     s.set_population("agent", n, cols)
+    s.time_ops_in_graphs(True)  # per-operation times from events inside the step graphs
     for _ in range(args.warmup):
         s.step(1)
     s.synchronize()
+    s.take_profile()
     kps = s.stats()["kernels_per_step"]
     stream = torch.cuda.ExternalStream(s.stream, device=dev)
     clocks = B.ClockSampler(local)
@@ -209,14 +220,13 @@ def run_spatial_large(name, args, world, rank, local):
         ev[k][0].record(stream)
         s.step(1)
         ev[k][1].record(stream)
+        ev[k][1].synchronize()
+        s.harvest_profile()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     device_ms = B.allreduce_max(world, sum(a.elapsed_time(b) for a, b in ev))
-    s.profile_ops(True)
-    s.step(1)
     prof = s.take_profile()
-    s.profile_ops(False)
     s.close()
     vm = 4 * dims + 16  # position + 4 payload floats
     va_r, va_w = vm, 16
@@ -228,7 +238,8 @@ def run_spatial_large(name, args, world, rank, local):
     stages = _stage_table(prof, algo)
     if "fn:in" in stages:
         stages["fn:in"]["candidate_pairs"] = cand
-        stages["fn:in"]["candidate_pairs_per_s"] = round(cand / (stages["fn:in"]["total_ms"] * 1e-3), 1)
+        stages["fn:in"]["candidate_pairs_per_s"] = round(cand * stages["fn:in"]["launches"] /
+                                                         (stages["fn:in"]["total_ms"] * 1e-3), 1)
     bd = stages.get("build:location", {})
     roof = {"bound": "hbm", "kernel": "build:location (5 kernels: bin, scan, perm, stabilise, long bins)",
             "achieved": bd.get("gbs"), "peak": peak, "unit": "GB/s",

@@ -85,6 +85,10 @@ class CUDASimulation {
         bool use_graphs = true;       // capture each step into a CUDA graph and replay it
         bool check_each_step = false; // synchronise and check device errors after every step()
         bool profile_ops = false;     // issue steps eagerly and time every operation with CUDA events
+        // Capture a pair of timing events around every operation into the step
+        // graphs; harvestOperationTimes() adds the times of the last replay of
+        // each graph to the operation profile. Steps stay graph replays.
+        bool time_ops_in_graphs = false;
         unsigned int message_stage_bytes = 96u * 1024u;  // shared memory per block for spatial neighbour windows (0: off)
         // Largest population an agent list may reach, births included: buffers
         // never grow past it, and a step that could exceed it (checked when the
@@ -156,6 +160,10 @@ class CUDASimulation {
     /** Per-operation device time since the last call ("fn:<name>", "build:<message>",
      *  "sort:<agent>", "compact:<agent>" -> total ms, count); needs CUDAConfig().profile_ops. */
     std::vector<std::tuple<std::string, double, unsigned long long>> takeOperationProfile();
+    /** With CUDAConfig().time_ops_in_graphs: waits for the stream, then adds the
+     *  operation times of the last replay of each graph replayed since the
+     *  previous call to the profile that takeOperationProfile() returns. */
+    void harvestOperationTimes();
 
     detail::SimulationImpl* getImpl() const { return impl.get(); }
 

@@ -6,10 +6,11 @@
 // and message state resident in HBM, and advance together — every poll issues
 // the next step of every admitted run on that run's own stream, so their
 // kernels overlap on the device, and runs that arrive meanwhile join at the
-// next poll (continuous batching). Each run keeps at most steps_in_flight steps
-// queued on the device, so a long run cannot bury a short one under its
-// backlog; runs with the least remaining work are issued first, and their
-// streams get a higher priority. A finished run is read back and its memory
+// next poll (continuous batching). Each run keeps a bounded number of steps
+// queued on the device (about work_in_flight agent-steps, at least
+// steps_in_flight), so a long run cannot bury a short one under its backlog
+// while a small run still advances many steps per poll; runs with the least
+// remaining work are issued first, and their streams get a higher priority. A finished run is read back and its memory
 // returned without waiting for the others; a run that fails is completed with
 // its error and the others carry on.
 #include <chrono>
@@ -34,7 +35,10 @@ class SimulationServer {
         size_t memory_budget = 150ull << 30;  // bytes of device memory runs may reserve
         unsigned int max_active = 64;         // runs on the device at once
         unsigned int steps_per_poll = 1;      // steps issued per run per poll
-        unsigned int steps_in_flight = 2;     // steps of one run queued on the device at once
+        unsigned int steps_in_flight = 2;     // steps of one run queued on the device at once (at least)
+        // ... and up to work_in_flight / (the run's initial agents) steps, at most 64:
+        // small runs keep enough steps queued to advance between two polls
+        double work_in_flight = 4.0e6;
         int device = 0;
         bool use_graphs = true;
     };

@@ -74,6 +74,12 @@ int fgs_profile_ops(fgs_sim* sim, int32_t enable);
 /* Per-operation totals since the last call as "label,total_ms,count;..." (see
  * CUDASimulation::takeOperationProfile). */
 int fgs_take_profile(fgs_sim* sim, char* buf, size_t len);
+/* Enable/disable timing events captured into the step graphs around every
+ * operation (CUDASimulation::Config::time_ops_in_graphs; rebuilds the graphs). */
+int fgs_time_ops_in_graphs(fgs_sim* sim, int32_t enable);
+/* Adds the operation times of the last replay of each graph replayed since the
+ * previous call to the profile read by fgs_take_profile (waits for the stream). */
+int fgs_harvest_profile(fgs_sim* sim);
 /* getElapsedTimeSteps (seconds) for up to cap steps; returns the count in *n. */
 int fgs_step_times(fgs_sim* sim, double* out, uint32_t cap, uint32_t* n);
 

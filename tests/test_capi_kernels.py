@@ -187,6 +187,27 @@ def test_build_one_heavy_bin_and_reuse():
 
 
 @pytest.mark.gpu
+def test_build_long_bins_sorted_and_ranked():
+    # bins of 33 .. 8192 messages are ordered by the shared-memory sort, 8193
+    # and more by chunk ranking; messages of all bins interleaved at random
+    rng = np.random.default_rng(11)
+    g = _capi().grid(3, (0, 0, 0), (8, 8, 8), 1.0)
+    sizes = [33, 64, 65, 257, 1000, 4096, 5000, 8191, 8192, 8193, 9000, 1, 2, 31, 32]
+    cells = rng.choice(512, len(sizes), replace=False)
+    pos = []
+    for c, k in zip(cells, sizes):
+        cx, cy, cz = c % 8, (c // 8) % 8, c // 64
+        pos.append(np.stack([cx + rng.uniform(0.01, 0.99, k), cy + rng.uniform(0.01, 0.99, k),
+                             cz + rng.uniform(0.01, 0.99, k)], 1))
+    pos = np.concatenate(pos).astype(np.float32)
+    pos = pos[rng.permutation(len(pos))]
+    pbm, srt, payload, _ = _build(g, pos, reps=2)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    np.testing.assert_array_equal(srt[:len(pos), 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 4095, 4096, 4097, 1_000_000, 17_000_001])
 def test_exclusive_scan(n):
     import torch

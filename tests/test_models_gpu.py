@@ -194,3 +194,34 @@ def test_birth_death_matches_oracle_exactly():
     np.testing.assert_array_equal(ids, io)
     np.testing.assert_array_equal(cnt, co)
     np.testing.assert_array_equal(f, fo)
+
+
+def test_operation_times_from_step_graphs():
+    # timing events captured into the step graphs: steps stay graph replays,
+    # results are unchanged, and every operation of the step is timed
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    cfg = dict(synth.BOIDS_SMALL)
+    params = synth.boids_params(cfg)
+    pop = synth.boids_population(cfg["n"], cfg["min_pos"], cfg["max_pos"], 3)
+    outs = []
+    for timed in (False, True):
+        s = S.Simulation("boids_spatial3d", params)
+        s.set_population("Boid", cfg["n"], pop)
+        if timed:
+            s.time_ops_in_graphs(True)
+        for _ in range(4):
+            s.step(1)
+            s.harvest_profile()
+        prof = s.take_profile()
+        st = s.stats()
+        outs.append({k: s.get("Boid", k, np.float32) for k in ("x", "fx")})
+        s.close()
+        if timed:
+            assert st["graph_launches"] == 4
+            for label in ("fn:outputdata", "fn:inputdata", "sort:Boid", "build:location"):
+                assert label in prof and prof[label][1] >= 2 and prof[label][0] > 0.0, (label, prof)
+        else:
+            assert prof == {}
+    for k in ("x", "fx"):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
