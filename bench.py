@@ -250,7 +250,7 @@ def run_boids_small(args, world, rank, local):
                    "l2": "flushed between bench steps (256 MiB write)", "parallelism": f"replicas x{world}"},
         "wall_s": round(wall, 4),
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": 28 * n, "d2h_bytes_per_step": 28 * n,
-                "path": "fgs_set_population + fgs_step(10) + fgs_get_variable x7 (C ABI, host buffers)"},
+                "path": "fgs_set_population + fgs_step(10) + fgs_get_population (C ABI, pinned host buffers)"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": None,
                      "peak_source": peak_kind, "per_launch_algorithmic_bytes": algo.get(dom)},

@@ -9,9 +9,10 @@
 //   k_stabilize  per sorted position: restores ascending original index inside
 //                short bins (<= kShortBin) and emits the record (or index);
 //                long bins are queued as 256-element chunks
-//   k_long       orders long bins: up to 8192 messages by a bitonic sort of
-//                their indices in shared memory, longer ones by ranking each
-//                256-element chunk against the whole bin
+//   k_long       orders long bins: up to 8192 messages by a bitmap over the
+//                span of their indices (narrow spans) or a bitonic sort in
+//                shared memory, longer ones by ranking each 256-element chunk
+//                against the whole bin
 // The automatic agent sort runs the same pipeline on the reference's sort key
 // and finally gathers every agent column by the stable permutation.
 #include <algorithm>
@@ -256,12 +257,17 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
     }
 }
 
-// Long bins. A bin of up to kSortCap messages is ordered by one block: its
-// original indices (distinct) are sorted ascending in shared memory with a
-// bitonic network (Batcher 1968), padded to a power of two, and emitted in
-// order; the bin's chunk 0 does the work and its other chunks are skipped.
-// Longer bins rank every element against the whole bin, chunk by chunk.
+// Long bins. A bin of up to kSortCap messages is ordered by one block (the
+// bin's chunk 0; its other chunks are skipped). When its original indices
+// span at most kSpanCap values (messages that arrive nearly in bin order, as
+// those of spatially sorted agents do), each index sets one bit of a bitmap
+// over that span and its rank is the number of set bits before it: O(length
+// + span / 32). Otherwise the indices (distinct) are sorted ascending in
+// shared memory with a bitonic network (Batcher 1968), padded to a power of
+// two. Longer bins rank every element against the whole bin, chunk by chunk.
 constexpr uint32_t kSortCap = 8192;
+constexpr uint32_t kSpanWords = kSortCap / 2;   // bitmap words; the other half holds their prefix counts
+constexpr uint32_t kSpanCap = kSpanWords * 32;  // 131,072 indices
 
 template <int EMIT>
 __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ RecordParams rp,
@@ -270,6 +276,8 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ Recor
                                                    const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
                                                    const WsHeader* h) {
     __shared__ uint32_t s_idx[kSortCap];
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_lo, s_hi;
     const uint32_t nchunks = min(h->long_count, chunk_cap);
     for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint2 ch = chunk_list[c];
@@ -277,6 +285,60 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ Recor
         const uint32_t len = e - s;
         if (len <= kSortCap) {
             if (ch.y != 0) continue;  // the bin's chunk 0 orders the whole bin
+            // span of the bin's original indices
+            uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+            for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) {
+                const uint32_t i = perm[s + k];
+                lo = min(lo, i);
+                hi = max(hi, i);
+            }
+            lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+            hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+            __syncthreads();  // the previous bin is done with shared memory
+            if (threadIdx.x == 0) {
+                s_lo = 0xFFFFFFFFu;
+                s_hi = 0u;
+            }
+            __syncthreads();
+            if ((threadIdx.x & 31u) == 0) {
+                atomicMin(&s_lo, lo);
+                atomicMax(&s_hi, hi);
+            }
+            __syncthreads();
+            lo = s_lo;
+            hi = s_hi;
+            if (hi - lo < kSpanCap) {
+                const uint32_t words = (hi - lo) / 32u + 1u;
+                uint32_t* bits = s_idx;
+                uint32_t* before = s_idx + kSpanWords;
+                for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0u;
+                __syncthreads();
+                for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) {
+                    const uint32_t d = perm[s + k] - lo;
+                    atomicOr(&bits[d >> 5], 1u << (d & 31u));
+                }
+                __syncthreads();
+                // set bits before each word: each thread sums a run of words,
+                // a block scan offsets the runs
+                const uint32_t per = (words + blockDim.x - 1) / blockDim.x;
+                const uint32_t w0 = threadIdx.x * per;
+                uint32_t run = 0;
+                for (uint32_t w = w0; w < min(w0 + per, words); ++w) run += __popc(bits[w]);
+                uint32_t total;
+                uint32_t acc = block_exclusive_scan(run, &total, s_warp);
+                for (uint32_t w = w0; w < min(w0 + per, words); ++w) {
+                    before[w] = acc;
+                    acc += __popc(bits[w]);
+                }
+                __syncthreads();
+                for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) {
+                    const uint32_t i = perm[s + k];
+                    const uint32_t d = i - lo;
+                    const uint32_t rank = before[d >> 5] + __popc(bits[d >> 5] & ((1u << (d & 31u)) - 1u));
+                    emit<EMIT>(rp, sperm, i, s + rank);
+                }
+                continue;
+            }
             uint32_t p2 = 64;
             while (p2 < len) p2 <<= 1;
             __syncthreads();

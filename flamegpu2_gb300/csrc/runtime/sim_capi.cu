@@ -107,6 +107,22 @@ extern "C" int fgs_configure(fgs_sim* s, uint32_t steps, uint64_t seed, int32_t 
 extern "C" int fgs_set_population(fgs_sim* s, const char* agent, const char* state, uint32_t n, int32_t nvars,
                                   const char* const* names, const void* const* cols) {
     return guarded([&] {
+        // every variable given with every id set: straight to the device
+        const auto* ad = s->model->Agent(agent).getData();
+        bool all = static_cast<size_t>(nvars) == ad->variables.size();
+        std::vector<std::pair<std::string, const void*>> direct;
+        for (int32_t k = 0; k < nvars && all; ++k) {
+            all = ad->find(names[k]) != nullptr;
+            direct.emplace_back(names[k], cols[k]);
+            if (all && std::strcmp(names[k], "_id") == 0) {
+                const flamegpu::id_t* ids = static_cast<const flamegpu::id_t*>(cols[k]);
+                for (uint32_t i = 0; i < n && all; ++i) all = ids[i] != flamegpu::ID_NOT_SET;
+            }
+        }
+        if (all) {
+            s->sim->setPopulationColumns(agent, state ? state : "default", n, direct);
+            return;
+        }
         flamegpu::AgentVector pop(s->model->Agent(agent), n);
         for (int32_t k = 0; k < nvars; ++k) {
             const size_t c = pop.columnIndex(names[k]);
@@ -164,14 +180,9 @@ extern "C" int fgs_get_variable(fgs_sim* s, const char* agent, const char* state
 extern "C" int fgs_get_population(fgs_sim* s, const char* agent, const char* state, int32_t nvars,
                                   const char* const* names, void* const* out, uint32_t cap, uint32_t* n) {
     return guarded([&] {
-        flamegpu::AgentVector pop(s->model->Agent(agent));
-        s->sim->getPopulationData(pop, state);
-        if (pop.size() > cap) throw flamegpu::exception::InvalidArgument("output buffers too small");
-        for (int32_t k = 0; k < nvars; ++k) {
-            const auto& col = pop.columns()[pop.columnIndex(names[k])];
-            std::memcpy(out[k], col.data(), col.size());
-        }
-        *n = pop.size();
+        std::vector<std::pair<std::string, void*>> cols;
+        for (int32_t k = 0; k < nvars; ++k) cols.emplace_back(names[k], out[k]);
+        *n = s->sim->getPopulationColumns(agent, state ? state : "default", cols, cap);
     });
 }
 

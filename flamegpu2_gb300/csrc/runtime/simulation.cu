@@ -55,6 +55,7 @@ namespace {
 
 __global__ void k_step_increment(uint32_t* d_step) { *d_step += 1; }
 __global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
+__global__ void k_max_u32(uint32_t* p, uint32_t v) { *p = *p > v ? *p : v; }
 
 // Device buffers of one simulation, taken stream-ordered from the device's
 // default memory pool: a finished simulation returns its memory without
@@ -1043,19 +1044,26 @@ struct SimulationImpl {
     }
 
     void check_errors() {
+        // the error record and every workspace's status word, read with one
+        // batch of async copies into pinned memory and one wait
+        uint32_t* hp = h_pinned + 64;
+        const uint32_t cap = 1024 - 64;
+        FG_CUDA(cudaMemcpyAsync(hp, d_error(), 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        std::vector<std::pair<void*, std::string>> ws;
+        for (auto& m : msgs)
+            if (m->build_ws) ws.emplace_back(m->build_ws, format("Message '%s' index build", m->msg->name.c_str()));
+        for (auto& l : lists)
+            if (l->comp_ws) ws.emplace_back(l->comp_ws, format("Compaction of agent '%s'", l->agent->name.c_str()));
+        for (size_t k = 0; k < ws.size() && 4 + k < cap; ++k)
+            FG_CUDA(cudaMemcpyAsync(hp + 4 + k, ws[k].first, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
         FG_CUDA(cudaStreamSynchronize(stream));
-        uint32_t err[4] = {0, 0, 0, 0};
-        FG_CUDA(cudaMemcpy(err, d_error(), sizeof(err), cudaMemcpyDeviceToHost));
-        for (auto& m : msgs) {
-            if (m->build_ws) {
-                const int s = fg_workspace_status(m->build_ws, m->build_ws_bytes, stream, 1);
-                if (s != FG_OK) THROW exception::DeviceError(format("Message '%s' index build reported status %d", m->msg->name.c_str(), s));
-            }
-        }
-        for (auto& l : lists) {
-            if (l->comp_ws) {
-                const int s = fg_workspace_status(l->comp_ws, l->comp_ws_bytes, stream, 1);
-                if (s != FG_OK) THROW exception::DeviceError(format("Compaction of agent '%s' reported status %d", l->agent->name.c_str(), s));
+        uint32_t err[4] = {hp[0], hp[1], hp[2], hp[3]};
+        for (size_t k = 0; k < ws.size() && 4 + k < cap; ++k) {
+            const int st = static_cast<int>(static_cast<int32_t>(hp[4 + k]));
+            if (st != FG_OK) {
+                FG_CUDA(cudaMemsetAsync(ws[k].first, 0, sizeof(uint32_t), stream));
+                FG_CUDA(cudaStreamSynchronize(stream));
+                THROW exception::DeviceError(format("%s reported status %d", ws[k].second.c_str(), st));
             }
         }
         if (err[0] != 0) {
@@ -1198,6 +1206,71 @@ void CUDASimulation::getPopulationData(AgentVector& pop, const std::string& stat
         const size_t b = l->agent->variables[v].bytes();
         if (n) FG_CUDA(cudaMemcpy(pop.columns()[v].data(), l->cols[v][l->parity], b * n, cudaMemcpyDeviceToHost));
     }
+}
+
+void CUDASimulation::setPopulationColumns(const std::string& agent, const std::string& state, uint32_t n,
+                                          const std::vector<std::pair<std::string, const void*>>& host_cols) {
+    detail::AgentList* l = impl->list_of(agent, state);
+    std::vector<const void*> src(l->cols.size(), nullptr);
+    for (const auto& c : host_cols) {
+        size_t v = 0;
+        while (v < l->agent->variables.size() && l->agent->variables[v].name != c.first) ++v;
+        if (v == l->agent->variables.size())
+            THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), c.first.c_str()));
+        src[v] = c.second;
+    }
+    size_t idc = l->cols.size();
+    for (size_t v = 0; v < src.size(); ++v) {
+        if (!src[v] && n)
+            THROW exception::InvalidArgument(format("setPopulationColumns: variable '%s' not given",
+                                                    l->agent->variables[v].name.c_str()));
+        if (l->agent->variables[v].name == "_id") idc = v;
+    }
+    id_t mx = 0;
+    if (idc < src.size() && n) {
+        const id_t* ids = static_cast<const id_t*>(src[idc]);
+        for (uint32_t i = 0; i < n; ++i) {
+            if (ids[i] == ID_NOT_SET) THROW exception::InvalidArgument("setPopulationColumns: every _id must be set");
+            mx = std::max(mx, ids[i]);
+        }
+    }
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    const uint32_t cap = std::max<uint32_t>(1024u, n);
+    if (cap > l->capacity) impl->ensure_capacity(*l, cap, 0);
+    for (size_t v = 0; v < l->cols.size(); ++v) {
+        const size_t b = l->agent->variables[v].bytes();
+        if (n) FG_CUDA(cudaMemcpyAsync(l->cols[v][l->parity], src[v], b * n, cudaMemcpyHostToDevice, impl->stream));
+    }
+    // next id: the larger of the device's and one past the largest given
+    detail::k_max_u32<<<1, 1, 0, impl->stream>>>(impl->d_next_id(impl->agent_index(l->agent)), mx + 1);
+    impl->h_pinned[2] = n;
+    FG_CUDA(cudaMemcpyAsync(l->d_count, impl->h_pinned + 2, sizeof(uint32_t), cudaMemcpyHostToDevice, impl->stream));
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    l->bound = n;
+    impl->forget_counts();
+    impl->ensure_all_allocated();
+}
+
+uint32_t CUDASimulation::getPopulationColumns(const std::string& agent, const std::string& state,
+                                              const std::vector<std::pair<std::string, void*>>& host_out,
+                                              uint32_t cap) {
+    detail::AgentList* l = impl->list_of(agent, state);
+    synchronize();
+    FG_CUDA(cudaMemcpyAsync(impl->h_pinned + 3, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, impl->stream));
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    const uint32_t n = impl->h_pinned[3];
+    l->bound = n;
+    if (n > cap) THROW exception::InvalidArgument(format("getPopulationColumns: %u agents, room for %u", n, cap));
+    for (const auto& o : host_out) {
+        size_t v = 0;
+        while (v < l->agent->variables.size() && l->agent->variables[v].name != o.first) ++v;
+        if (v == l->agent->variables.size())
+            THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), o.first.c_str()));
+        const size_t b = l->agent->variables[v].bytes();
+        if (n) FG_CUDA(cudaMemcpyAsync(o.second, l->cols[v][l->parity], b * n, cudaMemcpyDeviceToHost, impl->stream));
+    }
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    return n;
 }
 
 bool CUDASimulation::step() {

@@ -8,6 +8,13 @@ timings, outside the benchmark's timed loop.
   python -m flamegpu2_gb300.profile_cases ensemble --count 32
       The first `count` instances of the 256-instance Boids ensemble, 5 steps,
       as one batched simulation.
+  python -m flamegpu2_gb300.profile_cases build --dims 3
+      Five spatial message builds through the C ABI (fg_spatial_build) of the
+      large workloads' positions: 8,388,608 Gaussian-mixture messages on 256^3
+      bins (--dims 3) or 16,777,216 uniform messages on 1024^2 bins (--dims 2),
+      records of position + 4 payload words; prints the mean build time.
+      --sorted orders the messages by bin first, as the messages of agents
+      that the automatic spatial sort has ordered arrive in a simulation.
 """
 from __future__ import annotations
 
@@ -59,13 +66,60 @@ def ensemble(count: int, steps: int = 5):
     return {"instances": count, "agents": sum(sp["n"] for sp in specs), **st}
 
 
+def build(dims: int, presorted: bool = False, reps: int = 5):
+    import ctypes as C
+    import torch
+    from flamegpu2_gb300 import capi, synth, workloads
+    if dims == 3:
+        pos = workloads.gaussian_mixture_3d(1 << 23, 256.0, 16, 2.0, 2)
+        g = capi.grid(3, (0, 0, 0), (256, 256, 256), 1.0)
+    else:
+        n = 1 << 24
+        hi = np.nextafter(np.float32(4096.0), np.float32(0))
+        pos = np.stack([np.minimum(synth.uniform(3, a, n, 0.0, 4096.0), hi) for a in range(2)], 1)
+        g = capi.grid(2, (0, 0), (4096, 4096), 4.0)
+    n = pos.shape[0]
+    if presorted:
+        cell = [np.clip(np.floor((pos[:, a] - np.float32(g.min[a])) / np.float32(g.radius)).astype(np.int64), 0,
+                        g.gridDim[a] - 1) for a in range(dims)]
+        key = cell[0] + cell[1] * g.gridDim[0] + (cell[2] * g.gridDim[0] * g.gridDim[1] if dims == 3 else 0)
+        pos = pos[np.argsort(key, kind="stable")]
+    cols = [torch.from_numpy(np.ascontiguousarray(pos[:, a])).cuda() for a in range(dims)]
+    payload = torch.rand((n, 4), device="cuda")
+    rec = capi.record_desc(cols + [payload])
+    out = torch.empty((n, rec.words), dtype=torch.int32, device="cuda")
+    pbm = torch.empty(g.binCount + 1, dtype=torch.int32, device="cuda")
+    ws = capi.Workspace(capi.lib().fg_spatial_build_workspace_size(n, g.binCount))
+    st = capi.stream_handle()
+    args = (C.byref(g), n, None, cols[0].data_ptr(), cols[1].data_ptr(), cols[2].data_ptr() if dims == 3 else None,
+            None, C.byref(rec), out.data_ptr(), pbm.data_ptr(), ws.ptr, ws.nbytes, st)
+    capi.check(capi.lib().fg_spatial_build(*args), "fg_spatial_build")
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        capi.check(capi.lib().fg_spatial_build(*args), "fg_spatial_build")
+    b.record()
+    b.synchronize()
+    assert ws.status() == 0
+    return {"dims": dims, "sorted_input": presorted, "messages": n, "bins": g.binCount, "record_bytes": rec.words * 4,
+            "build_us": round(a.elapsed_time(b) * 1000 / reps, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["boids", "ensemble"])
+    ap.add_argument("case", choices=["boids", "ensemble", "build"])
+    ap.add_argument("--dims", type=int, default=3)
+    ap.add_argument("--sorted", action="store_true")
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--count", type=int, default=32)
     a = ap.parse_args()
-    out = boids(a.n) if a.case == "boids" else ensemble(a.count)
+    if a.case == "boids":
+        out = boids(a.n)
+    elif a.case == "ensemble":
+        out = ensemble(a.count)
+    else:
+        out = build(a.dims, a.sorted)
     print(json.dumps(out))
 
 

@@ -111,6 +111,15 @@ class CUDASimulation {
 
     void setPopulationData(AgentVector& population, const std::string& state = "default");
     void getPopulationData(AgentVector& population, const std::string& state = "default");
+    /** setPopulationData from named host columns (GB300 extension): every
+     *  variable, _id included and set, given as n elements; the columns are
+     *  copied straight to the device (asynchronously, then waited for). */
+    void setPopulationColumns(const std::string& agent, const std::string& state, uint32_t n,
+                              const std::vector<std::pair<std::string, const void*>>& host_columns);
+    /** getPopulationData into named host columns of room for `cap` agents
+     *  (GB300 extension); returns the population. */
+    uint32_t getPopulationColumns(const std::string& agent, const std::string& state,
+                                  const std::vector<std::pair<std::string, void*>>& host_columns, uint32_t cap);
 
     /** One step (all layers). Returns false if an exit condition requests a stop. */
     bool step();

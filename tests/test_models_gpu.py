@@ -225,3 +225,26 @@ def test_operation_times_from_step_graphs():
             assert prof == {}
     for k in ("x", "fx"):
         np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+def test_population_direct_columns_match_agent_vector_path():
+    # every variable given (ids set): copied straight to the device; one left
+    # out: the AgentVector path with defaults. Same state, same new ids.
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    n = 20_000
+    pop = synth.birth_death_population(n, 4)
+    outs = []
+    for cols in (pop, {k: v for k, v in pop.items() if k != "counter"}):
+        s = S.Simulation("birth_death", [0.30, 0.20, 4])
+        s.set_population("agent", n, cols)
+        s.step(6)
+        names = ["_id", "counter"] + [f"f{v}" for v in range(8)]
+        bufs = {k: np.zeros(4 * n, dtype=np.uint32 if k == "_id" else (np.int32 if k == "counter" else np.float32))
+                for k in names}
+        m = s.get_population("agent", bufs)
+        outs.append({k: v[:m].copy() for k, v in bufs.items()})
+        s.close()
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
+    assert outs[0]["_id"].max() > n  # births took fresh ids past the given ones
