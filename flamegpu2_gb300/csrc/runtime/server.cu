@@ -2,7 +2,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <future>
+#include <thread>
 
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu/simulation/SimulationServer.h"
@@ -22,6 +25,8 @@ struct SimulationServer::Job {
     size_t bytes = 0;
     std::unique_ptr<CUDASimulation> sim;
     std::vector<cudaEvent_t> ring;  // event of step k in ring[k % size]
+    std::future<void> setup;        // admission work running on its own thread
+    bool births = false;            // the model has agent output (birth)
     ~Job() {
         for (cudaEvent_t e : ring) cudaEventDestroy(e);
     }
@@ -37,9 +42,12 @@ SimulationServer::SimulationServer() : SimulationServer(Config()) {}
 SimulationServer::SimulationServer(const Config& c) : cfg(c), t0(std::chrono::steady_clock::now()) {}
 
 SimulationServer::~SimulationServer() {
-    // let in-flight work finish before the simulations free their buffers
-    for (auto& j : running)
-        if (j->sim) cudaStreamSynchronize(j->sim->getStream());
+    // let admissions and in-flight work finish before the simulations free their buffers
+    for (auto& j : admitting)
+        if (j->setup.valid()) j->setup.wait();
+    for (auto* list : {&admitting, &running})
+        for (auto& j : *list)
+            if (j->sim) cudaStreamSynchronize(j->sim->getStream());
 }
 
 double SimulationServer::now() const {
@@ -47,7 +55,7 @@ double SimulationServer::now() const {
 }
 
 size_t SimulationServer::queued() const { return queue.size(); }
-size_t SimulationServer::active() const { return running.size(); }
+size_t SimulationServer::active() const { return running.size() + admitting.size(); }
 size_t SimulationServer::reservedBytes() const { return reserved; }
 
 size_t SimulationServer::estimateBytes(const ModelDescription& model,
@@ -92,6 +100,8 @@ uint64_t SimulationServer::submit(std::shared_ptr<ModelDescription> model,
     j->arrival = now();
     j->bytes = estimateBytes(*j->model, j->populations);
     for (const auto& p : j->populations) j->agents += p.second.size();
+    for (const auto& a : j->model->getData()->agents)
+        for (const auto& f : a->functions) j->births = j->births || !f->agent_output.empty();
     const uint64_t id = j->id;
     queue.push_back(std::move(j));
     return id;
@@ -125,7 +135,11 @@ void SimulationServer::retire(Job& j, bool failed, const std::string& error) {
     completed.push_back(std::move(r));
 }
 
+SimulationServer::Counters SimulationServer::counters() const { return stats_; }
+
 size_t SimulationServer::poll() {
+    const auto t_poll = std::chrono::steady_clock::now();
+    ++stats_.polls;
     // 1. retire runs whose last step has completed (non-blocking test)
     for (size_t k = 0; k < running.size();) {
         Job& j = *running[k];
@@ -137,39 +151,64 @@ size_t SimulationServer::poll() {
             ++k;
         }
     }
-    // 2. admit queued runs in arrival order while a slot and the budget allow
-    while (!queue.empty() && running.size() < cfg.max_active &&
-           (reserved + queue.front()->bytes <= cfg.memory_budget || running.empty())) {
+    // 2. runs whose set-up has finished join the active ones
+    for (size_t k = 0; k < admitting.size();) {
+        Job& j = *admitting[k];
+        if (j.setup.wait_for(std::chrono::seconds(0)) != std::future_status::ready) {
+            ++k;
+            continue;
+        }
+        try {
+            j.setup.get();
+            running.push_back(std::move(admitting[k]));
+        } catch (const exception::FLAMEGPUException& e) {
+            retire(j, true, std::string(e.exception_type()) + ": " + e.what());
+        } catch (const std::exception& e) {
+            retire(j, true, e.what());
+        }
+        admitting.erase(admitting.begin() + static_cast<long>(k));
+    }
+    // 3. admit queued runs in arrival order while a slot and the budget allow;
+    //    each builds its simulation and uploads its populations on a thread of
+    //    its own, so a large upload does not hold up the steps of the others
+    while (!queue.empty() && running.size() + admitting.size() < cfg.max_active &&
+           (reserved + queue.front()->bytes <= cfg.memory_budget || (running.empty() && admitting.empty()))) {
         std::unique_ptr<Job> j = std::move(queue.front());
         queue.pop_front();
         j->admitted = now();
         reserved += j->bytes;
-        try {
-            j->sim = std::make_unique<CUDASimulation>(*j->model);
-            j->sim->CUDAConfig().device_id = cfg.device;
-            j->sim->CUDAConfig().use_graphs = cfg.use_graphs;
-            j->sim->CUDAConfig().stream_priority = priority_for(static_cast<double>(j->steps) * static_cast<double>(j->agents));
-            j->sim->SimulationConfig().random_seed = j->seed;
-            j->sim->SimulationConfig().steps = j->steps;
+        Job* jp = j.get();
+        const Config c = cfg;
+        const int prio = priority_for(static_cast<double>(j->steps) * static_cast<double>(j->agents));
+        jp->setup = std::async(std::launch::async, [jp, c, prio] {
+            jp->sim = std::make_unique<CUDASimulation>(*jp->model);
+            jp->sim->CUDAConfig().device_id = c.device;
+            jp->sim->CUDAConfig().use_graphs = c.use_graphs;
+            jp->sim->CUDAConfig().stream_priority = prio;
+            jp->sim->SimulationConfig().random_seed = jp->seed;
+            jp->sim->SimulationConfig().steps = jp->steps;
             // births may grow a population to four times its start (as budgeted), no further
             size_t largest = 1024;
-            for (const auto& p : j->populations) largest = std::max<size_t>(largest, p.second.size());
-            j->sim->CUDAConfig().max_agents = static_cast<unsigned int>(std::min<size_t>(4 * largest, (1u << 31) - 1));
-            for (auto& p : j->populations) j->sim->setPopulationData(p.second);
-            j->populations.clear();
-            const double by_work = cfg.work_in_flight / static_cast<double>(std::max<size_t>(j->agents, 1));
-            const unsigned int depth = static_cast<unsigned int>(
-                std::min(64.0, std::max(static_cast<double>(std::max(1u, cfg.steps_in_flight)), by_work)));
-            j->ring.assign(depth, nullptr);
-            for (cudaEvent_t& e : j->ring)
+            for (const auto& p : jp->populations) largest = std::max<size_t>(largest, p.second.size());
+            jp->sim->CUDAConfig().max_agents = static_cast<unsigned int>(std::min<size_t>(4 * largest, (1u << 31) - 1));
+            for (auto& p : jp->populations) jp->sim->setPopulationData(p.second);
+            jp->populations.clear();
+            // runs with births need a population count from the device to size
+            // the next step's output, so they keep few steps queued
+            const double by_work = c.work_in_flight / static_cast<double>(std::max<size_t>(jp->agents, 1));
+            const double depth = jp->births ? 1.0 : by_work;
+            const unsigned int ring = static_cast<unsigned int>(
+                std::min(64.0, std::max(static_cast<double>(std::max(1u, c.steps_in_flight)), depth)));
+            jp->ring.assign(ring, nullptr);
+            for (cudaEvent_t& e : jp->ring)
                 if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
                     throw exception::CUDAError("cudaEventCreate failed");
-            running.push_back(std::move(j));
-        } catch (const exception::FLAMEGPUException& e) {
-            retire(*j, true, std::string(e.exception_type()) + ": " + e.what());
-        }
+            if (cudaStreamSynchronize(jp->sim->getStream()) != cudaSuccess)
+                throw exception::CUDAError("population upload failed");
+        });
+        admitting.push_back(std::move(j));
     }
-    // 3. issue the next steps, least remaining work first, keeping at most
+    // 4. issue the next steps, least remaining work first, keeping at most
     //    steps_in_flight steps of a run queued on the device
     std::vector<Job*> order;
     order.reserve(running.size());
@@ -177,16 +216,24 @@ size_t SimulationServer::poll() {
     std::stable_sort(order.begin(), order.end(),
                      [](const Job* a, const Job* b) { return a->remaining_work() < b->remaining_work(); });
     std::vector<Job*> failed;
+    double inflight = 0.0;
+    for (Job* jp : order) {
+        jp->reap();
+        inflight += static_cast<double>(jp->issued - jp->completed) * static_cast<double>(jp->agents);
+    }
     for (Job* jp : order) {
         Job& j = *jp;
         try {
-            j.reap();
+            const double per_step = static_cast<double>(std::max<size_t>(j.agents, 1));
             const unsigned int per_poll = std::max<unsigned int>(cfg.steps_per_poll, static_cast<unsigned int>(j.ring.size()));
             for (unsigned int s = 0; s < per_poll && j.issued < j.steps && j.issued - j.completed < j.ring.size(); ++s) {
+                if (j.issued > j.completed && inflight + per_step > cfg.total_work_in_flight) break;
                 j.sim->step();
                 if (cudaEventRecord(j.ring[j.issued % j.ring.size()], j.sim->getStream()) != cudaSuccess)
                     throw exception::CUDAError("cudaEventRecord failed");
                 ++j.issued;
+                ++stats_.steps_issued;
+                inflight += per_step;
             }
         } catch (const exception::FLAMEGPUException& e) {
             // failure isolation: this run completes with its error, the others go on
@@ -200,7 +247,8 @@ size_t SimulationServer::poll() {
                                          return std::find(failed.begin(), failed.end(), j.get()) != failed.end();
                                      }),
                       running.end());
-    return queue.size() + running.size();
+    stats_.poll_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_poll).count();
+    return queue.size() + admitting.size() + running.size();
 }
 
 int SimulationServer::priority_for(double work) const {
@@ -215,6 +263,7 @@ int SimulationServer::priority_for(double work) const {
 
 void SimulationServer::runUntilIdle() {
     while (poll()) {
+        if (running.empty()) std::this_thread::yield();  // only admissions in progress
     }
 }
 

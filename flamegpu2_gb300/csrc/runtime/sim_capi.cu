@@ -544,3 +544,12 @@ extern "C" int fgv_stats(fgv_server* v, uint32_t* q, uint32_t* a, uint64_t* r) {
         if (r) *r = v->server->reservedBytes();
     });
 }
+
+extern "C" int fgv_counters(fgv_server* v, uint64_t* polls, double* poll_s, uint64_t* steps) {
+    return guarded([&] {
+        const auto c = v->server->counters();
+        if (polls) *polls = c.polls;
+        if (poll_s) *poll_s = c.poll_seconds;
+        if (steps) *steps = c.steps_issued;
+    });
+}

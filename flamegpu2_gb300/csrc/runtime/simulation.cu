@@ -634,6 +634,14 @@ struct SimulationImpl {
                     if (f.fn == fd && f.births && f.list == l) ++b;
         return b;
     }
+    // Rows to allocate for a population of n: with a population limit, a list
+    // that births can grow starts at the limit (the memory a served run was
+    // budgeted for), so capacity checks rarely need a count from the device.
+    uint32_t initial_capacity(const AgentList* l, uint32_t n) const {
+        uint32_t cap = std::max<uint32_t>(1024u, n);
+        if (cuda_config.max_agents && births_per_step(l) > 0) cap = std::max(cap, cuda_config.max_agents);
+        return cap;
+    }
     bool any_births() const {
         for (const auto& f : fns)
             if (f.births) return true;
@@ -880,7 +888,10 @@ struct SimulationImpl {
         P.env = d_env;
         cudaError_t e = cudaSuccess;
         const unsigned int smem = P.stage_bytes ? P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader)) : 0u;
-        timed("fn:" + f.fn->name, [&] { e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 16), kAgentBlock, smem, stream); });
+        // one block per 128 rows (no grid-stride reuse): blocks stay short, so
+        // kernels of other simulations on the device (a server's other runs,
+        // higher-priority streams) get SMs between them
+        timed("fn:" + f.fn->name, [&] { e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 1 << 16), kAgentBlock, smem, stream); });
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(e)));
         kernel_counter += 1;
@@ -1183,7 +1194,7 @@ void CUDASimulation::setPopulationData(AgentVector& pop, const std::string& stat
             if (ids[i] == ID_NOT_SET) ids[i] = next++;
         FG_CUDA(cudaMemcpy(impl->d_next_id(ai), &next, sizeof(uint32_t), cudaMemcpyHostToDevice));
     }
-    const uint32_t cap = std::max<uint32_t>(1024u, n);
+    const uint32_t cap = impl->initial_capacity(l, n);
     if (cap > l->capacity) impl->ensure_capacity(*l, cap, 0);
     for (size_t v = 0; v < l->cols.size(); ++v) {
         const size_t b = l->agent->variables[v].bytes();
@@ -1235,7 +1246,7 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
         }
     }
     FG_CUDA(cudaStreamSynchronize(impl->stream));
-    const uint32_t cap = std::max<uint32_t>(1024u, n);
+    const uint32_t cap = impl->initial_capacity(l, n);
     if (cap > l->capacity) impl->ensure_capacity(*l, cap, 0);
     for (size_t v = 0; v < l->cols.size(); ++v) {
         const size_t b = l->agent->variables[v].bytes();

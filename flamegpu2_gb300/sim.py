@@ -316,7 +316,8 @@ class Ensemble:
 
 
 SERVER_EXPORTS = ["fgv_create", "fgv_destroy", "fgv_submit", "fgv_poll", "fgv_run_until_idle", "fgv_take_completed",
-                  "fgv_result_info", "fgv_result_count", "fgv_result_variable", "fgv_release", "fgv_stats"]
+                  "fgv_result_info", "fgv_result_count", "fgv_result_variable", "fgv_release", "fgv_stats",
+                  "fgv_counters"]
 _srv_ready = False
 
 
@@ -338,6 +339,7 @@ def _srv():
         L.fgv_result_variable.argtypes = [vp, u64, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
         L.fgv_release.argtypes = [vp, u64]
         L.fgv_stats.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u64)]
+        L.fgv_counters.argtypes = [vp, C.POINTER(u64), C.POINTER(C.c_double), C.POINTER(u64)]
         _srv_ready = True
     return L
 
@@ -427,6 +429,11 @@ class Server:
 
     def release(self, rid: int):
         _check(_srv().fgv_release(self._h, rid))
+
+    def counters(self) -> dict:
+        p, t, n = C.c_uint64(), C.c_double(), C.c_uint64()
+        _check(_srv().fgv_counters(self._h, C.byref(p), C.byref(t), C.byref(n)))
+        return {"polls": p.value, "poll_seconds": t.value, "steps_issued": n.value}
 
     def stats(self) -> dict:
         q, a, r = C.c_uint32(), C.c_uint32(), C.c_uint64()

@@ -441,6 +441,7 @@ def run_served(args, world, rank, local):
             if remaining == 0:
                 time.sleep(max(0.0, min(0.001, arrivals[nxt] - now)))
         makespan = time.perf_counter() - t_start
+        counters = srv.counters()
         lat, detail = [], []
         for rid in srv.take_completed():
             info = srv.info(rid)
@@ -460,7 +461,7 @@ def run_served(args, world, rank, local):
             seq_lat.append(done - arrivals[i])
         per_rate.append({"rate_req_s": rate, "throughput": round(sum(work) / makespan, 1),
                          "p50_s": round(_percentile(lat, 50), 4), "p99_s": round(_percentile(lat, 99), 4),
-                         "makespan_s": round(makespan, 3),
+                         "makespan_s": round(makespan, 3), "scheduler": counters,
                          "requests": sorted(detail) if rate == max(rates) else None,
                          "sequential": {"throughput": round(sum(work) / done, 1),
                                         "p50_s": round(_percentile(seq_lat, 50), 4),

@@ -39,6 +39,11 @@ class SimulationServer {
         // ... and up to work_in_flight / (the run's initial agents) steps, at most 64:
         // small runs keep enough steps queued to advance between two polls
         double work_in_flight = 4.0e6;
+        // agent-steps queued on the device over all runs: steps are issued in
+        // order of least remaining work until this is reached, so the smallest
+        // runs go first and the largest fill what is left (shortest remaining
+        // work first, approximately); a run with nothing queued always gets a step
+        double total_work_in_flight = 2.0e7;
         int device = 0;
         bool use_graphs = true;
     };
@@ -72,6 +77,13 @@ class SimulationServer {
     size_t queued() const;
     size_t active() const;
     size_t reservedBytes() const;
+    /** Scheduling counters: polls, host seconds spent inside poll(), steps issued. */
+    struct Counters {
+        uint64_t polls = 0;
+        double poll_seconds = 0.0;
+        uint64_t steps_issued = 0;
+    };
+    Counters counters() const;
     double now() const;
     /** Device bytes a run is budgeted at: agent columns (twice, with head room
      *  for births), message columns and records, spatial indexes, scratch. */
@@ -86,9 +98,11 @@ class SimulationServer {
     std::chrono::steady_clock::time_point t0;
     uint64_t next_id = 1;
     std::deque<std::unique_ptr<Job>> queue;
+    std::vector<std::unique_ptr<Job>> admitting;  // set-up in progress on their own threads
     std::vector<std::unique_ptr<Job>> running;
     std::vector<Result> completed;
     size_t reserved = 0;
+    Counters stats_;
 };
 
 }  // namespace flamegpu

@@ -136,6 +136,8 @@ int fgv_result_variable(fgv_server* v, uint64_t id, const char* agent, const cha
 /* Drops a completed run's results. */
 int fgv_release(fgv_server* v, uint64_t id);
 int fgv_stats(fgv_server* v, uint32_t* queued, uint32_t* active, uint64_t* reserved_bytes);
+/* Scheduling counters: polls, host seconds inside poll, steps issued. */
+int fgv_counters(fgv_server* v, uint64_t* polls, double* poll_seconds, uint64_t* steps_issued);
 
 #ifdef __cplusplus
 }
