@@ -13,8 +13,8 @@
 //                span of their indices (narrow spans) or a bitonic sort in
 //                shared memory, longer ones by ranking each 256-element chunk
 //                against the whole bin
-// The automatic agent sort runs the same pipeline on the reference's sort key
-// and finally gathers every agent column by the stable permutation.
+// The automatic agent sort runs the same pipeline on the reference's sort key;
+// its k_stabilize / k_long write every agent column at the stable position.
 #include <algorithm>
 #include <mutex>
 
@@ -33,7 +33,7 @@ constexpr uint32_t kChunk = 256;     // elements of a long bin ranked by one blo
 constexpr uint32_t kRankTile = 2048; // bin elements staged in shared memory per pass
 
 enum KeyMode { kMessageBin = 0, kSortKey = 1 };
-enum EmitMode { kEmitRecord = 0, kEmitPerm = 1 };
+enum EmitMode { kEmitRecord = 0, kEmitPerm = 1, kEmitPermColumns = 2 };
 
 struct SortGrid {
     float min[3];
@@ -211,12 +211,51 @@ __device__ __forceinline__ void emit_record(const RecordParams& rp, uint32_t i, 
     }
 }
 
+struct ColumnParams {
+    fg_column col[FG_MAX_COLUMNS];
+    uint32_t ncols;
+};
+
+template <typename T>
+__device__ __forceinline__ void copy_elem(const void* in, void* out, uint32_t src, uint32_t dst) {
+    reinterpret_cast<T*>(out)[dst] = reinterpret_cast<const T*>(in)[src];
+}
+
+__device__ __forceinline__ void copy_column_elem(const fg_column& c, uint32_t src, uint32_t dst) {
+    switch (c.elem_bytes) {
+        case 4: copy_elem<uint32_t>(c.in, c.out, src, dst); break;
+        case 8: copy_elem<uint2>(c.in, c.out, src, dst); break;
+        case 16: copy_elem<uint4>(c.in, c.out, src, dst); break;
+        case 1: copy_elem<uint8_t>(c.in, c.out, src, dst); break;
+        case 2: copy_elem<uint16_t>(c.in, c.out, src, dst); break;
+        default: {
+            const uint8_t* a = reinterpret_cast<const uint8_t*>(c.in) + static_cast<size_t>(src) * c.elem_bytes;
+            uint8_t* b = reinterpret_cast<uint8_t*>(c.out) + static_cast<size_t>(dst) * c.elem_bytes;
+            if ((c.elem_bytes & 3) == 0) {
+                for (uint32_t k = 0; k < c.elem_bytes; k += 4)
+                    *reinterpret_cast<uint32_t*>(b + k) = *reinterpret_cast<const uint32_t*>(a + k);
+            } else {
+                for (uint32_t k = 0; k < c.elem_bytes; ++k) b[k] = a[k];
+            }
+        }
+    }
+}
+
+// What the last build kernels write for message (or agent) i at sorted
+// position dst: its record, its index, or its index and every agent column.
+struct EmitParams {
+    RecordParams rp;
+    ColumnParams cp;
+};
+
 template <int EMIT>
-__device__ __forceinline__ void emit(const RecordParams& rp, uint32_t* sperm, uint32_t i, uint32_t dst) {
+__device__ __forceinline__ void emit(const EmitParams& ep, uint32_t* sperm, uint32_t i, uint32_t dst) {
     if (EMIT == kEmitRecord) {
-        emit_record(rp, i, dst);
+        emit_record(ep.rp, i, dst);
     } else {
         sperm[dst] = i;
+        if (EMIT == kEmitPermColumns)
+            for (uint32_t c = 0; c < ep.cp.ncols; ++c) copy_column_elem(ep.cp.col[c], i, dst);
     }
 }
 
@@ -224,7 +263,7 @@ __device__ __forceinline__ void emit(const RecordParams& rp, uint32_t* sperm, ui
 // (count of smaller original indices in the bin); long bins are queued as
 // chunks (bucket, chunk index) for k_long.
 template <int EMIT>
-__global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ RecordParams rp, uint32_t nbuckets,
+__global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ EmitParams rp, uint32_t nbuckets,
                                                         const uint32_t* __restrict__ keys,
                                                         const uint32_t* __restrict__ pbm,
                                                         const uint32_t* __restrict__ perm, uint32_t* sperm,
@@ -234,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
         const uint32_t i = perm[p];
         const uint32_t b = keys[i];
         if (b & kPadBit) {  // padding row of a batch: keeps its slot, carries no message
-            if (EMIT == kEmitPerm) sperm[p] = i;
+            if (EMIT != kEmitRecord) sperm[p] = i;
             continue;
         }
         const uint32_t s = pbm[b], e = pbm[b + 1];
@@ -270,7 +309,7 @@ constexpr uint32_t kSpanWords = kSortCap / 2;   // bitmap words; the other half 
 constexpr uint32_t kSpanCap = kSpanWords * 32;  // 131,072 indices
 
 template <int EMIT>
-__global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ RecordParams rp,
+__global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitParams rp,
                                                    const uint32_t* __restrict__ pbm,
                                                    const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                    const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
@@ -378,46 +417,6 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ Recor
             }
         }
         if (act) emit<EMIT>(rp, sperm, i, s + rank);
-    }
-}
-
-struct ColumnParams {
-    fg_column col[FG_MAX_COLUMNS];
-    uint32_t ncols;
-};
-
-template <typename T>
-__device__ __forceinline__ void copy_elem(const void* in, void* out, uint32_t src, uint32_t dst) {
-    reinterpret_cast<T*>(out)[dst] = reinterpret_cast<const T*>(in)[src];
-}
-
-__device__ __forceinline__ void copy_column_elem(const fg_column& c, uint32_t src, uint32_t dst) {
-    switch (c.elem_bytes) {
-        case 4: copy_elem<uint32_t>(c.in, c.out, src, dst); break;
-        case 8: copy_elem<uint2>(c.in, c.out, src, dst); break;
-        case 16: copy_elem<uint4>(c.in, c.out, src, dst); break;
-        case 1: copy_elem<uint8_t>(c.in, c.out, src, dst); break;
-        case 2: copy_elem<uint16_t>(c.in, c.out, src, dst); break;
-        default: {
-            const uint8_t* a = reinterpret_cast<const uint8_t*>(c.in) + static_cast<size_t>(src) * c.elem_bytes;
-            uint8_t* b = reinterpret_cast<uint8_t*>(c.out) + static_cast<size_t>(dst) * c.elem_bytes;
-            if ((c.elem_bytes & 3) == 0) {
-                for (uint32_t k = 0; k < c.elem_bytes; k += 4)
-                    *reinterpret_cast<uint32_t*>(b + k) = *reinterpret_cast<const uint32_t*>(a + k);
-            } else {
-                for (uint32_t k = 0; k < c.elem_bytes; ++k) b[k] = a[k];
-            }
-        }
-    }
-}
-
-// out_c[p] = in_c[sperm[p]] for every column.
-__global__ void __launch_bounds__(kThreads) k_gather_columns(const __grid_constant__ ColumnParams cp, uint32_t max_n,
-                                                             const uint32_t* d_n, const uint32_t* __restrict__ sperm) {
-    const uint32_t n = load_count(d_n, max_n);
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const uint32_t i = sperm[p];
-        for (uint32_t c = 0; c < cp.ncols; ++c) copy_column_elem(cp.col[c], i, p);
     }
 }
 
@@ -566,7 +565,7 @@ struct BatchKeys {
 
 template <int MODE, int EMIT>
 int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets, uint32_t max_n, const uint32_t* d_n,
-                 const float* x, const float* y, const float* z, const uint32_t* valid, const RecordParams& rp,
+                 const float* x, const float* y, const float* z, const uint32_t* valid, const EmitParams& rp,
                  uint32_t* pbm_out, const BuildLayout& L, char* ws, cudaStream_t st, const BatchKeys& batch = BatchKeys()) {
     WsHeader* h = reinterpret_cast<WsHeader*>(ws);
     uint32_t* hist = reinterpret_cast<uint32_t*>(ws + L.hist);
@@ -574,7 +573,7 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     uint32_t* keys = reinterpret_cast<uint32_t*>(ws + L.keys);
     uint32_t* slot = reinterpret_cast<uint32_t*>(ws + L.slot);
     uint32_t* perm = reinterpret_cast<uint32_t*>(ws + L.perm);
-    uint32_t* sperm = EMIT == kEmitPerm ? reinterpret_cast<uint32_t*>(ws + L.sperm) : nullptr;
+    uint32_t* sperm = EMIT != kEmitRecord ? reinterpret_cast<uint32_t*>(ws + L.sperm) : nullptr;
     uint2* chunks = reinterpret_cast<uint2*>(ws + L.chunks);
     const uint32_t grid = grid_for(max_n);
     if (batch.inst)
@@ -603,9 +602,9 @@ extern "C" int fg_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const 
     if (reinterpret_cast<uintptr_t>(sorted) & 15) return FG_ERR_INVALID_ARGUMENT;
     const BuildLayout L = build_layout(max_n, g->binCount, false);
     if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
-    RecordParams rp;
-    rp.rec = *rec;
-    rp.out = sorted;
+    EmitParams rp{};
+    rp.rp.rec = *rec;
+    rp.rp.out = sorted;
     SortGrid sg{};
     return run_pipeline<kMessageBin, kEmitRecord>(g, sg, g->binCount, max_n, d_n, x, y, z, valid, rp, pbm, L,
                                                   static_cast<char*>(workspace), static_cast<cudaStream_t>(stream));
@@ -624,17 +623,16 @@ extern "C" int fg_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, 
     if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
     char* ws = static_cast<char*>(workspace);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    RecordParams rp{};
-    int rc = run_pipeline<kSortKey, kEmitPerm>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
-                                               reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st);
+    // the stable positions' kernels write every column directly (no gather pass)
+    EmitParams rp{};
+    for (uint32_t c = 0; c < ncols; ++c) rp.cp.col[c] = cols[c];
+    rp.cp.ncols = ncols;
+    int rc = ncols ? run_pipeline<kSortKey, kEmitPermColumns>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
+                                                              reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st)
+                   : run_pipeline<kSortKey, kEmitPerm>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
+                                                       reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st);
     if (rc != FG_OK) return rc;
     const uint32_t* sperm = reinterpret_cast<const uint32_t*>(ws + L.sperm);
-    if (ncols) {
-        ColumnParams cp{};
-        for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cols[c];
-        cp.ncols = ncols;
-        k_gather_columns<<<grid_for(max_n), kThreads, 0, st>>>(cp, max_n, d_n, sperm);
-    }
     if (perm_out && max_n) {
         cudaMemcpyAsync(perm_out, sperm, sizeof(uint32_t) * max_n, cudaMemcpyDeviceToDevice, st);
     }
@@ -784,9 +782,9 @@ extern "C" int fg_spatial_build_batched(const fg_batch_instance* instances, cons
     if ((reinterpret_cast<uintptr_t>(sorted) & 15) || total_buckets >= kPadBit) return FG_ERR_INVALID_ARGUMENT;
     const BuildLayout L = build_layout(total_rows, total_buckets, true);
     if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
-    RecordParams rp;
-    rp.rec = *rec;
-    rp.out = sorted;
+    EmitParams rp{};
+    rp.rp.rec = *rec;
+    rp.rp.out = sorted;
     SortGrid sg{};
     BatchKeys bk;
     bk.inst = instances;
@@ -812,7 +810,9 @@ extern "C" int fg_spatial_sort_agents_batched(const fg_batch_instance* instances
     if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
     char* ws = static_cast<char*>(workspace);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    RecordParams rp{};
+    EmitParams rp{};
+    for (uint32_t c = 0; c < ncols; ++c) rp.cp.col[c] = cols[c];
+    rp.cp.ncols = ncols;
     SortGrid sg{};
     BatchKeys bk;
     bk.inst = instances;
@@ -820,15 +820,13 @@ extern "C" int fg_spatial_sort_agents_batched(const fg_batch_instance* instances
     bk.ninst = ninst;
     bk.dims = dims;
     fg_spatial_grid dummy{};
-    int rc = run_pipeline<kSortKey, kEmitPerm>(&dummy, sg, total_buckets, total_rows, nullptr, x, y, z, nullptr, rp,
-                                               reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st, bk);
+    // padding rows (past an instance's count) keep their slot and carry no agent:
+    // their columns are left as they are
+    int rc = ncols ? run_pipeline<kSortKey, kEmitPermColumns>(&dummy, sg, total_buckets, total_rows, nullptr, x, y, z,
+                                                              nullptr, rp, reinterpret_cast<uint32_t*>(ws + L.pbm), L,
+                                                              ws, st, bk)
+                   : run_pipeline<kSortKey, kEmitPerm>(&dummy, sg, total_buckets, total_rows, nullptr, x, y, z, nullptr,
+                                                       rp, reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st, bk);
     if (rc != FG_OK) return rc;
-    if (ncols) {
-        ColumnParams cp{};
-        for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cols[c];
-        cp.ncols = ncols;
-        k_gather_columns<<<grid_for(total_rows), kThreads, 0, st>>>(cp, total_rows, nullptr,
-                                                                    reinterpret_cast<const uint32_t*>(ws + L.sperm));
-    }
     return check_launch();
 }

@@ -417,7 +417,7 @@ struct BatchedSim {
                                                 c.data(), static_cast<uint32_t>(c.size()), b.sort_ws, b.sort_ws_bytes,
                                                 stream));
         parity ^= 1;
-        kernels_per_step += 6;
+        kernels_per_step += 5;
     }
 
     void enqueue_build(BMsg& m, cudaStream_t st) {

@@ -802,7 +802,7 @@ struct SimulationImpl {
                                        cols.data(), static_cast<uint32_t>(cols.size()), nullptr, it->second.first,
                                        it->second.second, stream));
         l.parity ^= 1;
-        kernel_counter += 6;
+        kernel_counter += 5;
     }
 
     void enqueue_build(MsgList& m, cudaStream_t st) {

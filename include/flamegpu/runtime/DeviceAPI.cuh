@@ -126,9 +126,12 @@ __device__ __forceinline__ uint32_t grid_hash(const fg_spatial_grid& g, int x, i
     return static_cast<uint32_t>(z) * g.gridDim[0] * g.gridDim[1] + static_cast<uint32_t>(y) * g.gridDim[0] + ux;
 }
 __device__ __forceinline__ float virtual_coord(float p1, float p2, float width) {
-    // getVirtualX (MessageSpatial3DDevice.cuh:373-397)
+    // getVirtualX (MessageSpatial3DDevice.cuh:373-397): p2 - (d / |d|) * width
+    // when |d| > width / 2. For the finite non-zero d of that branch, d / |d| is
+    // exactly +-1 and width / 2 exactly width * 0.5, so the same value comes
+    // from a sign copy, without the division.
     const float d = p2 - p1;
-    return fabsf(d) > width / 2.0f ? p2 - (d / fabsf(d) * width) : p2;
+    return fabsf(d) > width * 0.5f ? p2 - copysignf(width, d) : p2;
 }
 
 // ---- shared-memory staging window of a block's spatial neighbourhood ----
