@@ -137,6 +137,11 @@ void SimulationServer::retire(Job& j, bool failed, const std::string& error) {
 
 SimulationServer::Counters SimulationServer::counters() const { return stats_; }
 
+void SimulationServer::setScheduling(double work_in_flight, double total_work_in_flight) {
+    if (work_in_flight > 0.0) cfg.work_in_flight = work_in_flight;
+    if (total_work_in_flight > 0.0) cfg.total_work_in_flight = total_work_in_flight;
+}
+
 size_t SimulationServer::poll() {
     const auto t_poll = std::chrono::steady_clock::now();
     ++stats_.polls;
@@ -227,7 +232,7 @@ size_t SimulationServer::poll() {
             const double per_step = static_cast<double>(std::max<size_t>(j.agents, 1));
             const unsigned int per_poll = std::max<unsigned int>(cfg.steps_per_poll, static_cast<unsigned int>(j.ring.size()));
             for (unsigned int s = 0; s < per_poll && j.issued < j.steps && j.issued - j.completed < j.ring.size(); ++s) {
-                if (j.issued > j.completed && inflight + per_step > cfg.total_work_in_flight) break;
+                if (inflight > 0.0 && inflight + per_step > cfg.total_work_in_flight) break;
                 j.sim->step();
                 if (cudaEventRecord(j.ring[j.issued % j.ring.size()], j.sim->getStream()) != cudaSuccess)
                     throw exception::CUDAError("cudaEventRecord failed");

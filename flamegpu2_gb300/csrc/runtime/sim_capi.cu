@@ -553,3 +553,7 @@ extern "C" int fgv_counters(fgv_server* v, uint64_t* polls, double* poll_s, uint
         if (steps) *steps = c.steps_issued;
     });
 }
+
+extern "C" int fgv_set_scheduling(fgv_server* v, double work, double total) {
+    return guarded([&] { v->server->setScheduling(work, total); });
+}

@@ -317,7 +317,7 @@ class Ensemble:
 
 SERVER_EXPORTS = ["fgv_create", "fgv_destroy", "fgv_submit", "fgv_poll", "fgv_run_until_idle", "fgv_take_completed",
                   "fgv_result_info", "fgv_result_count", "fgv_result_variable", "fgv_release", "fgv_stats",
-                  "fgv_counters"]
+                  "fgv_counters", "fgv_set_scheduling"]
 _srv_ready = False
 
 
@@ -340,6 +340,7 @@ def _srv():
         L.fgv_release.argtypes = [vp, u64]
         L.fgv_stats.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u64)]
         L.fgv_counters.argtypes = [vp, C.POINTER(u64), C.POINTER(C.c_double), C.POINTER(u64)]
+        L.fgv_set_scheduling.argtypes = [vp, C.c_double, C.c_double]
         _srv_ready = True
     return L
 
@@ -429,6 +430,9 @@ class Server:
 
     def release(self, rid: int):
         _check(_srv().fgv_release(self._h, rid))
+
+    def set_scheduling(self, work_in_flight: float = 0.0, total_work_in_flight: float = 0.0):
+        _check(_srv().fgv_set_scheduling(self._h, float(work_in_flight), float(total_work_in_flight)))
 
     def counters(self) -> dict:
         p, t, n = C.c_uint64(), C.c_double(), C.c_uint64()

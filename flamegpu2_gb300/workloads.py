@@ -382,6 +382,31 @@ def _percentile(v, q):
     return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if v else None
 
 
+def _srpt_latencies(arrivals, service):
+    """Completion minus arrival of each job under preemptive shortest remaining
+    service first on one server (event simulation)."""
+    n = len(arrivals)
+    rem = list(service)
+    done = [None] * n
+    t, nxt, active = 0.0, 0, []
+    order = sorted(range(n), key=lambda i: arrivals[i])
+    while nxt < n or active:
+        if not active:
+            t = max(t, arrivals[order[nxt]])
+        while nxt < n and arrivals[order[nxt]] <= t:
+            active.append(order[nxt])
+            nxt += 1
+        j = min(active, key=lambda i: rem[i])
+        horizon = arrivals[order[nxt]] if nxt < n else float("inf")
+        run = min(rem[j], horizon - t)
+        t += run
+        rem[j] -= run
+        if rem[j] <= 1e-12:
+            done[j] = t
+            active.remove(j)
+    return [done[i] - arrivals[i] for i in range(n)]
+
+
 def run_served(args, world, rank, local):
     """Poisson request streams served by SimulationServer (continuous
     batching under a 150 GB budget) against the same requests run one after
@@ -423,6 +448,8 @@ def run_served(args, world, rank, local):
         arrivals = np.cumsum(-np.log(1.0 - u) / rate)  # Poisson process: exponential gaps
         t_srv = time.perf_counter()  # the server's clock starts inside its constructor
         srv = sim.Server(device=local, memory_budget=150 << 30, max_active=64)
+        if os.environ.get("FG_SERVED_INFLIGHT"):
+            srv.set_scheduling(0.0, float(os.environ["FG_SERVED_INFLIGHT"]))
         ids, order = {}, {}
         t_start = time.perf_counter()
         nxt = 0
@@ -459,7 +486,12 @@ def run_served(args, world, rank, local):
             start = max(arrivals[i], done)
             done = start + service[i]
             seq_lat.append(done - arrivals[i])
+        # shortest-remaining-service-first on one server, preemptive, from the
+        # measured single-run service times: a reference point for the order
+        srpt_lat = _srpt_latencies(arrivals, service)
         per_rate.append({"rate_req_s": rate, "throughput": round(sum(work) / makespan, 1),
+                         "srpt_ideal": {"p50_s": round(_percentile(srpt_lat, 50), 4),
+                                        "p99_s": round(_percentile(srpt_lat, 99), 4)},
                          "p50_s": round(_percentile(lat, 50), 4), "p99_s": round(_percentile(lat, 99), 4),
                          "makespan_s": round(makespan, 3), "scheduler": counters,
                          "requests": sorted(detail) if rate == max(rates) else None,

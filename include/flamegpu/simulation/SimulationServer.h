@@ -41,9 +41,10 @@ class SimulationServer {
         double work_in_flight = 4.0e6;
         // agent-steps queued on the device over all runs: steps are issued in
         // order of least remaining work until this is reached, so the smallest
-        // runs go first and the largest fill what is left (shortest remaining
-        // work first, approximately); a run with nothing queued always gets a step
-        double total_work_in_flight = 2.0e7;
+        // runs go first and the largest wait for what is left (shortest
+        // remaining work first, approximately); a step larger than the budget
+        // is issued only when nothing else is queued
+        double total_work_in_flight = 6.0e6;
         int device = 0;
         bool use_graphs = true;
     };
@@ -84,6 +85,8 @@ class SimulationServer {
         uint64_t steps_issued = 0;
     };
     Counters counters() const;
+    /** Changes the in-flight limits of Config (values <= 0 keep the current one). */
+    void setScheduling(double work_in_flight, double total_work_in_flight);
     double now() const;
     /** Device bytes a run is budgeted at: agent columns (twice, with head room
      *  for births), message columns and records, spatial indexes, scratch. */

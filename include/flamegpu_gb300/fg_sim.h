@@ -136,6 +136,9 @@ int fgv_result_variable(fgv_server* v, uint64_t id, const char* agent, const cha
 /* Drops a completed run's results. */
 int fgv_release(fgv_server* v, uint64_t id);
 int fgv_stats(fgv_server* v, uint32_t* queued, uint32_t* active, uint64_t* reserved_bytes);
+/* In-flight limits (SimulationServer::Config::work_in_flight, total_work_in_flight;
+ * values <= 0 keep the current one). */
+int fgv_set_scheduling(fgv_server* v, double work_in_flight, double total_work_in_flight);
 /* Scheduling counters: polls, host seconds inside poll, steps issued. */
 int fgv_counters(fgv_server* v, uint64_t* polls, double* poll_seconds, uint64_t* steps_issued);
 
