@@ -33,6 +33,7 @@ EXPORTS = [
     "fg_spatial_sort_agents", "fg_compact_agents", "fg_scan_workspace_size", "fg_exclusive_scan_u32",
     "fg_last_cuda_error", "fg_version", "fg_batch_instance_init", "fg_batched_workspace_size",
     "fg_spatial_build_batched", "fg_spatial_sort_agents_batched", "fg_exclusive_scan_u32_noalloc",
+    "fg_partition_agents", "fg_append_rows",
 ]
 FG_NOALLOC_SCAN_MAX_N = 1 << 25
 
@@ -105,6 +106,8 @@ def lib():
                                             vp, vp, vp, u32, vp, sz, vp]
             L.fg_exclusive_scan_u32.argtypes = [vp, vp, u32, vp, sz, vp]
             L.fg_exclusive_scan_u32_noalloc.argtypes = [vp, vp, u32, vp]
+            L.fg_partition_agents.argtypes = [u32, vp, vp, C.POINTER(Column), u32, vp, vp, sz, vp]
+            L.fg_append_rows.argtypes = [C.POINTER(Column), u32, u32, vp, vp, vp, u32, vp, sz, vp]
             L.fg_version.restype = C.c_char_p
             L.fg_batch_instance_init.argtypes = [C.POINTER(BatchInstance), C.POINTER(SpatialGrid), u32, u32, u32,
                                                  C.c_int32, C.POINTER(u32)]

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
                                                       const uint32_t* __restrict__ born, uint32_t* d_next_id,
                                                       const uint32_t* d_alive_total, uint32_t* d_n_out,
                                                       uint32_t out_capacity, uint64_t* status0, uint32_t stride_tiles,
-                                                      WsHeader* h) {
+                                                      WsHeader* h, int partition, uint32_t* d_s_out) {
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_cnt_a[kCompItems][kThreads / 32];
     __shared__ uint32_t s_cnt_b[kCompItems][kThreads / 32];
@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
             const uint32_t i = base + k * kThreads + tid;
             const bool in = i < n;
             const bool a = in && (alive == nullptr || alive[i] != 0);
-            const bool b = in && born != nullptr && born[i] != 0;
+            // partition: every row not in the first group goes, in order, to the second
+            const bool b = in && (partition ? !a : (born != nullptr && born[i] != 0));
             ba[k] = __ballot_sync(0xFFFFFFFFu, a);
             bb[k] = __ballot_sync(0xFFFFFFFFu, b);
             if (lane == 0) {
@@ -214,6 +215,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
             uint32_t total = S + births;
             if (total > out_capacity) total = out_capacity;
             if (d_n_out) *d_n_out = total;
+            if (d_s_out) *d_s_out = S;
             if (d_next_id && cp.id_col >= 0) *d_next_id = next_id + births;
             h->pad[0] = 0;
             h->pad[1] = 0;
@@ -280,6 +282,88 @@ extern "C" int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint
     // workspace keeps working when max_n changes between calls
     const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
     k_compact<<<tiles, kThreads, 0, st>>>(cp, max_n, d_n, alive, born, d_next_id, d_alive_total, d_n_out,
-                                          out_capacity, status, stride_tiles, h);
+                                          out_capacity, status, stride_tiles, h, 0, nullptr);
+    return launch_err();
+}
+
+extern "C" int fg_partition_agents(uint32_t max_n, const uint32_t* d_n, const uint32_t* first_group,
+                                   const fg_column* cols, uint32_t ncols, uint32_t* d_first_count,
+                                   void* workspace, size_t workspace_bytes, void* stream) {
+    if (!workspace || !first_group || ncols > FG_MAX_COLUMNS || (ncols && !cols)) return FG_ERR_INVALID_ARGUMENT;
+    if (max_n >= (1u << 31)) return FG_ERR_UNSUPPORTED;
+    if (workspace_bytes < fg_compact_workspace_size(max_n) || (reinterpret_cast<uintptr_t>(workspace) & 255))
+        return FG_ERR_WORKSPACE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(workspace);
+    WsHeader* h = reinterpret_cast<WsHeader*>(ws);
+    uint64_t* status = reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader));
+    // the first group is the compaction's "survivors" (counted first, so the
+    // second group knows where it starts), the rest its "births" in row order
+    cudaMemsetAsync(&h->alive_total, 0, sizeof(uint32_t), st);
+    int dev = 0, sms = 132;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t grid = std::max(1u, std::min((max_n + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
+    k_count_alive<<<grid, kThreads, 0, st>>>(max_n, d_n, first_group, h);
+    CompactParams cp{};
+    for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cp.bcol[c] = cols[c];
+    cp.ncols = ncols;
+    cp.id_col = -1;
+    const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
+    k_compact<<<comp_tiles(max_n), kThreads, 0, st>>>(cp, max_n, d_n, first_group, nullptr, nullptr, nullptr, nullptr,
+                                                     max_n, status, stride_tiles, h, 1, d_first_count);
+    return launch_err();
+}
+
+namespace fgk {
+
+// rows [begin, end) of the source columns -> rows [dst0, dst0 + end - begin) of the destination
+__global__ void __launch_bounds__(kThreads) k_append_rows(const __grid_constant__ CompactParams cp, uint32_t max_rows,
+                                                          const uint32_t* d_begin, const uint32_t* d_end,
+                                                          const uint32_t* d_dst_count, uint32_t dst_capacity,
+                                                          WsHeader* h) {
+    const uint32_t begin = d_begin ? *d_begin : 0u;
+    const uint32_t end = min(*d_end, max_rows);
+    const uint32_t dst0 = *d_dst_count;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; begin + r < end; r += gridDim.x * blockDim.x) {
+        const uint32_t dst = dst0 + r;
+        if (dst >= dst_capacity) {
+            record_status(h, FG_ERR_CAPACITY);
+            return;
+        }
+        for (uint32_t c = 0; c < cp.ncols; ++c) copy_col(cp.col[c], begin + r, dst);
+    }
+}
+
+__global__ void k_append_counts(uint32_t max_rows, const uint32_t* d_begin, uint32_t* d_src_count,
+                                uint32_t* d_dst_count, uint32_t dst_capacity) {
+    const uint32_t begin = d_begin ? *d_begin : 0u;
+    const uint32_t end = min(*d_src_count, max_rows);
+    const uint32_t moved = end > begin ? end - begin : 0u;
+    const uint32_t total = *d_dst_count + moved;
+    *d_dst_count = total < dst_capacity ? total : dst_capacity;
+    *d_src_count = begin < end ? begin : end;
+}
+
+}  // namespace fgk
+
+extern "C" int fg_append_rows(const fg_column* cols, uint32_t ncols, uint32_t max_rows, const uint32_t* d_begin,
+                              uint32_t* d_src_count, uint32_t* d_dst_count, uint32_t dst_capacity, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+    if (!workspace || workspace_bytes < sizeof(WsHeader) || !d_src_count || !d_dst_count || ncols > FG_MAX_COLUMNS ||
+        (ncols && !cols))
+        return FG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    WsHeader* h = reinterpret_cast<WsHeader*>(workspace);
+    CompactParams cp{};
+    for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cols[c];
+    cp.ncols = ncols;
+    cp.id_col = -1;
+    int dev = 0, sms = 132;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t grid = std::max(1u, std::min((max_rows + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
+    k_append_rows<<<grid, kThreads, 0, st>>>(cp, max_rows, d_begin, d_src_count, d_dst_count, dst_capacity, h);
+    k_append_counts<<<1, 1, 0, st>>>(max_rows, d_begin, d_src_count, d_dst_count, dst_capacity);
     return launch_err();
 }

@@ -122,6 +122,7 @@ std::string batch_unsupported(const ModelData& m) {
         if (!l->host_functions.empty()) return "the model has host layer functions";
     for (const auto& f : a.functions) {
         if (f->has_agent_death || !f->agent_output.empty()) return "agent birth/death";
+        if (f->condition) return "an agent function condition";
         if (f->message_output_optional) return "optional message output";
         if (!f->message_input.empty() && m.message(f->message_input)->kind == MessageKind::BruteForce)
             return "brute-force message input";

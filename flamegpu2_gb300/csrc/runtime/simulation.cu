@@ -207,6 +207,9 @@ struct FnRt {
     std::unique_ptr<FunctionTables> tables[2];  // per buffer parity of the agent list
     bool sort_trigger = false;
     bool stage = false;  // spatial input and the agent has float x, y (, z): stage neighbour windows
+    uint32_t* cond_fail = nullptr;  // condition result per row (1 = failed), capacity + 1 entries
+    uint32_t* d_first = nullptr;    // rows that failed the condition (device)
+    AgentList* end_list = nullptr;  // state transition target, or null
 };
 
 struct SimulationImpl {
@@ -364,17 +367,22 @@ struct SimulationImpl {
         }
         for (const auto& a : model->agents)
             for (const auto& f : a->functions) {
-                if (f->initial_state != f->end_state)
-                    THROW exception::InvalidAgentFunc(format("Function '%s': agent state transitions are not supported yet", f->name.c_str()));
                 FnRt r;
                 r.fn = f.get();
                 r.list = list_of(a->name, f->initial_state);
+                if (f->initial_state != f->end_state) r.end_list = list_of(a->name, f->end_state);
                 r.in = f->message_input.empty() ? nullptr : msg_of(f->message_input);
                 r.out = f->message_output.empty() ? nullptr : msg_of(f->message_output);
                 if (r.out && f->message_output_optional) r.out->optional_any = true;
                 if (!f->agent_output.empty()) {
-                    if (f->agent_output != a->name || f->agent_output_state != f->initial_state)
-                        THROW exception::InvalidAgentFunc(format("Function '%s': agent output into another agent or state is not supported yet", f->name.c_str()));
+                    // births land after the function's surviving agents, which a
+                    // state transition then moves: the output state must be
+                    // where those agents end up
+                    if (f->agent_output != a->name || f->agent_output_state != f->end_state)
+                        THROW exception::InvalidAgentFunc(format(
+                            "Function '%s': agent output is supported into the function's own agent type and end state "
+                            "('%s'), not '%s' state '%s'",
+                            f->name.c_str(), f->end_state.c_str(), f->agent_output.c_str(), f->agent_output_state.c_str()));
                     r.births = true;
                 }
                 // determineAgentsToSort (CUDASimulation.cu:409-461)
@@ -437,6 +445,11 @@ struct SimulationImpl {
             if (f.fn->has_agent_death) {
                 mem.release(f.death_flags);
                 f.death_flags = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
+            }
+            if (f.fn->condition) {
+                mem.release(f.cond_fail);
+                f.cond_fail = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(cap) + 1)));
+                if (!f.d_first) f.d_first = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
             }
             if (f.births) {
                 mem.release(f.birth_flags);
@@ -680,8 +693,25 @@ struct SimulationImpl {
         c.used = true;
     }
 
+    bool any_transitions() const {
+        for (const auto& f : fns)
+            if (f.end_list) return true;
+        return false;
+    }
+    size_t list_index(const AgentList* l) const {
+        for (size_t i = 0; i < lists.size(); ++i)
+            if (lists[i].get() == l) return i;
+        return 0;
+    }
+    // A transition can move a whole list (its bound) into the end state's
+    // list once per step.
+    void add_transitions(std::vector<uint64_t>& bound, uint64_t rounds) const {
+        for (const auto& f : fns)
+            if (f.end_list) bound[list_index(f.end_list)] += bound[list_index(f.list)] * rounds;
+    }
+
     void prepare_capacity() {
-        if (!any_births()) return;
+        if (!any_births() && !any_transitions()) return;
         // newest reported counts
         const CountSlot* known = nullptr;
         for (size_t k = 0; k < count_ring.size(); ++k) {
@@ -699,13 +729,19 @@ struct SimulationImpl {
             } else {
                 bound[i] = grow_bound(lists[i]->bound, b);
             }
-            if (bound[i] > lists[i]->capacity) over = true;
         }
+        {
+            const uint64_t rounds = (known && known->step_after <= step_count) ? step_count - known->step_after + 1 : 1;
+            add_transitions(bound, rounds);
+        }
+        for (size_t i = 0; i < lists.size(); ++i)
+            if (bound[i] > lists[i]->capacity) over = true;
         if (over) {
             // exact counts after every issued step, then grow what needs it
             sync_counts();
+            for (size_t i = 0; i < lists.size(); ++i) bound[i] = grow_bound(lists[i]->bound, births_per_step(lists[i].get()));
+            add_transitions(bound, 1);
             for (size_t i = 0; i < lists.size(); ++i) {
-                bound[i] = grow_bound(lists[i]->bound, births_per_step(lists[i].get()));
                 if (cuda_config.max_agents && bound[i] > cuda_config.max_agents)
                     THROW exception::OutOfMemory(format("Agent '%s' may reach %llu agents in the next step, above the limit of %u",
                                                         lists[i]->agent->name.c_str(), static_cast<unsigned long long>(bound[i]),
@@ -854,11 +890,43 @@ struct SimulationImpl {
         }
         if (f.out && f.out->optional_any && !f.fn->message_output_optional)
             FG_CUDA(cudaMemsetAsync(f.out->valid, 1, sizeof(uint32_t) * f.out->capacity, stream));
+        if (f.fn->condition) {
+            // FLAMEGPU_AGENT_FUNCTION_CONDITION, then the failing agents to the
+            // front of the list and the others after them
+            // (CUDASimulation.cu:820-836, CUDAFatAgent.cu:186-236)
+            LaunchParams C;
+            std::memset(&C, 0, sizeof(C));
+            C.T = *f.tables[l.parity];
+            C.max_n = l.capacity;
+            C.d_n = l.d_count;
+            C.cond_fail = f.cond_fail;
+            C.d_step = d_step();
+            C.seed = config.random_seed;
+            C.fn_uid = f.fn->uid;
+            C.error = d_error();
+            C.env = d_env;
+            cudaError_t ce = cudaSuccess;
+            timed("cond:" + f.fn->name, [&] {
+                ce = f.fn->condition(C, grid_for(l.capacity + 1, kAgentBlock, 1 << 16), kAgentBlock, 0, stream);
+            });
+            if (ce != cudaSuccess)
+                THROW exception::CUDAError(format("Launch of the condition of '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(ce)));
+            std::vector<fg_column> pc(l.cols.size());
+            for (size_t v = 0; v < l.cols.size(); ++v)
+                pc[v] = fg_column{l.cols[v][l.parity], l.cols[v][l.parity ^ 1], l.agent->variables[v].bytes()};
+            timed("partition:" + l.agent->name, [&] {
+                FG_CAPI(fg_partition_agents(l.capacity, l.d_count, f.cond_fail, pc.data(), static_cast<uint32_t>(pc.size()),
+                                            f.d_first, l.comp_ws, l.comp_ws_bytes, stream));
+            });
+            l.parity ^= 1;
+            kernel_counter += 3;
+        }
         LaunchParams P;
         std::memset(&P, 0, sizeof(P));
         P.T = *f.tables[l.parity];
         P.max_n = l.capacity;
         P.d_n = l.d_count;
+        P.d_first = f.fn->condition ? f.d_first : nullptr;
         if (f.out) {
             P.msg_out_valid = f.fn->message_output_optional ? f.out->valid : nullptr;
             P.msg_out_count = f.out->d_count;
@@ -924,6 +992,21 @@ struct SimulationImpl {
                                           l.capacity, l.comp_ws, l.comp_ws_bytes, stream));
             });
             l.parity ^= 1;
+            kernel_counter += 2;
+        }
+        if (f.end_list) {
+            // state transition (CUDAFatAgent.cu:139-184): the agents that ran the
+            // function (and their births) are appended, in order, to the end
+            // state's list; the list keeps the agents that failed the condition
+            AgentList& E = *f.end_list;
+            std::vector<fg_column> tc(l.cols.size());
+            for (size_t v = 0; v < l.cols.size(); ++v)
+                tc[v] = fg_column{l.cols[v][l.parity], E.cols[v][E.parity], l.agent->variables[v].bytes()};
+            timed("transition:" + l.agent->name, [&] {
+                FG_CAPI(fg_append_rows(tc.data(), static_cast<uint32_t>(tc.size()), l.capacity,
+                                       f.fn->condition ? f.d_first : nullptr, l.d_count, E.d_count, E.capacity, E.comp_ws,
+                                       E.comp_ws_bytes, stream));
+            });
             kernel_counter += 2;
         }
     }
@@ -1050,6 +1133,7 @@ struct SimulationImpl {
                     if (f.fn != fd) continue;
                     AgentList& l = *f.list;
                     if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0) l.parity ^= 1;
+                    if (f.fn->condition) l.parity ^= 1;
                     if (f.fn->has_agent_death || f.births) l.parity ^= 1;
                 }
     }

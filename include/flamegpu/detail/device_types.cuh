@@ -134,6 +134,12 @@ struct LaunchParams {
     FunctionTables T;
     uint32_t max_n;              // capacity of the agent list (grid sizing bound)
     const uint32_t* d_n;         // agents in the list (device)
+    // Agent function condition (single simulations): rows [0, *d_first) failed
+    // the condition and are not run (their death / birth flags are written as
+    // alive / not born); rows [*d_first, n) are, and their message rows start
+    // at 0. Null: every row runs.
+    const uint32_t* d_first;
+    uint32_t* cond_fail;         // condition kernels: 1 per row that fails, 0 past the population
     // message output
     uint32_t* msg_out_valid;     // per-row output flag (optional outputs), or null
     uint32_t* msg_out_count;     // set to the agent count by the launch

@@ -55,6 +55,7 @@ struct AgentFunctionData {
     std::string name;
     AgentData* parent = nullptr;
     AgentFunctionLauncher launcher = nullptr;
+    AgentFunctionLauncher condition = nullptr;  // FLAMEGPU_AGENT_FUNCTION_CONDITION kernel, or null
     std::type_index msg_in_type = std::type_index(typeid(void));
     std::type_index msg_out_type = std::type_index(typeid(void));
     std::string message_input, message_output;
@@ -273,6 +274,11 @@ class AgentFunctionDescription {
     void setInitialState(const std::string& s);
     void setEndState(const std::string& s);
     void dependsOn(const AgentFunctionDescription& other) { fn->dependencies.push_back(other.fn); }
+    /** AgentFunctionDescription::setFunctionCondition (AgentFunctionDescription.h:263-271):
+     *  only agents for which the FLAMEGPU_AGENT_FUNCTION_CONDITION holds run the function. */
+    template <typename C>
+    void setFunctionCondition(C) { fn->condition = C::launcher(); }
+    bool hasFunctionCondition() const { return fn->condition != nullptr; }
     std::string getName() const { return fn->name; }
     std::string getMessageInputName() const { return fn->message_input; }
     std::string getMessageOutputName() const { return fn->message_output; }

@@ -57,7 +57,7 @@ __device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, u
         c.step = P.d_step ? *P.d_step : 0u;
         c.env = P.env;
         c.seed = P.seed;
-        c.row_begin = 0;
+        c.row_begin = P.d_first ? *P.d_first : 0u;  // rows before it failed the function's condition
         c.count = n_single;
         return;
     }
@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
     using MsgOut = typename F::MessageOut;
     // rows to visit: the population (single) or every row of the batch
     const uint32_t n = P.batch ? P.max_n : (P.d_n ? min(*P.d_n, P.max_n) : P.max_n);
-    if (P.msg_out_count && blockIdx.x == 0 && threadIdx.x == 0) *P.msg_out_count = n;
+    const uint32_t first_row = (!P.batch && P.d_first) ? min(*P.d_first, n) : 0u;
+    if (P.msg_out_count && blockIdx.x == 0 && threadIdx.x == 0) *P.msg_out_count = n - first_row;
     constexpr int kDims = std::is_same<MsgIn, MessageSpatial3D>::value ? 3 : (std::is_same<MsgIn, MessageSpatial2D>::value ? 2 : 0);
     bool first = true;
     if (!P.batch) {
@@ -102,7 +103,13 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
         }
         first = false;
         if (live == 0xFFFFFFFFu) continue;
-        DeviceAPI<MsgIn, MsgOut> api(P, idx);
+        if (idx < first_row) {  // failed the condition: kept as it is
+            if (P.death_flags) P.death_flags[idx] = static_cast<uint32_t>(ALIVE);
+            if (P.birth_flags) P.birth_flags[idx] = 0u;
+            continue;
+        }
+        const uint32_t msg_row = idx - first_row;
+        DeviceAPI<MsgIn, MsgOut> api(P, idx, msg_row);
         const AGENT_STATUS st = F()(&api);
         if (P.death_flags) {
             P.death_flags[idx] = static_cast<uint32_t>(st);
@@ -110,8 +117,34 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
             device_error(P, kDevDeathNotEnabled, 0, idx);
         }
         if (P.birth_flags) P.birth_flags[idx] = api.agent_out.born();
-        if (P.msg_out_valid) P.msg_out_valid[idx] = api.message_out.written();
+        if (P.msg_out_valid) P.msg_out_valid[msg_row] = api.message_out.written();
     }
+}
+
+// FLAMEGPU_AGENT_FUNCTION_CONDITION kernel (AgentFunctionCondition.cuh:44-100):
+// cond_fail[i] = 1 for each agent whose condition is false, 0 for those that
+// pass and for rows past the population up to max_n (an exclusive scan of the
+// max_n + 1 flags then counts and places the failing agents).
+template <typename C>
+__global__ void __launch_bounds__(kAgentBlock) agent_condition_kernel(const __grid_constant__ LaunchParams P) {
+    const uint32_t n = P.d_n ? min(*P.d_n, P.max_n) : P.max_n;
+    fill_ctx(P, 0, n);
+    __syncthreads();
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx <= P.max_n; idx += gridDim.x * blockDim.x) {
+        uint32_t fail = 0u;
+        if (idx < n) {
+            ReadOnlyDeviceAPI api(P, idx);
+            fail = C()(&api) ? 0u : 1u;
+        }
+        P.cond_fail[idx] = fail;
+    }
+}
+
+template <typename C>
+cudaError_t launch_agent_condition(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int,
+                                   cudaStream_t stream) {
+    agent_condition_kernel<C><<<grid, block, 0, stream>>>(p);
+    return cudaGetLastError();
 }
 
 template <typename F>
@@ -147,5 +180,18 @@ cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsi
     funcName##_impl funcName;                                                                                    \
     __device__ __forceinline__ flamegpu::AGENT_STATUS funcName##_impl::operator()(                               \
         flamegpu::DeviceAPI<message_in, message_out>* FLAMEGPU) const
+
+/** FLAMEGPU_AGENT_FUNCTION_CONDITION (include/flamegpu/runtime/AgentFunctionCondition_shim.cuh):
+ *  a device predicate over the read-only device API; agents for which it is
+ *  false skip the function they are attached to (setFunctionCondition). */
+#define FLAMEGPU_AGENT_FUNCTION_CONDITION(funcName)                                                              \
+    struct funcName##_cdn_impl {                                                                                 \
+        __device__ __forceinline__ bool operator()(flamegpu::ReadOnlyDeviceAPI* FLAMEGPU) const;                 \
+        static flamegpu::detail::AgentFunctionLauncher launcher() {                                              \
+            return &flamegpu::detail::launch_agent_condition<funcName##_cdn_impl>;                               \
+        }                                                                                                        \
+    };                                                                                                           \
+    funcName##_cdn_impl funcName;                                                                                \
+    __device__ __forceinline__ bool funcName##_cdn_impl::operator()(flamegpu::ReadOnlyDeviceAPI* FLAMEGPU) const
 
 #endif  // INCLUDE_FLAMEGPU_RUNTIME_AGENTFUNCTION_CUH_

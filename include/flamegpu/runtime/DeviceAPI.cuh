@@ -933,6 +933,10 @@ class DeviceAPI {
 
     __device__ DeviceAPI(const detail::LaunchParams& p, uint32_t idx)
         : message_in(p), message_out(p, idx), agent_out(p, idx), environment(p), random(p, idx), P(p), index(idx) {}
+    /** msg_row: the row this agent's output message takes (the agent's index
+     *  among those running the function). */
+    __device__ DeviceAPI(const detail::LaunchParams& p, uint32_t idx, uint32_t msg_row)
+        : message_in(p), message_out(p, msg_row), agent_out(p, idx), environment(p), random(p, idx), P(p), index(idx) {}
 
     template <typename T>
     __device__ T getVariable(detail::VarName name) const {
@@ -963,6 +967,32 @@ class DeviceAPI {
     typename MessageIn::In message_in;
     typename MessageOut::Out message_out;
     AgentOut agent_out;
+    DeviceEnvironment environment;
+    AgentRandom random;
+
+ private:
+    const detail::LaunchParams& P;
+    uint32_t index;
+};
+
+/** ReadOnlyDeviceAPI (DeviceAPI.cuh:42-142 of the reference): what an agent
+ *  function condition may use — the agent's variables and id, the step
+ *  counter, environment properties and random numbers; nothing is written. */
+class ReadOnlyDeviceAPI {
+ public:
+    __device__ ReadOnlyDeviceAPI(const detail::LaunchParams& p, uint32_t idx)
+        : environment(p), random(p, idx), P(p), index(idx) {}
+    template <typename T>
+    __device__ T getVariable(detail::VarName name) const {
+        return detail::read_rw<T>(P, &P.T.agent, name.hash, index);
+    }
+    template <typename T, flamegpu::size_type N>
+    __device__ T getVariable(detail::VarName name, unsigned int i) const {
+        return detail::read_rw<T>(P, &P.T.agent, name.hash, index, i);
+    }
+    __device__ id_t getID() const { return detail::read_rw<id_t>(P, &P.T.agent, detail::VarName("_id").hash, index); }
+    __device__ unsigned int getStepCounter() const { return detail::ctx().step; }
+
     DeviceEnvironment environment;
     AgentRandom random;
 

@@ -153,6 +153,31 @@ int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint32_t* alive
                       uint32_t* d_n_out, uint32_t out_capacity,
                       void* workspace, size_t workspace_bytes, void* stream);
 
+/* Stable two-way partition of an agent list. Replaces the agent function
+ * condition scatter of CUDAFatAgent::processFunctionCondition
+ * (src/flamegpu/simulation/detail/CUDAFatAgent.cu:186-236), which moves the
+ * agents whose condition failed to the front of the list and the others after
+ * them, each group in its original order. Rows i < n with first_group[i] != 0
+ * go first, the rest follow; every column is written from cols[c].in to
+ * cols[c].out (distinct arrays). *d_first_count receives the size of the first
+ * group (device). Workspace: fg_compact_workspace_size(max_n), shared with
+ * fg_compact_agents (calls on one workspace must be ordered). */
+int fg_partition_agents(uint32_t max_n, const uint32_t* d_n, const uint32_t* first_group,
+                        const fg_column* cols, uint32_t ncols, uint32_t* d_first_count,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Agent state transition. Replaces CUDAFatAgent::transitionState
+ * (src/flamegpu/simulation/detail/CUDAFatAgent.cu:139-184): rows
+ * [*d_begin (0 if NULL), *d_src_count) of the source columns (cols[c].in) are
+ * appended, in order, after the *d_dst_count rows of the destination columns
+ * (cols[c].out); then *d_dst_count grows by their number and *d_src_count
+ * becomes *d_begin. max_rows bounds the source rows (grid sizing); rows past
+ * dst_capacity are not written and the workspace records FG_ERR_CAPACITY
+ * (any workspace of at least 256 bytes initialised by fg_workspace_init). */
+int fg_append_rows(const fg_column* cols, uint32_t ncols, uint32_t max_rows, const uint32_t* d_begin,
+                   uint32_t* d_src_count, uint32_t* d_dst_count, uint32_t dst_capacity, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
 /* Exclusive scan of n u32 values (single pass, decoupled look-back); out may
  * alias in. Used for PBMs built elsewhere; replaces cub::DeviceScan::ExclusiveSum
  * on this path. */

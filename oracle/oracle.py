@@ -243,3 +243,55 @@ def predprey_run(params: dict, prey: dict, pred: dict, steps: int, next_prey_id:
     m, q = int(nprey[0]), int(npred[0])
     return ({"x": px[:m].copy(), "y": py[:m].copy(), "_id": pid[:m].copy()},
             {"x": qx[:q].copy(), "y": qy[:q].copy(), "_id": qid[:q].copy()}, int(nid[0]))
+
+
+def state_mix_run(pops: dict, next_id: int, steps: int, first_step: int = 0):
+    """The "state_mix" model of examples/state_tests/state_tests.cu, serially
+    (pure Python: small populations only). pops: {"A": {"_id", "v", "x"},
+    "B": {...}} of numpy arrays. Per function, following the reference:
+      condition  failing agents first, passing ones after, each in order
+                 (CUDAFatAgent::processFunctionCondition, CUDAFatAgent.cu:186-236);
+      death      the passing agents that return DEAD are removed, order kept
+                 (CUDAFatAgent::processDeath, CUDAFatAgent.cu:105-137);
+      transition the surviving passing agents are appended to the end state
+                 (CUDAFatAgent::transitionState, CUDAFatAgent.cu:139-184);
+      births     appended to the output state after that, in parent order,
+                 with consecutive new ids (CUDASimulation.cu:1064-1079,
+                 CUDAAgentStateList.cu:189-250).
+    Returns (pops, next_id)."""
+    f32 = np.float32
+    st = {k: [(int(i), int(v), f32(x)) for i, v, x in zip(p["_id"], p["v"], p["x"])] for k, p in pops.items()}
+
+    def run(src, dst, cond, body):
+        nonlocal next_id
+        fails = [a for a in st[src] if not cond(a)]
+        passes = [a for a in st[src] if cond(a)]
+        survivors, births = [], []
+        for a in passes:
+            new, child, alive = body(a)
+            if child is not None:
+                births.append(child)
+            if alive:
+                survivors.append(new)
+        births = [(next_id + k, v, x) for k, (v, x) in enumerate(births)]
+        next_id += len(births)
+        if src == dst:
+            st[src] = fails + survivors + births
+        else:
+            st[src] = fails
+            st[dst] = st[dst] + survivors + births
+
+    for s in range(first_step, first_step + steps):
+        def ab(a):
+            i, v, x = a
+            x = f32(x + f32(1.0))
+            child = (v + 1000, x) if i % 5 == 0 else None
+            return (i, v, x), child, i % 7 != 0
+        run("A", "B", lambda a: (a[0] + s) % 3 == 0, ab)
+        run("B", "A", lambda a: a[0] % 2 == 0, lambda a: ((a[0], a[1], f32(a[2] * f32(2.0))), None, True))
+        run("A", "A", lambda a: a[2] > f32(10.0), lambda a: ((a[0], a[1], f32(a[2] - f32(10.0))), None, True))
+    out = {}
+    for k, lst in st.items():
+        out[k] = {"_id": np.array([a[0] for a in lst], np.uint32), "v": np.array([a[1] for a in lst], np.uint32),
+                  "x": np.array([a[2] for a in lst], np.float32)}
+    return out, next_id
