@@ -120,6 +120,10 @@ std::string batch_unsupported(const ModelData& m) {
         return "the model has host functions";
     for (const auto& l : m.layers)
         if (!l->host_functions.empty()) return "the model has host layer functions";
+    for (const auto& f : a.functions)
+        for (const auto& g : a.functions)
+            if (f != g && !f->message_output.empty() && f->message_output == g->message_output)
+                return "a message list output by more than one function";
     for (const auto& f : a.functions) {
         if (f->has_agent_death || !f->agent_output.empty()) return "agent birth/death";
         if (f->condition) return "an agent function condition";

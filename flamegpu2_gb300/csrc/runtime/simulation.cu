@@ -191,6 +191,10 @@ struct MsgList {
     void* bf_ws = nullptr;
     size_t bf_ws_bytes = 0;
     bool needs_build = true;
+    // truncate / append (CUDASimulation.cu:598-601,874,1058): the first output
+    // of a step truncates the list, later ones append after its messages
+    bool written = false;            // host, while a step is being issued
+    uint32_t* d_base = nullptr;      // count before an appending output (device)
     bool spatial() const { return msg->kind != MessageKind::BruteForce; }
 };
 
@@ -347,6 +351,7 @@ struct SimulationImpl {
             auto ml = std::make_unique<MsgList>();
             ml->msg = m.get();
             ml->d_count = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
+            ml->d_base = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
             for (const auto& v : m->variables) ml->slot_bytes.push_back(round4(v.bytes()));
             if (m->kind != MessageKind::BruteForce) {
                 const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
@@ -441,7 +446,7 @@ struct SimulationImpl {
         // dependants: message lists written by this list's functions, birth staging, flags
         for (auto& f : fns) {
             if (f.list != &l) continue;
-            if (f.out) ensure_msg_capacity(*f.out, cap);
+            if (f.out) ensure_msg_capacity(*f.out, producers_capacity(*f.out));
             if (f.fn->has_agent_death) {
                 mem.release(f.death_flags);
                 f.death_flags = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
@@ -460,6 +465,15 @@ struct SimulationImpl {
             }
         }
         invalidate();
+    }
+
+    // Messages one step can put in a list: every function that outputs to it
+    // may append a message per agent of its list.
+    uint32_t producers_capacity(const MsgList& m) const {
+        uint64_t c = 0;
+        for (const auto& g : fns)
+            if (g.out == &m) c += g.list->capacity;
+        return static_cast<uint32_t>(std::min<uint64_t>(std::max<uint64_t>(c, 1), (1ull << 31) - 1));
     }
 
     void ensure_msg_capacity(MsgList& m, uint32_t cap) {
@@ -888,8 +902,11 @@ struct SimulationImpl {
             if (do_sort) timed("sort:" + l.agent->name, [&] { enqueue_sort(f); });
             if (do_build) timed("build:" + f.in->msg->name, [&] { enqueue_build(*f.in, stream); });
         }
-        if (f.out && f.out->optional_any && !f.fn->message_output_optional)
-            FG_CUDA(cudaMemsetAsync(f.out->valid, 1, sizeof(uint32_t) * f.out->capacity, stream));
+        const bool append = f.out && f.out->written;
+        if (f.out) {
+            f.out->written = true;
+            if (append) FG_CUDA(cudaMemcpyAsync(f.out->d_base, f.out->d_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+        }
         if (f.fn->condition) {
             // FLAMEGPU_AGENT_FUNCTION_CONDITION, then the failing agents to the
             // front of the list and the others after them
@@ -928,8 +945,10 @@ struct SimulationImpl {
         P.d_n = l.d_count;
         P.d_first = f.fn->condition ? f.d_first : nullptr;
         if (f.out) {
-            P.msg_out_valid = f.fn->message_output_optional ? f.out->valid : nullptr;
+            P.msg_out_valid = f.out->optional_any ? f.out->valid : nullptr;
+            P.msg_out_always = f.fn->message_output_optional ? 0 : 1;
             P.msg_out_count = f.out->d_count;
+            P.msg_out_base = append ? f.out->d_base : nullptr;
             P.msg_out_enabled = 1;
         }
         if (f.in) {
@@ -1013,8 +1032,10 @@ struct SimulationImpl {
 
     void enqueue_step() {
         kernel_counter = 0;
-        for (auto& m : msgs)
+        for (auto& m : msgs) {
             if (!m->msg->persistent) m->needs_build = true;
+            m->written = false;
+        }
         for (const auto& layer : model->layers) {
             for (auto* fd : layer->functions)
                 for (auto& f : fns)
@@ -1061,8 +1082,10 @@ struct SimulationImpl {
         if (has_layer_host_functions() || !cuda_config.use_graphs || profiling) {
             HostAPI api(this);
             kernel_counter = 0;
-            for (auto& m : msgs)
+            for (auto& m : msgs) {
                 if (!m->msg->persistent) m->needs_build = true;
+                m->written = false;
+            }
             for (const auto& layer : model->layers) {
                 if (!layer->host_functions.empty()) {
                     run_host_layer(layer.get(), api);

@@ -141,9 +141,11 @@ struct LaunchParams {
     const uint32_t* d_first;
     uint32_t* cond_fail;         // condition kernels: 1 per row that fails, 0 past the population
     // message output
-    uint32_t* msg_out_valid;     // per-row output flag (optional outputs), or null
-    uint32_t* msg_out_count;     // set to the agent count by the launch
+    uint32_t* msg_out_valid;     // per-row output flag (lists with an optional output), or null
+    uint32_t* msg_out_count;     // set to the message count by the launch
+    const uint32_t* msg_out_base;  // messages already in the list this step (append), or null (truncate)
     int msg_out_enabled;
+    int msg_out_always;          // every running agent outputs (not optional): valid = 1
     // message input
     fg_spatial_grid in_grid;     // spatial metadata (MessageSpatial3D::MetaData)
     const uint32_t* in_pbm;      // partition boundary matrix, binCount + 1 entries

@@ -426,6 +426,8 @@ class ModelDescription {
         detail::MessageData* d = new_message(name, kind_of<MsgType>());
         return typename MsgType::Description(model, d);
     }
+    /** ModelDescription::newMessage(name) (include/flamegpu/model/ModelDescription.h:110): a brute-force message list. */
+    MessageBruteForce::Description newMessage(const std::string& name) { return newMessage<MessageBruteForce>(name); }
     template <typename MsgType>
     typename MsgType::Description Message(const std::string& name) const {
         detail::MessageData* d = model->message(name);

@@ -81,7 +81,9 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
     // rows to visit: the population (single) or every row of the batch
     const uint32_t n = P.batch ? P.max_n : (P.d_n ? min(*P.d_n, P.max_n) : P.max_n);
     const uint32_t first_row = (!P.batch && P.d_first) ? min(*P.d_first, n) : 0u;
-    if (P.msg_out_count && blockIdx.x == 0 && threadIdx.x == 0) *P.msg_out_count = n - first_row;
+    // message rows: after those already output to the list this step (append), else from 0
+    const uint32_t msg_base = (!P.batch && P.msg_out_base) ? *P.msg_out_base : 0u;
+    if (P.msg_out_count && blockIdx.x == 0 && threadIdx.x == 0) *P.msg_out_count = msg_base + n - first_row;
     constexpr int kDims = std::is_same<MsgIn, MessageSpatial3D>::value ? 3 : (std::is_same<MsgIn, MessageSpatial2D>::value ? 2 : 0);
     bool first = true;
     if (!P.batch) {
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
             if (P.birth_flags) P.birth_flags[idx] = 0u;
             continue;
         }
-        const uint32_t msg_row = idx - first_row;
+        const uint32_t msg_row = msg_base + idx - first_row;
         DeviceAPI<MsgIn, MsgOut> api(P, idx, msg_row);
         const AGENT_STATUS st = F()(&api);
         if (P.death_flags) {
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __gri
             device_error(P, kDevDeathNotEnabled, 0, idx);
         }
         if (P.birth_flags) P.birth_flags[idx] = api.agent_out.born();
-        if (P.msg_out_valid) P.msg_out_valid[msg_row] = api.message_out.written();
+        if (P.msg_out_valid) P.msg_out_valid[msg_row] = P.msg_out_always ? 1u : api.message_out.written();
     }
 }
 
