@@ -266,6 +266,10 @@ extern "C" int fgs_time_ops_in_graphs(fgs_sim* s, int32_t enable) {
 
 extern "C" int fgs_harvest_profile(fgs_sim* s) { return guarded([&] { s->sim->harvestOperationTimes(); }); }
 
+extern "C" int fgs_export(fgs_sim* s, const char* path) { return guarded([&] { s->sim->exportData(path); }); }
+
+extern "C" int fgs_load_state(fgs_sim* s, const char* path) { return guarded([&] { s->sim->loadState(path); }); }
+
 extern "C" int fgs_take_profile(fgs_sim* s, char* buf, size_t len) {
     return guarded([&] {
         std::string out;

@@ -32,6 +32,7 @@
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu_gb300/fg_capi.h"
 #include "runtime/internal.h"
+#include "runtime/json.h"
 
 namespace flamegpu {
 namespace detail {
@@ -1265,7 +1266,236 @@ CUDASimulation::~CUDASimulation() = default;
 
 CUDASimulation::SimConfig& CUDASimulation::SimulationConfig() { return impl->config; }
 CUDASimulation::Config& CUDASimulation::CUDAConfig() { return impl->cuda_config; }
-void CUDASimulation::applyConfig() { impl->invalidate(); }
+void CUDASimulation::applyConfig() {
+    impl->invalidate();
+    if (!impl->config.input_file.empty()) loadState(impl->config.input_file);
+}
+
+// ------------------------------------------------------------ state files
+
+namespace {
+
+// One element of a column, as JSON number text (floats with enough digits to
+// read back the same value).
+std::string number_text(std::type_index t, const char* p) {
+    char buf[64];
+    if (t == std::type_index(typeid(float))) std::snprintf(buf, sizeof(buf), "%.9g", static_cast<double>(*reinterpret_cast<const float*>(p)));
+    else if (t == std::type_index(typeid(double))) std::snprintf(buf, sizeof(buf), "%.17g", *reinterpret_cast<const double*>(p));
+    else if (t == std::type_index(typeid(int64_t))) std::snprintf(buf, sizeof(buf), "%lld", static_cast<long long>(*reinterpret_cast<const int64_t*>(p)));
+    else if (t == std::type_index(typeid(uint64_t))) std::snprintf(buf, sizeof(buf), "%llu", static_cast<unsigned long long>(*reinterpret_cast<const uint64_t*>(p)));
+    else if (t == std::type_index(typeid(int32_t))) std::snprintf(buf, sizeof(buf), "%d", *reinterpret_cast<const int32_t*>(p));
+    else if (t == std::type_index(typeid(uint32_t))) std::snprintf(buf, sizeof(buf), "%u", *reinterpret_cast<const uint32_t*>(p));
+    else if (t == std::type_index(typeid(int16_t))) std::snprintf(buf, sizeof(buf), "%d", *reinterpret_cast<const int16_t*>(p));
+    else if (t == std::type_index(typeid(uint16_t))) std::snprintf(buf, sizeof(buf), "%u", *reinterpret_cast<const uint16_t*>(p));
+    else if (t == std::type_index(typeid(int8_t))) std::snprintf(buf, sizeof(buf), "%d", *reinterpret_cast<const int8_t*>(p));
+    else if (t == std::type_index(typeid(uint8_t))) std::snprintf(buf, sizeof(buf), "%u", *reinterpret_cast<const uint8_t*>(p));
+    else THROW exception::InvalidArgument("State files: unsupported variable type");
+    return buf;
+}
+
+void number_value(std::type_index t, const detail::json::Value& v, char* p) {
+    if (v.kind != detail::json::Value::Number) THROW exception::InvalidArgument("State file: a number was expected");
+    if (t == std::type_index(typeid(float))) *reinterpret_cast<float*>(p) = std::strtof(v.text.c_str(), nullptr);
+    else if (t == std::type_index(typeid(double))) *reinterpret_cast<double*>(p) = v.number();
+    else if (t == std::type_index(typeid(int64_t))) *reinterpret_cast<int64_t*>(p) = v.integer();
+    else if (t == std::type_index(typeid(uint64_t))) *reinterpret_cast<uint64_t*>(p) = v.uinteger();
+    else if (t == std::type_index(typeid(int32_t))) *reinterpret_cast<int32_t*>(p) = static_cast<int32_t>(v.integer());
+    else if (t == std::type_index(typeid(uint32_t))) *reinterpret_cast<uint32_t*>(p) = static_cast<uint32_t>(v.uinteger());
+    else if (t == std::type_index(typeid(int16_t))) *reinterpret_cast<int16_t*>(p) = static_cast<int16_t>(v.integer());
+    else if (t == std::type_index(typeid(uint16_t))) *reinterpret_cast<uint16_t*>(p) = static_cast<uint16_t>(v.uinteger());
+    else if (t == std::type_index(typeid(int8_t))) *reinterpret_cast<int8_t*>(p) = static_cast<int8_t>(v.integer());
+    else if (t == std::type_index(typeid(uint8_t))) *reinterpret_cast<uint8_t*>(p) = static_cast<uint8_t>(v.uinteger());
+    else THROW exception::InvalidArgument("State files: unsupported variable type");
+}
+
+// a scalar, or an array of `elements` values
+void write_elements(detail::json::Writer& w, std::type_index t, uint32_t size, uint32_t elements, const char* p) {
+    if (elements == 1) {
+        w.raw(number_text(t, p));
+        return;
+    }
+    w.begin_array();
+    for (uint32_t e = 0; e < elements; ++e) w.raw(number_text(t, p + static_cast<size_t>(e) * size));
+    w.end_array();
+}
+
+void read_elements(const detail::json::Value& v, std::type_index t, uint32_t size, uint32_t elements, char* p,
+                   const std::string& what) {
+    if (elements == 1) {
+        number_value(t, v, p);
+        return;
+    }
+    if (v.kind != detail::json::Value::Array || v.items.size() != elements)
+        THROW exception::InvalidArgument(format("State file: '%s' should be an array of %u values", what.c_str(), elements));
+    for (uint32_t e = 0; e < elements; ++e) number_value(t, v.items[e], p + static_cast<size_t>(e) * size);
+}
+
+}  // namespace
+
+void CUDASimulation::exportData(const std::string& path) {
+    // layout of the reference's JSONStateWriter (src/flamegpu/io/JSONStateWriter.cu:55-330):
+    // config, stats.step_count, environment, agents -> state -> [ {variable: value} ]
+    synchronize();
+    std::FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) THROW exception::InvalidArgument(format("Cannot open '%s' for writing", path.c_str()));
+    detail::json::Writer w(f);
+    const auto& m = *impl->model;
+    w.begin_object();
+    w.key("config");
+    w.begin_object();
+    w.key("simulation");
+    w.begin_object();
+    w.key("random_seed");
+    w.raw(std::to_string(impl->config.random_seed));
+    w.key("steps");
+    w.raw(std::to_string(impl->config.steps));
+    w.end_object();
+    w.key("cuda");
+    w.begin_object();
+    w.key("device_id");
+    w.raw(std::to_string(impl->cuda_config.device_id));
+    w.key("inLayerConcurrency");
+    w.raw(impl->cuda_config.inLayerConcurrency ? "true" : "false");
+    w.end_object();
+    w.end_object();
+    w.key("stats");
+    w.begin_object();
+    w.key("step_count");
+    w.raw(std::to_string(impl->step_count));
+    // GB300 extension: each agent type's next id, so a run resumed from this
+    // file gives births the ids the uninterrupted run would have
+    {
+        std::vector<uint32_t> next(m.agents.size(), 1u);
+        FG_CUDA(cudaMemcpy(next.data(), impl->d_next_id(0), sizeof(uint32_t) * next.size(), cudaMemcpyDeviceToHost));
+        w.key("next_id");
+        w.begin_object();
+        for (size_t i = 0; i < m.agents.size(); ++i) {
+            w.key(m.agents[i]->name);
+            w.raw(std::to_string(next[i]));
+        }
+        w.end_object();
+    }
+    w.end_object();
+    if (!m.environment.empty()) {
+        w.key("environment");
+        w.begin_object();
+        for (size_t i = 0; i < m.environment.size(); ++i) {
+            const auto& p = m.environment[i];
+            w.key(p.name);
+            write_elements(w, p.type, p.type_size, p.elements, impl->env_host.data() + impl->env_offset[i]);
+        }
+        w.end_object();
+    }
+    w.key("agents");
+    w.begin_object();
+    std::vector<const detail::AgentData*> agents;
+    for (const auto& a : m.agents) agents.push_back(a.get());
+    std::sort(agents.begin(), agents.end(), [](const detail::AgentData* x, const detail::AgentData* y) { return x->name < y->name; });
+    for (const auto* a : agents) {
+        w.key(a->name);
+        w.begin_object();
+        std::vector<size_t> order(a->variables.size());
+        for (size_t v = 0; v < order.size(); ++v) order[v] = v;
+        std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return a->variables[x].name < a->variables[y].name; });
+        for (const auto& st : a->states) {
+            AgentVector pop(AgentDescription(impl->model, const_cast<detail::AgentData*>(a)));
+            getPopulationData(pop, st);
+            if (pop.size() == 0) continue;
+            w.key(st);
+            w.begin_array();
+            for (uint32_t i = 0; i < pop.size(); ++i) {
+                w.begin_object();
+                for (size_t v : order) {
+                    const auto& var = a->variables[v];
+                    w.key(var.name);
+                    write_elements(w, var.type, var.type_size, var.elements,
+                                   pop.columns()[v].data() + static_cast<size_t>(i) * var.bytes());
+                }
+                w.end_object();
+            }
+            w.end_array();
+        }
+        w.end_object();
+    }
+    w.end_object();
+    w.end_object();
+    std::fputc('\n', f);
+    if (std::fclose(f) != 0) THROW exception::InvalidArgument(format("Writing '%s' failed", path.c_str()));
+}
+
+void CUDASimulation::loadState(const std::string& path) {
+    // the reference's JSONStateReader (src/flamegpu/io/JSONStateReader.cu): populations
+    // replace the lists they name, environment properties and the step counter are set
+    std::FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) THROW exception::InvalidArgument(format("Cannot open '%s'", path.c_str()));
+    std::string text;
+    char buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, got);
+    std::fclose(f);
+    detail::json::Value doc;
+    try {
+        doc = detail::json::Parser(text).parse();
+    } catch (const std::exception& e) {
+        THROW exception::InvalidArgument(format("'%s': %s", path.c_str(), e.what()));
+    }
+    auto& m = *impl->model;
+    if (const auto* cfg = doc.find("config")) {
+        if (const auto* sc = cfg->find("simulation")) {
+            if (const auto* v = sc->find("random_seed")) impl->config.random_seed = v->uinteger();
+            if (const auto* v = sc->find("steps")) impl->config.steps = static_cast<unsigned int>(v->uinteger());
+        }
+    }
+    if (const auto* env = doc.find("environment")) {
+        for (const auto& kv : env->fields) {
+            for (size_t i = 0; i < m.environment.size(); ++i) {
+                const auto& p = m.environment[i];
+                if (p.name != kv.first) continue;
+                read_elements(kv.second, p.type, p.type_size, p.elements, impl->env_host.data() + impl->env_offset[i], p.name);
+                impl->env_dirty = true;
+            }
+        }
+    }
+    if (const auto* agents = doc.find("agents")) {
+        for (const auto& ak : agents->fields) {
+            const detail::AgentData* a = nullptr;
+            for (const auto& x : m.agents)
+                if (x->name == ak.first) a = x.get();
+            if (!a) THROW exception::InvalidAgentName(format("State file: the model has no agent '%s'", ak.first.c_str()));
+            for (const auto& sk : ak.second.fields) {
+                const auto& rows = sk.second.items;
+                AgentVector pop(AgentDescription(impl->model, const_cast<detail::AgentData*>(a)),
+                                static_cast<flamegpu::size_type>(rows.size()));
+                for (size_t i = 0; i < rows.size(); ++i)
+                    for (const auto& vk : rows[i].fields) {
+                        const size_t v = pop.columnIndex(vk.first);
+                        const auto& var = a->variables[v];
+                        read_elements(vk.second, var.type, var.type_size, var.elements,
+                                      pop.columns()[v].data() + i * var.bytes(), vk.first);
+                    }
+                setPopulationData(pop, sk.first);
+            }
+        }
+    }
+    if (const auto* stats = doc.find("stats")) {
+        if (const auto* sc = stats->find("step_count")) {
+            FG_CUDA(cudaStreamSynchronize(impl->stream));
+            impl->step_count = static_cast<unsigned int>(sc->uinteger());
+            const uint32_t v = impl->step_count;
+            FG_CUDA(cudaMemcpy(impl->d_step(), &v, sizeof(uint32_t), cudaMemcpyHostToDevice));
+        }
+        if (const auto* ni = stats->find("next_id"))
+            for (const auto& kv : ni->fields)
+                for (size_t i = 0; i < m.agents.size(); ++i)
+                    if (m.agents[i]->name == kv.first) {
+                        uint32_t cur = 1;
+                        FG_CUDA(cudaMemcpy(&cur, impl->d_next_id(i), sizeof(uint32_t), cudaMemcpyDeviceToHost));
+                        const uint32_t want = std::max(cur, static_cast<uint32_t>(kv.second.uinteger()));
+                        FG_CUDA(cudaMemcpy(impl->d_next_id(i), &want, sizeof(uint32_t), cudaMemcpyHostToDevice));
+                    }
+    }
+    impl->upload_env_if_dirty();
+}
 cudaStream_t CUDASimulation::getStream() const { return impl->stream; }
 unsigned long long CUDASimulation::getGraphLaunches() const { return impl->graph_launches; }
 unsigned int CUDASimulation::getKernelsPerStep() const { return impl->kernels_last_step; }

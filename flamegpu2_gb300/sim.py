@@ -22,6 +22,7 @@ SIM_EXPORTS = [
     "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
     "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
     "fgs_set_stage_bytes", "fgs_reset_population_device", "fgs_time_ops_in_graphs", "fgs_harvest_profile",
+    "fgs_export", "fgs_load_state",
 ]
 
 _lock = threading.Lock()
@@ -69,6 +70,8 @@ def core():
             L.fgs_take_profile.argtypes = [vp, C.c_char_p, sz]
             L.fgs_time_ops_in_graphs.argtypes = [vp, i32]
             L.fgs_harvest_profile.argtypes = [vp]
+            L.fgs_export.argtypes = [vp, C.c_char_p]
+            L.fgs_load_state.argtypes = [vp, C.c_char_p]
             _core = L
         if _models is None:
             if not os.path.exists(MODELS_LIB):
@@ -206,6 +209,12 @@ class Simulation:
 
     def profile_ops(self, enable: bool = True):
         _check(core().fgs_profile_ops(self._h, int(enable)))
+
+    def export_data(self, path: str):
+        _check(core().fgs_export(self._h, str(path).encode()))
+
+    def load_state(self, path: str):
+        _check(core().fgs_load_state(self._h, str(path).encode()))
 
     def time_ops_in_graphs(self, enable: bool = True):
         _check(core().fgs_time_ops_in_graphs(self._h, int(enable)))

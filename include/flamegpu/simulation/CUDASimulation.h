@@ -75,6 +75,7 @@ class CUDASimulation {
     struct SimConfig {
         unsigned int steps = 1;
         uint64_t random_seed = 0;
+        std::string input_file;  // state file (JSON) loaded by applyConfig()
         bool verbose = false;
         bool timing = false;
     };
@@ -107,7 +108,17 @@ class CUDASimulation {
 
     SimConfig& SimulationConfig();
     Config& CUDAConfig();
+    /** Applies the configuration; loads SimulationConfig().input_file if set. */
     void applyConfig();
+    /** Simulation::exportData (include/flamegpu/simulation/Simulation.h): writes
+     *  the configuration, step counter, environment and every population to a
+     *  JSON state file in the reference's layout. */
+    void exportData(const std::string& path);
+    /** Reads a JSON state file (the reference's layout): the populations it
+     *  holds replace those lists, environment properties, the step counter and
+     *  the seed/steps configuration it names are set (GB300 extension; the
+     *  reference reads it through SimulationConfig().input_file). */
+    void loadState(const std::string& path);
 
     void setPopulationData(AgentVector& population, const std::string& state = "default");
     void getPopulationData(AgentVector& population, const std::string& state = "default");

@@ -80,6 +80,10 @@ int fgs_time_ops_in_graphs(fgs_sim* sim, int32_t enable);
 /* Adds the operation times of the last replay of each graph replayed since the
  * previous call to the profile read by fgs_take_profile (waits for the stream). */
 int fgs_harvest_profile(fgs_sim* sim);
+/* CUDASimulation::exportData / loadState: JSON state files in the reference's
+ * layout (config, stats.step_count, environment, agents -> state -> rows). */
+int fgs_export(fgs_sim* sim, const char* path);
+int fgs_load_state(fgs_sim* sim, const char* path);
 /* getElapsedTimeSteps (seconds) for up to cap steps; returns the count in *n. */
 int fgs_step_times(fgs_sim* sim, double* out, uint32_t cap, uint32_t* n);
 
