@@ -268,6 +268,84 @@ extern "C" int fgs_harvest_profile(fgs_sim* s) { return guarded([&] { s->sim->ha
 
 extern "C" int fgs_export(fgs_sim* s, const char* path) { return guarded([&] { s->sim->exportData(path); }); }
 
+namespace {
+
+template <typename T>
+void add_reduction(flamegpu::LoggingConfig::AgentLoggingConfig& a, const std::string& op, const std::string& var) {
+    if (op == "mean") a.logMean<T>(var);
+    else if (op == "sd") a.logStandardDev<T>(var);
+    else if (op == "min") a.logMin<T>(var);
+    else if (op == "max") a.logMax<T>(var);
+    else if (op == "sum") a.logSum<T>(var);
+    else throw flamegpu::exception::InvalidArgument("unknown log reduction " + op);
+}
+
+void apply_log_spec(flamegpu::LoggingConfig& cfg, const flamegpu::ModelDescription& model, const std::string& spec) {
+    size_t b = 0;
+    while (b <= spec.size()) {
+        size_t e = spec.find(';', b);
+        if (e == std::string::npos) e = spec.size();
+        const std::string item = spec.substr(b, e - b);
+        b = e + 1;
+        if (item.empty()) continue;
+        std::vector<std::string> f;
+        size_t p = 0;
+        while (true) {
+            const size_t q = item.find(':', p);
+            f.push_back(item.substr(p, q == std::string::npos ? std::string::npos : q - p));
+            if (q == std::string::npos) break;
+            p = q + 1;
+        }
+        if (f[0] == "env" && f.size() == 2) {
+            cfg.logEnvironment(f[1]);
+        } else if (f[0] == "count" && f.size() == 3) {
+            cfg.agent(f[1], f[2]).logCount();
+        } else if (f.size() == 4) {
+            auto a = cfg.agent(f[1], f[2]);
+            const flamegpu::detail::Variable* v = model.getData()->agent(f[1])->find(f[3]);
+            if (!v) throw flamegpu::exception::InvalidAgentVar("no variable " + f[3]);
+            const std::type_index t = v->type;
+            if (t == std::type_index(typeid(float))) add_reduction<float>(a, f[0], f[3]);
+            else if (t == std::type_index(typeid(double))) add_reduction<double>(a, f[0], f[3]);
+            else if (t == std::type_index(typeid(int32_t))) add_reduction<int32_t>(a, f[0], f[3]);
+            else if (t == std::type_index(typeid(uint32_t))) add_reduction<uint32_t>(a, f[0], f[3]);
+            else if (t == std::type_index(typeid(int64_t))) add_reduction<int64_t>(a, f[0], f[3]);
+            else if (t == std::type_index(typeid(uint64_t))) add_reduction<uint64_t>(a, f[0], f[3]);
+            else throw flamegpu::exception::InvalidVarType("unsupported variable type for the C ABI log");
+        } else {
+            throw flamegpu::exception::InvalidArgument("bad log entry '" + item + "'");
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int fgs_set_log(fgs_sim* s, int32_t exit, const char* spec, uint32_t frequency) {
+    return guarded([&] {
+        if (exit) {
+            flamegpu::LoggingConfig cfg(*s->model);
+            apply_log_spec(cfg, *s->model, spec ? spec : "");
+            s->sim->setExitLog(cfg);
+        } else {
+            flamegpu::StepLoggingConfig cfg(*s->model);
+            apply_log_spec(cfg, *s->model, spec ? spec : "");
+            cfg.setFrequency(frequency);
+            s->sim->setStepLog(cfg);
+        }
+    });
+}
+
+extern "C" int fgs_run_log(fgs_sim* s, char* buf, size_t len, size_t* needed) {
+    return guarded([&] {
+        const std::string j = s->sim->runLogJSON();
+        if (needed) *needed = j.size() + 1;
+        if (buf && len) {
+            std::strncpy(buf, j.c_str(), len - 1);
+            buf[len - 1] = 0;
+        }
+    });
+}
+
 extern "C" int fgs_load_state(fgs_sim* s, const char* path) { return guarded([&] { s->sim->loadState(path); }); }
 
 extern "C" int fgs_take_profile(fgs_sim* s, char* buf, size_t len) {

@@ -1147,6 +1147,7 @@ struct SimulationImpl {
             upload_env_if_dirty();
         }
         if (cuda_config.check_each_step) owner->synchronize();
+        owner->processStepLog(-1.0);
     }
 
     // The parity changes a step makes, replayed on the host for a cached graph.
@@ -1262,7 +1263,25 @@ CUDASimulation::CUDASimulation(const ModelDescription& model, int, const char**)
     impl->init();
 }
 
-CUDASimulation::~CUDASimulation() = default;
+CUDASimulation::~CUDASimulation() {
+    if (log_scratch) {
+        cudaStreamSynchronize(impl->stream);
+        cudaFree(log_scratch);
+    }
+}
+
+const std::shared_ptr<detail::ModelData>& CUDASimulation::getModelData() const { return impl->model; }
+
+void CUDASimulation::getEnvironmentRaw(const std::string& name, void* out, size_t bytes) {
+    for (size_t i = 0; i < impl->model->environment.size(); ++i) {
+        const auto& p = impl->model->environment[i];
+        if (p.name != name) continue;
+        if (p.value.size() != bytes) THROW exception::InvalidEnvPropertyType(format("Environment property '%s' has another size", name.c_str()));
+        std::memcpy(out, impl->env_host.data() + impl->env_offset[i], bytes);
+        return;
+    }
+    THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+}
 
 CUDASimulation::SimConfig& CUDASimulation::SimulationConfig() { return impl->config; }
 CUDASimulation::Config& CUDASimulation::CUDAConfig() { return impl->cuda_config; }
@@ -1641,6 +1660,7 @@ void CUDASimulation::simulate() {
         HostAPI api(impl.get());
         for (auto fn : impl->model->init_functions) fn(&api);
     }
+    processStepLog(0.0);  // the frame before the first step (CUDASimulation.cu:1263)
     for (unsigned int s = 0; s < impl->config.steps; ++s) impl->step_once(this);
     if (!impl->model->exit_functions.empty()) {
         FG_CUDA(cudaStreamSynchronize(impl->stream));
@@ -1652,6 +1672,7 @@ void CUDASimulation::simulate() {
     float ms = 0;
     cudaEventElapsedTime(&ms, s0, s1);
     impl->sim_ms = ms;
+    processExitLog(ms / 1000.0);
     cudaEventDestroy(s0);
     cudaEventDestroy(s1);
 }

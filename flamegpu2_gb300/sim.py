@@ -22,7 +22,7 @@ SIM_EXPORTS = [
     "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
     "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
     "fgs_set_stage_bytes", "fgs_reset_population_device", "fgs_time_ops_in_graphs", "fgs_harvest_profile",
-    "fgs_export", "fgs_load_state",
+    "fgs_export", "fgs_load_state", "fgs_set_log", "fgs_run_log",
 ]
 
 _lock = threading.Lock()
@@ -72,6 +72,8 @@ def core():
             L.fgs_harvest_profile.argtypes = [vp]
             L.fgs_export.argtypes = [vp, C.c_char_p]
             L.fgs_load_state.argtypes = [vp, C.c_char_p]
+            L.fgs_set_log.argtypes = [vp, i32, C.c_char_p, u32]
+            L.fgs_run_log.argtypes = [vp, C.c_char_p, sz, C.POINTER(sz)]
             _core = L
         if _models is None:
             if not os.path.exists(MODELS_LIB):
@@ -215,6 +217,21 @@ class Simulation:
 
     def load_state(self, path: str):
         _check(core().fgs_load_state(self._h, str(path).encode()))
+
+    def set_step_log(self, entries, frequency: int = 1):
+        """entries: "count:agent:state", "mean|sd|min|max|sum:agent:state:var", "env:name"."""
+        _check(core().fgs_set_log(self._h, 0, ";".join(entries).encode(), frequency))
+
+    def set_exit_log(self, entries):
+        _check(core().fgs_set_log(self._h, 1, ";".join(entries).encode(), 1))
+
+    def run_log(self) -> dict:
+        import json
+        need = C.c_size_t()
+        _check(core().fgs_run_log(self._h, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value)
+        _check(core().fgs_run_log(self._h, buf, need.value, C.byref(need)))
+        return json.loads(buf.value.decode())
 
     def time_ops_in_graphs(self, enable: bool = True):
         _check(core().fgs_time_ops_in_graphs(self._h, int(enable)))

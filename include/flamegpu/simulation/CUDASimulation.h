@@ -16,6 +16,7 @@
 
 #include "flamegpu/model/ModelDescription.h"
 #include "flamegpu/simulation/AgentVector.h"
+#include "flamegpu/simulation/LoggingConfig.h"
 
 namespace flamegpu {
 
@@ -185,10 +186,32 @@ class CUDASimulation {
      *  previous call to the profile that takeOperationProfile() returns. */
     void harvestOperationTimes();
 
+    /** CUDASimulation::setStepLog / setExitLog / getRunLog (include/flamegpu/simulation/Simulation.h,
+     *  CUDASimulation.cu:1949-2022): environment properties, agent counts and
+     *  variable reductions logged every `frequency` steps (and once before the
+     *  first step of simulate()) and at the end of simulate(). */
+    void setStepLog(const StepLoggingConfig& cfg);
+    void setExitLog(const LoggingConfig& cfg);
+    const RunLog& getRunLog() const { return run_log; }
+    /** The run log in the layout of the reference's JSONLogger
+     *  (src/flamegpu/io/JSONLogger.cu:80-200): config, steps, exit. */
+    std::string runLogJSON() const;
+    /** Raw bytes of an environment property (GB300 extension). */
+    void getEnvironmentRaw(const std::string& name, void* out, size_t bytes);
+    /** Logs the frame of the step just completed when it is due (called by the step). */
+    void processStepLog(double step_seconds);
+    /** Logs the exit frame (called at the end of simulate()). */
+    void processExitLog(double total_seconds);
+
     detail::SimulationImpl* getImpl() const { return impl.get(); }
+    const std::shared_ptr<detail::ModelData>& getModelData() const;
 
  private:
     std::unique_ptr<detail::SimulationImpl> impl;
+    std::unique_ptr<StepLoggingConfig> step_log;
+    std::unique_ptr<LoggingConfig> exit_log;
+    RunLog run_log;
+    char* log_scratch = nullptr;  // device buffer of the log reductions
 };
 
 }  // namespace flamegpu

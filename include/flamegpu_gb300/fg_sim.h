@@ -84,6 +84,13 @@ int fgs_harvest_profile(fgs_sim* sim);
  * layout (config, stats.step_count, environment, agents -> state -> rows). */
 int fgs_export(fgs_sim* sim, const char* path);
 int fgs_load_state(fgs_sim* sim, const char* path);
+/* Step (exit == 0) or exit (exit != 0) log configuration
+ * (CUDASimulation::setStepLog / setExitLog). spec lists entries separated by
+ * ';': "count:agent:state", "mean|sd|min|max|sum:agent:state:variable" (the
+ * variable's own type), "env:property". frequency applies to the step log. */
+int fgs_set_log(fgs_sim* sim, int32_t exit, const char* spec, uint32_t frequency);
+/* The run log as JSON (CUDASimulation::runLogJSON); *needed receives its size + 1. */
+int fgs_run_log(fgs_sim* sim, char* buf, size_t len, size_t* needed);
 /* getElapsedTimeSteps (seconds) for up to cap steps; returns the count in *n. */
 int fgs_step_times(fgs_sim* sim, double* out, uint32_t cap, uint32_t* n);
 
