@@ -75,7 +75,7 @@ __device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, u
 }
 
 template <typename F>
-__global__ void __launch_bounds__(kAgentBlock) agent_function_kernel(const __grid_constant__ LaunchParams P) {
+__global__ void __launch_bounds__(kAgentBlock, 8) agent_function_kernel(const __grid_constant__ LaunchParams P) {
     using MsgIn = typename F::MessageIn;
     using MsgOut = typename F::MessageOut;
     // rows to visit: the population (single) or every row of the batch
