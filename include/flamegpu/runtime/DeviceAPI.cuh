@@ -484,8 +484,13 @@ class RecordView {
  * WrapFilter: 3^DIMS single bins, x offset outer, then y, z offset inner
  * (nextCell, MessageSpatial3DDevice.cuh:264-276), every axis taken modulo
  * gridDim (:727-749); no radius test — user code filters.
- * Both iterators load the PBM bounds of the next strip or cell while the
- * current one is being read, so that load's latency is hidden.
+ * Both iterators first read the PBM bounds of all their strips or cells in
+ * lock step (unrolled, so every hash is a sum of registers) and keep one bit
+ * per non-empty one; they then visit only those, in order, loading the next
+ * one's bounds while the current one is being read. A lane whose strip or
+ * cell ends thus moves to the next non-empty one in one step, so the lanes of
+ * a warp advance at most once per message visited instead of each stepping
+ * through empty cells on its own (in sparse neighbourhoods most are empty).
  * A cell lies wholly inside or wholly outside the block's staged window, so
  * within a cell the record address just advances by one record.
  */
@@ -535,18 +540,23 @@ class SpatialIn {
         };
         class iterator {
          public:
-            __device__ iterator(const Filter& f, int strip) : F(f), s(strip), m(f.P, 0), end_(0) {
-                if (s < kStrips) {
-                    --s;
-                    advance();
+            __device__ iterator(const Filter& f, bool at_end) : F(f), m(f.P, 0), end_(0) {
+                if (at_end) return;
+#pragma unroll
+                for (int t = 0; t < kStrips; ++t) {
+                    uint32_t b, e;
+                    bounds(t, b, e);
+                    todo_ |= (b < e ? 1u : 0u) << t;
                 }
+                prefetch();
+                advance();
             }
             __device__ iterator& operator++() {
                 m.row += F.P.in_record_bytes;
                 if (++m.index >= end_) advance();
                 return *this;
             }
-            __device__ bool operator!=(const iterator&) const { return s < kStrips; }
+            __device__ bool operator!=(const iterator&) const { return m.index < end_; }
             __device__ bool operator==(const iterator& o) const { return !(*this != o); }
             __device__ const Message& operator*() const { return m; }
             __device__ const Message* operator->() const { return &m; }
@@ -555,7 +565,6 @@ class SpatialIn {
             // PBM bounds of strip t (empty when the strip lies outside the grid)
             __device__ void bounds(int t, uint32_t& b, uint32_t& e) const {
                 b = e = 0;
-                if (t >= kStrips) return;
                 const int ry = DIMS == 3 ? t / 3 - 1 : t - 1;
                 const int rz = DIMS == 3 ? t % 3 - 1 : 0;
                 const int ay = F.cell[1] + ry, az = F.cell[2] + rz;
@@ -567,24 +576,27 @@ class SpatialIn {
                 b = F.win.pbm_at(F.P, h0);
                 e = F.win.pbm_at(F.P, h1 + 1);
             }
-            __device__ void advance() {
-                if (s < 0) bounds(0, nb_, ne_);
-                while (++s < kStrips) {
-                    const uint32_t b = nb_, e = ne_;
-                    bounds(s + 1, nb_, ne_);  // in flight while strip s is read
-                    if (b < e) {
-                        m.index = b;
-                        m.row = F.win.row(F.P, b);
-                        end_ = e;
-                        return;
-                    }
+            // bounds of the next non-empty strip (an empty pair when none is left)
+            __device__ void prefetch() {
+                nb_ = ne_ = 0;
+                if (todo_) {
+                    const int t = __ffs(todo_) - 1;
+                    todo_ &= todo_ - 1u;
+                    bounds(t, nb_, ne_);
                 }
             }
+            // enter the prefetched strip (index == end ends the loop)
+            __device__ void advance() {
+                m.index = nb_;
+                m.row = F.win.row(F.P, nb_);
+                end_ = ne_;
+                prefetch();  // in flight while this strip is read
+            }
             const Filter& F;
-            int s;
             Message m;
             uint32_t end_;
-            uint32_t nb_ = 0, ne_ = 0;  // bounds of strip s + 1
+            uint32_t todo_ = 0;         // non-empty strips not yet entered
+            uint32_t nb_ = 0, ne_ = 0;  // bounds of the next one
         };
         __device__ Filter(const detail::LaunchParams& p, float x, float y, float z) : P(p) {
             loc[0] = x;
@@ -596,8 +608,8 @@ class SpatialIn {
             cell[2] = DIMS == 3 ? detail::grid_cell(gc, 2, z) : 0;
             win.load(p);
         }
-        __device__ iterator begin() const { return iterator(*this, 0); }
-        __device__ iterator end() const { return iterator(*this, kStrips); }
+        __device__ iterator begin() const { return iterator(*this, false); }
+        __device__ iterator end() const { return iterator(*this, true); }
 
         const detail::LaunchParams& P;
         float loc[3];
@@ -629,55 +641,57 @@ class SpatialIn {
         };
         class iterator {
          public:
-            __device__ iterator(const WrapFilter& f, int cell) : F(f), c(cell), m(f.P, 0, &f), end_(0) {
-                if (c < kCells) {
-                    --c;
-                    advance();
+            __device__ iterator(const WrapFilter& f, bool at_end) : F(f), m(f.P, 0, &f), end_(0) {
+                if (at_end) return;
+#pragma unroll
+                for (int t = 0; t < kCells; ++t) {
+                    const uint32_t h = hash(t);
+                    todo_ |= (F.win.pbm_at(F.P, h) < F.win.pbm_at(F.P, h + 1) ? 1u : 0u) << t;
                 }
+                prefetch();
+                advance();
             }
             __device__ iterator& operator++() {
                 m.row += F.P.in_record_bytes;
                 if (++m.index >= end_) advance();
                 return *this;
             }
-            __device__ bool operator!=(const iterator&) const { return c < kCells; }
+            __device__ bool operator!=(const iterator&) const { return m.index < end_; }
             __device__ bool operator==(const iterator& o) const { return !(*this != o); }
             __device__ const Message& operator*() const { return m; }
             __device__ const Message* operator->() const { return &m; }
 
          private:
-            // PBM bounds of cell t of the visit order (x offset outer, z inner)
-            __device__ void bounds(int t, uint32_t& b, uint32_t& e) const {
-                b = e = 0;
-                if (t >= kCells) return;
-                uint32_t h;
-                if (DIMS == 3) {
-                    h = pick(t / 9, F.hx0, F.hx1, F.hx2) + pick((t / 3) % 3, F.hy0, F.hy1, F.hy2) +
-                        pick(t % 3, F.hz0, F.hz1, F.hz2);
-                } else {
-                    h = pick(t / 3, F.hx0, F.hx1, F.hx2) + pick(t % 3, F.hy0, F.hy1, F.hy2);
-                }
-                b = F.win.pbm_at(F.P, h);
-                e = F.win.pbm_at(F.P, h + 1);
+            // hash of cell t of the visit order (x offset outer, z inner)
+            __device__ uint32_t hash(int t) const {
+                if (DIMS == 3)
+                    return pick(t / 9, F.hx0, F.hx1, F.hx2) + pick((t / 3) % 3, F.hy0, F.hy1, F.hy2) +
+                           pick(t % 3, F.hz0, F.hz1, F.hz2);
+                return pick(t / 3, F.hx0, F.hx1, F.hx2) + pick(t % 3, F.hy0, F.hy1, F.hy2);
             }
-            __device__ void advance() {
-                if (c < 0) bounds(0, nb_, ne_);
-                while (++c < kCells) {
-                    const uint32_t b = nb_, e = ne_;
-                    bounds(c + 1, nb_, ne_);  // in flight while cell c is read
-                    if (b < e) {
-                        m.index = b;
-                        m.row = F.win.row(F.P, b);
-                        end_ = e;
-                        return;
-                    }
+            // bounds of the next non-empty cell (an empty pair when none is left)
+            __device__ void prefetch() {
+                nb_ = ne_ = 0;
+                if (todo_) {
+                    const int t = __ffs(todo_) - 1;
+                    todo_ &= todo_ - 1u;
+                    const uint32_t h = hash(t);
+                    nb_ = F.win.pbm_at(F.P, h);
+                    ne_ = F.win.pbm_at(F.P, h + 1);
                 }
+            }
+            // enter the prefetched cell (index == end ends the loop)
+            __device__ void advance() {
+                m.index = nb_;
+                m.row = F.win.row(F.P, nb_);
+                end_ = ne_;
+                prefetch();  // in flight while this cell is read
             }
             const WrapFilter& F;
-            int c;
             Message m;
             uint32_t end_;
-            uint32_t nb_ = 0, ne_ = 0;  // bounds of cell c + 1
+            uint32_t todo_ = 0;         // non-empty cells not yet entered
+            uint32_t nb_ = 0, ne_ = 0;  // bounds of the next one
         };
         __device__ WrapFilter(const detail::LaunchParams& p, float x, float y, float z) : P(p) {
             loc[0] = x;
@@ -709,8 +723,8 @@ class SpatialIn {
             }
             win.load(p);
         }
-        __device__ iterator begin() const { return iterator(*this, 0); }
-        __device__ iterator end() const { return iterator(*this, kCells); }
+        __device__ iterator begin() const { return iterator(*this, false); }
+        __device__ iterator end() const { return iterator(*this, true); }
 
         const detail::LaunchParams& P;
         float loc[3];
