@@ -5,9 +5,20 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
+#include "flamegpu/detail/launch.cuh"
 #include "flamegpu_gb300/fg_capi.h"
 
 namespace fgk {
+
+// A launch of one of these kernels with no dynamic shared memory, programmatic
+// dependency included (flamegpu/detail/launch.cuh).
+template <typename... KernelArgs, typename... Args>
+inline cudaError_t launch(void (*kernel)(KernelArgs...), dim3 grid, dim3 block, cudaStream_t st, Args&&... args) {
+    return flamegpu::detail::launch_kernel(flamegpu::detail::pdl_enabled(), kernel, grid, block, 0, st,
+                                           std::forward<Args>(args)...);
+}
 
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr int kThreads = 256;

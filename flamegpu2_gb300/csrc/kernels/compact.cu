@@ -89,6 +89,7 @@ __device__ __forceinline__ void copy_col(const fg_column& c, uint32_t src, uint3
 
 __global__ void __launch_bounds__(kThreads) k_count_alive(uint32_t max_n, const uint32_t* d_n,
                                                           const uint32_t* __restrict__ alive, WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     const uint32_t n = d_n ? min(*d_n, max_n) : max_n;
     uint32_t c = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -98,6 +99,7 @@ __global__ void __launch_bounds__(kThreads) k_count_alive(uint32_t max_n, const 
 }
 
 __global__ void k_set_alive_total(uint32_t max_n, const uint32_t* d_n, WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     h->alive_total = d_n ? min(*d_n, max_n) : max_n;
 }
 
@@ -107,6 +109,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
                                                       const uint32_t* d_alive_total, uint32_t* d_n_out,
                                                       uint32_t out_capacity, uint64_t* status0, uint32_t stride_tiles,
                                                       WsHeader* h, int partition, uint32_t* d_s_out) {
+    flamegpu::detail::grid_dependency_enter();
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_cnt_a[kCompItems][kThreads / 32];
     __shared__ uint32_t s_cnt_b[kCompItems][kThreads / 32];
@@ -266,10 +269,10 @@ extern "C" int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const uint32_t grid = std::max(1u, std::min((max_n + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
-        k_count_alive<<<grid, kThreads, 0, st>>>(max_n, d_n, alive, h);
+        launch(k_count_alive, grid, kThreads, st, max_n, d_n, alive, h);
     } else if (!d_alive_total) {
         // every agent survives: S = n
-        k_set_alive_total<<<1, 1, 0, st>>>(max_n, d_n, h);
+        launch(k_set_alive_total, 1, 1, st, max_n, d_n, h);
     }
     CompactParams cp{};
     for (uint32_t c = 0; c < ncols; ++c) {
@@ -281,8 +284,8 @@ extern "C" int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint
     // both status arrays are strided by the workspace's tile capacity, so a
     // workspace keeps working when max_n changes between calls
     const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
-    k_compact<<<tiles, kThreads, 0, st>>>(cp, max_n, d_n, alive, born, d_next_id, d_alive_total, d_n_out,
-                                          out_capacity, status, stride_tiles, h, 0, nullptr);
+    launch(k_compact, tiles, kThreads, st, cp, max_n, d_n, alive, born, d_next_id, d_alive_total, d_n_out, out_capacity,
+           status, stride_tiles, h, 0, nullptr);
     return launch_err();
 }
 
@@ -304,14 +307,14 @@ extern "C" int fg_partition_agents(uint32_t max_n, const uint32_t* d_n, const ui
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t grid = std::max(1u, std::min((max_n + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
-    k_count_alive<<<grid, kThreads, 0, st>>>(max_n, d_n, first_group, h);
+    launch(k_count_alive, grid, kThreads, st, max_n, d_n, first_group, h);
     CompactParams cp{};
     for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cp.bcol[c] = cols[c];
     cp.ncols = ncols;
     cp.id_col = -1;
     const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
-    k_compact<<<comp_tiles(max_n), kThreads, 0, st>>>(cp, max_n, d_n, first_group, nullptr, nullptr, nullptr, nullptr,
-                                                     max_n, status, stride_tiles, h, 1, d_first_count);
+    launch(k_compact, comp_tiles(max_n), kThreads, st, cp, max_n, d_n, first_group, nullptr, nullptr, nullptr, nullptr,
+           max_n, status, stride_tiles, h, 1, d_first_count);
     return launch_err();
 }
 
@@ -322,6 +325,7 @@ __global__ void __launch_bounds__(kThreads) k_append_rows(const __grid_constant_
                                                           const uint32_t* d_begin, const uint32_t* d_end,
                                                           const uint32_t* d_dst_count, uint32_t dst_capacity,
                                                           WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     const uint32_t begin = d_begin ? *d_begin : 0u;
     const uint32_t end = min(*d_end, max_rows);
     const uint32_t dst0 = *d_dst_count;
@@ -337,6 +341,7 @@ __global__ void __launch_bounds__(kThreads) k_append_rows(const __grid_constant_
 
 __global__ void k_append_counts(uint32_t max_rows, const uint32_t* d_begin, uint32_t* d_src_count,
                                 uint32_t* d_dst_count, uint32_t dst_capacity) {
+    flamegpu::detail::grid_dependency_enter();
     const uint32_t begin = d_begin ? *d_begin : 0u;
     const uint32_t end = min(*d_src_count, max_rows);
     const uint32_t moved = end > begin ? end - begin : 0u;
@@ -363,7 +368,7 @@ extern "C" int fg_append_rows(const fg_column* cols, uint32_t ncols, uint32_t ma
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t grid = std::max(1u, std::min((max_rows + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
-    k_append_rows<<<grid, kThreads, 0, st>>>(cp, max_rows, d_begin, d_src_count, d_dst_count, dst_capacity, h);
-    k_append_counts<<<1, 1, 0, st>>>(max_rows, d_begin, d_src_count, d_dst_count, dst_capacity);
+    launch(k_append_rows, grid, kThreads, st, cp, max_rows, d_begin, d_src_count, d_dst_count, dst_capacity, h);
+    launch(k_append_counts, 1, 1, st, max_rows, d_begin, d_src_count, d_dst_count, dst_capacity);
     return launch_err();
 }

@@ -101,6 +101,7 @@ __device__ __forceinline__ uint32_t lookback_u32(const uint64_t* status, uint32_
 // kThreads threads.
 __global__ void __launch_bounds__(kThreads) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
                                                        uint64_t* status, WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_excl;

@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
                                                   const float* __restrict__ z, const uint32_t* __restrict__ valid,
                                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
                                                   uint32_t* hist, WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) h->long_count = 0;
     const uint32_t n = load_count(d_n, max_n);
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -135,6 +136,7 @@ __global__ void __launch_bounds__(kThreads) k_bin_batched(const fg_batch_instanc
                                                           const uint32_t* __restrict__ valid,
                                                           uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
                                                           uint32_t* hist, WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) h->long_count = 0;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total_rows; base += stride) {
@@ -179,6 +181,7 @@ __global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_
                                                    const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
                                                    const uint32_t* __restrict__ pbm, uint32_t* __restrict__ perm,
                                                    WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     const uint32_t n = load_count(d_n, max_n);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t k = keys[i];
@@ -268,6 +271,7 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
                                                         const uint32_t* __restrict__ pbm,
                                                         const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                         uint2* chunk_list, uint32_t chunk_cap, WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     const uint32_t total = pbm[nbuckets];
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
         const uint32_t i = perm[p];
@@ -314,6 +318,7 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
                                                    const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                    const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
                                                    const WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
     __shared__ uint32_t s_idx[kSortCap];
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_lo, s_hi;
@@ -577,16 +582,16 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     uint2* chunks = reinterpret_cast<uint2*>(ws + L.chunks);
     const uint32_t grid = grid_for(max_n);
     if (batch.inst)
-        k_bin_batched<MODE><<<grid, kThreads, 0, st>>>(batch.inst, batch.counts, batch.ninst, max_n, batch.dims, x, y, z,
-                                                      valid, keys, slot, hist, h);
+        launch(k_bin_batched<MODE>, grid, kThreads, st, batch.inst, batch.counts, batch.ninst, max_n, batch.dims, x, y, z,
+               valid, keys, slot, hist, h);
     else
-        k_bin<MODE><<<grid, kThreads, 0, st>>>(*g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
+        launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
     const uint32_t scan_n = nbuckets + 1;
-    k_scan_u32<<<scan_tiles(scan_n), kThreads, 0, st>>>(hist, pbm_out, scan_n, 1, sstat, h);
-    k_perm<<<grid, kThreads, 0, st>>>(max_n, d_n, keys, slot, pbm_out, perm, h);
-    k_stabilize<EMIT><<<grid, kThreads, 0, st>>>(rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
-    k_long<EMIT><<<static_cast<uint32_t>(sm_count() * 4), kThreads, 0, st>>>(rp, pbm_out, perm, sperm, chunks,
-                                                                              L.chunk_cap, h);
+    launch(k_scan_u32, scan_tiles(scan_n), kThreads, st, hist, pbm_out, scan_n, 1, sstat, h);
+    launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
+    launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
+    launch(k_long<EMIT>, static_cast<uint32_t>(sm_count() * 4), kThreads, st, rp, pbm_out, perm, sperm, chunks,
+           L.chunk_cap, h);
     return check_launch();
 }
 
@@ -650,8 +655,8 @@ extern "C" int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t
         return FG_ERR_WORKSPACE;
     if (!n) return FG_OK;
     char* ws = static_cast<char*>(workspace);
-    k_scan_u32<<<scan_tiles(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-        in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
+    launch(k_scan_u32, scan_tiles(n), kThreads, static_cast<cudaStream_t>(stream), in, out, n, 0,
+           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
     return check_launch();
 }
 
@@ -714,8 +719,8 @@ extern "C" int fg_exclusive_scan_u32_noalloc(const uint32_t* in, uint32_t* out, 
     const int rc = noalloc_scratch(&ws);
     if (rc != FG_OK) return rc;
     if (!n) return FG_OK;
-    k_scan_u32<<<scan_tiles(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-        in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
+    launch(k_scan_u32, scan_tiles(n), kThreads, static_cast<cudaStream_t>(stream), in, out, n, 0,
+           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
     return check_launch();
 }
 

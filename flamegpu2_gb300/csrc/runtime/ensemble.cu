@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "flamegpu/simulation/CUDAEnsemble.h"
+#include "flamegpu/detail/launch.cuh"
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu_gb300/fg_capi.h"
 #include "runtime/internal.h"
@@ -89,7 +90,10 @@ namespace detail {
 
 namespace {
 
-__global__ void k_batch_step_increment(uint32_t* d_step) { *d_step += 1; }
+__global__ void k_batch_step_increment(uint32_t* d_step) {
+    grid_dependency_enter();
+    *d_step += 1;
+}
 
 constexpr uint32_t kRowAlign = kAgentBlock;
 
@@ -482,7 +486,7 @@ struct BatchedSim {
         P.batch_counts = d_counts;
         P.batch_n = ninst;
         const uint32_t grid = std::min(total_rows / kAgentBlock, static_cast<uint32_t>(sms * 16));
-        const cudaError_t e = b.fn->launcher(P, std::max(1u, grid), kAgentBlock, smem, stream);
+        const cudaError_t e = b.fn->launcher(P, std::max(1u, grid), kAgentBlock, smem, stream, detail::pdl_enabled());
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", b.fn->name.c_str(), cudaGetErrorString(e)));
         kernels_per_step += 1;
@@ -515,7 +519,7 @@ struct BatchedSim {
                     launch_fn(b);
                     if (b.out) b.out->needs_build = true;
                 }
-        k_batch_step_increment<<<1, 1, 0, stream>>>(d_misc);
+        launch_kernel(pdl_enabled(), k_batch_step_increment, 1, 1, 0, stream, d_misc);
         kernels_per_step += 1;
     }
 

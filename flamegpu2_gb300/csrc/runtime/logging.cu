@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <type_traits>
 
+#include "flamegpu/detail/launch.cuh"
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu/simulation/LoggingConfig.h"
 
@@ -96,6 +97,7 @@ __device__ Partial block_combine(Partial p) {
 template <typename T>
 __global__ void __launch_bounds__(kLogThreads) k_log_partials(const T* __restrict__ col, const uint32_t* d_n,
                                                               const double* mean, int pass, Partial* out) {
+    grid_dependency_enter();
     const uint32_t n = *d_n;
     Partial p = identity();
     const double m = pass ? *mean : 0.0;
@@ -116,6 +118,7 @@ __global__ void __launch_bounds__(kLogThreads) k_log_partials(const T* __restric
 template <typename T>
 __global__ void __launch_bounds__(kLogThreads) k_log_final(const Partial* __restrict__ parts, const uint32_t* d_n,
                                                            int pass, Partial* result, double* mean) {
+    grid_dependency_enter();
     Partial p = identity();
     for (int b = threadIdx.x; b < kLogBlocks; b += blockDim.x) combine(p, parts[b]);
     p = block_combine(p);
@@ -148,11 +151,13 @@ void reduce_typed(const void* col, const uint32_t* d_n, const std::vector<Loggin
     double* mean = reinterpret_cast<double*>(result + 2);
     bool need_sd = false;
     for (auto r : want) need_sd = need_sd || r == LoggingConfig::StandardDev;
-    k_log_partials<T><<<kLogBlocks, kLogThreads, 0, st>>>(static_cast<const T*>(col), d_n, mean, 0, parts);
-    k_log_final<T><<<1, kLogThreads, 0, st>>>(parts, d_n, 0, result, mean);
+    launch_kernel(pdl_enabled(), k_log_partials<T>, kLogBlocks, kLogThreads, 0, st, static_cast<const T*>(col), d_n,
+                  mean, 0, parts);
+    launch_kernel(pdl_enabled(), k_log_final<T>, 1, kLogThreads, 0, st, parts, d_n, 0, result, mean);
     if (need_sd) {
-        k_log_partials<T><<<kLogBlocks, kLogThreads, 0, st>>>(static_cast<const T*>(col), d_n, mean, 1, parts);
-        k_log_final<T><<<1, kLogThreads, 0, st>>>(parts, d_n, 1, result, mean);
+        launch_kernel(pdl_enabled(), k_log_partials<T>, kLogBlocks, kLogThreads, 0, st, static_cast<const T*>(col),
+                      d_n, mean, 1, parts);
+        launch_kernel(pdl_enabled(), k_log_final<T>, 1, kLogThreads, 0, st, parts, d_n, 1, result, mean);
     }
     Partial res[2];
     double m = 0.0;

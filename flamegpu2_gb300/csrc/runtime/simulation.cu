@@ -29,6 +29,7 @@
 #include <tuple>
 #include <vector>
 
+#include "flamegpu/detail/launch.cuh"
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu_gb300/fg_capi.h"
 #include "runtime/internal.h"
@@ -54,9 +55,18 @@ using exception::format;
 
 namespace {
 
-__global__ void k_step_increment(uint32_t* d_step) { *d_step += 1; }
-__global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
-__global__ void k_max_u32(uint32_t* p, uint32_t v) { *p = *p > v ? *p : v; }
+__global__ void k_step_increment(uint32_t* d_step) {
+    grid_dependency_enter();
+    *d_step += 1;
+}
+__global__ void k_set_u32(uint32_t* p, uint32_t v) {
+    grid_dependency_enter();
+    *p = v;
+}
+__global__ void k_max_u32(uint32_t* p, uint32_t v) {
+    grid_dependency_enter();
+    *p = *p > v ? *p : v;
+}
 
 // Device buffers of one simulation, taken stream-ordered from the device's
 // default memory pool: a finished simulation returns its memory without
@@ -925,7 +935,8 @@ struct SimulationImpl {
             C.env = d_env;
             cudaError_t ce = cudaSuccess;
             timed("cond:" + f.fn->name, [&] {
-                ce = f.fn->condition(C, grid_for(l.capacity + 1, kAgentBlock, 1 << 16), kAgentBlock, 0, stream);
+                ce = f.fn->condition(C, grid_for(l.capacity + 1, kAgentBlock, 1 << 16), kAgentBlock, 0, stream,
+                                     detail::pdl_enabled());
             });
             if (ce != cudaSuccess)
                 THROW exception::CUDAError(format("Launch of the condition of '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(ce)));
@@ -979,7 +990,10 @@ struct SimulationImpl {
         // one block per 128 rows (no grid-stride reuse): blocks stay short, so
         // kernels of other simulations on the device (a server's other runs,
         // higher-priority streams) get SMs between them
-        timed("fn:" + f.fn->name, [&] { e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 1 << 16), kAgentBlock, smem, stream); });
+        timed("fn:" + f.fn->name, [&] {
+            e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 1 << 16), kAgentBlock, smem, stream,
+                               detail::pdl_enabled());
+        });
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(e)));
         kernel_counter += 1;
@@ -1048,7 +1062,7 @@ struct SimulationImpl {
                 FG_CUDA(cudaMemsetAsync(m->d_count, 0, sizeof(uint32_t), stream));
                 if (m->bf_count) FG_CUDA(cudaMemsetAsync(m->bf_count, 0, sizeof(uint32_t), stream));
             }
-        k_step_increment<<<1, 1, 0, stream>>>(d_step());
+        launch_kernel(pdl_enabled(), k_step_increment, 1, 1, 0, stream, d_step());
         kernel_counter += 1;
     }
 
@@ -1101,7 +1115,7 @@ struct SimulationImpl {
                     FG_CUDA(cudaMemsetAsync(m->d_count, 0, sizeof(uint32_t), stream));
                     if (m->bf_count) FG_CUDA(cudaMemsetAsync(m->bf_count, 0, sizeof(uint32_t), stream));
                 }
-            k_step_increment<<<1, 1, 0, stream>>>(d_step());
+            launch_kernel(pdl_enabled(), k_step_increment, 1, 1, 0, stream, d_step());
             kernels_last_step = kernel_counter + 1;
         } else {
             const std::vector<int> key = step_key();
@@ -1609,7 +1623,8 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
         if (n) FG_CUDA(cudaMemcpyAsync(l->cols[v][l->parity], src[v], b * n, cudaMemcpyHostToDevice, impl->stream));
     }
     // next id: the larger of the device's and one past the largest given
-    detail::k_max_u32<<<1, 1, 0, impl->stream>>>(impl->d_next_id(impl->agent_index(l->agent)), mx + 1);
+    detail::launch_kernel(detail::pdl_enabled(), detail::k_max_u32, 1, 1, 0, impl->stream,
+                         impl->d_next_id(impl->agent_index(l->agent)), mx + 1);
     impl->h_pinned[2] = n;
     FG_CUDA(cudaMemcpyAsync(l->d_count, impl->h_pinned + 2, sizeof(uint32_t), cudaMemcpyHostToDevice, impl->stream));
     FG_CUDA(cudaStreamSynchronize(impl->stream));

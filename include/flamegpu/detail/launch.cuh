@@ -1,0 +1,66 @@
+#ifndef INCLUDE_FLAMEGPU_DETAIL_LAUNCH_CUH_
+#define INCLUDE_FLAMEGPU_DETAIL_LAUNCH_CUH_
+// Kernel launches with programmatic dependent launch (PDL).
+//
+// A step is a chain of short dependent kernels; at small populations each one
+// costs more in launch and drain latency than in work. A launch carrying
+// cudaLaunchAttributeProgrammaticStreamSerialization (captured into a step
+// graph as a programmatic edge) is launched as soon as every block of the
+// kernel before it has exited, so its launch overlaps that kernel's drain and
+// memory flush. Every kernel of this project therefore begins with
+// grid_dependency_enter(), which waits until the grids it depends on have
+// completed and their writes are visible (griddepcontrol.wait, a no-op for a
+// launch without such a dependency). Because every kernel waits before it
+// reads or writes anything, no kernel completes before its predecessors, so
+// completion stays transitive along a chain of programmatic edges and results
+// are those of plain stream order.
+//
+// No kernel triggers its dependents early (griddepcontrol.launch_dependents):
+// measured on the two-branch Boids step at 1M agents, an early trigger let the
+// next kernel's blocks occupy SMs, waiting, while the other branch still had
+// work, and the step took 10% longer; at exit, the step is as fast as without
+// PDL there and faster at small populations.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <utility>
+
+namespace flamegpu {
+namespace detail {
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void grid_dependency_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+#endif
+
+/** Whether launches carry the programmatic dependency: on unless the
+ *  environment sets FLAMEGPU_PDL=0 (read once per process). */
+inline bool pdl_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("FLAMEGPU_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+/** Launch `kernel` on `stream`, with a programmatic dependency on the
+ *  stream's previous kernel when `pdl` is set. */
+template <typename... KernelArgs, typename... Args>
+inline cudaError_t launch_kernel(bool pdl, void (*kernel)(KernelArgs...), dim3 grid, dim3 block, size_t smem,
+                                 cudaStream_t stream, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1u : 0u;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+}  // namespace detail
+}  // namespace flamegpu
+
+#endif  // INCLUDE_FLAMEGPU_DETAIL_LAUNCH_CUH_

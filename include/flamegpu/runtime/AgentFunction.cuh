@@ -18,6 +18,7 @@
 #include <typeindex>
 #include <typeinfo>
 
+#include "flamegpu/detail/launch.cuh"
 #include "flamegpu/runtime/DeviceAPI.cuh"
 
 namespace flamegpu {
@@ -25,7 +26,7 @@ namespace detail {
 
 /** Launches the agent function kernel of one FLAMEGPU_AGENT_FUNCTION. */
 typedef cudaError_t (*AgentFunctionLauncher)(const LaunchParams& p, unsigned int grid, unsigned int block,
-                                             unsigned int smem, cudaStream_t stream);
+                                             unsigned int smem, cudaStream_t stream, bool pdl);
 
 constexpr unsigned int kAgentBlock = 128;
 
@@ -76,6 +77,7 @@ __device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, u
 
 template <typename F>
 __global__ void __launch_bounds__(kAgentBlock, 8) agent_function_kernel(const __grid_constant__ LaunchParams P) {
+    grid_dependency_enter();
     using MsgIn = typename F::MessageIn;
     using MsgOut = typename F::MessageOut;
     // rows to visit: the population (single) or every row of the batch
@@ -129,6 +131,7 @@ __global__ void __launch_bounds__(kAgentBlock, 8) agent_function_kernel(const __
 // max_n + 1 flags then counts and places the failing agents).
 template <typename C>
 __global__ void __launch_bounds__(kAgentBlock) agent_condition_kernel(const __grid_constant__ LaunchParams P) {
+    grid_dependency_enter();
     const uint32_t n = P.d_n ? min(*P.d_n, P.max_n) : P.max_n;
     fill_ctx(P, 0, n);
     __syncthreads();
@@ -144,14 +147,13 @@ __global__ void __launch_bounds__(kAgentBlock) agent_condition_kernel(const __gr
 
 template <typename C>
 cudaError_t launch_agent_condition(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int,
-                                   cudaStream_t stream) {
-    agent_condition_kernel<C><<<grid, block, 0, stream>>>(p);
-    return cudaGetLastError();
+                                   cudaStream_t stream, bool pdl) {
+    return launch_kernel(pdl, agent_condition_kernel<C>, grid, block, 0, stream, p);
 }
 
 template <typename F>
 cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int smem,
-                                  cudaStream_t stream) {
+                                  cudaStream_t stream, bool pdl) {
     static unsigned int configured = 48u * 1024u;
     if (smem > configured) {
         const cudaError_t e = cudaFuncSetAttribute(agent_function_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -159,8 +161,7 @@ cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsi
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    agent_function_kernel<F><<<grid, block, smem, stream>>>(p);
-    return cudaGetLastError();
+    return launch_kernel(pdl, agent_function_kernel<F>, grid, block, smem, stream, p);
 }
 #endif
 

@@ -248,3 +248,20 @@ def test_population_direct_columns_match_agent_vector_path():
     for k in outs[0]:
         np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
     assert outs[0]["_id"].max() > n  # births took fresh ids past the given ones
+
+
+def test_parity_holds_without_programmatic_dependent_launch():
+    # Every kernel waits for its predecessors before touching memory, so with
+    # or without the programmatic-dependency launch attribute the results are
+    # those of plain stream order: the bit-exact Boids and birth/death checks
+    # run again in a process with the attribute off.
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FLAMEGPU_PDL="0")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-p", "no:cacheprovider", "-m", "gpu",
+                        os.path.join(root, "tests", "test_models_gpu.py"),
+                        "-k", "boids_small_matches_oracle or boids_clamped or birth_death_matches"],
+                       cwd=root, env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert "4 passed" in r.stdout, r.stdout[-2000:]
