@@ -58,9 +58,11 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+// Read-only load (data not written while the kernel runs); not volatile, so
+// the compiler may schedule several before their first use.
 __device__ __forceinline__ uint32_t ld_nc_u32(const uint32_t* p) {
     uint32_t v;
-    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    asm("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
     return v;
 }
 

@@ -200,17 +200,22 @@ struct RecordParams {
     uint32_t* out;
 };
 
+// Gathers record i from its source columns and writes it at dst. Sixteen words
+// at a time are all loaded before any is stored, so their latencies overlap.
 __device__ __forceinline__ void emit_record(const RecordParams& rp, uint32_t i, uint32_t dst) {
     const uint32_t words = rp.rec.words;
     uint4* o = reinterpret_cast<uint4*>(rp.out + static_cast<size_t>(dst) * words);
-    for (uint32_t w = 0; w < words; w += 4) {
-        uint32_t v[4];
+    for (uint32_t w0 = 0; w0 < words; w0 += 16) {
+        uint32_t v[16];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t* src = rp.rec.src[w + k];
-            v[k] = src ? ld_nc_u32(src + static_cast<size_t>(i) * rp.rec.src_stride[w + k] + rp.rec.src_word[w + k]) : 0u;
+        for (uint32_t k = 0; k < 16; ++k) {
+            const uint32_t w = w0 + k;
+            const uint32_t* src = w < words ? rp.rec.src[w] : nullptr;
+            v[k] = src ? ld_nc_u32(src + static_cast<size_t>(i) * rp.rec.src_stride[w] + rp.rec.src_word[w]) : 0u;
         }
-        o[w >> 2] = make_uint4(v[0], v[1], v[2], v[3]);
+#pragma unroll
+        for (uint32_t k = 0; k < 16; k += 4)
+            if (w0 + k < words) o[(w0 + k) >> 2] = make_uint4(v[k], v[k + 1], v[k + 2], v[k + 3]);
     }
 }
 
@@ -251,14 +256,35 @@ struct EmitParams {
     ColumnParams cp;
 };
 
+// Every agent column's element i written at dst. Runs of four 4-byte columns
+// (the common float / int variables) are all loaded before any is stored, so
+// their latencies overlap; other columns are copied one by one.
+__device__ __forceinline__ void emit_columns(const ColumnParams& cp, uint32_t i, uint32_t dst) {
+    for (uint32_t c0 = 0; c0 < cp.ncols; c0 += 4) {
+        const uint32_t nk = min(4u, cp.ncols - c0);
+        bool words = true;
+        for (uint32_t k = 0; k < nk; ++k) words = words && cp.col[c0 + k].elem_bytes == 4u;
+        if (words) {
+            uint32_t v[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k)
+                if (k < nk) v[k] = static_cast<const uint32_t*>(cp.col[c0 + k].in)[i];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k)
+                if (k < nk) static_cast<uint32_t*>(cp.col[c0 + k].out)[dst] = v[k];
+        } else {
+            for (uint32_t k = 0; k < nk; ++k) copy_column_elem(cp.col[c0 + k], i, dst);
+        }
+    }
+}
+
 template <int EMIT>
 __device__ __forceinline__ void emit(const EmitParams& ep, uint32_t* sperm, uint32_t i, uint32_t dst) {
     if (EMIT == kEmitRecord) {
         emit_record(ep.rp, i, dst);
     } else {
         sperm[dst] = i;
-        if (EMIT == kEmitPermColumns)
-            for (uint32_t c = 0; c < ep.cp.ncols; ++c) copy_column_elem(ep.cp.col[c], i, dst);
+        if (EMIT == kEmitPermColumns) emit_columns(ep.cp, i, dst);
     }
 }
 
@@ -516,6 +542,8 @@ bool sort_grid_from(const fg_spatial_grid* g, SortGrid* s, uint32_t* nbuckets) {
 }  // namespace
 
 extern "C" int fg_last_cuda_error(void) { return g_last_cuda_error; }
+
+
 
 extern "C" int fg_spatial_grid_init(fg_spatial_grid* g, int32_t dims, const float* mn, const float* mx, float radius) {
     // MessageSpatial3D::CUDAModelHandler::CUDAModelHandler (MessageSpatial3D.cu:31-52)

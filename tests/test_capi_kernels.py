@@ -208,6 +208,50 @@ def test_build_long_bins_sorted_and_ranked():
 
 
 @pytest.mark.gpu
+def test_build_mixed_buckets_under_16k():
+    # a list of under 16,384 messages with short, warp-sized and long buckets,
+    # messages of all buckets interleaved at random
+    rng = np.random.default_rng(23)
+    g = _capi().grid(3, (0, 0, 0), (8, 8, 8), 1.0)
+    sizes = [33, 64, 200, 256, 257, 1000, 4096, 5000, 1, 2, 31, 32]
+    cells = rng.choice(512, len(sizes), replace=False)
+    pos = []
+    for c, k in zip(cells, sizes):
+        cx, cy, cz = c % 8, (c // 8) % 8, c // 64
+        pos.append(np.stack([cx + rng.uniform(0.01, 0.99, k), cy + rng.uniform(0.01, 0.99, k),
+                             cz + rng.uniform(0.01, 0.99, k)], 1))
+    pos = np.concatenate(pos).astype(np.float32)
+    pos = pos[rng.permutation(len(pos))]
+    assert len(pos) <= 16384
+    pbm, srt, payload, _ = _build(g, pos, reps=2)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    np.testing.assert_array_equal(srt[:len(pos), 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [16384, 16385])
+def test_build_one_bucket_and_optional_at_16k(n):
+    # every message in one bucket, then clustered optional output with a
+    # device count, at 16,384 messages and one more
+    rng = np.random.default_rng(n)
+    g = _capi().grid(3, (0, 0, 0), (8, 8, 8), 1.0)
+    pos = _positions(rng, n, (0, 0, 0), (8, 8, 8), "onebin")
+    pbm, srt, payload, _ = _build(g, pos)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    np.testing.assert_array_equal(srt[:n, 3:6].view(np.int32), payload[eperm])
+    pos = _positions(rng, n, (0, 0, 0), (8, 8, 8), "clusters")
+    valid = rng.random(n) < 0.7
+    pbm, srt, payload, _ = _build(g, pos, valid=valid, d_count=n - 1000)
+    epbm, eperm = _expect(g, pos, valid=valid, d_count=n - 1000)
+    np.testing.assert_array_equal(pbm, epbm)
+    m = int(epbm[-1])
+    np.testing.assert_array_equal(srt[:m, 0:3].view(np.float32), pos[eperm])
+    np.testing.assert_array_equal(srt[:m, 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 4095, 4096, 4097, 1_000_000, 17_000_001])
 def test_exclusive_scan(n):
     import torch
@@ -227,7 +271,8 @@ def test_exclusive_scan(n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dims,n,kind", [(3, 16384, "uniform"), (3, 50000, "outside"), (2, 30000, "clusters")])
+@pytest.mark.parametrize("dims,n,kind", [(3, 16384, "uniform"), (3, 50000, "outside"), (2, 30000, "clusters"),
+                                         (3, 12000, "clusters"), (2, 9000, "outside")])
 def test_spatial_sort_agents_parity(dims, n, kind):
     import torch
     capi = _capi()
