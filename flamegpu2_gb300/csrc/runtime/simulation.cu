@@ -55,13 +55,18 @@ using exception::format;
 
 namespace {
 
-__global__ void k_step_increment(uint32_t* d_step) {
+// End of a step in one launch: the message counts of the non-persistent
+// lists are cleared (CUDASimulation.cu:619-625) and the step counter advances.
+constexpr uint32_t kStepEndClears = 16;
+struct StepEnd {
+    uint32_t* clear[kStepEndClears];
+    uint32_t nclear;
+    uint32_t* d_step;
+};
+__global__ void k_step_end(const __grid_constant__ StepEnd e) {
     grid_dependency_enter();
-    *d_step += 1;
-}
-__global__ void k_set_u32(uint32_t* p, uint32_t v) {
-    grid_dependency_enter();
-    *p = v;
+    if (threadIdx.x < e.nclear) *e.clear[threadIdx.x] = 0u;
+    if (threadIdx.x == 0) *e.d_step += 1u;
 }
 __global__ void k_max_u32(uint32_t* p, uint32_t v) {
     grid_dependency_enter();
@@ -1056,14 +1061,27 @@ struct SimulationImpl {
                 for (auto& f : fns)
                     if (f.fn == fd) enqueue_function(f);
         }
-        // non-persistent messages are cleared at the end of the step (CUDASimulation.cu:619-625)
+        enqueue_step_end();
+        kernel_counter += 1;
+    }
+
+    // non-persistent messages are cleared at the end of the step
+    // (CUDASimulation.cu:619-625), then the step counter advances
+    void enqueue_step_end() {
+        StepEnd e{};
+        auto clear = [&](uint32_t* p) {
+            if (e.nclear < kStepEndClears)
+                e.clear[e.nclear++] = p;
+            else
+                FG_CUDA(cudaMemsetAsync(p, 0, sizeof(uint32_t), stream));
+        };
         for (auto& m : msgs)
             if (!m->msg->persistent) {
-                FG_CUDA(cudaMemsetAsync(m->d_count, 0, sizeof(uint32_t), stream));
-                if (m->bf_count) FG_CUDA(cudaMemsetAsync(m->bf_count, 0, sizeof(uint32_t), stream));
+                clear(m->d_count);
+                if (m->bf_count) clear(m->bf_count);
             }
-        launch_kernel(pdl_enabled(), k_step_increment, 1, 1, 0, stream, d_step());
-        kernel_counter += 1;
+        e.d_step = d_step();
+        FG_CUDA(launch_kernel(pdl_enabled(), k_step_end, 1, 32, 0, stream, e));
     }
 
     bool has_layer_host_functions() const {
@@ -1110,12 +1128,7 @@ struct SimulationImpl {
                     for (auto& f : fns)
                         if (f.fn == fd) enqueue_function(f);
             }
-            for (auto& m : msgs)
-                if (!m->msg->persistent) {
-                    FG_CUDA(cudaMemsetAsync(m->d_count, 0, sizeof(uint32_t), stream));
-                    if (m->bf_count) FG_CUDA(cudaMemsetAsync(m->bf_count, 0, sizeof(uint32_t), stream));
-                }
-            launch_kernel(pdl_enabled(), k_step_increment, 1, 1, 0, stream, d_step());
+            enqueue_step_end();
             kernels_last_step = kernel_counter + 1;
         } else {
             const std::vector<int> key = step_key();
