@@ -263,8 +263,9 @@ extern "C" int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint
     WsHeader* h = reinterpret_cast<WsHeader*>(ws);
     uint64_t* status = reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader));
     const uint32_t tiles = comp_tiles(max_n);
+    // h->alive_total is zero here: the workspace starts zeroed
+    // (fg_workspace_init) and each compaction's last block resets it
     if (!d_alive_total && alive) {
-        cudaMemsetAsync(&h->alive_total, 0, sizeof(uint32_t), st);
         int dev = 0, sms = 132;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -301,8 +302,8 @@ extern "C" int fg_partition_agents(uint32_t max_n, const uint32_t* d_n, const ui
     WsHeader* h = reinterpret_cast<WsHeader*>(ws);
     uint64_t* status = reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader));
     // the first group is the compaction's "survivors" (counted first, so the
-    // second group knows where it starts), the rest its "births" in row order
-    cudaMemsetAsync(&h->alive_total, 0, sizeof(uint32_t), st);
+    // second group knows where it starts), the rest its "births" in row order;
+    // h->alive_total is zero here (see fg_compact_agents)
     int dev = 0, sms = 132;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

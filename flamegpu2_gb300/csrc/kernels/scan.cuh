@@ -98,17 +98,27 @@ __device__ __forceinline__ uint32_t lookback_u32(const uint64_t* status, uint32_
 
 // Exclusive scan of in[0..n) into out[0..n). If zero_in, in[] is cleared to 0
 // after it has been read (in != out). Launch with ceil(n / kScanTile) blocks of
-// kThreads threads.
+// kThreads threads. With self_reset the last block to finish resets the ticket
+// and advances the epoch for the next scan on this workspace; without it the
+// kernel launched just before this one has done so (scan_reset), which spares
+// every block a fence and an atomic at its end.
+__device__ __forceinline__ void scan_reset(WsHeader* h) {
+    h->scan_ticket = 0u;
+    h->scan_epoch = (h->scan_epoch + 1u) & 0x3FFFFFFFu;
+}
+
 __global__ void __launch_bounds__(kThreads) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
-                                                       uint64_t* status, WsHeader* h) {
+                                                       uint64_t* status, WsHeader* h, int self_reset) {
     flamegpu::detail::grid_dependency_enter();
-    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_tile, s_epoch;
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_excl;
-    if (threadIdx.x == 0) s_tile = atomicAdd(&h->scan_ticket, 1u);
-    const uint32_t epoch = ld_acquire_u32(&h->scan_epoch);
+    if (threadIdx.x == 0) {
+        s_tile = atomicAdd(&h->scan_ticket, 1u);
+        s_epoch = ld_acquire_u32(&h->scan_epoch);
+    }
     __syncthreads();
-    const uint32_t tile = s_tile;
+    const uint32_t tile = s_tile, epoch = s_epoch;
     const uint64_t base = static_cast<uint64_t>(tile) * kScanTile + static_cast<uint64_t>(threadIdx.x) * kScanItems;
     uint32_t v[kScanItems];
     const bool full = base + kScanItems <= n;
@@ -171,6 +181,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_u32(const uint32_t* in, uint3
                 if (base + k < n) zin[base + k] = 0;
         }
     }
+    if (!self_reset) return;
     // the last block to finish resets the ticket and advances the epoch
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -89,7 +89,10 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
                                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
                                                   uint32_t* hist, WsHeader* h) {
     flamegpu::detail::grid_dependency_enter();
-    if (blockIdx.x == 0 && threadIdx.x == 0) h->long_count = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        h->long_count = 0;
+        scan_reset(h);  // for the scan launched next
+    }
     const uint32_t n = load_count(d_n, max_n);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -137,7 +140,10 @@ __global__ void __launch_bounds__(kThreads) k_bin_batched(const fg_batch_instanc
                                                           uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
                                                           uint32_t* hist, WsHeader* h) {
     flamegpu::detail::grid_dependency_enter();
-    if (blockIdx.x == 0 && threadIdx.x == 0) h->long_count = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        h->long_count = 0;
+        scan_reset(h);  // for the scan launched next
+    }
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total_rows; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -615,7 +621,7 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     else
         launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
     const uint32_t scan_n = nbuckets + 1;
-    launch(k_scan_u32, scan_tiles(scan_n), kThreads, st, hist, pbm_out, scan_n, 1, sstat, h);
+    launch(k_scan_u32, scan_tiles(scan_n), kThreads, st, hist, pbm_out, scan_n, 1, sstat, h, 0);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
     launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
     launch(k_long<EMIT>, static_cast<uint32_t>(sm_count() * 4), kThreads, st, rp, pbm_out, perm, sperm, chunks,
@@ -684,7 +690,7 @@ extern "C" int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t
     if (!n) return FG_OK;
     char* ws = static_cast<char*>(workspace);
     launch(k_scan_u32, scan_tiles(n), kThreads, static_cast<cudaStream_t>(stream), in, out, n, 0,
-           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
+           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws), 1);
     return check_launch();
 }
 
@@ -748,7 +754,7 @@ extern "C" int fg_exclusive_scan_u32_noalloc(const uint32_t* in, uint32_t* out, 
     if (rc != FG_OK) return rc;
     if (!n) return FG_OK;
     launch(k_scan_u32, scan_tiles(n), kThreads, static_cast<cudaStream_t>(stream), in, out, n, 0,
-           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws));
+           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws), 1);
     return check_launch();
 }
 
