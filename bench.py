@@ -153,6 +153,11 @@ def boids_bytes(n, bins):
     }
 
 
+def workloads_mod():
+    from flamegpu2_gb300 import workloads
+    return workloads
+
+
 def run_boids_small(args, world, rank, local):
     import torch
     from flamegpu2_gb300 import sim, synth
@@ -251,9 +256,11 @@ def run_boids_small(args, world, rank, local):
         "wall_s": round(wall, 4),
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": 28 * n, "d2h_bytes_per_step": 28 * n,
                 "path": "fgs_set_population + fgs_step(10) + fgs_get_population (C ABI, pinned host buffers)"},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": None,
-                     "peak_source": peak_kind, "per_launch_algorithmic_bytes": algo.get(dom)},
+        "roofline": workloads_mod()._with_traffic(
+            {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak,
+             "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": None,
+             "peak_source": peak_kind, "per_launch_algorithmic_bytes": algo.get(dom)},
+            "boids_small_inputdata" if dom == "fn:inputdata" else ""),
         "stages": stages,
         "stage_timing": "CUDA events captured into the step graphs around each operation, second timed pass "
                         "(sort and build run concurrently on two graph branches, each timed on its own stream)",

@@ -43,6 +43,27 @@ def _stage_table(prof: dict, algo: dict, per_launch: bool = True) -> dict:
     return out
 
 
+def profiled_traffic(summary: str):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+    a workload's roofline kernel, from one ncu capture summarised in
+    profiles/<summary>.md (line 'traffic_bytes_per_launch: N'); None if absent."""
+    import re
+    try:
+        with open(os.path.join(ROOT, "profiles", summary + ".md")) as f:
+            m = re.search(r"^traffic_bytes_per_launch:\s*(\d+)", f.read(), re.M)
+    except OSError:
+        return None
+    return int(m.group(1)) if m else None
+
+
+def _with_traffic(roof: dict, summary: str, what: str = None) -> dict:
+    t = profiled_traffic(summary)
+    if t is not None:
+        roof["traffic"] = t
+        roof["traffic_source"] = f"profiles/{summary}.md" + (f": {what}" if what else "")
+    return roof
+
+
 def _roofline(stages: dict, peak: float, peak_kind: str) -> dict:
     cands = [(k, v) for k, v in stages.items() if "gbs" in v and v.get("gbs")]
     if not cands:
@@ -144,7 +165,9 @@ def run_birth_death(args, world, rank, local):
         "wall_s": round(wall, 4),
         "e2e": {"value": round(agent_steps * e2e_n * world / e2e_s, 1), "unit": UNIT,
                 "h2d_bytes_per_step": n0 * row, "d2h_bytes_per_step": final * row},
-        "roofline": _roofline(stages, peak, peak_kind), "stages": stages,
+        "roofline": _with_traffic(_roofline(stages, peak, peak_kind), "birth_death_compact",
+                                  "k_compact alone (the stage also counts the survivors)"),
+        "stages": stages,
         "gpu_launches": kps * steps_per * k_steps, "clocks": clk,
     }
 
