@@ -197,7 +197,7 @@ extern "C" int fgs_get_variable_device(fgs_sim* s, const char* agent, const char
 
 extern "C" int fgs_step(fgs_sim* s, uint32_t steps) {
     return guarded([&] {
-        for (uint32_t i = 0; i < steps; ++i) s->sim->step();
+        s->sim->step(static_cast<unsigned int>(steps));
     });
 }
 

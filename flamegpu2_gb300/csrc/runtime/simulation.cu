@@ -274,7 +274,11 @@ struct SimulationImpl {
     std::map<std::vector<int>, std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>>> graph_op_events;
     std::set<std::vector<int>> replayed;
     // timing
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> step_events;
+    struct StepTimer {
+        cudaEvent_t e0, e1;
+        unsigned int steps;  // model steps between the two events
+    };
+    std::vector<StepTimer> step_events;
     std::vector<double> step_ms;
     double sim_ms = 0.0;
 
@@ -288,8 +292,8 @@ struct SimulationImpl {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         drop_graph_op_events();
         for (auto& e : step_events) {
-            cudaEventDestroy(e.first);
-            cudaEventDestroy(e.second);
+            cudaEventDestroy(e.e0);
+            cudaEventDestroy(e.e1);
         }
         for (auto& c : count_ring)
             if (c.ev) cudaEventDestroy(c.ev);
@@ -1164,7 +1168,7 @@ struct SimulationImpl {
             if (cuda_config.time_ops_in_graphs) replayed.insert(key);
         }
         FG_CUDA(cudaEventRecord(e1, stream));
-        step_events.emplace_back(e0, e1);
+        step_events.push_back({e0, e1, 1u});
         record_counts();
         ++step_count;
         if (!model->step_functions.empty()) {
@@ -1175,6 +1179,74 @@ struct SimulationImpl {
         }
         if (cuda_config.check_each_step) owner->synchronize();
         owner->processStepLog(-1.0);
+    }
+
+    // Whether steps may be replayed several per graph: no host work between
+    // steps (host layers, step functions, step log), no population growth
+    // (births, state transitions: their capacity is checked on the host each
+    // step), graphs on, no per-operation timing or per-step checks.
+    bool multi_step_ok(bool step_log) const {
+        return cuda_config.use_graphs && !cuda_config.profile_ops && !cuda_config.time_ops_in_graphs &&
+               !cuda_config.check_each_step && !step_log && !has_layer_host_functions() &&
+               model->step_functions.empty() && !any_births() && !any_transitions();
+    }
+
+    // S steps as one captured graph, cached by the buffer parities at its
+    // start and every step's sort decisions.
+    void step_block(unsigned int S) {
+        ensure_all_allocated();
+        prepare_capacity();
+        upload_env_if_dirty();
+        const unsigned int first = step_count;
+        std::vector<int> key{-static_cast<int>(S)};
+        std::vector<int> parity_before;
+        for (auto& l : lists) {
+            key.push_back(l->parity);
+            parity_before.push_back(l->parity);
+        }
+        for (unsigned int j = 0; j < S; ++j)
+            for (const auto& layer : model->layers)
+                for (auto* fd : layer->functions) {
+                    const unsigned p = fd->parent->sort_period;
+                    key.push_back(p != 0 && (first + j) % p == 0);
+                }
+        cudaEvent_t e0, e1;
+        FG_CUDA(cudaEventCreate(&e0));
+        FG_CUDA(cudaEventCreate(&e1));
+        FG_CUDA(cudaEventRecord(e0, stream));
+        profiling = false;
+        auto it = graphs.find(key);
+        if (it == graphs.end()) {
+            cudaGraph_t g;
+            FG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            capturing = true;
+            capture_key = key;
+            try {
+                for (unsigned int j = 0; j < S; ++j, ++step_count) enqueue_step();
+            } catch (...) {
+                step_count = first;
+                capturing = false;
+                cudaStreamEndCapture(stream, &g);
+                throw;
+            }
+            step_count = first;
+            capturing = false;
+            FG_CUDA(cudaStreamEndCapture(stream, &g));
+            cudaGraphExec_t ge;
+            FG_CUDA(cudaGraphInstantiate(&ge, g, 0));
+            cudaGraphDestroy(g);
+            it = graphs.emplace(key, ge).first;
+        } else {
+            for (size_t i = 0; i < lists.size(); ++i) lists[i]->parity = parity_before[i];
+            for (unsigned int j = 0; j < S; ++j, ++step_count) simulate_parity_flips();
+            step_count = first;
+        }
+        kernels_last_step = kernel_counter;
+        FG_CUDA(cudaGraphLaunch(it->second, stream));
+        ++graph_launches;
+        FG_CUDA(cudaEventRecord(e1, stream));
+        step_events.push_back({e0, e1, S});
+        step_count += S;
     }
 
     // The parity changes a step makes, replayed on the host for a cached graph.
@@ -1677,6 +1749,24 @@ bool CUDASimulation::step() {
     return true;
 }
 
+void CUDASimulation::step(unsigned int n) {
+    if (n == 0) return;
+    if (impl->step_count == 0 && !impl->model->init_functions.empty()) {
+        HostAPI api(impl.get());
+        for (auto fn : impl->model->init_functions) fn(&api);
+    }
+    if (!impl->multi_step_ok(step_log != nullptr)) {
+        for (unsigned int s = 0; s < n; ++s) impl->step_once(this);
+        return;
+    }
+    constexpr unsigned int kBlock = 16;
+    while (n) {
+        const unsigned int S = n < kBlock ? n : kBlock;
+        impl->step_block(S);
+        n -= S;
+    }
+}
+
 void CUDASimulation::simulate() {
     impl->ensure_all_allocated();
     cudaEvent_t s0, s1;
@@ -1689,7 +1779,15 @@ void CUDASimulation::simulate() {
         for (auto fn : impl->model->init_functions) fn(&api);
     }
     processStepLog(0.0);  // the frame before the first step (CUDASimulation.cu:1263)
-    for (unsigned int s = 0; s < impl->config.steps; ++s) impl->step_once(this);
+    if (impl->multi_step_ok(step_log != nullptr)) {
+        for (unsigned int n = impl->config.steps; n;) {
+            const unsigned int S = n < 16u ? n : 16u;
+            impl->step_block(S);
+            n -= S;
+        }
+    } else {
+        for (unsigned int s = 0; s < impl->config.steps; ++s) impl->step_once(this);
+    }
     if (!impl->model->exit_functions.empty()) {
         FG_CUDA(cudaStreamSynchronize(impl->stream));
         HostAPI api(impl.get());
@@ -1718,10 +1816,11 @@ void CUDASimulation::synchronize() {
     // resolve the step timers
     for (auto& e : impl->step_events) {
         float ms = 0;
-        cudaEventElapsedTime(&ms, e.first, e.second);
-        impl->step_ms.push_back(ms);
-        cudaEventDestroy(e.first);
-        cudaEventDestroy(e.second);
+        cudaEventElapsedTime(&ms, e.e0, e.e1);
+        // steps replayed as one graph share its time equally
+        for (unsigned int k = 0; k < e.steps; ++k) impl->step_ms.push_back(ms / e.steps);
+        cudaEventDestroy(e.e0);
+        cudaEventDestroy(e.e1);
     }
     impl->step_events.clear();
 }

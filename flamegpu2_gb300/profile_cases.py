@@ -39,6 +39,8 @@ def boids(n: int, steps: int = 20):
     s.step(5)
     prof = s.take_profile()
     s.profile_ops(False)
+    s.step(steps)  # captures the step graphs this call replays
+    s.synchronize()
     t = time.perf_counter()
     s.step(steps)
     s.synchronize()

@@ -135,6 +135,11 @@ class CUDASimulation {
 
     /** One step (all layers). Returns false if an exit condition requests a stop. */
     bool step();
+    /** n steps (GB300 extension). When no host work runs between steps (no
+     *  host layers, step functions or step log, no births or state changes
+     *  whose capacity the host checks), up to 16 steps are replayed as one
+     *  captured graph; the results are those of n calls of step(). */
+    void step(unsigned int n);
     /** SimulationConfig().steps steps. */
     void simulate();
     unsigned int getStepCounter() const;

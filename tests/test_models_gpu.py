@@ -161,7 +161,7 @@ def test_boids_small_matches_oracle(use_graphs):
     for k in ("x", "y", "z", "fx", "fy", "fz"):
         np.testing.assert_array_equal(out[k], ref[k], err_msg=k)
     if use_graphs:
-        assert st["graph_launches"] == 10
+        assert st["graph_launches"] == 1  # ten steps replayed as one captured graph
 
 
 def test_boids_clamped_matches_oracle():
@@ -265,3 +265,30 @@ def test_parity_holds_without_programmatic_dependent_launch():
                        cwd=root, env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
     assert "4 passed" in r.stdout, r.stdout[-2000:]
+
+
+def test_steps_replayed_as_one_graph_match_single_steps():
+    # step(n) replays up to 16 steps per captured graph when no host work runs
+    # between steps; the state after 37 steps (16 + 16 + 5) equals that of 37
+    # single steps, and the step counter and per-step timings cover every step
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    cfg = dict(synth.BOIDS_SMALL, n=3000, seed=9)
+    pop = synth.boids_population(cfg["n"], cfg["min_pos"], cfg["max_pos"], cfg["seed"])
+    outs, stats = [], []
+    for many in (False, True):
+        s = S.Simulation("boids_spatial3d", synth.boids_params(cfg))
+        s.set_population("Boid", cfg["n"], pop)
+        if many:
+            s.step(37)
+        else:
+            for _ in range(37):
+                s.step(1)
+        outs.append({k: s.get("Boid", k, np.float32) for k in ("x", "y", "z", "fx")})
+        outs[-1]["_id"] = s.get("Boid", "_id", np.uint32)
+        stats.append(s.stats())
+        s.close()
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
+    assert stats[0]["graph_launches"] == 37 and stats[1]["graph_launches"] == 3
+    assert stats[0]["step_counter"] == stats[1]["step_counter"] == 37
