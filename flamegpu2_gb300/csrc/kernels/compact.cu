@@ -103,6 +103,40 @@ __global__ void k_set_alive_total(uint32_t max_n, const uint32_t* d_n, WsHeader*
     h->alive_total = d_n ? min(*d_n, max_n) : max_n;
 }
 
+// Row i of every column written at dst (cols: the survivors' or the births'
+// sources). Runs of four 4-byte columns are all loaded before any is stored,
+// so their latencies overlap; the id column of births gets next_id + r.
+__device__ __forceinline__ void copy_row(const fg_column* cols, uint32_t ncols, uint32_t i, uint32_t dst, int id_col,
+                                         uint32_t id) {
+    for (uint32_t c0 = 0; c0 < ncols; c0 += 4) {
+        const uint32_t nk = min(4u, ncols - c0);
+        bool words = true;
+        for (uint32_t k = 0; k < nk; ++k) words = words && cols[c0 + k].elem_bytes == 4u;
+        if (words) {
+            uint32_t v[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k)
+                if (k < nk) v[k] = static_cast<int32_t>(c0 + k) == id_col ? id : reinterpret_cast<const uint32_t*>(cols[c0 + k].in)[i];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k)
+                if (k < nk) reinterpret_cast<uint32_t*>(cols[c0 + k].out)[dst] = v[k];
+        } else {
+            for (uint32_t k = 0; k < nk; ++k) {
+                if (static_cast<int32_t>(c0 + k) == id_col)
+                    reinterpret_cast<uint32_t*>(cols[c0 + k].out)[dst] = id;
+                else
+                    copy_col(cols[c0 + k], i, dst);
+            }
+        }
+    }
+}
+
+// Persistent tiles: each block takes tiles of kCompTile rows by ticket (in
+// launch order) until the rows [0, n) are covered, so the grid can be a few
+// blocks per SM whatever the capacity, and a small population costs a few
+// tiles rather than one block per tile of capacity. A tile waits only on
+// lower tiles, taken earlier by running blocks that publish their aggregate
+// before they look back themselves.
 __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ CompactParams cp, uint32_t max_n,
                                                       const uint32_t* d_n, const uint32_t* __restrict__ alive,
                                                       const uint32_t* __restrict__ born, uint32_t* d_next_id,
@@ -116,21 +150,21 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
     __shared__ uint32_t s_tot[2];
     __shared__ uint64_t s_excl;
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(&h->comp_ticket, 1u);
     const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
     const uint32_t n = d_n ? min(*d_n, max_n) : max_n;
     const uint32_t S = d_alive_total ? *d_alive_total : h->alive_total;
     const uint32_t next_id = d_next_id ? *d_next_id : 0u;
-    __syncthreads();
-    const uint32_t tile = s_tile;
     uint64_t* status = status0 + static_cast<size_t>(parity) * stride_tiles;
     // clear the whole status array the next call will use (its grid may differ)
     uint64_t* other = status0 + static_cast<size_t>(parity ^ 1u) * stride_tiles;
     for (uint32_t t = blockIdx.x * blockDim.x + tid; t < stride_tiles; t += gridDim.x * blockDim.x) other[t] = 0;
-    const uint32_t base = tile * kCompTile;
-    const bool active_tile = base < n;
-    uint32_t ba[kCompItems], bb[kCompItems];
-    if (active_tile) {
+    for (;;) {
+        if (tid == 0) s_tile = atomicAdd(&h->comp_ticket, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        const uint32_t base = tile * kCompTile;
+        if (base >= n) break;  // the same in every thread: no rows left
+        uint32_t ba[kCompItems], bb[kCompItems];
 #pragma unroll
         for (int k = 0; k < kCompItems; ++k) {
             const uint32_t i = base + k * kThreads + tid;
@@ -145,43 +179,41 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
                 s_cnt_b[k][warp] = __popc(bb[k]);
             }
         }
-    }
-    __syncthreads();
-    if (active_tile && tid == 0) {
-        uint32_t ra = 0, rb = 0;
-        for (int k = 0; k < kCompItems; ++k)
-            for (int w = 0; w < kThreads / 32; ++w) {
-                const uint32_t a = s_cnt_a[k][w], b = s_cnt_b[k][w];
-                s_cnt_a[k][w] = ra;
-                s_cnt_b[k][w] = rb;
-                ra += a;
-                rb += b;
-            }
-        s_tot[0] = ra;
-        s_tot[1] = rb;
-    }
-    __syncthreads();
-    if (active_tile && tid < 32) {
-        const uint64_t agg = (static_cast<uint64_t>(s_tot[0]) << 31) | s_tot[1];
-        uint64_t excl = 0;
-        if (tile == 0) {
-            if (tid == 0) st_release_u64(status, pair_pack(2, s_tot[0], s_tot[1]));
-        } else {
-            if (tid == 0) st_release_u64(status + tile, (1ull << 62) | agg);
-            excl = lookback_pair(status, tile, h);
-            if (tid == 0) st_release_u64(status + tile, (2ull << 62) | ((excl + agg) & kPairMask));
-        }
+        __syncthreads();
         if (tid == 0) {
-            s_excl = excl;
-            if (base + kCompTile >= n) {  // last active tile: publish the totals
-                const uint64_t inc = excl + agg;
-                h->pad[0] = static_cast<uint32_t>(inc & 0x7FFFFFFFu);          // births
-                h->pad[1] = static_cast<uint32_t>((inc >> 31) & 0x7FFFFFFFu);  // survivors
+            uint32_t ra = 0, rb = 0;
+            for (int k = 0; k < kCompItems; ++k)
+                for (int w = 0; w < kThreads / 32; ++w) {
+                    const uint32_t a = s_cnt_a[k][w], b = s_cnt_b[k][w];
+                    s_cnt_a[k][w] = ra;
+                    s_cnt_b[k][w] = rb;
+                    ra += a;
+                    rb += b;
+                }
+            s_tot[0] = ra;
+            s_tot[1] = rb;
+        }
+        __syncthreads();
+        if (tid < 32) {
+            const uint64_t agg = (static_cast<uint64_t>(s_tot[0]) << 31) | s_tot[1];
+            uint64_t excl = 0;
+            if (tile == 0) {
+                if (tid == 0) st_release_u64(status, pair_pack(2, s_tot[0], s_tot[1]));
+            } else {
+                if (tid == 0) st_release_u64(status + tile, (1ull << 62) | agg);
+                excl = lookback_pair(status, tile, h);
+                if (tid == 0) st_release_u64(status + tile, (2ull << 62) | ((excl + agg) & kPairMask));
+            }
+            if (tid == 0) {
+                s_excl = excl;
+                if (base + kCompTile >= n) {  // last tile with rows: publish the totals
+                    const uint64_t inc = excl + agg;
+                    h->pad[0] = static_cast<uint32_t>(inc & 0x7FFFFFFFu);          // births
+                    h->pad[1] = static_cast<uint32_t>((inc >> 31) & 0x7FFFFFFFu);  // survivors
+                }
             }
         }
-    }
-    __syncthreads();
-    if (active_tile) {
+        __syncthreads();
         const uint32_t ea = static_cast<uint32_t>((s_excl >> 31) & 0x7FFFFFFFu);
         const uint32_t eb = static_cast<uint32_t>(s_excl & 0x7FFFFFFFu);
         const uint32_t lt = lanemask_lt();
@@ -190,24 +222,18 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
             const uint32_t i = base + k * kThreads + tid;
             if ((ba[k] >> lane) & 1u) {
                 const uint32_t dst = ea + s_cnt_a[k][warp] + __popc(ba[k] & lt);
-                if (dst < out_capacity)
-                    for (uint32_t c = 0; c < cp.ncols; ++c) copy_col(cp.col[c], i, dst);
+                if (dst < out_capacity) copy_row(cp.col, cp.ncols, i, dst, -1, 0u);
             }
             if ((bb[k] >> lane) & 1u) {
                 const uint32_t r = eb + s_cnt_b[k][warp] + __popc(bb[k] & lt);
                 const uint32_t dst = S + r;
-                if (dst < out_capacity) {
-                    for (uint32_t c = 0; c < cp.ncols; ++c) {
-                        if (static_cast<int32_t>(c) == cp.id_col)
-                            reinterpret_cast<uint32_t*>(cp.col[c].out)[dst] = next_id + r;
-                        else
-                            copy_col(cp.bcol[c], i, dst);
-                    }
-                } else {
+                if (dst < out_capacity)
+                    copy_row(cp.bcol, cp.ncols, i, dst, cp.id_col, next_id + r);
+                else
                     record_status(h, FG_ERR_CAPACITY);
-                }
             }
         }
+        __syncthreads();  // s_tile, s_cnt_*, s_excl are reused by the next tile
     }
     // the last block to finish publishes the new count and resets the tickets
     __syncthreads();
@@ -241,6 +267,18 @@ int launch_err() {
     return e == cudaSuccess ? FG_OK : FG_ERR_CUDA;
 }
 uint32_t comp_tiles(uint32_t max_n) { return std::max(1u, (max_n + kCompTile - 1) / kCompTile); }
+uint32_t device_sms() {
+    int dev = 0, sms = 132;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return static_cast<uint32_t>(sms);
+}
+// persistent compaction blocks: four per SM, or one per tile of capacity if fewer
+uint32_t comp_grid(uint32_t max_n) { return std::min(comp_tiles(max_n), 4u * device_sms()); }
+// survivor-count blocks (grid-stride over the flags): four per SM at most
+uint32_t count_grid(uint32_t max_n) {
+    return std::max(1u, std::min((max_n + kThreads - 1) / kThreads, 4u * device_sms()));
+}
 }  // namespace
 
 extern "C" size_t fg_compact_workspace_size(uint32_t max_n) {
@@ -262,15 +300,11 @@ extern "C" int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint
     char* ws = static_cast<char*>(workspace);
     WsHeader* h = reinterpret_cast<WsHeader*>(ws);
     uint64_t* status = reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader));
-    const uint32_t tiles = comp_tiles(max_n);
+    const uint32_t tiles = comp_grid(max_n);
     // h->alive_total is zero here: the workspace starts zeroed
     // (fg_workspace_init) and each compaction's last block resets it
     if (!d_alive_total && alive) {
-        int dev = 0, sms = 132;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const uint32_t grid = std::max(1u, std::min((max_n + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
-        launch(k_count_alive, grid, kThreads, st, max_n, d_n, alive, h);
+        launch(k_count_alive, count_grid(max_n), kThreads, st, max_n, d_n, alive, h);
     } else if (!d_alive_total) {
         // every agent survives: S = n
         launch(k_set_alive_total, 1, 1, st, max_n, d_n, h);
@@ -304,17 +338,13 @@ extern "C" int fg_partition_agents(uint32_t max_n, const uint32_t* d_n, const ui
     // the first group is the compaction's "survivors" (counted first, so the
     // second group knows where it starts), the rest its "births" in row order;
     // h->alive_total is zero here (see fg_compact_agents)
-    int dev = 0, sms = 132;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t grid = std::max(1u, std::min((max_n + kThreads - 1) / kThreads, static_cast<uint32_t>(sms * 8)));
-    launch(k_count_alive, grid, kThreads, st, max_n, d_n, first_group, h);
+    launch(k_count_alive, count_grid(max_n), kThreads, st, max_n, d_n, first_group, h);
     CompactParams cp{};
     for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cp.bcol[c] = cols[c];
     cp.ncols = ncols;
     cp.id_col = -1;
     const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
-    launch(k_compact, comp_tiles(max_n), kThreads, st, cp, max_n, d_n, first_group, nullptr, nullptr, nullptr, nullptr,
+    launch(k_compact, comp_grid(max_n), kThreads, st, cp, max_n, d_n, first_group, nullptr, nullptr, nullptr, nullptr,
            max_n, status, stride_tiles, h, 1, d_first_count);
     return launch_err();
 }
