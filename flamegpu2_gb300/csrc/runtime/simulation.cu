@@ -803,7 +803,10 @@ struct SimulationImpl {
 
     std::vector<int> step_key() const {
         std::vector<int> k;
-        for (const auto& l : lists) k.push_back(l->parity);
+        for (const auto& l : lists) {
+            k.push_back(l->parity);
+            k.push_back(static_cast<int>(grid_rows(*l)));
+        }
         for (const auto& layer : model->layers)
             for (auto* fd : layer->functions) {
                 const unsigned p = fd->parent->sort_period;
@@ -898,6 +901,23 @@ struct SimulationImpl {
         kernel_counter += 5;
     }
 
+    // Rows an agent-function launch of list l covers with one block per 128
+    // rows: the host's bound on its population rounded up to a power of two
+    // (at least one wave of 8 blocks per SM), at most its capacity. The
+    // kernels loop over the rows, so a population above this takes more rounds
+    // per block, never a wrong result; a population far below its capacity
+    // (a decaying birth/death run) launches few blocks. The step graphs are
+    // keyed by it, so a change of class captures a graph sized for it.
+    uint32_t grid_rows(const AgentList& l) const {
+        uint64_t r = 1;
+        while (r < l.bound) r <<= 1;
+        r = std::max<uint64_t>(r, 8ull * static_cast<uint64_t>(sms) * kAgentBlock);
+        return static_cast<uint32_t>(std::min<uint64_t>(r, std::max(l.capacity, 1u)));
+    }
+    unsigned int agent_grid(uint32_t rows) const {
+        return std::min(std::max(1u, (rows + kAgentBlock - 1) / kAgentBlock), 1u << 16);
+    }
+
     static bool stage_window_fits(const MsgList& m, unsigned int stage_bytes) {
         const double per_bin = static_cast<double>(m.capacity) / std::max<uint32_t>(m.grid.binCount, 1u);
         return detail::stage_window_fits(m.grid, per_bin, m.record_words, kAgentBlock, stage_bytes);
@@ -944,8 +964,7 @@ struct SimulationImpl {
             C.env = d_env;
             cudaError_t ce = cudaSuccess;
             timed("cond:" + f.fn->name, [&] {
-                ce = f.fn->condition(C, grid_for(l.capacity + 1, kAgentBlock, 1 << 16), kAgentBlock, 0, stream,
-                                     detail::pdl_enabled());
+                ce = f.fn->condition(C, agent_grid(grid_rows(l) + 1), kAgentBlock, 0, stream, detail::pdl_enabled());
             });
             if (ce != cudaSuccess)
                 THROW exception::CUDAError(format("Launch of the condition of '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(ce)));
@@ -1000,8 +1019,7 @@ struct SimulationImpl {
         // kernels of other simulations on the device (a server's other runs,
         // higher-priority streams) get SMs between them
         timed("fn:" + f.fn->name, [&] {
-            e = f.fn->launcher(P, grid_for(l.capacity, kAgentBlock, 1 << 16), kAgentBlock, smem, stream,
-                               detail::pdl_enabled());
+            e = f.fn->launcher(P, agent_grid(grid_rows(l)), kAgentBlock, smem, stream, detail::pdl_enabled());
         });
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(e)));
@@ -1202,6 +1220,7 @@ struct SimulationImpl {
         std::vector<int> parity_before;
         for (auto& l : lists) {
             key.push_back(l->parity);
+            key.push_back(static_cast<int>(grid_rows(*l)));
             parity_before.push_back(l->parity);
         }
         for (unsigned int j = 0; j < S; ++j)
