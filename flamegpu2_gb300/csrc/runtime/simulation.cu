@@ -524,6 +524,19 @@ struct SimulationImpl {
         invalidate();
     }
 
+    // Step graphs are keyed by parities, population classes, sort decisions
+    // and block lengths; a long run with births can meet many keys. The cache
+    // is emptied when it reaches kGraphCache entries (the graphs are captured
+    // again as the keys recur).
+    static constexpr size_t kGraphCache = 256;
+    void trim_graph_cache() {
+        if (graphs.size() < kGraphCache) return;
+        FG_CUDA(cudaStreamSynchronize(stream));
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+        drop_graph_op_events();
+    }
+
     void invalidate() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         graphs.clear();
@@ -1174,6 +1187,7 @@ struct SimulationImpl {
                 cudaGraphExec_t ge;
                 FG_CUDA(cudaGraphInstantiate(&ge, g, 0));
                 cudaGraphDestroy(g);
+                trim_graph_cache();
                 it = graphs.emplace(key, ge).first;
                 kernels_last_step = kernel_counter;
             } else {
@@ -1200,21 +1214,35 @@ struct SimulationImpl {
     }
 
     // Whether steps may be replayed several per graph: no host work between
-    // steps (host layers, step functions, step log), no population growth
-    // (births, state transitions: their capacity is checked on the host each
-    // step), graphs on, no per-operation timing or per-step checks.
+    // steps (host layers, step functions, step log), no state transitions
+    // (their capacity is checked on the host each step), graphs on, no
+    // per-operation timing or per-step checks. Births are allowed: a block
+    // is only as long as the worst-case growth keeps within capacity.
     bool multi_step_ok(bool step_log) const {
         return cuda_config.use_graphs && !cuda_config.profile_ops && !cuda_config.time_ops_in_graphs &&
                !cuda_config.check_each_step && !step_log && !has_layer_host_functions() &&
-               model->step_functions.empty() && !any_births() && !any_transitions();
+               model->step_functions.empty() && !any_transitions();
     }
 
-    // S steps as one captured graph, cached by the buffer parities at its
-    // start and every step's sort decisions.
-    void step_block(unsigned int S) {
+    // Up to Smax steps as one captured graph, cached by the buffer parities
+    // and population classes at its start and every step's sort decisions.
+    // With births, the block ends where the population bound (doubling per
+    // birth function and step) could pass a list's capacity. Returns the
+    // steps run.
+    unsigned int step_block(unsigned int Smax) {
         ensure_all_allocated();
-        prepare_capacity();
+        prepare_capacity();  // room for one step; bounds after it
         upload_env_if_dirty();
+        unsigned int S = Smax;
+        for (auto& l : lists) {
+            const int b = births_per_step(l.get());
+            if (!b) continue;
+            uint64_t cap = l->capacity;
+            if (cuda_config.max_agents) cap = std::min<uint64_t>(cap, cuda_config.max_agents);
+            unsigned int k = 1;
+            while (k < S && grow_bound(l->bound, b * static_cast<int>(k)) <= cap) ++k;
+            S = k;
+        }
         const unsigned int first = step_count;
         std::vector<int> key{-static_cast<int>(S)};
         std::vector<int> parity_before;
@@ -1254,6 +1282,7 @@ struct SimulationImpl {
             cudaGraphExec_t ge;
             FG_CUDA(cudaGraphInstantiate(&ge, g, 0));
             cudaGraphDestroy(g);
+            trim_graph_cache();
             it = graphs.emplace(key, ge).first;
         } else {
             for (size_t i = 0; i < lists.size(); ++i) lists[i]->parity = parity_before[i];
@@ -1265,7 +1294,13 @@ struct SimulationImpl {
         ++graph_launches;
         FG_CUDA(cudaEventRecord(e1, stream));
         step_events.push_back({e0, e1, S});
-        step_count += S;
+        for (auto& l : lists)  // bounds after the block's S steps (after its first: prepare_capacity)
+            l->bound = static_cast<uint32_t>(
+                std::min<uint64_t>(grow_bound(l->bound, births_per_step(l.get()) * static_cast<int>(S - 1)), 0xFFFFFFFFu));
+        step_count += S - 1;
+        record_counts();  // the counts after the block, for later bounds
+        ++step_count;
+        return S;
     }
 
     // The parity changes a step makes, replayed on the host for a cached graph.
@@ -1779,11 +1814,7 @@ void CUDASimulation::step(unsigned int n) {
         return;
     }
     constexpr unsigned int kBlock = 16;
-    while (n) {
-        const unsigned int S = n < kBlock ? n : kBlock;
-        impl->step_block(S);
-        n -= S;
-    }
+    while (n) n -= impl->step_block(n < kBlock ? n : kBlock);
 }
 
 void CUDASimulation::simulate() {
@@ -1799,11 +1830,7 @@ void CUDASimulation::simulate() {
     }
     processStepLog(0.0);  // the frame before the first step (CUDASimulation.cu:1263)
     if (impl->multi_step_ok(step_log != nullptr)) {
-        for (unsigned int n = impl->config.steps; n;) {
-            const unsigned int S = n < 16u ? n : 16u;
-            impl->step_block(S);
-            n -= S;
-        }
+        for (unsigned int n = impl->config.steps; n;) n -= impl->step_block(n < 16u ? n : 16u);
     } else {
         for (unsigned int s = 0; s < impl->config.steps; ++s) impl->step_once(this);
     }
