@@ -8,6 +8,11 @@ timings, outside the benchmark's timed loop.
   python -m flamegpu2_gb300.profile_cases ensemble --count 32
       The first `count` instances of the 256-instance Boids ensemble, 5 steps,
       as one batched simulation.
+  python -m flamegpu2_gb300.profile_cases payload --dims 2 --n 4194304
+      The large spatial workloads' model (position + 4 payload words, squared
+      distance test) at population n and the same density (2D uniform, r = 4,
+      16 agents per bin; 3D Gaussian mixture, r = 1); per-operation timings and
+      graph step time.
   python -m flamegpu2_gb300.profile_cases build --dims 3
       Five spatial message builds through the C ABI (fg_spatial_build) of the
       large workloads' positions: 8,388,608 Gaussian-mixture messages on 256^3
@@ -47,6 +52,43 @@ def boids(n: int, steps: int = 20):
     el = time.perf_counter() - t
     s.close()
     return {"n": n, "edge": edge, "ms_per_step_graph": round(el / steps * 1000, 4),
+            "ops_us": {k: round(v[0] / max(v[1], 1) * 1000, 1) for k, v in prof.items()}}
+
+
+def payload(dims: int, n: int, steps: int = 5):
+    """The large spatial workloads' model at population n and their density:
+    2D uniform (r = 4, 16 agents per bin), 3D Gaussian mixture (r = 1)."""
+    from flamegpu2_gb300 import sim, synth, workloads
+    if dims == 2:
+        r = 4.0
+        edge = float(4.0 * np.sqrt(n / 16.0))
+        hi = np.nextafter(np.float32(edge), np.float32(0))
+        pos = np.stack([np.minimum(synth.uniform(3, a, n, 0.0, edge), hi) for a in range(2)], 1)
+    else:
+        r = 1.0
+        edge = float(np.ceil(256.0 * np.cbrt(n / float(8 << 20))))
+        pos = workloads.gaussian_mixture_3d(n, edge, 16, 2.0, 2)
+    cols = {"_id": np.arange(1, n + 1, dtype=np.uint32), "x": pos[:, 0].copy(), "y": pos[:, 1].copy()}
+    if dims == 3:
+        cols["z"] = pos[:, 2].copy()
+    for k in range(4):
+        cols[f"p{k}"] = synth.uniform(3, 20 + k, n, 0.0, 1.0)
+    s = sim.Simulation("spatial_payload", [dims, 0.0, edge, r])
+    s.set_population("agent", n, cols)
+    s.step(2)
+    s.synchronize()
+    s.profile_ops(True)
+    s.step(steps)
+    prof = s.take_profile()
+    s.profile_ops(False)
+    s.step(steps)
+    s.synchronize()
+    t = time.perf_counter()
+    s.step(steps)
+    s.synchronize()
+    el = time.perf_counter() - t
+    s.close()
+    return {"dims": dims, "n": n, "edge": edge, "ms_per_step_graph": round(el / steps * 1000, 4),
             "ops_us": {k: round(v[0] / max(v[1], 1) * 1000, 1) for k, v in prof.items()}}
 
 
@@ -110,7 +152,7 @@ def build(dims: int, presorted: bool = False, reps: int = 5):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["boids", "ensemble", "build"])
+    ap.add_argument("case", choices=["boids", "ensemble", "build", "payload"])
     ap.add_argument("--dims", type=int, default=3)
     ap.add_argument("--sorted", action="store_true")
     ap.add_argument("--n", type=int, default=1 << 20)
@@ -120,6 +162,8 @@ def main():
         out = boids(a.n)
     elif a.case == "ensemble":
         out = ensemble(a.count)
+    elif a.case == "payload":
+        out = payload(a.dims, a.n)
     else:
         out = build(a.dims, a.sorted)
     print(json.dumps(out))

@@ -453,13 +453,25 @@ class MessageBruteForce {
  * the record's address — in the block's shared-memory window when the
  * message is inside it, else in HBM — computed once per message by the
  * iterator; a field read is then one load at row + field offset, the offset
- * being a per-name constant of the launch.
+ * being a per-name constant of the launch. Every spatial record starts with
+ * its location (x, y and, in 3D, z: the message type's first variables) and
+ * is 16-byte aligned, so with device checks off those reads use constant
+ * offsets from an aligned address, which the compiler can fold and merge.
  */
+template <int DIMS>
 class RecordView {
  public:
     __device__ RecordView(const detail::LaunchParams& p, uint32_t i) : P(p), index(i), row(nullptr) {}
     template <typename T>
     __device__ T getVariable(detail::VarName name) const {
+#if !FLAMEGPU_SEATBELTS
+        if constexpr (sizeof(T) == 4) {
+            const char* r = static_cast<const char*>(__builtin_assume_aligned(row, 16));
+            if (name.hash == detail::VarName("x").hash) return *reinterpret_cast<const T*>(r);
+            if (name.hash == detail::VarName("y").hash) return *reinterpret_cast<const T*>(r + 4);
+            if (DIMS == 3 && name.hash == detail::VarName("z").hash) return *reinterpret_cast<const T*>(r + 8);
+        }
+#endif
         return *reinterpret_cast<const T*>(row + detail::record_offset<T>(P, name.hash, 0));
     }
     template <typename T, flamegpu::size_type N>
@@ -534,9 +546,9 @@ class SpatialIn {
 
     class Filter {
      public:
-        class Message : public RecordView {
+        class Message : public RecordView<DIMS> {
          public:
-            __device__ Message(const detail::LaunchParams& p, uint32_t i) : RecordView(p, i) {}
+            __device__ Message(const detail::LaunchParams& p, uint32_t i) : RecordView<DIMS>(p, i) {}
         };
         class iterator {
          public:
@@ -619,21 +631,24 @@ class SpatialIn {
 
     class WrapFilter {
      public:
-        class Message : public RecordView {
+        class Message : public RecordView<DIMS> {
          public:
             __device__ Message(const detail::LaunchParams& p, uint32_t i, const WrapFilter* f)
-                : RecordView(p, i), F(f) {}
+                : RecordView<DIMS>(p, i), F(f) {}
             __device__ float getVirtualX() const { return getVirtualX(F->loc[0]); }
             __device__ float getVirtualY() const { return getVirtualY(F->loc[1]); }
             __device__ float getVirtualZ() const { return getVirtualZ(F->loc[2]); }
             __device__ float getVirtualX(float x1) const {
-                return detail::virtual_coord(x1, getVariable<float>("x"), detail::ctx().grid.width[0]);
+                return detail::virtual_coord(x1, this->template getVariable<float>("x"),
+                                             detail::ctx().grid.width[0]);
             }
             __device__ float getVirtualY(float y1) const {
-                return detail::virtual_coord(y1, getVariable<float>("y"), detail::ctx().grid.width[1]);
+                return detail::virtual_coord(y1, this->template getVariable<float>("y"),
+                                             detail::ctx().grid.width[1]);
             }
             __device__ float getVirtualZ(float z1) const {
-                return detail::virtual_coord(z1, getVariable<float>("z"), detail::ctx().grid.width[2]);
+                return detail::virtual_coord(z1, this->template getVariable<float>("z"),
+                                             detail::ctx().grid.width[2]);
             }
 
          private:
