@@ -75,8 +75,17 @@ __device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, u
     c.count = __ldg(P.batch_counts + k);
 }
 
+// Resident blocks per SM the agent-function kernels are compiled for (the
+// register budget: 65,536 / (128 x this)). 8 (at most 64 registers) unless a
+// model source defines it before including flamegpu.h, for a model whose
+// functions fit fewer registers without spilling (more warps to hide latency).
+#ifndef FLAMEGPU_AGENT_MIN_BLOCKS
+#define FLAMEGPU_AGENT_MIN_BLOCKS 8
+#endif
+
 template <typename F>
-__global__ void __launch_bounds__(kAgentBlock, 8) agent_function_kernel(const __grid_constant__ LaunchParams P) {
+__global__ void __launch_bounds__(kAgentBlock, FLAMEGPU_AGENT_MIN_BLOCKS)
+    agent_function_kernel(const __grid_constant__ LaunchParams P) {
     grid_dependency_enter();
     using MsgIn = typename F::MessageIn;
     using MsgOut = typename F::MessageOut;
