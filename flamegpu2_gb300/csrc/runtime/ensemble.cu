@@ -163,6 +163,7 @@ struct BatchedSim {
         int dims = 0;
         std::vector<uint32_t> slot_bytes, field_word;
         uint32_t record_words = 0;
+        uint32_t pay_mult = 0, pay_shift = 0, pay_stride = 0;  // record layout of the non-location fields
         std::vector<void*> cols;
         uint32_t* records = nullptr;
         uint32_t* pbm = nullptr;
@@ -298,18 +299,20 @@ struct BatchedSim {
             auto bm = std::make_unique<BMsg>();
             bm->msg = m.get();
             bm->dims = m->kind == MessageKind::Spatial3D ? 3 : (m->kind == MessageKind::Spatial2D ? 2 : 0);
-            uint32_t w = 0;
+            std::vector<std::pair<uint32_t, uint32_t>> vars;
             for (const auto& v : m->variables) {
                 const uint32_t sb = (v.bytes() + 3u) & ~3u;
                 bm->slot_bytes.push_back(sb);
-                bm->field_word.push_back(w);
-                w += sb / 4;
+                vars.emplace_back(fnv1a32(v.name), sb);
                 bm->cols.push_back(mem.get(static_cast<size_t>(sb) * total_rows));
             }
             if (bm->dims) {
-                bm->record_words = std::max(4u, (w + 3u) & ~3u);
-                if (bm->record_words > FG_MAX_RECORD_WORDS)
-                    THROW exception::InvalidMessage(format("Message '%s' is too large", m->name.c_str()));
+                const SpatialRecordLayout L = spatial_record_layout(vars, bm->dims, m->name.c_str());
+                bm->field_word = L.field_word;
+                bm->record_words = L.record_words;
+                bm->pay_mult = L.pay_mult;
+                bm->pay_shift = L.pay_shift;
+                bm->pay_stride = L.pay_stride;
                 bm->records = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * bm->record_words * static_cast<size_t>(total_rows)));
                 uint32_t bucket = 0;
                 for (uint32_t k = 0; k < ninst; ++k) {
@@ -433,10 +436,10 @@ struct BatchedSim {
         fg_record_desc rec;
         std::memset(&rec, 0, sizeof(rec));
         rec.words = m.record_words;
-        uint32_t w = 0;
         for (size_t v = 0; v < m.cols.size(); ++v) {
             const uint32_t words = m.slot_bytes[v] / 4;
-            for (uint32_t k = 0; k < words; ++k, ++w) {
+            for (uint32_t k = 0; k < words; ++k) {
+                const uint32_t w = m.field_word[v] + k;
                 rec.src[w] = static_cast<const uint32_t*>(m.cols[v]);
                 rec.src_stride[w] = words;
                 rec.src_word[w] = k;
@@ -474,6 +477,9 @@ struct BatchedSim {
             P.in_pbm = b.in->pbm;
             P.in_records = reinterpret_cast<const char*>(b.in->records);
             P.in_record_bytes = b.in->record_words * 4u;
+            P.in_pay_mult = b.in->pay_mult;
+            P.in_pay_shift = b.in->pay_shift;
+            P.in_pay_stride = b.in->pay_stride;
             if (b.sort && cfg.message_stage_bytes >= 1024u && stage_pays(*b.in)) {
                 P.stage_bytes = (cfg.message_stage_bytes + 15u) & ~15u;
                 smem = P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader));

@@ -22,6 +22,22 @@ struct TableEntry {
  * slot = (hash * mult) >> shift; throws if no multiplier up to 64 slots works. */
 VarTable make_table(const std::vector<TableEntry>& e, const char* what);
 
+/** Layout of a spatial message record: the location (x, y[, z], 4 bytes
+ *  each) at words 0..dims-1, then every other variable at word
+ *  dims + slot * stride/4, slot being its perfect-hash slot among those
+ *  variables (pay_mult, pay_shift: the device computes the same slot from the
+ *  name). A field's offset is then arithmetic on launch constants, which the
+ *  compiler hoists out of the neighbour loop, instead of a table load in it. */
+struct SpatialRecordLayout {
+    std::vector<uint32_t> field_word;  // per message variable
+    uint32_t record_words = 0;         // multiple of 4
+    uint32_t pay_mult = 0, pay_shift = 0, pay_stride = 0;  // stride: bytes per slot
+};
+/** vars: (name hash, bytes rounded up to 4) of every message variable, the
+ *  location first; throws InvalidMessage if the location is not first. */
+SpatialRecordLayout spatial_record_layout(const std::vector<std::pair<uint32_t, uint32_t>>& vars, int dims,
+                                          const char* what);
+
 // Whether a block's neighbourhood window (the sorted records from one z/y slab
 // below its lowest bin to one above its highest) is expected to fit a staging
 // buffer of stage_bytes, with per_bin messages in every bin of grid g. Staging

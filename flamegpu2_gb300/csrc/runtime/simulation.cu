@@ -166,6 +166,38 @@ VarTable make_table(const std::vector<TableEntry>& e, const char* what) {
     THROW exception::InvalidArgument(format("Too many variables (%u) in one %s for the lookup table", n, what));
 }
 
+SpatialRecordLayout spatial_record_layout(const std::vector<std::pair<uint32_t, uint32_t>>& vars, int dims,
+                                          const char* what) {
+    static const uint32_t loc[3] = {fnv1a32("x", 1), fnv1a32("y", 1), fnv1a32("z", 1)};
+    if (vars.size() < static_cast<size_t>(dims))
+        THROW exception::InvalidMessage(format("Spatial message '%s' has no location", what));
+    for (int d = 0; d < dims; ++d)
+        if (vars[d].first != loc[d] || vars[d].second != 4u)
+            THROW exception::InvalidMessage(format("Spatial message '%s' does not start with its location", what));
+    SpatialRecordLayout L;
+    std::vector<TableEntry> pay;
+    uint32_t stride = 4;
+    for (size_t v = dims; v < vars.size(); ++v) {
+        pay.push_back({vars[v].first, nullptr, 0, 4, 1});
+        stride = std::max(stride, vars[v].second);
+    }
+    const VarTable t = make_table(pay, what);
+    uint32_t slots = 0;
+    for (const auto& x : pay) slots = std::max(slots, table_slot(t.mult, t.shift, x.hash) + 1u);
+    L.pay_mult = t.mult;
+    L.pay_shift = t.shift;
+    L.pay_stride = stride;
+    for (size_t v = 0; v < vars.size(); ++v)
+        L.field_word.push_back(v < static_cast<size_t>(dims)
+                                   ? static_cast<uint32_t>(v)
+                                   : static_cast<uint32_t>(dims) + table_slot(t.mult, t.shift, vars[v].first) * (stride / 4u));
+    const uint32_t words = static_cast<uint32_t>(dims) + slots * (stride / 4u);
+    L.record_words = std::max(4u, (words + 3u) & ~3u);
+    if (L.record_words > FG_MAX_RECORD_WORDS)
+        THROW exception::InvalidMessage(format("Message '%s' is larger than %d bytes", what, FG_MAX_RECORD_WORDS * 4));
+    return L;
+}
+
 struct AgentList {
     AgentData* agent = nullptr;
     std::string state;
@@ -198,6 +230,7 @@ struct MsgList {
     uint32_t pbm_alloc = 0;
     uint32_t* records = nullptr;
     uint32_t record_words = 0;
+    uint32_t pay_mult = 0, pay_shift = 0, pay_stride = 0;  // record layout of the non-location fields
     std::vector<uint32_t> field_word;
     void* build_ws = nullptr;
     size_t build_ws_bytes = 0;
@@ -379,14 +412,15 @@ struct SimulationImpl {
                 // PBM padded to a multiple of 4 entries (+4): the staging window copies 16-byte aligned slices
                 ml->pbm_alloc = (ml->grid.binCount + 1u + 3u) & ~3u;
                 ml->pbm = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(ml->pbm_alloc) + 4)));
-                uint32_t w = 0;
-                for (uint32_t b : ml->slot_bytes) {
-                    ml->field_word.push_back(w);
-                    w += b / 4;
-                }
-                ml->record_words = std::max(4u, (w + 3u) & ~3u);
-                if (ml->record_words > FG_MAX_RECORD_WORDS)
-                    THROW exception::InvalidMessage(format("Message '%s' is larger than %d bytes", m->name.c_str(), FG_MAX_RECORD_WORDS * 4));
+                std::vector<std::pair<uint32_t, uint32_t>> vars;
+                for (size_t v = 0; v < m->variables.size(); ++v)
+                    vars.emplace_back(fnv1a32(m->variables[v].name), ml->slot_bytes[v]);
+                const SpatialRecordLayout L = spatial_record_layout(vars, dims, m->name.c_str());
+                ml->field_word = L.field_word;
+                ml->record_words = L.record_words;
+                ml->pay_mult = L.pay_mult;
+                ml->pay_shift = L.pay_shift;
+                ml->pay_stride = L.pay_stride;
             }
             msgs.push_back(std::move(ml));
         }
@@ -895,10 +929,10 @@ struct SimulationImpl {
         fg_record_desc rec;
         std::memset(&rec, 0, sizeof(rec));
         rec.words = m.record_words;
-        uint32_t w = 0;
         for (size_t v = 0; v < m.cols.size(); ++v) {
             const uint32_t words = m.slot_bytes[v] / 4;
-            for (uint32_t k = 0; k < words; ++k, ++w) {
+            for (uint32_t k = 0; k < words; ++k) {
+                const uint32_t w = m.field_word[v] + k;
                 rec.src[w] = static_cast<const uint32_t*>(m.cols[v]);
                 rec.src_stride[w] = words;
                 rec.src_word[w] = k;
@@ -1011,6 +1045,9 @@ struct SimulationImpl {
                 P.in_count = f.in->pbm + f.in->grid.binCount;
                 P.in_records = reinterpret_cast<const char*>(f.in->records);
                 P.in_record_bytes = f.in->record_words * 4u;
+                P.in_pay_mult = f.in->pay_mult;
+                P.in_pay_shift = f.in->pay_shift;
+                P.in_pay_stride = f.in->pay_stride;
                 P.in_pbm_alloc = f.in->pbm_alloc;
                 if (f.stage && cuda_config.message_stage_bytes >= 1024u &&
                     stage_window_fits(*f.in, cuda_config.message_stage_bytes))

@@ -152,6 +152,9 @@ struct LaunchParams {
     const uint32_t* in_count;    // messages in the input list
     const char* in_records;      // sorted message records (spatial input)
     uint32_t in_record_bytes;    // bytes per record (multiple of 16)
+    // record layout: location words first, then each other variable at byte
+    // 4 * dims + slot * in_pay_stride, slot = table_slot(in_pay_mult, in_pay_shift, hash)
+    uint32_t in_pay_mult, in_pay_shift, in_pay_stride;
     uint32_t in_pbm_alloc;       // PBM entries readable (multiple of 4, >= binCount + 1)
     uint32_t stage_bytes;        // shared memory for staging neighbour records (0 = off)
     // birth / death

@@ -456,7 +456,11 @@ class MessageBruteForce {
  * being a per-name constant of the launch. Every spatial record starts with
  * its location (x, y and, in 3D, z: the message type's first variables) and
  * is 16-byte aligned, so with device checks off those reads use constant
- * offsets from an aligned address, which the compiler can fold and merge.
+ * offsets from an aligned address, which the compiler can fold and merge;
+ * every other field's offset is arithmetic on launch constants (its slot in
+ * the record's own perfect hash), which the compiler hoists out of the loop.
+ * With device checks on, reads go through the checked name table, whose
+ * entries point at the same fields.
  */
 template <int DIMS>
 class RecordView {
@@ -465,22 +469,34 @@ class RecordView {
     template <typename T>
     __device__ T getVariable(detail::VarName name) const {
 #if !FLAMEGPU_SEATBELTS
+        const char* r = static_cast<const char*>(__builtin_assume_aligned(row, 16));
         if constexpr (sizeof(T) == 4) {
-            const char* r = static_cast<const char*>(__builtin_assume_aligned(row, 16));
             if (name.hash == detail::VarName("x").hash) return *reinterpret_cast<const T*>(r);
             if (name.hash == detail::VarName("y").hash) return *reinterpret_cast<const T*>(r + 4);
             if (DIMS == 3 && name.hash == detail::VarName("z").hash) return *reinterpret_cast<const T*>(r + 8);
         }
-#endif
+        return *reinterpret_cast<const T*>(r + payload_offset(name.hash));
+#else
         return *reinterpret_cast<const T*>(row + detail::record_offset<T>(P, name.hash, 0));
+#endif
     }
     template <typename T, flamegpu::size_type N>
     __device__ T getVariable(detail::VarName name, unsigned int i) const {
+#if !FLAMEGPU_SEATBELTS
+        return *reinterpret_cast<const T*>(row + payload_offset(name.hash) + static_cast<size_t>(i) * sizeof(T));
+#else
         return *reinterpret_cast<const T*>(row + detail::record_offset<T>(P, name.hash, i));
+#endif
     }
     __device__ uint32_t getIndex() const { return index; }
 
  protected:
+    // byte offset of a non-location field: arithmetic on launch constants only
+    // (the slot of the name in the record's perfect hash), so the compiler
+    // computes it once outside the neighbour loop
+    __device__ __forceinline__ uint32_t payload_offset(uint32_t hash) const {
+        return 4u * DIMS + detail::table_slot(P.in_pay_mult, P.in_pay_shift, hash) * P.in_pay_stride;
+    }
     const detail::LaunchParams& P;
 
  public:
