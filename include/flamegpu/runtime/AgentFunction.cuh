@@ -79,13 +79,15 @@ __device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, u
 // register budget: 65,536 / (128 x this)). 8 (at most 64 registers) unless a
 // model source defines it before including flamegpu.h, for a model whose
 // functions fit fewer registers without spilling (more warps to hide latency).
+// Each function also has a variant compiled for one block per SM (no register
+// cap below 255), launched when the grid is at most one block per SM: there
+// occupancy is one block anyway, and spills only lengthen each agent's chain.
 #ifndef FLAMEGPU_AGENT_MIN_BLOCKS
 #define FLAMEGPU_AGENT_MIN_BLOCKS 8
 #endif
 
-template <typename F>
-__global__ void __launch_bounds__(kAgentBlock, FLAMEGPU_AGENT_MIN_BLOCKS)
-    agent_function_kernel(const __grid_constant__ LaunchParams P) {
+template <typename F, int MINB>
+__global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const __grid_constant__ LaunchParams P) {
     grid_dependency_enter();
     using MsgIn = typename F::MessageIn;
     using MsgOut = typename F::MessageOut;
@@ -160,17 +162,34 @@ cudaError_t launch_agent_condition(const LaunchParams& p, unsigned int grid, uns
     return launch_kernel(pdl, agent_condition_kernel<C>, grid, block, 0, stream, p);
 }
 
-template <typename F>
-cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int smem,
-                                  cudaStream_t stream, bool pdl) {
+template <typename F, int MINB>
+cudaError_t launch_agent_variant(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int smem,
+                                 cudaStream_t stream, bool pdl) {
     static unsigned int configured = 48u * 1024u;
     if (smem > configured) {
-        const cudaError_t e = cudaFuncSetAttribute(agent_function_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   static_cast<int>(smem));
+        const cudaError_t e = cudaFuncSetAttribute(agent_function_kernel<F, MINB>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    return launch_kernel(pdl, agent_function_kernel<F>, grid, block, smem, stream, p);
+    return launch_kernel(pdl, agent_function_kernel<F, MINB>, grid, block, smem, stream, p);
+}
+
+inline unsigned int device_sm_count() {
+    static const unsigned int n = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return static_cast<unsigned int>(sms > 0 ? sms : 1);
+    }();
+    return n;
+}
+
+template <typename F>
+cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int smem,
+                                  cudaStream_t stream, bool pdl) {
+    if (grid <= device_sm_count()) return launch_agent_variant<F, 1>(p, grid, block, smem, stream, pdl);
+    return launch_agent_variant<F, FLAMEGPU_AGENT_MIN_BLOCKS>(p, grid, block, smem, stream, pdl);
 }
 #endif
 
