@@ -1353,20 +1353,32 @@ struct SimulationImpl {
                 }
     }
 
-    void check_errors() {
-        // the error record and every workspace's status word, read with one
-        // batch of async copies into pinned memory and one wait
+    // The error record and every workspace's status word, read with one batch
+    // of async copies into pinned memory and one wait (check_errors), or as
+    // part of a caller's batch (enqueue_status_reads, its wait, raise_status).
+    void resolve_step_timers();  // step_events -> step_ms (their steps have completed)
+    using StatusList = std::vector<std::pair<void*, std::string>>;
+    StatusList enqueue_status_reads() {
         uint32_t* hp = h_pinned + 64;
         const uint32_t cap = 1024 - 64;
         FG_CUDA(cudaMemcpyAsync(hp, d_error(), 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-        std::vector<std::pair<void*, std::string>> ws;
+        StatusList ws;
         for (auto& m : msgs)
             if (m->build_ws) ws.emplace_back(m->build_ws, format("Message '%s' index build", m->msg->name.c_str()));
         for (auto& l : lists)
             if (l->comp_ws) ws.emplace_back(l->comp_ws, format("Compaction of agent '%s'", l->agent->name.c_str()));
         for (size_t k = 0; k < ws.size() && 4 + k < cap; ++k)
             FG_CUDA(cudaMemcpyAsync(hp + 4 + k, ws[k].first, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        return ws;
+    }
+    void check_errors() {
+        const StatusList ws = enqueue_status_reads();
         FG_CUDA(cudaStreamSynchronize(stream));
+        raise_status(ws);
+    }
+    void raise_status(const StatusList& ws) {
+        uint32_t* hp = h_pinned + 64;
+        const uint32_t cap = 1024 - 64;
         uint32_t err[4] = {hp[0], hp[1], hp[2], hp[3]};
         for (size_t k = 0; k < ws.size() && 4 + k < cap; ++k) {
             const int st = static_cast<int>(static_cast<int32_t>(hp[4 + k]));
@@ -1791,9 +1803,13 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
             mx = std::max(mx, ids[i]);
         }
     }
-    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    // copies are ordered after the stream's earlier work; only growing the
+    // buffers needs the stream idle
     const uint32_t cap = impl->initial_capacity(l, n);
-    if (cap > l->capacity) impl->ensure_capacity(*l, cap, 0);
+    if (cap > l->capacity) {
+        FG_CUDA(cudaStreamSynchronize(impl->stream));
+        impl->ensure_capacity(*l, cap, 0);
+    }
     for (size_t v = 0; v < l->cols.size(); ++v) {
         const size_t b = l->agent->variables[v].bytes();
         if (n) FG_CUDA(cudaMemcpyAsync(l->cols[v][l->parity], src[v], b * n, cudaMemcpyHostToDevice, impl->stream));
@@ -1813,21 +1829,31 @@ uint32_t CUDASimulation::getPopulationColumns(const std::string& agent, const st
                                               const std::vector<std::pair<std::string, void*>>& host_out,
                                               uint32_t cap) {
     detail::AgentList* l = impl->list_of(agent, state);
-    synchronize();
-    FG_CUDA(cudaMemcpyAsync(impl->h_pinned + 3, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, impl->stream));
-    FG_CUDA(cudaStreamSynchronize(impl->stream));
-    const uint32_t n = impl->h_pinned[3];
-    l->bound = n;
-    if (n > cap) THROW exception::InvalidArgument(format("getPopulationColumns: %u agents, room for %u", n, cap));
+    std::vector<size_t> vi;
     for (const auto& o : host_out) {
         size_t v = 0;
         while (v < l->agent->variables.size() && l->agent->variables[v].name != o.first) ++v;
         if (v == l->agent->variables.size())
             THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), o.first.c_str()));
-        const size_t b = l->agent->variables[v].bytes();
-        if (n) FG_CUDA(cudaMemcpyAsync(o.second, l->cols[v][l->parity], b * n, cudaMemcpyDeviceToHost, impl->stream));
+        vi.push_back(v);
+    }
+    // one batch and one wait: status words, the count, and the rows up to the
+    // host's bound on the count (never below it), as many as the caller has room for
+    const detail::SimulationImpl::StatusList ws = impl->enqueue_status_reads();
+    FG_CUDA(cudaMemcpyAsync(impl->h_pinned + 3, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, impl->stream));
+    const uint32_t rows = std::min(std::min(cap, l->bound), l->capacity);
+    for (size_t k = 0; k < host_out.size(); ++k) {
+        const size_t b = l->agent->variables[vi[k]].bytes();
+        if (rows)
+            FG_CUDA(cudaMemcpyAsync(host_out[k].second, l->cols[vi[k]][l->parity], b * rows, cudaMemcpyDeviceToHost,
+                                    impl->stream));
     }
     FG_CUDA(cudaStreamSynchronize(impl->stream));
+    impl->raise_status(ws);
+    impl->resolve_step_timers();
+    const uint32_t n = impl->h_pinned[3];
+    l->bound = n;
+    if (n > cap) THROW exception::InvalidArgument(format("getPopulationColumns: %u agents, room for %u", n, cap));
     return n;
 }
 
@@ -1896,16 +1922,19 @@ void CUDASimulation::resetStepCounter() {
 
 void CUDASimulation::synchronize() {
     impl->check_errors();
-    // resolve the step timers
-    for (auto& e : impl->step_events) {
+    impl->resolve_step_timers();
+}
+
+void detail::SimulationImpl::resolve_step_timers() {
+    for (auto& e : step_events) {
         float ms = 0;
         cudaEventElapsedTime(&ms, e.e0, e.e1);
         // steps replayed as one graph share its time equally
-        for (unsigned int k = 0; k < e.steps; ++k) impl->step_ms.push_back(ms / e.steps);
+        for (unsigned int k = 0; k < e.steps; ++k) step_ms.push_back(ms / e.steps);
         cudaEventDestroy(e.e0);
         cudaEventDestroy(e.e1);
     }
-    impl->step_events.clear();
+    step_events.clear();
 }
 
 double CUDASimulation::getElapsedTimeSimulation() const { return impl->sim_ms / 1000.0; }
