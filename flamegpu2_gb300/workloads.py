@@ -43,21 +43,21 @@ def _stage_table(prof: dict, algo: dict, per_launch: bool = True) -> dict:
     return out
 
 
-def profiled_traffic(summary: str):
+def profiled_traffic(summary: str, key: str = ""):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
     a workload's roofline kernel, from one ncu capture summarised in
-    profiles/<summary>.md (line 'traffic_bytes_per_launch: N'); None if absent."""
+    profiles/<summary>.md (line '[key ]traffic_bytes_per_launch: N'); None if absent."""
     import re
     try:
         with open(os.path.join(ROOT, "profiles", summary + ".md")) as f:
-            m = re.search(r"^traffic_bytes_per_launch:\s*(\d+)", f.read(), re.M)
+            m = re.search(r"^" + re.escape((key + " ") if key else "") + r"traffic_bytes_per_launch:\s*(\d+)", f.read(), re.M)
     except OSError:
         return None
     return int(m.group(1)) if m else None
 
 
-def _with_traffic(roof: dict, summary: str, what: str = None) -> dict:
-    t = profiled_traffic(summary)
+def _with_traffic(roof: dict, summary: str, what: str = None, key: str = "") -> dict:
+    t = profiled_traffic(summary, key)
     if t is not None:
         roof["traffic"] = t
         roof["traffic_source"] = f"profiles/{summary}.md" + (f": {what}" if what else "")
@@ -269,6 +269,7 @@ def run_spatial_large(name, args, world, rank, local):
             "frac": round(bd["gbs"] / peak, 4) if bd.get("gbs") else None, "traffic": None,
             "peak_source": peak_kind, "per_launch_algorithmic_bytes": algo["build:location"],
             "note": "iterate is on-chip bound here (see stages.fn:in.candidate_pairs_per_s)"}
+    roof = _with_traffic(roof, "spatial_large_build", "the five build kernels of one standalone build of this size", name)
     return {
         "metric": B.METRIC, "value": round(n * k_steps * world / (device_ms / 1000.0), 1), "unit": UNIT,
         "n_gpus": world, "steps": k_steps, "warmup": args.warmup, "ms_per_step": round(device_ms / k_steps, 4),
