@@ -9,9 +9,10 @@
 //   k_stabilize  per sorted position: restores ascending original index inside
 //                short bins (<= kShortBin) and emits the record (or index);
 //                long bins are queued as 256-element chunks
-//   k_long       orders long bins: up to 8192 messages by a bitmap over the
-//                span of their indices (narrow spans) or a bitonic sort in
-//                shared memory, longer ones by ranking each 256-element chunk
+//   k_long       orders long bins: up to 1024 messages one warp each (a
+//                bitmap over their indices), up to 8192 one block each (a
+//                bitmap over the span of their indices, or a bitonic sort in
+//                shared memory), longer ones by ranking each 256-element chunk
 //                against the whole bin
 // The automatic agent sort runs the same pipeline on the reference's sort key;
 // its k_stabilize / k_long write every agent column at the stable position.
@@ -333,7 +334,10 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
 }
 
 // Long bins. A bin of up to kSortCap messages is ordered by one block (the
-// bin's chunk 0; its other chunks are skipped). When its original indices
+// bin's chunk 0; its other chunks are skipped). When its original indices are
+// distinct values filling [min, max] (messages of agents in bin order), the
+// k-th smallest is min + k and they are copied in that order, without ranking.
+// Otherwise, when its original indices
 // span at most kSpanCap values (messages that arrive nearly in bin order, as
 // those of spatially sorted agents do), each index sets one bit of a bitmap
 // over that span and its rank is the number of set bits before it: O(length
@@ -343,6 +347,12 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
 constexpr uint32_t kSortCap = 8192;
 constexpr uint32_t kSpanWords = kSortCap / 2;   // bitmap words; the other half holds their prefix counts
 constexpr uint32_t kSpanCap = kSpanWords * 32;  // 131,072 indices
+// Bins of up to kWarpBin messages (most long bins of clustered inputs) are
+// ordered first, one warp each and without block barriers: a bitmap over
+// their indices when those span at most kWarpSpanWords * 32 values, else each
+// message ranked against the bin. The block pass then takes the longer ones.
+constexpr uint32_t kWarpBin = 1024;
+constexpr uint32_t kWarpSpanWords = 128;
 
 template <int EMIT>
 __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitParams rp,
@@ -354,11 +364,82 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
     __shared__ uint32_t s_idx[kSortCap];
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_lo, s_hi;
+    __shared__ uint32_t s_wbits[kThreads / 32][kWarpSpanWords];
+    __shared__ uint32_t s_wpre[kThreads / 32][kWarpSpanWords];
     const uint32_t nchunks = min(h->long_count, chunk_cap);
+    // warp pass: bins of up to kWarpBin messages
+    {
+        const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+        uint32_t* bits = s_wbits[wib];
+        uint32_t* pre = s_wpre[wib];
+        for (uint32_t c = blockIdx.x * (kThreads / 32) + wib; c < nchunks; c += gridDim.x * (kThreads / 32)) {
+            const uint2 ch = chunk_list[c];
+            const uint32_t s = pbm[ch.x], e = pbm[ch.x + 1];
+            const uint32_t len = e - s;
+            if (len > kWarpBin || ch.y != 0) continue;  // the same for every lane
+            uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+            for (uint32_t k = lane; k < len; k += 32u) {
+                const uint32_t i = perm[s + k];
+                lo = min(lo, i);
+                hi = max(hi, i);
+            }
+            lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+            hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+            if (hi - lo == len - 1u) {  // distinct indices filling [lo, hi]: already ascending from lo
+                for (uint32_t k = lane; k < len; k += 32u) emit<EMIT>(rp, sperm, lo + k, s + k);
+            } else if (hi - lo < kWarpSpanWords * 32u) {
+                const uint32_t words = (hi - lo) / 32u + 1u;
+                for (uint32_t w = lane; w < words; w += 32u) bits[w] = 0u;
+                __syncwarp();
+                for (uint32_t k = lane; k < len; k += 32u) {
+                    const uint32_t d = perm[s + k] - lo;
+                    atomicOr(&bits[d >> 5], 1u << (d & 31u));
+                }
+                __syncwarp();
+                // set bits before each word: lane l sums words 4l..4l+3, a warp scan offsets them
+                uint32_t cnt[4], sum = 0;
+#pragma unroll
+                for (uint32_t j = 0; j < 4; ++j) {
+                    const uint32_t w = lane * 4u + j;
+                    cnt[j] = w < words ? __popc(bits[w]) : 0u;
+                    sum += cnt[j];
+                }
+                uint32_t inc = sum;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+                    if (lane >= static_cast<uint32_t>(d)) inc += t;
+                }
+                uint32_t ex = inc - sum;
+#pragma unroll
+                for (uint32_t j = 0; j < 4; ++j) {
+                    const uint32_t w = lane * 4u + j;
+                    if (w < words) pre[w] = ex;
+                    ex += cnt[j];
+                }
+                __syncwarp();
+                for (uint32_t k = lane; k < len; k += 32u) {
+                    const uint32_t i = perm[s + k];
+                    const uint32_t d = i - lo;
+                    emit<EMIT>(rp, sperm, i, s + pre[d >> 5] + __popc(bits[d >> 5] & ((1u << (d & 31u)) - 1u)));
+                }
+                __syncwarp();  // bits and pre are reused by the warp's next bin
+            } else {
+                for (uint32_t k = lane; k < len; k += 32u) {
+                    const uint32_t i = perm[s + k];
+                    uint32_t rank = 0;
+                    for (uint32_t u = s; u < e; ++u) rank += perm[u] < i ? 1u : 0u;
+                    emit<EMIT>(rp, sperm, i, s + rank);
+                }
+            }
+        }
+    }
+    // block pass: longer bins
     for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint2 ch = chunk_list[c];
         const uint32_t s = pbm[ch.x], e = pbm[ch.x + 1];
         const uint32_t len = e - s;
+        if (len <= kWarpBin) continue;  // done by the warp pass
         if (len <= kSortCap) {
             if (ch.y != 0) continue;  // the bin's chunk 0 orders the whole bin
             // span of the bin's original indices
@@ -383,6 +464,10 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
             __syncthreads();
             lo = s_lo;
             hi = s_hi;
+            if (hi - lo == len - 1u) {  // distinct indices filling [lo, hi]: already ascending from lo
+                for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) emit<EMIT>(rp, sperm, lo + k, s + k);
+                continue;
+            }
             if (hi - lo < kSpanCap) {
                 const uint32_t words = (hi - lo) / 32u + 1u;
                 uint32_t* bits = s_idx;

@@ -208,6 +208,35 @@ def test_build_long_bins_sorted_and_ranked():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("order", ["bins", "local", "displaced"])
+def test_build_long_bins_in_bin_order(order):
+    # messages that arrive grouped by bin, as those of spatially sorted agents
+    # do: each bin's indices contiguous ("bins"), shuffled within windows of 64
+    # ("local"), or 1% of them exchanged at random ("displaced")
+    rng = np.random.default_rng(31)
+    g = _capi().grid(3, (0, 0, 0), (8, 8, 8), 1.0)
+    sizes = [33, 100, 500, 1000, 1024, 1025, 3000, 8192, 8193, 20000, 1, 31, 32]
+    cells = rng.choice(512, len(sizes), replace=False)
+    pos = []
+    for c, k in zip(cells, sizes):
+        cx, cy, cz = c % 8, (c // 8) % 8, c // 64
+        pos.append(np.stack([cx + rng.uniform(0.01, 0.99, k), cy + rng.uniform(0.01, 0.99, k),
+                             cz + rng.uniform(0.01, 0.99, k)], 1))
+    pos = np.concatenate(pos).astype(np.float32)
+    n = len(pos)
+    if order == "local":
+        pos = pos[np.argsort(np.arange(n) // 64 + rng.random(n), kind="stable")]
+    elif order == "displaced":
+        sel = rng.choice(n, n // 100, replace=False)
+        pos[sel] = pos[rng.permutation(sel)]
+    pbm, srt, payload, _ = _build(g, pos, reps=2)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    np.testing.assert_array_equal(srt[:n, 0:3].view(np.float32), pos[eperm])
+    np.testing.assert_array_equal(srt[:n, 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
 def test_build_mixed_buckets_under_16k():
     # a list of under 16,384 messages with short, warp-sized and long buckets,
     # messages of all buckets interleaved at random
