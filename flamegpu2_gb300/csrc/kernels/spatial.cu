@@ -295,6 +295,45 @@ __device__ __forceinline__ void emit(const EmitParams& ep, uint32_t* sperm, uint
     }
 }
 
+// Messages lo .. lo + len - 1 written at s .. s + len - 1 (a bin whose
+// original indices are already in order) by threads t, t + nt, ... of the
+// caller. Records of up to 8 words go four messages per thread at a time,
+// every load issued before any store, so each thread keeps four messages'
+// loads in flight instead of one.
+template <int EMIT>
+__device__ __forceinline__ void emit_run(const EmitParams& ep, uint32_t* sperm, uint32_t lo, uint32_t s,
+                                         uint32_t len, uint32_t t, uint32_t nt) {
+    if (EMIT == kEmitRecord && ep.rp.rec.words <= 8) {
+        const fg_record_desc& rec = ep.rp.rec;
+        const uint32_t words = rec.words;  // 4 or 8: records are 16-byte aligned
+        for (uint32_t k0 = t; k0 < len; k0 += 4 * nt) {
+            uint32_t v[4][8];
+#pragma unroll
+            for (uint32_t m = 0; m < 4; ++m) {
+                const uint32_t k = k0 + m * nt;
+#pragma unroll
+                for (uint32_t w = 0; w < 8; ++w) {
+                    const uint32_t* src = w < words ? rec.src[w] : nullptr;
+                    v[m][w] = (k < len && src)
+                                  ? ld_nc_u32(src + static_cast<size_t>(lo + k) * rec.src_stride[w] + rec.src_word[w])
+                                  : 0u;
+                }
+            }
+#pragma unroll
+            for (uint32_t m = 0; m < 4; ++m) {
+                const uint32_t k = k0 + m * nt;
+                if (k < len) {
+                    uint4* o = reinterpret_cast<uint4*>(ep.rp.out + static_cast<size_t>(s + k) * words);
+                    o[0] = make_uint4(v[m][0], v[m][1], v[m][2], v[m][3]);
+                    if (words > 4) o[1] = make_uint4(v[m][4], v[m][5], v[m][6], v[m][7]);
+                }
+            }
+        }
+        return;
+    }
+    for (uint32_t k = t; k < len; k += nt) emit<EMIT>(ep, sperm, lo + k, s + k);
+}
+
 // Sorted positions p < total = pbm[nbuckets]. Short bins are ranked in place
 // (count of smaller original indices in the bin); long bins are queued as
 // chunks (bucket, chunk index) for k_long.
@@ -386,7 +425,7 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
             lo = __reduce_min_sync(0xFFFFFFFFu, lo);
             hi = __reduce_max_sync(0xFFFFFFFFu, hi);
             if (hi - lo == len - 1u) {  // distinct indices filling [lo, hi]: already ascending from lo
-                for (uint32_t k = lane; k < len; k += 32u) emit<EMIT>(rp, sperm, lo + k, s + k);
+                emit_run<EMIT>(rp, sperm, lo, s, len, lane, 32u);
             } else if (hi - lo < kWarpSpanWords * 32u) {
                 const uint32_t words = (hi - lo) / 32u + 1u;
                 for (uint32_t w = lane; w < words; w += 32u) bits[w] = 0u;
@@ -465,7 +504,7 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
             lo = s_lo;
             hi = s_hi;
             if (hi - lo == len - 1u) {  // distinct indices filling [lo, hi]: already ascending from lo
-                for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) emit<EMIT>(rp, sperm, lo + k, s + k);
+                emit_run<EMIT>(rp, sperm, lo, s, len, threadIdx.x, blockDim.x);
                 continue;
             }
             if (hi - lo < kSpanCap) {
