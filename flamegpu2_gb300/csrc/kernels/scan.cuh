@@ -97,32 +97,22 @@ __device__ __forceinline__ uint32_t lookback_u32(const uint64_t* status, uint32_
 }
 
 // Exclusive scan of in[0..n) into out[0..n). If zero_in, in[] is cleared to 0
-// after it has been read (in != out). Launch with ceil(n / kScanTile) blocks of
-// kThreads threads. With self_reset the last block to finish resets the ticket
-// and advances the epoch for the next scan on this workspace; without it the
-// kernel launched just before this one has done so (scan_reset), which spares
-// every block a fence and an atomic at its end.
+// after it has been read (in != out). A tile is R sub-tiles of kScanTile
+// values: the block sums them (R block scans), publishes the tile's total and
+// looks back once, then reads them again (from L2) to write the prefixes. A
+// look-back resolves at most 32 tiles per round of the inclusive-prefix
+// frontier, so large scans take R = 4 and need a quarter of the rounds. With
+// self_reset the last block to finish resets the ticket and advances the epoch
+// for the next scan on this workspace; without it the kernel launched just
+// before this one has done so (scan_reset), which spares every block a fence
+// and an atomic at its end.
 __device__ __forceinline__ void scan_reset(WsHeader* h) {
     h->scan_ticket = 0u;
     h->scan_epoch = (h->scan_epoch + 1u) & 0x3FFFFFFFu;
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
-                                                       uint64_t* status, WsHeader* h, int self_reset) {
-    flamegpu::detail::grid_dependency_enter();
-    __shared__ uint32_t s_tile, s_epoch;
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_excl;
-    if (threadIdx.x == 0) {
-        s_tile = atomicAdd(&h->scan_ticket, 1u);
-        s_epoch = ld_acquire_u32(&h->scan_epoch);
-    }
-    __syncthreads();
-    const uint32_t tile = s_tile, epoch = s_epoch;
-    const uint64_t base = static_cast<uint64_t>(tile) * kScanTile + static_cast<uint64_t>(threadIdx.x) * kScanItems;
-    uint32_t v[kScanItems];
-    const bool full = base + kScanItems <= n;
-    const bool vec = full && ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
+__device__ __forceinline__ void scan_load(const uint32_t* in, uint64_t base, uint32_t n, bool vec,
+                                          uint32_t (&v)[kScanItems]) {
     if (vec) {
         const uint4* p = reinterpret_cast<const uint4*>(in + base);
 #pragma unroll
@@ -134,51 +124,85 @@ __global__ void __launch_bounds__(kThreads) k_scan_u32(const uint32_t* in, uint3
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) v[k] = (base + k < n) ? in[base + k] : 0u;
     }
-    uint32_t tsum = 0;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
+                                                       uint64_t* status, WsHeader* h, int self_reset) {
+    flamegpu::detail::grid_dependency_enter();
+    __shared__ uint32_t s_tile, s_epoch;
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_excl;
+    if (threadIdx.x == 0) {
+        s_tile = atomicAdd(&h->scan_ticket, 1u);
+        s_epoch = ld_acquire_u32(&h->scan_epoch);
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile, epoch = s_epoch;
+    const bool in_al = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
+    const bool out_al = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    uint32_t v[kScanItems];
+    uint32_t texcl[R];  // this thread's prefix inside the tile, per sub-tile
+    uint32_t ttotal = 0;
+    const uint64_t base0 = static_cast<uint64_t>(tile) * R * kScanTile + threadIdx.x * kScanItems;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) tsum += v[k];
-    uint32_t btotal;
-    const uint32_t texcl = block_exclusive_scan(tsum, &btotal, s_warp);
+    for (int r = 0; r < R; ++r) {
+        const uint64_t base = base0 + r * kScanTile;
+        scan_load(in, base, n, in_al && base + kScanItems <= n, v);
+        uint32_t tsum = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) tsum += v[k];
+        uint32_t btotal;
+        texcl[r] = ttotal + block_exclusive_scan(tsum, &btotal, s_warp);
+        ttotal += btotal;
+        if (R > 1) __syncthreads();  // s_warp is reused by the next sub-tile's scan
+    }
     // publish this tile and look back
     if (threadIdx.x < 32) {
         uint32_t excl = 0;
         if (tile == 0) {
-            if (threadIdx.x == 0) st_release_u64(status, scan_pack(2, epoch, btotal));
+            if (threadIdx.x == 0) st_release_u64(status, scan_pack(2, epoch, ttotal));
         } else {
-            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(1, epoch, btotal));
+            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(1, epoch, ttotal));
             excl = lookback_u32(status, tile, epoch, h);
-            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(2, epoch, excl + btotal));
+            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(2, epoch, excl + ttotal));
         }
         if (threadIdx.x == 0) s_excl = excl;
     }
     __syncthreads();
-    uint32_t run = s_excl + texcl;
-    uint32_t o[kScanItems];
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        o[k] = run;
-        run += v[k];
-    }
-    const bool ovec = full && ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
-    if (ovec) {
-        uint4* p = reinterpret_cast<uint4*>(out + base);
+    for (int r = 0; r < R; ++r) {
+        const uint64_t base = base0 + r * kScanTile;
+        const bool full = base + kScanItems <= n;
+        if (R > 1) scan_load(in, base, n, in_al && full, v);  // the one sub-tile of R = 1 is still held
+        uint32_t run = s_excl + texcl[r];
+        uint32_t o[kScanItems];
 #pragma unroll
-        for (int k = 0; k < kScanItems / 4; ++k) p[k] = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
-    } else {
+        for (int k = 0; k < kScanItems; ++k) {
+            o[k] = run;
+            run += v[k];
+        }
+        if (full && out_al) {
+            uint4* p = reinterpret_cast<uint4*>(out + base);
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k)
-            if (base + k < n) out[base + k] = o[k];
-    }
-    if (zero_in) {
-        uint32_t* zin = const_cast<uint32_t*>(in);
-        if (vec) {
-            uint4* p = reinterpret_cast<uint4*>(zin + base);
-#pragma unroll
-            for (int k = 0; k < kScanItems / 4; ++k) p[k] = make_uint4(0, 0, 0, 0);
+            for (int k = 0; k < kScanItems / 4; ++k)
+                p[k] = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
         } else {
 #pragma unroll
             for (int k = 0; k < kScanItems; ++k)
-                if (base + k < n) zin[base + k] = 0;
+                if (base + k < n) out[base + k] = o[k];
+        }
+        if (zero_in) {
+            uint32_t* zin = const_cast<uint32_t*>(in);
+            if (full && in_al) {
+                uint4* p = reinterpret_cast<uint4*>(zin + base);
+#pragma unroll
+                for (int k = 0; k < kScanItems / 4; ++k) p[k] = make_uint4(0, 0, 0, 0);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kScanItems; ++k)
+                    if (base + k < n) zin[base + k] = 0;
+            }
         }
     }
     if (!self_reset) return;
@@ -195,6 +219,19 @@ __global__ void __launch_bounds__(kThreads) k_scan_u32(const uint32_t* in, uint3
     }
 }
 
+// Tiles of a scan of n values with one sub-tile per tile (an upper bound on
+// the tiles of any scan of n values: sizes the status array).
 inline uint32_t scan_tiles(uint32_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+// Scans of more than this many values take four sub-tiles per tile.
+constexpr uint32_t kScanWideMin = 1u << 22;
+
+inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in, uint64_t* status,
+                               WsHeader* h, int self_reset, cudaStream_t st) {
+    if (n > kScanWideMin)
+        return launch(k_scan_u32<4>, (n + 4u * kScanTile - 1) / (4u * kScanTile), kThreads, st, in, out, n, zero_in,
+                      status, h, self_reset);
+    return launch(k_scan_u32<1>, scan_tiles(n), kThreads, st, in, out, n, zero_in, status, h, self_reset);
+}
 
 }  // namespace fgk

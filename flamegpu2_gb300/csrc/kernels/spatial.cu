@@ -388,10 +388,12 @@ constexpr uint32_t kSpanWords = kSortCap / 2;   // bitmap words; the other half 
 constexpr uint32_t kSpanCap = kSpanWords * 32;  // 131,072 indices
 // Bins of up to kWarpBin messages (most long bins of clustered inputs) are
 // ordered first, one warp each and without block barriers: a bitmap over
-// their indices when those span at most kWarpSpanWords * 32 values, else each
-// message ranked against the bin. The block pass then takes the longer ones.
+// their indices when those span at most kWarpSpanWords * 32 values, else a
+// bitonic sort of the indices in the warp's slice of shared memory. The block
+// pass then takes the longer ones.
 constexpr uint32_t kWarpBin = 1024;
 constexpr uint32_t kWarpSpanWords = 128;
+static_assert((kThreads / 32) * kWarpBin <= kSortCap, "a warp's bitonic slice lies in s_idx");
 
 template <int EMIT>
 __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitParams rp,
@@ -464,12 +466,30 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
                 }
                 __syncwarp();  // bits and pre are reused by the warp's next bin
             } else {
-                for (uint32_t k = lane; k < len; k += 32u) {
-                    const uint32_t i = perm[s + k];
-                    uint32_t rank = 0;
-                    for (uint32_t u = s; u < e; ++u) rank += perm[u] < i ? 1u : 0u;
-                    emit<EMIT>(rp, sperm, i, s + rank);
+                // indices spread wider: bitonic sort in the warp's slice of s_idx
+                // (the block pass below writes s_idx only after a block barrier)
+                uint32_t* w = s_idx + wib * kWarpBin;
+                uint32_t p2 = 32;
+                while (p2 < len) p2 <<= 1;
+                for (uint32_t k = lane; k < p2; k += 32u) w[k] = k < len ? perm[s + k] : 0xFFFFFFFFu;
+                __syncwarp();
+                for (uint32_t k = 2; k <= p2; k <<= 1) {
+                    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                        for (uint32_t t = lane; t < p2; t += 32u) {
+                            const uint32_t u = t ^ j;
+                            if (u > t) {
+                                const uint32_t a = w[t], b = w[u];
+                                if (((t & k) == 0) == (a > b)) {
+                                    w[t] = b;
+                                    w[u] = a;
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
                 }
+                for (uint32_t k = lane; k < len; k += 32u) emit<EMIT>(rp, sperm, w[k], s + k);
+                __syncwarp();  // w is reused by the warp's next bin
             }
         }
     }
@@ -745,7 +765,7 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     else
         launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
     const uint32_t scan_n = nbuckets + 1;
-    launch(k_scan_u32, scan_tiles(scan_n), kThreads, st, hist, pbm_out, scan_n, 1, sstat, h, 0);
+    launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
     launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
     launch(k_long<EMIT>, static_cast<uint32_t>(sm_count() * 4), kThreads, st, rp, pbm_out, perm, sperm, chunks,
@@ -813,8 +833,8 @@ extern "C" int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t
         return FG_ERR_WORKSPACE;
     if (!n) return FG_OK;
     char* ws = static_cast<char*>(workspace);
-    launch(k_scan_u32, scan_tiles(n), kThreads, static_cast<cudaStream_t>(stream), in, out, n, 0,
-           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws), 1);
+    launch_scan(in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws), 1,
+                static_cast<cudaStream_t>(stream));
     return check_launch();
 }
 
@@ -877,8 +897,8 @@ extern "C" int fg_exclusive_scan_u32_noalloc(const uint32_t* in, uint32_t* out, 
     const int rc = noalloc_scratch(&ws);
     if (rc != FG_OK) return rc;
     if (!n) return FG_OK;
-    launch(k_scan_u32, scan_tiles(n), kThreads, static_cast<cudaStream_t>(stream), in, out, n, 0,
-           reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws), 1);
+    launch_scan(in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws), 1,
+                static_cast<cudaStream_t>(stream));
     return check_launch();
 }
 

@@ -237,6 +237,20 @@ def test_build_long_bins_in_bin_order(order):
 
 
 @pytest.mark.gpu
+def test_build_on_256_cubed_bins():
+    # 16,777,216 bins: the PBM scan takes four sub-tiles per tile; two builds
+    # on one workspace check that the histogram is left cleared
+    rng = np.random.default_rng(41)
+    g = _capi().grid(3, (0, 0, 0), (256, 256, 256), 1.0)
+    pos = _positions(rng, 200_000, (0, 0, 0), (256, 256, 256), "clusters")
+    pbm, srt, payload, _ = _build(g, pos, reps=2)
+    epbm, eperm = _expect(g, pos)
+    np.testing.assert_array_equal(pbm, epbm)
+    np.testing.assert_array_equal(srt[:len(pos), 0:3].view(np.float32), pos[eperm])
+    np.testing.assert_array_equal(srt[:len(pos), 3:6].view(np.int32), payload[eperm])
+
+
+@pytest.mark.gpu
 def test_build_mixed_buckets_under_16k():
     # a list of under 16,384 messages with short, warp-sized and long buckets,
     # messages of all buckets interleaved at random
@@ -281,7 +295,7 @@ def test_build_one_bucket_and_optional_at_16k(n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n", [1, 4095, 4096, 4097, 1_000_000, 17_000_001])
+@pytest.mark.parametrize("n", [1, 4095, 4096, 4097, 1_000_000, 4_194_304, 4_194_305, 16_777_217, 17_000_001])
 def test_exclusive_scan(n):
     import torch
     capi = _capi()
