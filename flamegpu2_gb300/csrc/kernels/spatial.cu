@@ -229,6 +229,7 @@ __device__ __forceinline__ void emit_record(const RecordParams& rp, uint32_t i, 
 struct ColumnParams {
     fg_column col[FG_MAX_COLUMNS];
     uint32_t ncols;
+    uint32_t keep_perm;  // also write the stable permutation (the caller asked for it)
 };
 
 template <typename T>
@@ -290,7 +291,7 @@ __device__ __forceinline__ void emit(const EmitParams& ep, uint32_t* sperm, uint
     if (EMIT == kEmitRecord) {
         emit_record(ep.rp, i, dst);
     } else {
-        sperm[dst] = i;
+        if (EMIT == kEmitPerm || ep.cp.keep_perm) sperm[dst] = i;
         if (EMIT == kEmitPermColumns) emit_columns(ep.cp, i, dst);
     }
 }
@@ -327,6 +328,41 @@ __device__ __forceinline__ void emit_run(const EmitParams& ep, uint32_t* sperm, 
                     o[0] = make_uint4(v[m][0], v[m][1], v[m][2], v[m][3]);
                     if (words > 4) o[1] = make_uint4(v[m][4], v[m][5], v[m][6], v[m][7]);
                 }
+            }
+        }
+        return;
+    }
+    if (EMIT == kEmitPermColumns) {
+        // every column a straight copy of [lo, lo + len) to [s, s + len); runs of
+        // four 4-byte columns go four rows at a time (16 loads before any store)
+        const ColumnParams& cp = ep.cp;
+        if (cp.keep_perm)
+            for (uint32_t k = t; k < len; k += nt) sperm[s + k] = lo + k;
+        for (uint32_t c0 = 0; c0 < cp.ncols; c0 += 4) {
+            const uint32_t nk = min(4u, cp.ncols - c0);
+            bool words = true;
+            for (uint32_t c = 0; c < nk; ++c) words = words && cp.col[c0 + c].elem_bytes == 4u;
+            if (!words) {
+                for (uint32_t c = 0; c < nk; ++c)
+                    for (uint32_t k = t; k < len; k += nt) copy_column_elem(cp.col[c0 + c], lo + k, s + k);
+                continue;
+            }
+            for (uint32_t k0 = t; k0 < len; k0 += 4 * nt) {
+                uint32_t v[4][4];
+#pragma unroll
+                for (uint32_t c = 0; c < 4; ++c)
+#pragma unroll
+                    for (uint32_t m = 0; m < 4; ++m) {
+                        const uint32_t k = k0 + m * nt;
+                        v[c][m] = (c < nk && k < len) ? static_cast<const uint32_t*>(cp.col[c0 + c].in)[lo + k] : 0u;
+                    }
+#pragma unroll
+                for (uint32_t c = 0; c < 4; ++c)
+#pragma unroll
+                    for (uint32_t m = 0; m < 4; ++m) {
+                        const uint32_t k = k0 + m * nt;
+                        if (c < nk && k < len) static_cast<uint32_t*>(cp.col[c0 + c].out)[s + k] = v[c][m];
+                    }
             }
         }
         return;
@@ -810,6 +846,7 @@ extern "C" int fg_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, 
     EmitParams rp{};
     for (uint32_t c = 0; c < ncols; ++c) rp.cp.col[c] = cols[c];
     rp.cp.ncols = ncols;
+    rp.cp.keep_perm = perm_out != nullptr;
     int rc = ncols ? run_pipeline<kSortKey, kEmitPermColumns>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
                                                               reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st)
                    : run_pipeline<kSortKey, kEmitPerm>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
@@ -996,6 +1033,7 @@ extern "C" int fg_spatial_sort_agents_batched(const fg_batch_instance* instances
     EmitParams rp{};
     for (uint32_t c = 0; c < ncols; ++c) rp.cp.col[c] = cols[c];
     rp.cp.ncols = ncols;
+    rp.cp.keep_perm = 0;  // the batched sort returns columns only
     SortGrid sg{};
     BatchKeys bk;
     bk.inst = instances;

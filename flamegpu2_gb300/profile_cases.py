@@ -20,6 +20,10 @@ timings, outside the benchmark's timed loop.
       records of position + 4 payload words; prints the mean build time.
       --sorted orders the messages by bin first, as the messages of agents
       that the automatic spatial sort has ordered arrive in a simulation.
+  python -m flamegpu2_gb300.profile_cases sort --dims 3 --sorted
+      Five automatic spatial agent sorts through the C ABI
+      (fg_spatial_sort_agents) of the same positions with their agent columns
+      (8 x 4 bytes in 3D, 7 in 2D); --sorted gives an already sorted population.
 """
 from __future__ import annotations
 
@@ -150,9 +154,53 @@ def build(dims: int, presorted: bool = False, reps: int = 5):
             "build_us": round(a.elapsed_time(b) * 1000 / reps, 1)}
 
 
+def sort(dims: int, presorted: bool = False, reps: int = 5):
+    """Automatic spatial agent sorts through the C ABI (fg_spatial_sort_agents)
+    of the large workloads' populations: positions as in `build`, eight 4-byte
+    columns in 3D (x, y, z, four payload words, an id), seven in 2D."""
+    import ctypes as C
+    import torch
+    from flamegpu2_gb300 import capi, synth, workloads
+    if dims == 3:
+        pos = workloads.gaussian_mixture_3d(1 << 23, 256.0, 16, 2.0, 2)
+        g = capi.grid(3, (0, 0, 0), (256, 256, 256), 1.0)
+    else:
+        n = 1 << 24
+        hi = np.nextafter(np.float32(4096.0), np.float32(0))
+        pos = np.stack([np.minimum(synth.uniform(3, a, n, 0.0, 4096.0), hi) for a in range(2)], 1)
+        g = capi.grid(2, (0, 0), (4096, 4096), 4.0)
+    n = pos.shape[0]
+    if presorted:
+        cell = [np.clip(np.floor((pos[:, a] - np.float32(g.min[a])) / np.float32(g.radius)).astype(np.int64), 0,
+                        g.gridDim[a] - 1) for a in range(dims)]
+        key = cell[0] + cell[1] * g.gridDim[0] + (cell[2] * g.gridDim[0] * g.gridDim[1] if dims == 3 else 0)
+        pos = pos[np.argsort(key, kind="stable")]
+    ins = [torch.from_numpy(np.ascontiguousarray(pos[:, a])).cuda() for a in range(dims)]
+    ins += [torch.rand(n, device="cuda") for _ in range(4)]
+    ins.append(torch.arange(1, n + 1, dtype=torch.int32, device="cuda"))
+    outs = [torch.empty_like(c) for c in ins]
+    colarr = capi.columns(list(zip(ins, outs)))
+    perm = torch.empty(n, dtype=torch.int32, device="cuda")
+    ws = capi.Workspace(capi.lib().fg_spatial_sort_workspace_size(n, C.byref(g)))
+    st = capi.stream_handle()
+    args = (C.byref(g), n, None, ins[0].data_ptr(), ins[1].data_ptr(), ins[2].data_ptr() if dims == 3 else None,
+            colarr, len(ins), perm.data_ptr(), ws.ptr, ws.nbytes, st)
+    capi.check(capi.lib().fg_spatial_sort_agents(*args), "fg_spatial_sort_agents")
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        capi.check(capi.lib().fg_spatial_sort_agents(*args), "fg_spatial_sort_agents")
+    b.record()
+    b.synchronize()
+    assert ws.status() == 0
+    return {"dims": dims, "sorted_input": presorted, "agents": n, "columns": len(ins), "sort_us":
+            round(a.elapsed_time(b) * 1000 / reps, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["boids", "ensemble", "build", "payload"])
+    ap.add_argument("case", choices=["boids", "ensemble", "build", "payload", "sort"])
     ap.add_argument("--dims", type=int, default=3)
     ap.add_argument("--sorted", action="store_true")
     ap.add_argument("--n", type=int, default=1 << 20)
@@ -164,6 +212,8 @@ def main():
         out = ensemble(a.count)
     elif a.case == "payload":
         out = payload(a.dims, a.n)
+    elif a.case == "sort":
+        out = sort(a.dims, a.sorted)
     else:
         out = build(a.dims, a.sorted)
     print(json.dumps(out))

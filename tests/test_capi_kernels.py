@@ -348,6 +348,44 @@ def test_spatial_sort_agents_parity(dims, n, kind):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("order", ["sorted", "displaced"])
+@pytest.mark.parametrize("with_perm", [True, False])
+def test_spatial_sort_agents_in_key_order(order, with_perm):
+    # a population already in sort-key order (bins of up to thousands of
+    # agents, each bin's rows contiguous), or with 1% of its rows exchanged;
+    # 4-, 8- and 1-byte columns, with and without the permutation output
+    import torch
+    capi = _capi()
+    rng = np.random.default_rng(5)
+    n = 60_000
+    g = capi.grid(3, (0, 0, 0), (16, 16, 16), 2.0)
+    pos = _positions(rng, n, (0, 0, 0), (16, 16, 16), "clusters")
+    og = O.grid(3, (0, 0, 0), (16, 16, 16), 2.0)
+    pos = pos[O.stable_sort_perm(O.sort_keys(og, pos[:, 0], pos[:, 1], pos[:, 2]), O.sort_max_bit(og))]
+    if order == "displaced":
+        sel = rng.choice(n, n // 100, replace=False)
+        pos[sel] = pos[rng.permutation(sel)]
+    cols_in = [torch.from_numpy(np.ascontiguousarray(pos[:, a])).cuda() for a in range(3)]
+    w4 = [torch.arange(n, dtype=torch.int32, device="cuda") * (k + 2) for k in range(3)]
+    extra = torch.arange(n, dtype=torch.int64, device="cuda") * 3 + 1
+    tiny = (torch.arange(n, device="cuda") % 251).to(torch.uint8)
+    ins = cols_in + w4 + [extra, tiny]
+    outs = [torch.empty_like(c) for c in ins]
+    perm = torch.zeros(n, dtype=torch.int32, device="cuda") if with_perm else None
+    ws = capi.Workspace(capi.lib().fg_spatial_sort_workspace_size(n, C.byref(g)))
+    capi.check(capi.lib().fg_spatial_sort_agents(C.byref(g), n, None, cols_in[0].data_ptr(), cols_in[1].data_ptr(),
+                                                 cols_in[2].data_ptr(), capi.columns(list(zip(ins, outs))), len(ins),
+                                                 capi.ptr(perm), ws.ptr, ws.nbytes, capi.stream_handle()), "sort")
+    torch.cuda.synchronize()
+    eperm = O.stable_sort_perm(O.sort_keys(og, pos[:, 0], pos[:, 1], pos[:, 2]), O.sort_max_bit(og))
+    if with_perm:
+        np.testing.assert_array_equal(perm.cpu().numpy().view(np.uint32), eperm)
+    for a, b in zip(ins, outs):
+        np.testing.assert_array_equal(b.cpu().numpy(), a.cpu().numpy()[eperm])
+    assert ws.status() == 0
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("n", [0, 1, 2047, 2048, 2049, 300_001])
 @pytest.mark.parametrize("with_births", [False, True])
 def test_compact_agents_parity(n, with_births):
