@@ -804,8 +804,10 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
     launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
-    launch(k_long<EMIT>, static_cast<uint32_t>(sm_count() * 4), kThreads, st, rp, pbm_out, perm, sperm, chunks,
-           L.chunk_cap, h);
+    // a long bin has more than 32 rows and a chunk 256: one block per 128 rows
+    // covers every chunk of a small list at once; large lists get 4 per SM
+    const uint32_t long_grid = std::max(1u, std::min((max_n + 127u) / 128u, static_cast<uint32_t>(sm_count() * 4)));
+    launch(k_long<EMIT>, long_grid, kThreads, st, rp, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
     return check_launch();
 }
 
