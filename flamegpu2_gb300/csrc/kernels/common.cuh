@@ -3,11 +3,13 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include <utility>
 
 #include "flamegpu/detail/launch.cuh"
+#include "flamegpu/detail/spatial_keys.cuh"
 #include "flamegpu_gb300/fg_capi.h"
 
 namespace fgk {
@@ -44,6 +46,10 @@ struct WsHeader {
     uint32_t pad[55];
 };
 static_assert(sizeof(WsHeader) == 256, "header is 256 bytes");
+// words an agent-function launch resets when it computes a build's keys
+static_assert(offsetof(WsHeader, scan_epoch) == 4 * flamegpu::detail::kWsHdrScanEpoch, "header layout");
+static_assert(offsetof(WsHeader, scan_ticket) == 4 * flamegpu::detail::kWsHdrScanTicket, "header layout");
+static_assert(offsetof(WsHeader, long_count) == 4 * flamegpu::detail::kWsHdrLongCount, "header layout");
 
 __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
     uint64_t v;

@@ -3,7 +3,8 @@
 // One build = five kernels, no host synchronisation, no allocation:
 //   k_bin        bin index per message (clamped floor((p-min)/r), the reference's
 //                getGridPosition3D/getHash3D) + warp-aggregated histogram atomics;
-//                keeps each message's slot from the atomic
+//                keeps each message's slot from the atomic (an agent-function
+//                launch may do this instead)
 //   k_scan_u32   single-pass exclusive scan histogram -> PBM (clears the histogram)
 //   k_perm       unstable placement perm[PBM[bin] + slot] = message
 //   k_stabilize  per sorted position: restores ascending original index inside
@@ -17,6 +18,7 @@
 // The automatic agent sort runs the same pipeline on the reference's sort key;
 // its k_stabilize / k_long write every agent column at the stable position.
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -36,13 +38,9 @@ constexpr uint32_t kRankTile = 2048; // bin elements staged in shared memory per
 enum KeyMode { kMessageBin = 0, kSortKey = 1 };
 enum EmitMode { kEmitRecord = 0, kEmitPerm = 1, kEmitPermColumns = 2 };
 
-struct SortGrid {
-    float min[3];
-    float width[3];
-    float gd_f[3];
-    uint32_t gd[3];
-    uint32_t mask;
-};
+// The sort grid and both key functions are shared with agent-function
+// launches that compute the keys themselves (flamegpu/detail/spatial_keys.cuh).
+using SortGrid = flamegpu::detail::SortKeyGrid;
 
 __device__ __forceinline__ uint32_t load_count(const uint32_t* d_n, uint32_t max_n) {
     if (!d_n) return max_n;
@@ -50,37 +48,12 @@ __device__ __forceinline__ uint32_t load_count(const uint32_t* d_n, uint32_t max
     return n < max_n ? n : max_n;
 }
 
-// getGridPosition3D + getHash3D (MessageSpatial3DDevice.cuh:646-672) /
-// getGridPosition2D + getHash2D (MessageSpatial2DDevice.cuh:605-627).
 __device__ __forceinline__ uint32_t message_bin(const fg_spatial_grid& g, float x, float y, float z) {
-    int gx = static_cast<int>(floorf((x - g.min[0]) / g.radius));
-    int gy = static_cast<int>(floorf((y - g.min[1]) / g.radius));
-    const int dx = static_cast<int>(g.gridDim[0]), dy = static_cast<int>(g.gridDim[1]);
-    gx = gx < 0 ? 0 : (gx >= dx ? dx - 1 : gx);
-    gy = gy < 0 ? 0 : (gy >= dy ? dy - 1 : gy);
-    if (g.dims == 3) {
-        int gz = static_cast<int>(floorf((z - g.min[2]) / g.radius));
-        const int dz = static_cast<int>(g.gridDim[2]);
-        gz = gz < 0 ? 0 : (gz >= dz ? dz - 1 : gz);
-        return static_cast<uint32_t>(gz) * g.gridDim[0] * g.gridDim[1] + static_cast<uint32_t>(gy) * g.gridDim[0] +
-               static_cast<uint32_t>(gx);
-    }
-    return static_cast<uint32_t>(gy) * g.gridDim[0] + static_cast<uint32_t>(gx);
+    return flamegpu::detail::spatial_message_bin(g, x, y, z);
 }
 
-// calculateSpatialHash (src/flamegpu/simulation/CUDASimulation.cu:380-408): unclamped,
-// width based; masked to the radix sort's bit range (:569-571).
 __device__ __forceinline__ uint32_t sort_key(const SortGrid& s, int dims, float x, float y, float z) {
-    const int gx = static_cast<int>(floorf(((x - s.min[0]) / s.width[0]) * s.gd_f[0]));
-    const int gy = static_cast<int>(floorf(((y - s.min[1]) / s.width[1]) * s.gd_f[1]));
-    uint32_t h;
-    if (dims == 3) {
-        const int gz = static_cast<int>(floorf(((z - s.min[2]) / s.width[2]) * s.gd_f[2]));
-        h = static_cast<uint32_t>(gz * s.gd[0] * s.gd[1] + (gy * s.gd[0]) + gx);
-    } else {
-        h = static_cast<uint32_t>((gy * s.gd[0]) + gx);
-    }
-    return h & s.mask;
+    return flamegpu::detail::spatial_sort_key(s, dims, x, y, z);
 }
 
 template <int MODE>
@@ -332,7 +305,7 @@ __device__ __forceinline__ void emit_run(const EmitParams& ep, uint32_t* sperm, 
         }
         return;
     }
-    if (EMIT == kEmitPermColumns) {
+    if constexpr (EMIT == kEmitPermColumns) {
         // every column a straight copy of [lo, lo + len) to [s, s + len); runs of
         // four 4-byte columns go four rows at a time (16 loads before any store)
         const ColumnParams& cp = ep.cp;
@@ -365,9 +338,9 @@ __device__ __forceinline__ void emit_run(const EmitParams& ep, uint32_t* sperm, 
                     }
             }
         }
-        return;
+    } else {
+        for (uint32_t k = t; k < len; k += nt) emit<EMIT>(ep, sperm, lo + k, s + k);
     }
-    for (uint32_t k = t; k < len; k += nt) emit<EMIT>(ep, sperm, lo + k, s + k);
 }
 
 // Sorted positions p < total = pbm[nbuckets]. Short bins are ranked in place
@@ -785,7 +758,8 @@ struct BatchKeys {
 template <int MODE, int EMIT>
 int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets, uint32_t max_n, const uint32_t* d_n,
                  const float* x, const float* y, const float* z, const uint32_t* valid, const EmitParams& rp,
-                 uint32_t* pbm_out, const BuildLayout& L, char* ws, cudaStream_t st, const BatchKeys& batch = BatchKeys()) {
+                 uint32_t* pbm_out, const BuildLayout& L, char* ws, cudaStream_t st, const BatchKeys& batch = BatchKeys(),
+                 bool keys_ready = false) {
     WsHeader* h = reinterpret_cast<WsHeader*>(ws);
     uint32_t* hist = reinterpret_cast<uint32_t*>(ws + L.hist);
     uint64_t* sstat = reinterpret_cast<uint64_t*>(ws + L.scan_status);
@@ -795,11 +769,14 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     uint32_t* sperm = EMIT != kEmitRecord ? reinterpret_cast<uint32_t*>(ws + L.sperm) : nullptr;
     uint2* chunks = reinterpret_cast<uint2*>(ws + L.chunks);
     const uint32_t grid = grid_for(max_n);
-    if (batch.inst)
+    if (keys_ready) {
+        // the launch before wrote keys, slots and the histogram (key_targets_write)
+    } else if (batch.inst) {
         launch(k_bin_batched<MODE>, grid, kThreads, st, batch.inst, batch.counts, batch.ninst, max_n, batch.dims, x, y, z,
                valid, keys, slot, hist, h);
-    else
+    } else {
         launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
+    }
     const uint32_t scan_n = nbuckets + 1;
     launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
@@ -813,10 +790,9 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
 
 }  // namespace
 
-extern "C" int fg_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
-                                const float* y, const float* z, const uint32_t* valid, const fg_record_desc* rec,
-                                uint32_t* sorted, uint32_t* pbm, void* workspace, size_t workspace_bytes,
-                                void* stream) {
+int fgi_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x, const float* y,
+                      const float* z, const uint32_t* valid, const fg_record_desc* rec, uint32_t* sorted, uint32_t* pbm,
+                      void* workspace, size_t workspace_bytes, void* stream, bool keys_ready) {
     if (!g || !rec || !pbm || !workspace || (g->dims != 2 && g->dims != 3)) return FG_ERR_INVALID_ARGUMENT;
     if (rec->words == 0 || (rec->words & 3) || rec->words > FG_MAX_RECORD_WORDS) return FG_ERR_INVALID_ARGUMENT;
     if (max_n && (!x || !y || (g->dims == 3 && !z) || !sorted)) return FG_ERR_INVALID_ARGUMENT;
@@ -828,12 +804,20 @@ extern "C" int fg_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const 
     rp.rp.out = sorted;
     SortGrid sg{};
     return run_pipeline<kMessageBin, kEmitRecord>(g, sg, g->binCount, max_n, d_n, x, y, z, valid, rp, pbm, L,
-                                                  static_cast<char*>(workspace), static_cast<cudaStream_t>(stream));
+                                                  static_cast<char*>(workspace), static_cast<cudaStream_t>(stream),
+                                                  BatchKeys(), keys_ready);
 }
 
-extern "C" int fg_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
-                                      const float* y, const float* z, const fg_column* cols, uint32_t ncols,
-                                      uint32_t* perm_out, void* workspace, size_t workspace_bytes, void* stream) {
+extern "C" int fg_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
+                                const float* y, const float* z, const uint32_t* valid, const fg_record_desc* rec,
+                                uint32_t* sorted, uint32_t* pbm, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+    return fgi_spatial_build(g, max_n, d_n, x, y, z, valid, rec, sorted, pbm, workspace, workspace_bytes, stream, false);
+}
+
+int fgi_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
+                            const float* y, const float* z, const fg_column* cols, uint32_t ncols, uint32_t* perm_out,
+                            void* workspace, size_t workspace_bytes, void* stream, bool keys_ready) {
     if (!g || !workspace || (g->dims != 2 && g->dims != 3) || ncols > FG_MAX_COLUMNS) return FG_ERR_INVALID_ARGUMENT;
     if (max_n && (!x || !y || (g->dims == 3 && !z))) return FG_ERR_INVALID_ARGUMENT;
     if (ncols && !cols) return FG_ERR_INVALID_ARGUMENT;
@@ -850,15 +834,45 @@ extern "C" int fg_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, 
     rp.cp.ncols = ncols;
     rp.cp.keep_perm = perm_out != nullptr;
     int rc = ncols ? run_pipeline<kSortKey, kEmitPermColumns>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
-                                                              reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st)
+                                                              reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st,
+                                                              BatchKeys(), keys_ready)
                    : run_pipeline<kSortKey, kEmitPerm>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
-                                                       reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st);
+                                                       reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st,
+                                                       BatchKeys(), keys_ready);
     if (rc != FG_OK) return rc;
     const uint32_t* sperm = reinterpret_cast<const uint32_t*>(ws + L.sperm);
     if (perm_out && max_n) {
         cudaMemcpyAsync(perm_out, sperm, sizeof(uint32_t) * max_n, cudaMemcpyDeviceToDevice, st);
     }
     return check_launch();
+}
+
+extern "C" int fg_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
+                                      const float* y, const float* z, const fg_column* cols, uint32_t ncols,
+                                      uint32_t* perm_out, void* workspace, size_t workspace_bytes, void* stream) {
+    return fgi_spatial_sort_agents(g, max_n, d_n, x, y, z, cols, ncols, perm_out, workspace, workspace_bytes, stream,
+                                   false);
+}
+
+// Where a launch computing the keys of a build (sort_mode false) or an agent
+// sort (true) on this workspace writes them; the sort's grid for its keys.
+int fgi_key_target(const fg_spatial_grid* g, uint32_t max_n, bool sort_mode, void* workspace, size_t workspace_bytes,
+                   flamegpu::detail::KeyTarget* t) {
+    if (!g || !workspace || !t || (g->dims != 2 && g->dims != 3)) return FG_ERR_INVALID_ARGUMENT;
+    std::memset(t, 0, sizeof(*t));
+    uint32_t nb = g->binCount;
+    if (sort_mode && !sort_grid_from(g, &t->sort, &nb)) return FG_ERR_UNSUPPORTED;
+    const BuildLayout L = build_layout(max_n, nb, sort_mode);
+    if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
+    char* ws = static_cast<char*>(workspace);
+    t->mode = sort_mode ? flamegpu::detail::kKeySortKey : flamegpu::detail::kKeyMessageBin;
+    t->dims = static_cast<uint32_t>(g->dims);
+    t->grid = *g;
+    t->keys = reinterpret_cast<uint32_t*>(ws + L.keys);
+    t->slot = reinterpret_cast<uint32_t*>(ws + L.slot);
+    t->hist = reinterpret_cast<uint32_t*>(ws + L.hist);
+    t->header = reinterpret_cast<uint32_t*>(ws);
+    return FG_OK;
 }
 
 extern "C" size_t fg_scan_workspace_size(uint32_t n) {

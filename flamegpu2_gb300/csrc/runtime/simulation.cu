@@ -263,6 +263,11 @@ struct FnRt {
     uint32_t* cond_fail = nullptr;  // condition result per row (1 = failed), capacity + 1 entries
     uint32_t* d_first = nullptr;    // rows that failed the condition (device)
     AgentList* end_list = nullptr;  // state transition target, or null
+    // keys computed by this function's launch for what follows it (plan_keys)
+    MsgList* key_msg = nullptr;  // the build of this output list
+    FnRt* key_sort = nullptr;    // the agent sort before this function (same list)
+    bool build_keyed = false;    // this function's input build: keys already written
+    bool sort_keyed = false;     // this function's agent sort: keys already written
 };
 
 struct SimulationImpl {
@@ -907,6 +912,93 @@ struct SimulationImpl {
         op_events.clear();
     }
 
+    // Whether agent-function launches may compute the keys of the build and
+    // sort after them (FLAMEGPU_FUSE_KEYS=0 turns it off).
+    static bool fuse_keys_enabled() {
+        static const bool on = [] {
+            const char* e = std::getenv("FLAMEGPU_FUSE_KEYS");
+            return !(e && e[0] == '0');
+        }();
+        return on;
+    }
+
+    // Which launches compute the keys of the message build and the agent sort
+    // that follow them, so that those pipelines skip their key kernel. A
+    // launch f qualifies for the build of its spatial output list m when m is
+    // not persistent, f is its only writer this step (no append), f has no
+    // condition (its rows are the message rows) and a later function g reads
+    // m first; and for the agent sort before g as well when the sort is due,
+    // g runs on f's list and no function runs on that list between them, and
+    // f neither kills, gives birth nor changes state (the rows sorted are the
+    // rows f saw, with the positions f left). Layer host functions, which may
+    // change agents between layers, turn it off.
+    void plan_keys() {
+        for (auto& f : fns) {
+            f.key_msg = nullptr;
+            f.key_sort = nullptr;
+            f.build_keyed = f.sort_keyed = false;
+        }
+        if (!fuse_keys_enabled() || has_layer_host_functions()) return;
+        std::map<const MsgList*, std::pair<FnRt*, int>> writers;  // last writer and writes so far
+        std::map<const AgentList*, FnRt*> last_fn;                 // last function run on a list
+        std::set<const MsgList*> read;                              // lists already built this step
+        for (const auto& layer : model->layers)
+            for (auto* fd : layer->functions)
+                for (auto& g : fns) {
+                    if (g.fn != fd) continue;
+                    AgentList* L = g.list;
+                    if (g.in && g.in->spatial() && !g.in->msg->persistent && !read.count(g.in)) {
+                        read.insert(g.in);
+                        const auto w = writers.find(g.in);
+                        FnRt* f = w != writers.end() && w->second.second == 1 ? w->second.first : nullptr;
+                        if (f && !f->fn->condition && f->list->capacity > 0) {
+                            f->key_msg = g.in;
+                            g.build_keyed = true;
+                            const bool do_sort = g.sort_trigger && L->agent->sort_period != 0 &&
+                                                 step_count % L->agent->sort_period == 0;
+                            const auto lf = last_fn.find(L);
+                            if (do_sort && f->list == L && lf != last_fn.end() && lf->second == f &&
+                                !f->fn->has_agent_death && !f->births && !f->end_list) {
+                                f->key_sort = &g;
+                                g.sort_keyed = true;
+                            }
+                        }
+                    }
+                    if (g.out) {
+                        auto& w = writers[g.out];
+                        w.first = &g;
+                        ++w.second;
+                    }
+                    last_fn[L] = &g;
+                    if (g.end_list) last_fn[g.end_list] = &g;
+                }
+    }
+
+    // The key target of f's launch for the build of f.key_msg / the sort of
+    // its list before f.key_sort.
+    KeyTarget build_key_target(const FnRt& f) {
+        MsgList& m = *f.key_msg;
+        KeyTarget t;
+        FG_CAPI(fgi_key_target(&m.grid, m.capacity, false, m.build_ws, m.build_ws_bytes, &t));
+        t.x = static_cast<const float*>(m.cols[0]);  // x, y, z are the first message variables
+        t.y = static_cast<const float*>(m.cols[1]);
+        t.z = m.grid.dims == 3 ? static_cast<const float*>(m.cols[2]) : nullptr;
+        return t;
+    }
+    KeyTarget sort_key_target(const FnRt& f) {
+        const FnRt& g = *f.key_sort;
+        AgentList& l = *f.list;
+        const auto it = l.sort_ws.find(g.in);
+        if (it == l.sort_ws.end()) THROW exception::InvalidOperation("Sort workspace missing (not allocated before capture)");
+        KeyTarget t;
+        FG_CAPI(fgi_key_target(&g.in->grid, l.capacity, true, it->second.first, it->second.second, &t));
+        const int xi = l.var_index("x"), yi = l.var_index("y"), zi = l.var_index("z");
+        t.x = static_cast<const float*>(l.cols[xi][l.parity]);
+        t.y = static_cast<const float*>(l.cols[yi][l.parity]);
+        t.z = g.in->grid.dims == 3 ? static_cast<const float*>(l.cols[zi][l.parity]) : nullptr;
+        return t;
+    }
+
     void enqueue_sort(FnRt& f) {
         AgentList& l = *f.list;
         const fg_spatial_grid* g = &f.in->grid;
@@ -916,16 +1008,16 @@ struct SimulationImpl {
         for (size_t v = 0; v < l.cols.size(); ++v)
             cols[v] = fg_column{l.cols[v][l.parity], l.cols[v][l.parity ^ 1], l.agent->variables[v].bytes()};
         const int xi = l.var_index("x"), yi = l.var_index("y"), zi = l.var_index("z");
-        FG_CAPI(fg_spatial_sort_agents(g, l.capacity, l.d_count, static_cast<const float*>(l.cols[xi][l.parity]),
-                                       static_cast<const float*>(l.cols[yi][l.parity]),
-                                       g->dims == 3 ? static_cast<const float*>(l.cols[zi][l.parity]) : nullptr,
-                                       cols.data(), static_cast<uint32_t>(cols.size()), nullptr, it->second.first,
-                                       it->second.second, stream));
+        FG_CAPI(fgi_spatial_sort_agents(g, l.capacity, l.d_count, static_cast<const float*>(l.cols[xi][l.parity]),
+                                        static_cast<const float*>(l.cols[yi][l.parity]),
+                                        g->dims == 3 ? static_cast<const float*>(l.cols[zi][l.parity]) : nullptr,
+                                        cols.data(), static_cast<uint32_t>(cols.size()), nullptr, it->second.first,
+                                        it->second.second, stream, f.sort_keyed));
         l.parity ^= 1;
-        kernel_counter += 5;
+        kernel_counter += f.sort_keyed ? 4 : 5;
     }
 
-    void enqueue_build(MsgList& m, cudaStream_t st) {
+    void enqueue_build(MsgList& m, cudaStream_t st, bool keys_ready = false) {
         fg_record_desc rec;
         std::memset(&rec, 0, sizeof(rec));
         rec.words = m.record_words;
@@ -940,12 +1032,12 @@ struct SimulationImpl {
         }
         const int dims = m.grid.dims;
         const int xi = 0, yi = 1, zi = 2;  // x, y, z are the first message variables
-        FG_CAPI(fg_spatial_build(&m.grid, m.capacity, m.d_count, static_cast<const float*>(m.cols[xi]),
-                                 static_cast<const float*>(m.cols[yi]), dims == 3 ? static_cast<const float*>(m.cols[zi]) : nullptr,
-                                 m.optional_any ? m.valid : nullptr, &rec, m.records, m.pbm, m.build_ws, m.build_ws_bytes,
-                                 st));
+        FG_CAPI(fgi_spatial_build(&m.grid, m.capacity, m.d_count, static_cast<const float*>(m.cols[xi]),
+                                  static_cast<const float*>(m.cols[yi]), dims == 3 ? static_cast<const float*>(m.cols[zi]) : nullptr,
+                                  m.optional_any ? m.valid : nullptr, &rec, m.records, m.pbm, m.build_ws, m.build_ws_bytes,
+                                  st, keys_ready));
         m.needs_build = false;
-        kernel_counter += 5;
+        kernel_counter += keys_ready ? 4 : 5;
     }
 
     // Rows an agent-function launch of list l covers with one block per 128
@@ -981,13 +1073,13 @@ struct SimulationImpl {
             // two branches of the step graph (fork/join through events)
             FG_CUDA(cudaEventRecord(fork_ev, stream));
             FG_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
-            timed_on(side, "build:" + f.in->msg->name, [&] { enqueue_build(*f.in, side); });
+            timed_on(side, "build:" + f.in->msg->name, [&] { enqueue_build(*f.in, side, f.build_keyed); });
             timed_on(stream, "sort:" + l.agent->name, [&] { enqueue_sort(f); });
             FG_CUDA(cudaEventRecord(join_ev, side));
             FG_CUDA(cudaStreamWaitEvent(stream, join_ev, 0));
         } else {
             if (do_sort) timed("sort:" + l.agent->name, [&] { enqueue_sort(f); });
-            if (do_build) timed("build:" + f.in->msg->name, [&] { enqueue_build(*f.in, stream); });
+            if (do_build) timed("build:" + f.in->msg->name, [&] { enqueue_build(*f.in, stream, f.build_keyed); });
         }
         const bool append = f.out && f.out->written;
         if (f.out) {
@@ -1063,6 +1155,8 @@ struct SimulationImpl {
         P.fn_uid = f.fn->uid;
         P.error = d_error();
         P.env = d_env;
+        if (f.key_msg) P.keyed[0] = build_key_target(f);
+        if (f.key_sort) P.keyed[1] = sort_key_target(f);
         cudaError_t e = cudaSuccess;
         const unsigned int smem = P.stage_bytes ? P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader)) : 0u;
         // one block per 128 rows (no grid-stride reuse): blocks stay short, so
@@ -1128,6 +1222,7 @@ struct SimulationImpl {
             if (!m->msg->persistent) m->needs_build = true;
             m->written = false;
         }
+        plan_keys();
         for (const auto& layer : model->layers) {
             for (auto* fd : layer->functions)
                 for (auto& f : fns)
@@ -1191,6 +1286,7 @@ struct SimulationImpl {
                 if (!m->msg->persistent) m->needs_build = true;
                 m->written = false;
             }
+            plan_keys();
             for (const auto& layer : model->layers) {
                 if (!layer->host_functions.empty()) {
                     run_host_layer(layer.get(), api);

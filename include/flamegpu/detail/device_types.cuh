@@ -15,6 +15,7 @@
 #include <string_view>
 
 #include "flamegpu/defines.h"
+#include "flamegpu/detail/spatial_keys.cuh"
 #include "flamegpu_gb300/fg_capi.h"
 
 namespace flamegpu {
@@ -170,6 +171,10 @@ struct LaunchParams {
     const BatchInstanceRT* batch;
     const uint32_t* batch_counts;
     uint32_t batch_n;
+    // keys of the message build of this function's output and of its agents'
+    // spatial sort, when the runtime has the launch compute them (single
+    // simulations, rows not offset by a condition or an append)
+    KeyTarget keyed[2];
 };
 
 }  // namespace detail

@@ -96,7 +96,11 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
     const uint32_t first_row = (!P.batch && P.d_first) ? min(*P.d_first, n) : 0u;
     // message rows: after those already output to the list this step (append), else from 0
     const uint32_t msg_base = (!P.batch && P.msg_out_base) ? *P.msg_out_base : 0u;
-    if (P.msg_out_count && blockIdx.x == 0 && threadIdx.x == 0) *P.msg_out_count = msg_base + n - first_row;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (P.msg_out_count) *P.msg_out_count = msg_base + n - first_row;
+        if (P.keyed[0].mode) key_target_reset(P.keyed[0]);
+        if (P.keyed[1].mode) key_target_reset(P.keyed[1]);
+    }
     constexpr int kDims = std::is_same<MsgIn, MessageSpatial3D>::value ? 3 : (std::is_same<MsgIn, MessageSpatial2D>::value ? 2 : 0);
     bool first = true;
     if (!P.batch) {
@@ -124,6 +128,16 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
             continue;
         }
         const uint32_t msg_row = msg_base + idx - first_row;
+        // the agent's sort key at its position before the function, computed
+        // alongside the function's own work (again after it if it moved)
+        float pre[3] = {0.0f, 0.0f, 0.0f};
+        uint32_t pre_key = 0xFFFFFFFFu;
+        if (P.keyed[1].mode == kKeySortKey) {
+            pre[0] = P.keyed[1].x[idx];
+            pre[1] = P.keyed[1].y[idx];
+            if (P.keyed[1].dims == 3) pre[2] = P.keyed[1].z[idx];
+            pre_key = key_target_key(P.keyed[1], true, pre[0], pre[1], pre[2]);
+        }
         DeviceAPI<MsgIn, MsgOut> api(P, idx, msg_row);
         const AGENT_STATUS st = F()(&api);
         if (P.death_flags) {
@@ -132,7 +146,27 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
             device_error(P, kDevDeathNotEnabled, 0, idx);
         }
         if (P.birth_flags) P.birth_flags[idx] = api.agent_out.born();
-        if (P.msg_out_valid) P.msg_out_valid[msg_row] = P.msg_out_always ? 1u : api.message_out.written();
+        const bool wrote = P.msg_out_always || api.message_out.written();
+        if (P.msg_out_valid) P.msg_out_valid[msg_row] = wrote ? 1u : 0u;
+        // keys for the message build (by message row, if a message was output,
+        // at the location it was given) and for the agents' spatial sort (by
+        // agent row, at the position the function left) that follow
+        if (P.keyed[0].mode != kKeyNone || P.keyed[1].mode != kKeyNone) {
+            uint32_t k[2] = {0xFFFFFFFFu, 0xFFFFFFFFu};
+            if constexpr (!std::is_same<MsgOut, MessageNone>::value) {
+                if (P.keyed[0].mode == kKeyMessageBin)
+                    k[0] = key_target_key(P.keyed[0], wrote, api.message_out.location(0), api.message_out.location(1),
+                                          api.message_out.location(2));
+            }
+            if (P.keyed[1].mode == kKeySortKey)
+                k[1] = api.pos_set == 0u
+                           ? pre_key
+                           : key_target_key(P.keyed[1], true, (api.pos_set & 1u) ? api.pos[0] : pre[0],
+                                            (api.pos_set & 2u) ? api.pos[1] : pre[1],
+                                            (api.pos_set & 4u) ? api.pos[2] : pre[2]);
+            const uint32_t rows[2] = {msg_row, idx};
+            key_targets_write(P.keyed, rows, k);
+        }
     }
 }
 

@@ -368,6 +368,11 @@ class MessageOutBase {
         }
         detail::write_var<T>(P, &P.T.msg_out, name.hash, index, value);
         flag = 1;
+        if constexpr (std::is_same<T, float>::value) {  // the location, kept for the launch's epilogue
+            if (name.hash == detail::VarName("x").hash) loc[0] = value;
+            if (name.hash == detail::VarName("y").hash) loc[1] = value;
+            if (name.hash == detail::VarName("z").hash) loc[2] = value;
+        }
     }
     template <typename T, flamegpu::size_type N>
     __device__ void setVariable(detail::VarName name, unsigned int i, T value) const {
@@ -379,11 +384,14 @@ class MessageOutBase {
         flag = 1;
     }
     __device__ uint32_t written() const { return flag; }
+    /** The message's x, y, z as last set (spatial messages). */
+    __device__ float location(int a) const { return loc[a]; }
 
  protected:
     const detail::LaunchParams& P;
     uint32_t index;
     mutable uint32_t flag = 0;
+    mutable float loc[3] = {0.0f, 0.0f, 0.0f};
 };
 
 /** Message in an input list, addressed by its (sorted) index. */
@@ -1000,6 +1008,11 @@ class DeviceAPI {
         }
 #endif
         detail::write_var<T>(P, &P.T.agent, name.hash, index, value);
+        if constexpr (std::is_same<T, float>::value) {  // the position, kept for the launch's epilogue
+            if (name.hash == detail::VarName("x").hash) { pos[0] = value; pos_set |= 1u; }
+            if (name.hash == detail::VarName("y").hash) { pos[1] = value; pos_set |= 2u; }
+            if (name.hash == detail::VarName("z").hash) { pos[2] = value; pos_set |= 4u; }
+        }
     }
     template <typename T, flamegpu::size_type N>
     __device__ void setVariable(detail::VarName name, unsigned int i, T value) {
@@ -1014,6 +1027,10 @@ class DeviceAPI {
     AgentOut agent_out;
     DeviceEnvironment environment;
     AgentRandom random;
+    // float x, y, z this function set (bits 1, 2, 4 of pos_set), for the
+    // launch's epilogue
+    float pos[3] = {0.0f, 0.0f, 0.0f};
+    uint32_t pos_set = 0;
 
  private:
     const detail::LaunchParams& P;

@@ -267,6 +267,38 @@ def test_parity_holds_without_programmatic_dependent_launch():
     assert "4 passed" in r.stdout, r.stdout[-2000:]
 
 
+def test_parity_holds_without_key_fusion():
+    # The Boids output launch computes the message bins and the agents' sort
+    # keys itself (the build's and the sort's key kernels are not run); with
+    # that turned off the bit-exact checks hold the same.
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FLAMEGPU_FUSE_KEYS="0")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-p", "no:cacheprovider", "-m", "gpu",
+                        os.path.join(root, "tests", "test_models_gpu.py"),
+                        "-k", "boids_small_matches_oracle or boids_clamped or birth_death_matches or key_kernels"],
+                       cwd=root, env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert "5 passed" in r.stdout, r.stdout[-2000:]
+
+
+def test_key_kernels_fused_into_the_output_launch():
+    # Boids step: outputdata, agent sort (5 kernels), message build (5),
+    # inputdata, step end = 13 kernels; the output launch computing both key
+    # sets saves the two key kernels
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    cfg = dict(synth.BOIDS_SMALL, n=2000, seed=4)
+    s = S.Simulation("boids_spatial3d", synth.boids_params(cfg))
+    s.set_population("Boid", cfg["n"], synth.boids_population(cfg["n"], cfg["min_pos"], cfg["max_pos"], cfg["seed"]))
+    s.step(2)
+    s.synchronize()
+    k = s.stats()["kernels_per_step"]
+    s.close()
+    assert k == (13 if os.environ.get("FLAMEGPU_FUSE_KEYS") == "0" else 11), k
+
+
 def test_steps_replayed_as_one_graph_match_single_steps():
     # step(n) replays up to 16 steps per captured graph when no host work runs
     # between steps; the state after 37 steps (16 + 16 + 5) equals that of 37
