@@ -43,13 +43,15 @@ struct WsHeader {
     uint32_t comp_done;     // finished compaction blocks
     uint32_t comp_parity;   // which compaction status array is live
     uint32_t alive_total;   // survivors, when computed here
-    uint32_t pad[55];
+    uint32_t key_max;       // largest sort key of an agent sort (0 between sorts)
+    uint32_t pad[54];
 };
 static_assert(sizeof(WsHeader) == 256, "header is 256 bytes");
 // words an agent-function launch resets when it computes a build's keys
 static_assert(offsetof(WsHeader, scan_epoch) == 4 * flamegpu::detail::kWsHdrScanEpoch, "header layout");
 static_assert(offsetof(WsHeader, scan_ticket) == 4 * flamegpu::detail::kWsHdrScanTicket, "header layout");
 static_assert(offsetof(WsHeader, long_count) == 4 * flamegpu::detail::kWsHdrLongCount, "header layout");
+static_assert(offsetof(WsHeader, key_max) == 4 * flamegpu::detail::kWsHdrKeyMax, "header layout");
 
 __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
     uint64_t v;

@@ -69,6 +69,7 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
     }
     const uint32_t n = load_count(d_n, max_n);
     const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t kmax = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < n;
@@ -79,11 +80,18 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
         }
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, key != kInvalid);
         uint32_t s = 0;
-        if (key != kInvalid) s = warp_aggregated_inc(hist, key, m);
+        if (key != kInvalid) {
+            s = warp_aggregated_inc(hist, key, m);
+            kmax = max(kmax, key);
+        }
         if (act) {
             keys[i] = key;
             slot[i] = s;
         }
+    }
+    if (MODE == kSortKey) {  // the sort's scan stops past the largest key
+        kmax = __reduce_max_sync(0xFFFFFFFFu, kmax);
+        if (lane_id() == 0 && kmax != 0u) atomicMax(&h->key_max, kmax);
     }
 }
 
@@ -343,7 +351,8 @@ __device__ __forceinline__ void emit_run(const EmitParams& ep, uint32_t* sperm, 
     }
 }
 
-// Sorted positions p < total = pbm[nbuckets]. Short bins are ranked in place
+// Sorted positions p < total = pbm[nbuckets] (pbm[key_max + 1] for an agent
+// sort, whose scan stopped there). Short bins are ranked in place
 // (count of smaller original indices in the bin); long bins are queued as
 // chunks (bucket, chunk index) for k_long.
 template <int EMIT>
@@ -351,9 +360,11 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
                                                         const uint32_t* __restrict__ keys,
                                                         const uint32_t* __restrict__ pbm,
                                                         const uint32_t* __restrict__ perm, uint32_t* sperm,
-                                                        uint2* chunk_list, uint32_t chunk_cap, WsHeader* h) {
+                                                        uint2* chunk_list, uint32_t chunk_cap, WsHeader* h,
+                                                        const uint32_t* key_max) {
     flamegpu::detail::grid_dependency_enter();
-    const uint32_t total = pbm[nbuckets];
+    // key_max (agent sorts): the PBM ends at the largest key + 1
+    const uint32_t total = pbm[key_max ? min(nbuckets, *key_max + 1u) : nbuckets];
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
         const uint32_t i = perm[p];
         const uint32_t b = keys[i];
@@ -409,8 +420,10 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
                                                    const uint32_t* __restrict__ pbm,
                                                    const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                    const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
-                                                   const WsHeader* h) {
+                                                   const WsHeader* h, uint32_t* key_max_reset) {
     flamegpu::detail::grid_dependency_enter();
+    // the last kernel of an agent sort: the largest key is no longer read
+    if (key_max_reset && blockIdx.x == 0 && threadIdx.x == 0) *key_max_reset = 0u;
     __shared__ uint32_t s_idx[kSortCap];
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_lo, s_hi;
@@ -778,13 +791,18 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
         launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
     }
     const uint32_t scan_n = nbuckets + 1;
-    launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st);
+    // an agent sort's buckets (2^bits) run past the grid's cells: its scan stops
+    // past the largest key present, which the key kernel (or launch) recorded
+    uint32_t* key_max = (MODE == kSortKey && !batch.inst) ? &h->key_max : nullptr;
+    launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st, key_max);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
-    launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
+    launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h,
+           static_cast<const uint32_t*>(key_max));
     // a long bin has more than 32 rows and a chunk 256: one block per 128 rows
     // covers every chunk of a small list at once; large lists get 4 per SM
     const uint32_t long_grid = std::max(1u, std::min((max_n + 127u) / 128u, static_cast<uint32_t>(sm_count() * 4)));
-    launch(k_long<EMIT>, long_grid, kThreads, st, rp, pbm_out, perm, sperm, chunks, L.chunk_cap, h);
+    launch(k_long<EMIT>, long_grid, kThreads, st, rp, pbm_out, perm, sperm, chunks, L.chunk_cap,
+           static_cast<const WsHeader*>(h), key_max);
     return check_launch();
 }
 

@@ -57,6 +57,7 @@ __device__ __forceinline__ uint32_t spatial_sort_key(const SortKeyGrid& s, int d
 constexpr int kWsHdrScanEpoch = 1;
 constexpr int kWsHdrScanTicket = 2;
 constexpr int kWsHdrLongCount = 4;
+constexpr int kWsHdrKeyMax = 9;  // raised to the largest sort key (the sort's scan stops past it)
 
 /** Where a launch writes the keys of a build or an agent sort (mode 0: none). */
 struct KeyTarget {
@@ -109,6 +110,11 @@ __device__ __forceinline__ void key_targets_write(const KeyTarget (&t)[2], const
     for (int j = 0; j < 2; ++j)
         if (peers[j] && lane == static_cast<uint32_t>(__ffs(peers[j]) - 1))
             base[j] = atomicAdd(t[j].hist + k[j], static_cast<uint32_t>(__popc(peers[j])));
+    // an agent sort's scan stops past the largest key (every row has one)
+    if (t[1].mode == kKeySortKey) {
+        const uint32_t m = __reduce_max_sync(active, k[1]);
+        if (lane == static_cast<uint32_t>(__ffs(active) - 1) && m != 0u) atomicMax(t[1].header + kWsHdrKeyMax, m);
+    }
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         if (t[j].mode == kKeyNone) continue;
