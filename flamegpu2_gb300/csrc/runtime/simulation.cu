@@ -73,6 +73,75 @@ __global__ void k_max_u32(uint32_t* p, uint32_t v) {
     *p = *p > v ? *p : v;
 }
 
+// Population columns between the device and page-locked host memory in one
+// launch (the host buffers read or written by the kernel through their
+// mapped device addresses) instead of one copy per column: the set and get
+// of a small population cost a launch and a wait, not a dozen copies.
+constexpr int kHostXferCols = 32;
+constexpr int kHostXferWords = 24;
+struct HostXfer {
+    const char* src[kHostXferCols];
+    char* dst[kHostXferCols];
+    uint32_t elem_bytes[kHostXferCols];
+    uint32_t ncols;
+    uint32_t rows;             // rows to copy (at most, with d_rows)
+    const uint32_t* d_rows;    // device row count (get), or null (set: rows)
+    uint32_t* rows_out;        // set: the list's device count (= rows); get: a host word for the count
+    uint32_t* max_target;      // set: next id, raised to max_value
+    uint32_t max_value;
+    const uint32_t* word_src[kHostXferWords];  // get: status words copied to word_dst
+    uint32_t* word_dst[kHostXferWords];
+    uint32_t nwords;
+};
+
+__global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
+    grid_dependency_enter();
+    const uint32_t rows = x.d_rows ? min(*x.d_rows, x.rows) : x.rows;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    if (tid == 0) {
+        if (x.rows_out) *x.rows_out = x.d_rows ? *x.d_rows : rows;
+        if (x.max_target) *x.max_target = *x.max_target > x.max_value ? *x.max_target : x.max_value;
+    }
+    if (tid < x.nwords) *x.word_dst[tid] = *x.word_src[tid];
+    for (uint32_t c = 0; c < x.ncols; ++c) {
+        const size_t bytes = static_cast<size_t>(rows) * x.elem_bytes[c];
+        const char* s = x.src[c];
+        char* d = x.dst[c];
+        if (((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d) | bytes) & 15) == 0) {
+            const uint4* s4 = reinterpret_cast<const uint4*>(s);
+            uint4* d4 = reinterpret_cast<uint4*>(d);
+            for (size_t k = tid; k < bytes / 16; k += nthreads) d4[k] = s4[k];
+        } else if (((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d) | bytes) & 3) == 0) {
+            const uint32_t* s1 = reinterpret_cast<const uint32_t*>(s);
+            uint32_t* d1 = reinterpret_cast<uint32_t*>(d);
+            for (size_t k = tid; k < bytes / 4; k += nthreads) d1[k] = s1[k];
+        } else {
+            for (size_t k = tid; k < bytes; k += nthreads) d[k] = s[k];
+        }
+    }
+}
+
+// One 16-byte unit per thread (host memory is far: keep every copy in
+// flight at once), at most four blocks of 256 per SM.
+inline unsigned int host_xfer_grid(const HostXfer& x, int sms) {
+    size_t bytes = 0;
+    for (uint32_t c = 0; c < x.ncols; ++c) bytes += static_cast<size_t>(x.rows) * x.elem_bytes[c];
+    const size_t blocks = (bytes + 256 * 16 - 1) / (256 * 16);
+    return static_cast<unsigned int>(std::max<size_t>(1, std::min<size_t>(blocks, 4u * static_cast<unsigned int>(sms))));
+}
+
+// The device address of page-locked host memory, or null (pageable memory,
+// or not addressable from the device): such buffers take the copy path.
+inline void* host_mapped(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Device buffers of one simulation, taken stream-ordered from the device's
 // default memory pool: a finished simulation returns its memory without
 // stalling the other simulations of the process (cudaFree would wait for the
@@ -291,6 +360,7 @@ struct SimulationImpl {
     // misc device state
     uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record, [8..] next ids per agent
     uint32_t* h_pinned = nullptr;
+    uint32_t* h_pinned_dev = nullptr;  // its device address (null: not mapped)
     unsigned int step_count = 0;
     std::vector<uint32_t> next_id;  // host mirror per agent index (valid when synced)
     bool ids_on_device = true;
@@ -377,6 +447,7 @@ struct SimulationImpl {
         FG_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
         FG_CUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
         FG_CUDA(cudaMallocHost(&h_pinned, 4096));
+        h_pinned_dev = static_cast<uint32_t*>(host_mapped(h_pinned));
         std::memset(h_pinned, 0, 4096);
         d_misc = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (8 + model->agents.size() + 8)));
         next_id.assign(model->agents.size(), 1u);
@@ -1454,15 +1525,20 @@ struct SimulationImpl {
     // part of a caller's batch (enqueue_status_reads, its wait, raise_status).
     void resolve_step_timers();  // step_events -> step_ms (their steps have completed)
     using StatusList = std::vector<std::pair<void*, std::string>>;
-    StatusList enqueue_status_reads() {
-        uint32_t* hp = h_pinned + 64;
-        const uint32_t cap = 1024 - 64;
-        FG_CUDA(cudaMemcpyAsync(hp, d_error(), 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    // the workspaces whose status word a read checks
+    StatusList status_sources() const {
         StatusList ws;
         for (auto& m : msgs)
             if (m->build_ws) ws.emplace_back(m->build_ws, format("Message '%s' index build", m->msg->name.c_str()));
         for (auto& l : lists)
             if (l->comp_ws) ws.emplace_back(l->comp_ws, format("Compaction of agent '%s'", l->agent->name.c_str()));
+        return ws;
+    }
+    StatusList enqueue_status_reads() {
+        uint32_t* hp = h_pinned + 64;
+        const uint32_t cap = 1024 - 64;
+        FG_CUDA(cudaMemcpyAsync(hp, d_error(), 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        const StatusList ws = status_sources();
         for (size_t k = 0; k < ws.size() && 4 + k < cap; ++k)
             FG_CUDA(cudaMemcpyAsync(hp + 4 + k, ws[k].first, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
         return ws;
@@ -1906,15 +1982,36 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
         FG_CUDA(cudaStreamSynchronize(impl->stream));
         impl->ensure_capacity(*l, cap, 0);
     }
-    for (size_t v = 0; v < l->cols.size(); ++v) {
-        const size_t b = l->agent->variables[v].bytes();
-        if (n) FG_CUDA(cudaMemcpyAsync(l->cols[v][l->parity], src[v], b * n, cudaMemcpyHostToDevice, impl->stream));
+    // page-locked host columns: one launch copies them all, sets the count and
+    // the next id; otherwise one copy per column
+    detail::HostXfer x;
+    std::memset(&x, 0, sizeof(x));
+    bool mapped = l->cols.size() <= static_cast<size_t>(detail::kHostXferCols);
+    for (size_t v = 0; mapped && v < l->cols.size(); ++v) {
+        x.src[v] = static_cast<const char*>(n ? detail::host_mapped(src[v]) : l->cols[v][l->parity]);
+        x.dst[v] = static_cast<char*>(l->cols[v][l->parity]);
+        x.elem_bytes[v] = l->agent->variables[v].bytes();
+        mapped = x.src[v] != nullptr;
     }
-    // next id: the larger of the device's and one past the largest given
-    detail::launch_kernel(detail::pdl_enabled(), detail::k_max_u32, 1, 1, 0, impl->stream,
-                         impl->d_next_id(impl->agent_index(l->agent)), mx + 1);
-    impl->h_pinned[2] = n;
-    FG_CUDA(cudaMemcpyAsync(l->d_count, impl->h_pinned + 2, sizeof(uint32_t), cudaMemcpyHostToDevice, impl->stream));
+    if (mapped) {
+        x.ncols = static_cast<uint32_t>(l->cols.size());
+        x.rows = n;
+        x.rows_out = l->d_count;
+        x.max_target = impl->d_next_id(impl->agent_index(l->agent));
+        x.max_value = mx + 1;
+        FG_CUDA(detail::launch_kernel(detail::pdl_enabled(), detail::k_host_xfer, detail::host_xfer_grid(x, impl->sms),
+                                      256, 0, impl->stream, x));
+    } else {
+        for (size_t v = 0; v < l->cols.size(); ++v) {
+            const size_t b = l->agent->variables[v].bytes();
+            if (n) FG_CUDA(cudaMemcpyAsync(l->cols[v][l->parity], src[v], b * n, cudaMemcpyHostToDevice, impl->stream));
+        }
+        // next id: the larger of the device's and one past the largest given
+        detail::launch_kernel(detail::pdl_enabled(), detail::k_max_u32, 1, 1, 0, impl->stream,
+                             impl->d_next_id(impl->agent_index(l->agent)), mx + 1);
+        impl->h_pinned[2] = n;
+        FG_CUDA(cudaMemcpyAsync(l->d_count, impl->h_pinned + 2, sizeof(uint32_t), cudaMemcpyHostToDevice, impl->stream));
+    }
     FG_CUDA(cudaStreamSynchronize(impl->stream));
     l->bound = n;
     impl->forget_counts();
@@ -1935,14 +2032,49 @@ uint32_t CUDASimulation::getPopulationColumns(const std::string& agent, const st
     }
     // one batch and one wait: status words, the count, and the rows up to the
     // host's bound on the count (never below it), as many as the caller has room for
-    const detail::SimulationImpl::StatusList ws = impl->enqueue_status_reads();
-    FG_CUDA(cudaMemcpyAsync(impl->h_pinned + 3, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, impl->stream));
     const uint32_t rows = std::min(std::min(cap, l->bound), l->capacity);
-    for (size_t k = 0; k < host_out.size(); ++k) {
-        const size_t b = l->agent->variables[vi[k]].bytes();
-        if (rows)
-            FG_CUDA(cudaMemcpyAsync(host_out[k].second, l->cols[vi[k]][l->parity], b * rows, cudaMemcpyDeviceToHost,
-                                    impl->stream));
+    // page-locked host buffers: one launch copies the rows, the count and the
+    // status words; otherwise one copy each
+    detail::HostXfer x;
+    std::memset(&x, 0, sizeof(x));
+    bool mapped = host_out.size() <= static_cast<size_t>(detail::kHostXferCols) && impl->h_pinned_dev;
+    for (size_t k = 0; mapped && k < host_out.size(); ++k) {
+        x.src[k] = static_cast<const char*>(l->cols[vi[k]][l->parity]);
+        x.dst[k] = static_cast<char*>(detail::host_mapped(host_out[k].second));
+        x.elem_bytes[k] = l->agent->variables[vi[k]].bytes();
+        mapped = x.dst[k] != nullptr;
+    }
+    detail::SimulationImpl::StatusList ws;
+    if (mapped) {
+        ws = impl->status_sources();
+        mapped = ws.size() + 4 <= static_cast<size_t>(detail::kHostXferWords);
+    }
+    if (mapped) {
+        uint32_t* hp_dev = impl->h_pinned_dev + 64;  // the status words' host slots, as enqueue_status_reads uses
+        for (uint32_t k = 0; k < 4; ++k) {
+            x.word_src[k] = impl->d_error() + k;
+            x.word_dst[k] = hp_dev + k;
+        }
+        for (size_t k = 0; k < ws.size(); ++k) {
+            x.word_src[4 + k] = static_cast<const uint32_t*>(ws[k].first);
+            x.word_dst[4 + k] = hp_dev + 4 + k;
+        }
+        x.nwords = static_cast<uint32_t>(4 + ws.size());
+        x.ncols = static_cast<uint32_t>(host_out.size());
+        x.rows = rows;
+        x.d_rows = l->d_count;
+        x.rows_out = impl->h_pinned_dev + 3;
+        FG_CUDA(detail::launch_kernel(detail::pdl_enabled(), detail::k_host_xfer, detail::host_xfer_grid(x, impl->sms),
+                                      256, 0, impl->stream, x));
+    } else {
+        ws = impl->enqueue_status_reads();
+        FG_CUDA(cudaMemcpyAsync(impl->h_pinned + 3, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, impl->stream));
+        for (size_t k = 0; k < host_out.size(); ++k) {
+            const size_t b = l->agent->variables[vi[k]].bytes();
+            if (rows)
+                FG_CUDA(cudaMemcpyAsync(host_out[k].second, l->cols[vi[k]][l->parity], b * rows, cudaMemcpyDeviceToHost,
+                                        impl->stream));
+        }
     }
     FG_CUDA(cudaStreamSynchronize(impl->stream));
     impl->raise_status(ws);

@@ -283,6 +283,41 @@ def test_parity_holds_without_key_fusion():
     assert "5 passed" in r.stdout, r.stdout[-2000:]
 
 
+@pytest.mark.parametrize("n", [1001, 2048])
+def test_population_through_page_locked_buffers(n):
+    # page-locked host columns are read and written by one launch through
+    # their mapped addresses (16-byte or 4-byte units by alignment and size),
+    # pageable ones by one copy each: the same state either way
+    import torch
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    cfg = dict(synth.BOIDS_SMALL, n=n, seed=6)
+    pop = synth.boids_population(n, cfg["min_pos"], cfg["max_pos"], cfg["seed"])
+
+    def pinned_like(a):
+        buf = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory().numpy().view(a.dtype)
+        buf[:] = a
+        return buf
+
+    names = ("_id", "x", "y", "z", "fx", "fy", "fz")
+    res = []
+    for locked in (False, True):
+        s = S.Simulation("boids_spatial3d", synth.boids_params(cfg))
+        cols = {k: pinned_like(v) for k, v in pop.items()} if locked else pop
+        outs = {k: (pinned_like(pop[k]) if locked else np.empty_like(pop[k])) for k in names}
+        for _ in range(3):
+            s.set_population("Boid", n, cols)
+            s.step(2)
+            assert s.get_population("Boid", outs) == n
+            cols = {k: outs[k].copy() for k in names}
+            if locked:
+                cols = {k: pinned_like(v) for k, v in cols.items()}
+        s.close()
+        res.append({k: np.array(outs[k]) for k in names})
+    for k in names:
+        np.testing.assert_array_equal(res[0][k], res[1][k], err_msg=k)
+
+
 def test_key_kernels_fused_into_the_output_launch():
     # Boids step: outputdata, agent sort (5 kernels), message build (5),
     # inputdata, step end = 13 kernels; the output launch computing both key
