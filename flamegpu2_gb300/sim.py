@@ -151,7 +151,7 @@ class Simulation:
 
     def get(self, agent: str, var: str, dtype, elements: int = 1, state: str = "default") -> np.ndarray:
         n = self.count(agent, state)
-        out = np.zeros((n, elements) if elements > 1 else n, dtype=dtype)
+        out = np.empty((n, elements) if elements > 1 else n, dtype=dtype)
         _check(core().fgs_get_variable(self._h, agent.encode(), state.encode(), var.encode(),
                                        out.ctypes.data, out.nbytes))
         return out
@@ -328,7 +328,7 @@ class Ensemble:
         return n.value
 
     def get(self, run: int, agent: str, var: str, dtype) -> np.ndarray:
-        out = np.zeros(self.count(run, agent), dtype=dtype)
+        out = np.empty(self.count(run, agent), dtype=dtype)
         _check(_ens().fge_get_variable(self._h, run, agent.encode(), var.encode(), out.ctypes.data, out.nbytes))
         return out
 
@@ -449,7 +449,7 @@ class Server:
         return n.value
 
     def get(self, rid: int, agent: str, var: str, dtype, state: str = "default") -> np.ndarray:
-        out = np.zeros(self.count(rid, agent, state), dtype=dtype)
+        out = np.empty(self.count(rid, agent, state), dtype=dtype)
         _check(_srv().fgv_result_variable(self._h, rid, agent.encode(), state.encode(), var.encode(),
                                           out.ctypes.data, out.nbytes))
         return out
