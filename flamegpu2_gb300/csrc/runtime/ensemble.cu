@@ -58,6 +58,11 @@ void RunPlan::set_property(const std::string& name, std::type_index t, size_t si
     properties_[name] = std::move(bytes);
 }
 
+void RunPlan::setPopulation(AgentVector&& population, const std::string& state) {
+    const std::string name = population.getAgentName();
+    populations_[{name, state}] = std::make_shared<AgentVector>(std::move(population));
+}
+
 void RunPlan::setPopulation(const AgentVector& population, const std::string& state) {
     populations_[{population.getAgentName(), state}] = std::make_shared<AgentVector>(population);
 }
@@ -261,17 +266,25 @@ struct BatchedSim {
         for (uint32_t k = 0; k < ninst; ++k) {
             auto it = plans[k].populations().find({agent->name, state});
             if (it == plans[k].populations().end() || count[k] == 0) continue;
-            AgentVector pop = *it->second;  // ids are per run: fill unset ones (CUDAFatAgent.cu:311-319)
+            // ids are per run: unset ones are filled (CUDAFatAgent.cu:311-319), in
+            // a copy of the id column only
+            const AgentVector& pop = *it->second;
             const size_t idc = pop.columnIndex("_id");
-            id_t* ids = reinterpret_cast<id_t*>(pop.columns()[idc].data());
+            const id_t* ids = reinterpret_cast<const id_t*>(pop.columns()[idc].data());
+            std::vector<id_t> filled;
             id_t next = 1;
             for (uint32_t i = 0; i < count[k]; ++i) next = std::max<id_t>(next, ids[i] + 1);
-            for (uint32_t i = 0; i < count[k]; ++i)
-                if (ids[i] == ID_NOT_SET) ids[i] = next++;
+            for (uint32_t i = 0; i < count[k]; ++i) {
+                if (ids[i] != ID_NOT_SET) continue;
+                if (filled.empty()) filled.assign(ids, ids + count[k]);
+                filled[i] = next++;
+            }
             for (size_t v = 0; v < cols.size(); ++v) {
                 const size_t b = agent->variables[v].bytes();
-                FG_ECUDA(cudaMemcpy(static_cast<char*>(cols[v][0]) + b * row_begin[k], pop.columns()[v].data(),
-                                    b * count[k], cudaMemcpyHostToDevice));
+                const void* src = (v == idc && !filled.empty()) ? static_cast<const void*>(filled.data())
+                                                                 : static_cast<const void*>(pop.columns()[v].data());
+                FG_ECUDA(cudaMemcpy(static_cast<char*>(cols[v][0]) + b * row_begin[k], src, b * count[k],
+                                    cudaMemcpyHostToDevice));
             }
         }
         d_counts = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * ninst));
@@ -691,6 +704,16 @@ unsigned int CUDAEnsemble::simulate(const RunPlanVector& plans) {
     }
     impl->elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return failures;
+}
+
+std::shared_ptr<const AgentVector> CUDAEnsemble::getPopulationView(unsigned int run, const std::string& agent,
+                                                                    const std::string& state) const {
+    if (run >= impl->results.size()) THROW exception::OutOfBoundsException(format("Run %u out of range", run));
+    auto it = impl->results[run].find({agent, state});
+    if (it == impl->results[run].end() || !it->second)
+        THROW exception::InvalidAgentName(format("Run %u has no population of '%s' in state '%s'", run, agent.c_str(),
+                                                  state.c_str()));
+    return it->second;
 }
 
 void CUDAEnsemble::getPopulationData(unsigned int run, AgentVector& population, const std::string& state) const {

@@ -421,7 +421,7 @@ extern "C" int fge_add_run(fge_ensemble* e, uint32_t steps, uint64_t seed, const
                 const size_t c = pop.columnIndex(names[k]);
                 std::memcpy(pop.columns()[c].data(), cols[k], pop.columns()[c].size());
             }
-            plan.setPopulation(pop);
+            plan.setPopulation(std::move(pop));
         }
         if (message) plan.setSpatialMessageBounds(message, {mn[0], mn[1], mn[2]}, {mx[0], mx[1], mx[2]}, radius);
         e->plans->push_back(plan);
@@ -451,19 +451,14 @@ extern "C" int fge_simulate(fge_ensemble* e, uint32_t* failures) {
 }
 
 extern "C" int fge_get_count(fge_ensemble* e, uint32_t run, const char* agent, uint32_t* n) {
-    return guarded([&] {
-        flamegpu::AgentVector pop(e->model->Agent(agent));
-        e->ens->getPopulationData(run, pop);
-        *n = pop.size();
-    });
+    return guarded([&] { *n = e->ens->getPopulationView(run, agent)->size(); });
 }
 
 extern "C" int fge_get_variable(fge_ensemble* e, uint32_t run, const char* agent, const char* var, void* out,
                                 size_t bytes) {
     return guarded([&] {
-        flamegpu::AgentVector pop(e->model->Agent(agent));
-        e->ens->getPopulationData(run, pop);
-        const auto& col = pop.columns()[pop.columnIndex(var)];
+        const auto pop = e->ens->getPopulationView(run, agent);
+        const auto& col = pop->columns()[pop->columnIndex(var)];
         if (bytes < col.size()) throw flamegpu::exception::InvalidArgument("output buffer too small");
         std::memcpy(out, col.data(), col.size());
     });

@@ -41,6 +41,8 @@ class RunPlan {
     // ---- GB300 extensions ----
     /** Initial population of an agent (state) for this run. */
     void setPopulation(const AgentVector& population, const std::string& state = "default");
+    /** The same, taking the vector's storage instead of copying it. */
+    void setPopulation(AgentVector&& population, const std::string& state = "default");
     /** Per-run bounds and radius of a spatial message list (the model's are the default). */
     void setSpatialMessageBounds(const std::string& message, const std::vector<float>& min,
                                  const std::vector<float>& max, float radius);
@@ -109,6 +111,9 @@ class CUDAEnsemble {
     bool lastRunBatched() const;
     /** Final population of one run (GB300 extension; the reference reports through logs). */
     void getPopulationData(unsigned int run, AgentVector& population, const std::string& state = "default") const;
+    /** The same population without a copy (valid until the next simulate()). */
+    std::shared_ptr<const AgentVector> getPopulationView(unsigned int run, const std::string& agent,
+                                                          const std::string& state = "default") const;
     /** Kernel launches per batched step and graph replays of the last simulate(). */
     unsigned int getKernelsPerStep() const;
     unsigned long long getGraphLaunches() const;
