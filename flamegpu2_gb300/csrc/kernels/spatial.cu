@@ -10,11 +10,12 @@
 //   k_stabilize  per sorted position: restores ascending original index inside
 //                short bins (<= kShortBin) and emits the record (or index);
 //                long bins are queued as 256-element chunks
-//   k_long       orders long bins: up to 1024 messages one warp each (a
-//                bitmap over their indices), up to 8192 one block each (a
-//                bitmap over the span of their indices, or a bitonic sort in
-//                shared memory), longer ones by ranking each 256-element chunk
-//                against the whole bin
+//   k_long       orders long bins: a bin whose indices are contiguous is
+//                copied in order; otherwise up to 1024 messages one warp each
+//                (a bitmap over their indices, or a bitonic sort), up to 8192
+//                one block each (a bitmap over the span of their indices, or a
+//                bitonic sort in shared memory), longer ones by ranking each
+//                256-element chunk against the whole bin
 // The automatic agent sort runs the same pipeline on the reference's sort key;
 // its k_stabilize / k_long write every agent column at the stable position.
 #include <algorithm>
