@@ -129,7 +129,7 @@ __device__ __forceinline__ void scan_load(const uint32_t* in, uint64_t base, uin
 template <int R>
 __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
                                                        uint64_t* status, WsHeader* h, int self_reset,
-                                                       const uint32_t* last) {
+                                                       const uint32_t* last, uint32_t last_floor) {
     flamegpu::detail::grid_dependency_enter();
     __shared__ uint32_t s_tile, s_epoch;
     __shared__ uint32_t s_warp[33];
@@ -140,9 +140,9 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
     }
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
-    // last (no self reset): the values past index *last + 1 are zero and their
-    // prefixes unused; the tiles wholly past it have nothing to do
-    if (last) n = min(n, *last + 2u);
+    // last (no self reset): the values past index max(*last, last_floor) + 1
+    // are zero and their prefixes unused; the tiles wholly past it have nothing to do
+    if (last) n = min(n, max(*last, last_floor) + 2u);
     if (static_cast<uint64_t>(tile) * R * kScanTile >= n && tile != 0) return;
     const bool in_al = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
     const bool out_al = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
@@ -231,13 +231,15 @@ inline uint32_t scan_tiles(uint32_t n) { return (n + kScanTile - 1) / kScanTile;
 // Scans of more than this many values take four sub-tiles per tile.
 constexpr uint32_t kScanWideMin = 1u << 22;
 
-// last: optional (device), as in k_scan_u32; only without self_reset.
+// last, last_floor: optional (device) bound, as in k_scan_u32; only without self_reset.
 inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in, uint64_t* status,
-                               WsHeader* h, int self_reset, cudaStream_t st, const uint32_t* last = nullptr) {
+                               WsHeader* h, int self_reset, cudaStream_t st, const uint32_t* last = nullptr,
+                               uint32_t last_floor = 0) {
     if (n > kScanWideMin)
         return launch(k_scan_u32<4>, (n + 4u * kScanTile - 1) / (4u * kScanTile), kThreads, st, in, out, n, zero_in,
-                      status, h, self_reset, last);
-    return launch(k_scan_u32<1>, scan_tiles(n), kThreads, st, in, out, n, zero_in, status, h, self_reset, last);
+                      status, h, self_reset, last, last_floor);
+    return launch(k_scan_u32<1>, scan_tiles(n), kThreads, st, in, out, n, zero_in, status, h, self_reset, last,
+                  last_floor);
 }
 
 }  // namespace fgk

@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
     }
     const uint32_t n = load_count(d_n, max_n);
     const uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t kmax = 0;
+    const uint32_t cells = flamegpu::detail::sort_cells(sg);
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < n;
@@ -83,16 +83,14 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
         uint32_t s = 0;
         if (key != kInvalid) {
             s = warp_aggregated_inc(hist, key, m);
-            kmax = max(kmax, key);
+            // the sort's scan stops past the cells, or past the largest key of
+            // a row outside them (rare)
+            if (MODE == kSortKey && key >= cells) atomicMax(&h->key_max, key);
         }
         if (act) {
             keys[i] = key;
             slot[i] = s;
         }
-    }
-    if (MODE == kSortKey) {  // the sort's scan stops past the largest key
-        kmax = __reduce_max_sync(0xFFFFFFFFu, kmax);
-        if (lane_id() == 0 && kmax != 0u) atomicMax(&h->key_max, kmax);
     }
 }
 
@@ -352,8 +350,8 @@ __device__ __forceinline__ void emit_run(const EmitParams& ep, uint32_t* sperm, 
     }
 }
 
-// Sorted positions p < total = pbm[nbuckets] (pbm[key_max + 1] for an agent
-// sort, whose scan stopped there). Short bins are ranked in place
+// Sorted positions p < total = pbm[nbuckets] (for an agent sort, whose scan
+// stopped past max(recorded key, cells - 1), the PBM entry after that). Short bins are ranked in place
 // (count of smaller original indices in the bin); long bins are queued as
 // chunks (bucket, chunk index) for k_long.
 template <int EMIT>
@@ -362,10 +360,10 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
                                                         const uint32_t* __restrict__ pbm,
                                                         const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                         uint2* chunk_list, uint32_t chunk_cap, WsHeader* h,
-                                                        const uint32_t* key_max) {
+                                                        const uint32_t* key_max, uint32_t key_floor) {
     flamegpu::detail::grid_dependency_enter();
-    // key_max (agent sorts): the PBM ends at the largest key + 1
-    const uint32_t total = pbm[key_max ? min(nbuckets, *key_max + 1u) : nbuckets];
+    // key_max (agent sorts): the PBM ends at max(recorded key, key_floor) + 1
+    const uint32_t total = pbm[key_max ? min(nbuckets, max(*key_max, key_floor) + 1u) : nbuckets];
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
         const uint32_t i = perm[p];
         const uint32_t b = keys[i];
@@ -793,12 +791,14 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     }
     const uint32_t scan_n = nbuckets + 1;
     // an agent sort's buckets (2^bits) run past the grid's cells: its scan stops
-    // past the largest key present, which the key kernel (or launch) recorded
+    // past the cells, or past the largest key beyond them that the key kernel
+    // (or launch) recorded
     uint32_t* key_max = (MODE == kSortKey && !batch.inst) ? &h->key_max : nullptr;
-    launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st, key_max);
+    const uint32_t key_floor = flamegpu::detail::sort_cells(sg) - 1u;
+    launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st, key_max, key_floor);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
     launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h,
-           static_cast<const uint32_t*>(key_max));
+           static_cast<const uint32_t*>(key_max), key_floor);
     // a long bin has more than 32 rows and a chunk 256: one block per 128 rows
     // covers every chunk of a small list at once; large lists get 4 per SM
     const uint32_t long_grid = std::max(1u, std::min((max_n + 127u) / 128u, static_cast<uint32_t>(sm_count() * 4)));

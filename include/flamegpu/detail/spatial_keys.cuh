@@ -37,6 +37,10 @@ struct SortKeyGrid {
     uint32_t mask;
 };
 
+// Cells of the sort grid; keys at or past it come from positions outside the
+// environment (the key is not clamped).
+__host__ __device__ __forceinline__ uint32_t sort_cells(const SortKeyGrid& s) { return s.gd[0] * s.gd[1] * s.gd[2]; }
+
 // calculateSpatialHash (src/flamegpu/simulation/CUDASimulation.cu:380-408): unclamped,
 // width based; masked to the radix sort's bit range (:569-571).
 __device__ __forceinline__ uint32_t spatial_sort_key(const SortKeyGrid& s, int dims, float x, float y, float z) {
@@ -57,7 +61,9 @@ __device__ __forceinline__ uint32_t spatial_sort_key(const SortKeyGrid& s, int d
 constexpr int kWsHdrScanEpoch = 1;
 constexpr int kWsHdrScanTicket = 2;
 constexpr int kWsHdrLongCount = 4;
-constexpr int kWsHdrKeyMax = 9;  // raised to the largest sort key (the sort's scan stops past it)
+// raised to the largest sort key past the grid's cells (positions outside the
+// environment; 0 if none): the sort's scan stops past max(it, cells - 1)
+constexpr int kWsHdrKeyMax = 9;
 
 /** Where a launch writes the keys of a build or an agent sort (mode 0: none). */
 struct KeyTarget {
@@ -110,11 +116,9 @@ __device__ __forceinline__ void key_targets_write(const KeyTarget (&t)[2], const
     for (int j = 0; j < 2; ++j)
         if (peers[j] && lane == static_cast<uint32_t>(__ffs(peers[j]) - 1))
             base[j] = atomicAdd(t[j].hist + k[j], static_cast<uint32_t>(__popc(peers[j])));
-    // an agent sort's scan stops past the largest key (every row has one)
-    if (t[1].mode == kKeySortKey) {
-        const uint32_t m = __reduce_max_sync(active, k[1]);
-        if (lane == static_cast<uint32_t>(__ffs(active) - 1) && m != 0u) atomicMax(t[1].header + kWsHdrKeyMax, m);
-    }
+    // an agent sort's scan stops past the grid's cells, or past the largest
+    // key of a row outside them (rare: one atomic per such row)
+    if (t[1].mode == kKeySortKey && k[1] >= sort_cells(t[1].sort)) atomicMax(t[1].header + kWsHdrKeyMax, k[1]);
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         if (t[j].mode == kKeyNone) continue;
