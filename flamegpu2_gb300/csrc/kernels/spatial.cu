@@ -130,8 +130,13 @@ __global__ void __launch_bounds__(kThreads) k_bin_batched(const fg_batch_instanc
         const uint32_t i = base + threadIdx.x;
         const bool act = i < total_rows;
         uint32_t key = kInvalid;
+        // the instance of the warp's first row, searched once; a lane past that
+        // instance's rows (a warp across a boundary) searches its own
+        const uint32_t wrow = min(base + (threadIdx.x & ~31u), total_rows - 1u);
+        const uint32_t k0 = __shfl_sync(0xFFFFFFFFu, lane_id() == 0 ? find_instance(inst, ninst, wrow) : 0u, 0);
         if (act) {
-            const uint32_t k = find_instance(inst, ninst, i);
+            const bool in_k0 = k0 + 1 >= ninst || i < __ldg(&inst[k0 + 1].row_begin);
+            const uint32_t k = in_k0 ? k0 : find_instance(inst, ninst, i);
             const fg_batch_instance& I = inst[k];
             const uint32_t local = i - I.row_begin;
             const uint32_t bb = I.bucket_begin;
