@@ -80,6 +80,22 @@ def test_spatial2d_wrapped_lattice(off):
     assert np.all(r["result_x"] == 0.0) and np.all(r["result_y"] == 0.0)
 
 
+@pytest.mark.parametrize("optional", [False, True])
+def test_spatial3d_counts_and_order_with_agents_outside_the_bounds(optional):
+    # a third of the agents outside [0,5)^3: their messages fall in the clamped
+    # edge bins, their sort keys past the grid's cells (unclamped); the output
+    # launch computes both key sets, and the sort's scan runs past the cells
+    rng = np.random.default_rng(17 + optional)
+    n = 3000
+    pos = rng.uniform(-2.0, 7.0, (n, 3)).astype(np.float32)
+    do = (rng.random(n) < 0.6).astype(np.int32) if optional else None
+    r = _count_run(3, (0, 0, 0), (5, 5, 5), 1.0, False, optional, pos, do)
+    o = O.count_model(O.grid(3, (0, 0, 0), (5, 5, 5), 1.0), False, pos[:, 0], pos[:, 1], pos[:, 2], do_output=do)
+    agent = r["_id"] - 1
+    np.testing.assert_array_equal(agent, o["order"])
+    np.testing.assert_array_equal(r["count"], o["count"])  # both in the sorted order
+
+
 def test_spatial3d_bounds_not_factor_radius():
     h = np.float32(50.1) / np.float32(2)
     pos = np.array([[h, 0.0, h], [h, 18.0, h], [0.0, h, 0.5], [18.0, h, 0.5], [h, 50.0, 50.1],
