@@ -4,7 +4,9 @@
 // with the mean payload of the messages within the interaction radius:
 //   p_k <- 0.5 * p_k + 0.5 * mean_{|m - a| < r} m.p_k
 // Positions do not change, so every step does the same build + iterate work.
-// Registered as "spatial_payload"; parameters: dims (2|3), min, max, radius.
+// Registered as "spatial_payload"; parameters: dims (2|3), min, max, radius,
+// wrap (0: the clamped Moore neighbourhood; 1: the wrapped one, distances to
+// the messages' virtual positions across the periodic bounds).
 #ifndef FLAMEGPU_SEATBELTS
 #define FLAMEGPU_SEATBELTS 0  // benchmark model: device checks off, as in the reference's benchmark builds
 #endif
@@ -32,7 +34,7 @@ FLAMEGPU_AGENT_FUNCTION(payload_out2, flamegpu::MessageNone, flamegpu::MessageSp
     return flamegpu::ALIVE;
 }
 
-template <int DIMS, typename API>
+template <int DIMS, bool WRAP, typename API>
 __device__ __forceinline__ flamegpu::AGENT_STATUS payload_mix(API* FLAMEGPU) {
     const float x = FLAMEGPU->template getVariable<float>("x");
     const float y = FLAMEGPU->template getVariable<float>("y");
@@ -42,9 +44,16 @@ __device__ __forceinline__ flamegpu::AGENT_STATUS payload_mix(API* FLAMEGPU) {
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
     unsigned int c = 0;
     auto visit = [&](const auto& m) {
-        const float dx = m.template getVariable<float>("x") - x;
-        const float dy = m.template getVariable<float>("y") - y;
-        const float dz = DIMS == 3 ? m.template getVariable<float>("z") - z : 0.0f;
+        float dx, dy, dz;
+        if constexpr (WRAP) {
+            dx = m.getVirtualX() - x;
+            dy = m.getVirtualY() - y;
+            dz = DIMS == 3 ? m.getVirtualZ() - z : 0.0f;
+        } else {
+            dx = m.template getVariable<float>("x") - x;
+            dy = m.template getVariable<float>("y") - y;
+            dz = DIMS == 3 ? m.template getVariable<float>("z") - z : 0.0f;
+        }
         if (dx * dx + dy * dy + dz * dz < r2) {
             s0 += m.template getVariable<float>("p0");
             s1 += m.template getVariable<float>("p1");
@@ -53,8 +62,12 @@ __device__ __forceinline__ flamegpu::AGENT_STATUS payload_mix(API* FLAMEGPU) {
             ++c;
         }
     };
-    if constexpr (DIMS == 3) {
+    if constexpr (DIMS == 3 && WRAP) {
+        for (const auto& m : FLAMEGPU->message_in.wrap(x, y, z)) visit(m);
+    } else if constexpr (DIMS == 3) {
         for (const auto& m : FLAMEGPU->message_in(x, y, z)) visit(m);
+    } else if constexpr (WRAP) {
+        for (const auto& m : FLAMEGPU->message_in.wrap(x, y)) visit(m);
     } else {
         for (const auto& m : FLAMEGPU->message_in(x, y)) visit(m);
     }
@@ -69,10 +82,16 @@ __device__ __forceinline__ flamegpu::AGENT_STATUS payload_mix(API* FLAMEGPU) {
 }
 
 FLAMEGPU_AGENT_FUNCTION(payload_in3, flamegpu::MessageSpatial3D, flamegpu::MessageNone) {
-    return payload_mix<3>(FLAMEGPU);
+    return payload_mix<3, false>(FLAMEGPU);
 }
 FLAMEGPU_AGENT_FUNCTION(payload_in2, flamegpu::MessageSpatial2D, flamegpu::MessageNone) {
-    return payload_mix<2>(FLAMEGPU);
+    return payload_mix<2, false>(FLAMEGPU);
+}
+FLAMEGPU_AGENT_FUNCTION(payload_in3_wrapped, flamegpu::MessageSpatial3D, flamegpu::MessageNone) {
+    return payload_mix<3, true>(FLAMEGPU);
+}
+FLAMEGPU_AGENT_FUNCTION(payload_in2_wrapped, flamegpu::MessageSpatial2D, flamegpu::MessageNone) {
+    return payload_mix<2, true>(FLAMEGPU);
 }
 
 namespace {
@@ -80,6 +99,7 @@ void* make_spatial_payload(const double* p, int32_t np) {
     auto P = [&](int i, double d) { return i < np ? p[i] : d; };
     const int dims = static_cast<int>(P(0, 3));
     const float mn = static_cast<float>(P(1, 0.0)), mx = static_cast<float>(P(2, 256.0)), r = static_cast<float>(P(3, 1.0));
+    const bool wrap = P(4, 0.0) != 0.0;
     auto* model = new flamegpu::ModelDescription("SpatialPayload");
     flamegpu::AgentDescription a = model->newAgent("agent");
     a.newVariable<float>("x");
@@ -94,7 +114,7 @@ void* make_spatial_payload(const double* p, int32_t np) {
         for (const char* n : {"p0", "p1", "p2", "p3"}) m.newVariable<float>(n);
         auto fo = a.newFunction("out", payload_out3);
         fo.setMessageOutput("location");
-        auto fi = a.newFunction("in", payload_in3);
+        auto fi = wrap ? a.newFunction("in", payload_in3_wrapped) : a.newFunction("in", payload_in3);
         fi.setMessageInput("location");
         model->newLayer().addAgentFunction(fo);
         model->newLayer().addAgentFunction(fi);
@@ -106,7 +126,7 @@ void* make_spatial_payload(const double* p, int32_t np) {
         for (const char* n : {"p0", "p1", "p2", "p3"}) m.newVariable<float>(n);
         auto fo = a.newFunction("out", payload_out2);
         fo.setMessageOutput("location");
-        auto fi = a.newFunction("in", payload_in2);
+        auto fi = wrap ? a.newFunction("in", payload_in2_wrapped) : a.newFunction("in", payload_in2);
         fi.setMessageInput("location");
         model->newLayer().addAgentFunction(fo);
         model->newLayer().addAgentFunction(fi);

@@ -33,7 +33,7 @@ EXPORTS = [
     "fg_spatial_sort_agents", "fg_compact_agents", "fg_scan_workspace_size", "fg_exclusive_scan_u32",
     "fg_last_cuda_error", "fg_version", "fg_batch_instance_init", "fg_batched_workspace_size",
     "fg_spatial_build_batched", "fg_spatial_sort_agents_batched", "fg_exclusive_scan_u32_noalloc",
-    "fg_partition_agents", "fg_append_rows",
+    "fg_partition_agents", "fg_append_rows", "fg_workspace_set_wait_limit", "fg_noalloc_scan_status",
 ]
 FG_NOALLOC_SCAN_MAX_N = 1 << 25
 
@@ -106,6 +106,8 @@ def lib():
                                             vp, vp, vp, u32, vp, sz, vp]
             L.fg_exclusive_scan_u32.argtypes = [vp, vp, u32, vp, sz, vp]
             L.fg_exclusive_scan_u32_noalloc.argtypes = [vp, vp, u32, vp]
+            L.fg_noalloc_scan_status.argtypes = [vp, C.c_int32]
+            L.fg_workspace_set_wait_limit.argtypes = [vp, sz, u32, C.c_int32, vp]
             L.fg_partition_agents.argtypes = [u32, vp, vp, C.POINTER(Column), u32, vp, vp, sz, vp]
             L.fg_append_rows.argtypes = [C.POINTER(Column), u32, u32, vp, vp, vp, u32, vp, sz, vp]
             L.fg_version.restype = C.c_char_p
@@ -158,6 +160,10 @@ class Workspace:
 
     def status(self, clear=True, stream=None) -> int:
         return lib().fg_workspace_status(self.ptr, self.nbytes, stream_handle(stream), int(clear))
+
+    def set_wait_limit(self, spin_limit=0, withhold_first_tile=False, stream=None):
+        check(lib().fg_workspace_set_wait_limit(self.ptr, self.nbytes, int(spin_limit), int(bool(withhold_first_tile)),
+                                                stream_handle(stream)), "fg_workspace_set_wait_limit")
 
 
 def record_desc(columns) -> RecordDesc:

@@ -25,11 +25,13 @@ inline cudaError_t launch(void (*kernel)(KernelArgs...), dim3 grid, dim3 block, 
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr int kThreads = 256;
 
-// Upper bound on polls of one predecessor's status in a decoupled look-back.
-// A predecessor tile always belongs to a block that is already running (tiles
-// are handed out in launch order by a ticket counter), so the wait ends in
-// practice within microseconds; the bound only turns a broken invariant into
-// a recorded error instead of a hung GPU (~2^22 polls with backoff ≈ 1-2 s).
+// Default upper bound on polls of one predecessor's status in a decoupled
+// look-back. A predecessor tile always belongs to a block that is already
+// running (tiles are handed out in launch order by a ticket counter), so the
+// wait ends in practice within microseconds; the bound only turns a broken
+// invariant into a recorded error instead of a hung GPU (~2^22 polls with
+// backoff ≈ 1-2 s). A workspace header may carry a smaller bound
+// (WsHeader::spin_limit, set by fg_workspace_set_wait_limit).
 constexpr uint32_t kSpinLimit = 1u << 22;
 
 // Workspace header: the first 256 bytes of every workspace.
@@ -44,7 +46,9 @@ struct WsHeader {
     uint32_t comp_parity;   // which compaction status array is live
     uint32_t alive_total;   // survivors, when computed here
     uint32_t key_max;       // largest sort key of an agent sort (0 between sorts)
-    uint32_t pad[54];
+    uint32_t spin_limit;    // look-back poll bound (0 = kSpinLimit)
+    uint32_t withhold;      // non-zero: tile 0 of scans and compactions does not publish (wait test)
+    uint32_t pad[52];
 };
 static_assert(sizeof(WsHeader) == 256, "header is 256 bytes");
 // words an agent-function launch resets when it computes a build's keys
@@ -72,6 +76,20 @@ __device__ __forceinline__ uint32_t ld_nc_u32(const uint32_t* p) {
     uint32_t v;
     asm("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
     return v;
+}
+
+// The look-back poll bound of a workspace.
+__device__ __forceinline__ uint32_t spin_limit_of(const WsHeader* h) {
+    const uint32_t v = h->spin_limit;
+    return v ? v : kSpinLimit;
+}
+
+// A build or sort whose scan gave up (FG_ERR_DEVICE_TIMEOUT recorded) has no
+// valid PBM: the kernels after the scan skip their work, because a PBM that is
+// not monotonic would send them past the ends of their buffers. The status is
+// written by an earlier kernel of the same stream, so it is settled here.
+__device__ __forceinline__ bool scan_gave_up(const WsHeader* h) {
+    return *reinterpret_cast<const volatile uint32_t*>(&h->status) == static_cast<uint32_t>(FG_ERR_DEVICE_TIMEOUT);
 }
 
 __device__ __forceinline__ void record_status(WsHeader* h, int32_t code) {

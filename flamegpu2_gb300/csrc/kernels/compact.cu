@@ -31,7 +31,9 @@ __device__ __forceinline__ uint64_t pair_pack(uint32_t flag, uint32_t a, uint32_
 }
 
 // Look back over predecessor tiles; returns the exclusive packed (a << 31 | b).
-__device__ __forceinline__ uint64_t lookback_pair(const uint64_t* status, uint32_t tile, WsHeader* h) {
+// At most `limit` polls per predecessor (a give-up is recorded in the header).
+__device__ __forceinline__ uint64_t lookback_pair(const uint64_t* status, uint32_t tile, WsHeader* h,
+                                                  uint32_t limit) {
     const uint32_t lane = lane_id();
     uint64_t excl = 0;
     int64_t pred = static_cast<int64_t>(tile) - 1;
@@ -46,7 +48,7 @@ __device__ __forceinline__ uint64_t lookback_pair(const uint64_t* status, uint32
                 flag = static_cast<uint32_t>(s >> 62);
                 val = s & kPairMask;
                 if (flag != 0) break;
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     record_status(h, FG_ERR_DEVICE_TIMEOUT);
                     flag = 2;
                     val = 0;
@@ -151,6 +153,8 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
     __shared__ uint64_t s_excl;
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
     const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
+    const uint32_t limit = spin_limit_of(h);
+    const bool withhold = h->withhold != 0;
     const uint32_t n = d_n ? min(*d_n, max_n) : max_n;
     const uint32_t S = d_alive_total ? *d_alive_total : h->alive_total;
     const uint32_t next_id = d_next_id ? *d_next_id : 0u;
@@ -198,10 +202,10 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
             const uint64_t agg = (static_cast<uint64_t>(s_tot[0]) << 31) | s_tot[1];
             uint64_t excl = 0;
             if (tile == 0) {
-                if (tid == 0) st_release_u64(status, pair_pack(2, s_tot[0], s_tot[1]));
+                if (tid == 0 && !withhold) st_release_u64(status, pair_pack(2, s_tot[0], s_tot[1]));
             } else {
                 if (tid == 0) st_release_u64(status + tile, (1ull << 62) | agg);
-                excl = lookback_pair(status, tile, h);
+                excl = lookback_pair(status, tile, h, limit);
                 if (tid == 0) st_release_u64(status + tile, (2ull << 62) | ((excl + agg) & kPairMask));
             }
             if (tid == 0) {

@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_
                                                    const uint32_t* __restrict__ pbm, uint32_t* __restrict__ perm,
                                                    WsHeader* h) {
     flamegpu::detail::grid_dependency_enter();
+    if (scan_gave_up(h)) return;
     const uint32_t n = load_count(d_n, max_n);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t k = keys[i];
@@ -367,6 +368,7 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
                                                         uint2* chunk_list, uint32_t chunk_cap, WsHeader* h,
                                                         const uint32_t* key_max, uint32_t key_floor) {
     flamegpu::detail::grid_dependency_enter();
+    if (scan_gave_up(h)) return;
     // key_max (agent sorts): the PBM ends at max(recorded key, key_floor) + 1
     const uint32_t total = pbm[key_max ? min(nbuckets, max(*key_max, key_floor) + 1u) : nbuckets];
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
@@ -428,6 +430,7 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
     flamegpu::detail::grid_dependency_enter();
     // the last kernel of an agent sort: the largest key is no longer read
     if (key_max_reset && blockIdx.x == 0 && threadIdx.x == 0) *key_max_reset = 0u;
+    if (scan_gave_up(h)) return;  // the same in every thread
     __shared__ uint32_t s_idx[kSortCap];
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_lo, s_hi;
@@ -932,10 +935,13 @@ static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[kNoAllocSc
 
 namespace {
 
+// Set-up state of one device's scratch. Only a successful set-up is kept: a
+// failed one (e.g. while another thread holds a global-mode stream capture)
+// is tried again by the next call. The cached address assumes the device's
+// context lives as long as the process (cudaDeviceReset is not supported).
 struct NoAllocScratch {
-    std::once_flag once;
+    std::mutex mu;
     void* ptr = nullptr;
-    cudaError_t err = cudaSuccess;
 };
 NoAllocScratch g_noalloc_scratch[64];
 
@@ -949,17 +955,17 @@ int noalloc_scratch(char** out) {
     }
     if (dev < 0 || dev >= 64) return FG_ERR_UNSUPPORTED;
     NoAllocScratch& s = g_noalloc_scratch[dev];
-    std::call_once(s.once, [&s] {
+    std::lock_guard<std::mutex> lock(s.mu);
+    if (!s.ptr) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
         if (e == cudaSuccess) e = cudaMemset(p, 0, kNoAllocScanBytes);
         if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
-        s.err = e;
-        if (e == cudaSuccess) s.ptr = p;
-    });
-    if (s.err != cudaSuccess || !s.ptr) {
-        g_last_cuda_error = static_cast<int>(s.err);
-        return FG_ERR_CUDA;
+        if (e != cudaSuccess) {
+            g_last_cuda_error = static_cast<int>(e);
+            return FG_ERR_CUDA;
+        }
+        s.ptr = p;
     }
     *out = static_cast<char*>(s.ptr);
     return FG_OK;
@@ -976,6 +982,30 @@ extern "C" int fg_exclusive_scan_u32_noalloc(const uint32_t* in, uint32_t* out, 
     if (!n) return FG_OK;
     launch_scan(in, out, n, 0, reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader)), reinterpret_cast<WsHeader*>(ws), 1,
                 static_cast<cudaStream_t>(stream));
+    return check_launch();
+}
+
+extern "C" int fg_noalloc_scan_status(void* stream, int32_t clear) {
+    char* ws = nullptr;
+    const int rc = noalloc_scratch(&ws);
+    if (rc != FG_OK) return rc;
+    return fg_workspace_status(ws, sizeof(WsHeader), stream, clear);
+}
+
+namespace fgk {
+__global__ void k_set_wait_limit(WsHeader* h, uint32_t spin_limit, uint32_t withhold) {
+    flamegpu::detail::grid_dependency_enter();
+    h->spin_limit = spin_limit;
+    h->withhold = withhold;
+}
+}  // namespace fgk
+
+extern "C" int fg_workspace_set_wait_limit(void* workspace, size_t workspace_bytes, uint32_t spin_limit,
+                                           int32_t withhold_first_tile, void* stream) {
+    if (!workspace || workspace_bytes < sizeof(WsHeader) || (reinterpret_cast<uintptr_t>(workspace) & 255))
+        return FG_ERR_INVALID_ARGUMENT;
+    launch(k_set_wait_limit, 1, 1, static_cast<cudaStream_t>(stream), reinterpret_cast<WsHeader*>(workspace),
+           spin_limit, withhold_first_tile ? 1u : 0u);
     return check_launch();
 }
 

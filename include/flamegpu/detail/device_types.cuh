@@ -106,7 +106,8 @@ struct StageHeader {
     uint32_t pbm_n;    // staged PBM entries
     uint32_t rec_bytes;
     uint32_t phase;    // mbarrier phase of the next wait
-    uint32_t pad[2];
+    uint32_t pad[1];   // bytes expected by the current window's copies
+    uint32_t off;      // non-zero once a wait gave up: this block stages nothing more
     unsigned long long mbar;
     unsigned long long pad2[3];
 };

@@ -235,6 +235,7 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, bool active, b
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&h->mbar)) : "memory");
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             h->phase = 0;
+            h->off = 0;
         }
     }
     uint32_t key = 0xFFFFFFFFu, kmax = 0u;
@@ -264,7 +265,9 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, bool active, b
         h->pbm_n = 0;
         h->rec_lo = 0;
         h->pbm_lo = 0;
-        if (s_min != 0xFFFFFFFFu) {
+        // after a wait that gave up, copies of that window may still land on
+        // the mbarrier and in the buffer: the block reads from HBM from then on
+        if (s_min != 0xFFFFFFFFu && !h->off) {
             const fg_spatial_grid& g = ctx().grid;
             const uint32_t* pbm = ctx().pbm;
             const uint32_t B = g.binCount;
@@ -318,7 +321,8 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, bool active, b
     if (h->pad[0]) {
         const uint32_t phase = h->phase;
         // a copy that has not landed after the bounded wait is waited for once
-        // more (bounded), then the window is dropped: reads fall back to HBM
+        // more (bounded), then the window is dropped and staging is switched
+        // off for the rest of this block: reads fall back to HBM
         bool ok = stage_wait(h, phase);
         if (!ok) ok = stage_wait(h, phase);
         __syncthreads();
@@ -328,6 +332,7 @@ __device__ void stage_window(const LaunchParams& P, uint32_t idx, bool active, b
                 device_error(P, kDevStageTimeout, 0, idx);
                 h->rec_n = 0;
                 h->pbm_n = 0;
+                h->off = 1;
             }
         }
     }

@@ -97,6 +97,18 @@ int fg_workspace_init(void* workspace, size_t workspace_bytes, void* stream);
 /* Device-side status recorded in a workspace (FG_OK or FG_ERR_DEVICE_TIMEOUT);
  * synchronises `stream`. clear != 0 resets it. */
 int fg_workspace_status(void* workspace, size_t workspace_bytes, void* stream, int32_t clear);
+/* Bounded-wait controls kept in a workspace's header, applied by the scans and
+ * compactions launched on it after this call (stream-ordered). spin_limit is
+ * the number of polls of one predecessor tile's status after which a
+ * decoupled look-back gives up, records FG_ERR_DEVICE_TIMEOUT and finishes
+ * (0 = the default, 2^22 polls with back-off, about a second).
+ * withhold_first_tile != 0 makes tile 0 of those kernels skip publishing its
+ * status, so that every look-back that reaches it runs out its limit: a
+ * host-side fault injection for testing the give-up path with a short limit.
+ * fg_workspace_init() restores both defaults. No counterpart in the reference
+ * (CUB's look-back has no bound). */
+int fg_workspace_set_wait_limit(void* workspace, size_t workspace_bytes, uint32_t spin_limit,
+                                int32_t withhold_first_tile, void* stream);
 
 /* Spatial message index build. Replaces MessageSpatial3D::CUDAModelHandler::buildIndex
  * (src/flamegpu/runtime/messaging/MessageSpatial3D.cu:113-146; 2D: MessageSpatial2D.cu:114-141)
@@ -207,6 +219,12 @@ int fg_exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n,
  * threads at once) race and give wrong results. Order them, e.g. on one stream.
  * out may alias in. */
 int fg_exclusive_scan_u32_noalloc(const uint32_t* in, uint32_t* out, uint32_t n, void* stream);
+/* Device-side status of the allocation-free scan's scratch on the current
+ * device: FG_OK, or FG_ERR_DEVICE_TIMEOUT if a call's bounded look-back gave up
+ * (its output is then wrong). Synchronises `stream`; clear != 0 resets it (the
+ * status is sticky until cleared). The counterpart of fg_workspace_status for
+ * fg_exclusive_scan_u32_noalloc; does the same first-call set-up. */
+int fg_noalloc_scan_status(void* stream, int32_t clear);
 
 /* ------------------------------------------------------------- batches */
 

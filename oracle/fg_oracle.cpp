@@ -681,3 +681,109 @@ extern "C" void or_predprey_run(const or_predprey_params* p, uint32_t steps, uin
         *n_pred = q;
     }
 }
+
+// ------------------------------------------------------- spatial payload model
+
+// The large spatial workloads' model (examples/spatial_payload/spatial_payload.cu,
+// written against the reference API; the reference has no such example). Per
+// step: layer 1 outputs one message per agent (position + p0..p3, in agent
+// order); before layer 2 the agents are auto-sorted by the reference's sort key
+// (CUDASimulation.cu:670-681, as or_boids_run); layer 2 averages the payload of
+// the messages within the radius, visited in the order of the clamped Filter
+// (MessageSpatial3DDevice.cuh:693-719, 2D MessageSpatial2DDevice.cuh:646-672)
+// or the WrapFilter (:727-749, 2D :673-698) with distances to the virtual
+// positions (MessageSpatial3DDevice.cuh:373-397), and mixes it into its own:
+// p_k <- 0.5 p_k + 0.5 (sum_k / count).
+extern "C" void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_period, uint32_t n, uint32_t* id,
+                               float* x, float* y, float* z, float* p, uint32_t steps, uint32_t first_step,
+                               int32_t threads) {
+    const int dims = g->dims;
+    std::vector<uint32_t> pbm(static_cast<size_t>(g->binCount) + 1), perm(n), keys(n), tmpu;
+    std::vector<float> tmpf, mx, my, mz, mp[4], sx, sy, sz, sp[4];
+    const int nt = threads < 1 ? 1 : threads;
+    const float r = g->radius;
+    const float r2 = r * r;
+    auto virt = [](float p1, float p2, float width) {  // getVirtualX: p2 - (d / |d|) * width
+        const float d = p2 - p1;
+        return std::fabs(d) > width / 2.0f ? p2 - (d / std::fabs(d) * width) : p2;
+    };
+    for (uint32_t s = 0; s < steps; ++s) {
+        const uint32_t step = first_step + s;
+        mx.assign(x, x + n);
+        my.assign(y, y + n);
+        if (dims == 3) mz.assign(z, z + n);
+        for (int k = 0; k < 4; ++k) mp[k].assign(p + static_cast<size_t>(k) * n, p + static_cast<size_t>(k + 1) * n);
+        if (sort_period && step % sort_period == 0) {
+            for (uint32_t i = 0; i < n; ++i) keys[i] = or_sort_key(g, x[i], y[i], dims == 3 ? z[i] : 0.0f);
+            or_stable_sort_perm(n, keys.data(), or_sort_max_bit(g), perm.data());
+            apply_perm(tmpu, id, perm.data(), n);
+            apply_perm(tmpf, x, perm.data(), n);
+            apply_perm(tmpf, y, perm.data(), n);
+            if (dims == 3) apply_perm(tmpf, z, perm.data(), n);
+            for (int k = 0; k < 4; ++k) apply_perm(tmpf, p + static_cast<size_t>(k) * n, perm.data(), n);
+        }
+        or_spatial_build(g, n, mx.data(), my.data(), dims == 3 ? mz.data() : nullptr, pbm.data(), perm.data(), nullptr);
+        sx.resize(n); sy.resize(n); sz.resize(n);
+        for (int k = 0; k < 4; ++k) sp[k].resize(n);
+        for (uint32_t j = 0; j < n; ++j) {
+            const uint32_t i = perm[j];
+            sx[j] = mx[i];
+            sy[j] = my[i];
+            sz[j] = dims == 3 ? mz[i] : 0.0f;
+            for (int k = 0; k < 4; ++k) sp[k][j] = mp[k][i];
+        }
+        auto work = [&](uint32_t lo, uint32_t hi) {
+            std::vector<uint32_t> cand(1024);
+            for (uint32_t i = lo; i < hi; ++i) {
+                const float ax = x[i], ay = y[i], az = dims == 3 ? z[i] : 0.0f;
+                uint32_t nc = or_neighbours(g, pbm.data(), ax, ay, az, wrap, cand.data(), static_cast<uint32_t>(cand.size()));
+                if (nc > cand.size()) {
+                    cand.resize(nc);
+                    nc = or_neighbours(g, pbm.data(), ax, ay, az, wrap, cand.data(), nc);
+                }
+                float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+                uint32_t c = 0;
+                for (uint32_t q = 0; q < nc; ++q) {
+                    const uint32_t m = cand[q];
+                    float dx, dy, dz;
+                    if (wrap) {
+                        dx = virt(ax, sx[m], g->width[0]) - ax;
+                        dy = virt(ay, sy[m], g->width[1]) - ay;
+                        dz = dims == 3 ? virt(az, sz[m], g->width[2]) - az : 0.0f;
+                    } else {
+                        dx = sx[m] - ax;
+                        dy = sy[m] - ay;
+                        dz = dims == 3 ? sz[m] - az : 0.0f;
+                    }
+                    if (dx * dx + dy * dy + dz * dz < r2) {
+                        s0 += sp[0][m];
+                        s1 += sp[1][m];
+                        s2 += sp[2][m];
+                        s3 += sp[3][m];
+                        ++c;
+                    }
+                }
+                if (c) {
+                    const float inv = 1.0f / static_cast<float>(c);
+                    float* pk[4] = {p + i, p + static_cast<size_t>(n) + i, p + 2 * static_cast<size_t>(n) + i,
+                                    p + 3 * static_cast<size_t>(n) + i};
+                    *pk[0] = 0.5f * *pk[0] + 0.5f * s0 * inv;
+                    *pk[1] = 0.5f * *pk[1] + 0.5f * s1 * inv;
+                    *pk[2] = 0.5f * *pk[2] + 0.5f * s2 * inv;
+                    *pk[3] = 0.5f * *pk[3] + 0.5f * s3 * inv;
+                }
+            }
+        };
+        if (nt == 1 || n < 1024) {
+            work(0, n);
+        } else {
+            std::vector<std::thread> pool;
+            const uint32_t chunk = (n + nt - 1) / nt;
+            for (int t = 0; t < nt; ++t) {
+                const uint32_t lo = std::min<uint32_t>(n, t * chunk), hi = std::min<uint32_t>(n, lo + chunk);
+                pool.emplace_back(work, lo, hi);
+            }
+            for (auto& th : pool) th.join();
+        }
+    }
+}

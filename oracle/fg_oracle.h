@@ -138,6 +138,16 @@ void or_predprey_run(const or_predprey_params* p, uint32_t steps, uint32_t first
                      uint32_t* n_prey, uint32_t cap_prey, float* prey_x, float* prey_y, uint32_t* prey_id,
                      uint32_t* next_prey_id, uint32_t* n_pred, float* pred_x, float* pred_y, uint32_t* pred_id);
 
+/* The large spatial workloads' model (examples/spatial_payload/spatial_payload.cu):
+ * agents with a position and payload p0..p3 (p[k*n + i]) output a spatial
+ * message each step, are auto-sorted (every sort_period steps; 0 = never),
+ * then average the payload of the messages within the radius (clamped Filter,
+ * or WrapFilter with virtual positions when wrap != 0) and mix it into their
+ * own. z is ignored (may be NULL) in 2D. threads > 1 splits the per-agent
+ * loop over host threads. */
+void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_period, uint32_t n, uint32_t* id,
+                    float* x, float* y, float* z, float* p, uint32_t steps, uint32_t first_step, int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,8 @@ def lib():
             L.or_birth_death_run.restype = C.c_uint32
             L.or_predprey_run.argtypes = [P(PredPreyParams), C.c_uint32, C.c_uint32, u32p, C.c_uint32, f32p, f32p,
                                           u32p, u32p, u32p, f32p, f32p, u32p]
+            L.or_payload_run.argtypes = [P(Grid), C.c_int32, C.c_uint32, C.c_uint32, u32p, f32p, f32p, f32p, f32p,
+                                         C.c_uint32, C.c_uint32, C.c_int32]
             L.or_mix64.argtypes = [C.c_uint64]
             L.or_mix64.restype = C.c_uint64
             L.or_hash_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32]
@@ -216,6 +218,25 @@ def birth_death_run(f, counter, ids, next_id, cap, p_death, p_birth, seed, steps
                                  _p(nid, C.c_uint32), p_death, p_birth, seed, steps, first_step,
                                  _p(pops, C.c_uint32))
     return fb[:, :m].copy(), cb[:m].copy(), ib[:m].copy(), int(nid[0]), pops[:steps].copy()
+
+
+def payload_run(g: Grid, wrap: bool, state: dict, steps: int, first_step: int = 0, sort_period: int = 1,
+                threads: int = 1) -> dict:
+    """The large spatial workloads' model. state: id (u32), x, y[, z], p0..p3 (f32).
+    Returns a new dict in the agents' final order."""
+    dims = g.dims
+    keys = ["x", "y"] + (["z"] if dims == 3 else [])
+    s = {"id": np.array(state["id"], np.uint32, copy=True)}
+    for k in keys:
+        s[k] = np.array(state[k], np.float32, copy=True)
+    n = s["x"].shape[0]
+    pay = np.ascontiguousarray(np.stack([np.asarray(state[f"p{k}"], np.float32) for k in range(4)]))
+    lib().or_payload_run(C.byref(g), int(wrap), int(sort_period), n, _p(s["id"], C.c_uint32), _p(s["x"], C.c_float),
+                         _p(s["y"], C.c_float), _p(s.get("z"), C.c_float), _p(pay, C.c_float), steps, first_step,
+                         threads)
+    for k in range(4):
+        s[f"p{k}"] = pay[k].copy()
+    return s
 
 
 def hash_uniform(seed, key, step, stream) -> float:

@@ -1,26 +1,26 @@
 """Small, fixed cases for profiling single kernels (ncu) and per-operation
 timings, outside the benchmark's timed loop.
 
-  python -m flamegpu2_gb300.profile_cases boids --n 1048576
+  python profile_cases.py boids --n 1048576
       Boids (wrapped, radius 2) at about one agent per bin: edge =
       4 r cbrt(N/64), the density of the batched-ensemble instances;
       prints per-operation timings (CUDA events, eager) and graph step time.
-  python -m flamegpu2_gb300.profile_cases ensemble --count 32
+  python profile_cases.py ensemble --count 32
       The first `count` instances of the 256-instance Boids ensemble, 5 steps,
       as one batched simulation.
-  python -m flamegpu2_gb300.profile_cases payload --dims 2 --n 4194304
+  python profile_cases.py payload --dims 2 --n 4194304
       The large spatial workloads' model (position + 4 payload words, squared
       distance test) at population n and the same density (2D uniform, r = 4,
       16 agents per bin; 3D Gaussian mixture, r = 1); per-operation timings and
       graph step time.
-  python -m flamegpu2_gb300.profile_cases build --dims 3
+  python profile_cases.py build --dims 3
       Five spatial message builds through the C ABI (fg_spatial_build) of the
       large workloads' positions: 8,388,608 Gaussian-mixture messages on 256^3
       bins (--dims 3) or 16,777,216 uniform messages on 1024^2 bins (--dims 2),
       records of position + 4 payload words; prints the mean build time.
       --sorted orders the messages by bin first, as the messages of agents
       that the automatic spatial sort has ordered arrive in a simulation.
-  python -m flamegpu2_gb300.profile_cases sort --dims 3 --sorted
+  python profile_cases.py sort --dims 3 --sorted
       Five automatic spatial agent sorts through the C ABI
       (fg_spatial_sort_agents) of the same positions with their agent columns
       (8 x 4 bytes in 3D, 7 in 2D); --sorted gives an already sorted population.

@@ -5,9 +5,10 @@
 1. Compiles gen_golden.cpp (g++) — a restatement of the reference tests'
    population generators and host-side expectations — runs it, and packs its
    raw arrays into reference_tests.npz.
-2. When the reference tree is present, builds oracle/_ref/numeric_pin from the
-   reference's own include/flamegpu/detail/numeric.h (oracle/Makefile `ref`)
-   and stores its outputs as wrap_compatible.json.
+2. When FLAMEGPU2_REFERENCE names a FLAME GPU 2 source tree, builds
+   oracle/_ref/numeric_pin from the reference's own
+   include/flamegpu/detail/numeric.h (oracle/Makefile `ref`) and stores its
+   outputs as wrap_compatible.json.
 
 The fixtures are committed; the tests only read them.
 """
@@ -37,8 +38,9 @@ def main():
             arrays[name] = np.fromfile(os.path.join(td, fn), dtype=dt)
         np.savez_compressed(os.path.join(HERE, "reference_tests.npz"), **arrays)
         print("wrote reference_tests.npz:", ", ".join(f"{k}{v.shape}" for k, v in arrays.items()))
-    if os.path.isdir("/root/reference/include"):
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    ref = os.environ.get("FLAMEGPU2_REFERENCE", "")
+    if ref and os.path.isdir(os.path.join(ref, "include")):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + ref], check=True)
         out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "numeric_pin")], check=True,
                              capture_output=True, text=True).stdout
         rows = json.loads(out)
@@ -47,7 +49,7 @@ def main():
                        "rows": rows}, f, indent=0)
         print("wrote wrap_compatible.json:", len(rows), "rows")
     else:
-        print("reference tree absent: wrap_compatible.json left as committed", file=sys.stderr)
+        print("FLAMEGPU2_REFERENCE not set: wrap_compatible.json left as committed", file=sys.stderr)
 
 
 if __name__ == "__main__":

@@ -14,8 +14,9 @@ def _capi():
 
 def test_noalloc_scan_declared_and_exported():
     capi = _capi()
-    assert "fg_exclusive_scan_u32_noalloc" in capi.EXPORTS
-    assert hasattr(capi.lib(), "fg_exclusive_scan_u32_noalloc")
+    for name in ("fg_exclusive_scan_u32_noalloc", "fg_noalloc_scan_status"):
+        assert name in capi.EXPORTS
+        assert hasattr(capi.lib(), name)
 
 
 def test_noalloc_scan_rejects_before_touching_the_device():
@@ -47,19 +48,31 @@ def test_noalloc_scan_matches_workspace_scan(n):
         np.testing.assert_array_equal(got.cpu().numpy(), ref.cpu().numpy())
         expect = (np.cumsum(a.astype(np.uint64)) - a).astype(np.uint32)
         np.testing.assert_array_equal(got.cpu().numpy().view(np.uint32), expect)
+        # the device-side status of the static scratch: no bounded wait gave up
+        assert L.fg_noalloc_scan_status(st, 1) == capi.FG_OK
 
 
 @pytest.mark.gpu
-def test_noalloc_scan_in_place_and_max_size_refused():
+@pytest.mark.parametrize("n", [300_000, (1 << 22) + 4097, 1 << 25])
+def test_noalloc_scan_in_place(n):
+    # n above 2^22 takes the four-sub-tile path, which reads its input again
+    # after the look-back: in place, every tile must still see its own input
     import torch
     capi = _capi()
     L = capi.lib()
-    n = 300_000
     a = np.random.default_rng(5).integers(0, 9, n).astype(np.uint32)
     t = torch.from_numpy(a.view(np.int32)).cuda()
     capi.check(L.fg_exclusive_scan_u32_noalloc(t.data_ptr(), t.data_ptr(), n, capi.stream_handle()), "in place")
     torch.cuda.synchronize()
     np.testing.assert_array_equal(t.cpu().numpy().view(np.uint32), (np.cumsum(a.astype(np.uint64)) - a).astype(np.uint32))
+    assert L.fg_noalloc_scan_status(capi.stream_handle(), 1) == capi.FG_OK
+
+
+@pytest.mark.gpu
+def test_noalloc_scan_max_size_refused():
+    import torch
+    capi = _capi()
+    L = capi.lib()
     big = torch.zeros(16, dtype=torch.int32, device="cuda")
     assert L.fg_exclusive_scan_u32_noalloc(big.data_ptr(), big.data_ptr(), capi.FG_NOALLOC_SCAN_MAX_N + 1,
                                            capi.stream_handle()) == capi.FG_ERR_WORKSPACE
