@@ -272,7 +272,10 @@ def run_spatial_large(name, args, world, rank, local):
             "note": "iterate is on-chip bound here (see stages.fn:in.candidate_pairs_per_s)"}
     roof = _with_traffic(roof, "spatial_large_build", "the four build kernels a simulation step runs, from a "
                          "standalone build of this size", name)
-    return {
+    cpu = None
+    if world == 1 and rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_payload(dims, edge, r, cols, 20_000 if dims == 3 else 1_000_000)
+    out = {
         "metric": B.METRIC, "value": round(n * k_steps * world / (device_ms / 1000.0), 1), "unit": UNIT,
         "n_gpus": world, "steps": k_steps, "warmup": args.warmup, "ms_per_step": round(device_ms / k_steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -281,6 +284,30 @@ def run_spatial_large(name, args, world, rank, local):
                    "l2": "working set larger than L2"},
         "wall_s": round(wall, 4), "roofline": roof, "stages": stages, "gpu_launches": kps * k_steps, "clocks": clk,
     }
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
+    return out
+
+
+def cpu_baseline_payload(dims, edge, r, cols, m):
+    """The serial oracle on a bounded sample of the full-size workload: one
+    model step in which the oracle sorts and builds the whole population and
+    only m randomly chosen agents run the iterate layer, so each agent's
+    iterate costs what it costs at full size. The step time is extrapolated to
+    the whole population: t(sort + build) + t(iterate of m) * n / m."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import oracle as O
+    n = cols["x"].shape[0]
+    g = O.grid(dims, [0.0] * dims, [edge] * dims, r)
+    st = {"id": cols["_id"], **{k: v for k, v in cols.items() if k != "_id"}}
+    sample = np.sort(np.random.default_rng(11).choice(n, m, replace=False))
+    _, t_index, t_iter = O.payload_step_sampled(g, False, st, sample)
+    step_s = t_index + t_iter * n / m
+    return {"value": round(n / step_s, 1), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"one model step of the full {n:,}-agent population: serial sort + message build of all "
+                      f"agents ({t_index:.1f} s) and the iterate of {m:,} random agents ({t_iter:.1f} s), "
+                      f"extrapolated to {n:,} agents ({step_s:.0f} s per step)"}
 
 
 # ------------------------------------------------------------ batched ensemble

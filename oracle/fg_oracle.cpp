@@ -8,6 +8,7 @@
 #include "fg_oracle.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -694,9 +695,12 @@ extern "C" void or_predprey_run(const or_predprey_params* p, uint32_t steps, uin
 // or the WrapFilter (:727-749, 2D :673-698) with distances to the virtual
 // positions (MessageSpatial3DDevice.cuh:373-397), and mixes it into its own:
 // p_k <- 0.5 p_k + 0.5 (sum_k / count).
-extern "C" void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_period, uint32_t n, uint32_t* id,
-                               float* x, float* y, float* z, float* p, uint32_t steps, uint32_t first_step,
-                               int32_t threads) {
+namespace {
+// sample (m rows, optional): only these agents run layer 2; times (optional)
+// receives the seconds spent in the sort + build and in layer 2.
+void payload_impl(const or_grid* g, int32_t wrap, uint32_t sort_period, uint32_t n, uint32_t* id, float* x, float* y,
+                  float* z, float* p, uint32_t steps, uint32_t first_step, int32_t threads, const uint32_t* sample,
+                  uint32_t m, double* times) {
     const int dims = g->dims;
     std::vector<uint32_t> pbm(static_cast<size_t>(g->binCount) + 1), perm(n), keys(n), tmpu;
     std::vector<float> tmpf, mx, my, mz, mp[4], sx, sy, sz, sp[4];
@@ -707,8 +711,10 @@ extern "C" void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_per
         const float d = p2 - p1;
         return std::fabs(d) > width / 2.0f ? p2 - (d / std::fabs(d) * width) : p2;
     };
+    if (times) times[0] = times[1] = 0.0;
     for (uint32_t s = 0; s < steps; ++s) {
         const uint32_t step = first_step + s;
+        const auto t0 = std::chrono::steady_clock::now();
         mx.assign(x, x + n);
         my.assign(y, y + n);
         if (dims == 3) mz.assign(z, z + n);
@@ -732,9 +738,12 @@ extern "C" void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_per
             sz[j] = dims == 3 ? mz[i] : 0.0f;
             for (int k = 0; k < 4; ++k) sp[k][j] = mp[k][i];
         }
+        const auto t1 = std::chrono::steady_clock::now();
+        const uint32_t rows = sample ? m : n;
         auto work = [&](uint32_t lo, uint32_t hi) {
             std::vector<uint32_t> cand(1024);
-            for (uint32_t i = lo; i < hi; ++i) {
+            for (uint32_t r = lo; r < hi; ++r) {
+                const uint32_t i = sample ? sample[r] : r;
                 const float ax = x[i], ay = y[i], az = dims == 3 ? z[i] : 0.0f;
                 uint32_t nc = or_neighbours(g, pbm.data(), ax, ay, az, wrap, cand.data(), static_cast<uint32_t>(cand.size()));
                 if (nc > cand.size()) {
@@ -774,16 +783,33 @@ extern "C" void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_per
                 }
             }
         };
-        if (nt == 1 || n < 1024) {
-            work(0, n);
+        if (nt == 1 || rows < 1024) {
+            work(0, rows);
         } else {
             std::vector<std::thread> pool;
-            const uint32_t chunk = (n + nt - 1) / nt;
+            const uint32_t chunk = (rows + nt - 1) / nt;
             for (int t = 0; t < nt; ++t) {
-                const uint32_t lo = std::min<uint32_t>(n, t * chunk), hi = std::min<uint32_t>(n, lo + chunk);
+                const uint32_t lo = std::min<uint32_t>(rows, t * chunk), hi = std::min<uint32_t>(rows, lo + chunk);
                 pool.emplace_back(work, lo, hi);
             }
             for (auto& th : pool) th.join();
         }
+        if (times) {
+            const auto t2 = std::chrono::steady_clock::now();
+            times[0] += std::chrono::duration<double>(t1 - t0).count();
+            times[1] += std::chrono::duration<double>(t2 - t1).count();
+        }
     }
+}
+}  // namespace
+
+extern "C" void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_period, uint32_t n, uint32_t* id,
+                               float* x, float* y, float* z, float* p, uint32_t steps, uint32_t first_step,
+                               int32_t threads) {
+    payload_impl(g, wrap, sort_period, n, id, x, y, z, p, steps, first_step, threads, nullptr, 0, nullptr);
+}
+
+extern "C" void or_payload_step_sampled(const or_grid* g, int32_t wrap, uint32_t n, uint32_t* id, float* x, float* y,
+                                        float* z, float* p, uint32_t m, const uint32_t* sample, double* times) {
+    payload_impl(g, wrap, 1, n, id, x, y, z, p, 1, 0, 1, sample, m, times);
 }

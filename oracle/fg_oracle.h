@@ -147,6 +147,13 @@ void or_predprey_run(const or_predprey_params* p, uint32_t steps, uint32_t first
  * loop over host threads. */
 void or_payload_run(const or_grid* g, int32_t wrap, uint32_t sort_period, uint32_t n, uint32_t* id,
                     float* x, float* y, float* z, float* p, uint32_t steps, uint32_t first_step, int32_t threads);
+/* One step of the same model in which only the m agents sample[0..m) (indices
+ * after the step's automatic sort) run the iterate layer, serially: the CPU
+ * baseline's bounded sample of a full-size population. times[0] receives the
+ * seconds of the sort and the message build (whole population), times[1]
+ * those of the sample's iterate. */
+void or_payload_step_sampled(const or_grid* g, int32_t wrap, uint32_t n, uint32_t* id, float* x, float* y,
+                             float* z, float* p, uint32_t m, const uint32_t* sample, double* times);
 
 #ifdef __cplusplus
 }

@@ -90,6 +90,8 @@ def lib():
                                           u32p, u32p, u32p, f32p, f32p, u32p]
             L.or_payload_run.argtypes = [P(Grid), C.c_int32, C.c_uint32, C.c_uint32, u32p, f32p, f32p, f32p, f32p,
                                          C.c_uint32, C.c_uint32, C.c_int32]
+            L.or_payload_step_sampled.argtypes = [P(Grid), C.c_int32, C.c_uint32, u32p, f32p, f32p, f32p, f32p,
+                                                  C.c_uint32, u32p, P(C.c_double)]
             L.or_mix64.argtypes = [C.c_uint64]
             L.or_mix64.restype = C.c_uint64
             L.or_hash_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32]
@@ -237,6 +239,26 @@ def payload_run(g: Grid, wrap: bool, state: dict, steps: int, first_step: int = 
     for k in range(4):
         s[f"p{k}"] = pay[k].copy()
     return s
+
+
+def payload_step_sampled(g: Grid, wrap: bool, state: dict, sample) -> tuple:
+    """One serial step of the payload model over the whole population in which
+    only the agents at sorted positions `sample` iterate. Returns
+    (new state, seconds of sort + build, seconds of the sample's iterate)."""
+    dims = g.dims
+    s = {"id": np.array(state["id"], np.uint32, copy=True)}
+    for k in ["x", "y"] + (["z"] if dims == 3 else []):
+        s[k] = np.array(state[k], np.float32, copy=True)
+    n = s["x"].shape[0]
+    pay = np.ascontiguousarray(np.stack([np.asarray(state[f"p{k}"], np.float32) for k in range(4)]))
+    smp = np.ascontiguousarray(sample, np.uint32)
+    t = np.zeros(2, np.float64)
+    lib().or_payload_step_sampled(C.byref(g), int(wrap), n, _p(s["id"], C.c_uint32), _p(s["x"], C.c_float),
+                                  _p(s["y"], C.c_float), _p(s.get("z"), C.c_float), _p(pay, C.c_float),
+                                  smp.shape[0], _p(smp, C.c_uint32), _p(t, C.c_double))
+    for k in range(4):
+        s[f"p{k}"] = pay[k].copy()
+    return s, float(t[0]), float(t[1])
 
 
 def hash_uniform(seed, key, step, stream) -> float:
