@@ -34,6 +34,7 @@ EXPORTS = [
     "fg_last_cuda_error", "fg_version", "fg_batch_instance_init", "fg_batched_workspace_size",
     "fg_spatial_build_batched", "fg_spatial_sort_agents_batched", "fg_exclusive_scan_u32_noalloc",
     "fg_partition_agents", "fg_append_rows", "fg_workspace_set_wait_limit", "fg_noalloc_scan_status",
+    "fg_append_births",
 ]
 FG_NOALLOC_SCAN_MAX_N = 1 << 25
 
@@ -110,6 +111,7 @@ def lib():
             L.fg_workspace_set_wait_limit.argtypes = [vp, sz, u32, C.c_int32, vp]
             L.fg_partition_agents.argtypes = [u32, vp, vp, C.POINTER(Column), u32, vp, vp, sz, vp]
             L.fg_append_rows.argtypes = [C.POINTER(Column), u32, u32, vp, vp, vp, u32, vp, sz, vp]
+            L.fg_append_births.argtypes = [u32, vp, vp, C.POINTER(Column), u32, C.c_int32, vp, vp, u32, vp, sz, vp]
             L.fg_version.restype = C.c_char_p
             L.fg_batch_instance_init.argtypes = [C.POINTER(BatchInstance), C.POINTER(SpatialGrid), u32, u32, u32,
                                                  C.c_int32, C.POINTER(u32)]

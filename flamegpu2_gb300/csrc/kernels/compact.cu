@@ -173,9 +173,10 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
         for (int k = 0; k < kCompItems; ++k) {
             const uint32_t i = base + k * kThreads + tid;
             const bool in = i < n;
-            const bool a = in && (alive == nullptr || alive[i] != 0);
-            // partition: every row not in the first group goes, in order, to the second
-            const bool b = in && (partition ? !a : (born != nullptr && born[i] != 0));
+            // partition 2 (births only): no row is a survivor
+            const bool a = in && partition != 2 && (alive == nullptr || alive[i] != 0);
+            // partition 1: every row not in the first group goes, in order, to the second
+            const bool b = in && (partition == 1 ? !a : (born != nullptr && born[i] != 0));
             ba[k] = __ballot_sync(0xFFFFFFFFu, a);
             bb[k] = __ballot_sync(0xFFFFFFFFu, b);
             if (lane == 0) {
@@ -231,8 +232,10 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
             if ((bb[k] >> lane) & 1u) {
                 const uint32_t r = eb + s_cnt_b[k][warp] + __popc(bb[k] & lt);
                 const uint32_t dst = S + r;
+                // a birth flagged 2 claimed its id during the function: kept
+                const bool claimed = partition != 1 && born != nullptr && born[i] == 2u;
                 if (dst < out_capacity)
-                    copy_row(cp.bcol, cp.ncols, i, dst, cp.id_col, next_id + r);
+                    copy_row(cp.bcol, cp.ncols, i, dst, claimed ? -1 : cp.id_col, next_id + r);
                 else
                     record_status(h, FG_ERR_CAPACITY);
             }
@@ -350,6 +353,33 @@ extern "C" int fg_partition_agents(uint32_t max_n, const uint32_t* d_n, const ui
     const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
     launch(k_compact, comp_grid(max_n), kThreads, st, cp, max_n, d_n, first_group, nullptr, nullptr, nullptr, nullptr,
            max_n, status, stride_tiles, h, 1, d_first_count);
+    return launch_err();
+}
+
+extern "C" int fg_append_births(uint32_t max_n, const uint32_t* d_n, const uint32_t* born, const fg_column* cols,
+                                uint32_t ncols, int32_t id_col, uint32_t* d_next_id, uint32_t* d_dst_count,
+                                uint32_t dst_capacity, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!workspace || !born || !d_dst_count || ncols > FG_MAX_COLUMNS || (ncols && !cols))
+        return FG_ERR_INVALID_ARGUMENT;
+    if (id_col >= static_cast<int32_t>(ncols)) return FG_ERR_INVALID_ARGUMENT;
+    if (id_col >= 0 && (cols[id_col].elem_bytes != 4 || !d_next_id)) return FG_ERR_INVALID_ARGUMENT;
+    if (max_n >= (1u << 31)) return FG_ERR_UNSUPPORTED;
+    if (workspace_bytes < fg_compact_workspace_size(max_n) || (reinterpret_cast<uintptr_t>(workspace) & 255))
+        return FG_ERR_WORKSPACE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(workspace);
+    WsHeader* h = reinterpret_cast<WsHeader*>(ws);
+    uint64_t* status = reinterpret_cast<uint64_t*>(ws + sizeof(WsHeader));
+    // births-only compaction: no survivors, "S" = the destination's count, so
+    // birth r lands at *d_dst_count + r and the count grows by the births
+    CompactParams cp{};
+    for (uint32_t c = 0; c < ncols; ++c) cp.col[c] = cp.bcol[c] = cols[c];
+    cp.ncols = ncols;
+    cp.id_col = id_col;
+    const uint32_t stride_tiles = static_cast<uint32_t>((workspace_bytes - sizeof(WsHeader)) / (2 * sizeof(uint64_t)));
+    launch(k_compact, comp_grid(max_n), kThreads, st, cp, max_n, d_n, nullptr, born, id_col >= 0 ? d_next_id : nullptr,
+           static_cast<const uint32_t*>(d_dst_count), d_dst_count, dst_capacity, status, stride_tiles, h, 2,
+           nullptr);
     return launch_err();
 }
 

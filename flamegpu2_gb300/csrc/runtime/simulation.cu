@@ -322,6 +322,13 @@ struct FnRt {
     MsgList* in = nullptr;
     MsgList* out = nullptr;
     bool births = false;
+    // the list births go to (setAgentOutput's agent and state). Fused: it is the
+    // list where the function's own agents end up (their list, or the end
+    // state's), so one compaction writes survivors then births; otherwise the
+    // births are appended to it after the death compaction and the transition
+    AgentList* birth_list = nullptr;
+    bool births_fused = false;
+    uint32_t* d_launch_n = nullptr;  // rows the function ran over (unfused births)
     uint32_t* death_flags = nullptr;
     uint32_t* birth_flags = nullptr;
     std::vector<void*> birth_cols;
@@ -510,15 +517,12 @@ struct SimulationImpl {
                 r.out = f->message_output.empty() ? nullptr : msg_of(f->message_output);
                 if (r.out && f->message_output_optional) r.out->optional_any = true;
                 if (!f->agent_output.empty()) {
-                    // births land after the function's surviving agents, which a
-                    // state transition then moves: the output state must be
-                    // where those agents end up
-                    if (f->agent_output != a->name || f->agent_output_state != f->end_state)
-                        THROW exception::InvalidAgentFunc(format(
-                            "Function '%s': agent output is supported into the function's own agent type and end state "
-                            "('%s'), not '%s' state '%s'",
-                            f->name.c_str(), f->end_state.c_str(), f->agent_output.c_str(), f->agent_output_state.c_str()));
+                    // CUDASimulation.cu:1062-1080: death compaction, then the state
+                    // transition, then the births appended to the output list
                     r.births = true;
+                    r.birth_list = list_of(f->agent_output, f->agent_output_state);
+                    r.births_fused = r.birth_list == (r.end_list ? r.end_list : r.list);
+                    if (!r.births_fused) r.d_launch_n = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
                 }
                 // determineAgentsToSort (CUDASimulation.cu:409-461)
                 if (r.in && r.in->spatial()) {
@@ -587,11 +591,13 @@ struct SimulationImpl {
                 if (!f.d_first) f.d_first = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
             }
             if (f.births) {
+                // staging: one row of the output agent's variables per parent row
                 mem.release(f.birth_flags);
                 f.birth_flags = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
                 for (void* p : f.birth_cols) mem.release(p);
                 f.birth_cols.clear();
-                for (const auto& v : l.agent->variables) f.birth_cols.push_back(mem.alloc(static_cast<size_t>(v.bytes()) * cap));
+                for (const auto& v : f.birth_list->agent->variables)
+                    f.birth_cols.push_back(mem.alloc(static_cast<size_t>(v.bytes()) * cap));
             }
         }
         invalidate();
@@ -747,15 +753,16 @@ struct SimulationImpl {
                 std::vector<TableEntry> d;
                 std::vector<char> defaults;
                 std::vector<size_t> doff;
-                for (const auto& var : l.agent->variables) {
+                const AgentData* ba = f.birth_list->agent;
+                for (const auto& var : ba->variables) {
                     doff.push_back(defaults.size());
                     defaults.insert(defaults.end(), var.default_value.begin(), var.default_value.end());
                     defaults.resize((defaults.size() + 7) & ~size_t(7));
                 }
                 if (!f.birth_defaults) f.birth_defaults = mem.alloc(defaults.size());
                 FG_CUDA(cudaMemcpy(f.birth_defaults, defaults.data(), defaults.size(), cudaMemcpyHostToDevice));
-                for (size_t v = 0; v < l.agent->variables.size(); ++v) {
-                    const Variable& var = l.agent->variables[v];
+                for (size_t v = 0; v < ba->variables.size(); ++v) {
+                    const Variable& var = ba->variables[v];
                     e.push_back({fnv1a32(var.name), static_cast<char*>(f.birth_cols[v]), var.bytes(), var.type_size, var.elements});
                     d.push_back({fnv1a32(var.name), static_cast<char*>(f.birth_defaults) + doff[v], var.bytes(), var.type_size, var.elements});
                 }
@@ -796,30 +803,25 @@ struct SimulationImpl {
     size_t count_next = 0;
     uint32_t* count_pinned = nullptr;
 
-    int births_per_step(const AgentList* l) const {
-        int b = 0;
-        for (const auto& layer : model->layers)
-            for (auto* fd : layer->functions)
-                for (const auto& f : fns)
-                    if (f.fn == fd && f.births && f.list == l) ++b;
-        return b;
+    // Whether some function's births are written to list l (fused births are
+    // written to the function's own list first, then move with a transition).
+    bool receives_births(const AgentList* l) const {
+        for (const auto& f : fns)
+            if (f.births && (f.birth_list == l || (f.births_fused && f.list == l))) return true;
+        return false;
     }
     // Rows to allocate for a population of n: with a population limit, a list
     // that births can grow starts at the limit (the memory a served run was
     // budgeted for), so capacity checks rarely need a count from the device.
     uint32_t initial_capacity(const AgentList* l, uint32_t n) const {
         uint32_t cap = std::max<uint32_t>(1024u, n);
-        if (cuda_config.max_agents && births_per_step(l) > 0) cap = std::max(cap, cuda_config.max_agents);
+        if (cuda_config.max_agents && receives_births(l)) cap = std::max(cap, cuda_config.max_agents);
         return cap;
     }
     bool any_births() const {
         for (const auto& f : fns)
             if (f.births) return true;
         return false;
-    }
-    static uint64_t grow_bound(uint64_t base, int doublings) {
-        for (int d = 0; d < doublings && base < (1ull << 33); ++d) base *= 2;
-        return base;
     }
 
     // Populations were replaced from the host: earlier reports no longer apply.
@@ -860,11 +862,31 @@ struct SimulationImpl {
             if (lists[i].get() == l) return i;
         return 0;
     }
-    // A transition can move a whole list (its bound) into the end state's
-    // list once per step.
-    void add_transitions(std::vector<uint64_t>& bound, uint64_t rounds) const {
-        for (const auto& f : fns)
-            if (f.end_list) bound[list_index(f.end_list)] += bound[list_index(f.list)] * rounds;
+    // Upper bounds of every list's population `rounds` steps on from `bound`:
+    // in layer order, a function with births adds up to its list's bound to
+    // its output list, or, fused, to its own list (doubling it: survivors and
+    // births share it until a transition moves them on), and a state
+    // transition moves up to its list's bound into its end list (not
+    // subtracted from the source, so the result stays an upper bound). Capped
+    // at 2^33.
+    void advance_bounds(std::vector<uint64_t>& bound, uint64_t rounds) const {
+        constexpr uint64_t kMax = 1ull << 33;
+        if (!any_births() && !any_transitions()) return;
+        for (uint64_t r = 0; r < rounds; ++r)
+            for (const auto& layer : model->layers)
+                for (auto* fd : layer->functions)
+                    for (const auto& f : fns) {
+                        if (f.fn != fd) continue;
+                        const uint64_t src = bound[list_index(f.list)];
+                        if (f.births) {
+                            uint64_t& t = bound[list_index(f.births_fused ? f.list : f.birth_list)];
+                            t = std::min(t + src, kMax);
+                        }
+                        if (f.end_list) {
+                            uint64_t& t = bound[list_index(f.end_list)];
+                            t = std::min(t + bound[list_index(f.list)], kMax);
+                        }
+                    }
     }
 
     void prepare_capacity() {
@@ -878,26 +900,18 @@ struct SimulationImpl {
         }
         std::vector<uint64_t> bound(lists.size());
         bool over = false;
-        for (size_t i = 0; i < lists.size(); ++i) {
-            const int b = births_per_step(lists[i].get());
-            if (known && known->step_after <= step_count) {
-                const unsigned int pending = step_count - known->step_after;  // steps issued after the report
-                bound[i] = grow_bound(std::min<uint64_t>(known->host[i], lists[i]->bound), b * static_cast<int>(pending + 1));
-            } else {
-                bound[i] = grow_bound(lists[i]->bound, b);
-            }
-        }
-        {
-            const uint64_t rounds = (known && known->step_after <= step_count) ? step_count - known->step_after + 1 : 1;
-            add_transitions(bound, rounds);
-        }
+        // from the newest report: the steps issued after it, then this one
+        const bool have = known && known->step_after <= step_count;
+        for (size_t i = 0; i < lists.size(); ++i)
+            bound[i] = have ? std::min<uint64_t>(known->host[i], lists[i]->bound) : lists[i]->bound;
+        advance_bounds(bound, have ? step_count - known->step_after + 1 : 1);
         for (size_t i = 0; i < lists.size(); ++i)
             if (bound[i] > lists[i]->capacity) over = true;
         if (over) {
             // exact counts after every issued step, then grow what needs it
             sync_counts();
-            for (size_t i = 0; i < lists.size(); ++i) bound[i] = grow_bound(lists[i]->bound, births_per_step(lists[i].get()));
-            add_transitions(bound, 1);
+            for (size_t i = 0; i < lists.size(); ++i) bound[i] = lists[i]->bound;
+            advance_bounds(bound, 1);
             for (size_t i = 0; i < lists.size(); ++i) {
                 if (cuda_config.max_agents && bound[i] > cuda_config.max_agents)
                     THROW exception::OutOfMemory(format("Agent '%s' may reach %llu agents in the next step, above the limit of %u",
@@ -1220,6 +1234,7 @@ struct SimulationImpl {
             }
         }
         P.birth_flags = f.births ? f.birth_flags : nullptr;
+        P.birth_next_id = f.births ? d_next_id(agent_index(f.birth_list->agent)) : nullptr;
         P.death_flags = f.fn->has_agent_death ? f.death_flags : nullptr;
         P.d_step = d_step();
         P.seed = config.random_seed;
@@ -1251,20 +1266,26 @@ struct SimulationImpl {
                 kernel_counter += 2;
             }
         }
-        if (f.fn->has_agent_death || f.births) {
+        // births into another list: the rows the function ran over, before the
+        // death compaction and transition change the list's count
+        const bool fused = f.births && f.births_fused;
+        if (f.births && !fused) {
+            FG_CUDA(cudaMemcpyAsync(f.d_launch_n, l.d_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+        }
+        if (f.fn->has_agent_death || fused) {
             std::vector<fg_column> cols(l.cols.size()), bcols(l.cols.size());
             int id_col = -1;
             for (size_t v = 0; v < l.cols.size(); ++v) {
                 const uint32_t b = l.agent->variables[v].bytes();
                 cols[v] = fg_column{l.cols[v][l.parity], l.cols[v][l.parity ^ 1], b};
-                bcols[v] = fg_column{f.births ? f.birth_cols[v] : l.cols[v][l.parity], l.cols[v][l.parity ^ 1], b};
+                bcols[v] = fg_column{fused ? f.birth_cols[v] : l.cols[v][l.parity], l.cols[v][l.parity ^ 1], b};
                 if (l.agent->variables[v].name == "_id") id_col = static_cast<int>(v);
             }
             timed("compact:" + l.agent->name, [&] {
                 FG_CAPI(fg_compact_agents(l.capacity, l.d_count, f.fn->has_agent_death ? f.death_flags : nullptr,
-                                          f.births ? f.birth_flags : nullptr, cols.data(), bcols.data(),
-                                          static_cast<uint32_t>(cols.size()), f.births ? id_col : -1,
-                                          f.births ? d_next_id(agent_index(l.agent)) : nullptr, nullptr, l.d_count,
+                                          fused ? f.birth_flags : nullptr, cols.data(), bcols.data(),
+                                          static_cast<uint32_t>(cols.size()), fused ? id_col : -1,
+                                          fused ? d_next_id(agent_index(l.agent)) : nullptr, nullptr, l.d_count,
                                           l.capacity, l.comp_ws, l.comp_ws_bytes, stream));
             });
             l.parity ^= 1;
@@ -1284,6 +1305,23 @@ struct SimulationImpl {
                                        E.comp_ws_bytes, stream));
             });
             kernel_counter += 2;
+        }
+        if (f.births && !fused) {
+            // CUDAAgent::scatterNew (CUDAAgent.cu:427-450): the new agents are
+            // appended after the output list's agents, in parent order
+            AgentList& B = *f.birth_list;
+            std::vector<fg_column> bc(B.cols.size());
+            int id_col = -1;
+            for (size_t v = 0; v < B.cols.size(); ++v) {
+                bc[v] = fg_column{f.birth_cols[v], B.cols[v][B.parity], B.agent->variables[v].bytes()};
+                if (B.agent->variables[v].name == "_id") id_col = static_cast<int>(v);
+            }
+            timed("birth:" + B.agent->name, [&] {
+                FG_CAPI(fg_append_births(l.capacity, f.d_launch_n, f.birth_flags, bc.data(), static_cast<uint32_t>(bc.size()),
+                                         id_col, d_next_id(agent_index(B.agent)), B.d_count, B.capacity, l.comp_ws,
+                                         l.comp_ws_bytes, stream));
+            });
+            kernel_counter += 1;
         }
     }
 
@@ -1437,15 +1475,23 @@ struct SimulationImpl {
         ensure_all_allocated();
         prepare_capacity();  // room for one step; bounds after it
         upload_env_if_dirty();
-        unsigned int S = Smax;
-        for (auto& l : lists) {
-            const int b = births_per_step(l.get());
-            if (!b) continue;
-            uint64_t cap = l->capacity;
-            if (cuda_config.max_agents) cap = std::min<uint64_t>(cap, cuda_config.max_agents);
-            unsigned int k = 1;
-            while (k < S && grow_bound(l->bound, b * static_cast<int>(k)) <= cap) ++k;
-            S = k;
+        // the block ends before a step whose population bound could pass a
+        // list's capacity; `after` holds the bounds after its last step
+        unsigned int S = 1;
+        std::vector<uint64_t> after(lists.size());
+        for (size_t i = 0; i < lists.size(); ++i) after[i] = lists[i]->bound;
+        while (S < Smax) {
+            std::vector<uint64_t> next = after;
+            advance_bounds(next, 1);
+            bool fits = true;
+            for (size_t i = 0; i < lists.size(); ++i) {
+                uint64_t cap = lists[i]->capacity;
+                if (cuda_config.max_agents) cap = std::min<uint64_t>(cap, cuda_config.max_agents);
+                fits = fits && next[i] <= cap;
+            }
+            if (!fits) break;
+            after.swap(next);
+            ++S;
         }
         const unsigned int first = step_count;
         std::vector<int> key{-static_cast<int>(S)};
@@ -1498,9 +1544,8 @@ struct SimulationImpl {
         ++graph_launches;
         FG_CUDA(cudaEventRecord(e1, stream));
         step_events.push_back({e0, e1, S});
-        for (auto& l : lists)  // bounds after the block's S steps (after its first: prepare_capacity)
-            l->bound = static_cast<uint32_t>(
-                std::min<uint64_t>(grow_bound(l->bound, births_per_step(l.get()) * static_cast<int>(S - 1)), 0xFFFFFFFFu));
+        for (size_t i = 0; i < lists.size(); ++i)  // bounds after the block's S steps
+            lists[i]->bound = static_cast<uint32_t>(std::min<uint64_t>(after[i], 0xFFFFFFFFu));
         step_count += S - 1;
         record_counts();  // the counts after the block, for later bounds
         ++step_count;
@@ -1516,7 +1561,7 @@ struct SimulationImpl {
                     AgentList& l = *f.list;
                     if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0) l.parity ^= 1;
                     if (f.fn->condition) l.parity ^= 1;
-                    if (f.fn->has_agent_death || f.births) l.parity ^= 1;
+                    if (f.fn->has_agent_death || (f.births && f.births_fused)) l.parity ^= 1;
                 }
     }
 

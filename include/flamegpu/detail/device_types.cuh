@@ -160,7 +160,8 @@ struct LaunchParams {
     uint32_t in_pbm_alloc;       // PBM entries readable (multiple of 4, >= binCount + 1)
     uint32_t stage_bytes;        // shared memory for staging neighbour records (0 = off)
     // birth / death
-    uint32_t* birth_flags;       // 1 where agent_out was used (null if disabled)
+    uint32_t* birth_flags;       // 1 where agent_out was used, 2 if its id was also claimed (null if disabled)
+    uint32_t* birth_next_id;     // next id of the output agent (agent_out.getID() claims from it)
     uint32_t* death_flags;       // ALIVE / DEAD per agent (null if death disabled)
     // step data
     const uint32_t* d_step;      // step counter

@@ -950,23 +950,33 @@ class DeviceAPI {
             if (!start(name)) return;
             detail::write_var<T>(P, &P.T.birth, name.hash, index, value, i);
         }
-        /** Ids of new agents are assigned when the step's compaction appends them
-         * (next id + birth rank, deterministic), after this function returns. */
+        /** The new agent's id (DeviceAPI.cuh:546-557 of the reference: an atomic
+         * increment of the output agent's next id). A birth whose id is never
+         * asked for gets it when the step appends the new agents (next id +
+         * birth rank, deterministic); one that asks claims it here, and keeps it. */
         __device__ id_t getID() const {
-            detail::device_error(P, detail::kDevUnsupported, 0, index);
-            return ID_NOT_SET;
+            if (!start_row(0u)) return ID_NOT_SET;
+            if (is_born != 2u) {
+                claimed = atomicAdd(P.birth_next_id, 1u);
+                detail::write_var<id_t>(P, &P.T.birth, detail::VarName("_id").hash, index, claimed);
+                is_born = 2u;
+            }
+            return claimed;
         }
         __device__ uint32_t born() const { return is_born; }
 
      private:
         // First write of a birth: fill the staging row with the defaults.
         __device__ bool start(const detail::VarName& name) const {
-            if (!P.birth_flags) {
-                detail::device_error(P, detail::kDevBirthNotEnabled, name.hash, index);
+            if (name.reserved && P.birth_flags) {
+                detail::device_error(P, detail::kDevReservedName, name.hash, index);
                 return false;
             }
-            if (name.reserved) {
-                detail::device_error(P, detail::kDevReservedName, name.hash, index);
+            return start_row(name.hash);
+        }
+        __device__ bool start_row(uint32_t hash) const {
+            if (!P.birth_flags) {
+                detail::device_error(P, detail::kDevBirthNotEnabled, hash, index);
                 return false;
             }
             if (!is_born) {
@@ -986,7 +996,8 @@ class DeviceAPI {
         }
         const detail::LaunchParams& P;
         uint32_t index;
-        mutable uint32_t is_born = 0;
+        mutable uint32_t is_born = 0;  // 1: born, 2: born and its id claimed
+        mutable id_t claimed = ID_NOT_SET;
     };
 
     __device__ DeviceAPI(const detail::LaunchParams& p, uint32_t idx)

@@ -154,7 +154,9 @@ int fg_spatial_sort_agents(const fg_spatial_grid* msg_grid, uint32_t max_n, cons
  * move births; both write into the same `out` arrays. If id_col >= 0, births'
  * word id_col of cols[] receives *d_next_id + birth rank and *d_next_id is
  * advanced by the number of births (deterministic: the reference draws child
- * ids with atomicInc, DeviceAPI.cuh:546-557). d_alive_total (device) may carry
+ * ids with atomicInc, DeviceAPI.cuh:546-557); a birth row whose born flag is 2
+ * keeps the id its staging row holds (claimed on the device before the call,
+ * from *d_next_id, which is then read after those claims). d_alive_total (device) may carry
  * S if the caller already has it (else it is computed here). The new
  * population S + births is written to *d_n_out (device). out_capacity bounds
  * the output; births beyond it are dropped and the status word records
@@ -164,6 +166,25 @@ int fg_compact_agents(uint32_t max_n, const uint32_t* d_n, const uint32_t* alive
                       int32_t id_col, uint32_t* d_next_id, const uint32_t* d_alive_total,
                       uint32_t* d_n_out, uint32_t out_capacity,
                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* Agent birth into another list (another agent type, or another state of the
+ * same agent). Replaces CUDAAgent::scatterNew / CUDAAgentStateList::scatterNew
+ * (src/flamegpu/simulation/detail/CUDAAgent.cu:427-450,
+ * src/flamegpu/simulation/detail/CUDAAgentStateList.cu:189-250), which append
+ * the new agents after the destination list's agents in parent order:
+ *
+ *   out[D + r] = birth row i (the r-th row i < n with born[i] != 0),
+ *   D = *d_dst_count before the call; *d_dst_count grows by the births.
+ *
+ * cols[c].in are the per-parent staging rows, cols[c].out the destination
+ * columns (distinct arrays). If id_col >= 0, word id_col of each birth receives
+ * *d_next_id + r and *d_next_id advances by the births. Births past
+ * dst_capacity are dropped and the workspace records FG_ERR_CAPACITY.
+ * Workspace: fg_compact_workspace_size(max_n), shared with fg_compact_agents
+ * (calls on one workspace must be ordered). */
+int fg_append_births(uint32_t max_n, const uint32_t* d_n, const uint32_t* born, const fg_column* cols,
+                     uint32_t ncols, int32_t id_col, uint32_t* d_next_id, uint32_t* d_dst_count,
+                     uint32_t dst_capacity, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Stable two-way partition of an agent list. Replaces the agent function
  * condition scatter of CUDAFatAgent::processFunctionCondition

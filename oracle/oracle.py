@@ -338,3 +338,60 @@ def state_mix_run(pops: dict, next_id: int, steps: int, first_step: int = 0):
         out[k] = {"_id": np.array([a[0] for a in lst], np.uint32), "v": np.array([a[1] for a in lst], np.uint32),
                   "x": np.array([a[2] for a in lst], np.float32)}
     return out, next_id
+
+
+def cross_birth_run(pops: dict, next_id: dict, steps: int, first_step: int = 0):
+    """The "cross_birth" model of examples/agent_creation_tests/agent_creation.cu,
+    serially (pure Python: small populations only). pops: {("prey", "default"),
+    ("hunter", "roam"), ("hunter", "rest")} -> {"_id", "v", "x"}; next_id:
+    {agent: next id}. Per function, as state_mix_run, with the births appended
+    to the output agent's list after the death compaction and the transition,
+    with that agent's next ids (CUDASimulation.cu:1062-1080,
+    CUDAAgent.cu:427-450, CUDAAgentStateList.cu:189-250). Returns (pops, next_id)."""
+    f32 = np.float32
+    st = {k: [(int(i), int(v), f32(x)) for i, v, x in zip(p["_id"], p["v"], p["x"])] for k, p in pops.items()}
+    nid = dict(next_id)
+
+    def run(src, dst, out, cond, body):
+        fails = [a for a in st[src] if not cond(a)]
+        passes = [a for a in st[src] if cond(a)]
+        survivors, births = [], []
+        for a in passes:
+            new, child, alive = body(a)
+            if child is not None:
+                births.append(child)
+            if alive:
+                survivors.append(new)
+        if src == dst:
+            st[src] = fails + survivors
+        else:
+            st[src] = fails
+            st[dst] = st[dst] + survivors
+        agent = out[0]
+        st[out] = st[out] + [(nid[agent] + k, v, x) for k, (v, x) in enumerate(births)]
+        nid[agent] += len(births)
+
+    P, R, S = ("prey", "default"), ("hunter", "roam"), ("hunter", "rest")
+    for step in range(first_step, first_step + steps):
+        def spawn(a):
+            i, v, x = a
+            x = f32(x + f32(1.0))
+            child = (v + 1000, f32(x * f32(0.5))) if (i + step) % 3 == 0 else None
+            return (i, v, x), child, i % 11 != 0
+
+        def hunt(a):
+            i, v, x = a
+            x = f32(x + f32(2.0))
+            child = (v + 7, x) if i % 5 == 0 else None
+            return (i, v, x), child, True
+
+        def wake(a):
+            i, v, x = a
+            return (i, v, f32(x - f32(1.0))), None, True
+
+        run(P, P, R, lambda a: True, spawn)
+        run(R, S, P, lambda a: a[0] % 2 == 0, hunt)
+        run(S, R, R, lambda a: True, wake)
+    out = {k: {"_id": np.array([a[0] for a in v], np.uint32), "v": np.array([a[1] for a in v], np.uint32),
+               "x": np.array([a[2] for a in v], np.float32)} for k, v in st.items()}
+    return out, nid
