@@ -34,7 +34,7 @@ EXPORTS = [
     "fg_last_cuda_error", "fg_version", "fg_batch_instance_init", "fg_batched_workspace_size",
     "fg_spatial_build_batched", "fg_spatial_sort_agents_batched", "fg_exclusive_scan_u32_noalloc",
     "fg_partition_agents", "fg_append_rows", "fg_workspace_set_wait_limit", "fg_noalloc_scan_status",
-    "fg_append_births",
+    "fg_append_births", "fg_batch_compact_tiles", "fg_compact_batched_workspace_size", "fg_compact_agents_batched",
 ]
 FG_NOALLOC_SCAN_MAX_N = 1 << 25
 
@@ -111,6 +111,12 @@ def lib():
             L.fg_workspace_set_wait_limit.argtypes = [vp, sz, u32, C.c_int32, vp]
             L.fg_partition_agents.argtypes = [u32, vp, vp, C.POINTER(Column), u32, vp, vp, sz, vp]
             L.fg_append_rows.argtypes = [C.POINTER(Column), u32, u32, vp, vp, vp, u32, vp, sz, vp]
+            L.fg_batch_compact_tiles.argtypes = [C.POINTER(BatchInstance), u32, C.POINTER(u32)]
+            L.fg_batch_compact_tiles.restype = u32
+            L.fg_compact_batched_workspace_size.argtypes = [u32, u32]
+            L.fg_compact_batched_workspace_size.restype = sz
+            L.fg_compact_agents_batched.argtypes = [vp, vp, u32, u32, u32, vp, vp, vp, C.POINTER(Column),
+                                                    C.POINTER(Column), u32, C.c_int32, vp, vp, sz, vp]
             L.fg_append_births.argtypes = [u32, vp, vp, C.POINTER(Column), u32, C.c_int32, vp, vp, u32, vp, sz, vp]
             L.fg_version.restype = C.c_char_p
             L.fg_batch_instance_init.argtypes = [C.POINTER(BatchInstance), C.POINTER(SpatialGrid), u32, u32, u32,

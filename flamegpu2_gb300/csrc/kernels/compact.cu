@@ -437,3 +437,270 @@ extern "C" int fg_append_rows(const fg_column* cols, uint32_t ncols, uint32_t ma
     launch(k_append_counts, 1, 1, st, max_rows, d_begin, d_src_count, d_dst_count, dst_capacity);
     return launch_err();
 }
+
+// ------------------------------------------------------ segmented (batches)
+//
+// The same fused compaction over a batch of instances (fg_batch_instance):
+// instance k owns rows [row_begin_k, row_begin_k + row_capacity_k) of every
+// column and its first counts[k] rows are its agents. Its rows are cut into
+// tiles of kCompTile rows that never cross into another instance (tile_begin
+// maps instances to their first tile), so one launch compacts every instance
+// in place of its own segment: a tile looks back only over the tiles of its
+// instance, survivors of instance k land from row_begin_k, its births after
+// its S_k survivors (counted first, per instance), with ids from next_ids[k].
+// The last block to finish writes every instance's new count.
+namespace fgk {
+
+__device__ __forceinline__ uint32_t batch_instance_of_row(const fg_batch_instance* inst, uint32_t ninst, uint32_t row) {
+    uint32_t lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&inst[mid].row_begin) <= row)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// survivors per instance: rows below the instance's count with alive != 0
+// (alive == NULL: every agent survives)
+__global__ void __launch_bounds__(kThreads) k_count_alive_batched(const fg_batch_instance* __restrict__ inst,
+                                                                  uint32_t ninst, const uint32_t* __restrict__ counts,
+                                                                  uint32_t total_rows, const uint32_t* __restrict__ alive,
+                                                                  uint32_t* alive_total) {
+    flamegpu::detail::grid_dependency_enter();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total_rows; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        bool a = false;
+        uint32_t k = 0;
+        if (i < total_rows) {
+            k = batch_instance_of_row(inst, ninst, i);
+            const uint32_t local = i - __ldg(&inst[k].row_begin);
+            a = local < __ldg(counts + k) && (alive == nullptr || alive[i] != 0);
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, a);
+        if (a) {
+            const uint32_t peers = __match_any_sync(m, k);
+            if (lane_id() == static_cast<uint32_t>(__ffs(peers) - 1)) atomicAdd(alive_total + k, __popc(peers));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_compact_batched(
+    const __grid_constant__ CompactParams cp, const fg_batch_instance* __restrict__ inst,
+    const uint32_t* __restrict__ tile_begin, uint32_t ninst, uint32_t ntiles, uint32_t* counts,
+    const uint32_t* __restrict__ alive, const uint32_t* __restrict__ born, uint32_t* next_ids, uint32_t* alive_total,
+    uint32_t* birth_total, uint64_t* status0, uint32_t stride_tiles, WsHeader* h) {
+    flamegpu::detail::grid_dependency_enter();
+    __shared__ uint32_t s_tile, s_inst, s_last;
+    __shared__ uint32_t s_cnt_a[kCompItems][kThreads / 32];
+    __shared__ uint32_t s_cnt_b[kCompItems][kThreads / 32];
+    __shared__ uint32_t s_tot[2];
+    __shared__ uint64_t s_excl;
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
+    const uint32_t limit = spin_limit_of(h);
+    const bool withhold = h->withhold != 0;
+    uint64_t* status = status0 + static_cast<size_t>(parity) * stride_tiles;
+    uint64_t* other = status0 + static_cast<size_t>(parity ^ 1u) * stride_tiles;
+    for (uint32_t t = blockIdx.x * blockDim.x + tid; t < stride_tiles; t += gridDim.x * blockDim.x) other[t] = 0;
+    for (;;) {
+        if (tid == 0) {
+            const uint32_t t = atomicAdd(&h->comp_ticket, 1u);
+            s_tile = t;
+            if (t < ntiles) {  // the instance whose tiles hold t
+                uint32_t lo = 0, hi = ninst - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (__ldg(tile_begin + mid) <= t)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                s_inst = lo;
+            }
+        }
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;  // the same in every thread
+        const uint32_t k = s_inst;
+        const uint32_t t0 = __ldg(tile_begin + k);
+        const uint32_t local = tile - t0;
+        const uint32_t rb = __ldg(&inst[k].row_begin), cap = __ldg(&inst[k].row_capacity);
+        const uint32_t n = min(counts[k], cap);
+        const uint32_t lbase = local * kCompTile;
+        if (lbase >= n) {  // no agents in this tile (nor in the instance's later ones)
+            __syncthreads();
+            continue;
+        }
+        const uint32_t S = alive_total[k];
+        const uint32_t nid = next_ids ? next_ids[k] : 0u;
+        uint32_t ba[kCompItems], bb[kCompItems];
+#pragma unroll
+        for (int q = 0; q < kCompItems; ++q) {
+            const uint32_t li = lbase + q * kThreads + tid;
+            const bool in = li < n;
+            const bool a = in && (alive == nullptr || alive[rb + li] != 0);
+            const bool b = in && born != nullptr && born[rb + li] != 0;
+            ba[q] = __ballot_sync(0xFFFFFFFFu, a);
+            bb[q] = __ballot_sync(0xFFFFFFFFu, b);
+            if (lane == 0) {
+                s_cnt_a[q][warp] = __popc(ba[q]);
+                s_cnt_b[q][warp] = __popc(bb[q]);
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t ra = 0, rbb = 0;
+            for (int q = 0; q < kCompItems; ++q)
+                for (int w = 0; w < kThreads / 32; ++w) {
+                    const uint32_t a = s_cnt_a[q][w], b = s_cnt_b[q][w];
+                    s_cnt_a[q][w] = ra;
+                    s_cnt_b[q][w] = rbb;
+                    ra += a;
+                    rbb += b;
+                }
+            s_tot[0] = ra;
+            s_tot[1] = rbb;
+        }
+        __syncthreads();
+        if (tid < 32) {
+            const uint64_t agg = (static_cast<uint64_t>(s_tot[0]) << 31) | s_tot[1];
+            uint64_t excl = 0;
+            uint64_t* st = status + t0;
+            if (local == 0) {
+                if (tid == 0 && !(withhold && tile == 0)) st_release_u64(st, pair_pack(2, s_tot[0], s_tot[1]));
+            } else {
+                if (tid == 0) st_release_u64(st + local, (1ull << 62) | agg);
+                excl = lookback_pair(st, local, h, limit);
+                if (tid == 0) st_release_u64(st + local, (2ull << 62) | ((excl + agg) & kPairMask));
+            }
+            if (tid == 0) {
+                s_excl = excl;
+                if (lbase + kCompTile >= n)  // the instance's last tile with agents: its births
+                    birth_total[k] = static_cast<uint32_t>((excl + agg) & 0x7FFFFFFFu);
+            }
+        }
+        __syncthreads();
+        const uint32_t ea = static_cast<uint32_t>((s_excl >> 31) & 0x7FFFFFFFu);
+        const uint32_t eb = static_cast<uint32_t>(s_excl & 0x7FFFFFFFu);
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (int q = 0; q < kCompItems; ++q) {
+            const uint32_t i = rb + lbase + q * kThreads + tid;
+            if ((ba[q] >> lane) & 1u) copy_row(cp.col, cp.ncols, i, rb + ea + s_cnt_a[q][warp] + __popc(ba[q] & lt), -1, 0u);
+            if ((bb[q] >> lane) & 1u) {
+                const uint32_t r = eb + s_cnt_b[q][warp] + __popc(bb[q] & lt);
+                const bool claimed = born[i] == 2u;  // id claimed during the function: kept
+                if (S + r < cap)
+                    copy_row(cp.bcol, cp.ncols, i, rb + S + r, claimed ? -1 : cp.id_col, nid + r);
+                else
+                    record_status(h, FG_ERR_CAPACITY);
+            }
+        }
+        __syncthreads();  // shared state is reused by the next tile
+    }
+    // the last block to finish writes the counts and resets the tickets
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        s_last = atomicAdd(&h->comp_done, 1u) == gridDim.x - 1 ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (uint32_t k = tid; k < ninst; k += blockDim.x) {
+        const uint32_t births = *reinterpret_cast<volatile uint32_t*>(birth_total + k);
+        const uint32_t S = *reinterpret_cast<volatile uint32_t*>(alive_total + k);
+        const uint32_t cap = __ldg(&inst[k].row_capacity);
+        const uint32_t total = S + births;
+        counts[k] = total < cap ? total : cap;
+        if (next_ids && cp.id_col >= 0) next_ids[k] += births;
+        birth_total[k] = 0;
+        alive_total[k] = 0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        h->comp_ticket = 0;
+        h->comp_done = 0;
+        atomicExch(&h->comp_parity, parity ^ 1u);
+        __threadfence();
+    }
+}
+
+__global__ void k_set_alive_total_batched(const uint32_t* counts, uint32_t ninst, uint32_t* alive_total) {
+    flamegpu::detail::grid_dependency_enter();
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ninst; k += gridDim.x * blockDim.x)
+        alive_total[k] = counts[k];
+}
+
+struct BatchCompactLayout {
+    size_t alive, births, status, total;
+};
+inline BatchCompactLayout batch_compact_layout(uint32_t ntiles, uint32_t ninst) {
+    BatchCompactLayout L;
+    L.alive = sizeof(WsHeader);
+    L.births = L.alive + align_up(sizeof(uint32_t) * ninst, 256);
+    L.status = L.births + align_up(sizeof(uint32_t) * ninst, 256);
+    L.total = L.status + align_up(sizeof(uint64_t) * 2 * std::max(ntiles, 1u), 256);
+    return L;
+}
+
+}  // namespace fgk
+
+extern "C" uint32_t fg_batch_compact_tiles(const fg_batch_instance* instances, uint32_t ninst, uint32_t* tile_begin) {
+    uint32_t t = 0;
+    for (uint32_t k = 0; k < ninst; ++k) {
+        if (tile_begin) tile_begin[k] = t;
+        t += std::max(1u, (instances[k].row_capacity + kCompTile - 1) / kCompTile);
+    }
+    if (tile_begin) tile_begin[ninst] = t;
+    return t;
+}
+
+extern "C" size_t fg_compact_batched_workspace_size(uint32_t ntiles, uint32_t ninst) {
+    return batch_compact_layout(ntiles, ninst).total;
+}
+
+extern "C" int fg_compact_agents_batched(const fg_batch_instance* instances, const uint32_t* tile_begin, uint32_t ninst,
+                                         uint32_t ntiles, uint32_t total_rows, uint32_t* counts, const uint32_t* alive,
+                                         const uint32_t* born, const fg_column* cols, const fg_column* birth_cols,
+                                         uint32_t ncols, int32_t id_col, uint32_t* next_ids, void* workspace,
+                                         size_t workspace_bytes, void* stream) {
+    if (!instances || !tile_begin || !ninst || !counts || !workspace || ncols > FG_MAX_COLUMNS || (ncols && !cols))
+        return FG_ERR_INVALID_ARGUMENT;
+    if (born && ncols && !birth_cols) return FG_ERR_INVALID_ARGUMENT;
+    if (id_col >= static_cast<int32_t>(ncols)) return FG_ERR_INVALID_ARGUMENT;
+    if (id_col >= 0 && (cols[id_col].elem_bytes != 4 || !next_ids)) return FG_ERR_INVALID_ARGUMENT;
+    if (total_rows >= (1u << 31)) return FG_ERR_UNSUPPORTED;
+    const BatchCompactLayout L = batch_compact_layout(ntiles, ninst);
+    if (workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255)) return FG_ERR_WORKSPACE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(workspace);
+    WsHeader* h = reinterpret_cast<WsHeader*>(ws);
+    uint32_t* alive_total = reinterpret_cast<uint32_t*>(ws + L.alive);
+    uint32_t* birth_total = reinterpret_cast<uint32_t*>(ws + L.births);
+    uint64_t* status = reinterpret_cast<uint64_t*>(ws + L.status);
+    // alive_total / birth_total are zero here: the workspace starts zeroed and
+    // every call's last block clears them
+    if (alive)
+        launch(k_count_alive_batched, count_grid(total_rows), kThreads, st, instances, ninst,
+               static_cast<const uint32_t*>(counts), total_rows, alive, alive_total);
+    else
+        launch(k_set_alive_total_batched, std::max(1u, (ninst + kThreads - 1) / kThreads), kThreads, st,
+               static_cast<const uint32_t*>(counts), ninst, alive_total);
+    CompactParams cp{};
+    for (uint32_t c = 0; c < ncols; ++c) {
+        cp.col[c] = cols[c];
+        cp.bcol[c] = birth_cols ? birth_cols[c] : cols[c];
+    }
+    cp.ncols = ncols;
+    cp.id_col = id_col;
+    const uint32_t stride_tiles =
+        static_cast<uint32_t>((workspace_bytes - L.status) / (2 * sizeof(uint64_t)));
+    launch(k_compact_batched, std::min(ntiles, 4u * device_sms()), kThreads, st, cp, instances, tile_begin, ninst,
+           ntiles, counts, alive, born, next_ids, alive_total, birth_total, status, stride_tiles, h);
+    return launch_err();
+}

@@ -113,6 +113,19 @@ struct Alloc {
         ptrs.push_back(p);
         return p;
     }
+    // frees p (null: nothing); the device must be done with it
+    void release(void* p) {
+        if (!p) return;
+        auto it = std::find(ptrs.begin(), ptrs.end(), p);
+        if (it != ptrs.end()) {
+            cudaFree(p);
+            ptrs.erase(it);
+        }
+    }
+    void* release_and_get(void* p, size_t bytes) {
+        release(p);
+        return get(bytes);
+    }
     ~Alloc() {
         for (void* p : ptrs) cudaFree(p);
     }
@@ -134,7 +147,8 @@ std::string batch_unsupported(const ModelData& m) {
             if (f != g && !f->message_output.empty() && f->message_output == g->message_output)
                 return "a message list output by more than one function";
     for (const auto& f : a.functions) {
-        if (f->has_agent_death || !f->agent_output.empty()) return "agent birth/death";
+        if (!f->agent_output.empty() && (f->agent_output != a.name || f->agent_output_state != a.states[0]))
+            return "agent birth into another agent type or state";
         if (f->condition) return "an agent function condition";
         if (f->message_output_optional) return "optional message output";
         if (!f->message_input.empty() && m.message(f->message_input)->kind == MessageKind::BruteForce)
@@ -158,10 +172,32 @@ struct BatchedSim {
     std::vector<std::array<void*, 2>> cols;  // per agent variable
     int parity = 0;
     uint32_t* d_counts = nullptr;
+    uint32_t* d_next_ids = nullptr;  // next agent id per instance
     uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record
     std::vector<size_t> env_offset;
     size_t env_stride = 0;
     char* d_env = nullptr;
+    int id_col = -1;
+    // birth / death: births per step at most double an instance per birth
+    // function; bound[k] bounds instance k's population (host)
+    int birth_fns = 0;
+    bool death_or_birth = false;
+    std::vector<uint64_t> bound;
+    uint32_t* d_tile_begin = nullptr;  // compaction tiles per instance (ninst + 1)
+    uint32_t comp_tiles = 0;
+    void* comp_ws = nullptr;
+    size_t comp_ws_bytes = 0;
+    // population reports copied after steps, for bounds without a wait
+    struct Report {
+        cudaEvent_t ev = nullptr;
+        uint32_t* host = nullptr;
+        unsigned int step_after = 0;  // the report holds the counts entering this step
+        bool used = false;
+    };
+    std::vector<Report> reports;
+    size_t report_next = 0;
+    uint32_t* reports_pinned = nullptr;
+    unsigned int relayouts = 0;
 
     struct BMsg {
         MessageData* msg = nullptr;
@@ -186,28 +222,40 @@ struct BatchedSim {
         BMsg* in = nullptr;
         BMsg* out = nullptr;
         bool sort = false;
+        bool births = false;
         std::vector<fg_batch_instance> sort_inst;
         fg_batch_instance* d_sort_inst = nullptr;
         uint32_t sort_buckets = 0;
         void* sort_ws = nullptr;
         size_t sort_ws_bytes = 0;
         BatchInstanceRT* d_rt = nullptr;
+        uint32_t* death_flags = nullptr;
+        uint32_t* birth_flags = nullptr;
+        std::vector<void*> birth_cols;
+        void* birth_defaults = nullptr;
         std::unique_ptr<FunctionTables> tables[2];
     };
     std::vector<BFn> fns;
-    cudaGraphExec_t graphs[2] = {nullptr, nullptr};
     unsigned int kernels_per_step = 0;
     unsigned long long graph_launches = 0;
+    std::map<std::pair<int, bool>, cudaGraphExec_t> cache;
 
     BatchedSim(std::shared_ptr<ModelData> m, const RunPlanVector& p, const CUDAEnsemble::EnsembleConfig& c)
         : model(std::move(m)), plans(p), cfg(c) {}
     ~BatchedSim() {
-        for (auto& g : graphs)
-            if (g) cudaGraphExecDestroy(g);
+        drop_graphs();
+        for (auto& r : reports)
+            if (r.ev) cudaEventDestroy(r.ev);
+        if (reports_pinned) cudaFreeHost(reports_pinned);
         if (fork_ev) cudaEventDestroy(fork_ev);
         if (join_ev) cudaEventDestroy(join_ev);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
+    }
+
+    void drop_graphs() {
+        for (auto& c : cache) cudaGraphExecDestroy(c.second);
+        cache.clear();
     }
 
     BMsg* msg_of(const std::string& name) {
@@ -235,6 +283,15 @@ struct BatchedSim {
         return g;
     }
 
+    // Rows of an instance of n agents: its agents plus room for the births of
+    // two steps, rounded up to the agent block.
+    uint32_t rows_for(uint64_t n) const {
+        const uint64_t grow = birth_fns ? (1ull << std::min(2 * birth_fns, 8)) : 1ull;
+        const uint64_t r = std::max<uint64_t>(1, n) * grow;
+        if (r >= (1ull << 31)) THROW exception::OutOfMemory("An ensemble run may exceed 2^31 agents");
+        return round_rows(static_cast<uint32_t>(r));
+    }
+
     void setup() {
         FG_ECUDA(cudaSetDevice(cfg.device));
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device);
@@ -246,23 +303,27 @@ struct BatchedSim {
         agent = model->agents[0].get();
         const std::string state = agent->states[0];
         ninst = static_cast<uint32_t>(plans.size());
+        for (size_t v = 0; v < agent->variables.size(); ++v)
+            if (agent->variables[v].name == "_id") id_col = static_cast<int>(v);
+        for (const auto& f : agent->functions) {
+            if (!f->agent_output.empty()) ++birth_fns;
+            death_or_birth = death_or_birth || f->has_agent_death || !f->agent_output.empty();
+        }
         // ---- row segments
-        uint32_t row = 0;
         for (uint32_t k = 0; k < ninst; ++k) {
             auto it = plans[k].populations().find({agent->name, state});
             const uint32_t n = it == plans[k].populations().end() ? 0u : it->second->size();
-            row_begin.push_back(row);
             count.push_back(n);
-            cap.push_back(round_rows(n));
-            if (static_cast<uint64_t>(row) + cap.back() >= (1ull << 31)) THROW exception::OutOfMemory("Ensemble exceeds 2^31 agent rows");
-            row += cap.back();
+            bound.push_back(n);
+            cap.push_back(rows_for(n));
         }
-        total_rows = row;
+        place_rows();
         cols.resize(agent->variables.size());
         for (size_t v = 0; v < cols.size(); ++v) {
             const size_t b = agent->variables[v].bytes();
             cols[v] = {mem.get(b * total_rows), mem.get(b * total_rows)};
         }
+        std::vector<id_t> next(ninst, 1);
         for (uint32_t k = 0; k < ninst; ++k) {
             auto it = plans[k].populations().find({agent->name, state});
             if (it == plans[k].populations().end() || count[k] == 0) continue;
@@ -272,12 +333,11 @@ struct BatchedSim {
             const size_t idc = pop.columnIndex("_id");
             const id_t* ids = reinterpret_cast<const id_t*>(pop.columns()[idc].data());
             std::vector<id_t> filled;
-            id_t next = 1;
-            for (uint32_t i = 0; i < count[k]; ++i) next = std::max<id_t>(next, ids[i] + 1);
+            for (uint32_t i = 0; i < count[k]; ++i) next[k] = std::max<id_t>(next[k], ids[i] + 1);
             for (uint32_t i = 0; i < count[k]; ++i) {
                 if (ids[i] != ID_NOT_SET) continue;
                 if (filled.empty()) filled.assign(ids, ids + count[k]);
-                filled[i] = next++;
+                filled[i] = next[k]++;
             }
             for (size_t v = 0; v < cols.size(); ++v) {
                 const size_t b = agent->variables[v].bytes();
@@ -289,6 +349,8 @@ struct BatchedSim {
         }
         d_counts = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * ninst));
         FG_ECUDA(cudaMemcpy(d_counts, count.data(), sizeof(uint32_t) * ninst, cudaMemcpyHostToDevice));
+        d_next_ids = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * ninst));
+        FG_ECUDA(cudaMemcpy(d_next_ids, next.data(), sizeof(uint32_t) * ninst, cudaMemcpyHostToDevice));
         d_misc = static_cast<uint32_t*>(mem.get(64));
         // ---- environments: the model's values with each plan's overrides
         size_t off = 0;
@@ -307,7 +369,7 @@ struct BatchedSim {
             }
         d_env = static_cast<char*>(mem.get(envs.size()));
         FG_ECUDA(cudaMemcpy(d_env, envs.data(), envs.size(), cudaMemcpyHostToDevice));
-        // ---- message lists
+        // ---- message lists (row-independent part)
         for (const auto& m : model->messages) {
             auto bm = std::make_unique<BMsg>();
             bm->msg = m.get();
@@ -317,7 +379,6 @@ struct BatchedSim {
                 const uint32_t sb = (v.bytes() + 3u) & ~3u;
                 bm->slot_bytes.push_back(sb);
                 vars.emplace_back(fnv1a32(v.name), sb);
-                bm->cols.push_back(mem.get(static_cast<size_t>(sb) * total_rows));
             }
             if (bm->dims) {
                 const SpatialRecordLayout L = spatial_record_layout(vars, bm->dims, m->name.c_str());
@@ -326,31 +387,16 @@ struct BatchedSim {
                 bm->pay_mult = L.pay_mult;
                 bm->pay_shift = L.pay_shift;
                 bm->pay_stride = L.pay_stride;
-                bm->records = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * bm->record_words * static_cast<size_t>(total_rows)));
-                uint32_t bucket = 0;
-                for (uint32_t k = 0; k < ninst; ++k) {
-                    fg_batch_instance bi{};
-                    const fg_spatial_grid g = grid_of(m.get(), k);
-                    uint32_t nb = 0;
-                    FG_ECAPI(fg_batch_instance_init(&bi, &g, row_begin[k], cap[k], bucket, 0, &nb));
-                    bm->inst.push_back(bi);
-                    bucket += (nb + 3u) & ~3u;  // 16-byte aligned PBM slices (staging copies)
-                }
-                bm->total_buckets = bucket;
-                bm->d_inst = static_cast<fg_batch_instance*>(mem.get(sizeof(fg_batch_instance) * ninst));
-                FG_ECUDA(cudaMemcpy(bm->d_inst, bm->inst.data(), sizeof(fg_batch_instance) * ninst, cudaMemcpyHostToDevice));
-                bm->pbm = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * (static_cast<size_t>(bucket) + 8)));
-                bm->ws_bytes = fg_batched_workspace_size(total_rows, bucket);
-                bm->ws = mem.get(bm->ws_bytes);
             }
             msgs.push_back(std::move(bm));
         }
-        // ---- agent functions
+        // ---- agent functions (row-independent part)
         for (const auto& f : agent->functions) {
             BFn b;
             b.fn = f.get();
             b.in = f->message_input.empty() ? nullptr : msg_of(f->message_input);
             b.out = f->message_output.empty() ? nullptr : msg_of(f->message_output);
+            b.births = !f->agent_output.empty();
             if (b.in && b.in->dims) {
                 bool ok = true;
                 const char* ax[3] = {"x", "y", "z"};
@@ -360,7 +406,75 @@ struct BatchedSim {
                 }
                 b.sort = ok;
             }
+            if (b.births) {
+                std::vector<char> defaults;
+                for (const auto& var : agent->variables) {
+                    defaults.insert(defaults.end(), var.default_value.begin(), var.default_value.end());
+                    defaults.resize((defaults.size() + 7) & ~size_t(7));
+                }
+                b.birth_defaults = mem.get(defaults.size());
+                FG_ECUDA(cudaMemcpy(b.birth_defaults, defaults.data(), defaults.size(), cudaMemcpyHostToDevice));
+            }
+            fns.push_back(std::move(b));
+        }
+        layout_rows();
+        if (death_or_birth) {
+            FG_ECUDA(cudaMallocHost(&reports_pinned, sizeof(uint32_t) * ninst * 4));
+            reports.resize(4);
+            for (size_t r = 0; r < reports.size(); ++r) {
+                FG_ECUDA(cudaEventCreateWithFlags(&reports[r].ev, cudaEventDisableTiming));
+                reports[r].host = reports_pinned + r * ninst;
+            }
+        }
+    }
+
+    // row_begin from cap; total_rows
+    void place_rows() {
+        row_begin.assign(ninst, 0);
+        uint64_t row = 0;
+        for (uint32_t k = 0; k < ninst; ++k) {
+            row_begin[k] = static_cast<uint32_t>(row);
+            row += cap[k];
+            if (row >= (1ull << 31)) THROW exception::OutOfMemory("Ensemble exceeds 2^31 agent rows");
+        }
+        total_rows = static_cast<uint32_t>(row);
+    }
+
+    // Every buffer and table that depends on the row segments (columns excepted):
+    // message columns and records, the instance tables of the builds, sorts and
+    // agent launches, flags and birth staging, workspaces, function tables.
+    void layout_rows() {
+        for (auto& mp : msgs) {
+            BMsg& bm = *mp;
+            for (void* p : bm.cols) mem.release(p);
+            bm.cols.clear();
+            for (uint32_t sb : bm.slot_bytes) bm.cols.push_back(mem.get(static_cast<size_t>(sb) * total_rows));
+            if (!bm.dims) continue;
+            mem.release(bm.records);
+            bm.records = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * bm.record_words * static_cast<size_t>(total_rows)));
+            bm.inst.clear();
+            uint32_t bucket = 0;
+            for (uint32_t k = 0; k < ninst; ++k) {
+                fg_batch_instance bi{};
+                const fg_spatial_grid g = grid_of(bm.msg, k);
+                uint32_t nb = 0;
+                FG_ECAPI(fg_batch_instance_init(&bi, &g, row_begin[k], cap[k], bucket, 0, &nb));
+                bm.inst.push_back(bi);
+                bucket += (nb + 3u) & ~3u;  // 16-byte aligned PBM slices (staging copies)
+            }
+            if (!bm.pbm) {
+                bm.total_buckets = bucket;
+                bm.pbm = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * (static_cast<size_t>(bucket) + 8)));
+            }
+            if (!bm.d_inst) bm.d_inst = static_cast<fg_batch_instance*>(mem.get(sizeof(fg_batch_instance) * ninst));
+            FG_ECUDA(cudaMemcpy(bm.d_inst, bm.inst.data(), sizeof(fg_batch_instance) * ninst, cudaMemcpyHostToDevice));
+            mem.release(bm.ws);
+            bm.ws_bytes = fg_batched_workspace_size(total_rows, bm.total_buckets);
+            bm.ws = mem.get(bm.ws_bytes);
+        }
+        for (auto& b : fns) {
             if (b.sort) {
+                b.sort_inst.clear();
                 uint32_t bucket = 0;
                 for (uint32_t k = 0; k < ninst; ++k) {
                     fg_batch_instance bi{};
@@ -371,8 +485,9 @@ struct BatchedSim {
                     bucket += nb;
                 }
                 b.sort_buckets = bucket;
-                b.d_sort_inst = static_cast<fg_batch_instance*>(mem.get(sizeof(fg_batch_instance) * ninst));
+                if (!b.d_sort_inst) b.d_sort_inst = static_cast<fg_batch_instance*>(mem.get(sizeof(fg_batch_instance) * ninst));
                 FG_ECUDA(cudaMemcpy(b.d_sort_inst, b.sort_inst.data(), sizeof(fg_batch_instance) * ninst, cudaMemcpyHostToDevice));
+                mem.release(b.sort_ws);
                 b.sort_ws_bytes = fg_batched_workspace_size(total_rows, bucket);
                 b.sort_ws = mem.get(b.sort_ws_bytes);
             }
@@ -388,44 +503,167 @@ struct BatchedSim {
                     rt[k].in_bucket_begin = b.in->inst[k].bucket_begin;
                 }
             }
-            b.d_rt = static_cast<BatchInstanceRT*>(mem.get(sizeof(BatchInstanceRT) * ninst));
+            if (!b.d_rt) b.d_rt = static_cast<BatchInstanceRT*>(mem.get(sizeof(BatchInstanceRT) * ninst));
             FG_ECUDA(cudaMemcpy(b.d_rt, rt.data(), sizeof(BatchInstanceRT) * ninst, cudaMemcpyHostToDevice));
-            for (int par = 0; par < 2; ++par) {
-                auto T = std::make_unique<FunctionTables>();
-                std::memset(T.get(), 0, sizeof(FunctionTables));
-                std::vector<TableEntry> e;
+            if (b.fn->has_agent_death) {
+                mem.release(b.death_flags);
+                b.death_flags = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * total_rows));
+            }
+            if (b.births) {
+                mem.release(b.birth_flags);
+                b.birth_flags = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * total_rows));
+                for (void* p : b.birth_cols) mem.release(p);
+                b.birth_cols.clear();
+                for (const auto& v : agent->variables) b.birth_cols.push_back(mem.get(static_cast<size_t>(v.bytes()) * total_rows));
+            }
+            build_tables(b);
+        }
+        if (death_or_birth) {
+            std::vector<fg_batch_instance> ci(ninst);
+            for (uint32_t k = 0; k < ninst; ++k) {
+                ci[k] = fg_batch_instance{};
+                ci[k].row_begin = row_begin[k];
+                ci[k].row_capacity = cap[k];
+            }
+            std::vector<uint32_t> tb(ninst + 1);
+            comp_tiles = fg_batch_compact_tiles(ci.data(), ninst, tb.data());
+            mem.release(d_tile_begin);
+            d_tile_begin = static_cast<uint32_t*>(mem.get(sizeof(uint32_t) * (ninst + 1)));
+            FG_ECUDA(cudaMemcpy(d_tile_begin, tb.data(), sizeof(uint32_t) * (ninst + 1), cudaMemcpyHostToDevice));
+            comp_inst = static_cast<fg_batch_instance*>(mem.release_and_get(comp_inst, sizeof(fg_batch_instance) * ninst));
+            FG_ECUDA(cudaMemcpy(comp_inst, ci.data(), sizeof(fg_batch_instance) * ninst, cudaMemcpyHostToDevice));
+            mem.release(comp_ws);
+            comp_ws_bytes = fg_compact_batched_workspace_size(comp_tiles, ninst);
+            comp_ws = mem.get(comp_ws_bytes);
+        }
+        drop_graphs();
+    }
+    fg_batch_instance* comp_inst = nullptr;  // row segments, for the segmented compaction
+
+    void build_tables(BFn& b) {
+        for (int par = 0; par < 2; ++par) {
+            auto T = std::make_unique<FunctionTables>();
+            std::memset(T.get(), 0, sizeof(FunctionTables));
+            std::vector<TableEntry> e;
+            for (size_t v = 0; v < agent->variables.size(); ++v) {
+                const Variable& var = agent->variables[v];
+                e.push_back({fnv1a32(var.name), static_cast<char*>(cols[v][par]), var.bytes(), var.type_size, var.elements});
+            }
+            T->agent = make_table(e, "agent");
+            if (b.out) {
+                e.clear();
+                for (size_t v = 0; v < b.out->msg->variables.size(); ++v) {
+                    const Variable& var = b.out->msg->variables[v];
+                    e.push_back({fnv1a32(var.name), static_cast<char*>(b.out->cols[v]), b.out->slot_bytes[v], var.type_size, var.elements});
+                }
+                T->msg_out = make_table(e, "message");
+            }
+            if (b.in) {
+                e.clear();
+                for (size_t v = 0; v < b.in->msg->variables.size(); ++v) {
+                    const Variable& var = b.in->msg->variables[v];
+                    e.push_back({fnv1a32(var.name), reinterpret_cast<char*>(b.in->records + b.in->field_word[v]),
+                                 b.in->record_words * 4, var.type_size, var.elements});
+                }
+                T->msg_in = make_table(e, "message");
+            }
+            if (b.births) {
+                e.clear();
+                std::vector<TableEntry> d;
+                size_t doff = 0;
                 for (size_t v = 0; v < agent->variables.size(); ++v) {
                     const Variable& var = agent->variables[v];
-                    e.push_back({fnv1a32(var.name), static_cast<char*>(cols[v][par]), var.bytes(), var.type_size, var.elements});
+                    e.push_back({fnv1a32(var.name), static_cast<char*>(b.birth_cols[v]), var.bytes(), var.type_size, var.elements});
+                    d.push_back({fnv1a32(var.name), static_cast<char*>(b.birth_defaults) + doff, var.bytes(), var.type_size,
+                                 var.elements});
+                    doff = (doff + var.default_value.size() + 7) & ~size_t(7);
                 }
-                T->agent = make_table(e, "agent");
-                if (b.out) {
-                    e.clear();
-                    for (size_t v = 0; v < b.out->msg->variables.size(); ++v) {
-                        const Variable& var = b.out->msg->variables[v];
-                        e.push_back({fnv1a32(var.name), static_cast<char*>(b.out->cols[v]), b.out->slot_bytes[v], var.type_size, var.elements});
-                    }
-                    T->msg_out = make_table(e, "message");
-                }
-                if (b.in) {
-                    e.clear();
-                    for (size_t v = 0; v < b.in->msg->variables.size(); ++v) {
-                        const Variable& var = b.in->msg->variables[v];
-                        e.push_back({fnv1a32(var.name), reinterpret_cast<char*>(b.in->records + b.in->field_word[v]),
-                                     b.in->record_words * 4, var.type_size, var.elements});
-                    }
-                    T->msg_in = make_table(e, "message");
-                }
-                e.clear();
-                for (size_t i = 0; i < model->environment.size(); ++i) {
-                    const EnvProperty& p = model->environment[i];
-                    e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(env_offset[i]), 0, p.type_size, p.elements});
-                }
-                T->env = make_table(e, "environment");
-                b.tables[par] = std::move(T);
+                T->birth = make_table(e, "agent");
+                T->birth_def = make_table(d, "agent");
             }
-            fns.push_back(std::move(b));
+            e.clear();
+            for (size_t i = 0; i < model->environment.size(); ++i) {
+                const EnvProperty& p = model->environment[i];
+                e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(env_offset[i]), 0, p.type_size, p.elements});
+            }
+            T->env = make_table(e, "environment");
+            b.tables[par] = std::move(T);
         }
+    }
+
+    // Grow the row segments to new_cap (device idle; count holds the exact counts).
+    void relayout(const std::vector<uint32_t>& new_cap) {
+        const std::vector<uint32_t> old_begin = row_begin;
+        cap = new_cap;
+        place_rows();
+        for (size_t v = 0; v < cols.size(); ++v) {
+            const size_t b = agent->variables[v].bytes();
+            void* n0 = mem.get(b * total_rows);
+            void* n1 = mem.get(b * total_rows);
+            for (uint32_t k = 0; k < ninst; ++k)
+                if (count[k])
+                    FG_ECUDA(cudaMemcpyAsync(static_cast<char*>(n0) + b * row_begin[k],
+                                             static_cast<const char*>(cols[v][parity]) + b * old_begin[k], b * count[k],
+                                             cudaMemcpyDeviceToDevice, stream));
+            FG_ECUDA(cudaStreamSynchronize(stream));
+            mem.release(cols[v][0]);
+            mem.release(cols[v][1]);
+            cols[v] = {n0, n1};
+        }
+        parity = 0;
+        layout_rows();
+        ++relayouts;
+    }
+
+    // Before a step: every instance's population bound after it (its bound
+    // entering the step, doubled per birth function) must fit its segment.
+    // Bounds entering the step come from the newest population report that has
+    // arrived (doubled per birth function and step since); if that is not
+    // enough, wait for the exact counts, and grow the segments that still need it.
+    void prepare_capacity(unsigned int step) {
+        if (!birth_fns) return;
+        const Report* known = nullptr;
+        for (const auto& r : reports)
+            if (r.used && r.step_after <= step && (!known || r.step_after > known->step_after) &&
+                cudaEventQuery(r.ev) == cudaSuccess)
+                known = &r;
+        bool over = false;
+        for (uint32_t k = 0; k < ninst; ++k) {
+            uint64_t b = bound[k];
+            if (known) {
+                const int doublings = birth_fns * static_cast<int>(step - known->step_after);
+                b = std::min<uint64_t>(b, static_cast<uint64_t>(known->host[k]) << std::min(doublings, 31));
+            }
+            bound[k] = b;
+            over = over || (b << birth_fns) > cap[k];
+        }
+        if (!over) return;
+        FG_ECUDA(cudaStreamSynchronize(stream));
+        FG_ECUDA(cudaMemcpy(count.data(), d_counts, sizeof(uint32_t) * ninst, cudaMemcpyDeviceToHost));
+        std::vector<uint32_t> want = cap;
+        bool grow = false;
+        for (uint32_t k = 0; k < ninst; ++k) {
+            bound[k] = count[k];
+            if ((bound[k] << birth_fns) > cap[k]) {
+                want[k] = rows_for(count[k]);
+                grow = true;
+            }
+        }
+        if (grow) relayout(want);
+    }
+
+    // After a step: bounds advance by the births it may have had; the counts
+    // are copied out for later bounds.
+    void after_step(unsigned int step) {
+        if (!death_or_birth) return;
+        for (uint32_t k = 0; k < ninst; ++k) bound[k] = std::min<uint64_t>(bound[k], cap[k]);
+        Report& r = reports[report_next];
+        report_next = (report_next + 1) % reports.size();
+        if (r.used) FG_ECUDA(cudaEventSynchronize(r.ev));
+        FG_ECUDA(cudaMemcpyAsync(r.host, d_counts, sizeof(uint32_t) * ninst, cudaMemcpyDeviceToHost, stream));
+        FG_ECUDA(cudaEventRecord(r.ev, stream));
+        r.step_after = step + 1;
+        r.used = true;
     }
 
     void enqueue_sort(BFn& b) {
@@ -498,6 +736,9 @@ struct BatchedSim {
                 smem = P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader));
             }
         }
+        P.death_flags = b.fn->has_agent_death ? b.death_flags : nullptr;
+        P.birth_flags = b.births ? b.birth_flags : nullptr;
+        P.birth_next_id = b.births ? d_next_ids : nullptr;
         P.d_step = d_misc;
         P.fn_uid = b.fn->uid;
         P.error = d_misc + 1;
@@ -509,6 +750,24 @@ struct BatchedSim {
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", b.fn->name.c_str(), cudaGetErrorString(e)));
         kernels_per_step += 1;
+        if (b.fn->has_agent_death || b.births) {
+            // CUDAFatAgent::processDeath + CUDAAgentStateList::scatterNew of every
+            // run at once, each in its own row segment
+            std::vector<fg_column> c(cols.size()), bc(cols.size());
+            for (size_t v = 0; v < cols.size(); ++v) {
+                const uint32_t vb = agent->variables[v].bytes();
+                c[v] = fg_column{cols[v][parity], cols[v][parity ^ 1], vb};
+                bc[v] = fg_column{b.births ? b.birth_cols[v] : cols[v][parity], cols[v][parity ^ 1], vb};
+            }
+            FG_ECAPI(fg_compact_agents_batched(comp_inst, d_tile_begin, ninst, comp_tiles, total_rows, d_counts,
+                                               b.fn->has_agent_death ? b.death_flags : nullptr,
+                                               b.births ? b.birth_flags : nullptr, c.data(), bc.data(),
+                                               static_cast<uint32_t>(c.size()), b.births ? id_col : -1, d_next_ids,
+                                               comp_ws, comp_ws_bytes, stream));
+            parity ^= 1;
+            kernels_per_step += 2;
+            for (uint32_t k = 0; b.births && k < ninst; ++k) bound[k] = std::min<uint64_t>(bound[k] * 2, 1ull << 33);
+        }
     }
 
     bool sorts_at(unsigned int step) const {
@@ -542,10 +801,13 @@ struct BatchedSim {
         kernels_per_step += 1;
     }
 
+    // buffer flips of one step (sorts and compactions), replayed on the host for a cached graph
     int flips_at(unsigned int step) const {
         int f = 0;
-        for (const auto& b : fns)
+        for (const auto& b : fns) {
             if (b.sort && sorts_at(step)) ++f;
+            if (b.fn->has_agent_death || b.births) ++f;
+        }
         return f;
     }
 
@@ -568,12 +830,12 @@ struct BatchedSim {
         unsigned int max_steps = 0;
         for (const auto& p : plans) max_steps = std::max(max_steps, p.getSteps());
         results.assign(ninst, nullptr);
-        std::map<std::pair<int, bool>, cudaGraphExec_t> cache;
         cudaEvent_t t_begin = nullptr, t_end = nullptr;
         FG_ECUDA(cudaEventCreate(&t_begin));
         FG_ECUDA(cudaEventCreate(&t_end));
         FG_ECUDA(cudaEventRecord(t_begin, stream));
         for (unsigned int s = 0; s < max_steps; ++s) {
+            prepare_capacity(s);
             if (cfg.use_graphs) {
                 const auto key = std::make_pair(parity, sorts_at(s));
                 auto it = cache.find(key);
@@ -593,21 +855,27 @@ struct BatchedSim {
                     it = cache.emplace(key, ge).first;
                 } else {
                     if (flips_at(s) & 1) parity ^= 1;
+                    for (const auto& b : fns)
+                        if (b.births)
+                            for (uint32_t k = 0; k < ninst; ++k) bound[k] = std::min<uint64_t>(bound[k] * 2, 1ull << 33);
                 }
                 FG_ECUDA(cudaGraphLaunch(it->second, stream));
                 ++graph_launches;
             } else {
                 enqueue_step(s);
             }
+            after_step(s);
             // runs that end here: read them back and drop them from later steps
             bool any = false;
             for (uint32_t k = 0; k < ninst; ++k) any = any || (plans[k].getSteps() == s + 1 && s + 1 < max_steps);
             if (any) {
                 FG_ECUDA(cudaStreamSynchronize(stream));
+                if (death_or_birth) FG_ECUDA(cudaMemcpy(count.data(), d_counts, sizeof(uint32_t) * ninst, cudaMemcpyDeviceToHost));
                 for (uint32_t k = 0; k < ninst; ++k) {
                     if (plans[k].getSteps() != s + 1 || s + 1 >= max_steps) continue;
                     results[k] = std::make_shared<AgentVector>(read_instance(k));
                     count[k] = 0;
+                    bound[k] = 0;
                     FG_ECUDA(cudaMemcpy(d_counts + k, &count[k], sizeof(uint32_t), cudaMemcpyHostToDevice));
                 }
             }
@@ -619,10 +887,16 @@ struct BatchedSim {
         step_seconds = ms / 1000.0;
         cudaEventDestroy(t_begin);
         cudaEventDestroy(t_end);
-        for (auto& c : cache) cudaGraphExecDestroy(c.second);
+        drop_graphs();
         uint32_t err[4];
         FG_ECUDA(cudaMemcpy(err, d_misc + 1, sizeof(err), cudaMemcpyDeviceToHost));
         if (err[0]) THROW exception::DeviceError(format("Device error %u in a batched ensemble step (name hash 0x%08x, row %u)", err[0], err[1], err[2]));
+        if (death_or_birth) {
+            uint32_t st = 0;
+            FG_ECUDA(cudaMemcpy(&st, comp_ws, sizeof(st), cudaMemcpyDeviceToHost));
+            if (st) THROW exception::DeviceError(format("Batched compaction reported status %d", static_cast<int>(st)));
+            FG_ECUDA(cudaMemcpy(count.data(), d_counts, sizeof(uint32_t) * ninst, cudaMemcpyDeviceToHost));
+        }
         for (uint32_t k = 0; k < ninst; ++k)
             if (!results[k]) results[k] = std::make_shared<AgentVector>(read_instance(k));
     }

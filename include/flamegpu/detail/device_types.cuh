@@ -96,6 +96,7 @@ struct InstanceCtx {
     uint64_t seed;
     uint32_t row_begin;     // first row of the instance
     uint32_t count;         // agents in the instance
+    uint32_t inst;          // index of the instance in its batch (0 for a single simulation)
 };
 
 /** Header of the shared-memory staging window of one block (spatial input). */
@@ -161,7 +162,7 @@ struct LaunchParams {
     uint32_t stage_bytes;        // shared memory for staging neighbour records (0 = off)
     // birth / death
     uint32_t* birth_flags;       // 1 where agent_out was used, 2 if its id was also claimed (null if disabled)
-    uint32_t* birth_next_id;     // next id of the output agent (agent_out.getID() claims from it)
+    uint32_t* birth_next_id;     // next id of the output agent (agent_out.getID() claims from it; one per instance in a batch)
     uint32_t* death_flags;       // ALIVE / DEAD per agent (null if death disabled)
     // step data
     const uint32_t* d_step;      // step counter

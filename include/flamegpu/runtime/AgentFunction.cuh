@@ -60,6 +60,7 @@ __device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, u
         c.seed = P.seed;
         c.row_begin = P.d_first ? *P.d_first : 0u;  // rows before it failed the function's condition
         c.count = n_single;
+        c.inst = 0;
         return;
     }
     const uint32_t k = batch_find(P.batch, P.batch_n, base);
@@ -73,6 +74,7 @@ __device__ __forceinline__ void fill_ctx(const LaunchParams& P, uint32_t base, u
     c.seed = I.seed;
     c.row_begin = I.row_begin;
     c.count = __ldg(P.batch_counts + k);
+    c.inst = k;
 }
 
 // Resident blocks per SM the agent-function kernels are compiled for (the

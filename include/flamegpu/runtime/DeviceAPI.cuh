@@ -957,7 +957,8 @@ class DeviceAPI {
         __device__ id_t getID() const {
             if (!start_row(0u)) return ID_NOT_SET;
             if (is_born != 2u) {
-                claimed = atomicAdd(P.birth_next_id, 1u);
+                // a batch keeps one next id per instance
+                claimed = atomicAdd(P.birth_next_id + detail::ctx().inst, 1u);
                 detail::write_var<id_t>(P, &P.T.birth, detail::VarName("_id").hash, index, claimed);
                 is_born = 2u;
             }

@@ -289,6 +289,26 @@ int fg_spatial_sort_agents_batched(const fg_batch_instance* instances, const uin
                                    const float* z, int32_t dims, const fg_column* cols, uint32_t ncols,
                                    void* workspace, size_t workspace_bytes, void* stream);
 
+/* fg_compact_agents over a batch: every instance's agents compacted in place of
+ * its own row segment in one launch (the reference compacts each run on its
+ * own: CUDAFatAgent.cu:105-137, CUDAAgentStateList.cu:189-250). Instance k's
+ * first counts[k] rows (device, in/out) are its agents: survivors (alive, or
+ * all if NULL) go first from row_begin_k, in order, then births (born != 0, in
+ * parent order; birth_cols as in fg_compact_agents) with ids next_ids[k] + rank
+ * (a born flag of 2 keeps the staging row's id); counts[k] and next_ids[k]
+ * (device, per instance) are updated. Births past an instance's row_capacity
+ * are dropped and FG_ERR_CAPACITY recorded. `instances` (device) as for the
+ * batched builds; `tile_begin` (device, ninst + 1 entries) and `ntiles` from
+ * fg_batch_compact_tiles over the same instances (host copy). cols[c].in /
+ * .out are the whole concatenated columns (distinct arrays). */
+uint32_t fg_batch_compact_tiles(const fg_batch_instance* instances, uint32_t ninst, uint32_t* tile_begin);
+size_t fg_compact_batched_workspace_size(uint32_t ntiles, uint32_t ninst);
+int fg_compact_agents_batched(const fg_batch_instance* instances, const uint32_t* tile_begin, uint32_t ninst,
+                              uint32_t ntiles, uint32_t total_rows, uint32_t* counts, const uint32_t* alive,
+                              const uint32_t* born, const fg_column* cols, const fg_column* birth_cols,
+                              uint32_t ncols, int32_t id_col, uint32_t* next_ids, void* workspace,
+                              size_t workspace_bytes, void* stream);
+
 /* Last CUDA error seen by this library on the calling thread (cudaError_t). */
 int fg_last_cuda_error(void);
 /* Library version string. */

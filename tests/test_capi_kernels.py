@@ -26,7 +26,7 @@ def _capi():
 def test_header_symbols_exported():
     capi = _capi()
     hdr = open(os.path.join(ROOT, "include", "flamegpu_gb300", "fg_capi.h")).read()
-    declared = set(re.findall(r"^(?:int|size_t|const char\*)\s+(fg_\w+)\(", hdr, re.M))
+    declared = set(re.findall(r"^(?:int|size_t|uint32_t|const char\*)\s+(fg_\w+)\(", hdr, re.M))
     assert declared == set(capi.EXPORTS)
     L = capi.lib()
     for name in declared:
@@ -524,3 +524,84 @@ def test_batched_sort_matches_each_instance():
         keys = O.sort_keys(og, p[:, 0], p[:, 1], p[:, 2])
         eperm = O.stable_sort_perm(keys, O.sort_max_bit(og))
         np.testing.assert_array_equal(got_ids[i.row_begin:i.row_begin + count], i.row_begin + eperm)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("with_births", [False, True])
+def test_batched_compaction_matches_each_instance(with_births):
+    # instances of uneven size (empty, one block, several tiles, one with room
+    # for few births), each compacted in its own segment; order, ids and
+    # counts as a compaction of each instance alone (the oracle's)
+    import torch
+    capi = _capi()
+    L = capi.lib()
+    rng = np.random.default_rng(21 + with_births)
+    pops = [0, 1, 127, 5000, 2048, 9000, 300, 70_000]
+    caps = [128, 128, 256, 12_032, 4096, 9088, 640, 140_032]
+    g = capi.grid(3, (0, 0, 0), (8, 8, 8), 1.0)
+    arr = (capi.BatchInstance * len(pops))()
+    row = 0
+    for k, cap in enumerate(caps):
+        capi.check(L.fg_batch_instance_init(C.byref(arr[k]), C.byref(g), row, cap, 0, 0, None), "instance")
+        row += cap
+    total = row
+    tb = (C.c_uint32 * (len(pops) + 1))()
+    ntiles = L.fg_batch_compact_tiles(arr, len(pops), tb)
+    alive = np.zeros(total, np.uint32)
+    born = np.zeros(total, np.uint32)
+    f = rng.random(total).astype(np.float32)
+    ids = np.zeros(total, np.uint32)
+    nid = np.zeros(len(pops), np.uint32)
+    for k, (n, cap) in enumerate(zip(pops, caps)):
+        rb = arr[k].row_begin
+        alive[rb:rb + n] = rng.random(n) >= 0.3
+        if with_births:
+            born[rb:rb + n] = (rng.random(n) < 0.4) * (1 + (rng.random(n) < 0.1))  # some ids claimed (2)
+        ids[rb:rb + n] = np.arange(1, n + 1)
+        nid[k] = n + 1
+        alive[rb + n:rb + cap] = 1  # stale flags past the count must be ignored
+        born[rb + n:rb + cap] = 1
+    dev = "cuda"
+    d_inst = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev)
+    d_tb = torch.tensor(list(tb), dtype=torch.int32, device=dev)
+    counts = torch.tensor(pops, dtype=torch.int32, device=dev)
+    next_ids = torch.from_numpy(nid.view(np.int32)).to(dev)
+    f_in = torch.from_numpy(f).to(dev)
+    id_in = torch.from_numpy(ids.view(np.int32)).to(dev)
+    bf_in = f_in * 10 + 1
+    bid_in = torch.from_numpy((ids + 100_000).view(np.int32)).to(dev)  # a claimed birth keeps this id
+    f_out = torch.zeros(total, dtype=torch.float32, device=dev)
+    id_out = torch.zeros(total, dtype=torch.int32, device=dev)
+    cols = capi.columns([(f_in, f_out), (id_in, id_out)])
+    bcols = capi.columns([(bf_in, f_out), (bid_in, id_out)])
+    a_t = torch.from_numpy(alive.view(np.int32)).to(dev)
+    b_t = torch.from_numpy(born.view(np.int32)).to(dev) if with_births else None
+    ws = capi.Workspace(L.fg_compact_batched_workspace_size(ntiles, len(pops)))
+    for _ in range(2):  # the second call reuses the workspace (other status array)
+        capi.check(L.fg_compact_agents_batched(d_inst.data_ptr(), d_tb.data_ptr(), len(pops), ntiles, total,
+                                               counts.data_ptr(), a_t.data_ptr(), capi.ptr(b_t), cols, bcols, 2, 1,
+                                               next_ids.data_ptr(), ws.ptr, ws.nbytes, capi.stream_handle()),
+                   "fg_compact_agents_batched")
+        torch.cuda.synchronize()
+        got_f, got_id = f_out.cpu().numpy(), id_out.cpu().numpy().view(np.uint32)
+        got_n, got_nid = counts.cpu().numpy(), next_ids.cpu().numpy().view(np.uint32)
+        for k, (n, cap) in enumerate(zip(pops, caps)):
+            rb = arr[k].row_begin
+            surv = O.compact(alive[rb:rb + n])
+            kids = O.compact(born[rb:rb + n]) if with_births else np.zeros(0, np.uint32)
+            kids = kids[:max(0, cap - len(surv))]
+            m = len(surv) + len(kids)
+            assert got_n[k] == m, k
+            np.testing.assert_array_equal(got_f[rb:rb + len(surv)], f[rb + surv])
+            np.testing.assert_array_equal(got_id[rb:rb + len(surv)], ids[rb + surv])
+            if len(kids):
+                np.testing.assert_array_equal(got_f[rb + len(surv):rb + m], f[rb + kids] * 10 + 1)
+                claimed = born[rb + kids] == 2
+                r = np.arange(len(kids), dtype=np.uint32)
+                want = np.where(claimed, ids[rb + kids] + 100_000, n + 1 + r)
+                np.testing.assert_array_equal(got_id[rb + len(surv):rb + m], want)
+            assert got_nid[k] == n + 1 + (len(O.compact(born[rb:rb + n])) if with_births else 0)
+        # back to the inputs for the second call
+        counts.copy_(torch.tensor(pops, dtype=torch.int32))
+        next_ids.copy_(torch.from_numpy(nid.view(np.int32)))
+    assert ws.status() == (capi.FG_ERR_CAPACITY if with_births else capi.FG_OK)

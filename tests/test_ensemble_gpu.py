@@ -76,3 +76,58 @@ def test_batched_ensemble_matches_oracle():
         np.testing.assert_array_equal(got["_id"], ref["id"])
         for k in ("x", "y", "z", "fx", "fy", "fz"):
             np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+
+
+BD_NAMES = ("_id", "counter") + tuple(f"f{v}" for v in range(8))
+
+
+def _bd_runs(params, steps, batched):
+    """Birth/death ensemble: params = [(n, p_death, p_birth, seed)], steps per run."""
+    import ctypes as C
+    from flamegpu2_gb300 import sim, synth
+    ens = sim.Ensemble("birth_death", [0.3, 0.2, 1.0], batched=batched)
+    pops = []
+    for (n, pd, pb, seed), st in zip(params, steps):
+        pop = synth.birth_death_population(n, seed)
+        pops.append(pop)
+        r = ens.add_run(st, seed, "agent", n, pop)
+        ens.set_property(r, "P_DEATH", pd)
+        ens.set_property(r, "P_BIRTH", pb)
+        ens.set_property(r, "SEED", seed, C.c_uint64)
+    assert ens.simulate() == 0
+    out = [{k: ens.get(i, "agent", k, np.uint32 if k == "_id" else (np.int32 if k == "counter" else np.float32))
+            for k in BD_NAMES} for i in range(len(params))]
+    st = ens.stats()
+    ens.close()
+    return pops, out, st
+
+
+@pytest.mark.parametrize("graphs", [True])
+def test_batched_birth_death_equals_plain_runs_and_oracle(graphs):
+    # births and deaths inside one batched simulation (segmented compaction
+    # over every run's rows): each run equals its own plain run and the oracle,
+    # order and ids included. Growing runs (low death, high birth) outgrow
+    # their row segments several times, shrinking ones empty out.
+    import oracle as O
+    from flamegpu2_gb300 import sim
+    params = [(0, 0.3, 0.2, 3), (1, 0.0, 1.0, 4), (100, 0.3, 0.2, 5), (3000, 0.05, 0.6, 6), (20_000, 0.3, 0.2, 7),
+              (5000, 0.9, 0.1, 8), (777, 0.1, 0.5, 9), (40_000, 0.2, 0.3, 10)]
+    steps = [10, 12, 12, 12, 7, 12, 12, 9]
+    pops, out, st = _bd_runs(params, steps, batched=True)
+    assert st["batched"]
+    for (n, pd, pb, seed), stp, pop, got in zip(params, steps, pops, out):
+        s = sim.Simulation("birth_death", [pd, pb, seed])
+        s.set_population("agent", n, pop)
+        s.step(stp)
+        for k in BD_NAMES:
+            dt = np.uint32 if k == "_id" else (np.int32 if k == "counter" else np.float32)
+            np.testing.assert_array_equal(got[k], s.get("agent", k, dt), err_msg=f"run n={n} seed={seed} {k}")
+        s.close()
+        f = np.stack([pop[f"f{v}"] for v in range(8)]) if n else np.zeros((8, 0), np.float32)
+        cap = max(4 * n, 1024) * 64
+        fo, co, io, _, _ = O.birth_death_run(f, pop["counter"], pop["_id"], n + 1, cap, pd, pb, seed, stp)
+        np.testing.assert_array_equal(got["_id"], io)
+        np.testing.assert_array_equal(got["counter"], co)
+        for v in range(8):
+            np.testing.assert_array_equal(got[f"f{v}"], fo[v])
+    assert len(out[3]["_id"]) > 3000 * 10  # a run that grew well past its first segment
