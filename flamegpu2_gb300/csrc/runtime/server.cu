@@ -118,6 +118,7 @@ void SimulationServer::retire(Job& j, bool failed, const std::string& error) {
     r.error = error;
     if (!failed && j.sim) {
         try {
+            r.agent_steps = j.sim->getAgentStepCount();
             for (const auto& a : j.model->getData()->agents)
                 for (const auto& st : a->states) {
                     auto pop = std::make_shared<AgentVector>(AgentDescription(j.model->getData(), a.get()));

@@ -195,6 +195,10 @@ extern "C" int fgs_get_variable_device(fgs_sim* s, const char* agent, const char
     });
 }
 
+extern "C" int fgs_agent_steps(fgs_sim* s, uint64_t* agent_steps) {
+    return guarded([&] { *agent_steps = s->sim->getAgentStepCount(); });
+}
+
 extern "C" int fgs_step(fgs_sim* s, uint32_t steps) {
     return guarded([&] {
         s->sim->step(static_cast<unsigned int>(steps));
@@ -580,6 +584,10 @@ extern "C" int fgv_take_completed(fgv_server* v, uint64_t* ids, uint32_t cap, ui
         pending.erase(pending.begin(), pending.begin() + k);
         if (n) *n = k;
     });
+}
+
+extern "C" int fgv_result_agent_steps(fgv_server* v, uint64_t id, uint64_t* agent_steps) {
+    return guarded([&] { *agent_steps = result_of(v, id).agent_steps; });
 }
 
 extern "C" int fgv_result_info(fgv_server* v, uint64_t id, double* t, int32_t* failed, char* err, size_t len) {

@@ -58,15 +58,38 @@ namespace {
 // End of a step in one launch: the message counts of the non-persistent
 // lists are cleared (CUDASimulation.cu:619-625) and the step counter advances.
 constexpr uint32_t kStepEndClears = 16;
+constexpr uint32_t kStepEndCounts = 32;
 struct StepEnd {
     uint32_t* clear[kStepEndClears];
     uint32_t nclear;
     uint32_t* d_step;
+    // agent-steps: acc[0] += acc[1] (the agents that entered this step), then
+    // acc[1] = the agents of every list now (those entering the next one)
+    const uint32_t* counts[kStepEndCounts];
+    uint32_t ncounts;
+    unsigned long long* acc;
 };
 __global__ void k_step_end(const __grid_constant__ StepEnd e) {
     grid_dependency_enter();
     if (threadIdx.x < e.nclear) *e.clear[threadIdx.x] = 0u;
     if (threadIdx.x == 0) *e.d_step += 1u;
+    if (e.acc && threadIdx.x < 32) {
+        unsigned long long c = threadIdx.x < e.ncounts ? *e.counts[threadIdx.x] : 0ull;
+        for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, d);
+        if (threadIdx.x == 0) {
+            e.acc[0] += e.acc[1];
+            e.acc[1] = c;
+        }
+    }
+}
+// acc[1] = the agents of every list (after a population was set from the host)
+__global__ void k_recount(const __grid_constant__ StepEnd e) {
+    grid_dependency_enter();
+    if (threadIdx.x < 32) {
+        unsigned long long c = threadIdx.x < e.ncounts ? *e.counts[threadIdx.x] : 0ull;
+        for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, d);
+        if (threadIdx.x == 0) e.acc[1] = c;
+    }
 }
 __global__ void k_max_u32(uint32_t* p, uint32_t v) {
     grid_dependency_enter();
@@ -366,6 +389,7 @@ struct SimulationImpl {
     bool env_dirty = true;
     // misc device state
     uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record, [8..] next ids per agent
+    unsigned long long* d_agent_steps = nullptr;  // [0] agents summed over the steps run, [1] agents now
     uint32_t* h_pinned = nullptr;
     uint32_t* h_pinned_dev = nullptr;  // its device address (null: not mapped)
     unsigned int step_count = 0;
@@ -457,6 +481,7 @@ struct SimulationImpl {
         h_pinned_dev = static_cast<uint32_t*>(host_mapped(h_pinned));
         std::memset(h_pinned, 0, 4096);
         d_misc = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (8 + model->agents.size() + 8)));
+        d_agent_steps = static_cast<unsigned long long*>(mem.alloc(2 * sizeof(unsigned long long)));
         next_id.assign(model->agents.size(), 1u);
         std::vector<uint32_t> init_ids(model->agents.size(), 1u);
         FG_CUDA(cudaMemcpy(d_misc + 8, init_ids.data(), sizeof(uint32_t) * init_ids.size(), cudaMemcpyHostToDevice));
@@ -824,8 +849,10 @@ struct SimulationImpl {
         return false;
     }
 
-    // Populations were replaced from the host: earlier reports no longer apply.
+    // Populations were replaced from the host: earlier reports no longer apply,
+    // and the agents entering the next step are counted again.
     void forget_counts() {
+        recount();
         for (auto& c : count_ring) {
             if (c.used) cudaEventSynchronize(c.ev);
             c.used = false;
@@ -1357,7 +1384,22 @@ struct SimulationImpl {
                 if (m->bf_count) clear(m->bf_count);
             }
         e.d_step = d_step();
+        count_targets(e);
         FG_CUDA(launch_kernel(pdl_enabled(), k_step_end, 1, 32, 0, stream, e));
+    }
+
+    // Every list's count, for the agent-step accumulator (models of at most
+    // kStepEndCounts agent lists; beyond that, no count is kept).
+    void count_targets(StepEnd& e) const {
+        if (lists.size() > kStepEndCounts) return;
+        for (const auto& l : lists) e.counts[e.ncounts++] = l->d_count;
+        e.acc = d_agent_steps;
+    }
+    // After a population is set from the host: the agents entering the next step.
+    void recount() {
+        StepEnd e{};
+        count_targets(e);
+        if (e.acc) FG_CUDA(launch_kernel(pdl_enabled(), k_recount, 1, 32, 0, stream, e));
     }
 
     bool has_layer_host_functions() const {
@@ -2208,6 +2250,13 @@ void detail::SimulationImpl::resolve_step_timers() {
         cudaEventDestroy(e.e1);
     }
     step_events.clear();
+}
+
+unsigned long long CUDASimulation::getAgentStepCount() {
+    unsigned long long v = 0;
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    FG_CUDA(cudaMemcpy(&v, impl->d_agent_steps, sizeof(v), cudaMemcpyDeviceToHost));
+    return v;
 }
 
 double CUDASimulation::getElapsedTimeSimulation() const { return impl->sim_ms / 1000.0; }

@@ -22,7 +22,7 @@ SIM_EXPORTS = [
     "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
     "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
     "fgs_set_stage_bytes", "fgs_reset_population_device", "fgs_time_ops_in_graphs", "fgs_harvest_profile",
-    "fgs_export", "fgs_load_state", "fgs_set_log", "fgs_run_log",
+    "fgs_export", "fgs_load_state", "fgs_set_log", "fgs_run_log", "fgs_agent_steps",
 ]
 
 _lock = threading.Lock()
@@ -56,6 +56,7 @@ def core():
                                              C.POINTER(u32)]
             L.fgs_get_variable_device.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
             L.fgs_step.argtypes = [vp, u32]
+            L.fgs_agent_steps.argtypes = [vp, C.POINTER(C.c_uint64)]
             L.fgs_simulate.argtypes = [vp]
             L.fgs_synchronize.argtypes = [vp]
             L.fgs_set_environment.argtypes = [vp, C.c_char_p, vp, sz]
@@ -173,6 +174,12 @@ class Simulation:
 
     def step(self, n: int = 1):
         _check(core().fgs_step(self._h, n))
+
+    def agent_steps(self) -> int:
+        """Agents summed over the steps run (each step with the populations that entered it)."""
+        v = C.c_uint64()
+        _check(core().fgs_agent_steps(self._h, C.byref(v)))
+        return v.value
 
     def simulate(self):
         _check(core().fgs_simulate(self._h))
@@ -343,7 +350,7 @@ class Ensemble:
 
 SERVER_EXPORTS = ["fgv_create", "fgv_destroy", "fgv_submit", "fgv_poll", "fgv_run_until_idle", "fgv_take_completed",
                   "fgv_result_info", "fgv_result_count", "fgv_result_variable", "fgv_release", "fgv_stats",
-                  "fgv_counters", "fgv_set_scheduling"]
+                  "fgv_counters", "fgv_set_scheduling", "fgv_result_agent_steps"]
 _srv_ready = False
 
 
@@ -362,6 +369,7 @@ def _srv():
         L.fgv_take_completed.argtypes = [vp, C.POINTER(u64), u32, C.POINTER(u32)]
         L.fgv_result_info.argtypes = [vp, u64, C.POINTER(C.c_double), C.POINTER(i32), C.c_char_p, sz]
         L.fgv_result_count.argtypes = [vp, u64, C.c_char_p, C.c_char_p, C.POINTER(u32)]
+        L.fgv_result_agent_steps.argtypes = [vp, u64, C.POINTER(u64)]
         L.fgv_result_variable.argtypes = [vp, u64, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
         L.fgv_release.argtypes = [vp, u64]
         L.fgv_stats.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u64)]
@@ -440,8 +448,10 @@ class Server:
         f = C.c_int32()
         err = C.create_string_buffer(1024)
         _check(_srv().fgv_result_info(self._h, rid, t, C.byref(f), err, 1024))
+        a = C.c_uint64()
+        _check(_srv().fgv_result_agent_steps(self._h, rid, C.byref(a)))
         return {"arrival_s": t[0], "admitted_s": t[1], "completed_s": t[2], "failed": bool(f.value),
-                "error": err.value.decode()}
+                "error": err.value.decode(), "agent_steps": a.value}
 
     def count(self, rid: int, agent: str, state: str = "default") -> int:
         n = C.c_uint32()

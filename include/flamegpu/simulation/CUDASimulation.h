@@ -146,6 +146,10 @@ class CUDASimulation {
     void resetStepCounter();
 
     double getElapsedTimeSimulation() const;
+    /** Agents summed over the steps run so far (all agent types and states,
+     *  each step counted with the populations that entered it); waits for the
+     *  steps issued. An extension (the reference has no such counter). */
+    unsigned long long getAgentStepCount();
     std::vector<double> getElapsedTimeSteps() const;
     double getElapsedTimeStep(unsigned int step) const;
 

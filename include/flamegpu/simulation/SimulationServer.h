@@ -52,6 +52,7 @@ class SimulationServer {
         uint64_t id = 0;
         double arrival_s = 0, admitted_s = 0, completed_s = 0;  // seconds since the server started
         unsigned int steps = 0;
+        unsigned long long agent_steps = 0;  // agents summed over the steps run (CUDASimulation::getAgentStepCount)
         bool failed = false;
         std::string error;
         size_t reserved_bytes = 0;

@@ -60,6 +60,10 @@ int fgs_get_variable_device(fgs_sim* sim, const char* agent, const char* state, 
                             size_t bytes);
 int fgs_step(fgs_sim* sim, uint32_t steps);
 int fgs_simulate(fgs_sim* sim);
+/* Agents summed over the steps run so far (each step counted with the
+ * populations that entered it; CUDASimulation::getAgentStepCount). Waits for
+ * the steps issued. */
+int fgs_agent_steps(fgs_sim* sim, uint64_t* agent_steps);
 /* Waits for the simulation stream and reports recorded device errors. */
 int fgs_synchronize(fgs_sim* sim);
 int fgs_set_environment(fgs_sim* sim, const char* name, const void* value, size_t bytes);
@@ -141,6 +145,8 @@ int fgv_take_completed(fgv_server* v, uint64_t* ids, uint32_t cap, uint32_t* n);
 /* Times (seconds since the server started: arrival, admitted, completed) and
  * status of a completed run; the error text goes to err (len bytes) if failed. */
 int fgv_result_info(fgv_server* v, uint64_t id, double* times3, int32_t* failed, char* err, size_t len);
+/* Agents summed over the steps a completed run ran (CUDASimulation::getAgentStepCount). */
+int fgv_result_agent_steps(fgv_server* v, uint64_t id, uint64_t* agent_steps);
 int fgv_result_count(fgv_server* v, uint64_t id, const char* agent, const char* state, uint32_t* n);
 int fgv_result_variable(fgv_server* v, uint64_t id, const char* agent, const char* state, const char* var, void* out,
                         size_t bytes);

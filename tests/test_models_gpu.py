@@ -203,9 +203,12 @@ def test_birth_death_matches_oracle_exactly():
     f = np.stack([s.get("agent", f"f{v}", np.float32) for v in range(8)])
     cnt = s.get("agent", "counter", np.int32)
     ids = s.get("agent", "_id", np.uint32)
+    agent_steps = s.agent_steps()
     s.close()
     fo, co, io, nid, pops = O.birth_death_run(np.stack([pop[f"f{v}"] for v in range(8)]), pop["counter"],
                                               pop["_id"], n + 1, 4 * n, 0.30, 0.20, seed, steps)
+    # agent-steps counted on the device: the populations entering each step
+    assert agent_steps == int(pops.astype(np.int64).sum())
     assert len(ids) == len(io)
     np.testing.assert_array_equal(ids, io)
     np.testing.assert_array_equal(cnt, co)

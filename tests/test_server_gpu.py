@@ -31,7 +31,8 @@ def _plain_predprey(p, prey, pred, steps):
     s.set_population("predator", len(pred["x"]), pred)
     s.step(steps)
     out = ({k: s.get("prey", k, np.uint32 if k == "_id" else np.float32) for k in ("_id", "x", "y")},
-           {k: s.get("predator", k, np.uint32 if k == "_id" else np.float32) for k in ("_id", "x", "y")})
+           {k: s.get("predator", k, np.uint32 if k == "_id" else np.float32) for k in ("_id", "x", "y")},
+           s.agent_steps())
     s.close()
     return out
 
@@ -40,7 +41,7 @@ def _plain_predprey(p, prey, pred, steps):
 def test_predprey_matches_oracle_exactly(n_prey, n_pred, steps):
     from flamegpu2_gb300 import synth
     prey, pred = synth.predprey_population(n_prey, n_pred, PP["edge"], 3)
-    gp, gq = _plain_predprey(PP, prey, pred, steps)
+    gp, gq, _ = _plain_predprey(PP, prey, pred, steps)
     op, oq, _ = O.predprey_run(PP, prey, pred, steps, n_prey + 1)
     for k in ("_id", "x", "y"):
         np.testing.assert_array_equal(gp[k], op[k], err_msg=f"prey {k}")
@@ -99,8 +100,10 @@ def test_server_result_same_alone_and_in_the_mix():
     for a, b in zip(alone, mixed):
         for k in a:
             np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    mixed_steps = srv.info(rid)["agent_steps"]
     # and the plain CUDASimulation and the oracle agree with both
     plain = _plain_predprey(PS, prey, pred, steps)
+    assert mixed_steps == plain[2] > 0  # agent-steps of the run (populations entering each step)
     op, oq, _ = O.predprey_run(PS, prey, pred, steps, 12_001)
     for k in ("_id", "x", "y"):
         np.testing.assert_array_equal(plain[0][k], mixed[0][k])
