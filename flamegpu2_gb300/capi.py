@@ -35,6 +35,7 @@ EXPORTS = [
     "fg_spatial_build_batched", "fg_spatial_sort_agents_batched", "fg_exclusive_scan_u32_noalloc",
     "fg_partition_agents", "fg_append_rows", "fg_workspace_set_wait_limit", "fg_noalloc_scan_status",
     "fg_append_births", "fg_batch_compact_tiles", "fg_compact_batched_workspace_size", "fg_compact_agents_batched",
+    "fg_set_thread_tuning",
 ]
 FG_NOALLOC_SCAN_MAX_N = 1 << 25
 

@@ -236,12 +236,14 @@ inline uint32_t scan_tiles(uint32_t n) { return (n + kScanTile - 1) / kScanTile;
 
 // Scans of more than this many values take four sub-tiles per tile.
 constexpr uint32_t kScanWideMin = 1u << 22;
+// The threshold of the calling thread's scans (fg_set_thread_tuning).
+inline thread_local uint32_t t_scan_wide_min = kScanWideMin;
 
 // last, last_floor: optional (device) bound, as in k_scan_u32; only without self_reset.
 inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in, uint64_t* status,
                                WsHeader* h, int self_reset, cudaStream_t st, const uint32_t* last = nullptr,
                                uint32_t last_floor = 0) {
-    if (n > kScanWideMin)
+    if (n > t_scan_wide_min)
         return launch(k_scan_u32<4>, (n + 4u * kScanTile - 1) / (4u * kScanTile), kThreads, st, in, out, n, zero_in,
                       status, h, self_reset, last, last_floor);
     return launch(k_scan_u32<1>, scan_tiles(n), kThreads, st, in, out, n, zero_in, status, h, self_reset, last,

@@ -1028,6 +1028,12 @@ extern "C" int fg_workspace_status(void* workspace, size_t workspace_bytes, void
     return static_cast<int>(static_cast<int32_t>(v));
 }
 
+extern "C" int fg_set_thread_tuning(const fg_tuning* t) {
+    if (t && t->scan_wide_min > 0 && t->scan_wide_min < kScanTile) return FG_ERR_INVALID_ARGUMENT;
+    t_scan_wide_min = (t && t->scan_wide_min) ? t->scan_wide_min : kScanWideMin;
+    return FG_OK;
+}
+
 extern "C" const char* fg_version(void) { return "flamegpu2_gb300 0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------------ batches

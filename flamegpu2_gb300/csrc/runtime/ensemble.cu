@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -27,6 +29,7 @@
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu_gb300/fg_capi.h"
 #include "runtime/internal.h"
+#include "runtime/json.h"
 
 namespace flamegpu {
 
@@ -239,6 +242,19 @@ struct BatchedSim {
     unsigned int kernels_per_step = 0;
     unsigned long long graph_launches = 0;
     std::map<std::pair<int, bool>, cudaGraphExec_t> cache;
+
+    // Launch shape of the batched step (the autotuner's knobs): threads per
+    // agent-function block, resident blocks per SM of its grid-stride grid,
+    // shared memory for staged neighbourhoods, and the scans' wide-tile
+    // threshold (fg_tuning; 0: the library's default).
+    struct Shape {
+        uint32_t block = kAgentBlock;
+        uint32_t blocks_per_sm = 16;
+        uint32_t stage_bytes = 96u * 1024u;
+        uint32_t scan_wide_min = 0;
+    };
+    Shape shape;
+    std::string tuning_json = "{\"tuned\": false}";
 
     BatchedSim(std::shared_ptr<ModelData> m, const RunPlanVector& p, const CUDAEnsemble::EnsembleConfig& c)
         : model(std::move(m)), plans(p), cfg(c) {}
@@ -712,7 +728,7 @@ struct BatchedSim {
             const fg_spatial_grid& g = m.inst[k].grid;
             const double per_bin = static_cast<double>(count[k]) / std::max<uint32_t>(g.binCount, 1u);
             all += count[k];
-            if (detail::stage_window_fits(g, per_bin, m.record_words, kAgentBlock, cfg.message_stage_bytes)) fit += count[k];
+            if (detail::stage_window_fits(g, per_bin, m.record_words, shape.block, shape.stage_bytes)) fit += count[k];
         }
         return all > 0.0 && fit >= 0.5 * all;
     }
@@ -731,8 +747,8 @@ struct BatchedSim {
             P.in_pay_mult = b.in->pay_mult;
             P.in_pay_shift = b.in->pay_shift;
             P.in_pay_stride = b.in->pay_stride;
-            if (b.sort && cfg.message_stage_bytes >= 1024u && stage_pays(*b.in)) {
-                P.stage_bytes = (cfg.message_stage_bytes + 15u) & ~15u;
+            if (b.sort && shape.stage_bytes >= 1024u && stage_pays(*b.in)) {
+                P.stage_bytes = (shape.stage_bytes + 15u) & ~15u;
                 smem = P.stage_bytes + static_cast<unsigned int>(sizeof(StageHeader));
             }
         }
@@ -745,8 +761,8 @@ struct BatchedSim {
         P.batch = b.d_rt;
         P.batch_counts = d_counts;
         P.batch_n = ninst;
-        const uint32_t grid = std::min(total_rows / kAgentBlock, static_cast<uint32_t>(sms * 16));
-        const cudaError_t e = b.fn->launcher(P, std::max(1u, grid), kAgentBlock, smem, stream, detail::pdl_enabled());
+        const uint32_t grid = std::min(total_rows / shape.block, static_cast<uint32_t>(sms) * shape.blocks_per_sm);
+        const cudaError_t e = b.fn->launcher(P, std::max(1u, grid), shape.block, smem, stream, detail::pdl_enabled());
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", b.fn->name.c_str(), cudaGetErrorString(e)));
         kernels_per_step += 1;
@@ -825,6 +841,237 @@ struct BatchedSim {
         return pop;
     }
 
+    // One step: captured (or replayed) as a graph per buffer parity and sort decision.
+    void issue_step(unsigned int s) {
+        prepare_capacity(s);
+        fg_tuning t{};
+        t.scan_wide_min = shape.scan_wide_min;
+        FG_ECAPI(fg_set_thread_tuning(&t));
+        if (cfg.use_graphs) {
+            const auto key = std::make_pair(parity, sorts_at(s));
+            auto it = cache.find(key);
+            if (it == cache.end()) {
+                cudaGraph_t g;
+                FG_ECUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                try {
+                    enqueue_step(s);
+                } catch (...) {
+                    cudaStreamEndCapture(stream, &g);
+                    fg_set_thread_tuning(nullptr);
+                    throw;
+                }
+                FG_ECUDA(cudaStreamEndCapture(stream, &g));
+                cudaGraphExec_t ge;
+                FG_ECUDA(cudaGraphInstantiate(&ge, g, 0));
+                cudaGraphDestroy(g);
+                it = cache.emplace(key, ge).first;
+            } else {
+                if (flips_at(s) & 1) parity ^= 1;
+                for (const auto& b : fns)
+                    if (b.births)
+                        for (uint32_t k = 0; k < ninst; ++k) bound[k] = std::min<uint64_t>(bound[k] * 2, 1ull << 33);
+            }
+            FG_ECUDA(cudaGraphLaunch(it->second, stream));
+            ++graph_launches;
+        } else {
+            enqueue_step(s);
+        }
+        fg_set_thread_tuning(nullptr);
+        after_step(s);
+    }
+
+    // ---- autotuner
+    // The size class of this batch: GPU, model, and powers of two of the
+    // total agents, the runs and the agents per run.
+    std::string size_class() const {
+        cudaDeviceProp prop{};
+        cudaGetDeviceProperties(&prop, cfg.device);
+        uint64_t total = 0;
+        for (uint32_t k = 0; k < ninst; ++k) total += count[k];
+        auto lg = [](double v) { return static_cast<int>(std::lround(std::log2(std::max(v, 1.0)))); };
+        return format("%s|%s|agents 2^%d|runs 2^%d|per run 2^%d", prop.name, model->name.c_str(), lg(double(total)),
+                      lg(double(ninst)), lg(double(total) / std::max(1u, ninst)));
+    }
+    static std::string shape_json(const Shape& h) {
+        return format("{\"block\": %u, \"blocks_per_sm\": %u, \"stage_bytes\": %u, \"scan_wide_min\": %u}", h.block,
+                      h.blocks_per_sm, h.stage_bytes, h.scan_wide_min);
+    }
+    // The state every tuning trial starts from (agent columns, counts, ids, step).
+    struct Snapshot {
+        std::vector<void*> cols;
+        int parity = 0;
+        std::vector<uint32_t> counts, next_ids, misc;
+    };
+    Snapshot snapshot() {
+        Snapshot sn;
+        FG_ECUDA(cudaStreamSynchronize(stream));
+        sn.parity = parity;
+        for (size_t v = 0; v < cols.size(); ++v) {
+            const size_t b = agent->variables[v].bytes() * static_cast<size_t>(total_rows);
+            void* p = mem.get(b);
+            FG_ECUDA(cudaMemcpy(p, cols[v][parity], b, cudaMemcpyDeviceToDevice));
+            sn.cols.push_back(p);
+        }
+        sn.counts.resize(ninst);
+        sn.next_ids.resize(ninst);
+        sn.misc.resize(16);
+        FG_ECUDA(cudaMemcpy(sn.counts.data(), d_counts, sizeof(uint32_t) * ninst, cudaMemcpyDeviceToHost));
+        FG_ECUDA(cudaMemcpy(sn.next_ids.data(), d_next_ids, sizeof(uint32_t) * ninst, cudaMemcpyDeviceToHost));
+        FG_ECUDA(cudaMemcpy(sn.misc.data(), d_misc, sizeof(uint32_t) * 16, cudaMemcpyDeviceToHost));
+        return sn;
+    }
+    void restore(const Snapshot& sn) {
+        FG_ECUDA(cudaStreamSynchronize(stream));
+        parity = sn.parity;
+        for (size_t v = 0; v < cols.size(); ++v)
+            FG_ECUDA(cudaMemcpy(cols[v][parity], sn.cols[v], agent->variables[v].bytes() * static_cast<size_t>(total_rows),
+                                cudaMemcpyDeviceToDevice));
+        FG_ECUDA(cudaMemcpy(d_counts, sn.counts.data(), sizeof(uint32_t) * ninst, cudaMemcpyHostToDevice));
+        FG_ECUDA(cudaMemcpy(d_next_ids, sn.next_ids.data(), sizeof(uint32_t) * ninst, cudaMemcpyHostToDevice));
+        FG_ECUDA(cudaMemcpy(d_misc, sn.misc.data(), sizeof(uint32_t) * 16, cudaMemcpyHostToDevice));
+        count = sn.counts;
+    }
+    // Device milliseconds per step of a shape: one step to capture, then
+    // `steps` replays timed with CUDA events on the step's stream.
+    double time_shape(const Shape& h, const Snapshot& sn, unsigned int steps) {
+        restore(sn);
+        shape = h;
+        drop_graphs();
+        issue_step(0);
+        cudaEvent_t a, b;
+        FG_ECUDA(cudaEventCreate(&a));
+        FG_ECUDA(cudaEventCreate(&b));
+        FG_ECUDA(cudaEventRecord(a, stream));
+        for (unsigned int s = 1; s <= steps; ++s) issue_step(s);
+        FG_ECUDA(cudaEventRecord(b, stream));
+        FG_ECUDA(cudaEventSynchronize(b));
+        float ms = 0.0f;
+        FG_ECUDA(cudaEventElapsedTime(&ms, a, b));
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return ms / steps;
+    }
+    // mode 1: the cache's shape for this size class (defaults if none);
+    // mode 2: every candidate timed on this batch, the fastest kept and stored.
+    void autotune(int mode, const std::string& path) {
+        const std::string key = size_class();
+        Shape def;
+        def.stage_bytes = cfg.message_stage_bytes;
+        shape = def;
+        json::Value doc;
+        bool have_doc = false;
+        if (!path.empty()) {
+            if (std::FILE* f = std::fopen(path.c_str(), "rb")) {
+                std::string text;
+                char buf[4096];
+                size_t r;
+                while ((r = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, r);
+                std::fclose(f);
+                try {
+                    doc = json::Parser(text).parse();
+                    have_doc = doc.kind == json::Value::Object;
+                } catch (const std::exception&) {
+                    have_doc = false;
+                }
+            }
+        }
+        const json::Value* entries = have_doc ? doc.find("entries") : nullptr;
+        const json::Value* hit = entries ? entries->find(key) : nullptr;
+        if (mode == 1) {
+            if (hit) {
+                auto u = [&](const char* n, uint32_t d) {
+                    const json::Value* v = hit->find(n);
+                    return v ? static_cast<uint32_t>(v->uinteger()) : d;
+                };
+                shape.block = u("block", def.block);
+                shape.blocks_per_sm = u("blocks_per_sm", def.blocks_per_sm);
+                shape.stage_bytes = u("stage_bytes", def.stage_bytes);
+                shape.scan_wide_min = u("scan_wide_min", def.scan_wide_min);
+                if (shape.block != 32 && shape.block != 64 && shape.block != 128) shape.block = def.block;
+                if (!shape.blocks_per_sm) shape.blocks_per_sm = def.blocks_per_sm;
+            }
+            tuning_json = format("{\"tuned\": %s, \"source\": \"%s\", \"key\": \"%s\", \"shape\": %s}",
+                                 hit ? "true" : "false", hit ? "cache" : "default (no cache entry)", key.c_str(),
+                                 shape_json(shape).c_str());
+            return;
+        }
+        // measure
+        if (death_or_birth) {  // trials would move populations: keep the defaults
+            tuning_json = format("{\"tuned\": false, \"source\": \"default (birth/death model)\", \"key\": \"%s\", \"shape\": %s}",
+                                 key.c_str(), shape_json(shape).c_str());
+            return;
+        }
+        const Snapshot sn = snapshot();
+        std::vector<Shape> cand;
+        for (uint32_t block : {64u, 128u})
+            for (uint32_t bps : {4u, 8u, 16u, 32u})
+                for (uint32_t stage : {0u, def.stage_bytes})
+                    for (uint32_t wide : {0u, 1u << 30}) {
+                        Shape h;
+                        h.block = block;
+                        h.blocks_per_sm = bps;
+                        h.stage_bytes = stage;
+                        h.scan_wide_min = wide;
+                        cand.push_back(h);
+                    }
+        const double def_ms = time_shape(def, sn, 3);
+        double best_ms = def_ms;
+        Shape best = def;
+        std::string trials;
+        for (const Shape& h : cand) {
+            const double ms = time_shape(h, sn, 3);
+            trials += format("%s[%u, %u, %u, %u, %.4f]", trials.empty() ? "" : ", ", h.block, h.blocks_per_sm,
+                             h.stage_bytes, h.scan_wide_min, ms);
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = h;
+            }
+        }
+        // the winner again, against the defaults, to confirm it (noise)
+        const double again = time_shape(best, sn, 3);
+        const double def_again = time_shape(def, sn, 3);
+        if (again > def_again) {
+            best = def;
+            best_ms = def_again;
+        } else {
+            best_ms = again;
+        }
+        restore(sn);
+        for (void* p : sn.cols) mem.release(p);
+        drop_graphs();
+        shape = best;
+        tuning_json = format("{\"tuned\": true, \"source\": \"measured\", \"key\": \"%s\", \"shape\": %s, "
+                             "\"step_ms\": %.4f, \"default_step_ms\": %.4f, \"trials\": "
+                             "\"[block, blocks_per_sm, stage_bytes, scan_wide_min, ms]: %s\"}",
+                             key.c_str(), shape_json(best).c_str(), best_ms, def_again, trials.c_str());
+        if (path.empty()) return;
+        // store: the file's other entries kept, this size class replaced
+        std::vector<std::pair<std::string, std::string>> keep;
+        if (entries)
+            for (const auto& e : entries->fields) {
+                if (e.first == key) continue;
+                std::string body;
+                for (const auto& f : e.second.fields)
+                    body += format("%s\"%s\": %s", body.empty() ? "" : ", ", f.first.c_str(),
+                                   f.second.kind == json::Value::String ? ("\"" + f.second.text + "\"").c_str()
+                                                                        : f.second.text.c_str());
+                keep.emplace_back(e.first, "{" + body + "}");
+            }
+        keep.emplace_back(key, format("{\"block\": %u, \"blocks_per_sm\": %u, \"stage_bytes\": %u, "
+                                      "\"scan_wide_min\": %u, \"step_ms\": %.4f, \"default_step_ms\": %.4f}",
+                                      best.block, best.blocks_per_sm, best.stage_bytes, best.scan_wide_min, best_ms,
+                                      def_again));
+        if (std::FILE* f = std::fopen(path.c_str(), "wb")) {
+            std::fprintf(f, "{\n  \"about\": \"launch shapes of batched ensemble steps, measured by CUDAEnsemble's "
+                            "autotuner (tuning = 2) per GPU, model and size class\",\n  \"entries\": {\n");
+            for (size_t i = 0; i < keep.size(); ++i)
+                std::fprintf(f, "    \"%s\": %s%s\n", keep[i].first.c_str(), keep[i].second.c_str(),
+                             i + 1 < keep.size() ? "," : "");
+            std::fprintf(f, "  }\n}\n");
+            std::fclose(f);
+        }
+    }
+
     // Runs every plan to its step count; fills results[k].
     void run(std::vector<std::shared_ptr<AgentVector>>& results) {
         unsigned int max_steps = 0;
@@ -835,36 +1082,7 @@ struct BatchedSim {
         FG_ECUDA(cudaEventCreate(&t_end));
         FG_ECUDA(cudaEventRecord(t_begin, stream));
         for (unsigned int s = 0; s < max_steps; ++s) {
-            prepare_capacity(s);
-            if (cfg.use_graphs) {
-                const auto key = std::make_pair(parity, sorts_at(s));
-                auto it = cache.find(key);
-                if (it == cache.end()) {
-                    cudaGraph_t g;
-                    FG_ECUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-                    try {
-                        enqueue_step(s);
-                    } catch (...) {
-                        cudaStreamEndCapture(stream, &g);
-                        throw;
-                    }
-                    FG_ECUDA(cudaStreamEndCapture(stream, &g));
-                    cudaGraphExec_t ge;
-                    FG_ECUDA(cudaGraphInstantiate(&ge, g, 0));
-                    cudaGraphDestroy(g);
-                    it = cache.emplace(key, ge).first;
-                } else {
-                    if (flips_at(s) & 1) parity ^= 1;
-                    for (const auto& b : fns)
-                        if (b.births)
-                            for (uint32_t k = 0; k < ninst; ++k) bound[k] = std::min<uint64_t>(bound[k] * 2, 1ull << 33);
-                }
-                FG_ECUDA(cudaGraphLaunch(it->second, stream));
-                ++graph_launches;
-            } else {
-                enqueue_step(s);
-            }
-            after_step(s);
+            issue_step(s);
             // runs that end here: read them back and drop them from later steps
             bool any = false;
             for (uint32_t k = 0; k < ninst; ++k) any = any || (plans[k].getSteps() == s + 1 && s + 1 < max_steps);
@@ -911,6 +1129,7 @@ struct EnsembleImpl {
     bool batched = false;
     unsigned int kernels_per_step = 0;
     unsigned long long graph_launches = 0;
+    std::string tuning = "{\"tuned\": false}";
     explicit EnsembleImpl(const ModelDescription& d) : desc(d) {}
 };
 
@@ -923,6 +1142,7 @@ CUDAEnsemble::EnsembleConfig& CUDAEnsemble::Config() { return impl->cfg; }
 double CUDAEnsemble::getEnsembleElapsedTime() const { return impl->elapsed; }
 double CUDAEnsemble::getEnsembleStepTime() const { return impl->step_seconds; }
 bool CUDAEnsemble::lastRunBatched() const { return impl->batched; }
+const std::string& CUDAEnsemble::getTuning() const { return impl->tuning; }
 unsigned int CUDAEnsemble::getKernelsPerStep() const { return impl->kernels_per_step; }
 unsigned long long CUDAEnsemble::getGraphLaunches() const { return impl->graph_launches; }
 
@@ -938,6 +1158,8 @@ unsigned int CUDAEnsemble::simulate(const RunPlanVector& plans) {
     if (impl->batched) {
         detail::BatchedSim b(model, plans, impl->cfg);
         b.setup();
+        if (impl->cfg.tuning == 1 || impl->cfg.tuning == 2) b.autotune(impl->cfg.tuning, impl->cfg.tuning_cache);
+        impl->tuning = b.tuning_json;
         std::vector<std::shared_ptr<AgentVector>> res;
         b.run(res);
         const auto key = std::make_pair(model->agents[0]->name, model->agents[0]->states[0]);

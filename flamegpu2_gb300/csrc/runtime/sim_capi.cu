@@ -477,6 +477,24 @@ extern "C" int fge_stats(fge_ensemble* e, double* el, int32_t* batched, uint32_t
     });
 }
 
+extern "C" int fge_set_tuning(fge_ensemble* e, int32_t mode, const char* cache_path) {
+    return guarded([&] {
+        if (mode < 0 || mode > 2) THROW flamegpu::exception::InvalidArgument("tuning mode must be 0, 1 or 2");
+        e->ens->Config().tuning = mode;
+        e->ens->Config().tuning_cache = cache_path ? cache_path : "";
+    });
+}
+
+extern "C" int fge_tuning(fge_ensemble* e, char* json, size_t len) {
+    return guarded([&] {
+        const std::string& t = e->ens->getTuning();
+        if (json && len) {
+            std::strncpy(json, t.c_str(), len - 1);
+            json[len - 1] = 0;
+        }
+    });
+}
+
 extern "C" int fge_step_time(fge_ensemble* e, double* seconds) {
     return guarded([&] { *seconds = e->ens->getEnsembleStepTime(); });
 }

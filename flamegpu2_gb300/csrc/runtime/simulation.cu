@@ -1165,13 +1165,28 @@ struct SimulationImpl {
         r = std::max<uint64_t>(r, 8ull * static_cast<uint64_t>(sms) * kAgentBlock);
         return static_cast<uint32_t>(std::min<uint64_t>(r, std::max(l.capacity, 1u)));
     }
-    unsigned int agent_grid(uint32_t rows) const {
-        return std::min(std::max(1u, (rows + kAgentBlock - 1) / kAgentBlock), 1u << 16);
+    // Threads per agent-function block: CUDAConfig::agent_block if set (32,
+    // 64 or 128), else 128; FLAMEGPU_AGENT_BLOCK overrides it. Measured on
+    // the 16,384-agent Boids step (one block per SM or fewer): 64 threads ran
+    // as fast as 128 and 32 a third slower, since each agent's walk over its
+    // neighbourhood, not the number of SMs taking part, sets the time.
+    unsigned int agent_block(uint32_t) const {
+        static const unsigned int env = [] {
+            const char* e = std::getenv("FLAMEGPU_AGENT_BLOCK");
+            const unsigned int v = e ? static_cast<unsigned int>(std::atoi(e)) : 0u;
+            return (v == 32u || v == 64u || v == 128u) ? v : 0u;
+        }();
+        if (env) return env;
+        const unsigned int c = cuda_config.agent_block;
+        return (c == 32u || c == 64u || c == 128u) ? c : kAgentBlock;
+    }
+    unsigned int agent_grid(uint32_t rows, unsigned int block) const {
+        return std::min(std::max(1u, (rows + block - 1) / block), 1u << 17);
     }
 
-    static bool stage_window_fits(const MsgList& m, unsigned int stage_bytes) {
+    static bool stage_window_fits(const MsgList& m, unsigned int stage_bytes, unsigned int block) {
         const double per_bin = static_cast<double>(m.capacity) / std::max<uint32_t>(m.grid.binCount, 1u);
-        return detail::stage_window_fits(m.grid, per_bin, m.record_words, kAgentBlock, stage_bytes);
+        return detail::stage_window_fits(m.grid, per_bin, m.record_words, block, stage_bytes);
     }
 
     void enqueue_function(FnRt& f) {
@@ -1215,7 +1230,8 @@ struct SimulationImpl {
             C.env = d_env;
             cudaError_t ce = cudaSuccess;
             timed("cond:" + f.fn->name, [&] {
-                ce = f.fn->condition(C, agent_grid(grid_rows(l) + 1), kAgentBlock, 0, stream, detail::pdl_enabled());
+                ce = f.fn->condition(C, agent_grid(grid_rows(l) + 1, kAgentBlock), kAgentBlock, 0, stream,
+                                     detail::pdl_enabled());
             });
             if (ce != cudaSuccess)
                 THROW exception::CUDAError(format("Launch of the condition of '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(ce)));
@@ -1254,7 +1270,7 @@ struct SimulationImpl {
                 P.in_pay_stride = f.in->pay_stride;
                 P.in_pbm_alloc = f.in->pbm_alloc;
                 if (f.stage && cuda_config.message_stage_bytes >= 1024u &&
-                    stage_window_fits(*f.in, cuda_config.message_stage_bytes))
+                    stage_window_fits(*f.in, cuda_config.message_stage_bytes, agent_block(grid_rows(l))))
                     P.stage_bytes = (cuda_config.message_stage_bytes + 15u) & ~15u;
             } else {
                 P.in_count = f.in->optional_any ? f.in->bf_count : f.in->d_count;
@@ -1276,7 +1292,8 @@ struct SimulationImpl {
         // kernels of other simulations on the device (a server's other runs,
         // higher-priority streams) get SMs between them
         timed("fn:" + f.fn->name, [&] {
-            e = f.fn->launcher(P, agent_grid(grid_rows(l)), kAgentBlock, smem, stream, detail::pdl_enabled());
+            const unsigned int block = agent_block(grid_rows(l));
+            e = f.fn->launcher(P, agent_grid(grid_rows(l), block), block, smem, stream, detail::pdl_enabled());
         });
         if (e != cudaSuccess)
             THROW exception::CUDAError(format("Launch of agent function '%s' failed: %s", f.fn->name.c_str(), cudaGetErrorString(e)));

@@ -259,7 +259,8 @@ class Simulation:
 
 
 ENSEMBLE_EXPORTS = ["fge_create", "fge_destroy", "fge_configure", "fge_add_run", "fge_set_run_property",
-                    "fge_simulate", "fge_get_count", "fge_get_variable", "fge_stats", "fge_step_time"]
+                    "fge_simulate", "fge_get_count", "fge_get_variable", "fge_stats", "fge_step_time",
+                    "fge_set_tuning", "fge_tuning"]
 _ens_ready = False
 
 
@@ -272,6 +273,8 @@ def _ens():
         L.fge_create.restype = vp
         L.fge_destroy.argtypes = [vp]
         L.fge_configure.argtypes = [vp, i32, i32, u32]
+        L.fge_set_tuning.argtypes = [vp, i32, C.c_char_p]
+        L.fge_tuning.argtypes = [vp, C.c_char_p, sz]
         L.fge_add_run.argtypes = [vp, u32, C.c_uint64, C.c_char_p, u32, i32, C.POINTER(C.c_char_p), C.POINTER(vp),
                                   C.c_char_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float]
         L.fge_set_run_property.argtypes = [vp, u32, C.c_char_p, vp, sz]
@@ -284,18 +287,34 @@ def _ens():
     return L
 
 
+# Launch shapes of batched ensemble steps measured on GB300 (CUDAEnsemble's autotuner).
+TUNING_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning", "ensemble_shapes.json")
+
+
 class Ensemble:
     """CUDAEnsemble of a registered model: runs are added, then simulated together."""
 
     def __init__(self, model: str, params=(), device: int = 0, batched: bool = True, use_graphs: bool = True,
-                 stage_bytes: int = 96 * 1024):
+                 stage_bytes: int = 96 * 1024, tuning: str = "off", tuning_cache: str = TUNING_CACHE):
+        """tuning: "off" (fixed launch shapes), "cache" (the shape tuning_cache
+        holds for this GPU, model and size class) or "measure" (time every
+        candidate on the batch and write the fastest to tuning_cache)."""
         L = _ens()
         arr = (C.c_double * max(1, len(params)))(*[float(p) for p in params])
         self._h = L.fge_create(model.encode(), arr, len(params), device)
         if not self._h:
             raise SimError(L.fgs_last_error().decode())
         _check(L.fge_configure(self._h, int(batched), int(use_graphs), stage_bytes))
+        mode = {"off": 0, "cache": 1, "measure": 2}[tuning]
+        _check(L.fge_set_tuning(self._h, mode, tuning_cache.encode() if tuning_cache else None))
         self.runs = 0
+
+    def tuning(self) -> dict:
+        """The launch shape of the last batched simulate() and where it came from."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        _check(_ens().fge_tuning(self._h, buf, 1 << 16))
+        return json.loads(buf.value.decode())
 
     def close(self):
         if getattr(self, "_h", None):

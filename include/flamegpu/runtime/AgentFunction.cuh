@@ -221,10 +221,14 @@ inline unsigned int device_sm_count() {
     return n;
 }
 
+// block: 32, 64 or 128 threads (kAgentBlock divides into whole blocks). A
+// launch of at most one 128-thread block's worth of threads per SM takes the
+// variant compiled without a register cap: its blocks fit the SMs anyway.
 template <typename F>
 cudaError_t launch_agent_function(const LaunchParams& p, unsigned int grid, unsigned int block, unsigned int smem,
                                   cudaStream_t stream, bool pdl) {
-    if (grid <= device_sm_count()) return launch_agent_variant<F, 1>(p, grid, block, smem, stream, pdl);
+    if (static_cast<uint64_t>(grid) * block <= static_cast<uint64_t>(device_sm_count()) * kAgentBlock)
+        return launch_agent_variant<F, 1>(p, grid, block, smem, stream, pdl);
     return launch_agent_variant<F, FLAMEGPU_AGENT_MIN_BLOCKS>(p, grid, block, smem, stream, pdl);
 }
 #endif

@@ -95,6 +95,15 @@ class CUDAEnsemble {
         bool use_graphs = true;
         unsigned int message_stage_bytes = 96u * 1024u;
         bool timing = false;
+        // Launch shapes of the batched step (threads per agent block, blocks
+        // per SM, staging bytes, the scans' wide-tile threshold): 0 the fixed
+        // defaults; 1 the entry of tuning_cache for this GPU, model and size
+        // class (defaults if it has none); 2 measured now, every candidate
+        // timed by CUDA events on the batch's own step graph, the fastest
+        // kept and written to tuning_cache. The reference picks one block size
+        // per launch by occupancy (CUDASimulation.cu:988). GB300 extension.
+        int tuning = 0;
+        std::string tuning_cache;
     };
     explicit CUDAEnsemble(const ModelDescription& model, int argc = 0, const char** argv = nullptr);
     ~CUDAEnsemble();
@@ -109,6 +118,9 @@ class CUDAEnsemble {
     double getEnsembleStepTime() const;
     /** True if the last simulate() ran as one batched simulation. */
     bool lastRunBatched() const;
+    /** The launch shape the last batched simulate() used and where it came
+     *  from, as JSON ({"tuned", "source", "key", "shape", ...}). */
+    const std::string& getTuning() const;
     /** Final population of one run (GB300 extension; the reference reports through logs). */
     void getPopulationData(unsigned int run, AgentVector& population, const std::string& state = "default") const;
     /** The same population without a copy (valid until the next simulate()). */

@@ -100,6 +100,10 @@ class CUDASimulation {
         // Priority of the simulation's streams (cudaStreamCreateWithPriority: a
         // lower number runs first when kernels of several streams are waiting).
         int stream_priority = 0;
+        // Threads per agent-function block: 32, 64 or 128 (0: 128). The
+        // reference picks a block size per launch with
+        // cudaOccupancyMaxPotentialBlockSize (CUDASimulation.cu:988).
+        unsigned int agent_block = 0;
     };
 
     explicit CUDASimulation(const ModelDescription& model, int argc = 0, const char** argv = nullptr);

@@ -309,6 +309,18 @@ int fg_compact_agents_batched(const fg_batch_instance* instances, const uint32_t
                               uint32_t ncols, int32_t id_col, uint32_t* next_ids, void* workspace,
                               size_t workspace_bytes, void* stream);
 
+/* Launch-shape settings of the calling thread's later scan, build and sort
+ * calls: a tuner's knobs (fg_set_thread_tuning(NULL) restores the defaults).
+ * scan_wide_min: scans of more values than this take tiles of four 4,096-value
+ * sub-tiles, which need a quarter of the look-back rounds (0: the default,
+ * 4,194,304; otherwise at least 4,096). No counterpart in the reference (CUB
+ * picks its tile shapes at compile time). */
+typedef struct fg_tuning {
+    uint32_t scan_wide_min;
+    uint32_t reserved[3];
+} fg_tuning;
+int fg_set_thread_tuning(const fg_tuning* t);
+
 /* Last CUDA error seen by this library on the calling thread (cudaError_t). */
 int fg_last_cuda_error(void);
 /* Library version string. */

@@ -120,6 +120,11 @@ int fge_stats(fge_ensemble* e, double* elapsed_s, int32_t* batched, uint32_t* ke
               uint64_t* graph_launches);
 /* Device seconds of the last simulate()'s steps (CUDAEnsemble::getEnsembleStepTime). */
 int fge_step_time(fge_ensemble* e, double* seconds);
+/* Launch-shape tuning of batched steps (CUDAEnsemble::EnsembleConfig::tuning):
+ * 0 fixed defaults, 1 read cache_path, 2 measure and write cache_path. */
+int fge_set_tuning(fge_ensemble* e, int32_t mode, const char* cache_path);
+/* The shape the last simulate() used, as JSON (CUDAEnsemble::getTuning). */
+int fge_tuning(fge_ensemble* e, char* json, size_t len);
 
 /* --------------------------------------------------------------- server
  * flamegpu::SimulationServer (include/flamegpu/simulation/SimulationServer.h;

@@ -131,3 +131,47 @@ def test_batched_birth_death_equals_plain_runs_and_oracle(graphs):
         for v in range(8):
             np.testing.assert_array_equal(got[f"f{v}"], fo[v])
     assert len(out[3]["_id"]) > 3000 * 10  # a run that grew well past its first segment
+
+
+def test_autotuned_ensemble_same_results_and_cache(tmp_path):
+    # the autotuner times launch-shape candidates on the batch itself, keeps the
+    # fastest and stores it per GPU / model / size class; the results do not
+    # depend on the shape (bit-exact against the untuned run), and a second
+    # ensemble of the same size class reads the shape back from the cache
+    import json
+    from flamegpu2_gb300 import sim, synth
+    specs = synth.ensemble_instances(10, seed=300, n_lo=500, n_hi=20000)
+    cache = str(tmp_path / "shapes.json")
+
+    def run(tuning):
+        ens = sim.Ensemble("boids_spatial3d", synth.boids_params(dict(synth.BOIDS_SMALL)), tuning=tuning,
+                           tuning_cache=cache)
+        for sp in specs:
+            pop = synth.boids_population(sp["n"], 0.0, sp["edge"], sp["seed"])
+            r = ens.add_run(4, sp["seed"], "Boid", sp["n"], pop, "location", (0.0, 0.0, 0.0), (sp["edge"],) * 3,
+                            sp["radius"])
+            ens.set_property(r, "MIN_POSITION", 0.0)
+            ens.set_property(r, "MAX_POSITION", sp["edge"])
+            ens.set_property(r, "INTERACTION_RADIUS", sp["radius"])
+        assert ens.simulate() == 0
+        out = [{k: ens.get(i, "Boid", k, np.uint32 if k == "_id" else np.float32) for k in BOIDS_NAMES}
+               for i in range(len(specs))]
+        t = ens.tuning()
+        ens.close()
+        return out, t
+
+    base, t0 = run("off")
+    assert not t0["tuned"]
+    tuned, t1 = run("measure")
+    assert t1["tuned"] and t1["source"] == "measured"
+    assert t1["shape"]["block"] in (64, 128) and t1["step_ms"] <= t1["default_step_ms"]
+    for a, b in zip(base, tuned):
+        for k in BOIDS_NAMES:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    doc = json.load(open(cache))
+    assert t1["key"] in doc["entries"]
+    again, t2 = run("cache")
+    assert t2["tuned"] and t2["source"] == "cache" and t2["shape"] == t1["shape"]
+    for a, b in zip(base, again):
+        for k in BOIDS_NAMES:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
