@@ -213,12 +213,9 @@ extern "C" int fgs_set_environment(fgs_sim* s, const char* name, const void* val
     return guarded([&] {
         const auto* p = find_env(s, name);
         if (bytes != p->value.size()) throw flamegpu::exception::InvalidEnvPropertyType("size mismatch");
+        // the property's bytes, whatever its type (the size was checked)
         flamegpu::HostAPI::Environment e(s->sim->getImpl());
-        if (p->type == std::type_index(typeid(float))) e.setProperty<float>(name, *static_cast<const float*>(value));
-        else if (p->type == std::type_index(typeid(double))) e.setProperty<double>(name, *static_cast<const double*>(value));
-        else if (p->type == std::type_index(typeid(int32_t))) e.setProperty<int32_t>(name, *static_cast<const int32_t*>(value));
-        else if (p->type == std::type_index(typeid(uint32_t))) e.setProperty<uint32_t>(name, *static_cast<const uint32_t*>(value));
-        else throw flamegpu::exception::InvalidEnvPropertyType("unsupported property type for the C ABI");
+        e.setRaw(name, value, bytes);
     });
 }
 
@@ -226,12 +223,7 @@ extern "C" int fgs_get_environment(fgs_sim* s, const char* name, void* value, si
     return guarded([&] {
         const auto* p = find_env(s, name);
         if (bytes != p->value.size()) throw flamegpu::exception::InvalidEnvPropertyType("size mismatch");
-        flamegpu::HostAPI::Environment e(s->sim->getImpl());
-        if (p->type == std::type_index(typeid(float))) *static_cast<float*>(value) = e.getProperty<float>(name);
-        else if (p->type == std::type_index(typeid(double))) *static_cast<double*>(value) = e.getProperty<double>(name);
-        else if (p->type == std::type_index(typeid(int32_t))) *static_cast<int32_t*>(value) = e.getProperty<int32_t>(name);
-        else if (p->type == std::type_index(typeid(uint32_t))) *static_cast<uint32_t*>(value) = e.getProperty<uint32_t>(name);
-        else throw flamegpu::exception::InvalidEnvPropertyType("unsupported property type for the C ABI");
+        s->sim->getEnvironmentRaw(name, value, bytes);
     });
 }
 
@@ -351,6 +343,54 @@ extern "C" int fgs_run_log(fgs_sim* s, char* buf, size_t len, size_t* needed) {
 }
 
 extern "C" int fgs_load_state(fgs_sim* s, const char* path) { return guarded([&] { s->sim->loadState(path); }); }
+
+// SimulationConfig() / CUDAConfig() items by name, as text (the settings a state
+// file carries: the reference's Simulation::Config and CUDASimulation::Config)
+extern "C" int fgs_set_config(fgs_sim* s, const char* key, const char* value) {
+    return guarded([&] {
+        auto& c = s->sim->SimulationConfig();
+        auto& g = s->sim->CUDAConfig();
+        const std::string k = key, v = value ? value : "";
+        auto flag = [&] { return v == "1" || v == "true"; };
+        if (k == "input_file") c.input_file = v;
+        else if (k == "step_log_file") c.step_log_file = v;
+        else if (k == "exit_log_file") c.exit_log_file = v;
+        else if (k == "common_log_file") c.common_log_file = v;
+        else if (k == "truncate_log_files") c.truncate_log_files = flag();
+        else if (k == "random_seed") c.random_seed = std::strtoull(v.c_str(), nullptr, 10);
+        else if (k == "steps") c.steps = static_cast<unsigned int>(std::strtoul(v.c_str(), nullptr, 10));
+        else if (k == "verbosity") c.verbosity = static_cast<unsigned int>(std::strtoul(v.c_str(), nullptr, 10));
+        else if (k == "timing") c.timing = flag();
+        else if (k == "device_id") g.device_id = std::atoi(v.c_str());
+        else if (k == "inLayerConcurrency") g.inLayerConcurrency = flag();
+        else THROW flamegpu::exception::InvalidArgument(flamegpu::exception::format("No config item '%s'", key));
+    });
+}
+
+extern "C" int fgs_get_config(fgs_sim* s, const char* key, char* out, size_t len) {
+    return guarded([&] {
+        const auto& c = s->sim->SimulationConfig();
+        const auto& g = s->sim->CUDAConfig();
+        const std::string k = key;
+        std::string v;
+        if (k == "input_file") v = c.input_file;
+        else if (k == "step_log_file") v = c.step_log_file;
+        else if (k == "exit_log_file") v = c.exit_log_file;
+        else if (k == "common_log_file") v = c.common_log_file;
+        else if (k == "truncate_log_files") v = c.truncate_log_files ? "true" : "false";
+        else if (k == "random_seed") v = std::to_string(c.random_seed);
+        else if (k == "steps") v = std::to_string(c.steps);
+        else if (k == "verbosity") v = std::to_string(c.verbosity);
+        else if (k == "timing") v = c.timing ? "true" : "false";
+        else if (k == "device_id") v = std::to_string(g.device_id);
+        else if (k == "inLayerConcurrency") v = g.inLayerConcurrency ? "true" : "false";
+        else THROW flamegpu::exception::InvalidArgument(flamegpu::exception::format("No config item '%s'", key));
+        if (out && len) {
+            std::strncpy(out, v.c_str(), len - 1);
+            out[len - 1] = 0;
+        }
+    });
+}
 
 extern "C" int fgs_take_profile(fgs_sim* s, char* buf, size_t len) {
     return guarded([&] {

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
+#include <limits>
 #include <mutex>
 #include <chrono>
 #include <cstdio>
@@ -1776,6 +1778,10 @@ namespace {
 // read back the same value).
 std::string number_text(std::type_index t, const char* p) {
     char buf[64];
+    // JSON has no NaN or infinity: they are written as null, as the reference's
+    // writer (nlohmann::json) does, and read back as NaN
+    if (t == std::type_index(typeid(float)) && !std::isfinite(*reinterpret_cast<const float*>(p))) return "null";
+    if (t == std::type_index(typeid(double)) && !std::isfinite(*reinterpret_cast<const double*>(p))) return "null";
     if (t == std::type_index(typeid(float))) std::snprintf(buf, sizeof(buf), "%.9g", static_cast<double>(*reinterpret_cast<const float*>(p)));
     else if (t == std::type_index(typeid(double))) std::snprintf(buf, sizeof(buf), "%.17g", *reinterpret_cast<const double*>(p));
     else if (t == std::type_index(typeid(int64_t))) std::snprintf(buf, sizeof(buf), "%lld", static_cast<long long>(*reinterpret_cast<const int64_t*>(p)));
@@ -1791,7 +1797,15 @@ std::string number_text(std::type_index t, const char* p) {
 }
 
 void number_value(std::type_index t, const detail::json::Value& v, char* p) {
-    if (v.kind != detail::json::Value::Number) THROW exception::InvalidArgument("State file: a number was expected");
+    if (v.kind == detail::json::Value::Null && t == std::type_index(typeid(float))) {
+        *reinterpret_cast<float*>(p) = std::numeric_limits<float>::quiet_NaN();
+        return;
+    }
+    if (v.kind == detail::json::Value::Null && t == std::type_index(typeid(double))) {
+        *reinterpret_cast<double*>(p) = std::numeric_limits<double>::quiet_NaN();
+        return;
+    }
+    if (v.kind != detail::json::Value::Number) THROW exception::JSONError("State file: a number was expected");
     if (t == std::type_index(typeid(float))) *reinterpret_cast<float*>(p) = std::strtof(v.text.c_str(), nullptr);
     else if (t == std::type_index(typeid(double))) *reinterpret_cast<double*>(p) = v.number();
     else if (t == std::type_index(typeid(int64_t))) *reinterpret_cast<int64_t*>(p) = v.integer();
@@ -1802,7 +1816,7 @@ void number_value(std::type_index t, const detail::json::Value& v, char* p) {
     else if (t == std::type_index(typeid(uint16_t))) *reinterpret_cast<uint16_t*>(p) = static_cast<uint16_t>(v.uinteger());
     else if (t == std::type_index(typeid(int8_t))) *reinterpret_cast<int8_t*>(p) = static_cast<int8_t>(v.integer());
     else if (t == std::type_index(typeid(uint8_t))) *reinterpret_cast<uint8_t*>(p) = static_cast<uint8_t>(v.uinteger());
-    else THROW exception::InvalidArgument("State files: unsupported variable type");
+    else THROW exception::JSONError("State files: unsupported variable type");
 }
 
 // a scalar, or an array of `elements` values
@@ -1823,7 +1837,7 @@ void read_elements(const detail::json::Value& v, std::type_index t, uint32_t siz
         return;
     }
     if (v.kind != detail::json::Value::Array || v.items.size() != elements)
-        THROW exception::InvalidArgument(format("State file: '%s' should be an array of %u values", what.c_str(), elements));
+        THROW exception::JSONError(format("State file: '%s' should be an array of %u values", what.c_str(), elements));
     for (uint32_t e = 0; e < elements; ++e) number_value(t, v.items[e], p + static_cast<size_t>(e) * size);
 }
 
@@ -1840,12 +1854,27 @@ void CUDASimulation::exportData(const std::string& path) {
     w.begin_object();
     w.key("config");
     w.begin_object();
-    w.key("simulation");
+    w.key("simulation");  // the keys and order of JSONStateWriter::writeConfig (:55-77)
     w.begin_object();
+    const auto& sc = impl->config;
+    w.key("input_file");
+    w.string(sc.input_file);
+    w.key("step_log_file");
+    w.string(sc.step_log_file);
+    w.key("exit_log_file");
+    w.string(sc.exit_log_file);
+    w.key("common_log_file");
+    w.string(sc.common_log_file);
+    w.key("truncate_log_files");
+    w.raw(sc.truncate_log_files ? "true" : "false");
     w.key("random_seed");
-    w.raw(std::to_string(impl->config.random_seed));
+    w.raw(std::to_string(sc.random_seed));
     w.key("steps");
-    w.raw(std::to_string(impl->config.steps));
+    w.raw(std::to_string(sc.steps));
+    w.key("verbosity");
+    w.raw(std::to_string(sc.verbosity));
+    w.key("timing");
+    w.raw(sc.timing ? "true" : "false");
     w.end_object();
     w.key("cuda");
     w.begin_object();
@@ -1859,18 +1888,17 @@ void CUDASimulation::exportData(const std::string& path) {
     w.begin_object();
     w.key("step_count");
     w.raw(std::to_string(impl->step_count));
-    // GB300 extension: each agent type's next id, so a run resumed from this
-    // file gives births the ids the uninterrupted run would have
+    // GB300 extension: each agent type's next id ("next_id:<agent>"), so a run
+    // resumed from this file gives births the ids the uninterrupted run would
+    // have. Plain numbers: the reference's reader skips the values of "stats"
+    // it does not know (JSONStateReader.cu:203-205), but not nested objects.
     {
         std::vector<uint32_t> next(m.agents.size(), 1u);
         FG_CUDA(cudaMemcpy(next.data(), impl->d_next_id(0), sizeof(uint32_t) * next.size(), cudaMemcpyDeviceToHost));
-        w.key("next_id");
-        w.begin_object();
         for (size_t i = 0; i < m.agents.size(); ++i) {
-            w.key(m.agents[i]->name);
+            w.key("next_id:" + m.agents[i]->name);
             w.raw(std::to_string(next[i]));
         }
-        w.end_object();
     }
     w.end_object();
     if (!m.environment.empty()) {
@@ -1938,9 +1966,30 @@ void CUDASimulation::loadState(const std::string& path) {
     }
     auto& m = *impl->model;
     if (const auto* cfg = doc.find("config")) {
+        // JSONStateReader.cu:385-416: the known simulation and CUDA items are
+        // applied (input_file is not followed), any other is an error
         if (const auto* sc = cfg->find("simulation")) {
-            if (const auto* v = sc->find("random_seed")) impl->config.random_seed = v->uinteger();
-            if (const auto* v = sc->find("steps")) impl->config.steps = static_cast<unsigned int>(v->uinteger());
+            auto& c = impl->config;
+            for (const auto& kv : sc->fields) {
+                const std::string& k = kv.first;
+                const auto& v = kv.second;
+                if (k == "random_seed") c.random_seed = v.uinteger();
+                else if (k == "steps") c.steps = static_cast<unsigned int>(v.uinteger());
+                else if (k == "timing") c.timing = v.kind == detail::json::Value::Bool ? v.b : v.integer() != 0;
+                else if (k == "truncate_log_files") c.truncate_log_files = v.kind == detail::json::Value::Bool ? v.b : v.integer() != 0;
+                else if (k == "verbosity") c.verbosity = static_cast<unsigned int>(v.uinteger());
+                else if (k == "step_log_file") c.step_log_file = v.text;
+                else if (k == "exit_log_file") c.exit_log_file = v.text;
+                else if (k == "common_log_file") c.common_log_file = v.text;
+                else if (k == "input_file" || k == "console_mode") continue;
+                else THROW exception::JSONError(format("Unexpected simulation config item '%s' in input file '%s'", k.c_str(), path.c_str()));
+            }
+        }
+        if (const auto* cc = cfg->find("cuda")) {
+            for (const auto& kv : cc->fields) {
+                if (kv.first == "device_id" || kv.first == "inLayerConcurrency") continue;  // kept as configured
+                THROW exception::JSONError(format("Unexpected CUDA config item '%s' in input file '%s'", kv.first.c_str(), path.c_str()));
+            }
         }
     }
     if (const auto* env = doc.find("environment")) {
@@ -1958,7 +2007,7 @@ void CUDASimulation::loadState(const std::string& path) {
             const detail::AgentData* a = nullptr;
             for (const auto& x : m.agents)
                 if (x->name == ak.first) a = x.get();
-            if (!a) THROW exception::InvalidAgentName(format("State file: the model has no agent '%s'", ak.first.c_str()));
+            if (!a) THROW exception::JSONError(format("State file: the model has no agent '%s'", ak.first.c_str()));
             for (const auto& sk : ak.second.fields) {
                 const auto& rows = sk.second.items;
                 AgentVector pop(AgentDescription(impl->model, const_cast<detail::AgentData*>(a)),
@@ -1981,15 +2030,14 @@ void CUDASimulation::loadState(const std::string& path) {
             const uint32_t v = impl->step_count;
             FG_CUDA(cudaMemcpy(impl->d_step(), &v, sizeof(uint32_t), cudaMemcpyHostToDevice));
         }
-        if (const auto* ni = stats->find("next_id"))
-            for (const auto& kv : ni->fields)
-                for (size_t i = 0; i < m.agents.size(); ++i)
-                    if (m.agents[i]->name == kv.first) {
-                        uint32_t cur = 1;
-                        FG_CUDA(cudaMemcpy(&cur, impl->d_next_id(i), sizeof(uint32_t), cudaMemcpyDeviceToHost));
-                        const uint32_t want = std::max(cur, static_cast<uint32_t>(kv.second.uinteger()));
-                        FG_CUDA(cudaMemcpy(impl->d_next_id(i), &want, sizeof(uint32_t), cudaMemcpyHostToDevice));
-                    }
+        for (const auto& kv : stats->fields)
+            for (size_t i = 0; i < m.agents.size(); ++i)
+                if (kv.first == "next_id:" + m.agents[i]->name) {
+                    uint32_t cur = 1;
+                    FG_CUDA(cudaMemcpy(&cur, impl->d_next_id(i), sizeof(uint32_t), cudaMemcpyDeviceToHost));
+                    const uint32_t want = std::max(cur, static_cast<uint32_t>(kv.second.uinteger()));
+                    FG_CUDA(cudaMemcpy(impl->d_next_id(i), &want, sizeof(uint32_t), cudaMemcpyHostToDevice));
+                }
     }
     impl->upload_env_if_dirty();
 }
@@ -2021,6 +2069,19 @@ void CUDASimulation::setPopulationData(AgentVector& pop, const std::string& stat
     {
         const size_t idc = pop.columnIndex("_id");
         id_t* ids = reinterpret_cast<id_t*>(pop.columns()[idc].data());
+        // CUDAAgent::validateIDCollisions (CUDAAgent.cu:196-245): set ids must be unique
+        {
+            std::vector<id_t> set_ids;
+            set_ids.reserve(n);
+            for (uint32_t i = 0; i < n; ++i)
+                if (ids[i] != ID_NOT_SET) set_ids.push_back(ids[i]);
+            std::sort(set_ids.begin(), set_ids.end());
+            unsigned int dup = 0;
+            for (size_t i = 1; i < set_ids.size(); ++i) dup += set_ids[i] == set_ids[i - 1] ? 1u : 0u;
+            if (dup)
+                THROW exception::AgentIDCollision(format("%u agents of type '%s' share an ID with another agent of the same type",
+                                                         dup, l->agent->name.c_str()));
+        }
         id_t mx = 0;
         for (uint32_t i = 0; i < n; ++i) mx = std::max(mx, ids[i]);
         uint32_t next = std::max<uint32_t>(dev_next, mx + 1);

@@ -22,7 +22,8 @@ SIM_EXPORTS = [
     "fgs_get_variable_device", "fgs_step", "fgs_simulate", "fgs_synchronize", "fgs_set_environment",
     "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
     "fgs_set_stage_bytes", "fgs_reset_population_device", "fgs_time_ops_in_graphs", "fgs_harvest_profile",
-    "fgs_export", "fgs_load_state", "fgs_set_log", "fgs_run_log", "fgs_agent_steps",
+    "fgs_export", "fgs_load_state", "fgs_set_log", "fgs_run_log", "fgs_agent_steps", "fgs_set_config",
+    "fgs_get_config",
 ]
 
 _lock = threading.Lock()
@@ -57,6 +58,8 @@ def core():
             L.fgs_get_variable_device.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, vp, sz]
             L.fgs_step.argtypes = [vp, u32]
             L.fgs_agent_steps.argtypes = [vp, C.POINTER(C.c_uint64)]
+            L.fgs_set_config.argtypes = [vp, C.c_char_p, C.c_char_p]
+            L.fgs_get_config.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_size_t]
             L.fgs_simulate.argtypes = [vp]
             L.fgs_synchronize.argtypes = [vp]
             L.fgs_set_environment.argtypes = [vp, C.c_char_p, vp, sz]
@@ -174,6 +177,16 @@ class Simulation:
 
     def step(self, n: int = 1):
         _check(core().fgs_step(self._h, n))
+
+    def set_config(self, key: str, value):
+        """SimulationConfig() / CUDAConfig() item by name."""
+        v = ("true" if value else "false") if isinstance(value, bool) else str(value)
+        _check(core().fgs_set_config(self._h, key.encode(), v.encode()))
+
+    def get_config(self, key: str) -> str:
+        buf = C.create_string_buffer(4096)
+        _check(core().fgs_get_config(self._h, key.encode(), buf, 4096))
+        return buf.value.decode()
 
     def agent_steps(self) -> int:
         """Agents summed over the steps run (each step with the populations that entered it)."""

@@ -51,6 +51,8 @@ FLAMEGPU_DERIVED_EXCEPTION(DeviceError)
 FLAMEGPU_DERIVED_EXCEPTION(EnsembleError)
 FLAMEGPU_DERIVED_EXCEPTION(InvalidConfiguration)
 FLAMEGPU_DERIVED_EXCEPTION(ReservedName)
+FLAMEGPU_DERIVED_EXCEPTION(JSONError)
+FLAMEGPU_DERIVED_EXCEPTION(AgentIDCollision)
 #undef FLAMEGPU_DERIVED_EXCEPTION
 
 inline std::string format(const char* fmt, ...) {

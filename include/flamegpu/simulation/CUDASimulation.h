@@ -77,6 +77,13 @@ class CUDASimulation {
         unsigned int steps = 1;
         uint64_t random_seed = 0;
         std::string input_file;  // state file (JSON) loaded by applyConfig()
+        // kept and written to state files as the reference's Simulation::Config
+        // (include/flamegpu/simulation/Simulation.h:55-63) holds them
+        std::string step_log_file;
+        std::string exit_log_file;
+        std::string common_log_file;
+        bool truncate_log_files = false;
+        unsigned int verbosity = 1;  // Verbosity::Quiet 0, Default 1, Verbose 2
         bool verbose = false;
         bool timing = false;
     };

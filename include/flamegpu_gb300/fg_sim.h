@@ -88,6 +88,12 @@ int fgs_harvest_profile(fgs_sim* sim);
  * layout (config, stats.step_count, environment, agents -> state -> rows). */
 int fgs_export(fgs_sim* sim, const char* path);
 int fgs_load_state(fgs_sim* sim, const char* path);
+/* SimulationConfig() / CUDAConfig() items by name as text (input_file,
+ * step_log_file, exit_log_file, common_log_file, truncate_log_files,
+ * random_seed, steps, verbosity, timing, device_id, inLayerConcurrency): the
+ * settings a state file records. */
+int fgs_set_config(fgs_sim* sim, const char* key, const char* value);
+int fgs_get_config(fgs_sim* sim, const char* key, char* out, size_t len);
 /* Step (exit == 0) or exit (exit != 0) log configuration
  * (CUDASimulation::setStepLog / setExitLog). spec lists entries separated by
  * ';': "count:agent:state", "mean|sd|min|max|sum:agent:state:variable" (the
