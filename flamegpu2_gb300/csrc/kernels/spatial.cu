@@ -57,12 +57,14 @@ __device__ __forceinline__ uint32_t sort_key(const SortGrid& s, int dims, float 
     return flamegpu::detail::spatial_sort_key(s, dims, x, y, z);
 }
 
+// pstride: floats between one row's coordinate and the next row's (1 for
+// separate x, y, z columns; 2 or 3 for a packed "xy" / "xyz" array variable)
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg, uint32_t max_n, const uint32_t* d_n,
                                                   const float* __restrict__ x, const float* __restrict__ y,
                                                   const float* __restrict__ z, const uint32_t* __restrict__ valid,
                                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
-                                                  uint32_t* hist, WsHeader* h) {
+                                                  uint32_t* hist, WsHeader* h, uint32_t pstride) {
     flamegpu::detail::grid_dependency_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         h->long_count = 0;
@@ -76,7 +78,8 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
         const bool act = i < n;
         uint32_t key = kInvalid;
         if (act && (valid == nullptr || valid[i] != 0)) {
-            const float px = x[i], py = y[i], pz = (g.dims == 3) ? z[i] : 0.0f;
+            const size_t e = static_cast<size_t>(i) * pstride;
+            const float px = x[e], py = y[e], pz = (g.dims == 3) ? z[e] : 0.0f;
             key = (MODE == kMessageBin) ? message_bin(g, px, py, pz) : sort_key(sg, g.dims, px, py, pz);
         }
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, key != kInvalid);
@@ -779,7 +782,7 @@ template <int MODE, int EMIT>
 int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets, uint32_t max_n, const uint32_t* d_n,
                  const float* x, const float* y, const float* z, const uint32_t* valid, const EmitParams& rp,
                  uint32_t* pbm_out, const BuildLayout& L, char* ws, cudaStream_t st, const BatchKeys& batch = BatchKeys(),
-                 bool keys_ready = false) {
+                 bool keys_ready = false, uint32_t pos_stride = 1) {
     WsHeader* h = reinterpret_cast<WsHeader*>(ws);
     uint32_t* hist = reinterpret_cast<uint32_t*>(ws + L.hist);
     uint64_t* sstat = reinterpret_cast<uint64_t*>(ws + L.scan_status);
@@ -795,7 +798,7 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
         launch(k_bin_batched<MODE>, grid, kThreads, st, batch.inst, batch.counts, batch.ninst, max_n, batch.dims, x, y, z,
                valid, keys, slot, hist, h);
     } else {
-        launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h);
+        launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h, pos_stride);
     }
     const uint32_t scan_n = nbuckets + 1;
     // an agent sort's buckets (2^bits) run past the grid's cells: its scan stops
@@ -844,7 +847,9 @@ extern "C" int fg_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const 
 
 int fgi_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
                             const float* y, const float* z, const fg_column* cols, uint32_t ncols, uint32_t* perm_out,
-                            void* workspace, size_t workspace_bytes, void* stream, bool keys_ready) {
+                            void* workspace, size_t workspace_bytes, void* stream, bool keys_ready,
+                            uint32_t pos_stride) {
+    if (pos_stride < 1 || pos_stride > 3 || (keys_ready && pos_stride != 1)) return FG_ERR_INVALID_ARGUMENT;
     if (!g || !workspace || (g->dims != 2 && g->dims != 3) || ncols > FG_MAX_COLUMNS) return FG_ERR_INVALID_ARGUMENT;
     if (max_n && (!x || !y || (g->dims == 3 && !z))) return FG_ERR_INVALID_ARGUMENT;
     if (ncols && !cols) return FG_ERR_INVALID_ARGUMENT;
@@ -862,10 +867,10 @@ int fgi_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint
     rp.cp.keep_perm = perm_out != nullptr;
     int rc = ncols ? run_pipeline<kSortKey, kEmitPermColumns>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
                                                               reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st,
-                                                              BatchKeys(), keys_ready)
+                                                              BatchKeys(), keys_ready, pos_stride)
                    : run_pipeline<kSortKey, kEmitPerm>(g, sg, nb, max_n, d_n, x, y, z, nullptr, rp,
                                                        reinterpret_cast<uint32_t*>(ws + L.pbm), L, ws, st,
-                                                       BatchKeys(), keys_ready);
+                                                       BatchKeys(), keys_ready, pos_stride);
     if (rc != FG_OK) return rc;
     const uint32_t* sperm = reinterpret_cast<const uint32_t*>(ws + L.sperm);
     if (perm_out && max_n) {
@@ -878,7 +883,7 @@ extern "C" int fg_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, 
                                       const float* y, const float* z, const fg_column* cols, uint32_t ncols,
                                       uint32_t* perm_out, void* workspace, size_t workspace_bytes, void* stream) {
     return fgi_spatial_sort_agents(g, max_n, d_n, x, y, z, cols, ncols, perm_out, workspace, workspace_bytes, stream,
-                                   false);
+                                   false, 1);
 }
 
 // Where a launch computing the keys of a build (sort_mode false) or an agent

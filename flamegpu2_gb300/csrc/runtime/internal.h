@@ -62,8 +62,11 @@ inline bool stage_window_fits(const fg_spatial_grid& g, double per_bin, uint32_t
 int fgi_spatial_build(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x, const float* y,
                       const float* z, const uint32_t* valid, const fg_record_desc* rec, uint32_t* sorted, uint32_t* pbm,
                       void* workspace, size_t workspace_bytes, void* stream, bool keys_ready);
+// pos_stride: floats from one row's coordinate to the next (1: x, y, z
+// columns; 2 or 3: a packed "xy" / "xyz" array variable, never with keys_ready)
 int fgi_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint32_t* d_n, const float* x,
                             const float* y, const float* z, const fg_column* cols, uint32_t ncols, uint32_t* perm_out,
-                            void* workspace, size_t workspace_bytes, void* stream, bool keys_ready);
+                            void* workspace, size_t workspace_bytes, void* stream, bool keys_ready,
+                            uint32_t pos_stride = 1);
 int fgi_key_target(const fg_spatial_grid* g, uint32_t max_n, bool sort_mode, void* workspace, size_t workspace_bytes,
                    flamegpu::detail::KeyTarget* t);

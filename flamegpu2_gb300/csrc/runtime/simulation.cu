@@ -360,6 +360,7 @@ struct FnRt {
     void* birth_defaults = nullptr;
     std::unique_ptr<FunctionTables> tables[2];  // per buffer parity of the agent list
     bool sort_trigger = false;
+    int pos_var = -1;   // a packed "xyz" / "xy" position variable the sort reads, or -1 (x, y, z)
     bool stage = false;  // spatial input and the agent has float x, y (, z): stage neighbour windows
     uint32_t* cond_fail = nullptr;  // condition result per row (1 = failed), capacity + 1 entries
     uint32_t* d_first = nullptr;    // rows that failed the condition (device)
@@ -562,6 +563,17 @@ struct SimulationImpl {
                     }
                     r.sort_trigger = ok;
                     r.stage = ok;
+                    if (!ok) {  // or a packed position array of the message's dimensions
+                        const char* packed = dims == 3 ? "xyz" : "xy";
+                        for (size_t v = 0; v < a->variables.size(); ++v) {
+                            const Variable& var = a->variables[v];
+                            if (var.name == packed && var.type == std::type_index(typeid(float)) &&
+                                var.elements == static_cast<uint32_t>(dims)) {
+                                r.sort_trigger = true;
+                                r.pos_var = static_cast<int>(v);
+                            }
+                        }
+                    }
                 }
                 fns.push_back(std::move(r));
             }
@@ -1071,7 +1083,7 @@ struct SimulationImpl {
                             const bool do_sort = g.sort_trigger && L->agent->sort_period != 0 &&
                                                  step_count % L->agent->sort_period == 0;
                             const auto lf = last_fn.find(L);
-                            if (do_sort && f->list == L && lf != last_fn.end() && lf->second == f &&
+                            if (do_sort && g.pos_var < 0 && f->list == L && lf != last_fn.end() && lf->second == f &&
                                 !f->fn->has_agent_death && !f->births && !f->end_list) {
                                 f->key_sort = &g;
                                 g.sort_keyed = true;
@@ -1121,12 +1133,22 @@ struct SimulationImpl {
         std::vector<fg_column> cols(l.cols.size());
         for (size_t v = 0; v < l.cols.size(); ++v)
             cols[v] = fg_column{l.cols[v][l.parity], l.cols[v][l.parity ^ 1], l.agent->variables[v].bytes()};
-        const int xi = l.var_index("x"), yi = l.var_index("y"), zi = l.var_index("z");
-        FG_CAPI(fgi_spatial_sort_agents(g, l.capacity, l.d_count, static_cast<const float*>(l.cols[xi][l.parity]),
-                                        static_cast<const float*>(l.cols[yi][l.parity]),
-                                        g->dims == 3 ? static_cast<const float*>(l.cols[zi][l.parity]) : nullptr,
-                                        cols.data(), static_cast<uint32_t>(cols.size()), nullptr, it->second.first,
-                                        it->second.second, stream, f.sort_keyed));
+        const float *px, *py, *pz;
+        uint32_t stride = 1;
+        if (f.pos_var >= 0) {  // packed: row i's coordinates at [dims * i + a]
+            px = static_cast<const float*>(l.cols[f.pos_var][l.parity]);
+            py = px + 1;
+            pz = g->dims == 3 ? px + 2 : nullptr;
+            stride = static_cast<uint32_t>(g->dims);
+        } else {
+            const int xi = l.var_index("x"), yi = l.var_index("y"), zi = l.var_index("z");
+            px = static_cast<const float*>(l.cols[xi][l.parity]);
+            py = static_cast<const float*>(l.cols[yi][l.parity]);
+            pz = g->dims == 3 ? static_cast<const float*>(l.cols[zi][l.parity]) : nullptr;
+        }
+        FG_CAPI(fgi_spatial_sort_agents(g, l.capacity, l.d_count, px, py, pz, cols.data(),
+                                        static_cast<uint32_t>(cols.size()), nullptr, it->second.first,
+                                        it->second.second, stream, f.sort_keyed, stride));
         l.parity ^= 1;
         kernel_counter += f.sort_keyed ? 4 : 5;
     }
