@@ -15,6 +15,7 @@
 
 #include "flamegpu/detail/launch.cuh"
 #include "flamegpu/simulation/CUDASimulation.h"
+#include "flamegpu_gb300/fg_capi.h"
 #include "flamegpu/simulation/LoggingConfig.h"
 
 namespace flamegpu {
@@ -266,13 +267,17 @@ std::string log_number(const LogValue& v, size_t k = 0) {
 }
 
 // a frame as the reference's JSONLogger writes it (src/flamegpu/io/JSONLogger.cu:80-140)
-void write_frame(std::string& o, const LogFrame& f, const char* time_key, double time) {
-    o += "{\"step_index\": " + std::to_string(f.getStepCount());
-    if (time_key) {
+// One frame in JSONLogger::writeLogFrame's layout (src/flamegpu/io/JSONLogger.cu:80-140):
+// its times first (a step frame's step_time; an exit frame's rtc_time,
+// init_time, exit_time and total_time), then step_index, env, agents.
+void write_frame(std::string& o, const LogFrame& f, const std::vector<std::pair<const char*, double>>& times) {
+    o += "{";
+    for (const auto& t : times) {
         char buf[64];
-        std::snprintf(buf, sizeof(buf), "%.17g", time);
-        o += std::string(", \"") + time_key + "\": " + buf;
+        std::snprintf(buf, sizeof(buf), "%.17g", t.second);
+        o += std::string("\"") + t.first + "\": " + buf + ", ";
     }
+    o += "\"step_index\": " + std::to_string(f.getStepCount());
     if (!f.environment.empty()) {
         o += ", \"env\": {";
         bool first = true;
@@ -337,18 +342,40 @@ void write_frame(std::string& o, const LogFrame& f, const char* time_key, double
 
 }  // namespace
 
-std::string CUDASimulation::runLogJSON() const {
-    std::string o = "{\"config\": {\"random_seed\": " + std::to_string(run_log.getRandomSeed()) + "}, \"steps\": [";
+std::string CUDASimulation::runLogJSON(bool with_times) const {
+    // JSONLogger::logCommon (src/flamegpu/io/JSONLogger.cu:179-197): config,
+    // performance_specs (only with the times), steps, exit
+    std::string o = "{\"config\": {\"random_seed\": " + std::to_string(run_log.getRandomSeed()) + "}";
+    if (with_times) {
+        cudaDeviceProp prop{};
+        int rt = 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaGetDeviceProperties(&prop, dev);
+        cudaRuntimeGetVersion(&rt);
+        o += ", \"performance_specs\": {\"device_name\": \"" + std::string(prop.name) +
+             "\", \"device_cc_major\": " + std::to_string(prop.major) + ", \"device_cc_minor\": " +
+             std::to_string(prop.minor) + ", \"cuda_version\": " + std::to_string(rt) +
+             // device checks are compiled per model source here; on unless a source turns them off
+             ", \"seatbelts\": true, \"flamegpu_version\": \"" + fg_version() + "\"}";
+    }
+    o += ", \"steps\": [";
     bool first = true;
     for (const auto& f : run_log.getStepLog()) {
         if (!first) o += ", ";
         first = false;
-        write_frame(o, f, "step_time", f.getStepTime());
+        write_frame(o, f, with_times ? std::vector<std::pair<const char*, double>>{{"step_time", f.getStepTime()}}
+                                     : std::vector<std::pair<const char*, double>>{});
     }
     o += "]";
     if (exit_log) {
+        const ExitLogFrame& e = run_log.getExitLog();
         o += ", \"exit\": ";
-        write_frame(o, run_log.getExitLog(), "total_time", run_log.getExitLog().getTotalTime());
+        write_frame(o, e, with_times ? std::vector<std::pair<const char*, double>>{{"rtc_time", e.getRTCTime()},
+                                                                                    {"init_time", e.getInitTime()},
+                                                                                    {"exit_time", e.getExitTime()},
+                                                                                    {"total_time", e.getTotalTime()}}
+                                     : std::vector<std::pair<const char*, double>>{});
     }
     o += "}";
     return o;

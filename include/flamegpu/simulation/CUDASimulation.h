@@ -214,8 +214,11 @@ class CUDASimulation {
     void setExitLog(const LoggingConfig& cfg);
     const RunLog& getRunLog() const { return run_log; }
     /** The run log in the layout of the reference's JSONLogger
-     *  (src/flamegpu/io/JSONLogger.cu:80-200): config, steps, exit. */
-    std::string runLogJSON() const;
+     *  (src/flamegpu/io/JSONLogger.cu:80-200): config, performance_specs and
+     *  the frames' times (with_times: logStepTime / logExitTime), steps, exit.
+     *  An agent's "count" is written as the number (the reference's
+     *  j["count"][n] turns it into an array of n + 1 nulls). */
+    std::string runLogJSON(bool with_times = true) const;
     /** Raw bytes of an environment property (GB300 extension). */
     void getEnvironmentRaw(const std::string& name, void* out, size_t bytes);
     /** Logs the frame of the step just completed when it is due (called by the step). */

@@ -234,7 +234,12 @@ class StepLogFrame : public LogFrame {
 class ExitLogFrame : public LogFrame {
  public:
     double getTotalTime() const { return total_time; }
+    // run-time compilation (none here: 0), init and exit function seconds
+    double getRTCTime() const { return rtc_time; }
+    double getInitTime() const { return init_time; }
+    double getExitTime() const { return exit_time; }
     double total_time = 0.0;
+    double rtc_time = 0.0, init_time = 0.0, exit_time = 0.0;
 };
 
 /** RunLog (RunLog.h): the step frames and exit frame of one run. */

@@ -68,3 +68,41 @@ def test_logs_are_deterministic():
         s.close()
     strip = lambda frames: [{k: v for k, v in fr.items() if k != "step_time"} for fr in frames]
     assert strip(outs[0]) == strip(outs[1])
+
+
+def test_run_log_layout_matches_the_reference_logger():
+    # JSONLogger (src/flamegpu/io/JSONLogger.cu:80-200): top-level config,
+    # performance_specs (with the times), steps, exit; a step frame's
+    # step_time before step_index, env, agents; the exit frame's rtc_time,
+    # init_time, exit_time, total_time first; agents -> agent -> state -> a
+    # list of {count, variables -> variable -> reduction -> value}
+    import json
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    pop = synth.birth_death_population(5000, 2)
+    s = S.Simulation("birth_death", [0.30, 0.20, 2], steps=4)
+    s.configure(steps=4, seed=7)
+    s.set_population("agent", 5000, pop)
+    s.set_step_log(["count:agent:default", "env:P_DEATH", "sum:agent:default:counter", "mean:agent:default:f0"],
+                   frequency=2)
+    s.set_exit_log(["count:agent:default", "max:agent:default:f3", "min:agent:default:f3"])
+    s.simulate()
+    log = s.run_log()
+    s.close()
+    assert list(log) == ["config", "performance_specs", "steps", "exit"]
+    assert log["config"] == {"random_seed": 7}
+    assert list(log["performance_specs"]) == ["device_name", "device_cc_major", "device_cc_minor", "cuda_version",
+                                              "seatbelts", "flamegpu_version"]
+    for fr in log["steps"]:
+        assert list(fr) == ["step_time", "step_index", "env", "agents"]
+        assert list(fr["agents"]) == ["agent"] and list(fr["agents"]["agent"]) == ["default"]
+        entry = fr["agents"]["agent"]["default"]
+        assert isinstance(entry, list) and len(entry) == 1
+        assert list(entry[0]) == ["count", "variables"]
+        assert list(entry[0]["variables"]) == ["counter", "f0"]  # std::map order of (name, reduction)
+        assert list(entry[0]["variables"]["counter"]) == ["sum"]
+        assert list(entry[0]["variables"]["f0"]) == ["mean"]
+    ex = log["exit"]
+    assert list(ex) == ["rtc_time", "init_time", "exit_time", "total_time", "step_index", "agents"]
+    assert list(ex["agents"]["agent"]["default"][0]["variables"]["f3"]) == ["min", "max"]  # Reduction enum order
+    json.dumps(log)  # plain JSON throughout
