@@ -84,14 +84,6 @@ __device__ __forceinline__ uint32_t spin_limit_of(const WsHeader* h) {
     return v ? v : kSpinLimit;
 }
 
-// A build or sort whose scan gave up (FG_ERR_DEVICE_TIMEOUT recorded) has no
-// valid PBM: the kernels after the scan skip their work, because a PBM that is
-// not monotonic would send them past the ends of their buffers. The status is
-// written by an earlier kernel of the same stream, so it is settled here.
-__device__ __forceinline__ bool scan_gave_up(const WsHeader* h) {
-    return *reinterpret_cast<const volatile uint32_t*>(&h->status) == static_cast<uint32_t>(FG_ERR_DEVICE_TIMEOUT);
-}
-
 __device__ __forceinline__ void record_status(WsHeader* h, int32_t code) {
     atomicCAS(&h->status, 0u, static_cast<uint32_t>(code));
 }

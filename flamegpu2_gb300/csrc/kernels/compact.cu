@@ -152,9 +152,9 @@ __global__ void __launch_bounds__(kThreads) k_compact(const __grid_constant__ Co
     __shared__ uint32_t s_tot[2];
     __shared__ uint64_t s_excl;
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
-    const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
-    const uint32_t limit = spin_limit_of(h);
+    const uint32_t limit = spin_limit_of(h);  // before the acquire load (no extra round trip)
     const bool withhold = h->withhold != 0;
+    const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
     const uint32_t n = d_n ? min(*d_n, max_n) : max_n;
     const uint32_t S = d_alive_total ? *d_alive_total : h->alive_total;
     const uint32_t next_id = d_next_id ? *d_next_id : 0u;
@@ -500,9 +500,9 @@ __global__ void __launch_bounds__(kThreads) k_compact_batched(
     __shared__ uint32_t s_tot[2];
     __shared__ uint64_t s_excl;
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
-    const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
-    const uint32_t limit = spin_limit_of(h);
+    const uint32_t limit = spin_limit_of(h);  // before the acquire load (no extra round trip)
     const bool withhold = h->withhold != 0;
+    const uint32_t parity = ld_acquire_u32(&h->comp_parity) & 1u;
     uint64_t* status = status0 + static_cast<size_t>(parity) * stride_tiles;
     uint64_t* other = status0 + static_cast<size_t>(parity ^ 1u) * stride_tiles;
     for (uint32_t t = blockIdx.x * blockDim.x + tid; t < stride_tiles; t += gridDim.x * blockDim.x) other[t] = 0;

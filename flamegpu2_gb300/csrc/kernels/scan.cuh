@@ -54,11 +54,11 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 // Warp 0 of a block: look back over predecessor tiles of `tile` and return the
 // exclusive prefix. `status` must already hold this tile's aggregate.
-// At most `limit` polls per predecessor; a give-up is recorded in the header
-// and the predecessor counts as an inclusive prefix of 0, so the scan finishes
-// (with wrong prefixes) instead of hanging.
-__device__ __forceinline__ uint32_t lookback_u32(const uint64_t* status, uint32_t tile, uint32_t epoch, WsHeader* h,
-                                                 uint32_t limit) {
+// At most spin_limit_of(h) polls per predecessor (read once a wait gets
+// long, off the fast path); a give-up is recorded in the header and the
+// predecessor counts as an inclusive prefix of 0, so the scan finishes (with
+// wrong prefixes) instead of hanging.
+__device__ __forceinline__ uint32_t lookback_u32(const uint64_t* status, uint32_t tile, uint32_t epoch, WsHeader* h) {
     const uint32_t lane = lane_id();
     uint32_t excl = 0;
     int64_t pred = static_cast<int64_t>(tile) - 1;
@@ -66,13 +66,14 @@ __device__ __forceinline__ uint32_t lookback_u32(const uint64_t* status, uint32_
         const int64_t t = pred - lane;
         uint32_t flag = 2, val = 0;
         if (t >= 0) {
-            uint32_t spins = 0;
+            uint32_t spins = 0, limit = 0xFFFFFFFFu;
             for (;;) {
                 const uint64_t s = ld_acquire_u64(status + t);
                 const uint32_t e = static_cast<uint32_t>(s >> 32) & 0x3FFFFFFFu;
                 flag = static_cast<uint32_t>(s >> 62);
                 val = static_cast<uint32_t>(s);
                 if (flag != 0 && e == (epoch & 0x3FFFFFFFu)) break;
+                if (spins == 16) limit = spin_limit_of(h);
                 if (++spins > limit) {
                     record_status(h, FG_ERR_DEVICE_TIMEOUT);
                     flag = 2;
@@ -135,14 +136,17 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
                                                        uint64_t* status, WsHeader* h, int self_reset,
                                                        const uint32_t* last, uint32_t last_floor) {
     flamegpu::detail::grid_dependency_enter();
-    __shared__ uint32_t s_tile, s_epoch, s_limit, s_withhold;
+    __shared__ uint32_t s_tile, s_epoch;
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_excl;
+    // a test hook (fg_workspace_set_wait_limit): tile 0 does not publish. Only
+    // tile 0's thread 0 reads it, before its data loads, and uses it when it
+    // publishes, so the load adds nothing to the look-back chain
+    uint32_t withhold = 0;
     if (threadIdx.x == 0) {
         s_tile = atomicAdd(&h->scan_ticket, 1u);
         s_epoch = ld_acquire_u32(&h->scan_epoch);
-        s_limit = spin_limit_of(h);
-        s_withhold = h->withhold;
+        if (s_tile == 0) withhold = h->withhold;
     }
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
@@ -172,10 +176,10 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
     if (threadIdx.x < 32) {
         uint32_t excl = 0;
         if (tile == 0) {
-            if (threadIdx.x == 0 && !s_withhold) st_release_u64(status, scan_pack(2, epoch, ttotal));
+            if (threadIdx.x == 0 && !withhold) st_release_u64(status, scan_pack(2, epoch, ttotal));
         } else {
             if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(1, epoch, ttotal));
-            excl = lookback_u32(status, tile, epoch, h, s_limit);
+            excl = lookback_u32(status, tile, epoch, h);
             if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(2, epoch, excl + ttotal));
         }
         if (threadIdx.x == 0) s_excl = excl;

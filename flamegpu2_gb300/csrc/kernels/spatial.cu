@@ -177,7 +177,6 @@ __global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_
                                                    const uint32_t* __restrict__ pbm, uint32_t* __restrict__ perm,
                                                    WsHeader* h) {
     flamegpu::detail::grid_dependency_enter();
-    if (scan_gave_up(h)) return;
     const uint32_t n = load_count(d_n, max_n);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t k = keys[i];
@@ -371,7 +370,6 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
                                                         uint2* chunk_list, uint32_t chunk_cap, WsHeader* h,
                                                         const uint32_t* key_max, uint32_t key_floor) {
     flamegpu::detail::grid_dependency_enter();
-    if (scan_gave_up(h)) return;
     // key_max (agent sorts): the PBM ends at max(recorded key, key_floor) + 1
     const uint32_t total = pbm[key_max ? min(nbuckets, max(*key_max, key_floor) + 1u) : nbuckets];
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
@@ -382,6 +380,10 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
             continue;
         }
         const uint32_t s = pbm[b], e = pbm[b + 1];
+        // a PBM from a scan whose look-back gave up (FG_ERR_DEVICE_TIMEOUT
+        // recorded) may run backwards: such a bin is skipped, so no bin is
+        // queued or ranked past the messages (entries never exceed their count)
+        if (e < s) continue;
         const uint32_t len = e - s;
         if (len > kShortBin) {
             if (p == s) {
@@ -433,7 +435,6 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
     flamegpu::detail::grid_dependency_enter();
     // the last kernel of an agent sort: the largest key is no longer read
     if (key_max_reset && blockIdx.x == 0 && threadIdx.x == 0) *key_max_reset = 0u;
-    if (scan_gave_up(h)) return;  // the same in every thread
     __shared__ uint32_t s_idx[kSortCap];
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_lo, s_hi;

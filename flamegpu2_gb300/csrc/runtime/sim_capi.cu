@@ -260,6 +260,13 @@ extern "C" int fgs_time_ops_in_graphs(fgs_sim* s, int32_t enable) {
     });
 }
 
+extern "C" int fgs_time_op_in_graphs(fgs_sim* s, const char* label) {
+    return guarded([&] {
+        s->sim->CUDAConfig().time_op_label = label ? label : "";
+        s->sim->applyConfig();
+    });
+}
+
 extern "C" int fgs_harvest_profile(fgs_sim* s) { return guarded([&] { s->sim->harvestOperationTimes(); }); }
 
 extern "C" int fgs_export(fgs_sim* s, const char* path) { return guarded([&] { s->sim->exportData(path); }); }

@@ -393,6 +393,7 @@ struct SimulationImpl {
     // misc device state
     uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record, [8..] next ids per agent
     unsigned long long* d_agent_steps = nullptr;  // [0] agents summed over the steps run, [1] agents now
+    unsigned long long host_agent_steps = 0;      // the same for populations that only the host changes
     uint32_t* h_pinned = nullptr;
     uint32_t* h_pinned_dev = nullptr;  // its device address (null: not mapped)
     unsigned int step_count = 0;
@@ -1003,7 +1004,9 @@ struct SimulationImpl {
     // Config::time_ops_in_graphs is set.
     template <typename Op>
     void timed_on(cudaStream_t st, const std::string& label, Op&& op) {
-        const bool in_graph = capturing && cuda_config.time_ops_in_graphs;
+        const bool in_graph =
+            capturing && (cuda_config.time_ops_in_graphs ||
+                          (!cuda_config.time_op_label.empty() && label == cuda_config.time_op_label));
         if (!profiling && !in_graph) {
             op();
             return;
@@ -1393,6 +1396,12 @@ struct SimulationImpl {
         }
     }
 
+    // populations no kernel changes: the agents of the step being issued
+    void count_host_step() {
+        if (counts_on_device()) return;
+        for (const auto& l : lists) host_agent_steps += l->bound;
+    }
+
     void enqueue_step() {
         kernel_counter = 0;
         for (auto& m : msgs) {
@@ -1430,9 +1439,17 @@ struct SimulationImpl {
     }
 
     // Every list's count, for the agent-step accumulator (models of at most
-    // kStepEndCounts agent lists; beyond that, no count is kept).
+    // kStepEndCounts agent lists; beyond that, no count is kept). Only models
+    // whose populations change on the device (birth, death, state
+    // transitions) count there; the others' counts are the host's (host_steps).
+    bool counts_on_device() const {
+        if (any_births() || any_transitions()) return true;
+        for (const auto& f : fns)
+            if (f.fn->has_agent_death) return true;
+        return false;
+    }
     void count_targets(StepEnd& e) const {
-        if (lists.size() > kStepEndCounts) return;
+        if (lists.size() > kStepEndCounts || !counts_on_device()) return;
         for (const auto& l : lists) e.counts[e.ncounts++] = l->d_count;
         e.acc = d_agent_steps;
     }
@@ -1522,11 +1539,12 @@ struct SimulationImpl {
             }
             FG_CUDA(cudaGraphLaunch(it->second, stream));
             ++graph_launches;
-            if (cuda_config.time_ops_in_graphs) replayed.insert(key);
+            if (cuda_config.time_ops_in_graphs || !cuda_config.time_op_label.empty()) replayed.insert(key);
         }
         FG_CUDA(cudaEventRecord(e1, stream));
         step_events.push_back({e0, e1, 1u});
         record_counts();
+        count_host_step();
         ++step_count;
         if (!model->step_functions.empty()) {
             FG_CUDA(cudaStreamSynchronize(stream));
@@ -1625,8 +1643,10 @@ struct SimulationImpl {
         kernels_last_step = kernel_counter;
         FG_CUDA(cudaGraphLaunch(it->second, stream));
         ++graph_launches;
+        if (!cuda_config.time_op_label.empty()) replayed.insert(key);
         FG_CUDA(cudaEventRecord(e1, stream));
         step_events.push_back({e0, e1, S});
+        for (unsigned int j = 0; j < S; ++j) count_host_step();
         for (size_t i = 0; i < lists.size(); ++i)  // bounds after the block's S steps
             lists[i]->bound = static_cast<uint32_t>(std::min<uint64_t>(after[i], 0xFFFFFFFFu));
         step_count += S - 1;
@@ -2353,6 +2373,7 @@ void detail::SimulationImpl::resolve_step_timers() {
 }
 
 unsigned long long CUDASimulation::getAgentStepCount() {
+    if (!impl->counts_on_device()) return impl->host_agent_steps;
     unsigned long long v = 0;
     FG_CUDA(cudaStreamSynchronize(impl->stream));
     FG_CUDA(cudaMemcpy(&v, impl->d_agent_steps, sizeof(v), cudaMemcpyDeviceToHost));

@@ -23,7 +23,7 @@ SIM_EXPORTS = [
     "fgs_get_environment", "fgs_stream", "fgs_stats", "fgs_step_times", "fgs_profile_ops", "fgs_take_profile",
     "fgs_set_stage_bytes", "fgs_reset_population_device", "fgs_time_ops_in_graphs", "fgs_harvest_profile",
     "fgs_export", "fgs_load_state", "fgs_set_log", "fgs_run_log", "fgs_agent_steps", "fgs_set_config",
-    "fgs_get_config",
+    "fgs_get_config", "fgs_time_op_in_graphs",
 ]
 
 _lock = threading.Lock()
@@ -59,6 +59,7 @@ def core():
             L.fgs_step.argtypes = [vp, u32]
             L.fgs_agent_steps.argtypes = [vp, C.POINTER(C.c_uint64)]
             L.fgs_set_config.argtypes = [vp, C.c_char_p, C.c_char_p]
+            L.fgs_time_op_in_graphs.argtypes = [vp, C.c_char_p]
             L.fgs_get_config.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_size_t]
             L.fgs_simulate.argtypes = [vp]
             L.fgs_synchronize.argtypes = [vp]
@@ -255,6 +256,10 @@ class Simulation:
 
     def time_ops_in_graphs(self, enable: bool = True):
         _check(core().fgs_time_ops_in_graphs(self._h, int(enable)))
+
+    def time_op_in_graphs(self, label):
+        """Time one operation (e.g. "fn:inputdata") by events inside the multi-step graphs (None: off)."""
+        _check(core().fgs_time_op_in_graphs(self._h, label.encode() if label else None))
 
     def harvest_profile(self):
         _check(core().fgs_harvest_profile(self._h))

@@ -98,6 +98,11 @@ class CUDASimulation {
         // graphs; harvestOperationTimes() adds the times of the last replay of
         // each graph to the operation profile. Steps stay graph replays.
         bool time_ops_in_graphs = false;
+        // One operation (a label of the operation profile, e.g. "fn:inputdata")
+        // timed the same way while steps stay replayed several per graph:
+        // only its launches are bracketed by events, every replay's are read
+        // by harvestOperationTimes(). Empty: off.
+        std::string time_op_label;
         unsigned int message_stage_bytes = 96u * 1024u;  // shared memory per block for spatial neighbour windows (0: off)
         // Largest population an agent list may reach, births included: buffers
         // never grow past it, and a step that could exceed it (checked when the

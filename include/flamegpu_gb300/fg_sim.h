@@ -83,6 +83,10 @@ int fgs_take_profile(fgs_sim* sim, char* buf, size_t len);
 int fgs_time_ops_in_graphs(fgs_sim* sim, int32_t enable);
 /* Adds the operation times of the last replay of each graph replayed since the
  * previous call to the profile read by fgs_take_profile (waits for the stream). */
+/* One operation's launches timed by CUDA events inside the step graphs while
+ * steps stay replayed several per graph (CUDAConfig::time_op_label; NULL or ""
+ * turns it off); read with fgs_harvest_profile / fgs_take_profile. */
+int fgs_time_op_in_graphs(fgs_sim* sim, const char* label);
 int fgs_harvest_profile(fgs_sim* sim);
 /* CUDASimulation::exportData / loadState: JSON state files in the reference's
  * layout (config, stats.step_count, environment, agents -> state -> rows). */

@@ -378,3 +378,17 @@ def test_steps_replayed_as_one_graph_match_single_steps():
         np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
     assert stats[0]["graph_launches"] == 37 and stats[1]["graph_launches"] == 3
     assert stats[0]["step_counter"] == stats[1]["step_counter"] == 37
+
+
+def test_agent_steps_of_a_fixed_population():
+    # no birth, death or transition: counted on the host, n per step, whether
+    # steps are replayed one or ten per graph
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    cfg = dict(synth.BOIDS_SMALL, n=3000)
+    s = S.Simulation("boids_spatial3d", synth.boids_params(cfg))
+    s.set_population("Boid", 3000, synth.boids_population(3000, cfg["min_pos"], cfg["max_pos"], 2))
+    s.step(1)
+    s.step(10)
+    assert s.agent_steps() == 3000 * 11
+    s.close()
