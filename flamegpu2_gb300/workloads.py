@@ -43,24 +43,39 @@ def _stage_table(prof: dict, algo: dict, per_launch: bool = True) -> dict:
     return out
 
 
-def profiled_traffic(summary: str, key: str = ""):
-    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
-    a workload's roofline kernel, from one ncu capture summarised in
-    profiles/<summary>.md (line '[key ]traffic_bytes_per_launch: N'); None if absent."""
+def profiled_value(summary: str, name: str, key: str = ""):
+    """A per-launch figure of a workload's roofline kernel from one ncu capture
+    summarised in profiles/<summary>.md (line '[key ]<name>: N'); None if absent."""
     import re
     try:
         with open(os.path.join(ROOT, "profiles", summary + ".md")) as f:
-            m = re.search(r"^" + re.escape((key + " ") if key else "") + r"traffic_bytes_per_launch:\s*(\d+)", f.read(), re.M)
+            m = re.search(r"^" + re.escape((key + " ") if key else "") + re.escape(name) + r":\s*([0-9.]+)",
+                          f.read(), re.M)
     except OSError:
         return None
-    return int(m.group(1)) if m else None
+    return float(m.group(1)) if m else None
+
+
+def profiled_traffic(summary: str, key: str = ""):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)."""
+    t = profiled_value(summary, "traffic_bytes_per_launch", key)
+    return int(t) if t is not None else None
 
 
 def _with_traffic(roof: dict, summary: str, what: str = None, key: str = "") -> dict:
+    """Adds the profiled DRAM traffic and, where the summary records the same
+    launch's ncu duration (gpu__time_duration.sum), the roofline fraction that
+    duration gives: a cross-check of the live event timing, which inside a
+    graph also counts the event nodes and the lost programmatic launch overlap."""
     t = profiled_traffic(summary, key)
     if t is not None:
         roof["traffic"] = t
         roof["traffic_source"] = f"profiles/{summary}.md" + (f": {what}" if what else "")
+    us = profiled_value(summary, "ncu_duration_us_per_launch", key)
+    alg = roof.get("per_launch_algorithmic_bytes")
+    if us and alg and roof.get("peak"):
+        gbs = alg / (us * 1e-6) / 1e9
+        roof["ncu_check"] = {"duration_us": us, "achieved": round(gbs, 2), "frac": round(gbs / roof["peak"], 4)}
     return roof
 
 
