@@ -48,7 +48,8 @@ struct WsHeader {
     uint32_t key_max;       // largest sort key of an agent sort (0 between sorts)
     uint32_t spin_limit;    // look-back poll bound (0 = kSpinLimit)
     uint32_t withhold;      // non-zero: tile 0 of scans and compactions does not publish (wait test)
-    uint32_t pad[52];
+    uint32_t disorder;      // non-zero: a build's keys are not in row order (0 between builds)
+    uint32_t pad[51];
 };
 static_assert(sizeof(WsHeader) == 256, "header is 256 bytes");
 // words an agent-function launch resets when it computes a build's keys
@@ -56,6 +57,7 @@ static_assert(offsetof(WsHeader, scan_epoch) == 4 * flamegpu::detail::kWsHdrScan
 static_assert(offsetof(WsHeader, scan_ticket) == 4 * flamegpu::detail::kWsHdrScanTicket, "header layout");
 static_assert(offsetof(WsHeader, long_count) == 4 * flamegpu::detail::kWsHdrLongCount, "header layout");
 static_assert(offsetof(WsHeader, key_max) == 4 * flamegpu::detail::kWsHdrKeyMax, "header layout");
+static_assert(offsetof(WsHeader, disorder) == 4 * flamegpu::detail::kWsHdrDisorder, "header layout");
 
 __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
     uint64_t v;

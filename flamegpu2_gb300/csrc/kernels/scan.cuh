@@ -131,12 +131,36 @@ __device__ __forceinline__ void scan_load(const uint32_t* in, uint64_t base, uin
     }
 }
 
+// The row-order check a build's scan finishes for the key launch before it
+// (keys null: none). That launch compared each row's key with the row before
+// it inside 32-row groups; the scan compares the keys of rows 32w - 1 and 32w,
+// and raises the workspace's disorder flag at a descent.
+struct OrderCheck {
+    const uint32_t* keys = nullptr;
+    const uint32_t* d_n = nullptr;  // rows (device), at most max_n; null: max_n
+    uint32_t max_n = 0;
+};
+
+// The blocks share the 32-row group boundaries; unless the key launch already
+// found a descent (`pending` false), each block reads its boundaries' two keys.
+__device__ __forceinline__ void order_check_boundaries(const OrderCheck& oc, bool pending, WsHeader* h) {
+    bool bad = false;
+    if (pending) {
+        const uint32_t rows = oc.d_n ? min(*oc.d_n, oc.max_n) : oc.max_n;
+        for (uint32_t w = 1u + blockIdx.x * blockDim.x + threadIdx.x; static_cast<uint64_t>(w) * 32u < rows;
+             w += gridDim.x * blockDim.x)
+            bad = bad || oc.keys[32u * w - 1u] > oc.keys[32u * w];
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) h->disorder = 1u;
+}
+
 template <int R>
 __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
                                                        uint64_t* status, WsHeader* h, int self_reset,
-                                                       const uint32_t* last, uint32_t last_floor) {
+                                                       const uint32_t* last, uint32_t last_floor,
+                                                       const __grid_constant__ OrderCheck oc) {
     flamegpu::detail::grid_dependency_enter();
-    __shared__ uint32_t s_tile, s_epoch;
+    __shared__ uint32_t s_tile, s_epoch, s_pending;
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_excl;
     // a test hook (fg_workspace_set_wait_limit): tile 0 does not publish. Only
@@ -147,13 +171,18 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
         s_tile = atomicAdd(&h->scan_ticket, 1u);
         s_epoch = ld_acquire_u32(&h->scan_epoch);
         if (s_tile == 0) withhold = h->withhold;
+        s_pending = oc.keys != nullptr && h->disorder == 0u;
     }
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
+    const bool pending = s_pending != 0u;
     // last (no self reset): the values past index max(*last, last_floor) + 1
     // are zero and their prefixes unused; the tiles wholly past it have nothing to do
     if (last) n = min(n, max(*last, last_floor) + 2u);
-    if (static_cast<uint64_t>(tile) * R * kScanTile >= n && tile != 0) return;
+    if (static_cast<uint64_t>(tile) * R * kScanTile >= n && tile != 0) {
+        if (oc.keys) order_check_boundaries(oc, pending, h);
+        return;
+    }
     const bool in_al = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
     const bool out_al = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
     uint32_t v[kScanItems];
@@ -220,6 +249,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
             }
         }
     }
+    if (oc.keys) order_check_boundaries(oc, pending, h);
     if (!self_reset) return;
     // the last block to finish resets the ticket and advances the epoch
     __syncthreads();
@@ -246,12 +276,12 @@ inline thread_local uint32_t t_scan_wide_min = kScanWideMin;
 // last, last_floor: optional (device) bound, as in k_scan_u32; only without self_reset.
 inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in, uint64_t* status,
                                WsHeader* h, int self_reset, cudaStream_t st, const uint32_t* last = nullptr,
-                               uint32_t last_floor = 0) {
+                               uint32_t last_floor = 0, const OrderCheck& oc = OrderCheck()) {
     if (n > t_scan_wide_min)
         return launch(k_scan_u32<4>, (n + 4u * kScanTile - 1) / (4u * kScanTile), kThreads, st, in, out, n, zero_in,
-                      status, h, self_reset, last, last_floor);
+                      status, h, self_reset, last, last_floor, oc);
     return launch(k_scan_u32<1>, scan_tiles(n), kThreads, st, in, out, n, zero_in, status, h, self_reset, last,
-                  last_floor);
+                  last_floor, oc);
 }
 
 }  // namespace fgk

@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
     const uint32_t n = load_count(d_n, max_n);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t cells = flamegpu::detail::sort_cells(sg);
+    bool out_of_order = false;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < n;
@@ -94,7 +95,12 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
             keys[i] = key;
             slot[i] = s;
         }
+        // row order (rows 32w - 1, 32w are compared by the scan)
+        const uint32_t pk = __shfl_up_sync(0xFFFFFFFFu, key, 1);
+        out_of_order = out_of_order || (act && (key == kInvalid || (lane_id() > 0u && pk > key)));
     }
+    // one store per block at most (a store per warp to one word serialises)
+    if (__syncthreads_or(out_of_order) && threadIdx.x == 0) h->disorder = 1u;
 }
 
 // The slot came from the histogram atomics, so pbm[k] + slot < n holds as long
@@ -126,6 +132,7 @@ __global__ void __launch_bounds__(kThreads) k_bin_batched(const fg_batch_instanc
     flamegpu::detail::grid_dependency_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         h->long_count = 0;
+        h->disorder = 1u;  // batches always take the placement and ranking path
         scan_reset(h);  // for the scan launched next
     }
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -177,6 +184,7 @@ __global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_
                                                    const uint32_t* __restrict__ pbm, uint32_t* __restrict__ perm,
                                                    WsHeader* h) {
     flamegpu::detail::grid_dependency_enter();
+    if (h->disorder == 0u) return;  // keys in row order: every row keeps its place
     const uint32_t n = load_count(d_n, max_n);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t k = keys[i];
@@ -368,10 +376,18 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
                                                         const uint32_t* __restrict__ pbm,
                                                         const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                         uint2* chunk_list, uint32_t chunk_cap, WsHeader* h,
-                                                        const uint32_t* key_max, uint32_t key_floor) {
+                                                        const uint32_t* key_max, uint32_t key_floor, uint32_t max_n) {
     flamegpu::detail::grid_dependency_enter();
     // key_max (agent sorts): the PBM ends at max(recorded key, key_floor) + 1
     const uint32_t total = pbm[key_max ? min(nbuckets, max(*key_max, key_floor) + 1u) : nbuckets];
+    if (h->disorder == 0u) {
+        // keys in row order (the key launch and the scan found no descent):
+        // the stable order is the row order, so rows are emitted in place, as
+        // one run over the grid's threads (four rows in flight per thread)
+        emit_run<EMIT>(rp, sperm, 0u, 0u, min(total, max_n), blockIdx.x * blockDim.x + threadIdx.x,
+                       gridDim.x * blockDim.x);
+        return;
+    }
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
         const uint32_t i = perm[p];
         const uint32_t b = keys[i];
@@ -431,10 +447,15 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
                                                    const uint32_t* __restrict__ pbm,
                                                    const uint32_t* __restrict__ perm, uint32_t* sperm,
                                                    const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
-                                                   const WsHeader* h, uint32_t* key_max_reset) {
+                                                   WsHeader* h, uint32_t* key_max_reset) {
     flamegpu::detail::grid_dependency_enter();
-    // the last kernel of an agent sort: the largest key is no longer read
-    if (key_max_reset && blockIdx.x == 0 && threadIdx.x == 0) *key_max_reset = 0u;
+    // the last kernel of an agent sort: the largest key is no longer read;
+    // the last of any build: the order flag is no longer read (the next key
+    // launch raises it again where its keys descend)
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (key_max_reset) *key_max_reset = 0u;
+        h->disorder = 0u;
+    }
     __shared__ uint32_t s_idx[kSortCap];
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_lo, s_hi;
@@ -807,15 +828,16 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     // (or launch) recorded
     uint32_t* key_max = (MODE == kSortKey && !batch.inst) ? &h->key_max : nullptr;
     const uint32_t key_floor = flamegpu::detail::sort_cells(sg) - 1u;
-    launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st, key_max, key_floor);
+    // the scan also compares the keys of rows 32w - 1 and 32w (row order; a batch's keys are never in it)
+    const OrderCheck oc{batch.inst ? nullptr : keys, d_n, max_n};
+    launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st, key_max, key_floor, oc);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
     launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h,
-           static_cast<const uint32_t*>(key_max), key_floor);
+           static_cast<const uint32_t*>(key_max), key_floor, max_n);
     // a long bin has more than 32 rows and a chunk 256: one block per 128 rows
     // covers every chunk of a small list at once; large lists get 4 per SM
     const uint32_t long_grid = std::max(1u, std::min((max_n + 127u) / 128u, static_cast<uint32_t>(sm_count() * 4)));
-    launch(k_long<EMIT>, long_grid, kThreads, st, rp, pbm_out, perm, sperm, chunks, L.chunk_cap,
-           static_cast<const WsHeader*>(h), key_max);
+    launch(k_long<EMIT>, long_grid, kThreads, st, rp, pbm_out, perm, sperm, chunks, L.chunk_cap, h, key_max);
     return check_launch();
 }
 

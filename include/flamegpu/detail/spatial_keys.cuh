@@ -64,6 +64,10 @@ constexpr int kWsHdrLongCount = 4;
 // raised to the largest sort key past the grid's cells (positions outside the
 // environment; 0 if none): the sort's scan stops past max(it, cells - 1)
 constexpr int kWsHdrKeyMax = 9;
+// raised when a build's keys are not in row order (non-decreasing over rows
+// that all carry a key); left 0, the rows are already in the order the build
+// would give them and its placement and ranking are skipped
+constexpr int kWsHdrDisorder = 12;
 
 /** Where a launch writes the keys of a build or an agent sort (mode 0: none). */
 struct KeyTarget {
@@ -98,9 +102,13 @@ __device__ __forceinline__ uint32_t key_target_key(const KeyTarget& t, bool vali
 // Histogram counts and slots of the keys k[0], k[1] of rows row[0], row[1]
 // for the targets t[0], t[1] (mode kKeyNone: skipped), by the lanes that
 // reach it together: lanes with the same key share one atomic, and the two
-// targets' atomics are issued before either result is used.
-__device__ __forceinline__ void key_targets_write(const KeyTarget (&t)[2], const uint32_t (&row)[2],
-                                                  const uint32_t (&k)[2]) {
+// targets' atomics are issued before either result is used. Returns bit j set
+// where target j's rows here are out of order (the same in every lane); the
+// launch raises the targets' disorder flags once per block at its end
+// (key_targets_order_flush), so a launch over unsorted rows does not store to
+// one word from every warp.
+__device__ __forceinline__ uint32_t key_targets_write(const KeyTarget (&t)[2], const uint32_t (&row)[2],
+                                                      const uint32_t (&k)[2]) {
     // the lanes here together (rows skipped or finished earlier are not);
     // every one of them executes the ballots, those with a key the matches
     const uint32_t active = __activemask();
@@ -126,6 +134,33 @@ __device__ __forceinline__ void key_targets_write(const KeyTarget (&t)[2], const
         if (peers[j]) s = __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1) + __popc(peers[j] & ((1u << lane) - 1u));
         t[j].keys[row[j]] = k[j];
         t[j].slot[row[j]] = s;
+    }
+    // row order: each key against the key of the row before it when that row
+    // is the lane below's; a row whose predecessor is elsewhere is compared by
+    // the build's scan if it starts a 32-row group (rows 32w - 1, 32w), else
+    // counted as out of order. A row without a key is out of order.
+    uint32_t out_of_order = 0u;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (t[j].mode == kKeyNone) continue;
+        const uint32_t pk = __shfl_up_sync(active, k[j], 1);
+        const uint32_t pr = __shfl_up_sync(active, row[j], 1);
+        const bool has_prev = lane > 0u && ((active >> (lane - 1u)) & 1u) && pr + 1u == row[j];
+        const bool bad = k[j] == 0xFFFFFFFFu || (has_prev ? pk > k[j] : (row[j] & 31u) != 0u);
+        if (__ballot_sync(active, bad)) out_of_order |= 1u << j;
+    }
+    return out_of_order;
+}
+
+// End of a key-computing launch, reached by every thread of the block:
+// raises target j's disorder flag if any of the block's rows were out of
+// order for it (bit j of `out_of_order`, as key_targets_write returned).
+__device__ __forceinline__ void key_targets_order_flush(const KeyTarget (&t)[2], uint32_t out_of_order) {
+    const int any0 = __syncthreads_or(out_of_order & 1u);
+    const int any1 = __syncthreads_or(out_of_order & 2u);
+    if (threadIdx.x == 0) {
+        if (any0 && t[0].mode != kKeyNone) t[0].header[kWsHdrDisorder] = 1u;
+        if (any1 && t[1].mode != kKeyNone) t[1].header[kWsHdrDisorder] = 1u;
     }
 }
 

@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
     }
     constexpr int kDims = std::is_same<MsgIn, MessageSpatial3D>::value ? 3 : (std::is_same<MsgIn, MessageSpatial2D>::value ? 2 : 0);
     bool first = true;
+    uint32_t out_of_order = 0u;  // keyed targets whose rows were not in key order
     if (!P.batch) {
         fill_ctx(P, 0, n);
         __syncthreads();
@@ -167,9 +168,10 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
                                             (api.pos_set & 2u) ? api.pos[1] : pre[1],
                                             (api.pos_set & 4u) ? api.pos[2] : pre[2]);
             const uint32_t rows[2] = {msg_row, idx};
-            key_targets_write(P.keyed, rows, k);
+            out_of_order |= key_targets_write(P.keyed, rows, k);
         }
     }
+    if (P.keyed[0].mode != kKeyNone || P.keyed[1].mode != kKeyNone) key_targets_order_flush(P.keyed, out_of_order);
 }
 
 // FLAMEGPU_AGENT_FUNCTION_CONDITION kernel (AgentFunctionCondition.cuh:44-100):

@@ -87,3 +87,29 @@ def test_payload_model_empty_neighbourhoods_keep_payload():
     for k in range(4):
         np.testing.assert_array_equal(out[f"p{k}"], ref[f"p{k}"])
         np.testing.assert_array_equal(out[f"p{k}"], cols[f"p{k}"][out["_id"] - 1])
+
+
+@pytest.mark.parametrize("descent", [None, "group_boundary", "inside_group"])
+def test_payload_model_from_rows_in_bin_order(descent):
+    # the population starts in message-bin order (then every step's message
+    # build and agent sort see rows in key order and write them in place), or
+    # with one pair of neighbouring rows in different bins exchanged, at a
+    # 32-row group boundary or inside a group: the output launch and the
+    # build's scan must find that one descent
+    dims, n, edge, r = 2, 40_000, 128.0, 4.0
+    cols = _population(dims, n, edge, seed=19)
+    g = O.grid(dims, [0.0] * dims, [edge] * dims, r)
+    _, perm, bins = O.spatial_build(g, cols["x"], cols["y"])
+    cols = {k: v[perm] for k, v in cols.items()}
+    if descent:
+        bins = bins[perm]
+        j = 32 * 601 - 1 if descent == "group_boundary" else 32 * 300 + 5
+        while bins[j] == bins[j + 1]:
+            j += 32
+        for k in cols:
+            cols[k][[j, j + 1]] = cols[k][[j + 1, j]]
+    out = _run_gpu(dims, edge, r, False, cols, 4)
+    ref = O.payload_run(g, False, {"id": cols["_id"], **{k: v for k, v in cols.items() if k != "_id"}}, 4, threads=8)
+    np.testing.assert_array_equal(out["_id"], ref["id"])
+    for k in ["x", "y", "p0", "p1", "p2", "p3"]:
+        np.testing.assert_array_equal(out[k], ref[k], err_msg=k)
