@@ -132,24 +132,27 @@ __device__ __forceinline__ void scan_load(const uint32_t* in, uint64_t base, uin
 }
 
 // The row-order check a build's scan finishes for the key launch before it
-// (keys null: none). That launch compared each row's key with the row before
-// it inside 32-row groups; the scan compares the keys of rows 32w - 1 and 32w,
-// and raises the workspace's disorder flag at a descent.
+// (edges null: none). That launch compared each row's key with the row before
+// it inside 32-row groups and wrote each group's first and last key (edges[2w],
+// edges[2w + 1]); the scan compares the keys of rows 32w - 1 and 32w, and
+// raises the workspace's disorder flag at a descent.
 struct OrderCheck {
-    const uint32_t* keys = nullptr;
+    const uint32_t* edges = nullptr;
     const uint32_t* d_n = nullptr;  // rows (device), at most max_n; null: max_n
     uint32_t max_n = 0;
 };
 
 // The blocks share the 32-row group boundaries; unless the key launch already
-// found a descent (`pending` false), each block reads its boundaries' two keys.
+// found a descent (`pending` false), each block reads its boundaries' keys.
 __device__ __forceinline__ void order_check_boundaries(const OrderCheck& oc, bool pending, WsHeader* h) {
-    bool bad = false;
+    uint32_t bad = 0u;
     if (pending) {
         const uint32_t rows = oc.d_n ? min(*oc.d_n, oc.max_n) : oc.max_n;
+        const uint2* e = reinterpret_cast<const uint2*>(oc.edges);
+#pragma unroll 4
         for (uint32_t w = 1u + blockIdx.x * blockDim.x + threadIdx.x; static_cast<uint64_t>(w) * 32u < rows;
              w += gridDim.x * blockDim.x)
-            bad = bad || oc.keys[32u * w - 1u] > oc.keys[32u * w];
+            bad |= e[w - 1u].y > e[w].x ? 1u : 0u;
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) h->disorder = 1u;
 }
@@ -168,10 +171,13 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
     // publishes, so the load adds nothing to the look-back chain
     uint32_t withhold = 0;
     if (threadIdx.x == 0) {
+        // the key launch's flag is final (it completed before this launch):
+        // read before the acquire, so the two loads overlap
+        const bool pending = oc.edges != nullptr && h->disorder == 0u;
         s_tile = atomicAdd(&h->scan_ticket, 1u);
         s_epoch = ld_acquire_u32(&h->scan_epoch);
         if (s_tile == 0) withhold = h->withhold;
-        s_pending = oc.keys != nullptr && h->disorder == 0u;
+        s_pending = pending;
     }
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
@@ -180,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
     // are zero and their prefixes unused; the tiles wholly past it have nothing to do
     if (last) n = min(n, max(*last, last_floor) + 2u);
     if (static_cast<uint64_t>(tile) * R * kScanTile >= n && tile != 0) {
-        if (oc.keys) order_check_boundaries(oc, pending, h);
+        if (oc.edges) order_check_boundaries(oc, pending, h);
         return;
     }
     const bool in_al = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
@@ -249,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
             }
         }
     }
-    if (oc.keys) order_check_boundaries(oc, pending, h);
+    if (oc.edges) order_check_boundaries(oc, pending, h);
     if (!self_reset) return;
     // the last block to finish resets the ticket and advances the epoch
     __syncthreads();

@@ -64,7 +64,8 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
                                                   const float* __restrict__ x, const float* __restrict__ y,
                                                   const float* __restrict__ z, const uint32_t* __restrict__ valid,
                                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ slot,
-                                                  uint32_t* hist, WsHeader* h, uint32_t pstride) {
+                                                  uint32_t* hist, WsHeader* h, uint32_t pstride,
+                                                  uint32_t* __restrict__ edges) {
     flamegpu::detail::grid_dependency_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         h->long_count = 0;
@@ -95,7 +96,9 @@ __global__ void __launch_bounds__(kThreads) k_bin(fg_spatial_grid g, SortGrid sg
             keys[i] = key;
             slot[i] = s;
         }
-        // row order (rows 32w - 1, 32w are compared by the scan)
+        // row order (rows 32w - 1, 32w are compared by the scan, through the
+        // first and last key of every 32-row group)
+        if (act && (lane_id() == 0u || lane_id() == 31u)) edges[2u * (i >> 5) + (lane_id() ? 1u : 0u)] = key;
         const uint32_t pk = __shfl_up_sync(0xFFFFFFFFu, key, 1);
         out_of_order = out_of_order || (act && (key == kInvalid || (lane_id() > 0u && pk > key)));
     }
@@ -658,7 +661,7 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
 // ------------------------------------------------------------------- host side
 
 struct BuildLayout {
-    size_t hist, scan_status, keys, slot, perm, sperm, chunks, pbm, total;
+    size_t hist, scan_status, keys, slot, perm, sperm, chunks, pbm, edges, total;
     uint32_t chunk_cap;
 };
 
@@ -681,6 +684,7 @@ static BuildLayout build_layout(uint32_t max_n, uint32_t nbuckets, bool sort_mod
     L.perm = take(sizeof(uint32_t) * (static_cast<size_t>(max_n) + 1));
     L.chunk_cap = max_n / (kShortBin + 1) + max_n / kChunk + 16;
     L.chunks = take(sizeof(uint2) * L.chunk_cap);
+    L.edges = take(sizeof(uint32_t) * 2 * (static_cast<size_t>(max_n) / 32 + 1));
     if (sort_mode) {
         L.sperm = take(sizeof(uint32_t) * (static_cast<size_t>(max_n) + 1));
         L.pbm = take(sizeof(uint32_t) * (static_cast<size_t>(scan_n) + 4));
@@ -813,6 +817,7 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     uint32_t* perm = reinterpret_cast<uint32_t*>(ws + L.perm);
     uint32_t* sperm = EMIT != kEmitRecord ? reinterpret_cast<uint32_t*>(ws + L.sperm) : nullptr;
     uint2* chunks = reinterpret_cast<uint2*>(ws + L.chunks);
+    uint32_t* edges = reinterpret_cast<uint32_t*>(ws + L.edges);
     const uint32_t grid = grid_for(max_n);
     if (keys_ready) {
         // the launch before wrote keys, slots and the histogram (key_targets_write)
@@ -820,7 +825,8 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
         launch(k_bin_batched<MODE>, grid, kThreads, st, batch.inst, batch.counts, batch.ninst, max_n, batch.dims, x, y, z,
                valid, keys, slot, hist, h);
     } else {
-        launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h, pos_stride);
+        launch(k_bin<MODE>, grid, kThreads, st, *g, sg, max_n, d_n, x, y, z, valid, keys, slot, hist, h, pos_stride,
+               edges);
     }
     const uint32_t scan_n = nbuckets + 1;
     // an agent sort's buckets (2^bits) run past the grid's cells: its scan stops
@@ -829,7 +835,7 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     uint32_t* key_max = (MODE == kSortKey && !batch.inst) ? &h->key_max : nullptr;
     const uint32_t key_floor = flamegpu::detail::sort_cells(sg) - 1u;
     // the scan also compares the keys of rows 32w - 1 and 32w (row order; a batch's keys are never in it)
-    const OrderCheck oc{batch.inst ? nullptr : keys, d_n, max_n};
+    const OrderCheck oc{batch.inst ? nullptr : edges, d_n, max_n};
     launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st, key_max, key_floor, oc);
     launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
     launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h,
@@ -927,6 +933,7 @@ int fgi_key_target(const fg_spatial_grid* g, uint32_t max_n, bool sort_mode, voi
     t->slot = reinterpret_cast<uint32_t*>(ws + L.slot);
     t->hist = reinterpret_cast<uint32_t*>(ws + L.hist);
     t->header = reinterpret_cast<uint32_t*>(ws);
+    t->edges = reinterpret_cast<uint32_t*>(ws + L.edges);
     return FG_OK;
 }
 

@@ -82,6 +82,7 @@ struct KeyTarget {
     uint32_t* slot;          // per row: its place among the rows of its key (histogram order)
     uint32_t* hist;          // per key: rows counted (zero before the launch)
     uint32_t* header;        // the workspace header
+    uint32_t* edges;         // per 32-row group w: keys of rows 32w and 32w + 31 (row-order check)
 };
 constexpr uint32_t kKeyNone = 0, kKeyMessageBin = 1, kKeySortKey = 2;
 
@@ -137,12 +138,15 @@ __device__ __forceinline__ uint32_t key_targets_write(const KeyTarget (&t)[2], c
     }
     // row order: each key against the key of the row before it when that row
     // is the lane below's; a row whose predecessor is elsewhere is compared by
-    // the build's scan if it starts a 32-row group (rows 32w - 1, 32w), else
-    // counted as out of order. A row without a key is out of order.
+    // the build's scan if it starts a 32-row group (rows 32w - 1, 32w, through
+    // the group edge keys written here), else counted as out of order. A row
+    // without a key is out of order.
     uint32_t out_of_order = 0u;
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         if (t[j].mode == kKeyNone) continue;
+        const uint32_t g = row[j] & 31u;
+        if (g == 0u || g == 31u) t[j].edges[2u * (row[j] >> 5) + (g ? 1u : 0u)] = k[j];
         const uint32_t pk = __shfl_up_sync(active, k[j], 1);
         const uint32_t pr = __shfl_up_sync(active, row[j], 1);
         const bool has_prev = lane > 0u && ((active >> (lane - 1u)) & 1u) && pr + 1u == row[j];
