@@ -115,8 +115,11 @@ extern "C" int fgs_set_population(fgs_sim* s, const char* agent, const char* sta
             all = ad->find(names[k]) != nullptr;
             direct.emplace_back(names[k], cols[k]);
             if (all && std::strcmp(names[k], "_id") == 0) {
+                // one branch-free pass (it vectorises): any id left unset?
                 const flamegpu::id_t* ids = static_cast<const flamegpu::id_t*>(cols[k]);
-                for (uint32_t i = 0; i < n && all; ++i) all = ids[i] != flamegpu::ID_NOT_SET;
+                uint32_t unset = 0;
+                for (uint32_t i = 0; i < n; ++i) unset |= ids[i] == flamegpu::ID_NOT_SET ? 1u : 0u;
+                all = unset == 0;
             }
         }
         if (all) {

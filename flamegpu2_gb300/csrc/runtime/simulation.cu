@@ -128,14 +128,40 @@ __global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
         if (x.max_target) *x.max_target = *x.max_target > x.max_value ? *x.max_target : x.max_value;
     }
     if (tid < x.nwords) *x.word_dst[tid] = *x.word_src[tid];
+    // columns eight at a time: the 16-byte pieces of all eight are loaded
+    // before any is stored, so one round trip to host memory (set) covers
+    // every column instead of one per column
+    for (uint32_t c0 = 0; c0 < x.ncols; c0 += 8) {
+        const uint32_t nc = min(8u, x.ncols - c0);
+        size_t n16[8];
+        size_t most = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < 8; ++j) {
+            n16[j] = 0;
+            if (j < nc) {
+                const size_t bytes = static_cast<size_t>(rows) * x.elem_bytes[c0 + j];
+                const uintptr_t a = reinterpret_cast<uintptr_t>(x.src[c0 + j]) | reinterpret_cast<uintptr_t>(x.dst[c0 + j]);
+                if (((a | bytes) & 15) == 0) n16[j] = bytes / 16;
+                most = n16[j] > most ? n16[j] : most;
+            }
+        }
+        for (size_t k = tid; k < most; k += nthreads) {
+            uint4 v[8];
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j)
+                if (k < n16[j]) v[j] = reinterpret_cast<const uint4*>(x.src[c0 + j])[k];
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j)
+                if (k < n16[j]) reinterpret_cast<uint4*>(x.dst[c0 + j])[k] = v[j];
+        }
+    }
+    // the columns not 16-byte aligned: word or byte copies
     for (uint32_t c = 0; c < x.ncols; ++c) {
         const size_t bytes = static_cast<size_t>(rows) * x.elem_bytes[c];
         const char* s = x.src[c];
         char* d = x.dst[c];
         if (((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d) | bytes) & 15) == 0) {
-            const uint4* s4 = reinterpret_cast<const uint4*>(s);
-            uint4* d4 = reinterpret_cast<uint4*>(d);
-            for (size_t k = tid; k < bytes / 16; k += nthreads) d4[k] = s4[k];
+            continue;  // copied above
         } else if (((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d) | bytes) & 3) == 0) {
             const uint32_t* s1 = reinterpret_cast<const uint32_t*>(s);
             uint32_t* d1 = reinterpret_cast<uint32_t*>(d);
@@ -146,11 +172,11 @@ __global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
     }
 }
 
-// One 16-byte unit per thread (host memory is far: keep every copy in
-// flight at once), at most four blocks of 256 per SM.
+// One 16-byte unit of each column per thread (host memory is far: keep
+// every copy in flight at once), at most four blocks of 256 per SM.
 inline unsigned int host_xfer_grid(const HostXfer& x, int sms) {
     size_t bytes = 0;
-    for (uint32_t c = 0; c < x.ncols; ++c) bytes += static_cast<size_t>(x.rows) * x.elem_bytes[c];
+    for (uint32_t c = 0; c < x.ncols; ++c) bytes = std::max(bytes, static_cast<size_t>(x.rows) * x.elem_bytes[c]);
     const size_t blocks = (bytes + 256 * 16 - 1) / (256 * 16);
     return static_cast<unsigned int>(std::max<size_t>(1, std::min<size_t>(blocks, 4u * static_cast<unsigned int>(sms))));
 }
@@ -2176,11 +2202,14 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
     }
     id_t mx = 0;
     if (idc < src.size() && n) {
+        // one branch-free pass (it vectorises): the largest id, and whether any is unset
         const id_t* ids = static_cast<const id_t*>(src[idc]);
+        uint32_t unset = 0;
         for (uint32_t i = 0; i < n; ++i) {
-            if (ids[i] == ID_NOT_SET) THROW exception::InvalidArgument("setPopulationColumns: every _id must be set");
+            unset |= ids[i] == ID_NOT_SET ? 1u : 0u;
             mx = std::max(mx, ids[i]);
         }
+        if (unset) THROW exception::InvalidArgument("setPopulationColumns: every _id must be set");
     }
     // copies are ordered after the stream's earlier work; only growing the
     // buffers needs the stream idle
@@ -2219,9 +2248,11 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
         impl->h_pinned[2] = n;
         FG_CUDA(cudaMemcpyAsync(l->d_count, impl->h_pinned + 2, sizeof(uint32_t), cudaMemcpyHostToDevice, impl->stream));
     }
-    FG_CUDA(cudaStreamSynchronize(impl->stream));
+    // the recount is queued behind the copies before the one wait (the
+    // caller's buffers are free again when this returns)
     l->bound = n;
     impl->forget_counts();
+    FG_CUDA(cudaStreamSynchronize(impl->stream));
     impl->ensure_all_allocated();
 }
 

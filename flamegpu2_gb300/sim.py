@@ -104,6 +104,9 @@ class Simulation:
     def __init__(self, model: str, params=(), device: int = 0, steps: int = 1, seed: int = 0,
                  use_graphs: bool = True, check_each_step: bool = False):
         L = core()
+        self._lib = L
+        self._name_arrays = {}
+        self._last_ptrs = {}
         arr = (C.c_double * max(1, len(params)))(*[float(p) for p in params])
         self._h = L.fgs_create(model.encode(), arr, len(params), device)
         if not self._h:
@@ -124,15 +127,36 @@ class Simulation:
     def configure(self, steps=1, seed=0, use_graphs=True, check_each_step=False):
         _check(core().fgs_configure(self._h, steps, seed, int(use_graphs), int(check_each_step)))
 
+    def _names(self, names) -> "C.Array":
+        """The C array of column names, built once per distinct tuple of names."""
+        key = tuple(names)
+        cn = self._name_arrays.get(key)
+        if cn is None:
+            cn = (C.c_char_p * max(1, len(key)))(*[k.encode() for k in key])
+            self._name_arrays[key] = cn
+        return cn
+
+    def _pointers(self, slot: str, names: tuple, arrs: list) -> "C.Array":
+        """The C array of the columns' data pointers. A call passing the same
+        (contiguous) array objects as the previous one through this slot reuses
+        its array; the slot keeps those arrays alive, so their addresses hold."""
+        last = self._last_ptrs.get(slot)
+        if last is not None and last[0] == names and len(last[1]) == len(arrs) and \
+                all(x is y for x, y in zip(last[1], arrs)):
+            return last[2]
+        cp = (C.c_void_p * max(1, len(arrs)))(*[a.ctypes.data for a in arrs])
+        self._last_ptrs[slot] = (names, arrs, cp)
+        return cp
+
     def set_population(self, agent: str, n: int, columns: dict, state: str = "default"):
-        names = list(columns)
+        names = tuple(columns)
         arrs = [np.ascontiguousarray(columns[k]) for k in names]
         for k, a in zip(names, arrs):
             if a.shape[0] != n:
                 raise ValueError(f"column {k} has {a.shape[0]} rows, expected {n}")
-        cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
-        cp = (C.c_void_p * max(1, len(names)))(*[a.ctypes.data for a in arrs])
-        _check(core().fgs_set_population(self._h, agent.encode(), state.encode(), n, len(names), cn, cp))
+        cp = self._pointers("set", names, arrs)
+        _check(self._lib.fgs_set_population(self._h, agent.encode(), state.encode(), n, len(names), self._names(names),
+                                            cp))
 
     def set_population_device(self, agent: str, n: int, columns: dict, state: str = "default"):
         """columns: name -> torch CUDA tensor (kept alive by the caller until this returns)."""
@@ -163,12 +187,16 @@ class Simulation:
 
     def get_population(self, agent: str, outs: dict, state: str = "default") -> int:
         """Fill caller arrays (name -> numpy array with room for every agent); returns the count."""
-        names = list(outs)
-        cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
-        cp = (C.c_void_p * max(1, len(names)))(*[outs[k].ctypes.data for k in names])
-        cap = min(o.shape[0] for o in outs.values())
+        names = tuple(outs)
+        arrs = [outs[k] for k in names]
+        for k, a in zip(names, arrs):
+            if not a.flags.c_contiguous:
+                raise ValueError(f"output array {k} is not contiguous")
+        cp = self._pointers("get", names, arrs)
+        cap = min(o.shape[0] for o in arrs)
         n = C.c_uint32()
-        _check(core().fgs_get_population(self._h, agent.encode(), state.encode(), len(names), cn, cp, cap, C.byref(n)))
+        _check(self._lib.fgs_get_population(self._h, agent.encode(), state.encode(), len(names), self._names(names), cp,
+                                            cap, C.byref(n)))
         return n.value
 
     def get_device(self, agent: str, var: str, dst, state: str = "default"):
@@ -177,7 +205,7 @@ class Simulation:
                                               dst.data_ptr(), dst.numel() * dst.element_size()))
 
     def step(self, n: int = 1):
-        _check(core().fgs_step(self._h, n))
+        _check(self._lib.fgs_step(self._h, n))
 
     def set_config(self, key: str, value):
         """SimulationConfig() / CUDAConfig() item by name."""
