@@ -146,12 +146,15 @@ def boids_bytes(n, bins):
     """Algorithmic bytes per launch (each stage input read once, output written once):
     message 28 B (id,x,y,z,fx,fy,fz), agent read 28 B, agent write 24 B."""
     vm, va_r, va_w = 28, 28, 24
-    return {
+    out = {
         "fn:outputdata": n * va_r + n * vm,
         "build:location": 2 * n * vm + 4 * (bins + 1),
         "fn:inputdata": n * vm + 4 * (bins + 1) + n * (va_r + va_w),
         "sort:Boid": 2 * n * 28,
     }
+    # the agent sort and the message build as one chain of paired launches
+    out["sort+build:Boid/location"] = out["sort:Boid"] + out["build:location"]
+    return out
 
 
 def workloads_mod():

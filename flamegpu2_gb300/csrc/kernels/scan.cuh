@@ -142,53 +142,53 @@ struct OrderCheck {
     uint32_t max_n = 0;
 };
 
-// The blocks share the 32-row group boundaries; unless the key launch already
-// found a descent (`pending` false), each block reads its boundaries' keys.
-__device__ __forceinline__ void order_check_boundaries(const OrderCheck& oc, bool pending, WsHeader* h) {
+// The blocks share the 32-row group boundaries (block `b` of `nb` taking part);
+// unless the key launch already found a descent (`pending` false), each block
+// reads its boundaries' keys.
+__device__ __forceinline__ void order_check_boundaries(const OrderCheck& oc, bool pending, WsHeader* h, uint32_t b,
+                                                       uint32_t nb) {
     uint32_t bad = 0u;
     if (pending) {
         const uint32_t rows = oc.d_n ? min(*oc.d_n, oc.max_n) : oc.max_n;
         const uint2* e = reinterpret_cast<const uint2*>(oc.edges);
 #pragma unroll 4
-        for (uint32_t w = 1u + blockIdx.x * blockDim.x + threadIdx.x; static_cast<uint64_t>(w) * 32u < rows;
-             w += gridDim.x * blockDim.x)
+        for (uint32_t w = 1u + b * blockDim.x + threadIdx.x; static_cast<uint64_t>(w) * 32u < rows; w += nb * blockDim.x)
             bad |= e[w - 1u].y > e[w].x ? 1u : 0u;
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) h->disorder = 1u;
 }
 
+// One exclusive scan of a launch: in[0..n) into out[0..n) on the workspace
+// header h and its tile statuses; last, last_floor and oc as k_scan_u32's.
+struct ScanJob {
+    const uint32_t* in;
+    uint32_t* out;
+    uint32_t n;
+    int zero_in;
+    uint64_t* status;
+    WsHeader* h;
+    const uint32_t* last;
+    uint32_t last_floor;
+    OrderCheck oc;
+};
+
+// Tile `tile` (of `ntiles`) of scan j, by the whole block, under the epoch the
+// block read; withhold (tile 0: a test hook) and pending (the row-order check
+// is still open) as read by thread 0. Returns false for a tile wholly past the
+// scan's last value (it only takes part in the order check).
 template <int R>
-__global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in,
-                                                       uint64_t* status, WsHeader* h, int self_reset,
-                                                       const uint32_t* last, uint32_t last_floor,
-                                                       const __grid_constant__ OrderCheck oc) {
-    flamegpu::detail::grid_dependency_enter();
-    __shared__ uint32_t s_tile, s_epoch, s_pending;
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_excl;
-    // a test hook (fg_workspace_set_wait_limit): tile 0 does not publish. Only
-    // tile 0's thread 0 reads it, before its data loads, and uses it when it
-    // publishes, so the load adds nothing to the look-back chain
-    uint32_t withhold = 0;
-    if (threadIdx.x == 0) {
-        // the key launch's flag is final (it completed before this launch):
-        // read before the acquire, so the two loads overlap
-        const bool pending = oc.edges != nullptr && h->disorder == 0u;
-        s_tile = atomicAdd(&h->scan_ticket, 1u);
-        s_epoch = ld_acquire_u32(&h->scan_epoch);
-        if (s_tile == 0) withhold = h->withhold;
-        s_pending = pending;
-    }
-    __syncthreads();
-    const uint32_t tile = s_tile, epoch = s_epoch;
-    const bool pending = s_pending != 0u;
+__device__ __forceinline__ bool scan_tile(const ScanJob& j, uint32_t tile, uint32_t ntiles, uint32_t epoch,
+                                          bool withhold, bool pending, uint32_t* s_warp, uint32_t* s_excl) {
+    uint32_t n = j.n;
     // last (no self reset): the values past index max(*last, last_floor) + 1
     // are zero and their prefixes unused; the tiles wholly past it have nothing to do
-    if (last) n = min(n, max(*last, last_floor) + 2u);
+    if (j.last) n = min(n, max(*j.last, j.last_floor) + 2u);
     if (static_cast<uint64_t>(tile) * R * kScanTile >= n && tile != 0) {
-        if (oc.edges) order_check_boundaries(oc, pending, h);
-        return;
+        if (j.oc.edges) order_check_boundaries(j.oc, pending, j.h, tile, ntiles);
+        return false;
     }
+    const uint32_t* in = j.in;
+    uint32_t* out = j.out;
     const bool in_al = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
     const bool out_al = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
     uint32_t v[kScanItems];
@@ -211,13 +211,13 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
     if (threadIdx.x < 32) {
         uint32_t excl = 0;
         if (tile == 0) {
-            if (threadIdx.x == 0 && !withhold) st_release_u64(status, scan_pack(2, epoch, ttotal));
+            if (threadIdx.x == 0 && !withhold) st_release_u64(j.status, scan_pack(2, epoch, ttotal));
         } else {
-            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(1, epoch, ttotal));
-            excl = lookback_u32(status, tile, epoch, h);
-            if (threadIdx.x == 0) st_release_u64(status + tile, scan_pack(2, epoch, excl + ttotal));
+            if (threadIdx.x == 0) st_release_u64(j.status + tile, scan_pack(1, epoch, ttotal));
+            excl = lookback_u32(j.status, tile, epoch, j.h);
+            if (threadIdx.x == 0) st_release_u64(j.status + tile, scan_pack(2, epoch, excl + ttotal));
         }
-        if (threadIdx.x == 0) s_excl = excl;
+        if (threadIdx.x == 0) *s_excl = excl;
     }
     __syncthreads();
 #pragma unroll
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
         const uint64_t base = base0 + r * kScanTile;
         const bool full = base + kScanItems <= n;
         if (R > 1) scan_load(in, base, n, in_al && full, v);  // the one sub-tile of R = 1 is still held
-        uint32_t run = s_excl + texcl[r];
+        uint32_t run = *s_excl + texcl[r];
         uint32_t o[kScanItems];
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
             for (int k = 0; k < kScanItems; ++k)
                 if (base + k < n) out[base + k] = o[k];
         }
-        if (zero_in) {
+        if (j.zero_in) {
             uint32_t* zin = const_cast<uint32_t*>(in);
             if (full && in_al) {
                 uint4* p = reinterpret_cast<uint4*>(zin + base);
@@ -255,19 +255,75 @@ __global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const uint32_t* in, ui
             }
         }
     }
-    if (oc.edges) order_check_boundaries(oc, pending, h);
+    if (j.oc.edges) order_check_boundaries(j.oc, pending, j.h, tile, ntiles);
+    return true;
+}
+
+// Thread 0: the block's tile (ticket), the scan's epoch, and the test hook
+// and order-check state. The key launch's flag is final (it completed before
+// this launch): read before the acquire, so the loads overlap.
+struct ScanTicket {
+    uint32_t tile, epoch, withhold, pending;
+};
+__device__ __forceinline__ ScanTicket scan_ticket_of(const ScanJob& j, uint32_t ticket) {
+    ScanTicket t;
+    t.pending = j.oc.edges != nullptr && j.h->disorder == 0u;
+    t.tile = ticket;
+    t.epoch = ld_acquire_u32(&j.h->scan_epoch);
+    t.withhold = ticket == 0 ? j.h->withhold : 0u;
+    return t;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kThreads, 6) k_scan_u32(const __grid_constant__ ScanJob j, int self_reset) {
+    flamegpu::detail::grid_dependency_enter();
+    __shared__ ScanTicket s_t;
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_excl;
+    // a test hook (fg_workspace_set_wait_limit): tile 0 does not publish. Only
+    // tile 0's thread 0 reads it, before its data loads, and uses it when it
+    // publishes, so the load adds nothing to the look-back chain
+    if (threadIdx.x == 0) s_t = scan_ticket_of(j, atomicAdd(&j.h->scan_ticket, 1u));
+    __syncthreads();
+    const ScanTicket t = s_t;
+    if (!scan_tile<R>(j, t.tile, gridDim.x, t.epoch, t.withhold != 0u, t.pending != 0u, s_warp, &s_excl)) return;
     if (!self_reset) return;
     // the last block to finish resets the ticket and advances the epoch
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(&h->scan_done, 1u) == gridDim.x - 1) {
-            h->scan_ticket = 0;
-            h->scan_done = 0;
-            atomicExch(&h->scan_epoch, (epoch + 1) & 0x3FFFFFFFu);
+        if (atomicAdd(&j.h->scan_done, 1u) == gridDim.x - 1) {
+            j.h->scan_ticket = 0;
+            j.h->scan_done = 0;
+            atomicExch(&j.h->scan_epoch, (t.epoch + 1) & 0x3FFFFFFFu);
             __threadfence();
         }
     }
+}
+
+// Two scans in one launch (an agent sort's and a message build's): tickets
+// below `tiles_a` are scan a's tiles, the rest scan b's, so each tile still
+// waits only on lower tickets of its own scan. The tickets come from a's
+// header (reset by the launch before, as for a single scan); no self reset.
+template <int R>
+__global__ void __launch_bounds__(kThreads, 6) k_scan_pair(const __grid_constant__ ScanJob a,
+                                                           const __grid_constant__ ScanJob b, uint32_t tiles_a) {
+    flamegpu::detail::grid_dependency_enter();
+    __shared__ ScanTicket s_t;
+    __shared__ uint32_t s_in_b;
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_excl;
+    if (threadIdx.x == 0) {
+        const uint32_t ticket = atomicAdd(&a.h->scan_ticket, 1u);
+        s_in_b = ticket >= tiles_a;
+        s_t = ticket < tiles_a ? scan_ticket_of(a, ticket) : scan_ticket_of(b, ticket - tiles_a);
+    }
+    __syncthreads();
+    const ScanTicket t = s_t;
+    if (s_in_b)
+        scan_tile<R>(b, t.tile, gridDim.x - tiles_a, t.epoch, t.withhold != 0u, t.pending != 0u, s_warp, &s_excl);
+    else
+        scan_tile<R>(a, t.tile, tiles_a, t.epoch, t.withhold != 0u, t.pending != 0u, s_warp, &s_excl);
 }
 
 // Tiles of a scan of n values with one sub-tile per tile (an upper bound on
@@ -283,11 +339,19 @@ inline thread_local uint32_t t_scan_wide_min = kScanWideMin;
 inline cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, int zero_in, uint64_t* status,
                                WsHeader* h, int self_reset, cudaStream_t st, const uint32_t* last = nullptr,
                                uint32_t last_floor = 0, const OrderCheck& oc = OrderCheck()) {
+    const ScanJob j{in, out, n, zero_in, status, h, last, last_floor, oc};
     if (n > t_scan_wide_min)
-        return launch(k_scan_u32<4>, (n + 4u * kScanTile - 1) / (4u * kScanTile), kThreads, st, in, out, n, zero_in,
-                      status, h, self_reset, last, last_floor, oc);
-    return launch(k_scan_u32<1>, scan_tiles(n), kThreads, st, in, out, n, zero_in, status, h, self_reset, last,
-                  last_floor, oc);
+        return launch(k_scan_u32<4>, (n + 4u * kScanTile - 1) / (4u * kScanTile), kThreads, st, j, self_reset);
+    return launch(k_scan_u32<1>, scan_tiles(n), kThreads, st, j, self_reset);
+}
+
+// Scans a and b (no self reset) in one launch; both take four sub-tiles per
+// tile when either is wide.
+inline cudaError_t launch_scan_pair(const ScanJob& a, const ScanJob& b, cudaStream_t st) {
+    const uint32_t r = (a.n > t_scan_wide_min || b.n > t_scan_wide_min) ? 4u : 1u;
+    const uint32_t ta = (a.n + r * kScanTile - 1) / (r * kScanTile), tb = (b.n + r * kScanTile - 1) / (r * kScanTile);
+    if (r == 4u) return launch(k_scan_pair<4>, ta + tb, kThreads, st, a, b, ta);
+    return launch(k_scan_pair<1>, ta + tb, kThreads, st, a, b, ta);
 }
 
 }  // namespace fgk

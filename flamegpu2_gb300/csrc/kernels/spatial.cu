@@ -182,23 +182,47 @@ __global__ void __launch_bounds__(kThreads) k_bin_batched(const fg_batch_instanc
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_perm(uint32_t max_n, const uint32_t* d_n,
-                                                   const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
-                                                   const uint32_t* __restrict__ pbm, uint32_t* __restrict__ perm,
-                                                   WsHeader* h) {
-    flamegpu::detail::grid_dependency_enter();
-    if (h->disorder == 0u) return;  // keys in row order: every row keeps its place
-    const uint32_t n = load_count(d_n, max_n);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t k = keys[i];
+// One counting sort's placement: perm[PBM[key] + slot] = row.
+struct PermJob {
+    uint32_t max_n;
+    const uint32_t* d_n;
+    const uint32_t* keys;
+    const uint32_t* slot;
+    const uint32_t* pbm;
+    uint32_t* perm;
+    WsHeader* h;
+};
+
+// By block b of the nb blocks working on job j.
+__device__ __forceinline__ void perm_rows(const PermJob& j, uint32_t b, uint32_t nb) {
+    if (j.h->disorder == 0u) return;  // keys in row order: every row keeps its place
+    const uint32_t n = load_count(j.d_n, j.max_n);
+    for (uint32_t i = b * blockDim.x + threadIdx.x; i < n; i += nb * blockDim.x) {
+        const uint32_t k = j.keys[i];
         if (k != kInvalid) {
-            const uint32_t at = pbm[k & ~kPadBit] + slot[i];
+            const uint32_t at = j.pbm[k & ~kPadBit] + j.slot[i];
             if (at < n)
-                perm[at] = i;
+                j.perm[at] = i;
             else
-                record_status(h, FG_ERR_WORKSPACE);
+                record_status(j.h, FG_ERR_WORKSPACE);
         }
     }
+}
+
+__global__ void __launch_bounds__(kThreads) k_perm(const __grid_constant__ PermJob j) {
+    flamegpu::detail::grid_dependency_enter();
+    perm_rows(j, blockIdx.x, gridDim.x);
+}
+
+// an agent sort's placement (the first ga blocks) and a message build's (the
+// rest), in one launch: the two run side by side as two kernels would
+__global__ void __launch_bounds__(kThreads) k_perm_pair(const __grid_constant__ PermJob a,
+                                                        const __grid_constant__ PermJob b, uint32_t ga) {
+    flamegpu::detail::grid_dependency_enter();
+    if (blockIdx.x < ga)
+        perm_rows(a, blockIdx.x, ga);
+    else
+        perm_rows(b, blockIdx.x - ga, gridDim.x - ga);
 }
 
 struct RecordParams {
@@ -369,36 +393,48 @@ __device__ __forceinline__ void emit_run(const EmitParams& ep, uint32_t* sperm, 
     }
 }
 
+// What the stabilising and long-bin kernels of one counting sort read and
+// write: the emission, the keys, PBM and unstable placement, the stable
+// permutation (agent sorts), the long-bin chunk queue, the workspace header,
+// and for agent sorts the recorded largest key (key_max) and its floor.
+struct StabJob {
+    EmitParams rp;
+    uint32_t nbuckets;
+    const uint32_t* keys;
+    const uint32_t* pbm;
+    const uint32_t* perm;
+    uint32_t* sperm;
+    uint2* chunk_list;
+    uint32_t chunk_cap;
+    WsHeader* h;
+    uint32_t* key_max;
+    uint32_t key_floor;
+    uint32_t max_n;
+};
+
 // Sorted positions p < total = pbm[nbuckets] (for an agent sort, whose scan
 // stopped past max(recorded key, cells - 1), the PBM entry after that). Short bins are ranked in place
 // (count of smaller original indices in the bin); long bins are queued as
 // chunks (bucket, chunk index) for k_long.
 template <int EMIT>
-__global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ EmitParams rp, uint32_t nbuckets,
-                                                        const uint32_t* __restrict__ keys,
-                                                        const uint32_t* __restrict__ pbm,
-                                                        const uint32_t* __restrict__ perm, uint32_t* sperm,
-                                                        uint2* chunk_list, uint32_t chunk_cap, WsHeader* h,
-                                                        const uint32_t* key_max, uint32_t key_floor, uint32_t max_n) {
-    flamegpu::detail::grid_dependency_enter();
+__device__ __forceinline__ void stabilize_positions(const StabJob& j, uint32_t blk, uint32_t nblk) {
     // key_max (agent sorts): the PBM ends at max(recorded key, key_floor) + 1
-    const uint32_t total = pbm[key_max ? min(nbuckets, max(*key_max, key_floor) + 1u) : nbuckets];
-    if (h->disorder == 0u) {
+    const uint32_t total = j.pbm[j.key_max ? min(j.nbuckets, max(*j.key_max, j.key_floor) + 1u) : j.nbuckets];
+    if (j.h->disorder == 0u) {
         // keys in row order (the key launch and the scan found no descent):
         // the stable order is the row order, so rows are emitted in place, as
         // one run over the grid's threads (four rows in flight per thread)
-        emit_run<EMIT>(rp, sperm, 0u, 0u, min(total, max_n), blockIdx.x * blockDim.x + threadIdx.x,
-                       gridDim.x * blockDim.x);
+        emit_run<EMIT>(j.rp, j.sperm, 0u, 0u, min(total, j.max_n), blk * blockDim.x + threadIdx.x, nblk * blockDim.x);
         return;
     }
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
-        const uint32_t i = perm[p];
-        const uint32_t b = keys[i];
+    for (uint32_t p = blk * blockDim.x + threadIdx.x; p < total; p += nblk * blockDim.x) {
+        const uint32_t i = j.perm[p];
+        const uint32_t b = j.keys[i];
         if (b & kPadBit) {  // padding row of a batch: keeps its slot, carries no message
-            if (EMIT != kEmitRecord) sperm[p] = i;
+            if (EMIT != kEmitRecord) j.sperm[p] = i;
             continue;
         }
-        const uint32_t s = pbm[b], e = pbm[b + 1];
+        const uint32_t s = j.pbm[b], e = j.pbm[b + 1];
         // a PBM from a scan whose look-back gave up (FG_ERR_DEVICE_TIMEOUT
         // recorded) may run backwards: such a bin is skipped, so no bin is
         // queued or ranked past the messages (entries never exceed their count)
@@ -407,19 +443,37 @@ __global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ 
         if (len > kShortBin) {
             if (p == s) {
                 const uint32_t nch = (len + kChunk - 1) / kChunk;
-                const uint32_t at = atomicAdd(&h->long_count, nch);
+                const uint32_t at = atomicAdd(&j.h->long_count, nch);
                 for (uint32_t c = 0; c < nch; ++c)
-                    if (at + c < chunk_cap) chunk_list[at + c] = make_uint2(b, c);
-                if (at + nch > chunk_cap) record_status(h, FG_ERR_CAPACITY);
+                    if (at + c < j.chunk_cap) j.chunk_list[at + c] = make_uint2(b, c);
+                if (at + nch > j.chunk_cap) record_status(j.h, FG_ERR_CAPACITY);
             }
             continue;
         }
         uint32_t dst = s;
         if (len > 1) {
-            for (uint32_t q = s; q < e; ++q) dst += (perm[q] < i) ? 1u : 0u;
+            for (uint32_t q = s; q < e; ++q) dst += (j.perm[q] < i) ? 1u : 0u;
         }
-        emit<EMIT>(rp, sperm, i, dst);
+        emit<EMIT>(j.rp, j.sperm, i, dst);
     }
+}
+
+template <int EMIT>
+__global__ void __launch_bounds__(kThreads) k_stabilize(const __grid_constant__ StabJob j) {
+    flamegpu::detail::grid_dependency_enter();
+    stabilize_positions<EMIT>(j, blockIdx.x, gridDim.x);
+}
+
+// an agent sort's stable positions (EA, the first ga blocks) and a message
+// build's (EB, the rest), in one launch
+template <int EA, int EB>
+__global__ void __launch_bounds__(kThreads) k_stabilize_pair(const __grid_constant__ StabJob a,
+                                                             const __grid_constant__ StabJob b, uint32_t ga) {
+    flamegpu::detail::grid_dependency_enter();
+    if (blockIdx.x < ga)
+        stabilize_positions<EA>(a, blockIdx.x, ga);
+    else
+        stabilize_positions<EB>(b, blockIdx.x - ga, gridDim.x - ga);
 }
 
 // Long bins. A bin of up to kSortCap messages is ordered by one block (the
@@ -445,32 +499,33 @@ constexpr uint32_t kWarpBin = 1024;
 constexpr uint32_t kWarpSpanWords = 128;
 static_assert((kThreads / 32) * kWarpBin <= kSortCap, "a warp's bitonic slice lies in s_idx");
 
+// Shared memory of the long-bin pass.
+struct LongSmem {
+    uint32_t idx[kSortCap];
+    uint32_t warp[33];
+    uint32_t lo, hi;
+    uint32_t wbits[kThreads / 32][kWarpSpanWords];
+    uint32_t wpre[kThreads / 32][kWarpSpanWords];
+};
+
 template <int EMIT>
-__global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitParams rp,
-                                                   const uint32_t* __restrict__ pbm,
-                                                   const uint32_t* __restrict__ perm, uint32_t* sperm,
-                                                   const uint2* __restrict__ chunk_list, uint32_t chunk_cap,
-                                                   WsHeader* h, uint32_t* key_max_reset) {
-    flamegpu::detail::grid_dependency_enter();
-    // the last kernel of an agent sort: the largest key is no longer read;
-    // the last of any build: the order flag is no longer read (the next key
-    // launch raises it again where its keys descend)
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (key_max_reset) *key_max_reset = 0u;
-        h->disorder = 0u;
-    }
-    __shared__ uint32_t s_idx[kSortCap];
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_lo, s_hi;
-    __shared__ uint32_t s_wbits[kThreads / 32][kWarpSpanWords];
-    __shared__ uint32_t s_wpre[kThreads / 32][kWarpSpanWords];
-    const uint32_t nchunks = min(h->long_count, chunk_cap);
+__device__ __forceinline__ void long_bins(const StabJob& job, LongSmem& sm, uint32_t blk, uint32_t nblk) {
+    const EmitParams& rp = job.rp;
+    const uint32_t* __restrict__ pbm = job.pbm;
+    const uint32_t* __restrict__ perm = job.perm;
+    uint32_t* sperm = job.sperm;
+    const uint2* __restrict__ chunk_list = job.chunk_list;
+    uint32_t* s_idx = sm.idx;
+    uint32_t* s_warp = sm.warp;
+    uint32_t& s_lo = sm.lo;
+    uint32_t& s_hi = sm.hi;
+    const uint32_t nchunks = min(job.h->long_count, job.chunk_cap);
     // warp pass: bins of up to kWarpBin messages
     {
         const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
-        uint32_t* bits = s_wbits[wib];
-        uint32_t* pre = s_wpre[wib];
-        for (uint32_t c = blockIdx.x * (kThreads / 32) + wib; c < nchunks; c += gridDim.x * (kThreads / 32)) {
+        uint32_t* bits = sm.wbits[wib];
+        uint32_t* pre = sm.wpre[wib];
+        for (uint32_t c = blk * (kThreads / 32) + wib; c < nchunks; c += nblk * (kThreads / 32)) {
             const uint2 ch = chunk_list[c];
             const uint32_t s = pbm[ch.x], e = pbm[ch.x + 1];
             const uint32_t len = e - s;
@@ -551,7 +606,7 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
         }
     }
     // block pass: longer bins
-    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    for (uint32_t c = blk; c < nchunks; c += nblk) {
         const uint2 ch = chunk_list[c];
         const uint32_t s = pbm[ch.x], e = pbm[ch.x + 1];
         const uint32_t len = e - s;
@@ -658,6 +713,39 @@ __global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ EmitP
     }
 }
 
+template <int EMIT>
+__global__ void __launch_bounds__(kThreads) k_long(const __grid_constant__ StabJob j) {
+    flamegpu::detail::grid_dependency_enter();
+    // the last kernel of an agent sort: the largest key is no longer read;
+    // the last of any build: the order flag is no longer read (the next key
+    // launch raises it again where its keys descend)
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (j.key_max) *j.key_max = 0u;
+        j.h->disorder = 0u;
+    }
+    __shared__ LongSmem sm;
+    long_bins<EMIT>(j, sm, blockIdx.x, gridDim.x);
+}
+
+// an agent sort's long bins (EA) and a message build's (EB), in one launch
+template <int EA, int EB>
+__global__ void __launch_bounds__(kThreads) k_long_pair(const __grid_constant__ StabJob a,
+                                                        const __grid_constant__ StabJob b, uint32_t ga) {
+    flamegpu::detail::grid_dependency_enter();
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.key_max) *a.key_max = 0u;
+        a.h->disorder = 0u;
+        if (b.key_max) *b.key_max = 0u;
+        b.h->disorder = 0u;
+    }
+    __shared__ LongSmem sm;
+    // the first ga blocks take a's long bins, the rest b's
+    if (blockIdx.x < ga)
+        long_bins<EA>(a, sm, blockIdx.x, ga);
+    else
+        long_bins<EB>(b, sm, blockIdx.x - ga, gridDim.x - ga);
+}
+
 // ------------------------------------------------------------------- host side
 
 struct BuildLayout {
@@ -718,6 +806,12 @@ uint32_t grid_for(uint32_t max_n, int per_sm = 8) {
     const uint32_t need = (max_n + kThreads - 1) / kThreads;
     const uint32_t cap = static_cast<uint32_t>(sm_count() * per_sm);
     return std::max(1u, std::min(need, cap));
+}
+
+// a long bin has more than 32 rows and a chunk 256: one block per 128 rows
+// covers every chunk of a small list at once; large lists get 4 per SM
+uint32_t long_grid_for(uint32_t max_n) {
+    return std::max(1u, std::min((max_n + 127u) / 128u, static_cast<uint32_t>(sm_count() * 4)));
 }
 
 int check_launch() {
@@ -837,13 +931,10 @@ int run_pipeline(const fg_spatial_grid* g, const SortGrid& sg, uint32_t nbuckets
     // the scan also compares the keys of rows 32w - 1 and 32w (row order; a batch's keys are never in it)
     const OrderCheck oc{batch.inst ? nullptr : edges, d_n, max_n};
     launch_scan(hist, pbm_out, scan_n, 1, sstat, h, 0, st, key_max, key_floor, oc);
-    launch(k_perm, grid, kThreads, st, max_n, d_n, keys, slot, pbm_out, perm, h);
-    launch(k_stabilize<EMIT>, grid, kThreads, st, rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h,
-           static_cast<const uint32_t*>(key_max), key_floor, max_n);
-    // a long bin has more than 32 rows and a chunk 256: one block per 128 rows
-    // covers every chunk of a small list at once; large lists get 4 per SM
-    const uint32_t long_grid = std::max(1u, std::min((max_n + 127u) / 128u, static_cast<uint32_t>(sm_count() * 4)));
-    launch(k_long<EMIT>, long_grid, kThreads, st, rp, pbm_out, perm, sperm, chunks, L.chunk_cap, h, key_max);
+    launch(k_perm, grid, kThreads, st, PermJob{max_n, d_n, keys, slot, pbm_out, perm, h});
+    const StabJob sj{rp, nbuckets, keys, pbm_out, perm, sperm, chunks, L.chunk_cap, h, key_max, key_floor, max_n};
+    launch(k_stabilize<EMIT>, grid, kThreads, st, sj);
+    launch(k_long<EMIT>, long_grid_for(max_n), kThreads, st, sj);
     return check_launch();
 }
 
@@ -905,6 +996,63 @@ int fgi_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint
     if (perm_out && max_n) {
         cudaMemcpyAsync(perm_out, sperm, sizeof(uint32_t) * max_n, cudaMemcpyDeviceToDevice, st);
     }
+    return check_launch();
+}
+
+// The automatic agent sort of a list and the index build of the spatial
+// messages it output, both on the message list's grid, as one pipeline of
+// paired launches (scan, placement, stable positions, long bins, each doing
+// both sorts): one chain of four kernels instead of two concurrent chains
+// joined before the function that reads the messages. The launch before
+// wrote both key sets (keys_ready for both). Results are those of
+// fgi_spatial_sort_agents and fgi_spatial_build run one after the other.
+int fgi_spatial_sort_and_build(const fg_spatial_grid* g, uint32_t sort_max_n, const uint32_t* sort_d_n,
+                               const fg_column* cols, uint32_t ncols, void* sort_ws, size_t sort_ws_bytes,
+                               uint32_t msg_max_n, const uint32_t* msg_d_n, const fg_record_desc* rec,
+                               uint32_t* sorted, uint32_t* pbm, void* build_ws, size_t build_ws_bytes, void* stream) {
+    if (!g || (g->dims != 2 && g->dims != 3) || !cols || ncols == 0 || ncols > FG_MAX_COLUMNS) return FG_ERR_INVALID_ARGUMENT;
+    if (!rec || !pbm || !sort_ws || !build_ws) return FG_ERR_INVALID_ARGUMENT;
+    if (rec->words == 0 || (rec->words & 3) || rec->words > FG_MAX_RECORD_WORDS) return FG_ERR_INVALID_ARGUMENT;
+    if ((msg_max_n && !sorted) || (reinterpret_cast<uintptr_t>(sorted) & 15)) return FG_ERR_INVALID_ARGUMENT;
+    SortGrid sg{};
+    uint32_t nb = 0;
+    if (!sort_grid_from(g, &sg, &nb)) return FG_ERR_UNSUPPORTED;
+    const BuildLayout La = build_layout(sort_max_n, nb, true);
+    const BuildLayout Lb = build_layout(msg_max_n, g->binCount, false);
+    if (sort_ws_bytes < La.total || (reinterpret_cast<uintptr_t>(sort_ws) & 255)) return FG_ERR_WORKSPACE;
+    if (build_ws_bytes < Lb.total || (reinterpret_cast<uintptr_t>(build_ws) & 255)) return FG_ERR_WORKSPACE;
+    char* wa = static_cast<char*>(sort_ws);
+    char* wb = static_cast<char*>(build_ws);
+    WsHeader* ha = reinterpret_cast<WsHeader*>(wa);
+    WsHeader* hb = reinterpret_cast<WsHeader*>(wb);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto at = [](char* w, size_t off) { return reinterpret_cast<uint32_t*>(w + off); };
+    EmitParams ea{};
+    for (uint32_t c = 0; c < ncols; ++c) ea.cp.col[c] = cols[c];
+    ea.cp.ncols = ncols;
+    ea.cp.keep_perm = 0;
+    EmitParams eb{};
+    eb.rp.rec = *rec;
+    eb.rp.out = sorted;
+    uint32_t* pbm_a = at(wa, La.pbm);
+    const uint32_t key_floor = flamegpu::detail::sort_cells(sg) - 1u;
+    const ScanJob sa{at(wa, La.hist), pbm_a, nb + 1, 1, reinterpret_cast<uint64_t*>(wa + La.scan_status), ha,
+                     &ha->key_max, key_floor, OrderCheck{at(wa, La.edges), sort_d_n, sort_max_n}};
+    const ScanJob sb{at(wb, Lb.hist), pbm, g->binCount + 1, 1, reinterpret_cast<uint64_t*>(wb + Lb.scan_status), hb,
+                     nullptr, 0, OrderCheck{at(wb, Lb.edges), msg_d_n, msg_max_n}};
+    launch_scan_pair(sa, sb, st);
+    // each launch gives each sort the blocks its own kernel would have
+    const uint32_t ga = grid_for(sort_max_n), gb = grid_for(msg_max_n);
+    launch(k_perm_pair, ga + gb, kThreads, st, PermJob{sort_max_n, sort_d_n, at(wa, La.keys), at(wa, La.slot), pbm_a,
+                                                       at(wa, La.perm), ha},
+           PermJob{msg_max_n, msg_d_n, at(wb, Lb.keys), at(wb, Lb.slot), pbm, at(wb, Lb.perm), hb}, ga);
+    const StabJob ja{ea, nb, at(wa, La.keys), pbm_a, at(wa, La.perm), at(wa, La.sperm),
+                     reinterpret_cast<uint2*>(wa + La.chunks), La.chunk_cap, ha, &ha->key_max, key_floor, sort_max_n};
+    const StabJob jb{eb, g->binCount, at(wb, Lb.keys), pbm, at(wb, Lb.perm), nullptr,
+                     reinterpret_cast<uint2*>(wb + Lb.chunks), Lb.chunk_cap, hb, nullptr, 0, msg_max_n};
+    launch(k_stabilize_pair<kEmitPermColumns, kEmitRecord>, ga + gb, kThreads, st, ja, jb, ga);
+    const uint32_t la = long_grid_for(sort_max_n), lb = long_grid_for(msg_max_n);
+    launch(k_long_pair<kEmitPermColumns, kEmitRecord>, la + lb, kThreads, st, ja, jb, la);
     return check_launch();
 }
 

@@ -68,5 +68,12 @@ int fgi_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint
                             const float* y, const float* z, const fg_column* cols, uint32_t ncols, uint32_t* perm_out,
                             void* workspace, size_t workspace_bytes, void* stream, bool keys_ready,
                             uint32_t pos_stride = 1);
+// The agent sort of a list and the build of the spatial messages it output
+// on the same grid, as one chain of paired launches (both key sets written by
+// the launch before).
+int fgi_spatial_sort_and_build(const fg_spatial_grid* g, uint32_t sort_max_n, const uint32_t* sort_d_n,
+                               const fg_column* cols, uint32_t ncols, void* sort_ws, size_t sort_ws_bytes,
+                               uint32_t msg_max_n, const uint32_t* msg_d_n, const fg_record_desc* rec,
+                               uint32_t* sorted, uint32_t* pbm, void* build_ws, size_t build_ws_bytes, void* stream);
 int fgi_key_target(const fg_spatial_grid* g, uint32_t max_n, bool sort_mode, void* workspace, size_t workspace_bytes,
                    flamegpu::detail::KeyTarget* t);

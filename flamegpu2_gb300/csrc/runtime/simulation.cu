@@ -1077,6 +1077,21 @@ struct SimulationImpl {
         return on;
     }
 
+    // An agent sort and the build of the messages its function reads, both
+    // keyed by the launch before, can run as one chain of paired launches
+    // (fgi_spatial_sort_and_build: four kernels instead of two concurrent
+    // chains of four joined before the function). Measured on the 16,384-agent
+    // Boids step the paired chain took 38.0 us a step against 37.1 us for the
+    // two branches (each paired launch waits for the slower of its two sorts),
+    // so the branches stay the default; FLAMEGPU_PAIR_SORT_BUILD=1 pairs them.
+    static bool pair_sort_build_enabled() {
+        static const bool on = [] {
+            const char* e = std::getenv("FLAMEGPU_PAIR_SORT_BUILD");
+            return e && e[0] == '1';
+        }();
+        return on;
+    }
+
     // Which launches compute the keys of the message build and the agent sort
     // that follow them, so that those pipelines skip their key kernel. A
     // launch f qualifies for the build of its spatial output list m when m is
@@ -1182,7 +1197,9 @@ struct SimulationImpl {
         kernel_counter += f.sort_keyed ? 4 : 5;
     }
 
-    void enqueue_build(MsgList& m, cudaStream_t st, bool keys_ready = false) {
+    // The record layout of a message list's sorted records: each record word's
+    // source column, stride and word.
+    static fg_record_desc record_desc_of(const MsgList& m) {
         fg_record_desc rec;
         std::memset(&rec, 0, sizeof(rec));
         rec.words = m.record_words;
@@ -1195,6 +1212,29 @@ struct SimulationImpl {
                 rec.src_word[w] = k;
             }
         }
+        return rec;
+    }
+
+    // f's agent sort and its input's build as one chain (both keyed).
+    void enqueue_sort_and_build(FnRt& f) {
+        AgentList& l = *f.list;
+        MsgList& m = *f.in;
+        auto it = l.sort_ws.find(f.in);
+        if (it == l.sort_ws.end()) THROW exception::InvalidOperation("Sort workspace missing (not allocated before capture)");
+        std::vector<fg_column> cols(l.cols.size());
+        for (size_t v = 0; v < l.cols.size(); ++v)
+            cols[v] = fg_column{l.cols[v][l.parity], l.cols[v][l.parity ^ 1], l.agent->variables[v].bytes()};
+        const fg_record_desc rec = record_desc_of(m);
+        FG_CAPI(fgi_spatial_sort_and_build(&m.grid, l.capacity, l.d_count, cols.data(), static_cast<uint32_t>(cols.size()),
+                                           it->second.first, it->second.second, m.capacity, m.d_count, &rec, m.records,
+                                           m.pbm, m.build_ws, m.build_ws_bytes, stream));
+        l.parity ^= 1;
+        m.needs_build = false;
+        kernel_counter += 4;
+    }
+
+    void enqueue_build(MsgList& m, cudaStream_t st, bool keys_ready = false) {
+        const fg_record_desc rec = record_desc_of(m);
         const int dims = m.grid.dims;
         const int xi = 0, yi = 1, zi = 2;  // x, y, z are the first message variables
         FG_CAPI(fgi_spatial_build(&m.grid, m.capacity, m.d_count, static_cast<const float*>(m.cols[xi]),
@@ -1248,7 +1288,9 @@ struct SimulationImpl {
         if (f.sort_trigger && l.agent->sort_period != 0 && step_count % l.agent->sort_period == 0)
             do_sort = true;
         const bool do_build = f.in && f.in->spatial() && f.in->needs_build;
-        if (do_sort && do_build && cuda_config.inLayerConcurrency && !profiling) {
+        if (do_sort && do_build && f.sort_keyed && f.build_keyed && pair_sort_build_enabled()) {
+            timed("sort+build:" + l.agent->name + "/" + f.in->msg->name, [&] { enqueue_sort_and_build(f); });
+        } else if (do_sort && do_build && cuda_config.inLayerConcurrency && !profiling) {
             // the agent sort and the message index build touch disjoint buffers:
             // two branches of the step graph (fork/join through events)
             FG_CUDA(cudaEventRecord(fork_ev, stream));

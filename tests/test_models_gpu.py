@@ -238,7 +238,9 @@ def test_operation_times_from_step_graphs():
         s.close()
         if timed:
             assert st["graph_launches"] == 4
-            for label in ("fn:outputdata", "fn:inputdata", "sort:Boid", "build:location"):
+            paired = os.environ.get("FLAMEGPU_PAIR_SORT_BUILD") == "1" and os.environ.get("FLAMEGPU_FUSE_KEYS") != "0"
+            middle = ("sort+build:Boid/location",) if paired else ("sort:Boid", "build:location")
+            for label in ("fn:outputdata", "fn:inputdata") + middle:
                 assert label in prof and prof[label][1] >= 2 and prof[label][0] > 0.0, (label, prof)
         else:
             assert prof == {}
@@ -340,7 +342,8 @@ def test_population_through_page_locked_buffers(n):
 def test_key_kernels_fused_into_the_output_launch():
     # Boids step: outputdata, agent sort (5 kernels), message build (5),
     # inputdata, step end = 13 kernels; the output launch computing both key
-    # sets saves the two key kernels
+    # sets saves the two key kernels (11), and the sort and build then run as
+    # one chain of four paired launches (7)
     from flamegpu2_gb300 import synth
     S = _sim()
     cfg = dict(synth.BOIDS_SMALL, n=2000, seed=4)
@@ -350,7 +353,26 @@ def test_key_kernels_fused_into_the_output_launch():
     s.synchronize()
     k = s.stats()["kernels_per_step"]
     s.close()
-    assert k == (13 if os.environ.get("FLAMEGPU_FUSE_KEYS") == "0" else 11), k
+    if os.environ.get("FLAMEGPU_FUSE_KEYS") == "0":
+        assert k == 13, k
+    else:
+        assert k == (7 if os.environ.get("FLAMEGPU_PAIR_SORT_BUILD") == "1" else 11), k
+
+
+def test_parity_holds_with_sort_and_build_paired():
+    # The agent sort and the message build run as two graph branches by
+    # default; as one chain of paired launches (FLAMEGPU_PAIR_SORT_BUILD=1)
+    # the bit-exact checks hold the same
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FLAMEGPU_PAIR_SORT_BUILD="1")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-p", "no:cacheprovider", "-m", "gpu",
+                        os.path.join(root, "tests", "test_models_gpu.py"), os.path.join(root, "tests", "test_payload_gpu.py"),
+                        "-k", "boids_small_matches_oracle or boids_clamped or key_kernels or rows_in_bin_order"],
+                       cwd=root, env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert "7 passed" in r.stdout, r.stdout[-2000:]
 
 
 def test_steps_replayed_as_one_graph_match_single_steps():
