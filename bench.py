@@ -310,6 +310,10 @@ def run_boids_small(args, world, rank, local):
     }
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_boids(cfg, threads=1, budget_s=args.cpu_budget)
+    if world == 1 and not args.no_extras:
+        # the metric's other halves (ensemble agent-steps/s, served p50/p99 vs
+        # the plain path), after the timed region, in reduced form
+        out.update(workloads_mod().headline_extras(local))
     return out
 
 
@@ -378,6 +382,8 @@ def main():
                     choices=["boids_small", "birth_death", "spatial3d_large", "spatial2d_large", "ensemble", "served"])
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default line: skip the reduced ensemble and served summaries")
     ap.add_argument("--stage-bytes", type=int, default=None,
                     help="shared memory per block for spatial neighbour staging (0 disables)")
     args = ap.parse_args()

@@ -510,7 +510,8 @@ def run_served(args, world, rank, local):
     B = _bench_common()
     torch.cuda.set_device(local)
     count = max(8, min(int(os.environ.get("FG_SERVED_REQUESTS", "32")), 256))
-    rates = [float(r) for r in os.environ.get("FG_SERVED_RATES", "10,30,100,300,1000").split(",")]
+    rates = getattr(args, "served_rates", None) or \
+        [float(r) for r in os.environ.get("FG_SERVED_RATES", "10,30,100,300,1000").split(",")]
     reqs = _served_requests(count, 4 + 1000 * rank)
     # warm-up: a few small runs through both paths
     for _ in range(args.warmup):
@@ -624,3 +625,31 @@ def run(name, args, world, rank, local):
     if name in ("spatial3d_large", "spatial2d_large"):
         return run_spatial_large(name, args, world, rank, local)
     raise SystemExit(f"unknown workload {name}")
+
+
+def headline_extras(local):
+    """The ensemble and serving halves of the headline metric ("ensemble
+    agent-steps/s + p50/p99 vs plain"), in reduced form for the default bench
+    line: one timed pass of the 256-instance batched Boids ensemble (with its
+    fixed-shape and sequential plain-path counterparts), and the 32-request
+    served stream at 1,000 requests/s (with the sequential plain path on the
+    same arrivals). The full lines are the `ensemble` and `served` workloads."""
+    import types
+    a = types.SimpleNamespace(steps=1, warmup=1, no_cpu_baseline=True, served_rates=[1000.0])
+    e = run_ensemble(a, 1, 0, local)
+    v = run_served(a, 1, 0, local)
+    rate = v["config"]["rates"][-1]
+    ec = e["config"]
+    return {
+        "ensemble": {"workload": ec["workload"], "value": e["value"], "unit": UNIT, "e2e": e["e2e"]["value"],
+                     "ms_per_model_step": round(e["ms_per_step"] / ec["model_steps"], 3),
+                     "sequential_plain_path": ec["sequential_plain_path"]["value"],
+                     "speedup_vs_sequential": ec["speedup_vs_sequential"],
+                     "e2e_speedup_vs_sequential": ec["e2e_speedup_vs_sequential"],
+                     "tuned_over_fixed": ec["tuned_over_fixed"], "timed_passes": e["steps"]},
+        "served": {"workload": v["config"]["workload"], "rate_req_s": rate["rate_req_s"],
+                   "value": rate["throughput"], "unit": UNIT,
+                   "agent_steps": v["config"]["agent_steps"], "p50_s": rate["p50_s"], "p99_s": rate["p99_s"],
+                   "sequential_plain_path": rate["sequential"],
+                   "speedup_vs_sequential": round(rate["throughput"] / rate["sequential"]["throughput"], 2)},
+    }
