@@ -117,6 +117,11 @@ struct HostXfer {
     const uint32_t* word_src[kHostXferWords];  // get: status words copied to word_dst
     uint32_t* word_dst[kHostXferWords];
     uint32_t nwords;
+    // set: acc[1] = the sum of every list's count (rows_out's new value among
+    // them), as k_recount does after a population is set; acc null: none
+    const uint32_t* counts[kStepEndCounts];
+    uint32_t ncounts;
+    unsigned long long* acc;
 };
 
 __global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
@@ -126,6 +131,11 @@ __global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
     if (tid == 0) {
         if (x.rows_out) *x.rows_out = x.d_rows ? *x.d_rows : rows;
         if (x.max_target) *x.max_target = *x.max_target > x.max_value ? *x.max_target : x.max_value;
+        if (x.acc) {  // after rows_out: the same thread's store is visible to its loads
+            unsigned long long c = 0;
+            for (uint32_t k = 0; k < x.ncounts; ++k) c += *x.counts[k];
+            x.acc[1] = c;
+        }
     }
     if (tid < x.nwords) *x.word_dst[tid] = *x.word_src[tid];
     // columns eight at a time: the 16-byte pieces of all eight are loaded
@@ -892,8 +902,8 @@ struct SimulationImpl {
 
     // Populations were replaced from the host: earlier reports no longer apply,
     // and the agents entering the next step are counted again.
-    void forget_counts() {
-        recount();
+    void forget_counts(bool recounted = false) {
+        if (!recounted) recount();
         for (auto& c : count_ring) {
             if (c.used) cudaEventSynchronize(c.ev);
             c.used = false;
@@ -2277,6 +2287,12 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
         x.rows_out = l->d_count;
         x.max_target = impl->d_next_id(impl->agent_index(l->agent));
         x.max_value = mx + 1;
+        // the recount of the agents entering the next step, in the same launch
+        detail::StepEnd e{};
+        impl->count_targets(e);
+        for (uint32_t k = 0; k < e.ncounts; ++k) x.counts[k] = e.counts[k];
+        x.ncounts = e.ncounts;
+        x.acc = e.acc;
         FG_CUDA(detail::launch_kernel(detail::pdl_enabled(), detail::k_host_xfer, detail::host_xfer_grid(x, impl->sms),
                                       256, 0, impl->stream, x));
     } else {
@@ -2290,10 +2306,11 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
         impl->h_pinned[2] = n;
         FG_CUDA(cudaMemcpyAsync(l->d_count, impl->h_pinned + 2, sizeof(uint32_t), cudaMemcpyHostToDevice, impl->stream));
     }
-    // the recount is queued behind the copies before the one wait (the
-    // caller's buffers are free again when this returns)
+    // the recount (done by the transfer launch, else queued behind the
+    // copies) before the one wait (the caller's buffers are free again when
+    // this returns)
     l->bound = n;
-    impl->forget_counts();
+    impl->forget_counts(mapped);
     FG_CUDA(cudaStreamSynchronize(impl->stream));
     impl->ensure_all_allocated();
 }
