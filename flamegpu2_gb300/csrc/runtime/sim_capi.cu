@@ -107,24 +107,23 @@ extern "C" int fgs_configure(fgs_sim* s, uint32_t steps, uint64_t seed, int32_t 
 extern "C" int fgs_set_population(fgs_sim* s, const char* agent, const char* state, uint32_t n, int32_t nvars,
                                   const char* const* names, const void* const* cols) {
     return guarded([&] {
-        // every variable given with every id set: straight to the device
+        // every variable given: straight to the device, where the transfer
+        // also checks that every id is set; a population with ids to assign
+        // goes through AgentVector (the list is left empty by the failed try)
         const auto* ad = s->model->Agent(agent).getData();
         bool all = static_cast<size_t>(nvars) == ad->variables.size();
         std::vector<std::pair<std::string, const void*>> direct;
         for (int32_t k = 0; k < nvars && all; ++k) {
             all = ad->find(names[k]) != nullptr;
             direct.emplace_back(names[k], cols[k]);
-            if (all && std::strcmp(names[k], "_id") == 0) {
-                // one branch-free pass (it vectorises): any id left unset?
-                const flamegpu::id_t* ids = static_cast<const flamegpu::id_t*>(cols[k]);
-                uint32_t unset = 0;
-                for (uint32_t i = 0; i < n; ++i) unset |= ids[i] == flamegpu::ID_NOT_SET ? 1u : 0u;
-                all = unset == 0;
-            }
         }
         if (all) {
-            s->sim->setPopulationColumns(agent, state ? state : "default", n, direct);
-            return;
+            try {
+                s->sim->setPopulationColumns(agent, state ? state : "default", n, direct);
+                return;
+            } catch (const flamegpu::exception::InvalidArgument& e) {
+                if (!std::strstr(e.what(), "every _id must be set")) throw;
+            }
         }
         flamegpu::AgentVector pop(s->model->Agent(agent), n);
         for (int32_t k = 0; k < nvars; ++k) {

@@ -112,8 +112,10 @@ struct HostXfer {
     uint32_t rows;             // rows to copy (at most, with d_rows)
     const uint32_t* d_rows;    // device row count (get), or null (set: rows)
     uint32_t* rows_out;        // set: the list's device count (= rows); get: a host word for the count
-    uint32_t* max_target;      // set: next id, raised to max_value
+    uint32_t* max_target;      // set: next id, raised to max_value and past every id of column id_col
     uint32_t max_value;
+    int32_t id_col;            // set: the id column, checked here (16-byte path only); -1: none
+    uint32_t* id_unset;        // set: a host word raised when an id of id_col is unset (0)
     const uint32_t* word_src[kHostXferWords];  // get: status words copied to word_dst
     uint32_t* word_dst[kHostXferWords];
     uint32_t nwords;
@@ -130,7 +132,7 @@ __global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     if (tid == 0) {
         if (x.rows_out) *x.rows_out = x.d_rows ? *x.d_rows : rows;
-        if (x.max_target) *x.max_target = *x.max_target > x.max_value ? *x.max_target : x.max_value;
+        if (x.max_target && x.max_value) atomicMax(x.max_target, x.max_value);
         if (x.acc) {  // after rows_out: the same thread's store is visible to its loads
             unsigned long long c = 0;
             for (uint32_t k = 0; k < x.ncounts; ++k) c += *x.counts[k];
@@ -140,7 +142,9 @@ __global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
     if (tid < x.nwords) *x.word_dst[tid] = *x.word_src[tid];
     // columns eight at a time: the 16-byte pieces of all eight are loaded
     // before any is stored, so one round trip to host memory (set) covers
-    // every column instead of one per column
+    // every column instead of one per column. The ids of column id_col are
+    // checked on the way (the host does not read them again).
+    uint32_t id_max = 0, id_unset = 0;
     for (uint32_t c0 = 0; c0 < x.ncols; c0 += 8) {
         const uint32_t nc = min(8u, x.ncols - c0);
         size_t n16[8];
@@ -163,6 +167,20 @@ __global__ void k_host_xfer(const __grid_constant__ HostXfer x) {
 #pragma unroll
             for (uint32_t j = 0; j < 8; ++j)
                 if (k < n16[j]) reinterpret_cast<uint4*>(x.dst[c0 + j])[k] = v[j];
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j)
+                if (static_cast<int32_t>(c0 + j) == x.id_col && k < n16[j]) {
+                    id_max = max(max(max(id_max, v[j].x), max(v[j].y, v[j].z)), v[j].w);
+                    id_unset |= (v[j].x == 0u) | (v[j].y == 0u) | (v[j].z == 0u) | (v[j].w == 0u);
+                }
+        }
+    }
+    if (x.id_col >= 0) {
+        id_max = __reduce_max_sync(0xFFFFFFFFu, id_max);
+        id_unset = __reduce_or_sync(0xFFFFFFFFu, id_unset);
+        if ((threadIdx.x & 31u) == 0) {
+            if (id_max && x.max_target) atomicMax(x.max_target, id_max + 1u);
+            if (id_unset) *x.id_unset = 1u;
         }
     }
     // the columns not 16-byte aligned: word or byte copies
@@ -2252,17 +2270,6 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
                                                     l->agent->variables[v].name.c_str()));
         if (l->agent->variables[v].name == "_id") idc = v;
     }
-    id_t mx = 0;
-    if (idc < src.size() && n) {
-        // one branch-free pass (it vectorises): the largest id, and whether any is unset
-        const id_t* ids = static_cast<const id_t*>(src[idc]);
-        uint32_t unset = 0;
-        for (uint32_t i = 0; i < n; ++i) {
-            unset |= ids[i] == ID_NOT_SET ? 1u : 0u;
-            mx = std::max(mx, ids[i]);
-        }
-        if (unset) THROW exception::InvalidArgument("setPopulationColumns: every _id must be set");
-    }
     // copies are ordered after the stream's earlier work; only growing the
     // buffers needs the stream idle
     const uint32_t cap = impl->initial_capacity(l, n);
@@ -2274,6 +2281,7 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
     // the next id; otherwise one copy per column
     detail::HostXfer x;
     std::memset(&x, 0, sizeof(x));
+    x.id_col = -1;
     bool mapped = l->cols.size() <= static_cast<size_t>(detail::kHostXferCols);
     for (size_t v = 0; mapped && v < l->cols.size(); ++v) {
         x.src[v] = static_cast<const char*>(n ? detail::host_mapped(src[v]) : l->cols[v][l->parity]);
@@ -2281,12 +2289,33 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
         x.elem_bytes[v] = l->agent->variables[v].bytes();
         mapped = x.src[v] != nullptr;
     }
+    // the ids: checked (every one set) and their largest found by the transfer
+    // launch when the id column takes its 16-byte path, else here on the host
+    const bool dev_ids = mapped && idc < src.size() && n && impl->h_pinned_dev &&
+                         ((reinterpret_cast<uintptr_t>(x.src[idc]) | reinterpret_cast<uintptr_t>(x.dst[idc]) |
+                           (static_cast<size_t>(n) * sizeof(id_t))) & 15) == 0;
+    id_t mx = 0;
+    if (idc < src.size() && n && !dev_ids) {
+        // one branch-free pass (it vectorises): the largest id, and whether any is unset
+        const id_t* ids = static_cast<const id_t*>(src[idc]);
+        uint32_t unset = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            unset |= ids[i] == ID_NOT_SET ? 1u : 0u;
+            mx = std::max(mx, ids[i]);
+        }
+        if (unset) THROW exception::InvalidArgument("setPopulationColumns: every _id must be set");
+    }
     if (mapped) {
         x.ncols = static_cast<uint32_t>(l->cols.size());
         x.rows = n;
         x.rows_out = l->d_count;
         x.max_target = impl->d_next_id(impl->agent_index(l->agent));
-        x.max_value = mx + 1;
+        x.max_value = dev_ids ? 0u : mx + 1;
+        if (dev_ids) {
+            x.id_col = static_cast<int32_t>(idc);
+            impl->h_pinned[4] = 0u;
+            x.id_unset = impl->h_pinned_dev + 4;
+        }
         // the recount of the agents entering the next step, in the same launch
         detail::StepEnd e{};
         impl->count_targets(e);
@@ -2312,6 +2341,14 @@ void CUDASimulation::setPopulationColumns(const std::string& agent, const std::s
     l->bound = n;
     impl->forget_counts(mapped);
     FG_CUDA(cudaStreamSynchronize(impl->stream));
+    if (dev_ids && impl->h_pinned[4] != 0u) {
+        // an unset id: the list is left empty
+        FG_CUDA(cudaMemsetAsync(l->d_count, 0, sizeof(uint32_t), impl->stream));
+        impl->forget_counts();
+        FG_CUDA(cudaStreamSynchronize(impl->stream));
+        l->bound = 0;
+        THROW exception::InvalidArgument("setPopulationColumns: every _id must be set");
+    }
     impl->ensure_all_allocated();
 }
 

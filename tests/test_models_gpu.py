@@ -339,6 +339,46 @@ def test_population_through_page_locked_buffers(n):
         np.testing.assert_array_equal(res[0][k], res[1][k], err_msg=k)
 
 
+@pytest.mark.parametrize("locked", [False, True])
+def test_population_with_unset_ids_gets_ids_assigned(locked):
+    # page-locked columns: the transfer launch checks the ids on the device
+    # (the host does not read them); pageable: the host checks them. Either
+    # way an id left unset (0) sends the population through the path that
+    # assigns ids, and the next id follows the largest id given
+    import torch
+    from flamegpu2_gb300 import synth
+    S = _sim()
+    n = 4096
+    cfg = dict(synth.BOIDS_SMALL, n=n, seed=8)
+    pop = synth.boids_population(n, cfg["min_pos"], cfg["max_pos"], cfg["seed"])
+
+    def pinned_like(a):
+        buf = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory().numpy().view(a.dtype)
+        buf[:] = a
+        return buf
+
+    ids = np.arange(1, n + 1, dtype=np.uint32) * 3
+    ids[1234] = 0
+    pop = dict(pop, _id=ids)
+    cols = {k: pinned_like(v) for k, v in pop.items()} if locked else pop
+    s = S.Simulation("boids_spatial3d", synth.boids_params(cfg))
+    s.set_population("Boid", n, cols)
+    got = s.get("Boid", "_id", np.uint32)
+    assert len(got) == n and np.all(got != 0) and len(np.unique(got)) == n
+    # the ids that were set are kept; the unset one got a fresh id
+    keep = np.ones(n, bool)
+    keep[1234] = False
+    np.testing.assert_array_equal(got[keep], ids[keep])
+    # every id set: taken as given, and the population is not left empty by the first try
+    ids2 = np.arange(1, n + 1, dtype=np.uint32) * 5
+    cols2 = dict(cols, _id=pinned_like(ids2) if locked else ids2)
+    s.set_population("Boid", n, cols2)
+    np.testing.assert_array_equal(s.get("Boid", "_id", np.uint32), ids2)
+    s.step(1)
+    assert s.count("Boid") == n
+    s.close()
+
+
 def test_key_kernels_fused_into_the_output_launch():
     # Boids step: outputdata, agent sort (5 kernels), message build (5),
     # inputdata, step end = 13 kernels; the output launch computing both key
