@@ -288,6 +288,10 @@ uint32_t count_grid(uint32_t max_n) {
 }
 }  // namespace
 
+uint32_t* fgi_compact_survivor_word(void* workspace) {
+    return workspace ? &reinterpret_cast<WsHeader*>(workspace)->alive_total : nullptr;
+}
+
 extern "C" size_t fg_compact_workspace_size(uint32_t max_n) {
     return sizeof(WsHeader) + align_up(sizeof(uint64_t) * 2 * comp_tiles(max_n), 256);
 }

@@ -68,6 +68,10 @@ int fgi_spatial_sort_agents(const fg_spatial_grid* g, uint32_t max_n, const uint
                             const float* y, const float* z, const fg_column* cols, uint32_t ncols, uint32_t* perm_out,
                             void* workspace, size_t workspace_bytes, void* stream, bool keys_ready,
                             uint32_t pos_stride = 1);
+// The word of a compaction workspace's header that fg_compact_agents counts
+// the survivors into (zero between compactions): a launch that writes the
+// death flags may add its survivors there itself and pass it as d_alive_total.
+uint32_t* fgi_compact_survivor_word(void* workspace);
 // The agent sort of a list and the build of the spatial messages it output
 // on the same grid, as one chain of paired launches (both key sets written by
 // the launch before).

@@ -512,6 +512,9 @@ struct SimulationImpl {
         return 0;
     }
 
+    // The compaction workspace header's survivor word of list l (fg_compact_agents
+    // reads it as d_alive_total; its last block resets it to zero).
+    static uint32_t* survivors_word(const AgentList& l) { return fgi_compact_survivor_word(l.comp_ws); }
     AgentList* list_of(const std::string& agent, const std::string& state) {
         for (auto& l : lists)
             if (l->agent->name == agent && l->state == state) return l.get();
@@ -1402,6 +1405,10 @@ struct SimulationImpl {
         P.birth_flags = f.births ? f.birth_flags : nullptr;
         P.birth_next_id = f.births ? d_next_id(agent_index(f.birth_list->agent)) : nullptr;
         P.death_flags = f.fn->has_agent_death ? f.death_flags : nullptr;
+        // the survivors are counted by the launch itself into the compaction
+        // workspace's header (the compaction then reads them there, and its
+        // last block resets the word): no counting kernel before it
+        P.alive_count = f.fn->has_agent_death ? survivors_word(l) : nullptr;
         P.d_step = d_step();
         P.seed = config.random_seed;
         P.fn_uid = f.fn->uid;
@@ -1448,15 +1455,17 @@ struct SimulationImpl {
                 bcols[v] = fg_column{fused ? f.birth_cols[v] : l.cols[v][l.parity], l.cols[v][l.parity ^ 1], b};
                 if (l.agent->variables[v].name == "_id") id_col = static_cast<int>(v);
             }
+            // survivors: counted by the function's launch (death), else all n
+            const uint32_t* survivors = f.fn->has_agent_death ? survivors_word(l) : l.d_count;
             timed("compact:" + l.agent->name, [&] {
                 FG_CAPI(fg_compact_agents(l.capacity, l.d_count, f.fn->has_agent_death ? f.death_flags : nullptr,
                                           fused ? f.birth_flags : nullptr, cols.data(), bcols.data(),
                                           static_cast<uint32_t>(cols.size()), fused ? id_col : -1,
-                                          fused ? d_next_id(agent_index(l.agent)) : nullptr, nullptr, l.d_count,
+                                          fused ? d_next_id(agent_index(l.agent)) : nullptr, survivors, l.d_count,
                                           l.capacity, l.comp_ws, l.comp_ws_bytes, stream));
             });
             l.parity ^= 1;
-            kernel_counter += 2;
+            kernel_counter += 1;
         }
         if (f.end_list) {
             // state transition (CUDAFatAgent.cu:139-184): the agents that ran the

@@ -164,6 +164,7 @@ struct LaunchParams {
     uint32_t* birth_flags;       // 1 where agent_out was used, 2 if its id was also claimed (null if disabled)
     uint32_t* birth_next_id;     // next id of the output agent (agent_out.getID() claims from it; one per instance in a batch)
     uint32_t* death_flags;       // ALIVE / DEAD per agent (null if death disabled)
+    uint32_t* alive_count;       // the survivors are added here, one atomic per block (null: not counted)
     // step data
     const uint32_t* d_step;      // step counter
     uint64_t seed;               // simulation random seed

@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
     constexpr int kDims = std::is_same<MsgIn, MessageSpatial3D>::value ? 3 : (std::is_same<MsgIn, MessageSpatial2D>::value ? 2 : 0);
     bool first = true;
     uint32_t out_of_order = 0u;  // keyed targets whose rows were not in key order
+    uint32_t alive_rows = 0u;    // rows this thread left ALIVE (survivor count for the compaction)
     if (!P.batch) {
         fill_ctx(P, 0, n);
         __syncthreads();
@@ -127,6 +128,7 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
         if (live == 0xFFFFFFFFu) continue;
         if (idx < first_row) {  // failed the condition: kept as it is
             if (P.death_flags) P.death_flags[idx] = static_cast<uint32_t>(ALIVE);
+            ++alive_rows;
             if (P.birth_flags) P.birth_flags[idx] = 0u;
             continue;
         }
@@ -143,6 +145,7 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
         }
         DeviceAPI<MsgIn, MsgOut> api(P, idx, msg_row);
         const AGENT_STATUS st = F()(&api);
+        alive_rows += st == ALIVE ? 1u : 0u;
         if (P.death_flags) {
             P.death_flags[idx] = static_cast<uint32_t>(st);
         } else if (st == DEAD) {
@@ -172,6 +175,17 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
         }
     }
     if (P.keyed[0].mode != kKeyNone || P.keyed[1].mode != kKeyNone) key_targets_order_flush(P.keyed, out_of_order);
+    if (P.alive_count) {
+        // the block's survivors, one atomic per block (a warp's or a row's
+        // atomics on one word would serialise over a large population)
+        __shared__ uint32_t s_alive;
+        if (threadIdx.x == 0) s_alive = 0u;
+        __syncthreads();
+        const uint32_t c = __reduce_add_sync(0xFFFFFFFFu, alive_rows);
+        if ((threadIdx.x & 31u) == 0 && c) atomicAdd(&s_alive, c);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_alive) atomicAdd(P.alive_count, s_alive);
+    }
 }
 
 // FLAMEGPU_AGENT_FUNCTION_CONDITION kernel (AgentFunctionCondition.cuh:44-100):
