@@ -181,7 +181,7 @@ def run_birth_death(args, world, rank, local):
         "e2e": {"value": round(agent_steps * e2e_n * world / e2e_s, 1), "unit": UNIT,
                 "h2d_bytes_per_step": n0 * row, "d2h_bytes_per_step": final * row},
         "roofline": _with_traffic(_roofline(stages, peak, peak_kind), "birth_death_compact",
-                                  "k_compact alone (the stage also counts the survivors)"),
+                                  "k_compact (the whole stage: the agent-function launch counts the survivors)"),
         "stages": stages,
         "gpu_launches": kps * steps_per * k_steps, "clocks": clk,
     }
