@@ -213,6 +213,16 @@ void reduce_column(std::type_index t, const void* col, const uint32_t* d_n, cons
 size_t log_scratch_bytes();
 size_t log_scratch_bytes() { return sizeof(Partial) * (kLogBlocks + 2) + sizeof(double) * 2; }
 
+// One reduction of a column (HostAgentAPI reductions through CUDASimulation::reduceAgentVariable).
+void reduce_column_of(std::type_index t, const void* col, const uint32_t* d_n, LoggingConfig::Reduction r,
+                      cudaStream_t st, char* scratch, std::map<LoggingConfig::NameReduction, LogValue>& out,
+                      const std::string& var);
+void reduce_column_of(std::type_index t, const void* col, const uint32_t* d_n, LoggingConfig::Reduction r,
+                      cudaStream_t st, char* scratch, std::map<LoggingConfig::NameReduction, LogValue>& out,
+                      const std::string& var) {
+    reduce_column(t, col, d_n, {r}, st, scratch, out, var);
+}
+
 void fill_log_frame(const LoggingConfig& cfg, CUDASimulation& sim, char* scratch, LogFrame& frame) {
     const auto& model = *cfg.model();
     for (const auto& name : cfg.environment()) {
@@ -410,6 +420,23 @@ void CUDASimulation::processStepLog(double step_seconds) {
     detail::fill_log_frame(*step_log, *this, log_scratch, frame);
     run_log.random_seed = SimulationConfig().random_seed;
     run_log.step.push_back(std::move(frame));
+}
+
+LogValue CUDASimulation::reduceAgentVariable(const std::string& agent, const std::string& variable,
+                                             LoggingConfig::Reduction r, const std::string& state) {
+    if (!log_scratch && cudaMalloc(&log_scratch, detail::log_scratch_bytes()) != cudaSuccess)
+        THROW exception::CUDAError("Cannot allocate the log reduction buffer");
+    synchronize();
+    const detail::AgentData* a = nullptr;
+    for (const auto& x : getModelData()->agents)
+        if (x->name == agent) a = x.get();
+    if (!a) THROW exception::InvalidAgentName(exception::format("No agent '%s'", agent.c_str()));
+    const detail::Variable* var = a->find(variable);
+    if (!var) THROW exception::InvalidAgentVar(exception::format("Agent '%s' has no variable '%s'", agent.c_str(), variable.c_str()));
+    std::map<LoggingConfig::NameReduction, LogValue> out;
+    detail::reduce_column_of(var->type, getDeviceVariable(agent, variable, state), getDeviceCount(agent, state), r,
+                             getStream(), log_scratch, out, variable);
+    return out[{variable, r}];
 }
 
 void CUDASimulation::processExitLog(double total_seconds) {

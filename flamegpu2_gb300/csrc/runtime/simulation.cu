@@ -448,6 +448,10 @@ struct SimulationImpl {
     uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record, [8..] next ids per agent
     unsigned long long* d_agent_steps = nullptr;  // [0] agents summed over the steps run, [1] agents now
     unsigned long long host_agent_steps = 0;      // the same for populations that only the host changes
+    CUDASimulation* owner = nullptr;  // the simulation this implements (host functions reach it)
+    // agents created by host functions (HostAgentAPI::newAgent), per (agent, state),
+    // joining their populations when the host functions return
+    std::map<std::pair<std::string, std::string>, std::unique_ptr<AgentVector>> host_births;
     uint32_t* h_pinned = nullptr;
     uint32_t* h_pinned_dev = nullptr;  // its device address (null: not mapped)
     unsigned int step_count = 0;
@@ -1571,9 +1575,31 @@ struct SimulationImpl {
         return false;
     }
 
+    // Agents created by host functions join their populations (after the
+    // existing agents, in creation order, with fresh ids), as the reference adds
+    // them when the host function returns (HostAgentAPI::newAgent).
+    void flush_host_births() {
+        for (auto& kv : host_births) {
+            AgentVector& add = *kv.second;
+            if (add.empty()) continue;
+            AgentVector pop(AgentDescription(model, const_cast<AgentData*>(add.getAgentData())));
+            owner->getPopulationData(pop, kv.first.second);
+            const flamegpu::size_type n = pop.size(), k = add.size();
+            pop.resize(n + k);
+            const auto& vars = add.getAgentData()->variables;
+            for (size_t v = 0; v < vars.size(); ++v) {
+                const size_t b = vars[v].bytes();
+                std::memcpy(pop.columns()[v].data() + n * b, add.columns()[v].data(), k * b);
+            }
+            owner->setPopulationData(pop, kv.first.second);
+            add.clear();
+        }
+    }
+
     void run_host_layer(LayerData* layer, HostAPI& api) {
         FG_CUDA(cudaStreamSynchronize(stream));
         for (auto fn : layer->host_functions) fn(&api);
+        flush_host_births();
         upload_env_if_dirty();
     }
 
@@ -1655,6 +1681,7 @@ struct SimulationImpl {
             FG_CUDA(cudaStreamSynchronize(stream));
             HostAPI api(this);
             for (auto fn : model->step_functions) fn(&api);
+            flush_host_births();
             upload_env_if_dirty();
         }
         if (cuda_config.check_each_step) owner->synchronize();
@@ -1881,12 +1908,35 @@ unsigned int HostAPI::AgentAPI::count() const {
     return c;
 }
 
+HostNewAgentAPI HostAPI::AgentAPI::newAgent() {
+    detail::AgentList* l = sim->list_of(agent, state);
+    auto& buf = sim->host_births[{agent, state}];
+    if (!buf) buf = std::make_unique<AgentVector>(AgentDescription(sim->model, const_cast<detail::AgentData*>(l->agent)));
+    buf->push_back();
+    return HostNewAgentAPI(buf.get(), buf->size() - 1);
+}
+
+LogValue HostAPI::AgentAPI::reduce(const std::string& variable, const std::type_info& t, LoggingConfig::Reduction r) const {
+    // the checks of HostAgentAPI::sum (HostAgentAPI.cuh:536-546)
+    const detail::AgentList* l = sim->list_of(agent, state);
+    const int v = l->var_index(variable);
+    if (v < 0)
+        THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), variable.c_str()));
+    const auto& var = l->agent->variables[v];
+    if (var.elements != 1)
+        THROW exception::UnsupportedVarType(format("Reductions do not support agent array variables ('%s')", variable.c_str()));
+    if (var.type != std::type_index(t))
+        THROW exception::InvalidVarType(format("Wrong variable type for the reduction of '%s'", variable.c_str()));
+    return sim->owner->reduceAgentVariable(agent, variable, r, state);
+}
+
 unsigned int HostAPI::getStepCounter() const { return sim->step_count; }
 
 // ------------------------------------------------------------ CUDASimulation
 
 CUDASimulation::CUDASimulation(const ModelDescription& model, int, const char**)
     : impl(std::make_unique<SimulationImpl>(model.getData())) {
+    impl->owner = this;
     impl->init();
 }
 
@@ -2432,6 +2482,7 @@ bool CUDASimulation::step() {
     if (impl->step_count == 0 && !impl->model->init_functions.empty()) {
         HostAPI api(impl.get());
         for (auto fn : impl->model->init_functions) fn(&api);
+        impl->flush_host_births();
     }
     impl->step_once(this);
     return true;
@@ -2442,6 +2493,7 @@ void CUDASimulation::step(unsigned int n) {
     if (impl->step_count == 0 && !impl->model->init_functions.empty()) {
         HostAPI api(impl.get());
         for (auto fn : impl->model->init_functions) fn(&api);
+        impl->flush_host_births();
     }
     if (!impl->multi_step_ok(step_log != nullptr)) {
         for (unsigned int s = 0; s < n; ++s) impl->step_once(this);
@@ -2461,6 +2513,7 @@ void CUDASimulation::simulate() {
         FG_CUDA(cudaStreamSynchronize(impl->stream));
         HostAPI api(impl.get());
         for (auto fn : impl->model->init_functions) fn(&api);
+        impl->flush_host_births();
     }
     processStepLog(0.0);  // the frame before the first step (CUDASimulation.cu:1263)
     if (impl->multi_step_ok(step_log != nullptr)) {
@@ -2472,6 +2525,7 @@ void CUDASimulation::simulate() {
         FG_CUDA(cudaStreamSynchronize(impl->stream));
         HostAPI api(impl.get());
         for (auto fn : impl->model->exit_functions) fn(&api);
+        impl->flush_host_births();
     }
     FG_CUDA(cudaEventRecord(s1, impl->stream));
     synchronize();

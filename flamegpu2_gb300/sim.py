@@ -373,14 +373,16 @@ class Ensemble:
         except Exception:
             pass
 
-    def add_run(self, steps: int, seed: int, agent: str, n: int, columns: dict, message=None, mn=None, mx=None,
+    def add_run(self, steps: int, seed: int, agent=None, n: int = 0, columns=None, message=None, mn=None, mx=None,
                 radius: float = 0.0) -> int:
+        """One run plan; agent None: no initial population (the model's init functions may create one)."""
+        columns = columns or {}
         names = list(columns)
         arrs = [np.ascontiguousarray(columns[k]) for k in names]
         cn = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
         cp = (C.c_void_p * max(1, len(names)))(*[a.ctypes.data for a in arrs])
         f3 = lambda v: (C.c_float * 3)(*(list(v) + [0.0] * (3 - len(v)))) if v is not None else None
-        _check(_ens().fge_add_run(self._h, steps, seed, agent.encode(), n, len(names), cn, cp,
+        _check(_ens().fge_add_run(self._h, steps, seed, agent.encode() if agent else None, n, len(names), cn, cp,
                                   message.encode() if message else None, f3(mn), f3(mx), float(radius)))
         self.runs += 1
         return self.runs - 1

@@ -12,6 +12,9 @@
 #include <memory>
 #include <string>
 #include <tuple>
+#include <typeinfo>
+#include <utility>
+#include <array>
 #include <vector>
 
 #include "flamegpu/model/ModelDescription.h"
@@ -24,7 +27,33 @@ namespace detail {
 struct SimulationImpl;
 }
 
-/** Host-side API of init/step/exit/host-layer functions (reduced to properties and counts). */
+/** An agent created by a host function (HostNewAgentAPI,
+ * include/flamegpu/runtime/agent/HostNewAgentAPI.h): its variables start at
+ * their defaults; it joins its population when the host function returns, with
+ * a fresh id. */
+class HostNewAgentAPI {
+ public:
+    HostNewAgentAPI(AgentVector* v, flamegpu::size_type i) : agent_((*v)[i]) {}
+    template <typename T>
+    void setVariable(const std::string& name, T value) { agent_.setVariable<T>(name, value); }
+    template <typename T, flamegpu::size_type N>
+    void setVariable(const std::string& name, const std::array<T, N>& value) { agent_.setVariable<T, N>(name, value); }
+    template <typename T, flamegpu::size_type N = 0>
+    void setVariable(const std::string& name, flamegpu::size_type element, T value) {
+        agent_.setVariable<T, N>(name, element, value);
+    }
+    template <typename T>
+    T getVariable(const std::string& name) const { return agent_.getVariable<T>(name); }
+    template <typename T, flamegpu::size_type N>
+    std::array<T, N> getVariable(const std::string& name) const { return agent_.getVariable<T, N>(name); }
+
+ private:
+    AgentVector::Agent agent_;
+};
+
+/** Host-side API of init/step/exit/host-layer functions: environment
+ * properties, agent counts, reductions of agent variables (computed on the
+ * device) and agent creation. */
 class HostAPI {
  public:
     class Environment {
@@ -52,12 +81,50 @@ class HostAPI {
         void set(const std::string& name, const std::type_info& t, size_t size, const void* in);
         detail::SimulationImpl* sim;
     };
+    /** HostAgentAPI (include/flamegpu/runtime/agent/HostAgentAPI.cuh:134-227). */
     class AgentAPI {
      public:
         AgentAPI(detail::SimulationImpl* s, std::string a, std::string st) : sim(s), agent(std::move(a)), state(std::move(st)) {}
         unsigned int count() const;
+        /** A new agent of this type and state (HostAgentAPI::newAgent, :160). */
+        HostNewAgentAPI newAgent();
+        /** Sum of a variable over the population (:174-185): accumulated on
+         * the device in a fixed order (double for floating point, 64-bit
+         * integers otherwise), returned as OutT. */
+        template <typename InT>
+        InT sum(const std::string& variable) const { return sum<InT, InT>(variable); }
+        template <typename InT, typename OutT>
+        OutT sum(const std::string& variable) const {
+            return convert<OutT>(reduce(variable, typeid(InT), LoggingConfig::Sum));
+        }
+        /** Smallest / largest value of a variable (:206-216; 0 for an empty population). */
+        template <typename InT>
+        InT min(const std::string& variable) const { return convert<InT>(reduce(variable, typeid(InT), LoggingConfig::Min)); }
+        template <typename InT>
+        InT max(const std::string& variable) const { return convert<InT>(reduce(variable, typeid(InT), LoggingConfig::Max)); }
+        /** Mean and population standard deviation (:196). */
+        template <typename InT>
+        std::pair<double, double> meanStandardDeviation(const std::string& variable) const {
+            return {convert<double>(reduce(variable, typeid(InT), LoggingConfig::Mean)),
+                    convert<double>(reduce(variable, typeid(InT), LoggingConfig::StandardDev))};
+        }
 
      private:
+        LogValue reduce(const std::string& variable, const std::type_info& t, LoggingConfig::Reduction r) const;
+        template <typename OutT>
+        static OutT convert(const LogValue& v) {
+            const auto t = v.type;
+            if (t == std::type_index(typeid(double))) return static_cast<OutT>(v.as<double>("reduction"));
+            if (t == std::type_index(typeid(float))) return static_cast<OutT>(v.as<float>("reduction"));
+            if (t == std::type_index(typeid(int64_t))) return static_cast<OutT>(v.as<int64_t>("reduction"));
+            if (t == std::type_index(typeid(uint64_t))) return static_cast<OutT>(v.as<uint64_t>("reduction"));
+            if (t == std::type_index(typeid(int32_t))) return static_cast<OutT>(v.as<int32_t>("reduction"));
+            if (t == std::type_index(typeid(uint32_t))) return static_cast<OutT>(v.as<uint32_t>("reduction"));
+            if (t == std::type_index(typeid(int16_t))) return static_cast<OutT>(v.as<int16_t>("reduction"));
+            if (t == std::type_index(typeid(uint16_t))) return static_cast<OutT>(v.as<uint16_t>("reduction"));
+            if (t == std::type_index(typeid(int8_t))) return static_cast<OutT>(v.as<int8_t>("reduction"));
+            return static_cast<OutT>(v.as<uint8_t>("reduction"));
+        }
         detail::SimulationImpl* sim;
         std::string agent, state;
     };
@@ -189,6 +256,11 @@ class CUDASimulation {
     unsigned int getAgentCount(const std::string& agent, const std::string& state = "default");
     /** Device pointer to the current column of an agent variable (valid until the next step). */
     void* getDeviceVariable(const std::string& agent, const std::string& variable, const std::string& state = "default");
+    /** One reduction of an agent variable over its population, on the device
+     *  (the step / exit logs' reductions; HostAgentAPI's sum, min, max and
+     *  mean / standard deviation use it). GB300 extension. */
+    LogValue reduceAgentVariable(const std::string& agent, const std::string& variable, LoggingConfig::Reduction r,
+                                 const std::string& state = "default");
     /** Override the bounds and radius of a spatial message list before stepping
      *  (per-run spatial grids of an ensemble). */
     void setSpatialMessageBounds(const std::string& message, const std::vector<float>& min,
