@@ -93,6 +93,12 @@ __global__ void k_recount(const __grid_constant__ StepEnd e) {
         if (threadIdx.x == 0) e.acc[1] = c;
     }
 }
+// *base = the list's messages so far this step, or 0 if none has been output
+// by a launch with agents yet (the appending output then truncates it)
+__global__ void k_append_base(uint32_t* base, const uint32_t* count, const uint32_t* filled) {
+    grid_dependency_enter();
+    *base = *filled ? *count : 0u;
+}
 __global__ void k_max_u32(uint32_t* p, uint32_t v) {
     grid_dependency_enter();
     *p = *p > v ? *p : v;
@@ -392,6 +398,10 @@ struct MsgList {
     // of a step truncates the list, later ones append after its messages
     bool written = false;            // host, while a step is being issued
     uint32_t* d_base = nullptr;      // count before an appending output (device)
+    // 1 once a launch with at least one agent has output to the list this step
+    // (device; cleared at every step end): until then an output truncates it,
+    // and a launch over no agents leaves it as it was (CUDASimulation.cu:1050-1059)
+    uint32_t* d_filled = nullptr;
     bool spatial() const { return msg->kind != MessageKind::BruteForce; }
 };
 
@@ -578,6 +588,8 @@ struct SimulationImpl {
             ml->msg = m.get();
             ml->d_count = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
             ml->d_base = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
+            ml->d_filled = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
+            FG_CUDA(cudaMemsetAsync(ml->d_filled, 0, sizeof(uint32_t), stream));
             for (const auto& v : m->variables) ml->slot_bytes.push_back(round4(v.bytes()));
             if (m->kind != MessageKind::BruteForce) {
                 const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
@@ -1341,7 +1353,14 @@ struct SimulationImpl {
         const bool append = f.out && f.out->written;
         if (f.out) {
             f.out->written = true;
-            if (append) FG_CUDA(cudaMemcpyAsync(f.out->d_base, f.out->d_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+            // the base of an appending output: the messages so far this step,
+            // none if no launch with agents has output yet (the list is truncated)
+            if (append) {
+                FG_CUDA(launch_kernel(pdl_enabled(), k_append_base, 1, 1, 0, stream, f.out->d_base,
+                                      static_cast<const uint32_t*>(f.out->d_count),
+                                      static_cast<const uint32_t*>(f.out->d_filled)));
+                kernel_counter += 1;
+            }
         }
         if (f.fn->condition) {
             // FLAMEGPU_AGENT_FUNCTION_CONDITION, then the failing agents to the
@@ -1386,6 +1405,7 @@ struct SimulationImpl {
             P.msg_out_always = f.fn->message_output_optional ? 0 : 1;
             P.msg_out_count = f.out->d_count;
             P.msg_out_base = append ? f.out->d_base : nullptr;
+            P.msg_out_filled = f.out->d_filled;
             P.msg_out_enabled = 1;
         }
         if (f.in) {
@@ -1537,11 +1557,13 @@ struct SimulationImpl {
             else
                 FG_CUDA(cudaMemsetAsync(p, 0, sizeof(uint32_t), stream));
         };
-        for (auto& m : msgs)
+        for (auto& m : msgs) {
             if (!m->msg->persistent) {
                 clear(m->d_count);
                 if (m->bf_count) clear(m->bf_count);
             }
+            clear(m->d_filled);  // the next step's first output truncates the list
+        }
         e.d_step = d_step();
         count_targets(e);
         FG_CUDA(launch_kernel(pdl_enabled(), k_step_end, 1, 32, 0, stream, e));

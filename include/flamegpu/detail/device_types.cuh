@@ -147,6 +147,7 @@ struct LaunchParams {
     uint32_t* msg_out_valid;     // per-row output flag (lists with an optional output), or null
     uint32_t* msg_out_count;     // set to the message count by the launch
     const uint32_t* msg_out_base;  // messages already in the list this step (append), or null (truncate)
+    uint32_t* msg_out_filled;    // set to 1 by a launch that ran over at least one agent (null: none)
     int msg_out_enabled;
     int msg_out_always;          // every running agent outputs (not optional): valid = 1
     // message input

@@ -99,7 +99,13 @@ __global__ void __launch_bounds__(kAgentBlock, MINB) agent_function_kernel(const
     // message rows: after those already output to the list this step (append), else from 0
     const uint32_t msg_base = (!P.batch && P.msg_out_base) ? *P.msg_out_base : 0u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (P.msg_out_count) *P.msg_out_count = msg_base + n - first_row;
+        // a launch over no agents leaves the list as it was (the reference skips
+        // such a function, CUDASimulation.cu:1050-1059): a persistent list keeps
+        // its messages
+        if (P.msg_out_count && n > first_row) {
+            *P.msg_out_count = msg_base + n - first_row;
+            if (P.msg_out_filled) *P.msg_out_filled = 1u;
+        }
         if (P.keyed[0].mode) key_target_reset(P.keyed[0]);
         if (P.keyed[1].mode) key_target_reset(P.keyed[1]);
     }
