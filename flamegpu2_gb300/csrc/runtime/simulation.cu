@@ -588,8 +588,7 @@ struct SimulationImpl {
             ml->msg = m.get();
             ml->d_count = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
             ml->d_base = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
-            ml->d_filled = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
-            FG_CUDA(cudaMemsetAsync(ml->d_filled, 0, sizeof(uint32_t), stream));
+            ml->d_filled = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));  // zeroed
             for (const auto& v : m->variables) ml->slot_bytes.push_back(round4(v.bytes()));
             if (m->kind != MessageKind::BruteForce) {
                 const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
