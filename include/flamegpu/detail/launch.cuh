@@ -19,7 +19,9 @@
 // measured on the two-branch Boids step at 1M agents, an early trigger let the
 // next kernel's blocks occupy SMs, waiting, while the other branch still had
 // work, and the step took 10% longer; at exit, the step is as fast as without
-// PDL there and faster at small populations.
+// PDL there and faster at small populations. Triggering early only in launches
+// of at most one block per SM was slower too: the 16,384-agent Boids step took
+// 37.5 us against 36.7 us, and the served request mix lost 2% throughput.
 #include <cuda_runtime.h>
 
 #include <cstdlib>
