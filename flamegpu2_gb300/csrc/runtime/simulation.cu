@@ -1868,7 +1868,9 @@ struct SimulationImpl {
                                           "spatial radius is not a factor of the environment width (wrapped iterator)",
                                           "agent death is not enabled for this function",
                                           "agent output is not enabled for this function", "reserved variable name",
-                                          "unsupported device call", "message output is not enabled for this function"};
+                                          "unsupported device call", "message output is not enabled for this function",
+                                          "a neighbourhood staging wait gave up (bounded wait)",
+                                          "AgentRandom::uniform() with min > max"};
             const char* what = err[0] < sizeof(names) / sizeof(names[0]) ? names[err[0]] : "device error";
             THROW exception::DeviceError(format("Device error: %s (name hash 0x%08x, agent index %u, %u occurrences)", what,
                                                 err[1], err[2], err[3]));

@@ -128,6 +128,7 @@ enum DeviceErrorCode : uint32_t {
     kDevUnsupported = 9,
     kDevMessageOutNotEnabled = 10,
     kDevStageTimeout = 11,
+    kDevRandomRange = 12,
 };
 
 /** Kernel parameters of one agent function launch (passed __grid_constant__).

@@ -871,7 +871,12 @@ class DeviceEnvironment {
  * Per-agent random numbers (include/flamegpu/runtime/random/AgentRandom.cuh).
  * Counter-based: draw k of agent index i in step s of function f is a
  * SplitMix64 hash of (seed, f, s, i, k); no per-thread generator state is
- * kept. The reference's curand Philox values are not reproduced.
+ * kept. The reference's curand Philox values are not reproduced; the
+ * distributions and ranges are the reference's: uniform() in [0, 1),
+ * uniform(min, max) in [min, max] for integers and min + (max - min) * [0, 1)
+ * for floating point (min > max is a device error with seatbelts on),
+ * normal() standard normal, logNormal(mean, stddev) = exp(mean + stddev *
+ * normal()), poisson(mean) Poisson distributed.
  */
 class AgentRandom {
  public:
@@ -884,6 +889,8 @@ class AgentRandom {
     __device__ T normal() const;
     template <typename T>
     __device__ T logNormal(T mean, T stddev) const;
+    /** Poisson distributed count with the given mean (AgentRandom.cuh:50; 0 for mean <= 0). */
+    __device__ unsigned int poisson(double mean = 1.0) const;
 
  private:
     __device__ uint64_t next() const {
@@ -920,8 +927,49 @@ template <>
 __device__ inline double AgentRandom::logNormal<double>(double mean, double stddev) const {
     return exp(mean + stddev * normal<double>());
 }
+// Means below kPoissonSmall: Knuth's product of uniforms (The Art of Computer
+// Programming, vol. 2, 3.4.1): the count of factors before the running
+// product falls to exp(-mean). Larger means: Hormann's transformed rejection
+// with squeeze, PTRS ("The transformed rejection method for generating
+// Poisson random variables", Insurance: Mathematics and Economics 12, 1993),
+// which accepts about nine draws in ten. Both loops are bounded: past the
+// bound (a probability far below 2^-60) the nearest integer to the mean is
+// returned.
+constexpr double kPoissonSmall = 10.0;
+__device__ inline unsigned int AgentRandom::poisson(double mean) const {
+    if (!(mean > 0.0)) return 0u;
+    if (mean < kPoissonSmall) {
+        const double limit = exp(-mean);
+        double prod = 1.0;
+        for (unsigned int k = 0; k < 1024u; ++k) {
+            prod *= uniform<double>();
+            if (prod <= limit) return k;
+        }
+        return static_cast<unsigned int>(floor(mean + 0.5));
+    }
+    const double slam = sqrt(mean), loglam = log(mean);
+    const double b = 0.931 + 2.53 * slam;
+    const double a = -0.059 + 0.02483 * b;
+    const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4);
+    const double v_r = 0.9277 - 3.6224 / (b - 2.0);
+    for (int it = 0; it < 64; ++it) {
+        const double u = uniform<double>() - 0.5;
+        const double v = uniform<double>();
+        const double us = 0.5 - fabs(u);
+        if (us <= 0.0) continue;
+        const double k = floor((2.0 * a / us + b) * u + mean + 0.43);
+        if (us >= 0.07 && v <= v_r) return static_cast<unsigned int>(k);
+        if (k < 0.0 || (us < 0.013 && v > us)) continue;
+        if (log(v) + log(inv_alpha) - log(a / (us * us) + b) <= -mean + k * loglam - lgamma(k + 1.0))
+            return static_cast<unsigned int>(k);
+    }
+    return static_cast<unsigned int>(floor(mean + 0.5));
+}
 template <typename T>
 __device__ inline T AgentRandom::uniform(T min, T max) const {
+#if FLAMEGPU_SEATBELTS
+    if (min > max) detail::device_error(P, detail::kDevRandomRange, 0, index);
+#endif
     if constexpr (std::is_integral<T>::value) {
         const uint64_t span = static_cast<uint64_t>(static_cast<int64_t>(max) - static_cast<int64_t>(min)) + 1;
         return static_cast<T>(static_cast<int64_t>(min) + static_cast<int64_t>(next() % span));
