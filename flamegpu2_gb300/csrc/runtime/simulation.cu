@@ -1939,7 +1939,8 @@ HostNewAgentAPI HostAPI::AgentAPI::newAgent() {
     return HostNewAgentAPI(buf.get(), buf->size() - 1);
 }
 
-LogValue HostAPI::AgentAPI::reduce(const std::string& variable, const std::type_info& t, LoggingConfig::Reduction r) const {
+const void* HostAPI::AgentAPI::device_column(const std::string& variable, const std::type_info& t, const uint32_t** d_n,
+                                             cudaStream_t* stream) const {
     // the checks of HostAgentAPI::sum (HostAgentAPI.cuh:536-546)
     const detail::AgentList* l = sim->list_of(agent, state);
     const int v = l->var_index(variable);
@@ -1950,6 +1951,16 @@ LogValue HostAPI::AgentAPI::reduce(const std::string& variable, const std::type_
         THROW exception::UnsupportedVarType(format("Reductions do not support agent array variables ('%s')", variable.c_str()));
     if (var.type != std::type_index(t))
         THROW exception::InvalidVarType(format("Wrong variable type for the reduction of '%s'", variable.c_str()));
+    *d_n = l->d_count;
+    *stream = sim->stream;
+    return l->cols[v][l->parity];
+}
+
+LogValue HostAPI::AgentAPI::reduce_log(const std::string& variable, const std::type_info& t,
+                                       LoggingConfig::Reduction r) const {
+    const uint32_t* d_n = nullptr;
+    cudaStream_t st = nullptr;
+    device_column(variable, t, &d_n, &st);  // the checks
     return sim->owner->reduceAgentVariable(agent, variable, r, state);
 }
 

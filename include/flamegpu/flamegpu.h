@@ -10,4 +10,7 @@
 #include "flamegpu/simulation/CUDASimulation.h"
 #include "flamegpu/simulation/CUDAEnsemble.h"
 #include "flamegpu/simulation/SimulationServer.h"
+#ifdef __CUDACC__
+#include "flamegpu/runtime/HostReductions.cuh"
+#endif
 #endif  // INCLUDE_FLAMEGPU_FLAMEGPU_H_

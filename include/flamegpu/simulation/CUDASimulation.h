@@ -95,22 +95,48 @@ class HostAPI {
         InT sum(const std::string& variable) const { return sum<InT, InT>(variable); }
         template <typename InT, typename OutT>
         OutT sum(const std::string& variable) const {
-            return convert<OutT>(reduce(variable, typeid(InT), LoggingConfig::Sum));
+            return convert<OutT>(reduce_log(variable, typeid(InT), LoggingConfig::Sum));
         }
         /** Smallest / largest value of a variable (:206-216; 0 for an empty population). */
         template <typename InT>
-        InT min(const std::string& variable) const { return convert<InT>(reduce(variable, typeid(InT), LoggingConfig::Min)); }
+        InT min(const std::string& variable) const { return convert<InT>(reduce_log(variable, typeid(InT), LoggingConfig::Min)); }
         template <typename InT>
-        InT max(const std::string& variable) const { return convert<InT>(reduce(variable, typeid(InT), LoggingConfig::Max)); }
+        InT max(const std::string& variable) const { return convert<InT>(reduce_log(variable, typeid(InT), LoggingConfig::Max)); }
         /** Mean and population standard deviation (:196). */
         template <typename InT>
         std::pair<double, double> meanStandardDeviation(const std::string& variable) const {
-            return {convert<double>(reduce(variable, typeid(InT), LoggingConfig::Mean)),
-                    convert<double>(reduce(variable, typeid(InT), LoggingConfig::StandardDev))};
+            return {convert<double>(reduce_log(variable, typeid(InT), LoggingConfig::Mean)),
+                    convert<double>(reduce_log(variable, typeid(InT), LoggingConfig::StandardDev))};
         }
+        // The templates below launch kernels, so their definitions are in
+        // flamegpu/runtime/HostReductions.cuh (included by flamegpu.h when
+        // compiled by nvcc).
+        /** Agents whose variable equals value (:226-227). */
+        template <typename InT>
+        unsigned int count(const std::string& variable, InT value) const;
+        /** Counts of the variable's values in histogramBins equal bins over
+         * [lowerBound, upperBound); values outside are not counted (:240-243). */
+        template <typename InT>
+        std::vector<unsigned int> histogramEven(const std::string& variable, unsigned int histogramBins,
+                                                InT lowerBound, InT upperBound) const;
+        template <typename InT, typename OutT>
+        std::vector<OutT> histogramEven(const std::string& variable, unsigned int histogramBins, InT lowerBound,
+                                        InT upperBound) const;
+        /** Reduction of the variable by a FLAMEGPU_CUSTOM_REDUCTION operator,
+         * init combined once with the result (init alone for no agents) (:254-255). */
+        template <typename InT, typename ReductionT>
+        InT reduce(const std::string& variable, ReductionT reductionOperator, InT init) const;
+        /** The same over each value transformed by a FLAMEGPU_CUSTOM_TRANSFORM operator (:267-268). */
+        template <typename InT, typename OutT, typename TransformT, typename ReductionT>
+        OutT transformReduce(const std::string& variable, TransformT transformOperator, ReductionT reductionOperator,
+                             OutT init) const;
 
      private:
-        LogValue reduce(const std::string& variable, const std::type_info& t, LoggingConfig::Reduction r) const;
+        LogValue reduce_log(const std::string& variable, const std::type_info& t, LoggingConfig::Reduction r) const;
+        // The device column of a scalar variable of type t (the checks of the
+        // reductions), the population count on the device, and the stream.
+        const void* device_column(const std::string& variable, const std::type_info& t, const uint32_t** d_n,
+                                  cudaStream_t* stream) const;
         template <typename OutT>
         static OutT convert(const LogValue& v) {
             const auto t = v.type;
