@@ -757,6 +757,8 @@ struct BatchedSim {
         P.birth_next_id = b.births ? d_next_ids : nullptr;
         P.d_step = d_misc;
         P.fn_uid = b.fn->uid;
+        P.agent_hash = detail::fnv1a32(agent->name);
+        P.state_hash = detail::fnv1a32(b.fn->initial_state);
         P.error = d_misc + 1;
         P.batch = b.d_rt;
         P.batch_counts = d_counts;

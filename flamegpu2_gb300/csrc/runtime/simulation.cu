@@ -1374,6 +1374,8 @@ struct SimulationImpl {
             C.d_step = d_step();
             C.seed = config.random_seed;
             C.fn_uid = f.fn->uid;
+            C.agent_hash = fnv1a32(l.agent->name);
+            C.state_hash = fnv1a32(f.fn->initial_state);
             C.error = d_error();
             C.env = d_env;
             cudaError_t ce = cudaSuccess;
@@ -1435,6 +1437,8 @@ struct SimulationImpl {
         P.d_step = d_step();
         P.seed = config.random_seed;
         P.fn_uid = f.fn->uid;
+        P.agent_hash = fnv1a32(l.agent->name);
+        P.state_hash = fnv1a32(f.fn->initial_state);
         P.error = d_error();
         P.env = d_env;
         if (f.key_msg) P.keyed[0] = build_key_target(f);

@@ -171,6 +171,8 @@ struct LaunchParams {
     const uint32_t* d_step;      // step counter
     uint64_t seed;               // simulation random seed
     uint32_t fn_uid;             // unique id of this agent function (random streams)
+    uint32_t agent_hash;         // FNV-1a of the function's agent name and initial state (isAgent / isState)
+    uint32_t state_hash;
     uint32_t* error;             // device error record: [code, hash, index, count]
     const char* env;             // environment buffer (env table pointers are offsets into it)
     // batched launch (null batch: a single simulation)

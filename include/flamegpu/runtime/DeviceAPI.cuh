@@ -1012,6 +1012,8 @@ class DeviceAPI {
             }
             return claimed;
         }
+        /** Claims the new agent's id now (DeviceAPI.cuh:548-557 of the reference); getID() returns it. */
+        __device__ void genID() const { (void)getID(); }
         __device__ uint32_t born() const { return is_born; }
 
      private:
@@ -1086,6 +1088,10 @@ class DeviceAPI {
     __device__ id_t getID() const { return detail::read_rw<id_t>(P, &P.T.agent, detail::VarName("_id").hash, index); }
     __device__ unsigned int getStepCounter() const { return detail::ctx().step; }
     __device__ unsigned int getIndex() const { return index - detail::ctx().row_begin; }
+    /** Whether the function runs on agents of this name / in this state
+     *  (DeviceAPI.cuh:366-380 of the reference; names compared by hash). */
+    __device__ bool isAgent(const char* agent_name) const { return detail::fnv1a32(agent_name, ~0u) == P.agent_hash; }
+    __device__ bool isState(const char* agent_state) const { return detail::fnv1a32(agent_state, ~0u) == P.state_hash; }
 
     typename MessageIn::In message_in;
     typename MessageOut::Out message_out;
@@ -1119,6 +1125,9 @@ class ReadOnlyDeviceAPI {
     }
     __device__ id_t getID() const { return detail::read_rw<id_t>(P, &P.T.agent, detail::VarName("_id").hash, index); }
     __device__ unsigned int getStepCounter() const { return detail::ctx().step; }
+    __device__ unsigned int getIndex() const { return index - detail::ctx().row_begin; }
+    __device__ bool isAgent(const char* agent_name) const { return detail::fnv1a32(agent_name, ~0u) == P.agent_hash; }
+    __device__ bool isState(const char* agent_state) const { return detail::fnv1a32(agent_state, ~0u) == P.state_hash; }
 
     DeviceEnvironment environment;
     AgentRandom random;
