@@ -73,7 +73,7 @@ void RunPlan::setPopulation(const AgentVector& population, const std::string& st
 void RunPlan::setSpatialMessageBounds(const std::string& message, const std::vector<float>& mn,
                                       const std::vector<float>& mx, float radius) {
     const detail::MessageData* m = model_->message(message);
-    if (!m || m->kind == detail::MessageKind::BruteForce)
+    if (!m || (m->kind != detail::MessageKind::Spatial2D && m->kind != detail::MessageKind::Spatial3D))
         THROW exception::InvalidMessageName(format("No spatial message '%s'", message.c_str()));
     spatial_[message] = SpatialOverride{mn, mx, radius};
 }
@@ -156,6 +156,9 @@ std::string batch_unsupported(const ModelData& m) {
         if (f->message_output_optional) return "optional message output";
         if (!f->message_input.empty() && m.message(f->message_input)->kind == MessageKind::BruteForce)
             return "brute-force message input";
+        if ((!f->message_input.empty() && array_dims(m.message(f->message_input)->kind)) ||
+            (!f->message_output.empty() && array_dims(m.message(f->message_output)->kind)))
+            return "array messages";
     }
     return "";
 }

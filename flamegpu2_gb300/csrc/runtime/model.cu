@@ -41,7 +41,11 @@ detail::MessageData* ModelDescription::new_message(const std::string& name, deta
     m->name = name;
     m->kind = kind;
     const float zero = 0.0f;
-    if (kind != detail::MessageKind::BruteForce) {
+    if (detail::array_dims(kind)) {
+        // the index each message is output to (MessageArray2D.cu:155-158)
+        const uint32_t none = 0;
+        m->variables.push_back(detail::make_variable<uint32_t>("___INDEX", &none, 1));
+    } else if (kind != detail::MessageKind::BruteForce) {
         m->variables.push_back(detail::make_variable<float>("x", &zero, 1));
         m->variables.push_back(detail::make_variable<float>("y", &zero, 1));
         if (kind == detail::MessageKind::Spatial3D) m->variables.push_back(detail::make_variable<float>("z", &zero, 1));
@@ -159,12 +163,24 @@ flamegpu::size_type AgentDescription::getVariableLength(const std::string& name)
 
 // ---------------------------------------------------------------- function
 
+namespace {
+// The device message type a function must name for a message of this kind.
+std::type_index message_type_of(detail::MessageKind k) {
+    switch (k) {
+        case detail::MessageKind::Spatial3D: return std::type_index(typeid(MessageSpatial3D));
+        case detail::MessageKind::Spatial2D: return std::type_index(typeid(MessageSpatial2D));
+        case detail::MessageKind::Array1D: return std::type_index(typeid(MessageArray));
+        case detail::MessageKind::Array2D: return std::type_index(typeid(MessageArray2D));
+        case detail::MessageKind::Array3D: return std::type_index(typeid(MessageArray3D));
+        default: return std::type_index(typeid(MessageBruteForce));
+    }
+}
+}  // namespace
+
 void AgentFunctionDescription::setMessageInput(const std::string& name) {
     detail::MessageData* m = model->message(name);
     if (!m) THROW exception::InvalidMessageName(format("Model has no message '%s'", name.c_str()));
-    const std::type_index want = m->kind == detail::MessageKind::Spatial3D   ? std::type_index(typeid(MessageSpatial3D))
-                                 : m->kind == detail::MessageKind::Spatial2D ? std::type_index(typeid(MessageSpatial2D))
-                                                                             : std::type_index(typeid(MessageBruteForce));
+    const std::type_index want = message_type_of(m->kind);
     if (fn->msg_in_type != want)
         THROW exception::InvalidMessageType(format("Function '%s' input message type does not match message '%s'",
                                                    fn->name.c_str(), name.c_str()));
@@ -176,9 +192,7 @@ void AgentFunctionDescription::setMessageInput(const std::string& name) {
 void AgentFunctionDescription::setMessageOutput(const std::string& name) {
     detail::MessageData* m = model->message(name);
     if (!m) THROW exception::InvalidMessageName(format("Model has no message '%s'", name.c_str()));
-    const std::type_index want = m->kind == detail::MessageKind::Spatial3D   ? std::type_index(typeid(MessageSpatial3D))
-                                 : m->kind == detail::MessageKind::Spatial2D ? std::type_index(typeid(MessageSpatial2D))
-                                                                             : std::type_index(typeid(MessageBruteForce));
+    const std::type_index want = message_type_of(m->kind);
     if (fn->msg_out_type != want)
         THROW exception::InvalidMessageType(format("Function '%s' output message type does not match message '%s'",
                                                    fn->name.c_str(), name.c_str()));

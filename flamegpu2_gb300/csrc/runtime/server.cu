@@ -78,7 +78,10 @@ size_t SimulationServer::estimateBytes(const ModelDescription& model,
         size_t row = 0;
         for (const auto& v : msg->variables) row += (v.bytes() + 3) & ~size_t(3);
         total += max_pop * (2 * row + 32);  // columns, sorted records, build scratch
-        if (msg->kind != detail::MessageKind::BruteForce) {
+        if (detail::array_dims(msg->kind)) {
+            total += static_cast<size_t>(msg->dims[0]) * std::max(1u, msg->dims[1]) * std::max(1u, msg->dims[2]) *
+                     (row + 4);  // the array and its claim words
+        } else if (msg->kind != detail::MessageKind::BruteForce) {
             double bins = 1.0;
             const int dims = msg->kind == detail::MessageKind::Spatial3D ? 3 : 2;
             for (int d = 0; d < dims; ++d) bins *= std::ceil((msg->max[d] - msg->min[d]) / msg->radius);

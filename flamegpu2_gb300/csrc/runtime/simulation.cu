@@ -104,6 +104,48 @@ __global__ void k_max_u32(uint32_t* p, uint32_t v) {
     *p = *p > v ? *p : v;
 }
 
+// Array message build (MessageArray2D.cu:69-101 and CUDAScatter's
+// arrayMessageReorder): the array's columns and claim words were cleared
+// before this launch; every message output this step (valid, its index set)
+// is copied to its index. An index outside the array, or a second message at
+// one index, is a device error (the message is dropped).
+constexpr uint32_t kArrayCols = 32;
+constexpr uint32_t kArrayWriteConflict = 0xA77A0001u;  // the error's name-hash word: raised by the build
+struct ArrayScatter {
+    const char* src[kArrayCols];
+    char* dst[kArrayCols];
+    uint32_t bytes[kArrayCols];  // per column, a multiple of 4
+    uint32_t ncols;
+    const uint32_t* index;       // the ___INDEX column (output rows)
+    const uint32_t* valid;       // 1 where the row set its index
+    const uint32_t* d_count;     // rows output this step
+    uint32_t max_n;
+    uint32_t length;             // elements of the array
+    uint32_t* claim;             // per array element
+    uint32_t* error;             // [code, hash, index, count]
+};
+__global__ void k_array_scatter(const __grid_constant__ ArrayScatter a) {
+    grid_dependency_enter();
+    const uint32_t n = min(*a.d_count, a.max_n);
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        if (!a.valid[r]) continue;
+        const uint32_t at = a.index[r];
+        if (at >= a.length || atomicAdd(a.claim + at, 1u) != 0u) {
+            if (atomicCAS(&a.error[0], 0u, static_cast<uint32_t>(kDevArrayMessage)) == 0u) {
+                a.error[1] = kArrayWriteConflict;
+                a.error[2] = r;
+            }
+            atomicAdd(&a.error[3], 1u);
+            continue;
+        }
+        for (uint32_t c = 0; c < a.ncols; ++c) {
+            const uint32_t* s = reinterpret_cast<const uint32_t*>(a.src[c] + static_cast<size_t>(r) * a.bytes[c]);
+            uint32_t* d = reinterpret_cast<uint32_t*>(a.dst[c] + static_cast<size_t>(at) * a.bytes[c]);
+            for (uint32_t w = 0; w < a.bytes[c] / 4u; ++w) d[w] = s[w];
+        }
+    }
+}
+
 // Population columns between the device and page-locked host memory in one
 // launch (the host buffers read or written by the kernel through their
 // mapped device addresses) instead of one copy per column: the set and get
@@ -402,7 +444,16 @@ struct MsgList {
     // (device; cleared at every step end): until then an output truncates it,
     // and a launch over no agents leaves it as it was (CUDASimulation.cu:1050-1059)
     uint32_t* d_filled = nullptr;
-    bool spatial() const { return msg->kind != MessageKind::BruteForce; }
+    // array messages: the array (index order, one column per variable), its
+    // dimensions, a claim word per element (the build's duplicate check) and
+    // its length on the device (the input's message count)
+    uint32_t arr_dims[3] = {1, 1, 1};
+    uint32_t arr_len = 0;
+    std::vector<void*> arr_cols;
+    uint32_t* arr_claim = nullptr;
+    uint32_t* arr_count = nullptr;
+    bool array() const { return array_dims(msg->kind) != 0; }
+    bool spatial() const { return msg->kind == MessageKind::Spatial2D || msg->kind == MessageKind::Spatial3D; }
 };
 
 struct FnRt {
@@ -590,7 +641,19 @@ struct SimulationImpl {
             ml->d_base = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
             ml->d_filled = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));  // zeroed
             for (const auto& v : m->variables) ml->slot_bytes.push_back(round4(v.bytes()));
-            if (m->kind != MessageKind::BruteForce) {
+            if (array_dims(m->kind)) {
+                for (int a = 0; a < 3; ++a) ml->arr_dims[a] = a < array_dims(m->kind) ? m->dims[a] : 1u;
+                const uint64_t len = static_cast<uint64_t>(ml->arr_dims[0]) * ml->arr_dims[1] * ml->arr_dims[2];
+                if (len == 0 || len > 0x7FFFFFFFull)
+                    THROW exception::InvalidMessage(format("Array message '%s' has unset or too large dimensions", m->name.c_str()));
+                if (m->variables.size() > kArrayCols)
+                    THROW exception::InvalidMessage(format("Array message '%s' has more than %u variables", m->name.c_str(), kArrayCols));
+                ml->arr_len = static_cast<uint32_t>(len);
+                for (uint32_t b : ml->slot_bytes) ml->arr_cols.push_back(mem.alloc(static_cast<size_t>(b) * len));
+                ml->arr_claim = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * len));
+                ml->arr_count = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
+                FG_CUDA(cudaMemcpy(ml->arr_count, &ml->arr_len, sizeof(uint32_t), cudaMemcpyHostToDevice));
+            } else if (m->kind != MessageKind::BruteForce) {
                 const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
                 FG_CAPI(fg_spatial_grid_init(&ml->grid, dims, m->min, m->max, m->radius));
                 // PBM padded to a multiple of 4 entries (+4): the staging window copies 16-byte aligned slices
@@ -654,7 +717,7 @@ struct SimulationImpl {
 
     void validate_model() {
         for (const auto& m : model->messages) {
-            if (m->kind == MessageKind::BruteForce) continue;
+            if (m->kind != MessageKind::Spatial2D && m->kind != MessageKind::Spatial3D) continue;
             const int dims = m->kind == MessageKind::Spatial3D ? 3 : 2;
             if (std::isnan(m->radius))
                 THROW exception::InvalidMessage(format("Spatial message '%s' has no radius", m->name.c_str()));
@@ -729,7 +792,7 @@ struct SimulationImpl {
         for (void* p : m.cols) mem.release(p);
         m.cols.clear();
         for (uint32_t b : m.slot_bytes) m.cols.push_back(mem.alloc(static_cast<size_t>(b) * cap));
-        if (m.optional_any) {
+        if (m.optional_any || m.array()) {
             mem.release(m.valid);
             m.valid = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
         }
@@ -852,6 +915,9 @@ struct SimulationImpl {
                     if (f.in->spatial()) {
                         p = reinterpret_cast<char*>(f.in->records + f.in->field_word[v]);
                         stride = f.in->record_words * 4;
+                    } else if (f.in->array()) {
+                        p = static_cast<char*>(f.in->arr_cols[v]);
+                        stride = f.in->slot_bytes[v];
                     } else {
                         p = static_cast<char*>(f.in->optional_any ? f.in->bf_cols[v] : f.in->cols[v]);
                         stride = f.in->slot_bytes[v];
@@ -1291,6 +1357,37 @@ struct SimulationImpl {
         kernel_counter += keys_ready ? 4 : 5;
     }
 
+    // The array of message list m from this step's output: cleared, then each
+    // output message copied to its index (k_array_scatter).
+    void enqueue_array_build(MsgList& m) {
+        for (size_t v = 0; v < m.arr_cols.size(); ++v)
+            FG_CUDA(cudaMemsetAsync(m.arr_cols[v], 0, static_cast<size_t>(m.slot_bytes[v]) * m.arr_len, stream));
+        FG_CUDA(cudaMemsetAsync(m.arr_claim, 0, sizeof(uint32_t) * m.arr_len, stream));
+        if (m.capacity > 0) {
+            ArrayScatter a;
+            std::memset(&a, 0, sizeof(a));
+            int index_var = -1;
+            for (size_t v = 0; v < m.msg->variables.size(); ++v) {
+                if (m.msg->variables[v].name == "___INDEX") index_var = static_cast<int>(v);
+                a.src[v] = static_cast<const char*>(m.cols[v]);
+                a.dst[v] = static_cast<char*>(m.arr_cols[v]);
+                a.bytes[v] = m.slot_bytes[v];
+            }
+            a.ncols = static_cast<uint32_t>(m.msg->variables.size());
+            a.index = static_cast<const uint32_t*>(m.cols[index_var]);
+            a.valid = m.valid;
+            a.d_count = m.d_count;
+            a.max_n = m.capacity;
+            a.length = m.arr_len;
+            a.claim = m.arr_claim;
+            a.error = d_error();
+            const unsigned int grid = std::max(1u, std::min((m.capacity + 255u) / 256u, static_cast<unsigned int>(sms) * 8u));
+            FG_CUDA(launch_kernel(pdl_enabled(), k_array_scatter, grid, 256, 0, stream, a));
+            kernel_counter += 1;
+        }
+        m.needs_build = false;
+    }
+
     // Rows an agent-function launch of list l covers with one block per 128
     // rows: the host's bound on its population rounded up to a power of two
     // (at least one wave of 8 blocks per SM), at most its capacity. The
@@ -1349,6 +1446,8 @@ struct SimulationImpl {
             if (do_sort) timed("sort:" + l.agent->name, [&] { enqueue_sort(f); });
             if (do_build) timed("build:" + f.in->msg->name, [&] { enqueue_build(*f.in, stream, f.build_keyed); });
         }
+        if (f.in && f.in->array() && f.in->needs_build)
+            timed("build:" + f.in->msg->name, [&] { enqueue_array_build(*f.in); });
         const bool append = f.out && f.out->written;
         if (f.out) {
             f.out->written = true;
@@ -1402,8 +1501,10 @@ struct SimulationImpl {
         P.d_n = l.d_count;
         P.d_first = f.fn->condition ? f.d_first : nullptr;
         if (f.out) {
-            P.msg_out_valid = f.out->optional_any ? f.out->valid : nullptr;
-            P.msg_out_always = f.fn->message_output_optional ? 0 : 1;
+            // an array message is output where its agent set the index
+            P.msg_out_valid = (f.out->optional_any || f.out->array()) ? f.out->valid : nullptr;
+            P.msg_out_always = (f.fn->message_output_optional || f.out->array()) ? 0 : 1;
+            for (int a = 0; a < 3; ++a) P.out_dims[a] = f.out->arr_dims[a];
             P.msg_out_count = f.out->d_count;
             P.msg_out_base = append ? f.out->d_base : nullptr;
             P.msg_out_filled = f.out->d_filled;
@@ -1423,6 +1524,9 @@ struct SimulationImpl {
                 if (f.stage && cuda_config.message_stage_bytes >= 1024u &&
                     stage_window_fits(*f.in, cuda_config.message_stage_bytes, agent_block(grid_rows(l))))
                     P.stage_bytes = (cuda_config.message_stage_bytes + 15u) & ~15u;
+            } else if (f.in->array()) {
+                P.in_count = f.in->arr_count;
+                for (int a = 0; a < 3; ++a) P.in_dims[a] = f.in->arr_dims[a];
             } else {
                 P.in_count = f.in->optional_any ? f.in->bf_count : f.in->d_count;
             }
@@ -1457,7 +1561,7 @@ struct SimulationImpl {
         kernel_counter += 1;
         if (f.out) {
             f.out->needs_build = true;
-            if (!f.out->spatial() && f.out->optional_any) {
+            if (!f.out->spatial() && !f.out->array() && f.out->optional_any) {
                 // brute-force optional output: stable compaction of the message rows
                 std::vector<fg_column> cols(f.out->cols.size());
                 for (size_t v = 0; v < cols.size(); ++v) cols[v] = fg_column{f.out->cols[v], f.out->bf_cols[v], f.out->slot_bytes[v]};
@@ -1874,7 +1978,12 @@ struct SimulationImpl {
                                           "agent output is not enabled for this function", "reserved variable name",
                                           "unsupported device call", "message output is not enabled for this function",
                                           "a neighbourhood staging wait gave up (bounded wait)",
-                                          "AgentRandom::uniform() with min > max"};
+                                          "AgentRandom::uniform() with min > max",
+                                          "array message index or search radius out of range, or two messages output to one index"};
+            if (err[0] == kDevArrayMessage && err[1] == kArrayWriteConflict)
+                THROW exception::ArrayMessageWriteConflict(format(
+                    "Two array messages were output to one index, or one outside the array (message row %u, %u occurrences)",
+                    err[2], err[3]));
             const char* what = err[0] < sizeof(names) / sizeof(names[0]) ? names[err[0]] : "device error";
             THROW exception::DeviceError(format("Device error: %s (name hash 0x%08x, agent index %u, %u occurrences)", what,
                                                 err[1], err[2], err[3]));

@@ -129,6 +129,7 @@ enum DeviceErrorCode : uint32_t {
     kDevMessageOutNotEnabled = 10,
     kDevStageTimeout = 11,
     kDevRandomRange = 12,
+    kDevArrayMessage = 13,
 };
 
 /** Kernel parameters of one agent function launch (passed __grid_constant__).
@@ -161,6 +162,8 @@ struct LaunchParams {
     // 4 * dims + slot * in_pay_stride, slot = table_slot(in_pay_mult, in_pay_shift, hash)
     uint32_t in_pay_mult, in_pay_shift, in_pay_stride;
     uint32_t in_pbm_alloc;       // PBM entries readable (multiple of 4, >= binCount + 1)
+    uint32_t in_dims[3];         // array message input: dimensions (1 past the last used)
+    uint32_t out_dims[3];        // array message output: dimensions
     uint32_t stage_bytes;        // shared memory for staging neighbour records (0 = off)
     // birth / death
     uint32_t* birth_flags;       // 1 where agent_out was used, 2 if its id was also claimed (null if disabled)

@@ -53,6 +53,7 @@ FLAMEGPU_DERIVED_EXCEPTION(InvalidConfiguration)
 FLAMEGPU_DERIVED_EXCEPTION(ReservedName)
 FLAMEGPU_DERIVED_EXCEPTION(JSONError)
 FLAMEGPU_DERIVED_EXCEPTION(AgentIDCollision)
+FLAMEGPU_DERIVED_EXCEPTION(ArrayMessageWriteConflict)
 #undef FLAMEGPU_DERIVED_EXCEPTION
 
 inline std::string format(const char* fmt, ...) {

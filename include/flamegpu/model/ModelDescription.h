@@ -37,7 +37,11 @@ typedef void (*FLAMEGPU_HOST_FUNCTION_POINTER)(HostAPI* api);
 
 namespace detail {
 
-enum class MessageKind { BruteForce = 1, Spatial2D = 2, Spatial3D = 3 };
+enum class MessageKind { BruteForce = 1, Spatial2D = 2, Spatial3D = 3, Array1D = 4, Array2D = 5, Array3D = 6 };
+// the array message kinds' dimension count (0: not an array)
+inline int array_dims(MessageKind k) {
+    return k == MessageKind::Array1D ? 1 : k == MessageKind::Array2D ? 2 : k == MessageKind::Array3D ? 3 : 0;
+}
 
 struct Variable {
     std::string name;
@@ -92,6 +96,7 @@ struct MessageData {
     float max[3] = {std::numeric_limits<float>::quiet_NaN(), std::numeric_limits<float>::quiet_NaN(),
                     std::numeric_limits<float>::quiet_NaN()};
     bool persistent = false;
+    uint32_t dims[3] = {0, 0, 0};  // array messages: length along each dimension (0: unset)
     const Variable* find(const std::string& n) const {
         for (const auto& v : variables)
             if (v.name == n) return &v;
@@ -255,6 +260,52 @@ class MessageSpatial3D::Description : public MessageSpatial2D::Description {
     void setMaxZ(float v) { check_max(2, v); data->max[2] = v; }
     float getMinZ() const { return data->min[2]; }
     float getMaxZ() const { return data->max[2]; }
+};
+
+/** MessageArray::Description (MessageArrayHost.h): a list of setLength() messages,
+ *  each output to the index its agent sets. */
+class MessageArray::Description : public MessageBruteForce::Description {
+ public:
+    using MessageBruteForce::Description::Description;
+    void setLength(flamegpu::size_type len) {
+        if (len == 0) THROW exception::InvalidArgument("Array message length must be above zero");
+        data->dims[0] = len;
+        data->dims[1] = data->dims[2] = 1;
+    }
+    flamegpu::size_type getLength() const { return data->dims[0]; }
+};
+
+/** MessageArray2D::Description (MessageArray2DHost.h, MessageArray2D.cu:139-148). */
+class MessageArray2D::Description : public MessageBruteForce::Description {
+ public:
+    using MessageBruteForce::Description::Description;
+    void setDimensions(flamegpu::size_type x, flamegpu::size_type y) {
+        if (x == 0 || y == 0) THROW exception::InvalidArgument("All dimensions must be above zero in array2D message");
+        data->dims[0] = x;
+        data->dims[1] = y;
+        data->dims[2] = 1;
+    }
+    void setDimensions(const std::array<flamegpu::size_type, 2>& d) { setDimensions(d[0], d[1]); }
+    std::array<flamegpu::size_type, 2> getDimensions() const { return {data->dims[0], data->dims[1]}; }
+    flamegpu::size_type getDimX() const { return data->dims[0]; }
+    flamegpu::size_type getDimY() const { return data->dims[1]; }
+};
+
+/** MessageArray3D::Description (MessageArray3DHost.h). */
+class MessageArray3D::Description : public MessageBruteForce::Description {
+ public:
+    using MessageBruteForce::Description::Description;
+    void setDimensions(flamegpu::size_type x, flamegpu::size_type y, flamegpu::size_type z) {
+        if (x == 0 || y == 0 || z == 0) THROW exception::InvalidArgument("All dimensions must be above zero in array3D message");
+        data->dims[0] = x;
+        data->dims[1] = y;
+        data->dims[2] = z;
+    }
+    void setDimensions(const std::array<flamegpu::size_type, 3>& d) { setDimensions(d[0], d[1], d[2]); }
+    std::array<flamegpu::size_type, 3> getDimensions() const { return {data->dims[0], data->dims[1], data->dims[2]}; }
+    flamegpu::size_type getDimX() const { return data->dims[0]; }
+    flamegpu::size_type getDimY() const { return data->dims[1]; }
+    flamegpu::size_type getDimZ() const { return data->dims[2]; }
 };
 
 // --------------------------------------------------------- agent functions
@@ -456,6 +507,9 @@ class ModelDescription {
     static detail::MessageKind kind_of() {
         if constexpr (std::is_same_v<MsgType, MessageSpatial3D>) return detail::MessageKind::Spatial3D;
         else if constexpr (std::is_same_v<MsgType, MessageSpatial2D>) return detail::MessageKind::Spatial2D;
+        else if constexpr (std::is_same_v<MsgType, MessageArray>) return detail::MessageKind::Array1D;
+        else if constexpr (std::is_same_v<MsgType, MessageArray2D>) return detail::MessageKind::Array2D;
+        else if constexpr (std::is_same_v<MsgType, MessageArray3D>) return detail::MessageKind::Array3D;
         else return detail::MessageKind::BruteForce;
     }
     detail::MessageData* new_message(const std::string& name, detail::MessageKind kind);

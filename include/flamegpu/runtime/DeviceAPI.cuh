@@ -24,6 +24,9 @@ class MessageNone;
 class MessageBruteForce;
 class MessageSpatial2D;
 class MessageSpatial3D;
+class MessageArray;
+class MessageArray2D;
+class MessageArray3D;
 
 namespace detail {
 
@@ -460,6 +463,270 @@ class MessageBruteForce {
     };
 };
 
+
+/**
+ * Array messages (MessageArrayDevice.cuh, MessageArray2DDevice.cuh,
+ * MessageArray3DDevice.cuh): the input list is the array itself, index
+ * x + dim_x * (y + dim_y * z), holding the message output to that index this
+ * step or zeros. A search iterates the Moore (or von Neumann, |dx| + |dy| +
+ * |dz| <= radius) neighbourhood of a cell, origin excluded, x offset outermost
+ * and z innermost, clamped to the array or wrapped around it.
+ */
+template <int D>
+class ArrayIn {
+ public:
+    /** A message of the array (at(), or a neighbour of a search; an index past
+     *  the array is an invalid message whose variables read 0). */
+    class Message : public MessageView {
+     public:
+        __device__ Message(const detail::LaunchParams& p, uint32_t i, int ox = 0, int oy = 0, int oz = 0)
+            : MessageView(p, i), off{ox, oy, oz} {}
+        template <typename T>
+        __device__ T getVariable(detail::VarName name) const {
+            if (index >= P.in_dims[0] * P.in_dims[1] * P.in_dims[2]) {
+                detail::device_error(P, detail::kDevArrayMessage, name.hash, index);
+                return T{};
+            }
+            return MessageView::getVariable<T>(name);
+        }
+        template <typename T, flamegpu::size_type N>
+        __device__ T getVariable(detail::VarName name, unsigned int i) const {
+            if (index >= P.in_dims[0] * P.in_dims[1] * P.in_dims[2]) {
+                detail::device_error(P, detail::kDevArrayMessage, name.hash, index);
+                return T{};
+            }
+            return MessageView::getVariable<T, N>(name, i);
+        }
+        __device__ uint32_t getX() const { return index % P.in_dims[0]; }
+        __device__ uint32_t getY() const { return (index / P.in_dims[0]) % P.in_dims[1]; }
+        __device__ uint32_t getZ() const { return index / (P.in_dims[0] * P.in_dims[1]); }
+        __device__ int getOffsetX() const { return off[0]; }
+        __device__ int getOffsetY() const { return off[1]; }
+        __device__ int getOffsetZ() const { return off[2]; }
+
+     private:
+        int off[3];
+    };
+
+    /** The neighbourhood of loc within radius: clamped to the array (WRAP
+     *  false) or wrapped around it, Moore (VN false) or von Neumann. */
+    template <bool WRAP, bool VN>
+    class Filter {
+     public:
+        class iterator {
+         public:
+            __device__ iterator(const Filter& f, bool at_end) : F(f) {
+                for (int a = 0; a < 3; ++a) d[a] = F.lo[a];
+                if (at_end || F.empty) {
+                    d[0] = F.hi[0] + 1;
+                    return;
+                }
+                skip();
+            }
+            __device__ iterator& operator++() {
+                step();
+                skip();
+                return *this;
+            }
+            __device__ bool operator!=(const iterator& o) const { return d[0] != o.d[0] || d[1] != o.d[1] || d[2] != o.d[2]; }
+            __device__ bool operator==(const iterator& o) const { return !(*this != o); }
+            __device__ Message operator*() const {
+                uint32_t idx = 0, mul = 1;
+                for (int a = 0; a < D; ++a) {
+                    const int dim = static_cast<int>(F.P.in_dims[a]);
+                    int c = static_cast<int>(F.loc[a]) + d[a];
+                    if (WRAP) c = (c % dim + dim) % dim;
+                    idx += static_cast<uint32_t>(c) * mul;
+                    mul *= static_cast<uint32_t>(dim);
+                }
+                return Message(F.P, idx, d[0], d[1], d[2]);
+            }
+
+         private:
+            // next offset: the innermost axis first
+            __device__ void step() {
+                for (int a = D - 1; a >= 0; --a) {
+                    if (d[a] < F.hi[a] || a == 0) {
+                        ++d[a];
+                        return;
+                    }
+                    d[a] = F.lo[a];
+                }
+            }
+            // past the origin and, for von Neumann, the cells beyond the radius
+            __device__ void skip() {
+                while (d[0] <= F.hi[0]) {
+                    const int manhattan = abs(d[0]) + abs(d[1]) + abs(d[2]);
+                    if (manhattan != 0 && (!VN || manhattan <= F.radius)) return;
+                    step();
+                }
+            }
+            const Filter& F;
+            int d[3];
+        };
+        __device__ Filter(const detail::LaunchParams& p, const uint32_t (&l)[3], uint32_t r, bool bad)
+            : P(p), radius(static_cast<int>(r)), empty(bad) {
+            for (int a = 0; a < 3; ++a) {
+                loc[a] = l[a];
+                if (a >= D) {
+                    lo[a] = hi[a] = 0;
+                } else if (WRAP) {
+                    lo[a] = -radius;
+                    hi[a] = radius;
+                } else {
+                    const int x = static_cast<int>(l[a]), dim = static_cast<int>(p.in_dims[a]);
+                    lo[a] = x - radius < 0 ? -x : -radius;
+                    hi[a] = x + radius >= dim ? dim - 1 - x : radius;
+                }
+            }
+        }
+        __device__ iterator begin() const { return iterator(*this, false); }
+        __device__ iterator end() const { return iterator(*this, true); }
+
+        const detail::LaunchParams& P;
+        uint32_t loc[3];
+        int lo[3], hi[3];
+        int radius;
+        bool empty;
+    };
+
+    __device__ explicit ArrayIn(const detail::LaunchParams& p) : P(p) {}
+    __device__ uint32_t getDimX() const { return P.in_dims[0]; }
+    __device__ uint32_t getDimY() const { return P.in_dims[1]; }
+    __device__ uint32_t getDimZ() const { return P.in_dims[2]; }
+    __device__ uint32_t size() const { return P.in_dims[0] * P.in_dims[1] * P.in_dims[2]; }
+
+ protected:
+    // The message at loc (an invalid one, reading 0, outside the array).
+    __device__ Message at_loc(const uint32_t (&l)[3]) const {
+        bool out = false;
+        for (int a = 0; a < D; ++a) out = out || l[a] >= P.in_dims[a];
+        if (out) {
+#if FLAMEGPU_SEATBELTS
+            detail::device_error(P, detail::kDevArrayMessage, 0, 0);
+#endif
+            return Message(P, size());
+        }
+        return Message(P, l[0] + P.in_dims[0] * (l[1] + P.in_dims[1] * l[2]));
+    }
+    // Whether a search at loc within radius is invalid (MessageArray2DDevice.cuh:1013-1025,
+    // :1043-1058): radius 0, an origin outside the array, or for a wrapped
+    // search a diameter wider than the array (cells would be read twice).
+    __device__ bool bad_search(const uint32_t (&l)[3], uint32_t radius, bool wrap) const {
+        bool bad = radius == 0;
+        for (int a = 0; a < D; ++a) {
+            bad = bad || l[a] >= P.in_dims[a];
+            if (wrap) bad = bad || 2u * radius + 1u > P.in_dims[a];
+        }
+#if FLAMEGPU_SEATBELTS
+        if (bad) detail::device_error(P, detail::kDevArrayMessage, 0, radius);
+#endif
+        return bad;
+    }
+    template <bool WRAP, bool VN>
+    __device__ Filter<WRAP, VN> search(const uint32_t (&l)[3], uint32_t radius) const {
+        return Filter<WRAP, VN>(P, l, radius, bad_search(l, radius, WRAP));
+    }
+    const detail::LaunchParams& P;
+};
+
+/** Output half of the array messages: setIndex places the message. */
+template <int D>
+class ArrayOut : public MessageOutBase {
+ public:
+    __device__ ArrayOut(const detail::LaunchParams& p, uint32_t idx) : MessageOutBase(p, idx) {}
+    /** Whether setIndex was called: the message is output (MessageArray2DDevice.cuh:1360-1375). */
+    __device__ uint32_t written() const { return index_set; }
+
+ protected:
+    __device__ void set_index(const uint32_t (&l)[3]) const {
+        bool out = false;
+        for (int a = 0; a < D; ++a) out = out || l[a] >= P.out_dims[a];
+        if (out) {
+            detail::device_error(P, detail::kDevArrayMessage, 0, index);
+            return;
+        }
+        detail::write_var<uint32_t>(P, &P.T.msg_out, detail::VarName("___INDEX").hash, index,
+                                    l[0] + P.out_dims[0] * (l[1] + P.out_dims[1] * l[2]));
+        index_set = 1;
+    }
+    mutable uint32_t index_set = 0;
+};
+
+class MessageArray {
+ public:
+    class Description;
+    class In : public ArrayIn<1> {
+     public:
+        __device__ explicit In(const detail::LaunchParams& p) : ArrayIn<1>(p) {}
+        __device__ Message at(uint32_t x) const { return at_loc({x, 0u, 0u}); }
+        __device__ Filter<false, false> operator()(uint32_t x, uint32_t radius = 1) const {
+            return search<false, false>({x, 0u, 0u}, radius);
+        }
+        __device__ Filter<true, false> wrap(uint32_t x, uint32_t radius = 1) const {
+            return search<true, false>({x, 0u, 0u}, radius);
+        }
+    };
+    class Out : public ArrayOut<1> {
+     public:
+        __device__ Out(const detail::LaunchParams& p, uint32_t idx) : ArrayOut<1>(p, idx) {}
+        __device__ void setIndex(uint32_t x) const { set_index({x, 0u, 0u}); }
+    };
+};
+
+class MessageArray2D {
+ public:
+    class Description;
+    class In : public ArrayIn<2> {
+     public:
+        __device__ explicit In(const detail::LaunchParams& p) : ArrayIn<2>(p) {}
+        __device__ Message at(uint32_t x, uint32_t y) const { return at_loc({x, y, 0u}); }
+        __device__ Filter<false, false> operator()(uint32_t x, uint32_t y, uint32_t radius = 1) const {
+            return search<false, false>({x, y, 0u}, radius);
+        }
+        __device__ Filter<true, false> wrap(uint32_t x, uint32_t y, uint32_t radius = 1) const {
+            return search<true, false>({x, y, 0u}, radius);
+        }
+        __device__ Filter<false, true> vn(uint32_t x, uint32_t y, uint32_t radius = 1) const {
+            return search<false, true>({x, y, 0u}, radius);
+        }
+        __device__ Filter<true, true> vn_wrap(uint32_t x, uint32_t y, uint32_t radius = 1) const {
+            return search<true, true>({x, y, 0u}, radius);
+        }
+    };
+    class Out : public ArrayOut<2> {
+     public:
+        __device__ Out(const detail::LaunchParams& p, uint32_t idx) : ArrayOut<2>(p, idx) {}
+        __device__ void setIndex(uint32_t x, uint32_t y) const { set_index({x, y, 0u}); }
+    };
+};
+
+class MessageArray3D {
+ public:
+    class Description;
+    class In : public ArrayIn<3> {
+     public:
+        __device__ explicit In(const detail::LaunchParams& p) : ArrayIn<3>(p) {}
+        __device__ Message at(uint32_t x, uint32_t y, uint32_t z) const { return at_loc({x, y, z}); }
+        __device__ Filter<false, false> operator()(uint32_t x, uint32_t y, uint32_t z, uint32_t radius = 1) const {
+            return search<false, false>({x, y, z}, radius);
+        }
+        __device__ Filter<true, false> wrap(uint32_t x, uint32_t y, uint32_t z, uint32_t radius = 1) const {
+            return search<true, false>({x, y, z}, radius);
+        }
+        __device__ Filter<false, true> vn(uint32_t x, uint32_t y, uint32_t z, uint32_t radius = 1) const {
+            return search<false, true>({x, y, z}, radius);
+        }
+        __device__ Filter<true, true> vn_wrap(uint32_t x, uint32_t y, uint32_t z, uint32_t radius = 1) const {
+            return search<true, true>({x, y, z}, radius);
+        }
+    };
+    class Out : public ArrayOut<3> {
+     public:
+        __device__ Out(const detail::LaunchParams& p, uint32_t idx) : ArrayOut<3>(p, idx) {}
+        __device__ void setIndex(uint32_t x, uint32_t y, uint32_t z) const { set_index({x, y, z}); }
+    };
+};
 
 /**
  * A message of a spatial input list: a view of its sorted record. `row` is
