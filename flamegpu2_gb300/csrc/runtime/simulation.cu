@@ -510,6 +510,12 @@ struct SimulationImpl {
     unsigned long long* d_agent_steps = nullptr;  // [0] agents summed over the steps run, [1] agents now
     unsigned long long host_agent_steps = 0;      // the same for populations that only the host changes
     CUDASimulation* owner = nullptr;  // the simulation this implements (host functions reach it)
+    // HostRandom's engine: seeded with the simulation's random seed when the
+    // configuration is applied (RandomManager::reseed)
+    std::mt19937_64 host_rng{0};
+    uint64_t host_rng_seed = 0;
+    bool host_rng_applied = false;
+    uint64_t host_rng_applied_seed = 0;
     // agents created by host functions (HostAgentAPI::newAgent), per (agent, state),
     // joining their populations when the host functions return
     std::map<std::pair<std::string, std::string>, std::unique_ptr<AgentVector>> host_births;
@@ -2024,6 +2030,44 @@ void HostAPI::Environment::set(const std::string& name, const std::type_info& t,
     THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
 }
 
+void HostAPI::Environment::element(const std::string& name, const std::type_info& t, size_t size,
+                                    flamegpu::size_type n, flamegpu::size_type index, void* out, const void* in) const {
+    for (size_t i = 0; i < sim->model->environment.size(); ++i) {
+        const auto& p = sim->model->environment[i];
+        if (p.name != name) continue;
+        if (p.type != std::type_index(t) || p.type_size != size)
+            THROW exception::InvalidEnvPropertyType(format("Environment property '%s' has another type", name.c_str()));
+        if (n != 0 && n != p.elements)
+            THROW exception::OutOfBoundsException(format("Environment property '%s' has %u elements, not %u", name.c_str(),
+                                                         p.elements, static_cast<unsigned>(n)));
+        if (index >= p.elements)
+            THROW exception::OutOfBoundsException(format("Index %u is past the %u elements of environment property '%s'",
+                                                         static_cast<unsigned>(index), p.elements, name.c_str()));
+        char* at = sim->env_host.data() + sim->env_offset[i] + static_cast<size_t>(index) * size;
+        std::memcpy(out, at, size);
+        if (in) {
+            if (p.is_const) THROW exception::ReservedName(format("Environment property '%s' is constant", name.c_str()));
+            std::memcpy(at, in, size);
+            sim->env_dirty = true;
+        }
+        return;
+    }
+    THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+}
+
+size_t HostAPI::Environment::elements(const std::string& name) const {
+    for (const auto& p : sim->model->environment)
+        if (p.name == name) return p.elements;
+    THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+}
+
+std::mt19937_64& HostAPI::Random::engine() const { return sim->host_rng; }
+void HostAPI::Random::setSeed(uint64_t seed) {
+    sim->host_rng_seed = seed;
+    sim->host_rng.seed(seed);
+}
+uint64_t HostAPI::Random::getSeed() const { return sim->host_rng_seed; }
+
 void HostAPI::Environment::setRaw(const std::string& name, const void* in, size_t size) {
     for (size_t i = 0; i < sim->model->environment.size(); ++i) {
         const auto& p = sim->model->environment[i];
@@ -2111,6 +2155,14 @@ CUDASimulation::SimConfig& CUDASimulation::SimulationConfig() { return impl->con
 CUDASimulation::Config& CUDASimulation::CUDAConfig() { return impl->cuda_config; }
 void CUDASimulation::applyConfig() {
     impl->invalidate();
+    // RandomManager::reseed: the host draws follow the simulation's seed (a
+    // reapplied configuration with the same seed keeps the sequence going)
+    if (!impl->host_rng_applied || impl->host_rng_applied_seed != impl->config.random_seed) {
+        impl->host_rng_applied = true;
+        impl->host_rng_applied_seed = impl->config.random_seed;
+        impl->host_rng_seed = impl->config.random_seed;
+        impl->host_rng.seed(impl->config.random_seed);
+    }
     if (!impl->config.input_file.empty()) loadState(impl->config.input_file);
 }
 

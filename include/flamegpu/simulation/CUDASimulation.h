@@ -10,6 +10,7 @@
 
 #include <cstdint>
 #include <memory>
+#include <random>
 #include <string>
 #include <tuple>
 #include <typeinfo>
@@ -72,6 +73,47 @@ class HostAPI {
             set(name, typeid(T), sizeof(T), &value);
             return old;
         }
+        /** Array properties (HostEnvironment.cuh:208-262): the whole array, one
+         *  element (N = 0: any length), or as a vector; set returns the old value(s). */
+        template <typename T, flamegpu::size_type N>
+        std::array<T, N> getProperty(const std::string& name) const {
+            std::array<T, N> v;
+            for (flamegpu::size_type i = 0; i < N; ++i) element(name, typeid(T), sizeof(T), N, i, &v[i], nullptr);
+            return v;
+        }
+        template <typename T, flamegpu::size_type N = 0>
+        T getProperty(const std::string& name, flamegpu::size_type index) const {
+            T v;
+            element(name, typeid(T), sizeof(T), N, index, &v, nullptr);
+            return v;
+        }
+        template <typename T>
+        std::vector<T> getPropertyArray(const std::string& name) const {
+            std::vector<T> v(elements(name));
+            for (size_t i = 0; i < v.size(); ++i) element(name, typeid(T), sizeof(T), 0, static_cast<flamegpu::size_type>(i), &v[i], nullptr);
+            return v;
+        }
+        template <typename T, flamegpu::size_type N>
+        std::array<T, N> setProperty(const std::string& name, const std::array<T, N>& value) {
+            std::array<T, N> old;
+            for (flamegpu::size_type i = 0; i < N; ++i) element(name, typeid(T), sizeof(T), N, i, &old[i], &value[i]);
+            return old;
+        }
+        template <typename T, flamegpu::size_type N = 0>
+        T setProperty(const std::string& name, flamegpu::size_type index, T value) {
+            T old;
+            element(name, typeid(T), sizeof(T), N, index, &old, &value);
+            return old;
+        }
+        template <typename T>
+        std::vector<T> setPropertyArray(const std::string& name, const std::vector<T>& value) {
+            if (value.size() != elements(name))
+                THROW exception::OutOfBoundsException(exception::format("Environment property '%s' has another length", name.c_str()));
+            std::vector<T> old(value.size());
+            for (size_t i = 0; i < value.size(); ++i)
+                element(name, typeid(T), sizeof(T), 0, static_cast<flamegpu::size_type>(i), &old[i], &value[i]);
+            return old;
+        }
 
         /** Set a property from raw bytes (size checked). */
         void setRaw(const std::string& name, const void* value, size_t size);
@@ -79,6 +121,49 @@ class HostAPI {
      private:
         void get(const std::string& name, const std::type_info& t, size_t size, void* out) const;
         void set(const std::string& name, const std::type_info& t, size_t size, const void* in);
+        // element index of an array property (length n, 0: any): read into out, then written from in if given
+        void element(const std::string& name, const std::type_info& t, size_t size, flamegpu::size_type n,
+                     flamegpu::size_type index, void* out, const void* in) const;
+        size_t elements(const std::string& name) const;
+        detail::SimulationImpl* sim;
+    };
+    /** HostRandom (include/flamegpu/runtime/random/HostRandom.cuh:22-66): host-side
+     *  draws from one std::mt19937_64 per simulation, seeded with its random seed
+     *  (setSeed reseeds it). */
+    class Random {
+     public:
+        explicit Random(detail::SimulationImpl* s) : sim(s) {}
+        template <typename T>
+        T uniform() const {
+            static_assert(std::is_floating_point<T>::value, "HostRandom::uniform<T>() takes a floating point type");
+            return std::uniform_real_distribution<T>(T(0), T(1))(engine());
+        }
+        template <typename T>
+        T normal() const {
+            static_assert(std::is_floating_point<T>::value, "HostRandom::normal<T>() takes a floating point type");
+            return std::normal_distribution<T>(T(0), T(1))(engine());
+        }
+        template <typename T>
+        T logNormal(T mean, T stddev) const {
+            static_assert(std::is_floating_point<T>::value, "HostRandom::logNormal<T>() takes a floating point type");
+            return std::lognormal_distribution<T>(mean, stddev)(engine());
+        }
+        /** An integer in [min, max] (HostRandom.cuh:96-140). */
+        template <typename T>
+        T uniform(T min, T max) const {
+            static_assert(std::is_integral<T>::value, "HostRandom::uniform<T>(min, max) takes an integer type");
+            using W = typename std::conditional<std::is_signed<T>::value, int64_t, uint64_t>::type;
+            return static_cast<T>(std::uniform_int_distribution<W>(static_cast<W>(min), static_cast<W>(max))(engine()));
+        }
+        template <typename T = unsigned int>
+        unsigned int poisson(double mean = 1.0) const {
+            return static_cast<unsigned int>(std::poisson_distribution<unsigned int>(mean)(engine()));
+        }
+        void setSeed(uint64_t seed);
+        uint64_t getSeed() const;
+
+     private:
+        std::mt19937_64& engine() const;
         detail::SimulationImpl* sim;
     };
     /** HostAgentAPI (include/flamegpu/runtime/agent/HostAgentAPI.cuh:134-227). */
@@ -154,14 +239,20 @@ class HostAPI {
         detail::SimulationImpl* sim;
         std::string agent, state;
     };
-    explicit HostAPI(detail::SimulationImpl* s) : environment(s), sim(s) {}
+    explicit HostAPI(detail::SimulationImpl* s) : environment(s), random(s), sim(s) {}
     AgentAPI agent(const std::string& name, const std::string& state = "default") { return AgentAPI(sim, name, state); }
     unsigned int getStepCounter() const;
     Environment environment;
+    Random random;
 
  private:
     detail::SimulationImpl* sim;
 };
+
+/** The reference's names of the host API's parts. */
+using HostAgentAPI = HostAPI::AgentAPI;
+using HostEnvironment = HostAPI::Environment;
+using HostRandom = HostAPI::Random;
 
 class CUDASimulation {
  public:
