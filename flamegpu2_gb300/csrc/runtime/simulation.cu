@@ -146,6 +146,103 @@ __global__ void k_array_scatter(const __grid_constant__ ArrayScatter a) {
     }
 }
 
+// HostAgentAPI::sort (HostAgentAPI.cuh:856-1017, a radix sort of (key, row)
+// pairs, then every column gathered): a least-significant-digit radix sort
+// of 8-bit digits. Keys are the variable's bits made order-preserving as
+// unsigned integers (sign bit flipped for signed integers; for floating
+// point, all bits of negatives and the sign bit of the rest), inverted for a
+// descending sort, cut to bits [begin, end). Each pass: per 2,048-row tile
+// the digit counts (digit-major, so that one scan gives every tile's start
+// for every digit), then each tile writes its rows in row order: within a
+// round of 256 rows a row's place is the rows of its digit in earlier rounds,
+// in lower warps of this round and in lower lanes of its warp. Stable, so a
+// second key sorts ties of the first.
+constexpr uint32_t kSortTile = 2048;
+__global__ void k_hsort_keys(const char* col, uint32_t kind, uint32_t bytes, uint32_t invert, uint32_t begin,
+                             uint32_t bits, uint32_t n, uint64_t* keys, uint32_t* rows) {
+    grid_dependency_enter();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t u = 0;
+        const char* p = col + static_cast<size_t>(i) * bytes;
+        switch (bytes) {
+            case 1: u = *reinterpret_cast<const uint8_t*>(p); break;
+            case 2: u = *reinterpret_cast<const uint16_t*>(p); break;
+            case 4: u = *reinterpret_cast<const uint32_t*>(p); break;
+            default: u = *reinterpret_cast<const uint64_t*>(p); break;
+        }
+        const uint32_t w = 8u * bytes;
+        const uint64_t sign = 1ull << (w - 1u);
+        const uint64_t all = w == 64u ? ~0ull : ((1ull << w) - 1ull);
+        if (kind == 1u) u ^= sign;                                // signed integer
+        else if (kind == 2u) u ^= (u & sign) ? all : sign;        // floating point
+        if (invert) u = ~u & all;
+        u >>= begin;
+        if (bits < 64u) u &= (1ull << bits) - 1ull;
+        keys[i] = u;
+        rows[i] = i;
+    }
+}
+__global__ void __launch_bounds__(256) k_hsort_counts(const uint64_t* keys, uint32_t n, uint32_t shift, uint32_t ntiles,
+                                                     uint32_t* counts) {
+    grid_dependency_enter();
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kSortTile;
+    for (uint32_t r = 0; r < kSortTile / 256u; ++r) {
+        const uint32_t row = base + r * 256u + threadIdx.x;
+        if (row < n) atomicAdd(&h[(keys[row] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    counts[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+__global__ void __launch_bounds__(256) k_hsort_scatter(const uint64_t* keys_in, const uint32_t* rows_in, uint64_t* keys_out,
+                                                      uint32_t* rows_out, uint32_t n, uint32_t shift, uint32_t ntiles,
+                                                      const uint32_t* starts) {
+    grid_dependency_enter();
+    __shared__ uint32_t run[256];      // the tile's next place per digit
+    __shared__ uint32_t wc[8][256];    // this round's rows per warp and digit
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    run[t] = starts[t * ntiles + blockIdx.x];
+    const uint32_t base = blockIdx.x * kSortTile;
+    for (uint32_t r = 0; r < kSortTile / 256u; ++r) {
+        for (uint32_t w = 0; w < 8u; ++w) wc[w][t] = 0u;
+        __syncthreads();
+        const uint32_t row = base + r * 256u + t;
+        const bool act = row < n;
+        const uint64_t key = act ? keys_in[row] : 0ull;
+        const uint32_t d = act ? static_cast<uint32_t>((key >> shift) & 255u) : 256u + lane;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (act && lane == static_cast<uint32_t>(__ffs(peers) - 1)) wc[warp][d] = __popc(peers);
+        __syncthreads();
+        if (act) {
+            uint32_t at = run[d] + rank;
+            for (uint32_t w = 0; w < warp; ++w) at += wc[w][d];
+            keys_out[at] = key;
+            rows_out[at] = rows_in[row];
+        }
+        __syncthreads();
+        uint32_t tot = 0;
+        for (uint32_t w = 0; w < 8u; ++w) tot += wc[w][t];
+        run[t] += tot;
+        __syncthreads();
+    }
+}
+// every column's rows gathered in sorted order: out[p] = in[rows[p]]
+__global__ void k_hsort_gather(const char* in, char* out, uint32_t bytes, const uint32_t* rows, uint32_t n) {
+    grid_dependency_enter();
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const char* s = in + static_cast<size_t>(rows[p]) * bytes;
+        char* o = out + static_cast<size_t>(p) * bytes;
+        if ((bytes & 3u) == 0u) {
+            for (uint32_t b = 0; b < bytes; b += 4) *reinterpret_cast<uint32_t*>(o + b) = *reinterpret_cast<const uint32_t*>(s + b);
+        } else {
+            for (uint32_t b = 0; b < bytes; ++b) o[b] = s[b];
+        }
+    }
+}
+
 // Population columns between the device and page-locked host memory in one
 // launch (the host buffers read or written by the kernel through their
 // mapped device addresses) instead of one copy per column: the set and get
@@ -2111,6 +2208,73 @@ const void* HostAPI::AgentAPI::device_column(const std::string& variable, const 
     *d_n = l->d_count;
     *stream = sim->stream;
     return l->cols[v][l->parity];
+}
+
+void HostAPI::AgentAPI::sort_by(const std::string& variable, const std::type_info& t, uint32_t kind, uint32_t bytes,
+                                bool descending, int begin_bit, int end_bit) {
+    const uint32_t* d_n = nullptr;
+    cudaStream_t st = nullptr;
+    device_column(variable, t, &d_n, &st);  // the checks
+    if (begin_bit < 0 || end_bit > static_cast<int>(8 * bytes) || begin_bit >= end_bit)
+        THROW exception::InvalidArgument(format("HostAgentAPI::sort: bits [%d, %d) are not within the variable's %u bits",
+                                                begin_bit, end_bit, 8 * bytes));
+    detail::AgentList* l = sim->list_of(agent, state);
+    FG_CUDA(cudaStreamSynchronize(st));
+    uint32_t n = 0;
+    FG_CUDA(cudaMemcpy(&n, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (n < 2) return;
+    const uint32_t ntiles = (n + detail::kSortTile - 1) / detail::kSortTile;
+    const uint32_t ncount = 256u * ntiles;
+    const size_t scan_ws = fg_scan_workspace_size(ncount);
+    // scratch: two key and two row buffers, the digit counts and starts, the scan's workspace (256-byte aligned)
+    const size_t kb = sizeof(uint64_t) * n, rb = sizeof(uint32_t) * n, cb = sizeof(uint32_t) * (ncount + 4u);
+    auto align = [](size_t o) { return (o + 255) & ~size_t(255); };
+    size_t at[7];
+    const size_t sizes[7] = {kb, kb, rb, rb, cb, cb, scan_ws};
+    size_t total = 0;
+    for (int r = 0; r < 7; ++r) {
+        at[r] = total;
+        total = align(total + sizes[r]);
+    }
+    char* scratch = nullptr;
+    FG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), total, st));
+    uint64_t* keys[2] = {reinterpret_cast<uint64_t*>(scratch + at[0]), reinterpret_cast<uint64_t*>(scratch + at[1])};
+    uint32_t* rows[2] = {reinterpret_cast<uint32_t*>(scratch + at[2]), reinterpret_cast<uint32_t*>(scratch + at[3])};
+    uint32_t* counts = reinterpret_cast<uint32_t*>(scratch + at[4]);
+    uint32_t* starts = reinterpret_cast<uint32_t*>(scratch + at[5]);
+    void* ws = scratch + at[6];
+    try {
+        FG_CUDA(cudaMemsetAsync(ws, 0, scan_ws, st));
+        const int v = l->var_index(variable);
+        const unsigned int grid = std::min((n + 255u) / 256u, static_cast<unsigned int>(sim->sms) * 8u);
+        const uint32_t bits = static_cast<uint32_t>(end_bit - begin_bit);
+        FG_CUDA(detail::launch_kernel(false, detail::k_hsort_keys, grid, 256, 0, st,
+                              static_cast<const char*>(l->cols[v][l->parity]), kind, bytes, descending ? 1u : 0u,
+                              static_cast<uint32_t>(begin_bit), bits, n, keys[0], rows[0]));
+        int cur = 0;
+        for (uint32_t shift = 0; shift < bits; shift += 8, cur ^= 1) {
+            FG_CUDA(detail::launch_kernel(false, detail::k_hsort_counts, ntiles, 256, 0, st, static_cast<const uint64_t*>(keys[cur]),
+                                  n, shift, ntiles, counts));
+            const int rc = fg_exclusive_scan_u32(counts, starts, ncount, ws, scan_ws, st);
+            if (rc != FG_OK)
+                THROW exception::CUDAError(format("HostAgentAPI::sort: the digit scan failed (%d, %s)", rc,
+                                                  cudaGetErrorString(static_cast<cudaError_t>(fg_last_cuda_error()))));
+            FG_CUDA(detail::launch_kernel(false, detail::k_hsort_scatter, ntiles, 256, 0, st, static_cast<const uint64_t*>(keys[cur]),
+                                  static_cast<const uint32_t*>(rows[cur]), keys[cur ^ 1], rows[cur ^ 1], n, shift, ntiles,
+                                  static_cast<const uint32_t*>(starts)));
+        }
+        // every column in sorted order into the other buffer of the list
+        for (size_t c = 0; c < l->cols.size(); ++c)
+            FG_CUDA(detail::launch_kernel(false, detail::k_hsort_gather, grid, 256, 0, st, static_cast<const char*>(l->cols[c][l->parity]),
+                                  static_cast<char*>(l->cols[c][l->parity ^ 1]), l->agent->variables[c].bytes(),
+                                  static_cast<const uint32_t*>(rows[cur]), n));
+        l->parity ^= 1;
+        FG_CUDA(cudaFreeAsync(scratch, st));
+        FG_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        cudaFreeAsync(scratch, st);
+        throw;
+    }
 }
 
 LogValue HostAPI::AgentAPI::reduce_log(const std::string& variable, const std::type_info& t,

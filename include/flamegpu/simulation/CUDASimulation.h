@@ -216,7 +216,26 @@ class HostAPI {
         OutT transformReduce(const std::string& variable, TransformT transformOperator, ReductionT reductionOperator,
                              OutT init) const;
 
+        /** HostAgentAPI::Order (HostAgentAPI.cuh:131). */
+        enum Order { Asc = 0, Desc = 1 };
+        /** Sorts the population by a scalar variable (HostAgentAPI.cuh:287-290):
+         *  stable, ascending or descending, on bits [beginBit, endBit) of the key. */
+        template <typename VarT>
+        void sort(const std::string& variable, Order order, int beginBit = 0, int endBit = sizeof(VarT) * 8) {
+            static_assert(std::is_arithmetic<VarT>::value && sizeof(VarT) <= 8, "HostAgentAPI::sort takes a scalar type");
+            const uint32_t kind = std::is_floating_point<VarT>::value ? 2u : (std::is_signed<VarT>::value ? 1u : 0u);
+            sort_by(variable, typeid(VarT), kind, sizeof(VarT), order == Desc, beginBit, endBit);
+        }
+        /** By variable1, ties by variable2 (HostAgentAPI.cuh:301-302). */
+        template <typename Var1T, typename Var2T>
+        void sort(const std::string& variable1, Order order1, const std::string& variable2, Order order2) {
+            sort<Var2T>(variable2, order2);
+            sort<Var1T>(variable1, order1);
+        }
+
      private:
+        void sort_by(const std::string& variable, const std::type_info& t, uint32_t kind, uint32_t bytes, bool descending,
+                     int begin_bit, int end_bit);
         LogValue reduce_log(const std::string& variable, const std::type_info& t, LoggingConfig::Reduction r) const;
         // The device column of a scalar variable of type t (the checks of the
         // reductions), the population count on the device, and the stream.
