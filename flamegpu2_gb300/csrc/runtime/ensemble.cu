@@ -159,6 +159,9 @@ std::string batch_unsupported(const ModelData& m) {
         if ((!f->message_input.empty() && array_dims(m.message(f->message_input)->kind)) ||
             (!f->message_output.empty() && array_dims(m.message(f->message_output)->kind)))
             return "array messages";
+        if ((!f->message_input.empty() && m.message(f->message_input)->kind == MessageKind::Bucket) ||
+            (!f->message_output.empty() && m.message(f->message_output)->kind == MessageKind::Bucket))
+            return "bucket messages";
     }
     return "";
 }

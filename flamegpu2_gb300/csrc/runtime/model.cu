@@ -41,7 +41,11 @@ detail::MessageData* ModelDescription::new_message(const std::string& name, deta
     m->name = name;
     m->kind = kind;
     const float zero = 0.0f;
-    if (detail::array_dims(kind)) {
+    if (kind == detail::MessageKind::Bucket) {
+        // the key each message is output with (MessageBucketDevice.cuh:275-290)
+        const int32_t none = 0;
+        m->variables.push_back(detail::make_variable<int32_t>("___KEY", &none, 1));
+    } else if (detail::array_dims(kind)) {
         // the index each message is output to (MessageArray2D.cu:155-158)
         const uint32_t none = 0;
         m->variables.push_back(detail::make_variable<uint32_t>("___INDEX", &none, 1));
@@ -172,6 +176,7 @@ std::type_index message_type_of(detail::MessageKind k) {
         case detail::MessageKind::Array1D: return std::type_index(typeid(MessageArray));
         case detail::MessageKind::Array2D: return std::type_index(typeid(MessageArray2D));
         case detail::MessageKind::Array3D: return std::type_index(typeid(MessageArray3D));
+        case detail::MessageKind::Bucket: return std::type_index(typeid(MessageBucket));
         default: return std::type_index(typeid(MessageBruteForce));
     }
 }

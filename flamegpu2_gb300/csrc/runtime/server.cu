@@ -78,7 +78,10 @@ size_t SimulationServer::estimateBytes(const ModelDescription& model,
         size_t row = 0;
         for (const auto& v : msg->variables) row += (v.bytes() + 3) & ~size_t(3);
         total += max_pop * (2 * row + 32);  // columns, sorted records, build scratch
-        if (detail::array_dims(msg->kind)) {
+        if (msg->kind == detail::MessageKind::Bucket) {
+            total += max_pop * (row + 24) +
+                     (static_cast<size_t>(static_cast<int64_t>(msg->bucket_upper) - msg->bucket_lower) + 2) * 8;
+        } else if (detail::array_dims(msg->kind)) {
             total += static_cast<size_t>(msg->dims[0]) * std::max(1u, msg->dims[1]) * std::max(1u, msg->dims[2]) *
                      (row + 4);  // the array and its claim words
         } else if (msg->kind != detail::MessageKind::BruteForce) {

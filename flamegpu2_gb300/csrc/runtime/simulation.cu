@@ -243,6 +243,29 @@ __global__ void k_hsort_gather(const char* in, char* out, uint32_t bytes, const 
     }
 }
 
+// Bucket message build (MessageBucket.cu:98-137): each message output this
+// step (valid, its key set) gets the sort key key - lower and is counted in
+// its bucket; every other row of the list's capacity gets the key `buckets`
+// (past the last bucket, so it sorts after every message). The stable sort
+// of the rows by key then orders the messages by bucket, in output order.
+__global__ void k_bucket_keys(const int32_t* key_col, const uint32_t* valid, const uint32_t* d_count, uint32_t cap,
+                              int32_t lower, uint32_t buckets, uint64_t* keys, uint32_t* rows, uint32_t* hist) {
+    grid_dependency_enter();
+    const uint32_t n = min(*d_count, cap);
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < cap; r += gridDim.x * blockDim.x) {
+        uint32_t k = buckets;
+        if (r < n && valid[r]) {
+            const int64_t d = static_cast<int64_t>(key_col[r]) - lower;
+            if (d >= 0 && d < static_cast<int64_t>(buckets)) {
+                k = static_cast<uint32_t>(d);
+                atomicAdd(hist + k, 1u);
+            }
+        }
+        keys[r] = k;
+        rows[r] = r;
+    }
+}
+
 // Population columns between the device and page-locked host memory in one
 // launch (the host buffers read or written by the kernel through their
 // mapped device addresses) instead of one copy per column: the set and get
@@ -549,6 +572,21 @@ struct MsgList {
     std::vector<void*> arr_cols;
     uint32_t* arr_claim = nullptr;
     uint32_t* arr_count = nullptr;
+    // bucket messages: keys lower .. lower + buckets - 1; the messages sorted
+    // by bucket (one column per variable), the PBM (buckets + 1 entries), the
+    // bucket counts, and the radix sort's scratch (sized by the capacity)
+    int32_t bk_lower = 0;
+    uint32_t bk_buckets = 0;
+    std::vector<void*> bk_cols;
+    uint32_t* bk_pbm = nullptr;
+    uint32_t* bk_hist = nullptr;
+    uint64_t* bk_keys[2] = {nullptr, nullptr};
+    uint32_t* bk_rows[2] = {nullptr, nullptr};
+    uint32_t* bk_counts = nullptr;
+    uint32_t* bk_starts = nullptr;
+    void* bk_ws = nullptr;
+    size_t bk_ws_bytes = 0;
+    bool bucket() const { return msg->kind == MessageKind::Bucket; }
     bool array() const { return array_dims(msg->kind) != 0; }
     bool spatial() const { return msg->kind == MessageKind::Spatial2D || msg->kind == MessageKind::Spatial3D; }
 };
@@ -744,7 +782,17 @@ struct SimulationImpl {
             ml->d_base = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));
             ml->d_filled = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t)));  // zeroed
             for (const auto& v : m->variables) ml->slot_bytes.push_back(round4(v.bytes()));
-            if (array_dims(m->kind)) {
+            if (m->kind == MessageKind::Bucket) {
+                if (m->bucket_upper == std::numeric_limits<int32_t>::max())
+                    THROW exception::InvalidMessage(format("Bucket message '%s' has no upper bound", m->name.c_str()));
+                const int64_t buckets = static_cast<int64_t>(m->bucket_upper) - m->bucket_lower + 1;
+                if (buckets <= 0 || buckets > (1ll << 30))
+                    THROW exception::InvalidMessage(format("Bucket message '%s' has too many keys", m->name.c_str()));
+                ml->bk_lower = m->bucket_lower;
+                ml->bk_buckets = static_cast<uint32_t>(buckets);
+                ml->bk_pbm = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(buckets) + 2)));
+                ml->bk_hist = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (static_cast<size_t>(buckets) + 2)));
+            } else if (array_dims(m->kind)) {
                 for (int a = 0; a < 3; ++a) ml->arr_dims[a] = a < array_dims(m->kind) ? m->dims[a] : 1u;
                 const uint64_t len = static_cast<uint64_t>(ml->arr_dims[0]) * ml->arr_dims[1] * ml->arr_dims[2];
                 if (len == 0 || len > 0x7FFFFFFFull)
@@ -895,9 +943,28 @@ struct SimulationImpl {
         for (void* p : m.cols) mem.release(p);
         m.cols.clear();
         for (uint32_t b : m.slot_bytes) m.cols.push_back(mem.alloc(static_cast<size_t>(b) * cap));
-        if (m.optional_any || m.array()) {
+        if (m.optional_any || m.array() || m.bucket()) {
             mem.release(m.valid);
             m.valid = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
+        }
+        if (m.bucket()) {
+            for (void* p : m.bk_cols) mem.release(p);
+            m.bk_cols.clear();
+            for (uint32_t b : m.slot_bytes) m.bk_cols.push_back(mem.alloc(static_cast<size_t>(b) * cap));
+            for (int k = 0; k < 2; ++k) {
+                mem.release(m.bk_keys[k]);
+                mem.release(m.bk_rows[k]);
+                m.bk_keys[k] = static_cast<uint64_t*>(mem.alloc(sizeof(uint64_t) * cap));
+                m.bk_rows[k] = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * cap));
+            }
+            const uint32_t ncount = 256u * ((cap + kSortTile - 1) / kSortTile);
+            mem.release(m.bk_counts);
+            mem.release(m.bk_starts);
+            m.bk_counts = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (ncount + 4)));
+            m.bk_starts = static_cast<uint32_t*>(mem.alloc(sizeof(uint32_t) * (ncount + 4)));
+            mem.release(m.bk_ws);
+            m.bk_ws_bytes = fg_scan_workspace_size(std::max(ncount, m.bk_buckets + 1u));
+            m.bk_ws = mem.alloc(m.bk_ws_bytes);
         }
         if (m.spatial()) {
             mem.release(m.records);
@@ -905,7 +972,7 @@ struct SimulationImpl {
             mem.release(m.build_ws);
             m.build_ws_bytes = fg_spatial_build_workspace_size(cap, m.grid.binCount);
             m.build_ws = mem.alloc(m.build_ws_bytes);
-        } else if (m.optional_any) {
+        } else if (m.optional_any && !m.array() && !m.bucket()) {
             for (void* p : m.bf_cols) mem.release(p);
             m.bf_cols.clear();
             for (uint32_t b : m.slot_bytes) m.bf_cols.push_back(mem.alloc(static_cast<size_t>(b) * cap));
@@ -1020,6 +1087,9 @@ struct SimulationImpl {
                         stride = f.in->record_words * 4;
                     } else if (f.in->array()) {
                         p = static_cast<char*>(f.in->arr_cols[v]);
+                        stride = f.in->slot_bytes[v];
+                    } else if (f.in->bucket()) {
+                        p = static_cast<char*>(f.in->bk_cols.empty() ? f.in->cols[v] : f.in->bk_cols[v]);
                         stride = f.in->slot_bytes[v];
                     } else {
                         p = static_cast<char*>(f.in->optional_any ? f.in->bf_cols[v] : f.in->cols[v]);
@@ -1491,6 +1561,51 @@ struct SimulationImpl {
         m.needs_build = false;
     }
 
+    // The buckets of message list m from this step's output: the rows' keys
+    // (k_bucket_keys), a stable radix sort of the rows by key over the list's
+    // capacity (the host sort's kernels), the PBM as the exclusive scan of the
+    // bucket counts, every column gathered in sorted order.
+    void enqueue_bucket_build(MsgList& m) {
+        FG_CUDA(cudaMemsetAsync(m.bk_hist, 0, sizeof(uint32_t) * (static_cast<size_t>(m.bk_buckets) + 2), stream));
+        const uint32_t cap = m.capacity;
+        if (cap == 0) {
+            FG_CUDA(cudaMemsetAsync(m.bk_pbm, 0, sizeof(uint32_t) * (static_cast<size_t>(m.bk_buckets) + 2), stream));
+            m.needs_build = false;
+            return;
+        }
+        int key_var = -1;
+        for (size_t v = 0; v < m.msg->variables.size(); ++v)
+            if (m.msg->variables[v].name == "___KEY") key_var = static_cast<int>(v);
+        const unsigned int grid = std::max(1u, std::min((cap + 255u) / 256u, static_cast<unsigned int>(sms) * 8u));
+        FG_CUDA(launch_kernel(pdl_enabled(), k_bucket_keys, grid, 256, 0, stream, static_cast<const int32_t*>(m.cols[key_var]),
+                              static_cast<const uint32_t*>(m.valid), static_cast<const uint32_t*>(m.d_count), cap, m.bk_lower,
+                              m.bk_buckets, m.bk_keys[0], m.bk_rows[0], m.bk_hist));
+        kernel_counter += 1;
+        uint32_t bits = 1;
+        while (bits < 32 && (1ull << bits) <= m.bk_buckets) ++bits;  // keys 0 .. buckets
+        const uint32_t ntiles = (cap + kSortTile - 1) / kSortTile;
+        int cur = 0;
+        for (uint32_t shift = 0; shift < bits; shift += 8, cur ^= 1) {
+            FG_CUDA(launch_kernel(pdl_enabled(), k_hsort_counts, ntiles, 256, 0, stream,
+                                  static_cast<const uint64_t*>(m.bk_keys[cur]), cap, shift, ntiles, m.bk_counts));
+            FG_CAPI(fg_exclusive_scan_u32(m.bk_counts, m.bk_starts, 256u * ntiles, m.bk_ws, m.bk_ws_bytes, stream));
+            FG_CUDA(launch_kernel(pdl_enabled(), k_hsort_scatter, ntiles, 256, 0, stream,
+                                  static_cast<const uint64_t*>(m.bk_keys[cur]), static_cast<const uint32_t*>(m.bk_rows[cur]),
+                                  m.bk_keys[cur ^ 1], m.bk_rows[cur ^ 1], cap, shift, ntiles,
+                                  static_cast<const uint32_t*>(m.bk_starts)));
+            kernel_counter += 3;
+        }
+        FG_CAPI(fg_exclusive_scan_u32(m.bk_hist, m.bk_pbm, m.bk_buckets + 1u, m.bk_ws, m.bk_ws_bytes, stream));
+        kernel_counter += 1;
+        for (size_t v = 0; v < m.cols.size(); ++v) {
+            FG_CUDA(launch_kernel(pdl_enabled(), k_hsort_gather, grid, 256, 0, stream, static_cast<const char*>(m.cols[v]),
+                                  static_cast<char*>(m.bk_cols[v]), m.slot_bytes[v], static_cast<const uint32_t*>(m.bk_rows[cur]),
+                                  cap));
+            kernel_counter += 1;
+        }
+        m.needs_build = false;
+    }
+
     // Rows an agent-function launch of list l covers with one block per 128
     // rows: the host's bound on its population rounded up to a power of two
     // (at least one wave of 8 blocks per SM), at most its capacity. The
@@ -1551,6 +1666,8 @@ struct SimulationImpl {
         }
         if (f.in && f.in->array() && f.in->needs_build)
             timed("build:" + f.in->msg->name, [&] { enqueue_array_build(*f.in); });
+        if (f.in && f.in->bucket() && f.in->needs_build)
+            timed("build:" + f.in->msg->name, [&] { enqueue_bucket_build(*f.in); });
         const bool append = f.out && f.out->written;
         if (f.out) {
             f.out->written = true;
@@ -1605,9 +1722,13 @@ struct SimulationImpl {
         P.d_first = f.fn->condition ? f.d_first : nullptr;
         if (f.out) {
             // an array message is output where its agent set the index
-            P.msg_out_valid = (f.out->optional_any || f.out->array()) ? f.out->valid : nullptr;
-            P.msg_out_always = (f.fn->message_output_optional || f.out->array()) ? 0 : 1;
+            // an array or bucket message is output where its agent set the index or key
+            const bool placed = f.out->array() || f.out->bucket();
+            P.msg_out_valid = (f.out->optional_any || placed) ? f.out->valid : nullptr;
+            P.msg_out_always = (f.fn->message_output_optional || placed) ? 0 : 1;
             for (int a = 0; a < 3; ++a) P.out_dims[a] = f.out->arr_dims[a];
+            P.out_key_lo = f.out->bk_lower;
+            P.out_key_hi = static_cast<int32_t>(static_cast<int64_t>(f.out->bk_lower) + f.out->bk_buckets);
             P.msg_out_count = f.out->d_count;
             P.msg_out_base = append ? f.out->d_base : nullptr;
             P.msg_out_filled = f.out->d_filled;
@@ -1630,6 +1751,11 @@ struct SimulationImpl {
             } else if (f.in->array()) {
                 P.in_count = f.in->arr_count;
                 for (int a = 0; a < 3; ++a) P.in_dims[a] = f.in->arr_dims[a];
+            } else if (f.in->bucket()) {
+                P.in_pbm = f.in->bk_pbm;
+                P.in_count = f.in->bk_pbm + f.in->bk_buckets;
+                P.in_key_lo = f.in->bk_lower;
+                P.in_key_hi = static_cast<int32_t>(static_cast<int64_t>(f.in->bk_lower) + f.in->bk_buckets);
             } else {
                 P.in_count = f.in->optional_any ? f.in->bf_count : f.in->d_count;
             }
@@ -1664,7 +1790,7 @@ struct SimulationImpl {
         kernel_counter += 1;
         if (f.out) {
             f.out->needs_build = true;
-            if (!f.out->spatial() && !f.out->array() && f.out->optional_any) {
+            if (!f.out->spatial() && !f.out->array() && !f.out->bucket() && f.out->optional_any) {
                 // brute-force optional output: stable compaction of the message rows
                 std::vector<fg_column> cols(f.out->cols.size());
                 for (size_t v = 0; v < cols.size(); ++v) cols[v] = fg_column{f.out->cols[v], f.out->bf_cols[v], f.out->slot_bytes[v]};
@@ -2082,7 +2208,8 @@ struct SimulationImpl {
                                           "unsupported device call", "message output is not enabled for this function",
                                           "a neighbourhood staging wait gave up (bounded wait)",
                                           "AgentRandom::uniform() with min > max",
-                                          "array message index or search radius out of range, or two messages output to one index"};
+                                          "array message index or search radius out of range, or two messages output to one index",
+                                          "bucket message key outside the bounds"};
             if (err[0] == kDevArrayMessage && err[1] == kArrayWriteConflict)
                 THROW exception::ArrayMessageWriteConflict(format(
                     "Two array messages were output to one index, or one outside the array (message row %u, %u occurrences)",

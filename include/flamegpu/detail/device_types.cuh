@@ -130,6 +130,7 @@ enum DeviceErrorCode : uint32_t {
     kDevStageTimeout = 11,
     kDevRandomRange = 12,
     kDevArrayMessage = 13,
+    kDevBucketMessage = 14,
 };
 
 /** Kernel parameters of one agent function launch (passed __grid_constant__).
@@ -164,6 +165,8 @@ struct LaunchParams {
     uint32_t in_pbm_alloc;       // PBM entries readable (multiple of 4, >= binCount + 1)
     uint32_t in_dims[3];         // array message input: dimensions (1 past the last used)
     uint32_t out_dims[3];        // array message output: dimensions
+    int32_t in_key_lo, in_key_hi;    // bucket message input: keys [lo, hi) (PBM in in_pbm)
+    int32_t out_key_lo, out_key_hi;  // bucket message output: keys [lo, hi)
     uint32_t stage_bytes;        // shared memory for staging neighbour records (0 = off)
     // birth / death
     uint32_t* birth_flags;       // 1 where agent_out was used, 2 if its id was also claimed (null if disabled)

@@ -37,7 +37,7 @@ typedef void (*FLAMEGPU_HOST_FUNCTION_POINTER)(HostAPI* api);
 
 namespace detail {
 
-enum class MessageKind { BruteForce = 1, Spatial2D = 2, Spatial3D = 3, Array1D = 4, Array2D = 5, Array3D = 6 };
+enum class MessageKind { BruteForce = 1, Spatial2D = 2, Spatial3D = 3, Array1D = 4, Array2D = 5, Array3D = 6, Bucket = 7 };
 // the array message kinds' dimension count (0: not an array)
 inline int array_dims(MessageKind k) {
     return k == MessageKind::Array1D ? 1 : k == MessageKind::Array2D ? 2 : k == MessageKind::Array3D ? 3 : 0;
@@ -97,6 +97,9 @@ struct MessageData {
                     std::numeric_limits<float>::quiet_NaN()};
     bool persistent = false;
     uint32_t dims[3] = {0, 0, 0};  // array messages: length along each dimension (0: unset)
+    // bucket messages: keys lower .. upper, both inclusive (upper unset: INT32_MAX)
+    int32_t bucket_lower = 0;
+    int32_t bucket_upper = std::numeric_limits<int32_t>::max();
     const Variable* find(const std::string& n) const {
         for (const auto& v : variables)
             if (v.name == n) return &v;
@@ -308,6 +311,33 @@ class MessageArray3D::Description : public MessageBruteForce::Description {
     flamegpu::size_type getDimZ() const { return data->dims[2]; }
 };
 
+/** MessageBucket::Description (MessageBucketHost.h:180-245, MessageBucket.cu:190-215):
+ *  integer keys lowerBound .. upperBound, both inclusive. */
+class MessageBucket::Description : public MessageBruteForce::Description {
+ public:
+    using MessageBruteForce::Description::Description;
+    void setLowerBound(int32_t min) {
+        if (data->bucket_upper != std::numeric_limits<int32_t>::max() && min >= data->bucket_upper)
+            THROW exception::InvalidArgument(exception::format("Bucket lower bound %d must be below the upper bound %d", min,
+                                                               data->bucket_upper));
+        data->bucket_lower = min;
+    }
+    void setUpperBound(int32_t max) {
+        if (max <= data->bucket_lower)
+            THROW exception::InvalidArgument(exception::format("Bucket upper bound %d must be above the lower bound %d", max,
+                                                               data->bucket_lower));
+        data->bucket_upper = max;
+    }
+    void setBounds(int32_t min, int32_t max) {
+        if (max <= min)
+            THROW exception::InvalidArgument(exception::format("Bucket upper bound %d must be above the lower bound %d", max, min));
+        data->bucket_lower = min;
+        data->bucket_upper = max;
+    }
+    int32_t getLowerBound() const { return data->bucket_lower; }
+    int32_t getUpperBound() const { return data->bucket_upper; }
+};
+
 // --------------------------------------------------------- agent functions
 
 class AgentFunctionDescription {
@@ -510,6 +540,7 @@ class ModelDescription {
         else if constexpr (std::is_same_v<MsgType, MessageArray>) return detail::MessageKind::Array1D;
         else if constexpr (std::is_same_v<MsgType, MessageArray2D>) return detail::MessageKind::Array2D;
         else if constexpr (std::is_same_v<MsgType, MessageArray3D>) return detail::MessageKind::Array3D;
+        else if constexpr (std::is_same_v<MsgType, MessageBucket>) return detail::MessageKind::Bucket;
         else return detail::MessageKind::BruteForce;
     }
     detail::MessageData* new_message(const std::string& name, detail::MessageKind kind);

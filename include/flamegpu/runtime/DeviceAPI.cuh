@@ -27,6 +27,7 @@ class MessageSpatial3D;
 class MessageArray;
 class MessageArray2D;
 class MessageArray3D;
+class MessageBucket;
 
 namespace detail {
 
@@ -725,6 +726,88 @@ class MessageArray3D {
      public:
         __device__ Out(const detail::LaunchParams& p, uint32_t idx) : ArrayOut<3>(p, idx) {}
         __device__ void setIndex(uint32_t x, uint32_t y, uint32_t z) const { set_index({x, y, z}); }
+    };
+};
+
+/**
+ * Bucket messages (MessageBucketDevice.cuh): each message carries an integer
+ * key in [lowerBound, upperBound]; the input iterates the messages of one key,
+ * or of the keys [begin, end), in the order they were output.
+ */
+class MessageBucket {
+ public:
+    class Description;
+    class In {
+     public:
+        class Message : public MessageView {
+         public:
+            __device__ Message(const detail::LaunchParams& p, uint32_t i) : MessageView(p, i) {}
+        };
+        class Filter {
+         public:
+            class iterator {
+             public:
+                __device__ iterator(const detail::LaunchParams& p, uint32_t i) : m(p, i) {}
+                __device__ iterator& operator++() {
+                    ++m.index;
+                    return *this;
+                }
+                __device__ bool operator!=(const iterator& o) const { return m.index != o.m.index; }
+                __device__ bool operator==(const iterator& o) const { return m.index == o.m.index; }
+                __device__ const Message& operator*() const { return m; }
+                __device__ const Message* operator->() const { return &m; }
+
+             private:
+                Message m;
+            };
+            __device__ Filter(const detail::LaunchParams& p, uint32_t b, uint32_t e) : P(p), first(b), last(e) {}
+            __device__ iterator begin() const { return iterator(P, first); }
+            __device__ iterator end() const { return iterator(P, last); }
+            __device__ uint32_t size() const { return last - first; }
+
+         private:
+            const detail::LaunchParams& P;
+            uint32_t first, last;
+        };
+        __device__ explicit In(const detail::LaunchParams& p) : P(p) {}
+        /** The messages of one key (MessageBucketDevice.cuh:207-221). */
+        __device__ Filter operator()(int32_t key) const {
+            if (key < P.in_key_lo || key >= P.in_key_hi) {
+                detail::device_error(P, detail::kDevBucketMessage, 0, static_cast<uint32_t>(key));
+                return Filter(P, 0, 0);
+            }
+            const uint32_t k = static_cast<uint32_t>(key - P.in_key_lo);
+            return Filter(P, __ldg(P.in_pbm + k), __ldg(P.in_pbm + k + 1));
+        }
+        /** The messages of the keys [beginKey, endKey) (:228-245). */
+        __device__ Filter operator()(int32_t beginKey, int32_t endKey) const {
+            if (beginKey < P.in_key_lo || endKey > P.in_key_hi || endKey <= beginKey) {
+                detail::device_error(P, detail::kDevBucketMessage, 0, static_cast<uint32_t>(beginKey));
+                return Filter(P, 0, 0);
+            }
+            return Filter(P, __ldg(P.in_pbm + (beginKey - P.in_key_lo)), __ldg(P.in_pbm + (endKey - P.in_key_lo)));
+        }
+
+     private:
+        const detail::LaunchParams& P;
+    };
+    class Out : public MessageOutBase {
+     public:
+        __device__ Out(const detail::LaunchParams& p, uint32_t idx) : MessageOutBase(p, idx) {}
+        /** The message's key (MessageBucketDevice.cuh:275-290); a key outside the bounds is a device error. */
+        __device__ void setKey(int32_t key) const {
+            if (key < P.out_key_lo || key >= P.out_key_hi) {
+                detail::device_error(P, detail::kDevBucketMessage, 0, index);
+                return;
+            }
+            detail::write_var<int32_t>(P, &P.T.msg_out, detail::VarName("___KEY").hash, index, key);
+            key_set = 1;
+        }
+        /** Whether setKey was called: the message is output. */
+        __device__ uint32_t written() const { return key_set; }
+
+     private:
+        mutable uint32_t key_set = 0;
     };
 };
 
