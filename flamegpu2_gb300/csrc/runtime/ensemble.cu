@@ -145,6 +145,7 @@ std::string batch_unsupported(const ModelData& m) {
         return "the model has host functions";
     for (const auto& l : m.layers)
         if (!l->host_functions.empty()) return "the model has host layer functions";
+    if (!m.macro_environment.empty()) return "the model has environment macro properties";
     for (const auto& f : a.functions)
         for (const auto& g : a.functions)
             if (f != g && !f->message_output.empty() && f->message_output == g->message_output)

@@ -263,7 +263,7 @@ void LayerDescription::addAgentFunction(const std::string& agent_name, const std
 void EnvironmentDescription::add(const std::string& name, std::type_index t, uint32_t size, uint32_t n, const void* v,
                                  bool c) {
     detail::check_name(name, "Environment property");
-    if (model->property(name))
+    if (model->property(name) || model->macro_property(name))
         THROW exception::InvalidEnvProperty(format("Environment already has property '%s'", name.c_str()));
     detail::EnvProperty p;
     p.name = name;
@@ -274,6 +274,22 @@ void EnvironmentDescription::add(const std::string& name, std::type_index t, uin
     std::memcpy(p.value.data(), v, p.value.size());
     p.is_const = c;
     model->environment.push_back(std::move(p));
+}
+
+void EnvironmentDescription::add_macro(const std::string& name, std::type_index t, uint32_t size, const uint32_t (&dims)[4]) {
+    detail::check_name(name, "Environment macro property");
+    if (model->property(name) || model->macro_property(name))
+        THROW exception::InvalidEnvProperty(format("Environment already has property '%s'", name.c_str()));
+    uint64_t n = 1;
+    for (uint32_t d : dims) n *= d;
+    if (n * size > (1ull << 34))
+        THROW exception::InvalidEnvProperty(format("Environment macro property '%s' is too large", name.c_str()));
+    detail::MacroProperty p;
+    p.name = name;
+    p.type = t;
+    p.type_size = size;
+    for (int a = 0; a < 4; ++a) p.dims[a] = dims[a];
+    model->macro_environment.push_back(std::move(p));
 }
 
 const detail::EnvProperty* EnvironmentDescription::find(const std::string& name, const std::type_info& t,

@@ -29,6 +29,7 @@
 #include <set>
 #include <string>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "flamegpu/detail/launch.cuh"
@@ -640,6 +641,11 @@ struct SimulationImpl {
     std::vector<size_t> env_offset;
     char* d_env = nullptr;
     bool env_dirty = true;
+    // macro properties: after the plain properties in the environment buffer
+    // (offsets from its start, 8-byte aligned), never uploaded from env_host;
+    // the host views that are alive, by name
+    std::vector<size_t> macro_offset;
+    std::unordered_map<std::string, std::weak_ptr<HostMacroData>> macro_views;
     // misc device state
     uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record, [8..] next ids per agent
     unsigned long long* d_agent_steps = nullptr;  // [0] agents summed over the steps run, [1] agents now
@@ -762,7 +768,12 @@ struct SimulationImpl {
         env_host.assign(std::max<size_t>(off, 8), 0);
         for (size_t i = 0; i < model->environment.size(); ++i)
             std::memcpy(env_host.data() + env_offset[i], model->environment[i].value.data(), model->environment[i].value.size());
-        d_env = static_cast<char*>(mem.alloc(env_host.size()));
+        size_t macro_end = env_host.size();
+        for (const auto& p : model->macro_environment) {
+            macro_offset.push_back(macro_end);
+            macro_end += (static_cast<size_t>(p.type_size) * p.elements() + 7) & ~size_t(7);
+        }
+        d_env = static_cast<char*>(mem.alloc(macro_end));  // zeroed: macro properties start at 0
         FG_CUDA(cudaMemcpy(d_env, env_host.data(), env_host.size(), cudaMemcpyHostToDevice));
         env_dirty = false;
         // agent lists (one per state)
@@ -1125,6 +1136,11 @@ struct SimulationImpl {
                 const EnvProperty& p = model->environment[i];
                 // offsets into the environment buffer (LaunchParams::env)
                 e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(env_offset[i]), 0, p.type_size, p.elements});
+            }
+            // macro properties: stride 1 marks them (the device API checks it)
+            for (size_t i = 0; i < model->macro_environment.size(); ++i) {
+                const MacroProperty& p = model->macro_environment[i];
+                e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(macro_offset[i]), 1, p.type_size, p.elements()});
             }
             T->env = make_table(e, "environment");
             f.tables[par].reset(T);
@@ -2283,6 +2299,39 @@ size_t HostAPI::Environment::elements(const std::string& name) const {
     for (const auto& p : sim->model->environment)
         if (p.name == name) return p.elements;
     THROW exception::InvalidEnvProperty(format("Environment has no property '%s'", name.c_str()));
+}
+
+detail::HostMacroData::~HostMacroData() {
+    if (!dirty || !device) return;
+    // a destructor does not throw: a failed copy is left to the next checked call
+    if (cudaStreamSynchronize(stream) == cudaSuccess)
+        cudaMemcpy(device, host.data(), host.size(), cudaMemcpyHostToDevice);
+}
+
+std::shared_ptr<detail::HostMacroData> HostAPI::Environment::macro(const std::string& name, const std::type_info& t, size_t size,
+                                                           const uint32_t (&dims)[4]) const {
+    const auto& props = sim->model->macro_environment;
+    for (size_t i = 0; i < props.size(); ++i) {
+        const detail::MacroProperty& p = props[i];
+        if (p.name != name) continue;
+        if (p.type != std::type_index(t) || p.type_size != size)
+            THROW exception::InvalidEnvPropertyType(format("Environment macro property '%s' has another type", name.c_str()));
+        for (int a = 0; a < 4; ++a)
+            if (p.dims[a] != dims[a])
+                THROW exception::InvalidEnvPropertyType(format(
+                    "Environment macro property '%s' has dimensions %u x %u x %u x %u, not %u x %u x %u x %u", name.c_str(),
+                    p.dims[0], p.dims[1], p.dims[2], p.dims[3], dims[0], dims[1], dims[2], dims[3]));
+        if (auto live = sim->macro_views[name].lock()) return live;
+        auto d = std::make_shared<detail::HostMacroData>();
+        d->device = sim->d_env + sim->macro_offset[i];
+        d->stream = sim->stream;
+        d->host.resize(static_cast<size_t>(p.type_size) * p.elements());
+        FG_CUDA(cudaStreamSynchronize(sim->stream));
+        FG_CUDA(cudaMemcpy(d->host.data(), d->device, d->host.size(), cudaMemcpyDeviceToHost));
+        sim->macro_views[name] = d;
+        return d;
+    }
+    THROW exception::InvalidEnvProperty(format("Environment has no macro property '%s'", name.c_str()));
 }
 
 std::mt19937_64& HostAPI::Random::engine() const { return sim->host_rng; }

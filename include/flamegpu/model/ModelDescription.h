@@ -122,8 +122,20 @@ struct EnvProperty {
     bool is_const = false;
 };
 
+/** An environment macro property: a zero-initialised array of up to four
+ *  dimensions that agent functions update atomically
+ *  (include/flamegpu/model/EnvironmentDescription.h newMacroProperty). */
+struct MacroProperty {
+    std::string name;
+    std::type_index type = std::type_index(typeid(void));
+    uint32_t type_size = 0;
+    uint32_t dims[4] = {1, 1, 1, 1};
+    uint32_t elements() const { return dims[0] * dims[1] * dims[2] * dims[3]; }
+};
+
 struct ModelData {
     std::string name;
+    std::vector<MacroProperty> macro_environment;
     std::vector<std::shared_ptr<AgentData>> agents;
     std::vector<std::shared_ptr<MessageData>> messages;
     std::vector<std::shared_ptr<LayerData>> layers;
@@ -143,6 +155,11 @@ struct ModelData {
     }
     EnvProperty* property(const std::string& n) {
         for (auto& p : environment)
+            if (p.name == n) return &p;
+        return nullptr;
+    }
+    MacroProperty* macro_property(const std::string& n) {
+        for (auto& p : macro_environment)
             if (p.name == n) return &p;
         return nullptr;
     }
@@ -490,8 +507,22 @@ class EnvironmentDescription {
         return old;
     }
     bool hasProperty(const std::string& name) const { return model->property(name) != nullptr; }
+    /** EnvironmentDescription::newMacroProperty<T, I, J, K, W>
+     *  (include/flamegpu/model/EnvironmentDescription.h:271-285): a property of
+     *  I x J x K x W elements, zero at the start of a simulation, written by
+     *  agent functions with atomic operations and by host functions. Its name
+     *  is not also a plain property's (the two share one device table). */
+    template <typename T, flamegpu::size_type I = 1, flamegpu::size_type J = 1, flamegpu::size_type K = 1,
+              flamegpu::size_type W = 1>
+    void newMacroProperty(const std::string& name) {
+        static_assert(I > 0 && J > 0 && K > 0 && W > 0, "macro property dimensions must be positive");
+        const uint32_t dims[4] = {I, J, K, W};
+        add_macro(name, std::type_index(typeid(T)), sizeof(T), dims);
+    }
+    bool hasMacroProperty(const std::string& name) const { return model->macro_property(name) != nullptr; }
 
  private:
+    void add_macro(const std::string& name, std::type_index t, uint32_t size, const uint32_t (&dims)[4]);
     void add(const std::string& name, std::type_index t, uint32_t size, uint32_t n, const void* v, bool c);
     const detail::EnvProperty* find(const std::string& name, const std::type_info& t, size_t size) const;
     std::shared_ptr<detail::ModelData> model;

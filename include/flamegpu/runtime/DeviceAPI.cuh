@@ -1197,6 +1197,158 @@ class MessageSpatial3D {
 
 // ------------------------------------------------------- environment, random
 
+namespace detail {
+// Atomic operations on a 4- or 8-byte macro property element, through the
+// native atomics where the type has them and a compare-and-swap loop on the
+// element's bits otherwise.
+template <typename T>
+__device__ __forceinline__ auto as_word(T v) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "macro property atomics need 4- or 8-byte types");
+    if constexpr (sizeof(T) == 4) {
+        unsigned int u;
+        memcpy(&u, &v, 4);
+        return u;
+    } else {
+        unsigned long long u;
+        memcpy(&u, &v, 8);
+        return u;
+    }
+}
+template <typename T, typename U>
+__device__ __forceinline__ T from_word(U u) {
+    T v;
+    memcpy(&v, &u, sizeof(T));
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ auto word_ptr(T* p) {
+    if constexpr (sizeof(T) == 4) return reinterpret_cast<unsigned int*>(p);
+    else return reinterpret_cast<unsigned long long*>(p);
+}
+// old value of *p, *p replaced by f(old)
+template <typename T, typename F>
+__device__ __forceinline__ T atomic_update(T* p, F f) {
+    auto* w = word_ptr(p);
+    auto old = *reinterpret_cast<volatile decltype(as_word(T{}))*>(w);
+    while (true) {
+        const auto seen = atomicCAS(w, old, as_word<T>(f(from_word<T>(old))));
+        if (seen == old) return from_word<T>(old);
+        old = seen;
+    }
+}
+template <typename T>
+__device__ __forceinline__ T atomic_add(T* p, T v) {
+    if constexpr (std::is_same<T, float>::value || std::is_same<T, double>::value || std::is_same<T, int>::value ||
+                  std::is_same<T, unsigned int>::value || std::is_same<T, unsigned long long>::value) {
+        return atomicAdd(p, v);
+    } else if constexpr (std::is_integral<T>::value && sizeof(T) == 8) {
+        // two's complement: the unsigned sum has the same bits
+        return static_cast<T>(atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v)));
+    } else if constexpr (std::is_integral<T>::value && sizeof(T) == 4) {
+        return static_cast<T>(atomicAdd(reinterpret_cast<unsigned int*>(p), static_cast<unsigned int>(v)));
+    } else {
+        return atomic_update(p, [v](T o) { return o + v; });
+    }
+}
+template <typename T>
+__device__ __forceinline__ T atomic_sub(T* p, T v) {
+    if constexpr (std::is_integral<T>::value) {
+        using U = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned int>::type;
+        return static_cast<T>(atomicAdd(reinterpret_cast<U*>(p), static_cast<U>(0) - static_cast<U>(v)));
+    } else {
+        return atomic_add(p, static_cast<T>(-v));
+    }
+}
+template <typename T>
+__device__ __forceinline__ T atomic_min(T* p, T v) {
+    if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned int>::value ||
+                  std::is_same<T, long long>::value || std::is_same<T, unsigned long long>::value) {
+        return atomicMin(p, v);
+    } else if constexpr (std::is_same<T, long>::value || std::is_same<T, unsigned long>::value) {
+        using U = typename std::conditional<std::is_signed<T>::value, long long, unsigned long long>::type;
+        return static_cast<T>(atomicMin(reinterpret_cast<U*>(p), static_cast<U>(v)));
+    } else {
+        return atomic_update(p, [v](T o) { return v < o ? v : o; });
+    }
+}
+template <typename T>
+__device__ __forceinline__ T atomic_max(T* p, T v) {
+    if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned int>::value ||
+                  std::is_same<T, long long>::value || std::is_same<T, unsigned long long>::value) {
+        return atomicMax(p, v);
+    } else if constexpr (std::is_same<T, long>::value || std::is_same<T, unsigned long>::value) {
+        using U = typename std::conditional<std::is_signed<T>::value, long long, unsigned long long>::type;
+        return static_cast<T>(atomicMax(reinterpret_cast<U*>(p), static_cast<U>(v)));
+    } else {
+        return atomic_update(p, [v](T o) { return v > o ? v : o; });
+    }
+}
+}  // namespace detail
+
+/**
+ * DeviceMacroProperty<T, I, J, K, W> (include/flamegpu/runtime/environment/
+ * DeviceMacroProperty.cuh:88-205): an agent function's view of an
+ * environment macro property. operator[] selects along the first dimension
+ * (an index past it is a device error, and the view stays at element 0); a
+ * view of one element reads as T and updates atomically: +=, -=, addAtomic /
+ * subAtomic (the new value), + and - (plain reads), ++ and -- (pre: the new
+ * value, post: the old), min / max (the value left), CAS (the old value),
+ * exchange (the old value). Within one agent function a property is either
+ * read or updated (the reference's rule; not checked here).
+ */
+template <typename T, flamegpu::size_type I = 1, flamegpu::size_type J = 1, flamegpu::size_type K = 1,
+          flamegpu::size_type W = 1>
+class DeviceMacroProperty {
+ public:
+    __device__ DeviceMacroProperty(const detail::LaunchParams& p, T* at) : P(p), ptr(at) {}
+    __device__ DeviceMacroProperty<T, J, K, W, 1> operator[](unsigned int i) const {
+        if (i >= I) {
+            detail::device_error(P, detail::kDevArrayIndex, 0, i);
+            return DeviceMacroProperty<T, J, K, W, 1>(P, nullptr);
+        }
+        return DeviceMacroProperty<T, J, K, W, 1>(P, ptr ? ptr + static_cast<size_t>(i) * J * K * W : nullptr);
+    }
+    __device__ operator T() const { return ptr ? *reinterpret_cast<const volatile T*>(ptr) : T{}; }
+    __device__ DeviceMacroProperty& operator+=(T v) {
+        if (ptr) detail::atomic_add(ptr, v);
+        return *this;
+    }
+    __device__ DeviceMacroProperty& operator-=(T v) {
+        if (ptr) detail::atomic_sub(ptr, v);
+        return *this;
+    }
+    __device__ T addAtomic(T v) { return ptr ? detail::atomic_add(ptr, v) + v : T{}; }
+    __device__ T subAtomic(T v) { return ptr ? detail::atomic_sub(ptr, v) - v : T{}; }
+    __device__ T operator+(T v) const { return static_cast<T>(*this) + v; }
+    __device__ T operator-(T v) const { return static_cast<T>(*this) - v; }
+    __device__ T operator++() { return ptr ? detail::atomic_add(ptr, static_cast<T>(1)) + static_cast<T>(1) : T{}; }
+    __device__ T operator--() { return ptr ? detail::atomic_sub(ptr, static_cast<T>(1)) - static_cast<T>(1) : T{}; }
+    __device__ T operator++(int) { return ptr ? detail::atomic_add(ptr, static_cast<T>(1)) : T{}; }
+    __device__ T operator--(int) { return ptr ? detail::atomic_sub(ptr, static_cast<T>(1)) : T{}; }
+    __device__ T min(T v) {
+        if (!ptr) return T{};
+        const T old = detail::atomic_min(ptr, v);
+        return v < old ? v : old;
+    }
+    __device__ T max(T v) {
+        if (!ptr) return T{};
+        const T old = detail::atomic_max(ptr, v);
+        return v > old ? v : old;
+    }
+    __device__ T CAS(T compare, T v) {
+        if (!ptr) return T{};
+        return detail::from_word<T>(atomicCAS(detail::word_ptr(ptr), detail::as_word(compare), detail::as_word(v)));
+    }
+    __device__ T exchange(T v) {
+        if (!ptr) return T{};
+        return detail::from_word<T>(atomicExch(detail::word_ptr(ptr), detail::as_word(v)));
+    }
+
+ private:
+    const detail::LaunchParams& P;
+    T* ptr;  // null after a device error: reads give 0, updates do nothing
+};
+
 /** Read-only environment properties (include/flamegpu/runtime/environment/DeviceEnvironment.cuh). */
 class DeviceEnvironment {
  public:
@@ -1211,6 +1363,22 @@ class DeviceEnvironment {
     __device__ T getProperty(detail::VarName name, unsigned int i) const {
         const T* off = detail::var_addr<T>(P, &P.T.env, name.hash, 0, i);
         return detail::ldg_any(reinterpret_cast<const T*>(detail::ctx().env + reinterpret_cast<size_t>(off)));
+    }
+    /** DeviceEnvironment::getMacroProperty (DeviceEnvironment.cuh:95-112). A
+     *  name that is not a macro property of this type and these dimensions is
+     *  a device error, and the view then reads 0 and ignores updates. */
+    template <typename T, flamegpu::size_type I = 1, flamegpu::size_type J = 1, flamegpu::size_type K = 1,
+              flamegpu::size_type W = 1>
+    __device__ DeviceMacroProperty<T, I, J, K, W> getMacroProperty(detail::VarName name) const {
+        const detail::VarTable* t = &P.T.env;
+        const detail::VarSlot* vs = &t->slot[detail::table_slot(t->mult, t->shift, name.hash)];
+        if (vs->hash != name.hash || vs->stride != 1 || vs->elem_bytes != sizeof(T) || vs->elements != I * J * K * W) {
+            detail::device_error(P, vs->hash != name.hash ? detail::kDevUnknownVariable : detail::kDevTypeMismatch,
+                                 name.hash, 0);
+            return DeviceMacroProperty<T, I, J, K, W>(P, nullptr);
+        }
+        char* base = const_cast<char*>(detail::ctx().env) + reinterpret_cast<size_t>(vs->ptr);
+        return DeviceMacroProperty<T, I, J, K, W>(P, reinterpret_cast<T*>(base));
     }
 
  private:

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <memory>
 #include <random>
 #include <string>
@@ -55,6 +56,78 @@ class HostNewAgentAPI {
 /** Host-side API of init/step/exit/host-layer functions: environment
  * properties, agent counts, reductions of agent variables (computed on the
  * device) and agent creation. */
+namespace detail {
+/** The host copy of one macro property while host functions hold it: read
+ *  from the device when the first handle is made, written back when the last
+ *  one goes (if a handle wrote to it). */
+struct HostMacroData {
+    std::vector<char> host;
+    void* device = nullptr;
+    cudaStream_t stream = nullptr;
+    bool dirty = false;
+    ~HostMacroData();
+};
+}  // namespace detail
+
+/**
+ * HostMacroProperty<T, I, J, K, W> (include/flamegpu/runtime/environment/
+ * HostMacroProperty.cuh:96-260): a host function's view of an environment
+ * macro property. operator[] selects along the first dimension; a view of one
+ * element converts to T and supports assignment, +=, -=, *=, /= and the
+ * increment and decrement operators; zero() clears the whole property.
+ */
+template <typename T, flamegpu::size_type I = 1, flamegpu::size_type J = 1, flamegpu::size_type K = 1,
+          flamegpu::size_type W = 1>
+class HostMacroProperty {
+ public:
+    HostMacroProperty(std::shared_ptr<detail::HostMacroData> d, size_t first) : data(std::move(d)), at(first) {}
+    HostMacroProperty<T, J, K, W, 1> operator[](flamegpu::size_type i) const {
+        if (I == 1 && J == 1 && K == 1 && W == 1)
+            THROW exception::OutOfBoundsException("Indexing a macro property element that has no further dimension");
+        if (i >= I)
+            THROW exception::OutOfBoundsException(exception::format("Macro property index %u is past its dimension of %u",
+                                                                    static_cast<unsigned>(i), static_cast<unsigned>(I)));
+        return HostMacroProperty<T, J, K, W, 1>(data, at + static_cast<size_t>(i) * J * K * W);
+    }
+    operator T() const { return value(); }
+    HostMacroProperty& operator=(T v) {
+        ref() = v;
+        return *this;
+    }
+    HostMacroProperty& operator+=(T v) { ref() += v; return *this; }
+    HostMacroProperty& operator-=(T v) { ref() -= v; return *this; }
+    HostMacroProperty& operator*=(T v) { ref() *= v; return *this; }
+    HostMacroProperty& operator/=(T v) { ref() /= v; return *this; }
+    T operator++() { return ++ref(); }
+    T operator--() { return --ref(); }
+    T operator++(int) { return ref()++; }
+    T operator--(int) { return ref()--; }
+    /** Every element of this view set to 0. */
+    void zero() {
+        std::memset(data->host.data() + at * sizeof(T), 0, sizeof(T) * I * J * K * W);
+        data->dirty = true;
+    }
+
+ private:
+    T value() const {
+        scalar_only();
+        T v;
+        std::memcpy(&v, data->host.data() + at * sizeof(T), sizeof(T));
+        return v;
+    }
+    T& ref() {
+        scalar_only();
+        data->dirty = true;
+        return *reinterpret_cast<T*>(data->host.data() + at * sizeof(T));
+    }
+    static void scalar_only() {
+        if (I != 1 || J != 1 || K != 1 || W != 1)
+            THROW exception::InvalidOperation("A macro property with dimensions is used as one value; index it first");
+    }
+    std::shared_ptr<detail::HostMacroData> data;
+    size_t at;
+};
+
 class HostAPI {
  public:
     class Environment {
@@ -118,7 +191,20 @@ class HostAPI {
         /** Set a property from raw bytes (size checked). */
         void setRaw(const std::string& name, const void* value, size_t size);
 
+        /** HostEnvironment::getMacroProperty (HostEnvironment.cuh:148-160): the
+         *  macro property's values, read back from the device; what the
+         *  returned view writes reaches the device when the last view of the
+         *  property is gone. */
+        template <typename T, flamegpu::size_type I = 1, flamegpu::size_type J = 1, flamegpu::size_type K = 1,
+                  flamegpu::size_type W = 1>
+        HostMacroProperty<T, I, J, K, W> getMacroProperty(const std::string& name) const {
+            const uint32_t dims[4] = {I, J, K, W};
+            return HostMacroProperty<T, I, J, K, W>(macro(name, typeid(T), sizeof(T), dims), 0);
+        }
+
      private:
+        std::shared_ptr<detail::HostMacroData> macro(const std::string& name, const std::type_info& t, size_t size,
+                                                     const uint32_t (&dims)[4]) const;
         void get(const std::string& name, const std::type_info& t, size_t size, void* out) const;
         void set(const std::string& name, const std::type_info& t, size_t size, const void* in);
         // element index of an array property (length n, 0: any): read into out, then written from in if given
