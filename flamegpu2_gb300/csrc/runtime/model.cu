@@ -330,6 +330,20 @@ void AgentVector::resize(flamegpu::size_type n) {
 
 void AgentVector::push_back() { resize(count + 1); }
 
+void AgentVector::erase(flamegpu::size_type first, flamegpu::size_type last) {
+    if (first > last || last > count)
+        THROW exception::OutOfBoundsException(
+            format("AgentVector::erase: [%u, %u) is not within the %u agents", first, last, count));
+    if (first == last) return;
+    for (size_t v = 0; v < cols.size(); ++v) {
+        const size_t b = agent->variables[v].bytes();
+        char* d = cols[v].data();
+        std::memmove(d + first * b, d + last * b, (count - last) * b);
+        cols[v].resize(static_cast<size_t>(count - (last - first)) * b);
+    }
+    count -= last - first;
+}
+
 void AgentVector::setCountRaw(flamegpu::size_type n) {
     for (size_t v = 0; v < cols.size(); ++v) cols[v].resize(static_cast<size_t>(n) * agent->variables[v].bytes());
     count = n;

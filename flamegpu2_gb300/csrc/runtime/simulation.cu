@@ -660,6 +660,9 @@ struct SimulationImpl {
     // agents created by host functions (HostAgentAPI::newAgent), per (agent, state),
     // joining their populations when the host functions return
     std::map<std::pair<std::string, std::string>, std::unique_ptr<AgentVector>> host_births;
+    // populations host functions read with getPopulationData, per (agent, state),
+    // written back when the host functions return
+    std::map<std::pair<std::string, std::string>, std::unique_ptr<AgentVector>> host_views;
     uint32_t* h_pinned = nullptr;
     uint32_t* h_pinned_dev = nullptr;  // its device address (null: not mapped)
     unsigned int step_count = 0;
@@ -1952,7 +1955,22 @@ struct SimulationImpl {
     // Agents created by host functions join their populations (after the
     // existing agents, in creation order, with fresh ids), as the reference adds
     // them when the host function returns (HostAgentAPI::newAgent).
+    // A host function's population view reaches the device before a device
+    // reduction or sort of that population reads it, and a sort reorders it
+    // (the reference's DeviceAgentVector synchronisation).
+    void sync_host_view(const std::string& a, const std::string& s) {
+        auto it = host_views.find({a, s});
+        if (it != host_views.end() && it->second) owner->setPopulationData(*it->second, s);
+    }
+    void refresh_host_view(const std::string& a, const std::string& s) {
+        auto it = host_views.find({a, s});
+        if (it != host_views.end() && it->second) owner->getPopulationData(*it->second, s);
+    }
+
     void flush_host_births() {
+        for (auto& kv : host_views)
+            if (kv.second) owner->setPopulationData(*kv.second, kv.first.second);
+        host_views.clear();
         for (auto& kv : host_births) {
             AgentVector& add = *kv.second;
             if (add.empty()) continue;
@@ -2355,6 +2373,7 @@ void HostAPI::Environment::setRaw(const std::string& name, const void* in, size_
 
 unsigned int HostAPI::AgentAPI::count() const {
     detail::AgentList* l = sim->list_of(agent, state);
+    sim->sync_host_view(agent, state);
     uint32_t c = 0;
     FG_CUDA(cudaStreamSynchronize(sim->stream));
     FG_CUDA(cudaMemcpy(&c, l->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -2369,10 +2388,21 @@ HostNewAgentAPI HostAPI::AgentAPI::newAgent() {
     return HostNewAgentAPI(buf.get(), buf->size() - 1);
 }
 
+AgentVector& HostAPI::AgentAPI::getPopulationData() {
+    detail::AgentList* l = sim->list_of(agent, state);
+    auto& v = sim->host_views[{agent, state}];
+    if (!v) {
+        v = std::make_unique<AgentVector>(AgentDescription(sim->model, const_cast<detail::AgentData*>(l->agent)));
+        sim->owner->getPopulationData(*v, state);
+    }
+    return *v;
+}
+
 const void* HostAPI::AgentAPI::device_column(const std::string& variable, const std::type_info& t, const uint32_t** d_n,
                                              cudaStream_t* stream) const {
     // the checks of HostAgentAPI::sum (HostAgentAPI.cuh:536-546)
     const detail::AgentList* l = sim->list_of(agent, state);
+    sim->sync_host_view(agent, state);
     const int v = l->var_index(variable);
     if (v < 0)
         THROW exception::InvalidAgentVar(format("Agent '%s' has no variable '%s'", agent.c_str(), variable.c_str()));
@@ -2447,6 +2477,7 @@ void HostAPI::AgentAPI::sort_by(const std::string& variable, const std::type_inf
         l->parity ^= 1;
         FG_CUDA(cudaFreeAsync(scratch, st));
         FG_CUDA(cudaStreamSynchronize(st));
+        sim->refresh_host_view(agent, state);
     } catch (...) {
         cudaFreeAsync(scratch, st);
         throw;

@@ -90,6 +90,10 @@ class AgentVector {
     Agent front() { return at(0); }
     Agent back() { return at(count - 1); }
     void push_back();
+    void pop_back() { resize(count ? count - 1 : 0); }
+    /** Remove the agent at pos, or the agents of [first, last); the agents after them move up in order. */
+    void erase(flamegpu::size_type pos) { erase(pos, pos + 1); }
+    void erase(flamegpu::size_type first, flamegpu::size_type last);
     void resize(flamegpu::size_type n);
     void reserve(flamegpu::size_type n);
     void clear() { resize(0); }

@@ -128,6 +128,10 @@ class HostMacroProperty {
     size_t at;
 };
 
+/** DeviceAgentVector (include/flamegpu/runtime/agent/DeviceAgentVector.h): a
+ *  host function's view of an agent population (HostAgentAPI::getPopulationData). */
+typedef AgentVector& DeviceAgentVector;
+
 class HostAPI {
  public:
     class Environment {
@@ -259,6 +263,12 @@ class HostAPI {
         unsigned int count() const;
         /** A new agent of this type and state (HostAgentAPI::newAgent, :160). */
         HostNewAgentAPI newAgent();
+        /** HostAgentAPI::getPopulationData (HostAgentAPI.cuh:227-236): the
+         *  population, read back from the device. What the host function
+         *  changes in it, agents added (fresh ids for those without one) and
+         *  removed included, replaces the population when the host function
+         *  returns, before the agents made with newAgent() join it. */
+        AgentVector& getPopulationData();
         /** Sum of a variable over the population (:174-185): accumulated on
          * the device in a fixed order (double for floating point, 64-bit
          * integers otherwise), returned as OutT. */
