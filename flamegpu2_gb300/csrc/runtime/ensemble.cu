@@ -141,7 +141,8 @@ std::string batch_unsupported(const ModelData& m) {
     if (m.agents.size() != 1) return "the model has more than one agent type";
     const AgentData& a = *m.agents[0];
     if (a.states.size() != 1) return "the agent has more than one state";
-    if (!m.init_functions.empty() || !m.step_functions.empty() || !m.exit_functions.empty())
+    if (!m.init_functions.empty() || !m.step_functions.empty() || !m.exit_functions.empty() ||
+        !m.exit_conditions.empty())
         return "the model has host functions";
     for (const auto& l : m.layers)
         if (!l->host_functions.empty()) return "the model has host layer functions";

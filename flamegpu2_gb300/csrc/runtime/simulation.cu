@@ -666,6 +666,7 @@ struct SimulationImpl {
     uint32_t* h_pinned = nullptr;
     uint32_t* h_pinned_dev = nullptr;  // its device address (null: not mapped)
     unsigned int step_count = 0;
+    bool exit_requested = false;  // an exit condition returned EXIT in the last step
     std::vector<uint32_t> next_id;  // host mirror per agent index (valid when synced)
     bool ids_on_device = true;
     // graphs
@@ -2068,14 +2069,22 @@ struct SimulationImpl {
         step_events.push_back({e0, e1, 1u});
         record_counts();
         count_host_step();
-        ++step_count;
-        if (!model->step_functions.empty()) {
+        // step functions, then exit conditions, see the step that is ending;
+        // the counter advances after them (CUDASimulation.cu:612-637)
+        exit_requested = false;
+        if (!model->step_functions.empty() || !model->exit_conditions.empty()) {
             FG_CUDA(cudaStreamSynchronize(stream));
             HostAPI api(this);
             for (auto fn : model->step_functions) fn(&api);
+            for (auto fn : model->exit_conditions)
+                if (fn(&api) == EXIT) {
+                    exit_requested = true;
+                    break;
+                }
             flush_host_births();
             upload_env_if_dirty();
         }
+        ++step_count;
         if (cuda_config.check_each_step) owner->synchronize();
         owner->processStepLog(-1.0);
     }
@@ -2088,7 +2097,7 @@ struct SimulationImpl {
     bool multi_step_ok(bool step_log) const {
         return cuda_config.use_graphs && !cuda_config.profile_ops && !cuda_config.time_ops_in_graphs &&
                !cuda_config.check_each_step && !step_log && !has_layer_host_functions() &&
-               model->step_functions.empty() && !any_transitions();
+               model->step_functions.empty() && model->exit_conditions.empty() && !any_transitions();
     }
 
     // Up to Smax steps as one captured graph, cached by the buffer parities
@@ -3055,7 +3064,7 @@ bool CUDASimulation::step() {
         impl->flush_host_births();
     }
     impl->step_once(this);
-    return true;
+    return !impl->exit_requested;
 }
 
 void CUDASimulation::step(unsigned int n) {
@@ -3066,7 +3075,10 @@ void CUDASimulation::step(unsigned int n) {
         impl->flush_host_births();
     }
     if (!impl->multi_step_ok(step_log != nullptr)) {
-        for (unsigned int s = 0; s < n; ++s) impl->step_once(this);
+        for (unsigned int s = 0; s < n; ++s) {
+            impl->step_once(this);
+            if (impl->exit_requested) break;
+        }
         return;
     }
     constexpr unsigned int kBlock = 16;
@@ -3088,8 +3100,15 @@ void CUDASimulation::simulate() {
     processStepLog(0.0);  // the frame before the first step (CUDASimulation.cu:1263)
     if (impl->multi_step_ok(step_log != nullptr)) {
         for (unsigned int n = impl->config.steps; n;) n -= impl->step_block(n < 16u ? n : 16u);
+    } else if (impl->config.steps == 0 && !impl->model->exit_conditions.empty()) {
+        // steps 0: until an exit condition ends the simulation
+        do impl->step_once(this);
+        while (!impl->exit_requested);
     } else {
-        for (unsigned int s = 0; s < impl->config.steps; ++s) impl->step_once(this);
+        for (unsigned int s = 0; s < impl->config.steps; ++s) {
+            impl->step_once(this);
+            if (impl->exit_requested) break;
+        }
     }
     if (!impl->model->exit_functions.empty()) {
         FG_CUDA(cudaStreamSynchronize(impl->stream));

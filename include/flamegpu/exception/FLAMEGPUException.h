@@ -43,6 +43,7 @@ FLAMEGPU_DERIVED_EXCEPTION(InvalidMessageType)
 FLAMEGPU_DERIVED_EXCEPTION(InvalidEnvProperty)
 FLAMEGPU_DERIVED_EXCEPTION(InvalidEnvPropertyType)
 FLAMEGPU_DERIVED_EXCEPTION(InvalidOperation)
+FLAMEGPU_DERIVED_EXCEPTION(InvalidHostFunc)
 FLAMEGPU_DERIVED_EXCEPTION(InvalidDependencyGraph)
 FLAMEGPU_DERIVED_EXCEPTION(OutOfBoundsException)
 FLAMEGPU_DERIVED_EXCEPTION(OutOfMemory)

@@ -34,6 +34,9 @@ class EnvironmentDescription;
 class HostAPI;
 
 typedef void (*FLAMEGPU_HOST_FUNCTION_POINTER)(HostAPI* api);
+/** What an exit condition returns (include/flamegpu/defines.h CONDITION_RESULT). */
+enum CONDITION_RESULT { CONTINUE, EXIT };
+typedef CONDITION_RESULT (*FLAMEGPU_EXIT_CONDITION_POINTER)(HostAPI* api);
 
 namespace detail {
 
@@ -141,6 +144,7 @@ struct ModelData {
     std::vector<std::shared_ptr<LayerData>> layers;
     std::vector<EnvProperty> environment;
     std::vector<FLAMEGPU_HOST_FUNCTION_POINTER> init_functions, step_functions, exit_functions;
+    std::vector<FLAMEGPU_EXIT_CONDITION_POINTER> exit_conditions;
     std::vector<AgentFunctionData*> execution_roots;
     uint32_t next_fn_uid = 1;
     AgentData* agent(const std::string& n) const {
@@ -164,6 +168,14 @@ struct ModelData {
         return nullptr;
     }
 };
+
+template <typename F>
+void add_host_fn(std::vector<F>& list, F fn, const char* kind) {
+    for (F g : list)
+        if (g == fn)
+            THROW exception::InvalidHostFunc(exception::format("This %s function has already been added", kind));
+    list.push_back(fn);
+}
 
 template <typename T>
 Variable make_variable(const std::string& name, const T* def, uint32_t elements) {
@@ -463,7 +475,9 @@ class LayerDescription {
     }
     void addAgentFunction(const AgentFunctionDescription& f) { add(f.getData()); }
     void addAgentFunction(const std::string& agent_name, const std::string& function_name);
-    void addHostFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { layer->host_functions.push_back(fn); }
+    /** LayerDescription::addHostFunction (LayerDescription.h:120-127): a function
+     *  may be in several layers, once per layer. */
+    void addHostFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { detail::add_host_fn(layer->host_functions, fn, "host layer"); }
     std::string getName() const { return layer->name; }
     flamegpu::size_type getAgentFunctionsCount() const { return static_cast<flamegpu::size_type>(layer->functions.size()); }
 
@@ -551,9 +565,16 @@ class ModelDescription {
     LayerDescription Layer(flamegpu::size_type index) const;
     LayerDescription Layer(const std::string& name) const;
     EnvironmentDescription Environment() const { return EnvironmentDescription(model); }
-    void addInitFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { model->init_functions.push_back(fn); }
-    void addStepFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { model->step_functions.push_back(fn); }
-    void addExitFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { model->exit_functions.push_back(fn); }
+    /** ModelDescription::addInitFunction / addStepFunction / addExitFunction /
+     *  addExitCondition (ModelDescription.h:150-200): each runs in the order
+     *  added; adding one twice is InvalidHostFunc. Exit conditions run after
+     *  the step functions of every step; the first to return EXIT ends
+     *  simulate() after that step (with SimulationConfig().steps == 0 a
+     *  simulation runs until one does). */
+    void addInitFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { detail::add_host_fn(model->init_functions, fn, "init"); }
+    void addStepFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { detail::add_host_fn(model->step_functions, fn, "step"); }
+    void addExitFunction(FLAMEGPU_HOST_FUNCTION_POINTER fn) { detail::add_host_fn(model->exit_functions, fn, "exit"); }
+    void addExitCondition(FLAMEGPU_EXIT_CONDITION_POINTER fn) { detail::add_host_fn(model->exit_conditions, fn, "exit condition"); }
     void addExecutionRoot(const AgentFunctionDescription& f) { model->execution_roots.push_back(f.getData()); }
     /** Layers from the dependency graph (src/flamegpu/model/DependencyGraph.cpp:89-180). */
     void generateLayers();
@@ -584,5 +605,6 @@ class ModelDescription {
 #define FLAMEGPU_STEP_FUNCTION(name) void name(flamegpu::HostAPI* FLAMEGPU)
 #define FLAMEGPU_EXIT_FUNCTION(name) void name(flamegpu::HostAPI* FLAMEGPU)
 #define FLAMEGPU_HOST_FUNCTION(name) void name(flamegpu::HostAPI* FLAMEGPU)
+#define FLAMEGPU_EXIT_CONDITION(name) flamegpu::CONDITION_RESULT name(flamegpu::HostAPI* FLAMEGPU)
 
 #endif  // INCLUDE_FLAMEGPU_MODEL_MODELDESCRIPTION_H_
