@@ -65,7 +65,24 @@ FLAMEGPU_STEP_FUNCTION(hp_autosync) {
     if (av.back().getVariable<int>("x") != -5) ++g_errors;
 }
 
+// test_device_agent_vector.cu Insert: n copies of agent 0 inserted n / 2 from the end.
+FLAMEGPU_STEP_FUNCTION(hp_insert) {
+    flamegpu::DeviceAgentVector av = FLAMEGPU->agent("agent").getPopulationData();
+    const flamegpu::size_type n = av.size();
+    if (n == 0) return;
+    flamegpu::AgentInstance ai(av[0]);
+    av.insert(av.size() - n / 2, n, ai);
+}
+
 namespace {
+void* make_host_population_insert(const double*, int32_t) {
+    auto* m = new flamegpu::ModelDescription("host_population_insert");
+    flamegpu::AgentDescription a = m->newAgent("agent");
+    a.newVariable<int>("x", 0);
+    a.newVariable<int>("y", 0);
+    m->addStepFunction(hp_insert);
+    return m;
+}
 void* make_host_population_sync(const double*, int32_t) {
     auto* m = new flamegpu::ModelDescription("host_population_sync");
     flamegpu::AgentDescription a = m->newAgent("agent");
@@ -88,6 +105,7 @@ struct Register {
     Register() {
         fgs_register_model("host_population", &make_host_population);
         fgs_register_model("host_population_sync", &make_host_population_sync);
+        fgs_register_model("host_population_insert", &make_host_population_insert);
     }
 } reg;
 }  // namespace

@@ -330,6 +330,37 @@ void AgentVector::resize(flamegpu::size_type n) {
 
 void AgentVector::push_back() { resize(count + 1); }
 
+AgentVector AgentVector::row(flamegpu::size_type i) const {
+    if (i >= count) THROW exception::OutOfBoundsException(format("Agent index %u out of range (%u agents)", i, count));
+    AgentVector r(AgentDescription(model, agent), 0);
+    for (size_t v = 0; v < cols.size(); ++v) {
+        const size_t b = agent->variables[v].bytes();
+        r.cols[v].assign(cols[v].begin() + static_cast<std::ptrdiff_t>(i * b),
+                         cols[v].begin() + static_cast<std::ptrdiff_t>((i + 1) * b));
+    }
+    r.count = 1;
+    return r;
+}
+
+void AgentVector::insert(flamegpu::size_type pos, flamegpu::size_type n, const AgentInstance& a) {
+    const AgentVector& src = a.values();
+    if (src.agent != agent)
+        THROW exception::InvalidArgument(format("AgentInstance of agent '%s' inserted into a vector of agent '%s'",
+                                                src.agent->name.c_str(), agent->name.c_str()));
+    if (pos > count) THROW exception::OutOfBoundsException(format("Insert position %u past the %u agents", pos, count));
+    for (size_t v = 0; v < cols.size(); ++v) {
+        const detail::Variable& var = agent->variables[v];
+        const size_t b = var.bytes();
+        std::vector<char> one(src.cols[v].begin(), src.cols[v].begin() + static_cast<std::ptrdiff_t>(b));
+        if (var.name == "_id") std::memset(one.data(), 0, b);  // ID_NOT_SET: a fresh id when set
+        std::vector<char> block;
+        block.reserve(static_cast<size_t>(n) * b);
+        for (flamegpu::size_type k = 0; k < n; ++k) block.insert(block.end(), one.begin(), one.end());
+        cols[v].insert(cols[v].begin() + static_cast<std::ptrdiff_t>(static_cast<size_t>(pos) * b), block.begin(), block.end());
+    }
+    count += n;
+}
+
 void AgentVector::erase(flamegpu::size_type first, flamegpu::size_type last) {
     if (first > last || last > count)
         THROW exception::OutOfBoundsException(

@@ -15,6 +15,8 @@
 
 namespace flamegpu {
 
+class AgentInstance;
+
 class AgentVector {
  public:
     class Agent {
@@ -62,6 +64,7 @@ class AgentVector {
         flamegpu::size_type getIndex() const { return index; }
 
      private:
+        friend class AgentInstance;
         AgentVector* vec;
         flamegpu::size_type index;
     };
@@ -83,6 +86,8 @@ class AgentVector {
     };
 
     explicit AgentVector(const AgentDescription& agent, flamegpu::size_type count = 0);
+    /** One agent's values (of row i) as a vector of one agent. */
+    AgentVector row(flamegpu::size_type i) const;
     flamegpu::size_type size() const { return count; }
     bool empty() const { return count == 0; }
     Agent operator[](flamegpu::size_type i) { return Agent(this, i); }
@@ -90,6 +95,13 @@ class AgentVector {
     Agent front() { return at(0); }
     Agent back() { return at(count - 1); }
     void push_back();
+    /** Append a copy of `agent` (it gets a fresh id when the vector is set). */
+    void push_back(const AgentInstance& agent) { insert(count, 1, agent); }
+    /** Insert n copies of `agent` before pos (AgentVector::insert,
+     *  AgentVector.h:376-420); the copies have no id until the vector is set,
+     *  when they get fresh ones. */
+    void insert(flamegpu::size_type pos, flamegpu::size_type n, const AgentInstance& agent);
+    void insert(flamegpu::size_type pos, const AgentInstance& agent) { insert(pos, 1, agent); }
     void pop_back() { resize(count ? count - 1 : 0); }
     /** Remove the agent at pos, or the agents of [first, last); the agents after them move up in order. */
     void erase(flamegpu::size_type pos) { erase(pos, pos + 1); }
@@ -117,6 +129,31 @@ class AgentVector {
     detail::AgentData* agent;
     std::vector<std::vector<char>> cols;
     flamegpu::size_type count = 0;
+};
+
+/**
+ * AgentInstance (include/flamegpu/simulation/AgentInstance.h): one agent's
+ * variables outside a population, made with the agent's default values or
+ * copied from an agent of a vector; AgentVector::insert / push_back copy it in.
+ */
+class AgentInstance {
+ public:
+    explicit AgentInstance(const AgentDescription& agent) : one(agent, 1) {}
+    AgentInstance(const AgentVector::Agent& agent) : one(agent.vec->row(agent.index)) {}  // NOLINT: implicit as in the reference
+    template <typename T>
+    void setVariable(const std::string& name, T value) { one[0].setVariable<T>(name, value); }
+    template <typename T, flamegpu::size_type N>
+    void setVariable(const std::string& name, const std::array<T, N>& value) { one[0].setVariable<T, N>(name, value); }
+    template <typename T>
+    T getVariable(const std::string& name) const { return const_cast<AgentVector&>(one)[0].getVariable<T>(name); }
+    template <typename T, flamegpu::size_type N>
+    std::array<T, N> getVariable(const std::string& name) const {
+        return const_cast<AgentVector&>(one)[0].getVariable<T, N>(name);
+    }
+    const AgentVector& values() const { return one; }
+
+ private:
+    AgentVector one;
 };
 
 }  // namespace flamegpu

@@ -68,3 +68,23 @@ def test_reductions_and_sort_see_the_view():
     assert _errors() == 0
     want = np.concatenate([x + 10, [-5]])
     np.testing.assert_array_equal(got, np.sort(want)[::-1])
+
+
+@pytest.mark.parametrize("n", [1, 1024])
+def test_insert_copies_of_an_agent(n):
+    # test_device_agent_vector.cu Insert: n copies of agent 0 inserted n / 2 from the end, fresh ids
+    S = _sim()
+    s = S.Simulation("host_population_insert", [], check_each_step=True)
+    x = np.arange(n, dtype=np.int32)
+    s.set_population("agent", n, {"x": x, "y": x + 7})
+    ids0 = s.get("agent", "_id", np.uint32)
+    s.step(1)
+    at = n - n // 2
+    want = np.concatenate([x[:at], np.zeros(n, np.int32), x[at:]])
+    np.testing.assert_array_equal(s.get("agent", "x", np.int32), want)
+    np.testing.assert_array_equal(s.get("agent", "y", np.int32), want + 7)
+    ids = s.get("agent", "_id", np.uint32)
+    np.testing.assert_array_equal(np.concatenate([ids[:at], ids[at + n:]]), ids0)
+    assert len(np.unique(ids)) == 2 * n
+    assert (ids[at:at + n] > ids0.max()).all()
+    s.close()
