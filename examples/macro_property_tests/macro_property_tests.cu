@@ -31,6 +31,8 @@
 //  18 contention: every agent adds 1 to count, id to total (double), and
 //     takes min and max of id; a second layer reads them into a, cd, b, c
 //  19 index past the first dimension of int[2][3][4][5] (a device error)
+//  20 WriteRead: += then a read of int in one agent function (a device error)
+//  21 ReadWrite: a read then += of int in one agent function (a device error)
 //   fg_test_macro_errors() returns the host layers' failed checks.
 #include <cstdint>
 #include <mutex>
@@ -178,6 +180,17 @@ FLAMEGPU_AGENT_FUNCTION(mp_contend_read, MessageNone, MessageNone) {
     FLAMEGPU->setVariable<double>("cd", MP(double)("total"));
     FLAMEGPU->setVariable<unsigned int>("b", static_cast<unsigned int>(static_cast<int>(MP(int)("lo"))));
     FLAMEGPU->setVariable<unsigned int>("c", static_cast<unsigned int>(static_cast<int>(MP(int)("hi"))));
+    return flamegpu::ALIVE;
+}
+FLAMEGPU_AGENT_FUNCTION(mp_write_read, MessageNone, MessageNone) {
+    UINT_MP += FLAMEGPU->getVariable<unsigned int>("a");
+    FLAMEGPU->setVariable<unsigned int>("b", UINT_MP);
+    return flamegpu::ALIVE;
+}
+FLAMEGPU_AGENT_FUNCTION(mp_read_write, MessageNone, MessageNone) {
+    const unsigned int t = UINT_MP;
+    UINT_MP += FLAMEGPU->getVariable<unsigned int>("a");
+    FLAMEGPU->setVariable<unsigned int>("b", t);
     return flamegpu::ALIVE;
 }
 FLAMEGPU_AGENT_FUNCTION(mp_bad_index, MessageNone, MessageNone) {
@@ -348,6 +361,8 @@ void* make_macro_properties(const double* p, int32_t np) {
             layer(m, a.newFunction("contend", mp_contend));
             layer(m, a.newFunction("read", mp_contend_read));
             break;
+        case 20: layer(m, a.newFunction("write_read", mp_write_read)); break;
+        case 21: layer(m, a.newFunction("read_write", mp_read_write)); break;
         default: layer(m, a.newFunction("bad", mp_bad_index)); break;
     }
     return m;

@@ -645,6 +645,7 @@ struct SimulationImpl {
     // (offsets from its start, 8-byte aligned), never uploaded from env_host;
     // the host views that are alive, by name
     std::vector<size_t> macro_offset;
+    size_t macro_flags_offset = 0, macro_flag_bytes = 0;
     std::unordered_map<std::string, std::weak_ptr<HostMacroData>> macro_views;
     // misc device state
     uint32_t* d_misc = nullptr;  // [0] step, [1..4] error record, [8..] next ids per agent
@@ -772,7 +773,11 @@ struct SimulationImpl {
         env_host.assign(std::max<size_t>(off, 8), 0);
         for (size_t i = 0; i < model->environment.size(); ++i)
             std::memcpy(env_host.data() + env_offset[i], model->environment[i].value.data(), model->environment[i].value.size());
-        size_t macro_end = env_host.size();
+        // one flag word per macro property (read / updated by the running agent
+        // function), then the macro properties
+        macro_flags_offset = env_host.size();
+        macro_flag_bytes = sizeof(uint32_t) * model->macro_environment.size();
+        size_t macro_end = macro_flags_offset + ((macro_flag_bytes + 7) & ~size_t(7));
         for (const auto& p : model->macro_environment) {
             macro_offset.push_back(macro_end);
             macro_end += (static_cast<size_t>(p.type_size) * p.elements() + 7) & ~size_t(7);
@@ -1141,10 +1146,12 @@ struct SimulationImpl {
                 // offsets into the environment buffer (LaunchParams::env)
                 e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(env_offset[i]), 0, p.type_size, p.elements});
             }
-            // macro properties: stride 1 marks them (the device API checks it)
+            // macro properties: the stride field holds the offset of the
+            // property's flag word (never 0), which marks them as macro properties
             for (size_t i = 0; i < model->macro_environment.size(); ++i) {
                 const MacroProperty& p = model->macro_environment[i];
-                e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(macro_offset[i]), 1, p.type_size, p.elements()});
+                const uint32_t flag = static_cast<uint32_t>(macro_flags_offset + sizeof(uint32_t) * i);
+                e.push_back({fnv1a32(p.name), reinterpret_cast<char*>(macro_offset[i]), flag, p.type_size, p.elements()});
             }
             T->env = make_table(e, "environment");
             f.tables[par].reset(T);
@@ -1879,6 +1886,8 @@ struct SimulationImpl {
             });
             kernel_counter += 1;
         }
+        // every agent function starts with its macro properties neither read nor updated
+        if (macro_flag_bytes) FG_CUDA(cudaMemsetAsync(d_env + macro_flags_offset, 0, macro_flag_bytes, stream));
     }
 
     // populations no kernel changes: the agents of the step being issued
@@ -2252,7 +2261,8 @@ struct SimulationImpl {
                                           "a neighbourhood staging wait gave up (bounded wait)",
                                           "AgentRandom::uniform() with min > max",
                                           "array message index or search radius out of range, or two messages output to one index",
-                                          "bucket message key outside the bounds"};
+                                          "bucket message key outside the bounds",
+                                          "environment macro property both read and updated in one agent function"};
             if (err[0] == kDevArrayMessage && err[1] == kArrayWriteConflict)
                 THROW exception::ArrayMessageWriteConflict(format(
                     "Two array messages were output to one index, or one outside the array (message row %u, %u occurrences)",

@@ -131,6 +131,7 @@ enum DeviceErrorCode : uint32_t {
     kDevRandomRange = 12,
     kDevArrayMessage = 13,
     kDevBucketMessage = 14,
+    kDevMacroConflict = 15,
 };
 
 /** Kernel parameters of one agent function launch (passed __grid_constant__).

@@ -1300,53 +1300,71 @@ template <typename T, flamegpu::size_type I = 1, flamegpu::size_type J = 1, flam
           flamegpu::size_type W = 1>
 class DeviceMacroProperty {
  public:
-    __device__ DeviceMacroProperty(const detail::LaunchParams& p, T* at) : P(p), ptr(at) {}
+    __device__ DeviceMacroProperty(const detail::LaunchParams& p, T* at, uint32_t* f) : P(p), ptr(at), flag(f) {}
     __device__ DeviceMacroProperty<T, J, K, W, 1> operator[](unsigned int i) const {
         if (i >= I) {
             detail::device_error(P, detail::kDevArrayIndex, 0, i);
-            return DeviceMacroProperty<T, J, K, W, 1>(P, nullptr);
+            return DeviceMacroProperty<T, J, K, W, 1>(P, nullptr, nullptr);
         }
-        return DeviceMacroProperty<T, J, K, W, 1>(P, ptr ? ptr + static_cast<size_t>(i) * J * K * W : nullptr);
+        return DeviceMacroProperty<T, J, K, W, 1>(P, ptr ? ptr + static_cast<size_t>(i) * J * K * W : nullptr, flag);
     }
-    __device__ operator T() const { return ptr ? *reinterpret_cast<const volatile T*>(ptr) : T{}; }
+    __device__ operator T() const { return read() ? *reinterpret_cast<const volatile T*>(ptr) : T{}; }
     __device__ DeviceMacroProperty& operator+=(T v) {
-        if (ptr) detail::atomic_add(ptr, v);
+        if (update()) detail::atomic_add(ptr, v);
         return *this;
     }
     __device__ DeviceMacroProperty& operator-=(T v) {
-        if (ptr) detail::atomic_sub(ptr, v);
+        if (update()) detail::atomic_sub(ptr, v);
         return *this;
     }
-    __device__ T addAtomic(T v) { return ptr ? detail::atomic_add(ptr, v) + v : T{}; }
-    __device__ T subAtomic(T v) { return ptr ? detail::atomic_sub(ptr, v) - v : T{}; }
+    __device__ T addAtomic(T v) { return update() ? detail::atomic_add(ptr, v) + v : T{}; }
+    __device__ T subAtomic(T v) { return update() ? detail::atomic_sub(ptr, v) - v : T{}; }
     __device__ T operator+(T v) const { return static_cast<T>(*this) + v; }
     __device__ T operator-(T v) const { return static_cast<T>(*this) - v; }
-    __device__ T operator++() { return ptr ? detail::atomic_add(ptr, static_cast<T>(1)) + static_cast<T>(1) : T{}; }
-    __device__ T operator--() { return ptr ? detail::atomic_sub(ptr, static_cast<T>(1)) - static_cast<T>(1) : T{}; }
-    __device__ T operator++(int) { return ptr ? detail::atomic_add(ptr, static_cast<T>(1)) : T{}; }
-    __device__ T operator--(int) { return ptr ? detail::atomic_sub(ptr, static_cast<T>(1)) : T{}; }
+    __device__ T operator++() { return update() ? detail::atomic_add(ptr, static_cast<T>(1)) + static_cast<T>(1) : T{}; }
+    __device__ T operator--() { return update() ? detail::atomic_sub(ptr, static_cast<T>(1)) - static_cast<T>(1) : T{}; }
+    __device__ T operator++(int) { return update() ? detail::atomic_add(ptr, static_cast<T>(1)) : T{}; }
+    __device__ T operator--(int) { return update() ? detail::atomic_sub(ptr, static_cast<T>(1)) : T{}; }
     __device__ T min(T v) {
-        if (!ptr) return T{};
+        if (!update()) return T{};
         const T old = detail::atomic_min(ptr, v);
         return v < old ? v : old;
     }
     __device__ T max(T v) {
-        if (!ptr) return T{};
+        if (!update()) return T{};
         const T old = detail::atomic_max(ptr, v);
         return v > old ? v : old;
     }
     __device__ T CAS(T compare, T v) {
-        if (!ptr) return T{};
+        if (!update()) return T{};
         return detail::from_word<T>(atomicCAS(detail::word_ptr(ptr), detail::as_word(compare), detail::as_word(v)));
     }
     __device__ T exchange(T v) {
-        if (!ptr) return T{};
+        if (!update()) return T{};
         return detail::from_word<T>(atomicExch(detail::word_ptr(ptr), detail::as_word(v)));
     }
 
  private:
+    // With device checks on, the property's flag word records a read (1) and
+    // an update (2) in this agent function; both is a device error
+    // (DeviceMacroProperty.cuh:219-235).
+    __device__ bool read() const {
+        if (!ptr) return false;
+#if FLAMEGPU_SEATBELTS
+        if ((atomicOr(flag, 1u) & 2u) != 0u) detail::device_error(P, detail::kDevMacroConflict, 0, 0);
+#endif
+        return true;
+    }
+    __device__ bool update() const {
+        if (!ptr) return false;
+#if FLAMEGPU_SEATBELTS
+        if ((atomicOr(flag, 2u) & 1u) != 0u) detail::device_error(P, detail::kDevMacroConflict, 0, 0);
+#endif
+        return true;
+    }
     const detail::LaunchParams& P;
-    T* ptr;  // null after a device error: reads give 0, updates do nothing
+    T* ptr;         // null after a device error: reads give 0, updates do nothing
+    uint32_t* flag;  // read / update record of the whole property
 };
 
 /** Read-only environment properties (include/flamegpu/runtime/environment/DeviceEnvironment.cuh). */
@@ -1372,13 +1390,15 @@ class DeviceEnvironment {
     __device__ DeviceMacroProperty<T, I, J, K, W> getMacroProperty(detail::VarName name) const {
         const detail::VarTable* t = &P.T.env;
         const detail::VarSlot* vs = &t->slot[detail::table_slot(t->mult, t->shift, name.hash)];
-        if (vs->hash != name.hash || vs->stride != 1 || vs->elem_bytes != sizeof(T) || vs->elements != I * J * K * W) {
+        // a macro property's slot holds the offset of its flag word as its stride (never 0)
+        if (vs->hash != name.hash || vs->stride == 0 || vs->elem_bytes != sizeof(T) || vs->elements != I * J * K * W) {
             detail::device_error(P, vs->hash != name.hash ? detail::kDevUnknownVariable : detail::kDevTypeMismatch,
                                  name.hash, 0);
-            return DeviceMacroProperty<T, I, J, K, W>(P, nullptr);
+            return DeviceMacroProperty<T, I, J, K, W>(P, nullptr, nullptr);
         }
-        char* base = const_cast<char*>(detail::ctx().env) + reinterpret_cast<size_t>(vs->ptr);
-        return DeviceMacroProperty<T, I, J, K, W>(P, reinterpret_cast<T*>(base));
+        char* env = const_cast<char*>(detail::ctx().env);
+        return DeviceMacroProperty<T, I, J, K, W>(P, reinterpret_cast<T*>(env + reinterpret_cast<size_t>(vs->ptr)),
+                                                  reinterpret_cast<uint32_t*>(env + vs->stride));
     }
 
  private:

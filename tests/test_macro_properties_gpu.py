@@ -10,7 +10,8 @@ examples/macro_property_tests/macro_property_tests.cu:
   written on the host and read by agents, zeroed on the host; the host
   arithmetic over nine types;
 * 70,001 agents updating one property at once (count, sum, min, max);
-* an index past a dimension is a device error.
+* an index past a dimension is a device error, and so is a property both
+  read and updated in one agent function (WriteRead, ReadWrite).
 """
 import ctypes as C
 
@@ -143,4 +144,25 @@ def test_index_past_a_dimension_is_a_device_error():
     s.set_population("agent", 4, {"a": np.zeros(4, np.uint32)})
     with pytest.raises(S.SimError, match="DeviceError"):
         s.step(1)
+    s.close()
+
+
+@pytest.mark.parametrize("variant", [20, 21], ids=["WriteRead", "ReadWrite"])
+def test_read_and_update_in_one_function_is_a_device_error(variant):
+    # test_device_macro_property.cu:40-104 (WriteRead, ReadWrite with seatbelts on)
+    S = _sim()
+    s = S.Simulation("macro_properties", [variant], check_each_step=True)
+    s.set_population("agent", 1, {"a": np.array([12], np.uint32)})
+    with pytest.raises(S.SimError, match="DeviceError"):
+        s.step(1)
+    s.close()
+
+
+def test_separate_functions_may_read_and_update_every_step():
+    # the flags clear after every agent function: init / update / read run for several steps
+    S = _sim()
+    s = S.Simulation("macro_properties", [0], check_each_step=True)
+    s.set_population("agent", 1, {"a": np.array([12], np.uint32)})
+    s.step(3)
+    assert int(s.get("agent", "b", np.uint32)[0]) == 13
     s.close()
